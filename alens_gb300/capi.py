@@ -1,0 +1,373 @@
+"""ctypes mirror of ``include/alens_gpu.h`` and thin Python wrappers.
+
+``GpuSystem`` drives the CUDA library ``libalens_gpu.so`` through its C ABI;
+this is the Python face of the drop-in boundary and what the tests and the
+benchmark call.  Loading fails loudly if the library has not been built:
+there is no CPU fallback.
+
+``OracleSystem`` (in :mod:`alens_gb300.oracle_api`) wraps the CPU oracle with
+the same methods for the tests.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+ALENS_OK = 0
+ALENS_INVALID_ARG = 1
+ALENS_CUDA_ERROR = 2
+ALENS_NOT_CONVERGED = 3
+ALENS_CAPACITY = 4
+ALENS_TIMEOUT = 5
+ALENS_NAN_DETECTED = 6
+ALENS_NO_DEVICE = 7
+ALENS_NOT_READY = 8
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+WARM_ZERO = 0
+WARM_PREV = 1
+WARM_MLP = 2
+
+STATUS_NAMES = {
+    0: "OK", 1: "INVALID_ARG", 2: "CUDA_ERROR", 3: "NOT_CONVERGED", 4: "CAPACITY",
+    5: "TIMEOUT", 6: "NAN_DETECTED", 7: "NO_DEVICE", 8: "NOT_READY",
+}
+
+
+class AlensConfig(C.Structure):
+    _fields_ = [
+        ("simBoxLow", C.c_double * 3),
+        ("simBoxHigh", C.c_double * 3),
+        ("simBoxPBC", C.c_int32 * 3),
+        ("monolayer", C.c_int32),
+        ("viscosity", C.c_double),
+        ("KBT", C.c_double),
+        ("dt", C.c_double),
+        ("sylinderDiameterColRatio", C.c_double),
+        ("sylinderLengthColRatio", C.c_double),
+        ("sylinderColBuf", C.c_double),
+        ("conResTol", C.c_double),
+        ("conMaxIte", C.c_int32),
+        ("conSolverChoice", C.c_int32),
+        ("rngSeed", C.c_uint64),
+        ("precision", C.c_int32),
+        ("warmStart", C.c_int32),
+        ("maxConstraints", C.c_int32),
+        ("useGraph", C.c_int32),
+        ("stageTiming", C.c_int32),
+        ("stream", C.c_void_p),
+    ]
+
+
+class AlensBlock(C.Structure):
+    _fields_ = [
+        ("delta0", C.c_double),
+        ("gamma", C.c_double),
+        ("gidI", C.c_int64),
+        ("gidJ", C.c_int64),
+        ("globalIndexI", C.c_int32),
+        ("globalIndexJ", C.c_int32),
+        ("normI", C.c_double * 3),
+        ("normJ", C.c_double * 3),
+        ("posI", C.c_double * 3),
+        ("posJ", C.c_double * 3),
+        ("labI", C.c_double * 3),
+        ("labJ", C.c_double * 3),
+        ("oneSide", C.c_int32),
+        ("bilateral", C.c_int32),
+        ("kappa", C.c_double),
+        ("gammaLB", C.c_double),
+        ("stress", C.c_double * 9),
+    ]
+
+
+class AlensStepStats(C.Structure):
+    _fields_ = [
+        ("step", C.c_int64),
+        ("nRods", C.c_int32),
+        ("nCollision", C.c_int32),
+        ("nBilateral", C.c_int32),
+        ("iterations", C.c_int32),
+        ("refineIterations", C.c_int32),
+        ("converged", C.c_int32),
+        ("status", C.c_int32),
+        ("residual", C.c_double),
+        ("constraintsNeeded", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+def make_config(box_low=(0.0, 0.0, 0.0), box_high=(5.0, 5.0, 5.0), pbc=(1, 1, 1),
+                monolayer=False, viscosity=0.01, kbt=0.00411, dt=1e-4,
+                col_ratio_d=1.0, col_ratio_l=1.0, col_buf=0.025, tol=1e-5,
+                max_ite=2000, seed=0, precision=PREC_FP64, warm=WARM_ZERO,
+                max_constraints=0, use_graph=1, stage_timing=0, stream=None) -> AlensConfig:
+    c = AlensConfig()
+    for d in range(3):
+        c.simBoxLow[d] = float(box_low[d])
+        c.simBoxHigh[d] = float(box_high[d])
+        c.simBoxPBC[d] = int(bool(pbc[d]))
+    c.monolayer = int(bool(monolayer))
+    c.viscosity = viscosity
+    c.KBT = kbt
+    c.dt = dt
+    c.sylinderDiameterColRatio = col_ratio_d
+    c.sylinderLengthColRatio = col_ratio_l
+    c.sylinderColBuf = col_buf
+    c.conResTol = tol
+    c.conMaxIte = int(max_ite)
+    c.conSolverChoice = 0
+    c.rngSeed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    c.precision = int(precision)
+    c.warmStart = int(warm)
+    c.maxConstraints = int(max_constraints)
+    c.useGraph = int(use_graph)
+    c.stageTiming = int(stage_timing)
+    c.stream = stream
+    return c
+
+
+class AlensError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} ({status})")
+        self.status = status
+
+
+def _p(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype)) if a is not None else None
+
+
+_PD = C.POINTER(C.c_double)
+_PI32 = C.POINTER(C.c_int32)
+_PI64 = C.POINTER(C.c_int64)
+
+_LIB = None
+
+
+def load_library(path: str | Path | None = None) -> C.CDLL:
+    """Load libalens_gpu.so; raises if it is missing (no fallback)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else _build.lib_path()
+    if not p.exists():
+        raise RuntimeError(f"CUDA library not built: {p} (run __graft_entry__.build())")
+    lib = C.CDLL(str(p))
+    vp = C.c_void_p
+    sigs = {
+        "alens_config_default": (None, [C.POINTER(AlensConfig)]),
+        "alens_status_str": (C.c_char_p, [C.c_int]),
+        "alens_create": (C.c_int, [C.POINTER(AlensConfig), C.POINTER(vp)]),
+        "alens_create_ensemble": (C.c_int, [C.POINTER(AlensConfig), C.c_int, C.POINTER(vp)]),
+        "alens_destroy": (C.c_int, [vp]),
+        "alens_set_rods": (C.c_int, [vp, C.c_int, C.c_int, _PI64, _PD, _PD, _PD, _PD, _PI32]),
+        "alens_update_rods": (C.c_int, [vp, C.c_int, C.c_int, _PD, _PD]),
+        "alens_get_rods": (C.c_int, [vp, C.c_int, C.c_int, _PD, _PD]),
+        "alens_get_velocity": (C.c_int, [vp, C.c_int, C.c_int, _PD, _PD]),
+        "alens_add_bilateral": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(AlensBlock)]),
+        "alens_step": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
+        "alens_detect": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
+        "alens_solve": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
+        "alens_advance": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
+        "alens_get_replica_stats": (C.c_int, [vp, C.c_int, C.POINTER(AlensStepStats)]),
+        "alens_get_num_constraints": (C.c_int, [vp, C.c_int, _PI32, _PI32]),
+        "alens_get_constraints": (C.c_int, [vp, C.c_int, C.c_int, _PI32, _PI32, _PI32, _PD, _PD, _PD]),
+        "alens_get_con_stress": (C.c_int, [vp, C.c_int, _PD]),
+        "alens_get_step_count": (C.c_int, [vp, _PI64]),
+        "alens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
+        "alens_get_launch_count": (C.c_int, [vp, _PI64]),
+        "alens_get_stage_times": (C.c_int, [vp, _PD]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def exported_symbols_from_header(header: Path | None = None) -> list[str]:
+    """Names of the functions declared in include/*.h."""
+    import re
+    names = []
+    hdrs = [header] if header else sorted((_build.ROOT / "include").glob("*.h"))
+    for h in hdrs:
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(alens_[a-z0-9_]+)\s*\(", text):
+            if m.group(1) not in names:
+                names.append(m.group(1))
+    return names
+
+
+def _ck(rc: int, where: str, ok=(ALENS_OK,)) -> int:
+    if rc not in ok:
+        raise AlensError(rc, where)
+    return rc
+
+
+class RodState:
+    """Host-side rod arrays in the C ABI layout (orientation stored x,y,z,w)."""
+
+    def __init__(self, gid, pos, quat, length, radius, immovable=None):
+        self.gid = np.ascontiguousarray(gid, dtype=np.int64)
+        self.pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        self.quat = np.ascontiguousarray(quat, dtype=np.float64).reshape(-1, 4)
+        self.length = np.ascontiguousarray(length, dtype=np.float64)
+        self.radius = np.ascontiguousarray(radius, dtype=np.float64)
+        self.immovable = (np.ascontiguousarray(immovable, dtype=np.int32)
+                          if immovable is not None else None)
+
+    @property
+    def n(self) -> int:
+        return int(self.gid.shape[0])
+
+    def copy(self) -> "RodState":
+        return RodState(self.gid.copy(), self.pos.copy(), self.quat.copy(), self.length.copy(),
+                        self.radius.copy(), None if self.immovable is None else self.immovable.copy())
+
+
+class GpuSystem:
+    """One context of the CUDA library (``nrep`` replicas, default 1)."""
+
+    def __init__(self, cfg: AlensConfig | list[AlensConfig], lib: C.CDLL | None = None):
+        self.lib = lib or load_library()
+        self.h = C.c_void_p()
+        if isinstance(cfg, (list, tuple)):
+            arr = (AlensConfig * len(cfg))(*cfg)
+            _ck(self.lib.alens_create_ensemble(arr, len(cfg), C.byref(self.h)), "alens_create_ensemble")
+            self.nrep = len(cfg)
+        else:
+            _ck(self.lib.alens_create(C.byref(cfg), C.byref(self.h)), "alens_create")
+            self.nrep = 1
+        self.n = [0] * self.nrep
+
+    def close(self):
+        if self.h:
+            self.lib.alens_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_rods(self, rods: RodState, replica: int = 0):
+        _ck(self.lib.alens_set_rods(self.h, replica, rods.n, _p(rods.gid, C.c_int64), _p(rods.pos, C.c_double),
+                                    _p(rods.quat, C.c_double), _p(rods.length, C.c_double),
+                                    _p(rods.radius, C.c_double), _p(rods.immovable, C.c_int32)),
+            "alens_set_rods")
+        self.n[replica] = rods.n
+
+    def update_rods(self, pos, quat, replica: int = 0):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        quat = np.ascontiguousarray(quat, dtype=np.float64)
+        _ck(self.lib.alens_update_rods(self.h, replica, self.n[replica], _p(pos, C.c_double),
+                                       _p(quat, C.c_double)), "alens_update_rods")
+
+    def get_rods(self, replica: int = 0, out=None):
+        n = self.n[replica]
+        pos, quat = out if out is not None else (np.empty((n, 3)), np.empty((n, 4)))
+        _ck(self.lib.alens_get_rods(self.h, replica, n, _p(pos, C.c_double), _p(quat, C.c_double)),
+            "alens_get_rods")
+        return pos, quat
+
+    def get_velocity(self, replica: int = 0):
+        n = self.n[replica]
+        v = np.empty((n, 3))
+        w = np.empty((n, 3))
+        _ck(self.lib.alens_get_velocity(self.h, replica, n, _p(v, C.c_double), _p(w, C.c_double)),
+            "alens_get_velocity")
+        return v, w
+
+    def add_bilateral(self, blocks, replica: int = 0):
+        arr = (AlensBlock * len(blocks))(*blocks)
+        _ck(self.lib.alens_add_bilateral(self.h, replica, len(blocks), arr), "alens_add_bilateral")
+
+    def _stage(self, fn, name, ok=(ALENS_OK,)):
+        st = AlensStepStats()
+        rc = fn(self.h, C.byref(st))
+        _ck(rc, name, ok)
+        d = st.as_dict()
+        d["rc"] = rc
+        return d
+
+    def step(self, allow_not_converged=True):
+        ok = (ALENS_OK, ALENS_NOT_CONVERGED) if allow_not_converged else (ALENS_OK,)
+        return self._stage(self.lib.alens_step, "alens_step", ok)
+
+    def detect(self):
+        return self._stage(self.lib.alens_detect, "alens_detect")
+
+    def solve(self, allow_not_converged=True):
+        ok = (ALENS_OK, ALENS_NOT_CONVERGED) if allow_not_converged else (ALENS_OK,)
+        return self._stage(self.lib.alens_solve, "alens_solve", ok)
+
+    def advance(self):
+        return self._stage(self.lib.alens_advance, "alens_advance")
+
+    def replica_stats(self, replica: int):
+        st = AlensStepStats()
+        _ck(self.lib.alens_get_replica_stats(self.h, replica, C.byref(st)), "alens_get_replica_stats")
+        return st.as_dict()
+
+    def num_constraints(self, replica: int = 0):
+        a = C.c_int32()
+        b = C.c_int32()
+        _ck(self.lib.alens_get_num_constraints(self.h, replica, C.byref(a), C.byref(b)),
+            "alens_get_num_constraints")
+        return a.value, b.value
+
+    def constraints(self, replica: int = 0):
+        nc, nb = self.num_constraints(replica)
+        n = nc + nb
+        ii = np.empty(n, np.int32)
+        jj = np.empty(n, np.int32)
+        im = np.empty(n, np.int32)
+        d0 = np.empty(n)
+        g = np.empty(n)
+        jac = np.empty((n, 12))
+        _ck(self.lib.alens_get_constraints(self.h, replica, n, _p(ii, C.c_int32), _p(jj, C.c_int32),
+                                           _p(im, C.c_int32), _p(d0, C.c_double), _p(g, C.c_double),
+                                           _p(jac, C.c_double)), "alens_get_constraints")
+        return dict(i=ii, j=jj, image=im, delta0=d0, gamma=g, jac=jac, ncoll=nc, nbil=nb)
+
+    def con_stress(self, replica: int = 0):
+        s = np.empty(9)
+        _ck(self.lib.alens_get_con_stress(self.h, replica, _p(s, C.c_double)), "alens_get_con_stress")
+        return s.reshape(3, 3)
+
+    def step_count(self) -> int:
+        c = C.c_int64()
+        _ck(self.lib.alens_get_step_count(self.h, C.byref(c)), "alens_get_step_count")
+        return c.value
+
+    def launch_count(self) -> int:
+        c = C.c_int64()
+        _ck(self.lib.alens_get_launch_count(self.h, C.byref(c)), "alens_get_launch_count")
+        return c.value
+
+    def stage_times(self):
+        t = np.zeros(5)
+        _ck(self.lib.alens_get_stage_times(self.h, _p(t, C.c_double)), "alens_get_stage_times")
+        return t
+
+    def stream_handle(self) -> int:
+        s = C.c_void_p()
+        _ck(self.lib.alens_get_stream(self.h, C.byref(s)), "alens_get_stream")
+        return s.value or 0

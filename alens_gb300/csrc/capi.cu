@@ -1,0 +1,216 @@
+// capi.cu - the C ABI of include/alens_gpu.h.  Every entry point converts
+// exceptions into status codes; nothing crosses the ABI as a C++ exception.
+#include <cstring>
+#include <new>
+
+#include "engine.h"
+
+struct AlensCtx {
+    alens::Engine *eng;
+};
+
+namespace {
+
+template <class F>
+int guarded(F &&f) {
+    try {
+        return f();
+    } catch (const alens::ApiError &e) {
+        return e.status;
+    } catch (const alens::CudaFailure &e) {
+        cudaGetLastError();
+        return ALENS_CUDA_ERROR;
+    } catch (const std::bad_alloc &) {
+        return ALENS_CUDA_ERROR;
+    } catch (...) {
+        return ALENS_CUDA_ERROR;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void alens_config_default(AlensConfig *c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    for (int d = 0; d < 3; d++) {
+        c->simBoxLow[d] = 0.0;
+        c->simBoxHigh[d] = 1.0;
+        c->simBoxPBC[d] = 0;
+    }
+    c->monolayer = 0;
+    c->viscosity = 0.01;
+    c->KBT = 0.00411;
+    c->dt = 1e-4;
+    c->sylinderDiameterColRatio = 1.0;
+    c->sylinderLengthColRatio = 1.0;
+    c->sylinderColBuf = 0.025;
+    c->conResTol = 1e-5;
+    c->conMaxIte = 2000;
+    c->conSolverChoice = 0;
+    c->rngSeed = 1234;
+    c->precision = ALENS_PREC_FP64;
+    c->warmStart = ALENS_WARM_ZERO;
+    c->maxConstraints = 0;
+    c->useGraph = 1;
+    c->stageTiming = 0;
+    c->stream = nullptr;
+}
+
+const char *alens_status_str(int s) {
+    switch (s) {
+        case ALENS_OK: return "ok";
+        case ALENS_INVALID_ARG: return "invalid argument";
+        case ALENS_CUDA_ERROR: return "CUDA error";
+        case ALENS_NOT_CONVERGED: return "BBPGD did not converge";
+        case ALENS_CAPACITY: return "constraint capacity exceeded";
+        case ALENS_TIMEOUT: return "device wait timed out";
+        case ALENS_NAN_DETECTED: return "NaN or Inf detected";
+        case ALENS_NO_DEVICE: return "no CUDA device";
+        case ALENS_NOT_READY: return "call order violated";
+        default: return "unknown status";
+    }
+}
+
+int alens_create(const AlensConfig *cfg, AlensCtx **out) { return alens_create_ensemble(cfg, 1, out); }
+
+int alens_create_ensemble(const AlensConfig *cfgs, int nReplica, AlensCtx **out) {
+    if (!cfgs || !out || nReplica < 1) return ALENS_INVALID_ARG;
+    *out = nullptr;
+    return guarded([&] {
+        AlensCtx *c = new AlensCtx{new alens::Engine(cfgs, nReplica)};
+        *out = c;
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_destroy(AlensCtx *ctx) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        delete ctx->eng;
+        delete ctx;
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_set_rods(AlensCtx *ctx, int replica, int n, const int64_t *gid, const double *pos,
+                   const double *orientation, const double *length, const double *radius,
+                   const int32_t *immovable) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->setRods(replica, n, gid, pos, orientation, length, radius, immovable);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_update_rods(AlensCtx *ctx, int replica, int n, const double *pos, const double *orientation) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->updateRods(replica, n, pos, orientation);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_rods(AlensCtx *ctx, int replica, int n, double *pos, double *orientation) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->getRods(replica, n, pos, orientation);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_velocity(AlensCtx *ctx, int replica, int n, double *vel, double *omega) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->getVelocity(replica, n, vel, omega);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_add_bilateral(AlensCtx *ctx, int replica, int n, const AlensBlock *blocks) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->addBilateral(replica, n, blocks);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_step(AlensCtx *ctx, AlensStepStats *stats) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] { return ctx->eng->step(stats); });
+}
+
+int alens_detect(AlensCtx *ctx, AlensStepStats *stats) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] { return ctx->eng->detect(stats); });
+}
+
+int alens_solve(AlensCtx *ctx, AlensStepStats *stats) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] { return ctx->eng->solve(stats); });
+}
+
+int alens_advance(AlensCtx *ctx, AlensStepStats *stats) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] { return ctx->eng->advance(stats); });
+}
+
+int alens_get_replica_stats(AlensCtx *ctx, int replica, AlensStepStats *stats) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->replicaStats(replica, stats);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_num_constraints(AlensCtx *ctx, int replica, int *nCollision, int *nBilateral) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->numConstraints(replica, nCollision, nBilateral);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_constraints(AlensCtx *ctx, int replica, int cap, int32_t *indexI, int32_t *indexJ,
+                          int32_t *image, double *delta0, double *gamma, double *jac) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->getConstraints(replica, cap, indexI, indexJ, image, delta0, gamma, jac);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_con_stress(AlensCtx *ctx, int replica, double *stress9) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        ctx->eng->conStress(replica, stress9);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_step_count(AlensCtx *ctx, int64_t *count) {
+    if (!ctx || !count) return ALENS_INVALID_ARG;
+    *count = ctx->eng->stepCount();
+    return ALENS_OK;
+}
+
+int alens_get_launch_count(AlensCtx *ctx, int64_t *count) {
+    if (!ctx || !count) return ALENS_INVALID_ARG;
+    *count = ctx->eng->launches();
+    return ALENS_OK;
+}
+
+int alens_get_stage_times(AlensCtx *ctx, double *ms5) {
+    if (!ctx || !ms5) return ALENS_INVALID_ARG;
+    for (int i = 0; i < 5; i++) ms5[i] = ctx->eng->stageMs()[i];
+    return ALENS_OK;
+}
+
+int alens_get_stream(AlensCtx *ctx, void **stream) {
+    if (!ctx || !stream) return ALENS_INVALID_ARG;
+    *stream = (void *)ctx->eng->stream();
+    return ALENS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,719 @@
+// engine.cu - host side of a context: device memory, the per-step launch
+// sequence (optionally replayed as one CUDA graph), capacity growth and
+// statistics.  Everything the reference's SylinderSystem keeps per rank
+// (rod container, constraint pool, solver) lives here for one GPU.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+
+namespace alens {
+
+namespace {
+
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ULL;  // 2 s
+
+bool config_ok(const AlensConfig &c) {
+    for (int d = 0; d < 3; d++)
+        if (!(c.simBoxHigh[d] > c.simBoxLow[d]) || !std::isfinite(c.simBoxLow[d]) ||
+            !std::isfinite(c.simBoxHigh[d]))
+            return false;
+    return c.dt > 0 && c.viscosity > 0 && c.sylinderColBuf >= 0 && c.sylinderDiameterColRatio > 0 &&
+           c.sylinderLengthColRatio > 0 && c.conMaxIte >= 0 && c.conResTol > 0 &&
+           c.conSolverChoice == 0 && (c.precision == ALENS_PREC_FP64 || c.precision == ALENS_PREC_MIXED) &&
+           c.warmStart >= 0 && c.warmStart <= 2 && c.maxConstraints >= 0;
+}
+
+}  // namespace
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) throw CudaFailure(e_, #call);       \
+    } while (0)
+
+Engine::Engine(const AlensConfig *cfgs, int nrep) {
+    if (nrep < 1) throw ApiError(ALENS_INVALID_ARG);
+    for (int r = 0; r < nrep; r++)
+        if (!config_ok(cfgs[r])) throw ApiError(ALENS_INVALID_ARG);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        throw ApiError(ALENS_NO_DEVICE);
+    }
+    CK(cudaGetDevice(&device_));
+    CK(cudaDeviceGetAttribute(&numSM_, cudaDevAttrMultiProcessorCount, device_));
+    cfg_.assign(cfgs, cfgs + nrep);
+    R_ = nrep;
+    rods_.resize(R_);
+    queue_.resize(R_);
+    repStats_.assign(R_, AlensStepStats{});
+    if (cfg_[0].stream) {
+        stream_ = (cudaStream_t)cfg_[0].stream;
+        ownStream_ = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+        ownStream_ = true;
+    }
+    precision_ = cfg_[0].precision;
+    warm_ = cfg_[0].warmStart;
+    useGraph_ = cfg_[0].useGraph != 0;
+    fixedCap_ = cfg_[0].maxConstraints;
+    stageTiming_ = cfg_[0].stageTiming != 0;
+    if (const char *e = std::getenv("ALENS_SOLVER_BLOCKS_PER_SM")) solverBlocksPerSM_ = std::max(1, atoi(e));
+    CK(cudaMallocHost(&hCtl_, sizeof(DevCtl)));
+    CK(cudaMallocHost(&hDyn_, sizeof(RepDyn) * R_));
+    CK(cudaMallocHost(&hBilPrefix_, sizeof(int) * (R_ + 1)));
+    std::memset(hCtl_, 0, sizeof(DevCtl));
+    std::memset(hDyn_, 0, sizeof(RepDyn) * R_);
+    std::memset(hBilPrefix_, 0, sizeof(int) * (R_ + 1));
+}
+
+Engine::~Engine() {
+    if (graphExec_) cudaGraphExecDestroy(graphExec_);
+    for (auto &e : events_)
+        if (e) cudaEventDestroy(e);
+    if (stream_) cudaStreamSynchronize(stream_);
+    freeGroup(rodAllocs_);
+    freeGroup(conAllocs_);
+    freeGroup(blockAllocs_);
+    freeGroup(fixedAllocs_);
+    if (hCtl_) cudaFreeHost(hCtl_);
+    if (hDyn_) cudaFreeHost(hDyn_);
+    if (hBilPrefix_) cudaFreeHost(hBilPrefix_);
+    if (hBlocks_) cudaFreeHost(hBlocks_);
+    if (hBlockRep_) cudaFreeHost(hBlockRep_);
+    if (ownStream_ && stream_) cudaStreamDestroy(stream_);
+}
+
+void Engine::freeGroup(std::vector<void *> &g) {
+    for (void *p : g) cudaFree(p);
+    g.clear();
+}
+
+template <class T>
+T *Engine::alloc(std::vector<void *> &group, size_t n) {
+    void *p = nullptr;
+    const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    CK(cudaMalloc(&p, bytes));
+    group.push_back(p);
+    return (T *)p;
+}
+
+// ------------------------------------------------------------------ rods
+void Engine::setRods(int rep, int n, const int64_t *gid, const double *pos, const double *quat,
+                     const double *len, const double *rad, const int32_t *imm) {
+    if (rep < 0 || rep >= R_ || n < 0 || n > (4 << 20)) throw ApiError(ALENS_INVALID_ARG);
+    if (n > 0 && (!gid || !pos || !quat || !len || !rad)) throw ApiError(ALENS_INVALID_ARG);
+    for (int i = 0; i < n; i++)
+        if (!(len[i] >= 0.0) || !(rad[i] > 0.0) || !std::isfinite(len[i]) || !std::isfinite(rad[i]))
+            throw ApiError(ALENS_INVALID_ARG);
+    HostRods h;
+    h.n = n;
+    h.gid.assign(gid, gid + n);
+    h.pos.assign(pos, pos + 3 * (size_t)n);
+    h.quat.assign(quat, quat + 4 * (size_t)n);
+    h.len.assign(len, len + n);
+    h.rad.assign(rad, rad + n);
+    h.imm.assign(n, 0);
+    if (imm)
+        for (int i = 0; i < n; i++) h.imm[i] = imm[i] ? 1 : 0;
+    h.set = true;
+    // cell grid (validates the box against the search cutoff)
+    RepParams P;
+    makeParams(rep, h, P);
+    rods_[rep] = std::move(h);
+    dirty_ = true;
+}
+
+void Engine::makeParams(int rep, const HostRods &h, RepParams &P) const {
+    const AlensConfig &c = cfg_[rep];
+    std::memset(&P, 0, sizeof(P));
+    double mx = 0.0;
+    for (int i = 0; i < h.n; i++) {
+        const bool sphere = h.len[i] < 2.0 * h.rad[i];
+        const double hh = sphere ? 0.0 : 0.5 * (h.len[i] * c.sylinderLengthColRatio);
+        const double rc = h.rad[i] * c.sylinderDiameterColRatio;
+        mx = std::max(mx, 2.0 * hh + 2.0 * rc);
+    }
+    const double cutoff = mx + c.sylinderColBuf;
+    long long total = 1;
+    for (int d = 0; d < 3; d++) {
+        P.lo[d] = c.simBoxLow[d];
+        P.hi[d] = c.simBoxHigh[d];
+        P.L[d] = c.simBoxHigh[d] - c.simBoxLow[d];
+        P.pbc[d] = c.simBoxPBC[d] ? 1 : 0;
+        if (P.pbc[d] && P.L[d] < cutoff) throw ApiError(ALENS_INVALID_ARG);
+        int nc = cutoff > 0 ? (int)std::floor(P.L[d] / cutoff) : 1;
+        nc = std::max(1, std::min(nc, 1024));
+        P.ncell[d] = nc;
+    }
+    // keep the cell count proportional to the rod count (the grid only
+    // affects the candidate enumeration, never the result)
+    const long long limit = std::max<long long>(64, 2LL * h.n);
+    while ((total = (long long)P.ncell[0] * P.ncell[1] * P.ncell[2]) > limit) {
+        int d = 0;
+        for (int e = 1; e < 3; e++)
+            if (P.ncell[e] > P.ncell[d]) d = e;
+        P.ncell[d] = std::max(1, P.ncell[d] / 2);
+    }
+    for (int d = 0; d < 3; d++) P.cellsz[d] = P.L[d] / P.ncell[d];
+    P.mu = c.viscosity;
+    P.kT = c.KBT;
+    P.dt = c.dt;
+    P.colRatioD = c.sylinderDiameterColRatio;
+    P.colRatioL = c.sylinderLengthColRatio;
+    P.colBuf = c.sylinderColBuf;
+    P.tol = c.conResTol;
+    P.seed = c.rngSeed;
+    P.mono = c.monolayer ? 1 : 0;
+    P.maxIte = c.conMaxIte;
+    P.nRods = h.n;
+}
+
+void Engine::finalize() {
+    if (!dirty_) return;
+    for (int r = 0; r < R_; r++)
+        if (!rods_[r].set) throw ApiError(ALENS_NOT_READY);
+    CK(cudaStreamSynchronize(stream_));
+    invalidateGraph();
+    freeGroup(rodAllocs_);
+    freeGroup(conAllocs_);
+    freeGroup(fixedAllocs_);
+    freeGroup(blockAllocs_);
+    blockCap_ = 0;
+    hostPar_.resize(R_);
+    int rodOff = 0, cellOff = 0;
+    for (int r = 0; r < R_; r++) {
+        makeParams(r, rods_[r], hostPar_[r]);
+        hostPar_[r].rodOffset = rodOff;
+        hostPar_[r].cellOffset = cellOff;
+        rodOff += rods_[r].n;
+        cellOff += hostPar_[r].ncell[0] * hostPar_[r].ncell[1] * hostPar_[r].ncell[2];
+    }
+    const int N = rodOff;
+    const int C = cellOff;
+    // the three-pass scan handles up to 4096 x 1024 elements
+    if (N > (4 << 20) || C > (4 << 20)) throw ApiError(ALENS_INVALID_ARG);
+    DevState &S = S_;
+    std::memset(&S, 0, sizeof(S));
+    S.R = R_;
+    S.nRods = N;
+    S.nCells = C;
+    S.warm = warm_;
+    S.precision = precision_;
+    // fixed-size control
+    S.par = alloc<RepParams>(fixedAllocs_, R_);
+    S.dyn = alloc<RepDyn>(fixedAllocs_, R_);
+    S.ctl = alloc<DevCtl>(fixedAllocs_, 1);
+    S.bilPrefix = alloc<int>(fixedAllocs_, R_ + 1);
+    S.stress = alloc<double>(fixedAllocs_, 9 * (size_t)R_);
+    S.scanTmp = alloc<int>(fixedAllocs_, 4096);
+    S.prevCount = alloc<int>(fixedAllocs_, 1);
+    CK(cudaMemcpyAsync(S.par, hostPar_.data(), sizeof(RepParams) * R_, cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemsetAsync(S.dyn, 0, sizeof(RepDyn) * R_, stream_));
+    CK(cudaMemsetAsync(S.bilPrefix, 0, sizeof(int) * (R_ + 1), stream_));
+    CK(cudaMemsetAsync(S.prevCount, 0, sizeof(int), stream_));
+    std::memset(hCtl_, 0, sizeof(DevCtl));
+    hCtl_->step = stepCount_;
+    CK(cudaMemcpyAsync(S.ctl, hCtl_, sizeof(DevCtl), cudaMemcpyHostToDevice, stream_));
+    // rods
+    auto &G = rodAllocs_;
+    double **rodD[] = {&S.px, &S.py, &S.pz, &S.qx, &S.qy, &S.qz, &S.qw, &S.len, &S.rad,
+                       &S.ax, &S.ay, &S.az, &S.hcol, &S.rcol, &S.m0, &S.m1, &S.m2,
+                       &S.sx, &S.sy, &S.sz, &S.sax, &S.say, &S.saz, &S.sh, &S.sr};
+    for (double **p : rodD) *p = alloc<double>(G, N);
+    S.gid = alloc<long long>(G, N);
+    S.imm = alloc<int>(G, N);
+    S.rodRep = alloc<int>(G, N);
+    S.sph = alloc<unsigned char>(G, N);
+    S.unc = alloc<double>(G, 6 * (size_t)N);
+    S.vel = alloc<double>(G, 6 * (size_t)N);
+    S.U = alloc<double>(G, 6 * (size_t)N);
+    S.U32 = alloc<float>(G, 6 * (size_t)N);
+    S.stage = alloc<double>(G, 7 * (size_t)N);
+    S.cellOf = alloc<int>(G, N);
+    S.sidx = alloc<int>(G, N);
+    S.pairCount = alloc<int>(G, N);
+    S.pairOff = alloc<int>(G, N + 1);
+    S.pairCursor = alloc<int>(G, N);
+    S.rowCount = alloc<int>(G, N);
+    S.rowPtr = alloc<int>(G, N + 1);
+    S.rowCursor = alloc<int>(G, N);
+    S.cellCount = alloc<int>(G, C);
+    S.cellStart = alloc<int>(G, C + 1);
+    S.cellCursor = alloc<int>(G, C);
+    CK(cudaMemsetAsync(S.vel, 0, sizeof(double) * 6 * (size_t)N, stream_));
+    // upload SoA
+    {
+        std::vector<double> buf((size_t)N);
+        std::vector<long long> gbuf((size_t)N);
+        std::vector<int> ibuf((size_t)N), rbuf((size_t)N);
+        auto up = [&](double *dst, auto getter) {
+            size_t o = 0;
+            for (int r = 0; r < R_; r++)
+                for (int i = 0; i < rods_[r].n; i++) buf[o++] = getter(rods_[r], i);
+            CK(cudaMemcpy(dst, buf.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+        };
+        up(S.px, [](const HostRods &h, int i) { return h.pos[3 * i]; });
+        up(S.py, [](const HostRods &h, int i) { return h.pos[3 * i + 1]; });
+        up(S.pz, [](const HostRods &h, int i) { return h.pos[3 * i + 2]; });
+        up(S.qx, [](const HostRods &h, int i) { return h.quat[4 * i]; });
+        up(S.qy, [](const HostRods &h, int i) { return h.quat[4 * i + 1]; });
+        up(S.qz, [](const HostRods &h, int i) { return h.quat[4 * i + 2]; });
+        up(S.qw, [](const HostRods &h, int i) { return h.quat[4 * i + 3]; });
+        up(S.len, [](const HostRods &h, int i) { return h.len[i]; });
+        up(S.rad, [](const HostRods &h, int i) { return h.rad[i]; });
+        size_t o = 0;
+        for (int r = 0; r < R_; r++)
+            for (int i = 0; i < rods_[r].n; i++, o++) {
+                gbuf[o] = rods_[r].gid[i];
+                ibuf[o] = rods_[r].imm[i];
+                rbuf[o] = r;
+            }
+        CK(cudaMemcpy(S.gid, gbuf.data(), sizeof(long long) * N, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.imm, ibuf.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.rodRep, rbuf.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    }
+    // constraints
+    int want = fixedCap_ > 0 ? fixedCap_ : std::max(4096, 4 * N + 1024);
+    allocConstraints(want, false);
+    solverGrid_ = 0;
+    dirty_ = false;
+    haveDetect_ = false;
+    haveSolve_ = false;
+    CK(cudaStreamSynchronize(stream_));
+}
+
+void Engine::allocConstraints(int cap, bool keepPrev) {
+    DevState &S = S_;
+    unsigned long long *oldKeys = S.prevKeys;
+    double *oldGamma = S.prevGamma;
+    std::vector<void *> old;
+    old.swap(conAllocs_);
+    const int prevN = keepPrev ? hCtl_->totalColl : 0;
+    auto &G = conAllocs_;
+    S.cap = cap;
+    S.tileCap = cap / kTile + R_ + 2;
+    S.workCap = S.tileCap / kChunk + 2;
+    S.rawKeys = alloc<unsigned long long>(G, cap);
+    S.keys = alloc<unsigned long long>(G, cap);
+    S.prevKeys = alloc<unsigned long long>(G, cap);
+    S.prevGamma = alloc<double>(G, cap);
+    S.conI = alloc<int>(G, cap);
+    S.conJ = alloc<int>(G, cap);
+    S.conImg = alloc<int>(G, cap);
+    S.jac = alloc<double>(G, 12 * (size_t)cap);
+    double **cd[] = {&S.phi0, &S.q, &S.gamma, &S.g, &S.lb, &S.cinv};
+    for (double **p : cd) *p = alloc<double>(G, cap);
+    S.lab = alloc<double>(G, 6 * (size_t)cap);
+    S.rowEnt = alloc<int>(G, 2 * (size_t)cap);
+    if (precision_ == ALENS_PREC_MIXED) {
+        S.jac32 = alloc<float>(G, 12 * (size_t)cap);
+        float **fd[] = {&S.gamma32, &S.g32, &S.q32, &S.lb32, &S.cinv32};
+        for (float **p : fd) *p = alloc<float>(G, cap);
+    }
+    S.part = alloc<double>(G, 9 * (size_t)S.tileCap);
+    S.work = alloc<double>(G, 9 * (size_t)S.workCap);
+    S.tileRep = alloc<int>(G, S.tileCap);
+    if (keepPrev && prevN > 0 && oldKeys) {
+        const int n = std::min(prevN, cap);
+        CK(cudaMemcpyAsync(S.prevKeys, oldKeys, sizeof(unsigned long long) * n, cudaMemcpyDeviceToDevice, stream_));
+        CK(cudaMemcpyAsync(S.prevGamma, oldGamma, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+    freeGroup(old);
+}
+
+void Engine::updateRods(int rep, int n, const double *pos, const double *quat) {
+    if (rep < 0 || rep >= R_ || !rods_[rep].set || n != rods_[rep].n || !pos || !quat)
+        throw ApiError(ALENS_INVALID_ARG);
+    if (dirty_) {
+        std::copy(pos, pos + 3 * (size_t)n, rods_[rep].pos.begin());
+        std::copy(quat, quat + 4 * (size_t)n, rods_[rep].quat.begin());
+        return;
+    }
+    const int off = hostPar_[rep].rodOffset;
+    CK(cudaMemcpyAsync(S_.stage, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(S_.stage + 3 * (size_t)n, quat, sizeof(double) * 4 * (size_t)n,
+                       cudaMemcpyHostToDevice, stream_));
+    launch_unpack_rods(S_, off, n, stream_);
+    CK(cudaGetLastError());
+    haveDetect_ = haveSolve_ = false;
+}
+
+void Engine::getRods(int rep, int n, double *pos, double *quat) {
+    if (rep < 0 || rep >= R_ || !rods_[rep].set || n != rods_[rep].n) throw ApiError(ALENS_INVALID_ARG);
+    if (dirty_) {
+        if (pos) std::copy(rods_[rep].pos.begin(), rods_[rep].pos.end(), pos);
+        if (quat) std::copy(rods_[rep].quat.begin(), rods_[rep].quat.end(), quat);
+        return;
+    }
+    const int off = hostPar_[rep].rodOffset;
+    launch_pack_rods(S_, off, n, 0, stream_);
+    CK(cudaGetLastError());
+    if (pos) CK(cudaMemcpyAsync(pos, S_.stage, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, stream_));
+    if (quat)
+        CK(cudaMemcpyAsync(quat, S_.stage + 3 * (size_t)n, sizeof(double) * 4 * (size_t)n,
+                           cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+}
+
+void Engine::getVelocity(int rep, int n, double *vel, double *omega) {
+    if (rep < 0 || rep >= R_ || !rods_[rep].set || n != rods_[rep].n) throw ApiError(ALENS_INVALID_ARG);
+    if (dirty_) throw ApiError(ALENS_NOT_READY);
+    const int off = hostPar_[rep].rodOffset;
+    launch_pack_rods(S_, off, n, 1, stream_);
+    CK(cudaGetLastError());
+    if (vel) CK(cudaMemcpyAsync(vel, S_.stage, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, stream_));
+    if (omega)
+        CK(cudaMemcpyAsync(omega, S_.stage + 3 * (size_t)n, sizeof(double) * 3 * (size_t)n,
+                           cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+}
+
+void Engine::addBilateral(int rep, int n, const AlensBlock *blocks) {
+    if (rep < 0 || rep >= R_ || n < 0 || (n > 0 && !blocks)) throw ApiError(ALENS_INVALID_ARG);
+    const int nr = rods_[rep].n;
+    for (int b = 0; b < n; b++) {
+        const AlensBlock &B = blocks[b];
+        if (B.globalIndexI < 0 || B.globalIndexI >= nr) throw ApiError(ALENS_INVALID_ARG);
+        if (!B.oneSide && (B.globalIndexJ < 0 || B.globalIndexJ >= nr)) throw ApiError(ALENS_INVALID_ARG);
+    }
+    queue_[rep].insert(queue_[rep].end(), blocks, blocks + n);
+}
+
+// --------------------------------------------------------------- blocks
+void Engine::uploadBlocks() {
+    int total = 0;
+    hBilPrefix_[0] = 0;
+    for (int r = 0; r < R_; r++) {
+        total += (int)queue_[r].size();
+        hBilPrefix_[r + 1] = total;
+    }
+    if (total > blockCap_) {
+        CK(cudaStreamSynchronize(stream_));
+        invalidateGraph();
+        freeGroup(blockAllocs_);
+        if (hBlocks_) cudaFreeHost(hBlocks_);
+        if (hBlockRep_) cudaFreeHost(hBlockRep_);
+        blockCap_ = std::max(total, blockCap_ * 3 / 2);
+        S_.blocks = alloc<AlensBlock>(blockAllocs_, blockCap_);
+        S_.blockRep = alloc<int>(blockAllocs_, blockCap_);
+        CK(cudaMallocHost(&hBlocks_, sizeof(AlensBlock) * blockCap_));
+        CK(cudaMallocHost(&hBlockRep_, sizeof(int) * blockCap_));
+    }
+    S_.blockCap = blockCap_;
+    if (total > 0) {
+        // the previous step's copies out of the pinned buffers are complete:
+        // every step ends with a stream synchronisation
+        int o = 0;
+        for (int r = 0; r < R_; r++) {
+            std::memcpy(hBlocks_ + o, queue_[r].data(), sizeof(AlensBlock) * queue_[r].size());
+            for (size_t b = 0; b < queue_[r].size(); b++) hBlockRep_[o + b] = r;
+            o += (int)queue_[r].size();
+        }
+        CK(cudaMemcpyAsync(S_.blocks, hBlocks_, sizeof(AlensBlock) * total, cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync(S_.blockRep, hBlockRep_, sizeof(int) * total, cudaMemcpyHostToDevice, stream_));
+    }
+    CK(cudaMemcpyAsync(S_.bilPrefix, hBilPrefix_, sizeof(int) * (R_ + 1), cudaMemcpyHostToDevice, stream_));
+    nBilQueued_ = total;
+}
+
+// ---------------------------------------------------------- launch paths
+int Engine::enqueueDetect() {
+    DevState &S = S_;
+    int n = 0;
+    CK(cudaMemsetAsync(&S.ctl->rawCount, 0, 2 * sizeof(int), stream_));  // rawCount, errFlags
+    CK(cudaMemsetAsync(S.cellCount, 0, sizeof(int) * S.nCells, stream_));
+    CK(cudaMemsetAsync(S.cellCursor, 0, sizeof(int) * S.nCells, stream_));
+    CK(cudaMemsetAsync(S.pairCursor, 0, sizeof(int) * S.nRods, stream_));
+    CK(cudaMemsetAsync(S.rowCount, 0, sizeof(int) * S.nRods, stream_));
+    CK(cudaMemsetAsync(S.rowCursor, 0, sizeof(int) * S.nRods, stream_));
+    launch_prep(S, stream_);
+    n += 1;
+    n += launch_scan(S.cellCount, S.cellStart, S.nCells, S.scanTmp, stream_);
+    launch_scatter(S, stream_);
+    launch_pairs(S, stream_);
+    n += 2;
+    n += launch_scan(S.pairCount, S.pairOff, S.nRods, S.scanTmp, stream_);
+    n += launch_pair_sort(S, stream_);
+    launch_ranges(S, stream_);
+    launch_build(S, stream_);
+    n += 2;
+    n += launch_rows(S, stream_);
+    CK(cudaGetLastError());
+    return n;
+}
+
+void Engine::ensureSolverGrid() {
+    if (solverGrid_ > 0) return;
+    const int maxg = solver_max_grid(precision_);
+    solverGrid_ = std::min(maxg, numSM_ * solverBlocksPerSM_);
+    if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "solver occupancy");
+}
+
+int Engine::enqueueSolve(cudaEvent_t *ev) {
+    ensureSolverGrid();
+    int n = 0;
+    CK(launch_solve(S_, solverGrid_, precision_, kBarrierTimeoutNs, stream_, ev, &n));
+    return n;
+}
+
+int Engine::enqueueAdvance() {
+    launch_advance(S_, stream_);
+    CK(cudaGetLastError());
+    return 1;
+}
+
+void Engine::invalidateGraph() {
+    if (graphExec_) {
+        cudaGraphExecDestroy(graphExec_);
+        graphExec_ = nullptr;
+    }
+}
+
+bool Engine::buildGraph() {
+    ensureSolverGrid();
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    bool ok = true;
+    int n = 0;
+    try {
+        n += enqueueDetect();
+        n += enqueueSolve(nullptr);
+        n += enqueueAdvance();
+    } catch (...) {
+        ok = false;
+    }
+    cudaError_t e = cudaStreamEndCapture(stream_, &g);
+    if (!ok || e != cudaSuccess || !g) {
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        return false;
+    }
+    e = cudaGraphInstantiate(&graphExec_, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        graphExec_ = nullptr;
+        return false;
+    }
+    graphLaunches_ = n;
+    return true;
+}
+
+void Engine::readBack() {
+    CK(cudaMemcpyAsync(hCtl_, S_.ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaMemcpyAsync(hDyn_, S_.dyn, sizeof(RepDyn) * R_, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+}
+
+// Returns true if the constraint buffers were grown (the step must rerun).
+bool Engine::handleOverflow() {
+    if (!(hCtl_->errFlags & kErrOverflow)) return false;
+    const long long needColl = std::max<long long>(hCtl_->rawCount, hCtl_->totalColl);
+    const long long need = needColl + nBilQueued_;
+    lastNeeded_ = need;
+    if (fixedCap_ > 0) throw ApiError(ALENS_CAPACITY);
+    if (need >= (1LL << 30)) throw ApiError(ALENS_CAPACITY);
+    CK(cudaStreamSynchronize(stream_));
+    invalidateGraph();
+    allocConstraints((int)std::min<long long>(need + need / 2 + 1024, (1LL << 30) - 1), true);
+    return true;
+}
+
+int Engine::collectStats(int stage) {
+    int status = ALENS_OK;
+    const int fl = hCtl_->errFlags;
+    if (fl & kErrNaN) status = ALENS_NAN_DETECTED;
+    if (fl & kErrTimeout) status = ALENS_TIMEOUT;
+    AlensStepStats tot{};
+    tot.step = stepCount_;
+    tot.converged = 1;
+    for (int r = 0; r < R_; r++) {
+        const RepDyn &d = hDyn_[r];
+        AlensStepStats &s = repStats_[r];
+        s = AlensStepStats{};
+        s.step = stepCount_;
+        s.nRods = rods_[r].n;
+        s.nCollision = d.collEnd - d.collStart;
+        s.nBilateral = hBilPrefix_[r + 1] - hBilPrefix_[r];
+        if (stage >= 1) {
+            if (precision_ == ALENS_PREC_MIXED) {
+                s.iterations = d.refineIter;
+                s.refineIterations = d.iter;
+            } else {
+                s.iterations = d.iter;
+            }
+            s.residual = d.res;
+            s.converged = d.converged;
+            s.status = d.status;
+            if (d.status == ALENS_NOT_CONVERGED && status == ALENS_OK) status = ALENS_NOT_CONVERGED;
+            if (d.status == ALENS_NAN_DETECTED) status = ALENS_NAN_DETECTED;
+        }
+        tot.nRods += s.nRods;
+        tot.nCollision += s.nCollision;
+        tot.nBilateral += s.nBilateral;
+        tot.iterations = std::max(tot.iterations, s.iterations);
+        tot.refineIterations = std::max(tot.refineIterations, s.refineIterations);
+        tot.residual = std::max(tot.residual, s.residual);
+        tot.converged = tot.converged && (stage < 1 || s.converged);
+    }
+    tot.status = status;
+    last_ = tot;
+    return status;
+}
+
+void Engine::ensureEvents() {
+    if (events_[0]) return;
+    for (auto &e : events_) CK(cudaEventCreate(&e));
+}
+
+void Engine::recordStageTimes() {
+    float t[5] = {0, 0, 0, 0, 0};
+    // events: 0 detect start, 1 detect end / solve start, 2 main end,
+    // 3 refine start, 4 refine end, 5 advance end
+    CK(cudaEventElapsedTime(&t[0], events_[0], events_[1]));
+    CK(cudaEventElapsedTime(&t[1], events_[1], events_[2]));
+    if (precision_ == ALENS_PREC_MIXED) CK(cudaEventElapsedTime(&t[2], events_[3], events_[4]));
+    CK(cudaEventElapsedTime(&t[3], events_[4], events_[5]));
+    CK(cudaEventElapsedTime(&t[4], events_[0], events_[5]));
+    for (int i = 0; i < 5; i++) stageMs_[i] = t[i];
+}
+
+int Engine::step(AlensStepStats *out) {
+    finalize();
+    for (int attempt = 0; attempt < 8; attempt++) {
+        uploadBlocks();
+        bool launched = false;
+        if (useGraph_ && !stageTiming_) {
+            if (!graphExec_ && !graphFailed_) {
+                if (!buildGraph()) graphFailed_ = true;
+            }
+            if (graphExec_) {
+                CK(cudaGraphLaunch(graphExec_, stream_));
+                launches_ += graphLaunches_;
+                launched = true;
+            }
+        }
+        if (!launched) {
+            if (stageTiming_) {
+                ensureEvents();
+                CK(cudaEventRecord(events_[0], stream_));
+                launches_ += enqueueDetect();
+                // solve records events 1..4 (start, main end, refine start, refine end)
+                launches_ += enqueueSolve(&events_[1]);
+                launches_ += enqueueAdvance();
+                CK(cudaEventRecord(events_[5], stream_));
+            } else {
+                launches_ += enqueueDetect();
+                launches_ += enqueueSolve(nullptr);
+                launches_ += enqueueAdvance();
+            }
+        }
+        readBack();
+        if (handleOverflow()) continue;
+        if (stageTiming_ && !launched) recordStageTimes();
+        const int status = collectStats(2);
+        if (status == ALENS_OK || status == ALENS_NOT_CONVERGED) {
+            for (auto &q : queue_) q.clear();
+            stepCount_++;
+            last_.step = stepCount_ - 1;
+        }
+        haveDetect_ = haveSolve_ = false;
+        if (out) *out = last_;
+        return status;
+    }
+    throw ApiError(ALENS_CAPACITY);
+}
+
+int Engine::detect(AlensStepStats *out) {
+    finalize();
+    for (int attempt = 0; attempt < 8; attempt++) {
+        uploadBlocks();
+        launches_ += enqueueDetect();
+        readBack();
+        if (handleOverflow()) continue;
+        const int status = collectStats(0);
+        haveDetect_ = status == ALENS_OK;
+        haveSolve_ = false;
+        if (out) *out = last_;
+        return status;
+    }
+    throw ApiError(ALENS_CAPACITY);
+}
+
+int Engine::solve(AlensStepStats *out) {
+    if (!haveDetect_) throw ApiError(ALENS_NOT_READY);
+    launches_ += enqueueSolve(nullptr);
+    readBack();
+    const int status = collectStats(1);
+    haveSolve_ = (status == ALENS_OK || status == ALENS_NOT_CONVERGED);
+    if (out) *out = last_;
+    return status;
+}
+
+int Engine::advance(AlensStepStats *out) {
+    if (!haveSolve_) throw ApiError(ALENS_NOT_READY);
+    launches_ += enqueueAdvance();
+    readBack();
+    for (auto &q : queue_) q.clear();
+    stepCount_++;
+    haveDetect_ = haveSolve_ = false;
+    if (out) *out = last_;
+    return ALENS_OK;
+}
+
+void Engine::replicaStats(int rep, AlensStepStats *out) const {
+    if (rep < 0 || rep >= R_ || !out) throw ApiError(ALENS_INVALID_ARG);
+    *out = repStats_[rep];
+}
+
+void Engine::numConstraints(int rep, int *nColl, int *nBil) const {
+    if (rep < 0 || rep >= R_) throw ApiError(ALENS_INVALID_ARG);
+    if (nColl) *nColl = hDyn_[rep].collEnd - hDyn_[rep].collStart;
+    if (nBil) *nBil = hBilPrefix_[rep + 1] - hBilPrefix_[rep];
+}
+
+void Engine::getConstraints(int rep, int cap, int32_t *ii, int32_t *jj, int32_t *img, double *d0,
+                            double *gam, double *jac) {
+    if (rep < 0 || rep >= R_) throw ApiError(ALENS_INVALID_ARG);
+    if (dirty_) throw ApiError(ALENS_NOT_READY);
+    const RepDyn &d = hDyn_[rep];
+    const int n = d.nCon;
+    if (cap < n) throw ApiError(ALENS_CAPACITY);
+    if (n == 0) return;
+    const int k0 = d.conStart;
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream_));
+    };
+    if (ii) cp(ii, S_.conI + k0, sizeof(int) * n);
+    if (jj) cp(jj, S_.conJ + k0, sizeof(int) * n);
+    if (img) cp(img, S_.conImg + k0, sizeof(int) * n);
+    if (d0) cp(d0, S_.phi0 + k0, sizeof(double) * n);
+    if (gam) cp(gam, S_.gamma + k0, sizeof(double) * n);
+    if (jac) cp(jac, S_.jac + 12 * (size_t)k0, sizeof(double) * 12 * n);
+    CK(cudaStreamSynchronize(stream_));
+    const int off = hostPar_[rep].rodOffset;
+    for (int k = 0; k < n; k++) {
+        if (ii) ii[k] -= off;
+        if (jj && jj[k] >= 0) jj[k] -= off;
+    }
+}
+
+void Engine::conStress(int rep, double *out9) {
+    if (rep < 0 || rep >= R_ || !out9) throw ApiError(ALENS_INVALID_ARG);
+    if (dirty_) throw ApiError(ALENS_NOT_READY);
+    launch_stress(S_, stream_);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out9, S_.stress + 9 * (size_t)rep, sizeof(double) * 9, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+}
+
+}  // namespace alens

@@ -1,0 +1,132 @@
+// engine.cuh - device state of a context and the kernel launchers.
+//
+// Layout in HBM (all replicas of a context concatenated):
+//   rods        SoA FP64: px py pz | qx qy qz qw | len rad (72 B/rod) + gid,
+//               per-step axis, collision half-length/radius, mobilities,
+//               known velocity (6 SoA) and solver velocity U (6 SoA)
+//   cells       count/start/cursor per cell; cell-sorted copy of the search
+//               geometry (centre, axis, half-length, radius, rod index)
+//   pairs       raw 64-bit keys (i<<32 | j<<5 | image), per-rod counts and
+//               offsets, canonical keys sorted by (i, j, image)
+//   constraints AoS Jacobian 12 x FP64 (96 B) [+ 12 x FP32 copy for the
+//               mixed solver], rod indices I/J, phi0, q, gamma, g, lower
+//               bound, compliance, lab points
+//   rod rows    rod-major rows of D: entries 2k+side, ascending (CSR)
+//   reduction   level-1 tile partials (4 kinds) + chunk work space
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "alens_gpu.h"
+#include "common.cuh"
+
+namespace alens {
+
+struct RepParams {
+    double lo[3], hi[3], L[3];
+    double cellsz[3];
+    double mu, kT, dt, colRatioD, colRatioL, colBuf, tol;
+    unsigned long long seed;
+    int pbc[3];
+    int mono;
+    int ncell[3];
+    int cellOffset;
+    int rodOffset;
+    int nRods;
+    int maxIte;
+    int pad;
+};
+
+// per-replica state produced on the device
+struct RepDyn {
+    int collStart, collEnd;   // range in the canonical collision list
+    int conStart, nCon;       // constraint range
+    int tileStart, nTiles;    // level-1 tiles of the constraint range
+    int iter, active, converged, status;
+    int counter;              // last-arriver ticket of the current pass
+    int refineIter;
+    double alpha, res;
+};
+
+struct DevCtl {
+    long long step;
+    int rawCount;     // collision pairs found (may exceed capacity)
+    int errFlags;     // kErr* bits
+    int totalColl, totalBil, totalCon, nTiles;
+    int activeCount;
+    int maxIte;       // max over replicas
+    GridBarrier bar;
+};
+
+// Device pointers and sizes of one context; passed to kernels by value.
+struct DevState {
+    int R, nRods, cap, nCells, tileCap, workCap, blockCap;
+    int warm, precision;
+    RepParams *par;
+    RepDyn *dyn;
+    DevCtl *ctl;
+    int *bilPrefix;  // [R+1] blocks per replica (prefix, host-written)
+    // rods
+    double *px, *py, *pz, *qx, *qy, *qz, *qw, *len, *rad;
+    long long *gid;
+    int *imm, *rodRep;
+    double *ax, *ay, *az, *hcol, *rcol, *m0, *m1, *m2;
+    unsigned char *sph;
+    double *unc, *vel, *U;  // 6 x nRods SoA each
+    float *U32;             // 6 x nRods SoA (mixed solver)
+    double *stage;          // 7 x nRods host-transfer staging (interleaved)
+    // cells
+    int *cellOf, *cellCount, *cellStart, *cellCursor;
+    double *sx, *sy, *sz, *sax, *say, *saz, *sh, *sr;
+    int *sidx;
+    // pairs
+    int *pairCount, *pairOff, *pairCursor;
+    unsigned long long *rawKeys, *keys;
+    // constraints
+    int *conI, *conJ, *conImg;
+    double *jac;
+    float *jac32;
+    double *phi0, *q, *gamma, *g, *lb, *cinv, *lab;
+    float *gamma32, *g32, *q32, *lb32, *cinv32;
+    int *rowCount, *rowPtr, *rowCursor, *rowEnt;
+    unsigned long long *prevKeys;
+    double *prevGamma;
+    int *prevCount;
+    AlensBlock *blocks;
+    int *blockRep;
+    // reductions
+    double *part;   // 4 x tileCap
+    double *work;   // 4 x workCap
+    int *tileRep;   // tileCap
+    double *stress; // 9 x R outputs
+    // scan scratch
+    int *scanTmp;
+};
+
+// ---- detect stage (kernels_detect.cu)
+void launch_prep(const DevState &S, cudaStream_t st);
+int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st);  // returns kernels launched
+void launch_scatter(const DevState &S, cudaStream_t st);
+void launch_pairs(const DevState &S, cudaStream_t st);
+int launch_pair_sort(const DevState &S, cudaStream_t st);
+void launch_ranges(const DevState &S, cudaStream_t st);
+void launch_build(const DevState &S, cudaStream_t st);
+int launch_rows(const DevState &S, cudaStream_t st);
+void launch_unpack_rods(const DevState &S, int rodOffset, int n, cudaStream_t st);
+void launch_pack_rods(const DevState &S, int rodOffset, int n, int what, cudaStream_t st);
+
+// ---- solve / advance (kernels_solve.cu)
+struct SolveLaunch {
+    int grid;
+    int block;
+};
+int solver_max_grid(int precision);  // cooperative residency limit
+// precision == MIXED: FP32 kernel, state reset, FP64 refinement kernel
+// (events ev[0..3] recorded around the two kernels when non-null).
+cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned long long timeout_ns,
+                         cudaStream_t st, cudaEvent_t *ev, int *launches);
+void launch_advance(const DevState &S, cudaStream_t st);
+void launch_stress(const DevState &S, cudaStream_t st);
+
+}  // namespace alens

@@ -1,0 +1,116 @@
+// engine.h - host-side context of the GPU rod step (one CUDA stream).
+#pragma once
+
+#include <cstdlib>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace alens {
+
+struct ApiError {
+    int status;
+    explicit ApiError(int s) : status(s) {}
+};
+
+struct CudaFailure {
+    cudaError_t err;
+    const char *where;
+    CudaFailure(cudaError_t e, const char *w) : err(e), where(w) {}
+};
+
+class Engine {
+  public:
+    Engine(const AlensConfig *cfgs, int nrep);
+    ~Engine();
+    Engine(const Engine &) = delete;
+    Engine &operator=(const Engine &) = delete;
+
+    void setRods(int rep, int n, const int64_t *gid, const double *pos, const double *quat,
+                 const double *len, const double *rad, const int32_t *imm);
+    void updateRods(int rep, int n, const double *pos, const double *quat);
+    void getRods(int rep, int n, double *pos, double *quat);
+    void getVelocity(int rep, int n, double *vel, double *omega);
+    void addBilateral(int rep, int n, const AlensBlock *blocks);
+    int step(AlensStepStats *out);
+    int detect(AlensStepStats *out);
+    int solve(AlensStepStats *out);
+    int advance(AlensStepStats *out);
+    void replicaStats(int rep, AlensStepStats *out) const;
+    void numConstraints(int rep, int *nColl, int *nBil) const;
+    void getConstraints(int rep, int cap, int32_t *ii, int32_t *jj, int32_t *img, double *d0,
+                        double *gam, double *jac);
+    void conStress(int rep, double *out9);
+    long long stepCount() const { return stepCount_; }
+    cudaStream_t stream() const { return stream_; }
+    long long lastNeeded() const { return lastNeeded_; }
+    long long launches() const { return launches_; }
+    const double *stageMs() const { return stageMs_; }
+    const DevState &state() const { return S_; }
+    int replicas() const { return R_; }
+
+  private:
+    struct HostRods {
+        int n = 0;
+        bool set = false;
+        std::vector<long long> gid;
+        std::vector<double> pos, quat, len, rad;
+        std::vector<int> imm;
+    };
+
+    void makeParams(int rep, const HostRods &h, RepParams &P) const;
+    void finalize();
+    void allocConstraints(int cap, bool keepPrev);
+    void uploadBlocks();
+    int enqueueDetect();
+    int enqueueSolve(cudaEvent_t *ev);
+    void ensureSolverGrid();
+    int enqueueAdvance();
+    void ensureEvents();
+    void recordStageTimes();
+    bool buildGraph();
+    void invalidateGraph();
+    void readBack();
+    bool handleOverflow();
+    int collectStats(int stage);
+    void freeGroup(std::vector<void *> &g);
+    template <class T>
+    T *alloc(std::vector<void *> &group, size_t n);
+
+    std::vector<AlensConfig> cfg_;
+    int R_ = 0;
+    int device_ = 0, numSM_ = 0;
+    cudaStream_t stream_ = nullptr;
+    bool ownStream_ = false;
+    int precision_ = 0, warm_ = 0;
+    bool useGraph_ = true, graphFailed_ = false;
+    int fixedCap_ = 0;
+    int solverBlocksPerSM_ = 2;
+    int solverGrid_ = 0;
+    std::vector<HostRods> rods_;
+    std::vector<std::vector<AlensBlock>> queue_;
+    std::vector<RepParams> hostPar_;
+    bool dirty_ = true;
+    bool haveDetect_ = false, haveSolve_ = false;
+    DevState S_{};
+    std::vector<void *> rodAllocs_, conAllocs_, blockAllocs_, fixedAllocs_;
+    int blockCap_ = 0;
+    int nBilQueued_ = 0;
+    AlensBlock *hBlocks_ = nullptr;
+    int *hBlockRep_ = nullptr;
+    DevCtl *hCtl_ = nullptr;
+    RepDyn *hDyn_ = nullptr;
+    int *hBilPrefix_ = nullptr;
+    cudaGraphExec_t graphExec_ = nullptr;
+    int graphLaunches_ = 0;
+    long long launches_ = 0;
+    bool stageTiming_ = false;
+    cudaEvent_t events_[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    double stageMs_[5] = {0, 0, 0, 0, 0};
+    long long stepCount_ = 0;
+    long long lastNeeded_ = 0;
+    AlensStepStats last_{};
+    std::vector<AlensStepStats> repStats_;
+};
+
+}  // namespace alens

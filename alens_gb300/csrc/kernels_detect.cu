@@ -1,0 +1,681 @@
+// kernels_detect.cu - detect stage of the rod step: known (Brownian)
+// velocity, cell binning, near-pair search with segment-segment closest
+// points, canonical pair order, constraint assembly (Jacobian D, phi0, q,
+// initial gamma) and the rod-major rows of D.
+//
+// The role of SimToolbox's FDPS near-neighbour search + CalcSylinderNearForce
+// + DCPQuery + ConstraintCollector (called from SylinderSystem::runStep,
+// SRC/TubuleSystem.cpp:223; collision buffer sylinderColBuf,
+// docs/source/quickstart.md:346-348; bilateral blocks as built in
+// SRC/TubuleSystem.cpp:714-742).
+//
+// Compiled with --fmad=false: FP64 results equal the oracle's bit for bit.
+#include <cmath>
+
+#include "engine.cuh"
+
+namespace alens {
+
+namespace {
+
+__device__ __forceinline__ int flags(const DevState &S) { return ld_volatile_i32(&S.ctl->errFlags); }
+
+__device__ __forceinline__ int cell_coord(double v, double lo, double cs, int n) {
+    const double f = floor((v - lo) / cs);
+    return f < 0.0 ? 0 : (f > (double)(n - 1) ? n - 1 : (int)f);
+}
+
+// ------------------------------------------------------------------ prep
+__global__ void k_prep(DevState S) {
+    const long long step = S.ctl->step;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
+        const int rep = S.rodRep[r];
+        const RepParams &P = S.par[rep];
+        double p[3] = {S.px[r], S.py[r], S.pz[r]};
+        const double qx = S.qx[r], qy = S.qy[r], qz = S.qz[r], qw = S.qw[r];
+        if (!isfinite(p[0]) || !isfinite(p[1]) || !isfinite(p[2]) || !isfinite(qx) ||
+            !isfinite(qy) || !isfinite(qz) || !isfinite(qw)) {
+            atomicOr(&S.ctl->errFlags, kErrNaN);
+            S.cellOf[r] = P.cellOffset;
+            atomicAdd(&S.cellCount[P.cellOffset], 1);
+            continue;
+        }
+        for (int d = 0; d < 3; d++) {
+            if (!P.pbc[d]) continue;
+            const double lo = P.lo[d], hi = P.hi[d], Lb = P.L[d];
+            double v = p[d];
+            for (int k = 0; k < 64; k++) {
+                if (v < lo)
+                    v = v + Lb;
+                else if (v >= hi)
+                    v = v - Lb;
+                else
+                    break;
+            }
+            p[d] = v;
+        }
+        S.px[r] = p[0];
+        S.py[r] = p[1];
+        S.pz[r] = p[2];
+        double a[3];
+        quat_axis(qx, qy, qz, qw, a);
+        S.ax[r] = a[0];
+        S.ay[r] = a[1];
+        S.az[r] = a[2];
+        const double L = S.len[r], rad = S.rad[r];
+        const bool sphere = L < 2.0 * rad;
+        S.sph[r] = sphere ? 1 : 0;
+        S.hcol[r] = sphere ? 0.0 : 0.5 * (L * P.colRatioL);
+        S.rcol[r] = rad * P.colRatioD;
+        double m[3] = {0.0, 0.0, 0.0};
+        const bool imm = S.imm[r] != 0;
+        if (!imm) mobility_coeffs(L, rad, P.mu, sphere, m);
+        S.m0[r] = m[0];
+        S.m1[r] = m[1];
+        S.m2[r] = m[2];
+        double u[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (P.kT > 0.0 && !imm) {
+            const double bc = sqrt(2.0 * P.kT / P.dt);
+            double z[6];
+            normals6(P.seed, S.gid[r], step, z);
+            if (P.mono) {
+                z[2] = 0.0;
+                z[3] = 0.0;
+                z[4] = 0.0;
+            }
+            double w[6];
+            if (sphere) {
+                const double st = sqrt(m[0]), sr = sqrt(m[2]);
+                w[0] = st * z[0];
+                w[1] = st * z[1];
+                w[2] = st * z[2];
+                w[3] = sr * z[3];
+                w[4] = sr * z[4];
+                w[5] = sr * z[5];
+            } else {
+                const double sp = sqrt(m[0]), sq = sqrt(m[1]), sr = sqrt(m[2]);
+                const double za = a[0] * z[0] + a[1] * z[1] + a[2] * z[2];
+                w[0] = sp * za * a[0] + sq * (z[0] - za * a[0]);
+                w[1] = sp * za * a[1] + sq * (z[1] - za * a[1]);
+                w[2] = sp * za * a[2] + sq * (z[2] - za * a[2]);
+                const double ra = a[0] * z[3] + a[1] * z[4] + a[2] * z[5];
+                w[3] = sr * (z[3] - ra * a[0]);
+                w[4] = sr * (z[4] - ra * a[1]);
+                w[5] = sr * (z[5] - ra * a[2]);
+            }
+            if (P.mono) {
+                w[2] = 0.0;
+                w[3] = 0.0;
+                w[4] = 0.0;
+            }
+#pragma unroll
+            for (int k = 0; k < 6; k++) u[k] = bc * w[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 6; k++) S.unc[(size_t)k * S.nRods + r] = u[k];
+        const int cx = cell_coord(p[0], P.lo[0], P.cellsz[0], P.ncell[0]);
+        const int cy = cell_coord(p[1], P.lo[1], P.cellsz[1], P.ncell[1]);
+        const int cz = cell_coord(p[2], P.lo[2], P.cellsz[2], P.ncell[2]);
+        const int cid = P.cellOffset + (cz * P.ncell[1] + cy) * P.ncell[0] + cx;
+        S.cellOf[r] = cid;
+        atomicAdd(&S.cellCount[cid], 1);
+    }
+}
+
+// ------------------------------------------------------------------ scan
+// Exclusive scan of n ints: out[0..n] (out[n] = total).  Three passes:
+// per-block scan of 1024 elements, scan of block totals, add.
+constexpr int kScanBlock = 256;
+constexpr int kScanPer = 4;
+constexpr int kScanSpan = kScanBlock * kScanPer;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *smem32, int *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int o = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += o;
+    }
+    if (lane == 31) smem32[warp] = incl;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    if (warp == 0) {
+        int w = lane < nw ? smem32[lane] : 0;
+        int wi = w;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int o = __shfl_up_sync(0xffffffffu, wi, off);
+            if (lane >= off) wi += o;
+        }
+        if (lane < nw) smem32[lane] = wi - w;
+        if (lane == nw - 1) smem32[32] = wi;
+    }
+    __syncthreads();
+    const int res = incl - v + smem32[warp];
+    if (total) *total = smem32[32];
+    __syncthreads();
+    return res;
+}
+
+__global__ void k_scan_block(const int *in, int *out, int n, int *tmp) {
+    __shared__ int sm[33];
+    const int base = blockIdx.x * kScanSpan + threadIdx.x * kScanPer;
+    int v[kScanPer];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        s += v[k];
+    }
+    int tot;
+    int ex = block_exclusive_scan(s, sm, &tot);
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+        if (base + k < n) out[base + k] = ex;
+        ex += v[k];
+    }
+    if (threadIdx.x == 0) tmp[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_top(int *tmp, int nb, int *out, int n) {
+    __shared__ int sm[33];
+    // up to 1024 threads x 4 = 4096 block totals
+    const int base = threadIdx.x * 4;
+    int v[4];
+    int s = 0;
+    for (int k = 0; k < 4; k++) {
+        v[k] = (base + k < nb) ? tmp[base + k] : 0;
+        s += v[k];
+    }
+    int tot;
+    int ex = block_exclusive_scan(s, sm, &tot);
+    for (int k = 0; k < 4; k++) {
+        if (base + k < nb) tmp[base + k] = ex;
+        ex += v[k];
+    }
+    if (threadIdx.x == 0) out[n] = tot;
+}
+
+__global__ void k_scan_add(int *out, int n, const int *tmp) {
+    const int add = tmp[blockIdx.x];
+    const int base = blockIdx.x * kScanSpan + threadIdx.x * kScanPer;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++)
+        if (base + k < n) out[base + k] += add;
+}
+
+// ------------------------------------------------------------- scatter
+__global__ void k_scatter(DevState S) {
+    if (flags(S) & kErrNaN) return;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
+        const int cid = S.cellOf[r];
+        const int slot = S.cellStart[cid] + atomicAdd(&S.cellCursor[cid], 1);
+        S.sx[slot] = S.px[r];
+        S.sy[slot] = S.py[r];
+        S.sz[slot] = S.pz[r];
+        S.sax[slot] = S.ax[r];
+        S.say[slot] = S.ay[r];
+        S.saz[slot] = S.az[r];
+        S.sh[slot] = S.hcol[r];
+        S.sr[slot] = S.rcol[r];
+        S.sidx[slot] = r;
+    }
+}
+
+// ---------------------------------------------------------- pair search
+constexpr int kPairBuf = 16;
+constexpr int kPairThreads = 128;
+
+__device__ __forceinline__ void flush_keys(const DevState &S, const unsigned long long *buf, int nb) {
+    const int base = atomicAdd(&S.ctl->rawCount, nb);
+    for (int e = 0; e < nb; e++) {
+        const int pos = base + e;
+        if (pos < S.cap)
+            S.rawKeys[pos] = buf[e];
+        else
+            atomicOr(&S.ctl->errFlags, kErrOverflow);
+    }
+}
+
+// One thread per cell-sorted slot; the warp walks neighbour cells mostly in
+// lockstep, so candidate loads are broadcasts.
+__global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = t < S.nRods && !(flags(S) & kErrNaN);
+    unsigned long long buf[kPairBuf];
+    int nb = 0;
+    if (valid) {
+        int cnt = 0;
+        const int i = S.sidx[t];
+        const RepParams &P = S.par[S.rodRep[i]];
+        const double pi[3] = {S.sx[t], S.sy[t], S.sz[t]};
+        const double ai[3] = {S.sax[t], S.say[t], S.saz[t]};
+        const double hi_ = S.sh[t], ri = S.sr[t];
+        const double colBuf = P.colBuf;
+        const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
+        const int lc = S.cellOf[i] - P.cellOffset;
+        const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
+        for (int oz = -1; oz <= 1; oz++) {
+            int z = cz + oz, sz = 0;
+            if (z < 0 || z >= nz) {
+                if (!P.pbc[2]) continue;
+                if (z < 0) {
+                    z += nz;
+                    sz = -1;
+                } else {
+                    z -= nz;
+                    sz = 1;
+                }
+            }
+            for (int oy = -1; oy <= 1; oy++) {
+                int y = cy + oy, sy = 0;
+                if (y < 0 || y >= ny) {
+                    if (!P.pbc[1]) continue;
+                    if (y < 0) {
+                        y += ny;
+                        sy = -1;
+                    } else {
+                        y -= ny;
+                        sy = 1;
+                    }
+                }
+                for (int ox = -1; ox <= 1; ox++) {
+                    int xx = cx + ox, sx = 0;
+                    if (xx < 0 || xx >= nx) {
+                        if (!P.pbc[0]) continue;
+                        if (xx < 0) {
+                            xx += nx;
+                            sx = -1;
+                        } else {
+                            xx -= nx;
+                            sx = 1;
+                        }
+                    }
+                    const int img = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
+                    const double S0 = (double)sx * P.L[0];
+                    const double S1 = (double)sy * P.L[1];
+                    const double S2 = (double)sz * P.L[2];
+                    const int cell = P.cellOffset + (z * ny + y) * nx + xx;
+                    const int m1 = S.cellStart[cell + 1];
+                    for (int m = S.cellStart[cell]; m < m1; m++) {
+                        const int j = S.sidx[m];
+                        if (j < i) continue;
+                        if (j == i && img <= kImageNone) continue;
+                        const double c2[3] = {S.sx[m] + S0, S.sy[m] + S1, S.sz[m] + S2};
+                        const double d0 = pi[0] - c2[0], d1 = pi[1] - c2[1], d2 = pi[2] - c2[2];
+                        const double dd = d0 * d0 + d1 * d1 + d2 * d2;
+                        const double hj = S.sh[m], rj = S.sr[m];
+                        const double lim = hi_ + hj + ri + rj + colBuf;
+                        if (dd > lim * lim * (1.0 + 1e-10) + 1e-300) continue;
+                        const double aj[3] = {S.sax[m], S.say[m], S.saz[m]};
+                        const DcpResult R = dcp_segseg(pi, ai, hi_, c2, aj, hj);
+                        const double sep = R.dist - ri - rj;
+                        if (sep < colBuf) {
+                            if (nb == kPairBuf) {
+                                flush_keys(S, buf, nb);
+                                nb = 0;
+                            }
+                            buf[nb++] = pair_key(i, j, img);
+                            cnt++;
+                        }
+                    }
+                }
+            }
+        }
+        S.pairCount[i] = cnt;
+    }
+    // warp-aggregated append of the remaining keys
+    const int lane = threadIdx.x & 31;
+    int incl = nb;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int o = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += o;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(&S.ctl->rawCount, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    const int start = base + incl - nb;
+    for (int e = 0; e < nb; e++) {
+        const int pos = start + e;
+        if (pos < S.cap)
+            S.rawKeys[pos] = buf[e];
+        else
+            atomicOr(&S.ctl->errFlags, kErrOverflow);
+    }
+}
+
+// Place raw keys into their rod's segment, then sort each segment: the
+// canonical order is (i, j, image) ascending.
+__global__ void k_pair_bucket(DevState S) {
+    if (flags(S) & (kErrNaN | kErrOverflow)) return;
+    const int n = S.ctl->rawCount;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const unsigned long long key = S.rawKeys[p];
+        const int i = (int)(key >> 32);
+        const int slot = S.pairOff[i] + atomicAdd(&S.pairCursor[i], 1);
+        S.keys[slot] = key;
+    }
+}
+
+__global__ void k_pair_segsort(DevState S) {
+    if (flags(S) & (kErrNaN | kErrOverflow)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nRods; i += gridDim.x * blockDim.x) {
+        const int b = S.pairOff[i], e = S.pairOff[i + 1];
+        for (int x = b + 1; x < e; x++) {
+            const unsigned long long v = S.keys[x];
+            int y = x - 1;
+            while (y >= b && S.keys[y] > v) {
+                S.keys[y + 1] = S.keys[y];
+                y--;
+            }
+            S.keys[y + 1] = v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- ranges
+// One block: per-replica constraint/tile ranges, totals, solver state.
+__global__ void k_ranges(DevState S) {
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        DevCtl *c = S.ctl;
+        int tile = 0, active = 0, maxIte = 0;
+        const int totalColl = S.pairOff[S.nRods];
+        for (int r = 0; r < S.R; r++) {
+            const RepParams &P = S.par[r];
+            RepDyn &d = S.dyn[r];
+            d.collStart = S.pairOff[P.rodOffset];
+            d.collEnd = S.pairOff[P.rodOffset + P.nRods];
+            const int nBil = S.bilPrefix[r + 1] - S.bilPrefix[r];
+            d.conStart = d.collStart + S.bilPrefix[r];
+            d.nCon = (d.collEnd - d.collStart) + nBil;
+            d.nTiles = (d.nCon + kTile - 1) / kTile;
+            d.tileStart = tile;
+            tile += d.nTiles;
+            d.iter = 0;
+            d.refineIter = 0;
+            d.active = d.nCon > 0 ? 1 : 0;
+            d.converged = d.nCon > 0 ? 0 : 1;
+            d.status = 0;
+            d.counter = 0;
+            d.alpha = 0.0;
+            d.res = 0.0;
+            active += d.active;
+            maxIte = P.maxIte > maxIte ? P.maxIte : maxIte;
+        }
+        c->totalColl = totalColl;
+        c->totalBil = S.bilPrefix[S.R];
+        c->totalCon = totalColl + S.bilPrefix[S.R];
+        c->nTiles = tile;
+        c->activeCount = active;
+        c->maxIte = maxIte;
+        c->bar.count = 0;
+        c->bar.gen = 0;
+        int ok = 1;
+        if (c->totalCon > S.cap || tile > S.tileCap) {
+            atomicOr(&c->errFlags, kErrOverflow);
+            ok = 0;
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok || (flags(S) & (kErrNaN | kErrOverflow))) return;
+    for (int r = 0; r < S.R; r++) {
+        const RepDyn &d = S.dyn[r];
+        for (int t = threadIdx.x; t < d.nTiles; t += blockDim.x) S.tileRep[d.tileStart + t] = r;
+    }
+}
+
+// ----------------------------------------------------------------- build
+__device__ __forceinline__ double dot6s(const double *J, const double *U, size_t stride, int r) {
+    return J[0] * U[r] + J[1] * U[stride + r] + J[2] * U[2 * stride + r] + J[3] * U[3 * stride + r] +
+           J[4] * U[4 * stride + r] + J[5] * U[5 * stride + r];
+}
+
+__device__ void finish_constraint(const DevState &S, int k, const RepParams &P, int I, int J,
+                                  const double *jac, double phi0, double gamma0, double lb,
+                                  double cinv) {
+    const size_t st = (size_t)S.nRods;
+    const double dI = dot6s(jac, S.unc, st, I);
+    const double dJ = J >= 0 ? dot6s(jac + 6, S.unc, st, J) : 0.0;
+    const double q = phi0 + P.dt * (dI + dJ);
+    const double g0 = gamma0 < lb ? lb : gamma0;
+    S.q[k] = q;
+    S.gamma[k] = g0;
+    S.lb[k] = lb;
+    S.cinv[k] = cinv;
+    S.phi0[k] = phi0;
+    atomicAdd(&S.rowCount[I], 1);
+    if (J >= 0) atomicAdd(&S.rowCount[J], 1);
+    if (S.precision == ALENS_PREC_MIXED) {
+#pragma unroll
+        for (int c = 0; c < 12; c++) S.jac32[12 * (size_t)k + c] = (float)jac[c];
+        S.q32[k] = (float)q;
+        S.gamma32[k] = (float)g0;
+        S.lb32[k] = (float)lb;
+        S.cinv32[k] = (float)cinv;
+    }
+}
+
+__global__ void k_build(DevState S) {
+    if (flags(S) & (kErrNaN | kErrOverflow)) return;
+    const int totalColl = S.ctl->totalColl, totalBil = S.ctl->totalBil;
+    const bool warmPrev = S.warm == ALENS_WARM_PREV || S.warm == ALENS_WARM_MLP;
+    const int prevN = *S.prevCount;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < totalColl; p += gridDim.x * blockDim.x) {
+        const unsigned long long key = S.keys[p];
+        const int i = (int)(key >> 32), j = (int)((key >> 5) & 0x7ffffff), img = (int)(key & 31);
+        const int rep = S.rodRep[i];
+        const RepParams &P = S.par[rep];
+        const int k = p + S.bilPrefix[rep];
+        const int sv[3] = {img / 9 - 1, (img / 3) % 3 - 1, img % 3 - 1};
+        const double c1[3] = {S.px[i], S.py[i], S.pz[i]};
+        const double c2[3] = {S.px[j] + (double)sv[0] * P.L[0], S.py[j] + (double)sv[1] * P.L[1],
+                              S.pz[j] + (double)sv[2] * P.L[2]};
+        const double ai[3] = {S.ax[i], S.ay[i], S.az[i]};
+        const double aj[3] = {S.ax[j], S.ay[j], S.az[j]};
+        const DcpResult R = dcp_segseg(c1, ai, S.hcol[i], c2, aj, S.hcol[j]);
+        double n[3];
+        contact_normal(R, ai, aj, n);
+        const double sep = R.dist - S.rcol[i] - S.rcol[j];
+        double J[12];
+        const double rI[3] = {R.s * ai[0], R.s * ai[1], R.s * ai[2]};
+        const double rJ[3] = {R.t * aj[0], R.t * aj[1], R.t * aj[2]};
+        const double nJ[3] = {-n[0], -n[1], -n[2]};
+        J[0] = n[0];
+        J[1] = n[1];
+        J[2] = n[2];
+        cross3(rI, n, J + 3);
+        J[6] = nJ[0];
+        J[7] = nJ[1];
+        J[8] = nJ[2];
+        cross3(rJ, nJ, J + 9);
+#pragma unroll
+        for (int c = 0; c < 12; c++) S.jac[12 * (size_t)k + c] = J[c];
+        S.conI[k] = i;
+        S.conJ[k] = j;
+        S.conImg[k] = img;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            S.lab[6 * (size_t)k + d] = R.P[d];
+            S.lab[6 * (size_t)k + 3 + d] = R.Q[d];
+        }
+        double g0 = 0.0;
+        if (warmPrev && prevN > 0) {
+            int lo = 0, hi = prevN;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (S.prevKeys[mid] < key)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            if (lo < prevN && S.prevKeys[lo] == key) g0 = S.prevGamma[lo];
+        }
+        finish_constraint(S, k, P, i, j, J, sep, g0, 0.0, 0.0);
+    }
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < totalBil; b += gridDim.x * blockDim.x) {
+        const AlensBlock &B = S.blocks[b];
+        const int rep = S.blockRep[b];
+        const RepParams &P = S.par[rep];
+        const int k = S.dyn[rep].collEnd + b;
+        const int I = P.rodOffset + B.globalIndexI;
+        const int Jr = B.oneSide ? -1 : P.rodOffset + B.globalIndexJ;
+        double J[12];
+        J[0] = B.normI[0];
+        J[1] = B.normI[1];
+        J[2] = B.normI[2];
+        cross3(B.posI, B.normI, J + 3);
+        if (!B.oneSide) {
+            J[6] = B.normJ[0];
+            J[7] = B.normJ[1];
+            J[8] = B.normJ[2];
+            cross3(B.posJ, B.normJ, J + 9);
+        } else {
+#pragma unroll
+            for (int c = 6; c < 12; c++) J[c] = 0.0;
+        }
+#pragma unroll
+        for (int c = 0; c < 12; c++) S.jac[12 * (size_t)k + c] = J[c];
+        S.conI[k] = I;
+        S.conJ[k] = Jr;
+        S.conImg[k] = -1;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            S.lab[6 * (size_t)k + d] = B.labI[d];
+            S.lab[6 * (size_t)k + 3 + d] = B.labJ[d];
+        }
+        const double lb = B.bilateral ? -INFINITY : B.gammaLB;
+        const double cinv = (B.bilateral && B.kappa > 0.0) ? 1.0 / B.kappa : 0.0;
+        finish_constraint(S, k, P, I, Jr, J, B.delta0, B.gamma, lb, cinv);
+    }
+}
+
+// ------------------------------------------------------------- rod rows
+__global__ void k_rows_fill(DevState S) {
+    if (flags(S) & (kErrNaN | kErrOverflow)) return;
+    const int nc = S.ctl->totalCon;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) {
+        const int I = S.conI[k], J = S.conJ[k];
+        S.rowEnt[S.rowPtr[I] + atomicAdd(&S.rowCursor[I], 1)] = 2 * k;
+        if (J >= 0) S.rowEnt[S.rowPtr[J] + atomicAdd(&S.rowCursor[J], 1)] = 2 * k + 1;
+    }
+}
+
+__global__ void k_rows_sort(DevState S) {
+    if (flags(S) & (kErrNaN | kErrOverflow)) return;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
+        const int b = S.rowPtr[r], e = S.rowPtr[r + 1];
+        for (int x = b + 1; x < e; x++) {
+            const int v = S.rowEnt[x];
+            int y = x - 1;
+            while (y >= b && S.rowEnt[y] > v) {
+                S.rowEnt[y + 1] = S.rowEnt[y];
+                y--;
+            }
+            S.rowEnt[y + 1] = v;
+        }
+    }
+}
+
+// ------------------------------------------------- host <-> device rods
+// stage layout: pos[3n] then quat[4n] (x,y,z,w), interleaved per rod.
+__global__ void k_unpack_rods(DevState S, int off, int n) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const double *p = S.stage + 3 * (size_t)r;
+        const double *q = S.stage + 3 * (size_t)n + 4 * (size_t)r;
+        S.px[off + r] = p[0];
+        S.py[off + r] = p[1];
+        S.pz[off + r] = p[2];
+        S.qx[off + r] = q[0];
+        S.qy[off + r] = q[1];
+        S.qz[off + r] = q[2];
+        S.qw[off + r] = q[3];
+    }
+}
+
+__global__ void k_pack_rods(DevState S, int off, int n, int what) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        if (what == 0) {
+            double *p = S.stage + 3 * (size_t)r;
+            double *q = S.stage + 3 * (size_t)n + 4 * (size_t)r;
+            p[0] = S.px[off + r];
+            p[1] = S.py[off + r];
+            p[2] = S.pz[off + r];
+            q[0] = S.qx[off + r];
+            q[1] = S.qy[off + r];
+            q[2] = S.qz[off + r];
+            q[3] = S.qw[off + r];
+        } else {
+            double *v = S.stage + 3 * (size_t)r;
+            double *w = S.stage + 3 * (size_t)n + 3 * (size_t)r;
+            const size_t st = (size_t)S.nRods;
+            for (int c = 0; c < 3; c++) {
+                v[c] = S.vel[c * st + off + r];
+                w[c] = S.vel[(c + 3) * st + off + r];
+            }
+        }
+    }
+}
+
+int grid_for(int n, int block, int maxBlocks = 4096) {
+    int g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > maxBlocks) g = maxBlocks;
+    return g;
+}
+
+}  // namespace
+
+void launch_prep(const DevState &S, cudaStream_t st) {
+    k_prep<<<grid_for(S.nRods, 256), 256, 0, st>>>(S);
+}
+
+int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st) {
+    const int nb = (n + kScanSpan - 1) / kScanSpan;
+    if (nb > 0) k_scan_block<<<nb, kScanBlock, 0, st>>>(in, out, n, tmp);
+    k_scan_top<<<1, 1024, 0, st>>>(tmp, nb, out, n);
+    if (nb > 0) k_scan_add<<<nb, kScanBlock, 0, st>>>(out, n, tmp);
+    return nb > 0 ? 3 : 1;
+}
+
+void launch_scatter(const DevState &S, cudaStream_t st) {
+    k_scatter<<<grid_for(S.nRods, 256), 256, 0, st>>>(S);
+}
+
+void launch_pairs(const DevState &S, cudaStream_t st) {
+    const int g = (S.nRods + kPairThreads - 1) / kPairThreads;
+    k_pairs<<<g > 0 ? g : 1, kPairThreads, 0, st>>>(S);
+}
+
+int launch_pair_sort(const DevState &S, cudaStream_t st) {
+    k_pair_bucket<<<grid_for(S.cap, 256), 256, 0, st>>>(S);
+    k_pair_segsort<<<grid_for(S.nRods, 128), 128, 0, st>>>(S);
+    return 2;
+}
+
+void launch_ranges(const DevState &S, cudaStream_t st) { k_ranges<<<1, 256, 0, st>>>(S); }
+
+void launch_build(const DevState &S, cudaStream_t st) {
+    k_build<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
+}
+
+int launch_rows(const DevState &S, cudaStream_t st) {
+    const int n = launch_scan(S.rowCount, S.rowPtr, S.nRods, S.scanTmp, st);
+    k_rows_fill<<<grid_for(S.cap, 256), 256, 0, st>>>(S);
+    k_rows_sort<<<grid_for(S.nRods, 128), 128, 0, st>>>(S);
+    return n + 2;
+}
+
+void launch_unpack_rods(const DevState &S, int rodOffset, int n, cudaStream_t st) {
+    k_unpack_rods<<<grid_for(n, 256), 256, 0, st>>>(S, rodOffset, n);
+}
+
+void launch_pack_rods(const DevState &S, int rodOffset, int n, int what, cudaStream_t st) {
+    k_pack_rods<<<grid_for(n, 256), 256, 0, st>>>(S, rodOffset, n, what);
+}
+
+}  // namespace alens

@@ -1,0 +1,387 @@
+#!/usr/bin/env python3
+"""Benchmark of the rod collision-and-constraint step (one SylinderSystem::runStep
+per "step") on GB300.
+
+Headline metric: rod-steps/s at BBPGD residual <= 1e-5 for the dense quasi-2D
+layer (20,000 rods of length 1 um, diameter 0.025 um, 40 x 40 um periodic
+slab of thickness 0.1 um, von Mises kappa = 5 about x; seeded synthetic
+data).  Two GPU forms run from the same relaxed state:
+  plain : FP64 solve, zero initial gamma
+  fast  : FP32-bulk / FP64-reduction solve with FP64 refinement, warm start
+          from the previous step's gamma  (the reported `value`)
+
+`value` is device time (CUDA events on the library's stream, L2 flushed
+between steps, inputs resident in HBM).  `e2e` runs the same steps through
+the C ABI with host buffers: positions/orientations copied in from pinned
+memory and copied back every step.
+
+`--impl reference` times the CPU oracle (FP64, OpenMP, all host cores) on
+the same workload; the reference's own SimToolbox code is not available.
+Under torchrun every rank runs an independent replica ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rod-steps/s at BBPGD residual <=1e-5 (warm-start+mixed; plain FP64 alongside)"
+UNIT = "rod-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--pre-steps", type=int, default=40,
+                    help="untimed FP64 steps that relax the random initial overlaps")
+    ap.add_argument("--rods", type=int, default=20000)
+    ap.add_argument("--side", type=float, default=40.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="bounded CPU-oracle sample for cpu_baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def b_iter(nc, nr, s):
+    """Algorithmic bytes of one BBPGD pass: D read twice (12 values + 2 int32
+    indices), gamma/q/gamma_prev/g_prev read and gamma/g written (FP64), per-rod
+    mobility data read, F and U written and read."""
+    sd = 12 * s + 8
+    return nc * (2 * sd + 6 * 8) + nr * (6 * s + 4 * 6 * s)
+
+
+def workload(args, rank):
+    from alens_gb300 import workloads
+    return workloads.dense_monolayer(n=args.rods, side=args.side, seed=rank)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during timing."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), parts[4:9]))
+                except ValueError:
+                    continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        mx = max(r[1] for r in rows)
+        load = [r[0] for r in rows]
+        names = ["active_mask", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for n, v in zip(names[1:], r[2][1:]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def relaxed_state(w, pre_steps, make_sys):
+    sysg = make_sys(w.cfg)
+    sysg.set_rods(w.rods)
+    for _ in range(pre_steps):
+        sysg.step()
+    pos, quat = sysg.get_rods()
+    sysg.close() if hasattr(sysg, "close") else None
+    from alens_gb300.capi import RodState
+    return RodState(w.rods.gid, pos, quat, w.rods.length, w.rods.radius)
+
+
+def run_arm(torch, stream, cfg, rods, warmup, steps, flush, e2e=False):
+    """Time `steps` steps with CUDA events on the library stream; L2 flushed
+    (256 MB write) before every step, outside the timed interval."""
+    from alens_gb300 import capi
+    cfg.stream = stream.cuda_stream
+    sysg = capi.GpuSystem(cfg)
+    sysg.set_rods(rods)
+    n = rods.n
+    pos_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    quat_h = torch.empty((n, 4), dtype=torch.float64, pin_memory=True).numpy()
+    for _ in range(warmup):
+        sysg.step()
+    pos_h[:], quat_h[:] = sysg.get_rods()
+    l0 = sysg.launch_count()
+    times, iters, refine, ncon, resid = [], [], [], [], []
+    conv = True
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        if e2e:
+            sysg.update_rods(pos_h, quat_h)
+        st = sysg.step()
+        if e2e:
+            sysg.get_rods(out=(pos_h, quat_h))
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        iters.append(st["iterations"])
+        refine.append(st["refineIterations"])
+        ncon.append(st["nCollision"] + st["nBilateral"])
+        resid.append(st["residual"])
+        conv = conv and bool(st["converged"])
+    launches = sysg.launch_count() - l0
+    sysg.close()
+    return dict(ms=times, iters=iters, refine=refine, ncon=ncon, resid=resid, converged=conv,
+                launches=launches)
+
+
+def solver_roofline(torch, stream, cfg, rods, steps, peak):
+    """Per-launch time of the main BBPGD kernel from the library's stage
+    events (direct launches) and its algorithmic bytes."""
+    from alens_gb300 import capi, workloads
+    c = workloads.config_with(cfg, stageTiming=1, useGraph=0)
+    c.stream = stream.cuda_stream
+    sysg = capi.GpuSystem(c)
+    sysg.set_rods(rods)
+    sysg.step()
+    nr = rods.n
+    s = 4 if cfg.precision == capi.PREC_MIXED else 8
+    tot_b, tot_ms, ref_b, ref_ms = 0.0, 0.0, 0.0, 0.0
+    for _ in range(steps):
+        st = sysg.step()
+        t = sysg.stage_times()
+        nc = st["nCollision"] + st["nBilateral"]
+        it = st["iterations"]
+        passes = 1 + (1 + it if it > 0 else 0)
+        tot_b += passes * b_iter(nc, nr, s)
+        tot_ms += t[1]
+        if cfg.precision == capi.PREC_MIXED:
+            r = st["refineIterations"]
+            ref_b += (1 + (1 + r if r > 0 else 0)) * b_iter(nc, nr, 8)
+            ref_ms += t[2]
+    sysg.close()
+    achieved = tot_b / (tot_ms * 1e-3) / 1e9
+    return {"kernel": "k_solve<float>" if s == 4 else "k_solve<double>",
+            "achieved": achieved, "avg_launch_ms": tot_ms / steps,
+            "bytes_per_launch": tot_b / steps,
+            "refine_gbs": (ref_b / (ref_ms * 1e-3) / 1e9) if ref_ms > 0 else None}
+
+
+def cpu_baseline(w_cfg, rods, seconds, threads):
+    """The oracle (FP64, OpenMP) on the same relaxed workload, bounded to
+    about `seconds` of CPU time."""
+    from alens_gb300 import oracle_api
+    oracle_api.set_threads(threads)
+    o = oracle_api.OracleSystem(w_cfg)
+    o.set_rods(rods)
+    o.step()  # first step allocates
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        o.step()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 200:
+            break
+    o.close()
+    return rods.n * n / el, n, el
+
+
+def reference_arm(args):
+    """--impl reference: the CPU oracle on all host cores (rank 0 only)."""
+    from alens_gb300 import oracle_api, workloads
+    threads = os.cpu_count() or 1
+    oracle_api.set_threads(threads)
+    w = workload(args, 0)
+    rods = relaxed_state(w, args.pre_steps, oracle_api.OracleSystem)
+    o = oracle_api.OracleSystem(w.cfg)
+    o.set_rods(rods)
+    for _ in range(args.warmup):
+        o.step()
+    times, iters = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st = o.step()
+        times.append(time.perf_counter() - t0)
+        iters.append(st["iterations"])
+    tot = sum(times)
+    value = rods.n * args.steps / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": w.name, "rods": rods.n, "pre_steps": args.pre_steps,
+                   "form": "CPU oracle FP64, zero start", "l2": "n/a (CPU)"},
+        "iterations_per_step": float(np.mean(iters)),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} steps of the {rods.n}-rod layer after {args.pre_steps} relaxation steps"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "SimToolbox (the reference's hot path) is absent from the reference checkout; "
+                "the timed CPU path is the project's FP64 OpenMP restatement (oracle/)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        return
+    import torch
+    import torch.distributed as dist
+    from alens_gb300 import build, capi, workloads
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    build.build_lib()
+    w = workload(args, rank)
+    nr = w.rods.n
+    stream = torch.cuda.Stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    rods = relaxed_state(w, args.pre_steps, capi.GpuSystem)
+    cfg_plain = workloads.config_with(w.cfg, precision=capi.PREC_FP64, warmStart=capi.WARM_ZERO)
+    cfg_fast = workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_PREV)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    with Clocks(local) as clk:
+        barrier()
+        plain = run_arm(torch, stream, cfg_plain, rods, args.warmup, args.steps, flush)
+        fast = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush)
+        e2e = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush, e2e=True)
+        barrier()
+    clocks = clk.summary()
+
+    def total_s(arm):
+        t = torch.tensor([sum(arm["ms"]) * 1e-3], dtype=torch.float64, device="cuda")
+        if world > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    t_fast, t_plain, t_e2e = total_s(fast), total_s(plain), total_s(e2e)
+    value = world * nr * args.steps / t_fast
+    plain_value = world * nr * args.steps / t_plain
+    e2e_value = world * nr * args.steps / t_e2e
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = measured_peaks()
+    roof_fast = solver_roofline(torch, stream, cfg_fast, rods, 10, peak)
+    roof_plain = solver_roofline(torch, stream, cfg_plain, rods, 10, peak)
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cv, csteps, cel = cpu_baseline(w.cfg, rods, args.cpu_seconds, threads)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{csteps} FP64 oracle steps ({cel:.1f} s) of the same relaxed {nr}-rod layer"}
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "solver_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("bytes_per_launch_scaled")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum(fast["ms"]) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk / f64 dots+residual+refine",
+        "data": "synthetic (seeded)",
+        "config": {"workload": w.name, "rods": nr, "box_um": [args.side, args.side, 0.1],
+                   "pre_steps": args.pre_steps, "form": "mixed precision + previous-gamma warm start",
+                   "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": f"replicas x{world}"},
+        "plain_fp64": {"value": plain_value, "ms_per_step": sum(plain["ms"]) / args.steps,
+                       "iterations_per_step": float(np.mean(plain["iters"])),
+                       "max_residual": float(np.max(plain["resid"])), "converged": plain["converged"]},
+        "fast": {"iterations_per_step": float(np.mean(fast["iters"])),
+                 "refine_iterations_per_step": float(np.mean(fast["refine"])),
+                 "max_residual": float(np.max(fast["resid"])), "converged": fast["converged"],
+                 "constraints_per_step": float(np.mean(fast["ncon"]))},
+        "speedup_fast_vs_plain": value / plain_value,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nr * 7 * 8,
+                "d2h_bytes_per_step": nr * 7 * 8 + 64},
+        "roofline": {"bound": "hbm", "achieved": roof_fast["achieved"], "peak": peak, "unit": "GB/s",
+                     "frac": roof_fast["achieved"] / peak, "traffic": traffic,
+                     "kernel": roof_fast["kernel"], "peak_kind": f"{peak_kind} hbm_gbs",
+                     "avg_launch_ms": roof_fast["avg_launch_ms"],
+                     "bytes_per_launch": roof_fast["bytes_per_launch"],
+                     "plain_fp64_kernel": {"achieved": roof_plain["achieved"],
+                                           "frac": roof_plain["achieved"] / peak,
+                                           "avg_launch_ms": roof_plain["avg_launch_ms"]}},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": int(fast["launches"]),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,244 @@
+/*
+ * alens_gpu.h - C ABI of the GB300 rod collision-and-constraint step.
+ *
+ * One call of alens_step() performs what SimToolbox's
+ * SylinderSystem::runStep() does for rigid spherocylinders ("sylinders") in
+ * aLENS, on one GPU:
+ *
+ *   Brownian (known) velocity -> cell-list near-pair search -> segment-segment
+ *   closest points -> constraint Jacobian D -> BBPGD solve of the bound
+ *   constrained QP on  A = dt D^T M D (+ compliance)  -> velocity write-back
+ *   -> Euler update of positions and orientations.
+ *
+ * The caller is aLENS's TubuleSystem (SRC/TubuleSystem.cpp:223 calls
+ * rodSystem.runStep()); the entry points below are what a binding of that
+ * call surface needs.  Each declaration cites the reference interface it
+ * replaces.  The reference's SimToolbox submodule is not part of the
+ * reference checkout, so those citations name the aLENS call site.
+ *
+ * Conventions
+ *   - Every function returns an AlensStatus code; nothing throws or exits.
+ *   - The library owns all device memory; the caller owns host buffers,
+ *     which are only read or written during the call.
+ *   - One context = one CUDA stream.  A context is not thread safe: call it
+ *     from one host thread at a time (the reference calls runStep from the
+ *     master thread, outside OpenMP regions, SRC/TubuleSystem.cpp:221-226).
+ *   - A context may hold several independent systems ("replicas") that are
+ *     stepped together in one launch sequence; a plain system is replica 0.
+ *   - Units follow aLENS: um, pN, s (Protein/ProteinModel.md:14-19).
+ *   - Orientation quaternions are stored (x, y, z, w), the storage order of
+ *     Sylinder::orientation (an Eigen quaternion, SRC/TubuleBind.hpp:63); the
+ *     rod axis is q * (0,0,1).
+ */
+#ifndef ALENS_GPU_H
+#define ALENS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  Replaces std::exit / assert error handling of the reference
+ * (SRC/TubuleSystem.cpp:500,642). */
+typedef enum AlensStatus {
+    ALENS_OK = 0,
+    ALENS_INVALID_ARG = 1,   /* bad argument, size or configuration          */
+    ALENS_CUDA_ERROR = 2,    /* a CUDA runtime call failed                   */
+    ALENS_NOT_CONVERGED = 3, /* BBPGD hit conMaxIte; the step still completed */
+    ALENS_CAPACITY = 4,      /* fixed constraint capacity too small          */
+    ALENS_TIMEOUT = 5,       /* a bounded device-side wait gave up           */
+    ALENS_NAN_DETECTED = 6,  /* NaN/Inf in rod state or in the solve         */
+    ALENS_NO_DEVICE = 7,     /* no usable CUDA device                        */
+    ALENS_NOT_READY = 8      /* call order violated (e.g. no rods set)       */
+} AlensStatus;
+
+typedef enum AlensPrecision {
+    ALENS_PREC_FP64 = 0,  /* everything FP64 (the oracle's arithmetic)        */
+    ALENS_PREC_MIXED = 1  /* FP32 SpMV/projection, FP64 dots, residual and
+                             final refinement sweeps                          */
+} AlensPrecision;
+
+typedef enum AlensWarmStart {
+    ALENS_WARM_ZERO = 0,  /* gamma0 = 0 for collisions (block.gamma for
+                             bilateral blocks)                                */
+    ALENS_WARM_PREV = 1,  /* previous step's gamma for persisting pairs       */
+    ALENS_WARM_MLP = 2    /* learned prediction (see alens_mlp_*), falling
+                             back to the previous gamma when not loaded       */
+} AlensWarmStart;
+
+/* Hot-path subset of SimToolbox SylinderConfig (RunConfig.yaml keys,
+ * docs/source/quickstart.md:316-358; example Examples/DenseMonoLayer/
+ * RunConfig.yaml:1-36).  Field names keep the YAML key names. */
+typedef struct AlensConfig {
+    double simBoxLow[3];
+    double simBoxHigh[3];
+    int32_t simBoxPBC[3];
+    int32_t monolayer;               /* motion restricted to the x-y plane    */
+    double viscosity;                /* pN s / um^2                           */
+    double KBT;                      /* pN um; <= 0 disables Brownian noise   */
+    double dt;                       /* s                                     */
+    double sylinderDiameterColRatio; /* collision diameter / diameter         */
+    double sylinderLengthColRatio;   /* collision length / length             */
+    double sylinderColBuf;           /* record pairs with separation < this   */
+    double conResTol;                /* BBPGD residual tolerance (um)         */
+    int32_t conMaxIte;               /* BBPGD iteration cap                   */
+    int32_t conSolverChoice;         /* 0 = BBPGD (the only solver here)      */
+    uint64_t rngSeed;
+    /* GPU-specific knobs (no counterpart in SylinderConfig) */
+    int32_t precision;               /* AlensPrecision                        */
+    int32_t warmStart;               /* AlensWarmStart                        */
+    int32_t maxConstraints;          /* 0 = grow automatically; >0 = fixed
+                                        capacity, overflow -> ALENS_CAPACITY  */
+    int32_t useGraph;                /* 1 = replay the step as a CUDA graph   */
+    int32_t stageTiming;             /* 1 = time each stage with CUDA events
+                                        (direct launches, no graph)           */
+    void *stream;                    /* cudaStream_t to run on; NULL = own    */
+} AlensConfig;
+
+/* One constraint block as the reference builds it in
+ * TubuleSystem::setProteinConstraints (SRC/TubuleSystem.cpp:727-736),
+ * fields in the constructor's argument order, plus the 3x3 stress of
+ * setStress (:742).  Column of D for this block: rod I gets force normI and
+ * torque posI x normI; rod J gets normJ and posJ x normJ (absent when
+ * oneSide).  Bilateral blocks with kappa > 0 carry compliance 1/kappa. */
+typedef struct AlensBlock {
+    double delta0;       /* current separation (unilateral) or extension  */
+    double gamma;        /* initial guess of the constraint force         */
+    int64_t gidI, gidJ;
+    int32_t globalIndexI, globalIndexJ; /* rod indices within the replica */
+    double normI[3], normJ[3];
+    double posI[3], posJ[3]; /* lever arms relative to the rod centres    */
+    double labI[3], labJ[3]; /* lab-frame contact points (stress only)    */
+    int32_t oneSide;
+    int32_t bilateral;
+    double kappa;
+    double gammaLB;      /* lower bound of gamma for unilateral blocks    */
+    double stress[9];
+} AlensBlock;
+
+/* Per-step statistics (the reference prints them through Teuchos timers,
+ * SRC/TubuleSystem.cpp:148-167, and spdlog). */
+typedef struct AlensStepStats {
+    int64_t step;            /* step index this call executed              */
+    int32_t nRods;
+    int32_t nCollision;      /* collision constraints found                */
+    int32_t nBilateral;      /* bilateral/user blocks in the solve         */
+    int32_t iterations;      /* BBPGD iterations (max over replicas)       */
+    int32_t refineIterations;/* FP64 refinement iterations (mixed mode)    */
+    int32_t converged;       /* 1 if every replica reached conResTol       */
+    int32_t status;          /* AlensStatus of the step                    */
+    double residual;         /* final residual (max over replicas)         */
+    int64_t constraintsNeeded; /* on ALENS_CAPACITY: capacity to retry with */
+} AlensStepStats;
+
+typedef struct AlensCtx AlensCtx;
+
+/* Fill *cfg with the defaults of SylinderConfig for the keys above. */
+void alens_config_default(AlensConfig *cfg);
+
+/* Text of a status code. */
+const char *alens_status_str(int status);
+
+/* Create a context for one system (replaces SylinderSystem::initialize's
+ * configuration part, SRC/TubuleSystem.cpp:79).  Returns ALENS_NO_DEVICE
+ * when no CUDA device is usable. */
+int alens_create(const AlensConfig *cfg, AlensCtx **out);
+
+/* Create a context holding nReplica independent systems with their own
+ * configurations (box, seed, tolerances); all replicas share precision,
+ * warmStart, maxConstraints, useGraph and stream of cfgs[0].  No
+ * counterpart in the reference, which runs one system per process. */
+int alens_create_ensemble(const AlensConfig *cfgs, int nReplica,
+                          AlensCtx **out);
+
+int alens_destroy(AlensCtx *ctx);
+
+/* Set the rods of one replica (replaces reading TubuleInitial.dat inside
+ * SylinderSystem::initialize / reinitialize, SRC/TubuleSystem.cpp:38,79).
+ * pos[3n], orientation[4n] as (x,y,z,w), length[n], radius[n] (physical),
+ * gid[n], immovable[n] (nullable; 1 = 'S' stationary rod). */
+int alens_set_rods(AlensCtx *ctx, int replica, int n, const int64_t *gid,
+                   const double *pos, const double *orientation,
+                   const double *length, const double *radius,
+                   const int32_t *immovable);
+
+/* Overwrite the positions and orientations of one replica (same layout as
+ * alens_set_rods; the rod set is unchanged). */
+int alens_update_rods(AlensCtx *ctx, int replica, int n, const double *pos,
+                      const double *orientation);
+
+/* Copy rod state back (what SylinderSystem::getContainer() exposes). */
+int alens_get_rods(AlensCtx *ctx, int replica, int n, double *pos,
+                   double *orientation);
+
+/* Velocity of the last step: vel[3n], omega[3n] (total = known +
+ * constraint). */
+int alens_get_velocity(AlensCtx *ctx, int replica, int n, double *vel,
+                       double *omega);
+
+/* Queue blocks for the next alens_step of one replica.  Replaces appending
+ * to rodSystem.getConstraintPoolNonConst()[tid]
+ * (SRC/TubuleSystem.cpp:697-743).  The blocks are copied; the queue is
+ * consumed (emptied) by the next step. */
+int alens_add_bilateral(AlensCtx *ctx, int replica, int n,
+                        const AlensBlock *blocks);
+
+/* One full step (replaces SylinderSystem::runStep, SRC/TubuleSystem.cpp:223).
+ * Returns ALENS_OK, ALENS_NOT_CONVERGED (step completed with the last
+ * iterate), or an error; *stats (nullable) receives the summary. */
+int alens_step(AlensCtx *ctx, AlensStepStats *stats);
+
+/* The three parts of alens_step, for staged use and testing:
+ * detect = known velocity + pair search + constraint assembly,
+ * solve = BBPGD, advance = velocity write-back + Euler update
+ * (SylinderSystem::stepEuler, SRC/TubuleSystem.cpp:55). */
+int alens_detect(AlensCtx *ctx, AlensStepStats *stats);
+int alens_solve(AlensCtx *ctx, AlensStepStats *stats);
+int alens_advance(AlensCtx *ctx, AlensStepStats *stats);
+
+/* Per-replica statistics of the last step. */
+int alens_get_replica_stats(AlensCtx *ctx, int replica,
+                            AlensStepStats *stats);
+
+/* Constraint count of one replica after detect: collisions then blocks. */
+int alens_get_num_constraints(AlensCtx *ctx, int replica, int *nCollision,
+                              int *nBilateral);
+
+/* Constraints of one replica in canonical order: collisions sorted by
+ * (indexI, indexJ, image) with indexI <= indexJ, then queued blocks in
+ * queue order.  Any pointer may be NULL.  image = (sx+1)*9+(sy+1)*3+(sz+1)
+ * for the periodic shift applied to rod J (13 = none; -1 for blocks).
+ * jac[12*k] = (normI, posI x normI, normJ, posJ x normJ). */
+int alens_get_constraints(AlensCtx *ctx, int replica, int cap,
+                          int32_t *indexI, int32_t *indexJ, int32_t *image,
+                          double *delta0, double *gamma, double *jac);
+
+/* Sum over the constraints of one replica of the pair virial
+ * gamma * (lab_I - lab_J) (x) n  (3x3 row-major); the role of
+ * SylinderSystem::calcConStress (SRC/TubuleSystem.cpp:224). */
+int alens_get_con_stress(AlensCtx *ctx, int replica, double *stress9);
+
+/* Steps executed so far (SylinderSystem::getStepCount). */
+int alens_get_step_count(AlensCtx *ctx, int64_t *count);
+
+/* The CUDA stream of the context (cudaStream_t), for event timing. */
+int alens_get_stream(AlensCtx *ctx, void **stream);
+
+/* Kernels launched by this context so far (graph replays included).  The
+ * role of the reference's per-phase Teuchos counters
+ * (SRC/TubuleSystem.cpp:148-167) for device work. */
+int alens_get_launch_count(AlensCtx *ctx, int64_t *count);
+
+/* CUDA-event times (ms) of the stages of the last step when stageTiming is
+ * on: ms[0] detect, ms[1] main solve kernel (FP32 kernel in mixed mode),
+ * ms[2] FP64 refinement (mixed mode; 0 otherwise), ms[3] advance,
+ * ms[4] whole step.  The stage split of TubuleSystem's step timers
+ * (SRC/TubuleSystem.cpp:148-167). */
+int alens_get_stage_times(AlensCtx *ctx, double *ms5);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ALENS_GPU_H */

@@ -1,0 +1,351 @@
+"""CPU tests of the oracle: known answers, the canonical reduction tree, the
+BBPGD optimality conditions checked independently in numpy, invariances and
+host-side failure handling.  No GPU needed."""
+import math
+
+import numpy as np
+import pytest
+
+from alens_gb300 import capi, workloads
+from alens_gb300 import oracle_api as O
+
+
+# ------------------------------------------------------------ Philox KAT
+# Known-answer vectors published with the Random123 library for
+# Philox4x32-10 (counter, key -> output).
+PHILOX_KAT = [
+    ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+    ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+    ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+     [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
+]
+
+
+@pytest.mark.parametrize("ctr,key,out", PHILOX_KAT)
+def test_philox_known_answers(ctr, key, out):
+    assert list(O.philox4x32(ctr, key)) == out
+
+
+def test_det_log_accuracy():
+    rng = np.random.default_rng(1)
+    xs = np.concatenate([10.0 ** rng.uniform(-300, 300, 2000), rng.uniform(0.5, 2.0, 2000),
+                         [5e-324, 1e-310, 0.025, 0.0125 / 1.5, 1.0, 2.0, 0.5]])
+    for x in xs:
+        ref = math.log(x)
+        got = O.det_log(x)
+        assert abs(got - ref) <= 4e-16 * max(1.0, abs(ref)), (x, got, ref)
+
+
+def test_det_sincos_accuracy():
+    for x in np.concatenate([np.linspace(-math.pi, math.pi, 2001), [0.0, 1e-300, 1e-8, 0.0625, 0.07]]):
+        s, c = O.det_sincos(float(x))
+        assert abs(s - math.sin(x)) <= 2e-15 and abs(c - math.cos(x)) <= 2e-15, x
+
+
+def test_normals_distribution_and_mapping():
+    z = np.array([O.normals6(12345, g, 7) for g in range(20000)]).ravel()
+    assert abs(z.mean()) < 0.02 and abs(z.std() - 1.0) < 0.02
+    # Box-Muller mapping re-derived here from the Philox words
+    w = np.concatenate([O.philox4x32([3, 0, 9, b], [5, 0]) for b in range(3)])
+    u = [((int(w[2 * i]) >> 5) * 67108864.0 + (int(w[2 * i + 1]) >> 6) + 0.5) / 9007199254740992.0
+         for i in range(6)]
+    ref = []
+    for p in range(3):
+        r = math.sqrt(-2.0 * math.log(u[2 * p]))
+        th = 2 * math.pi * u[2 * p + 1]
+        ref += [r * math.cos(th), r * math.sin(th)]
+    got = O.normals6(5, 3, 9)
+    assert np.allclose(got, ref, rtol=0, atol=1e-13)
+
+
+# --------------------------------------------------------------- DCP KAT
+def _dcp(c1, u1, h1, c2, u2, h2):
+    return O.dcp(np.array(c1, float), np.array(u1, float), h1, np.array(c2, float),
+                 np.array(u2, float), h2)
+
+
+def test_dcp_crossing():
+    s, t, P, Q, d = _dcp([0, 0, 0], [1, 0, 0], 1.0, [0, 0, 0.5], [0, 1, 0], 1.0)
+    assert (s, t, d) == (0.0, 0.0, 0.5)
+    assert np.array_equal(P, [0, 0, 0]) and np.array_equal(Q, [0, 0, 0.5])
+
+
+def test_dcp_parallel_overlap_midpoint():
+    s, t, P, Q, d = _dcp([0, 0, 0], [1, 0, 0], 1.0, [0.5, 0.3, 0], [1, 0, 0], 1.0)
+    assert s == pytest.approx(0.25) and t == pytest.approx(-0.25) and d == pytest.approx(0.3)
+    s, t, P, Q, d = _dcp([0, 0, 0], [1, 0, 0], 1.0, [0.5, 0.3, 0], [-1, 0, 0], 1.0)
+    assert s == pytest.approx(0.25) and t == pytest.approx(0.25) and d == pytest.approx(0.3)
+    assert np.allclose(Q, [0.25, 0.3, 0])
+
+
+def test_dcp_collinear_disjoint():
+    s, t, P, Q, d = _dcp([0, 0, 0], [1, 0, 0], 1.0, [3, 0, 0], [1, 0, 0], 1.0)
+    assert (s, t, d) == (1.0, -1.0, 1.0)
+
+
+def test_dcp_endpoint_endpoint():
+    s, t, P, Q, d = _dcp([0, 0, 0], [1, 0, 0], 1.0, [2, 1, 0], [0, 1, 0], 0.5)
+    assert s == 1.0 and t == -0.5 and d == pytest.approx(math.sqrt(1.25))
+
+
+def test_dcp_t_shape():
+    # segment J's end touches the middle of I at distance 0.2
+    s, t, P, Q, d = _dcp([0, 0, 0], [1, 0, 0], 1.0, [0.3, 0.7, 0], [0, 1, 0], 0.5)
+    assert s == pytest.approx(0.3) and t == -0.5 and d == pytest.approx(0.2)
+
+
+def test_dcp_point_segment_and_point_point():
+    s, t, P, Q, d = _dcp([0.3, 0.4, 0], [0, 0, 1], 0.0, [0, 0, 0], [1, 0, 0], 1.0)
+    assert s == 0.0 and t == pytest.approx(0.3) and d == pytest.approx(0.4)
+    s, t, P, Q, d = _dcp([0, 0, 0], [0, 0, 1], 0.0, [0.3, 0.4, 0], [0, 1, 0], 0.0)
+    assert d == pytest.approx(0.5)
+
+
+def test_dcp_random_against_brute_force():
+    rng = np.random.default_rng(3)
+    for _ in range(300):
+        c1, c2 = rng.normal(size=3), rng.normal(size=3) * 0.5
+        u1, u2 = rng.normal(size=3), rng.normal(size=3)
+        u1 /= np.linalg.norm(u1)
+        u2 /= np.linalg.norm(u2)
+        h1, h2 = rng.uniform(0, 1, 2)
+        s, t, P, Q, d = _dcp(c1, u1, h1, c2, u2, h2)
+        ss = np.linspace(-h1, h1, 201)
+        tt = np.linspace(-h2, h2, 201)
+        X = c1[None, None, :] + ss[:, None, None] * u1 - (c2[None, None, :] + tt[None, :, None] * u2)
+        dmin = np.sqrt((X ** 2).sum(-1)).min()
+        assert d <= dmin + 1e-12
+        assert d >= dmin - 2e-2 * (h1 + h2 + 1e-3)
+
+
+# ------------------------------------------------- canonical reduction
+def _tree256(lanes):
+    lanes = list(lanes)
+    for w in range(8):
+        v = lanes[32 * w:32 * w + 32]
+        off = 16
+        while off >= 1:
+            for l in range(off):
+                v[l] = v[l] + v[l + off]
+            off //= 2
+        lanes[32 * w] = v[0]
+    ws = [lanes[32 * w] for w in range(8)]
+    for off in (4, 2, 1):
+        for i in range(off):
+            ws[i] = ws[i] + ws[i + off]
+    return ws[0]
+
+
+def _canon_py(v):
+    v = [float(x) for x in v]
+    n = len(v)
+    if n == 0:
+        return 0.0
+    T = [_tree256([v[b + l] if b + l < n else 0.0 for l in range(256)]) for b in range(0, n, 256)]
+    while True:
+        m = len(T)
+        R = []
+        for c in range(0, m, 2048):
+            lanes = []
+            for l in range(256):
+                acc = 0.0
+                for k in range(8):
+                    i = c + l + 256 * k
+                    if i < m:
+                        acc = acc + T[i]
+                lanes.append(acc)
+            R.append(_tree256(lanes))
+        if len(R) == 1:
+            return R[0]
+        T = R
+
+
+@pytest.mark.parametrize("n", [0, 1, 255, 256, 257, 5000, 70000])
+def test_canonical_sum_tree(n):
+    rng = np.random.default_rng(n)
+    v = rng.normal(size=n) * 10.0 ** rng.uniform(-8, 8, size=n)
+    got = O.canon_sum(v)
+    assert got == _canon_py(v)
+    assert got == pytest.approx(math.fsum(v), rel=1e-9, abs=1e-300)
+
+
+def test_canonical_sum_multilevel():
+    v = np.random.default_rng(5).normal(size=600000)
+    assert O.canon_sum(v) == pytest.approx(math.fsum(v), rel=1e-10, abs=1e-9)
+
+
+def test_mobility_slender_body_and_sphere():
+    mu = 0.01
+    for L, r in [(1.0, 0.0125), (0.5, 0.0125), (2.0, 0.0125)]:
+        b = -(1 + 2 * math.log(r / L))
+        ref = [b / (4 * math.pi * mu * L), (b + 2) / (8 * math.pi * mu * L),
+               3 * (b + 2) / (2 * math.pi * mu * L ** 3)]
+        assert np.allclose(O.mobility(L, r, mu), ref, rtol=1e-14)
+    ref = [1 / (6 * math.pi * mu * 0.1), 1 / (6 * math.pi * mu * 0.1), 1 / (8 * math.pi * mu * 0.1 ** 3)]
+    assert np.allclose(O.mobility(0.15, 0.1, mu), ref, rtol=1e-14)
+
+
+# ---------------------------------------------- solve: independent KKT
+def _assemble(sysO, rods, cfg):
+    """D (6N x Nc), block mobility M and U_nc rebuilt in numpy."""
+    con = sysO.constraints()
+    n = rods.n
+    nc = len(con["gamma"])
+    D = np.zeros((6 * n, nc))
+    for k in range(nc):
+        i, j = con["i"][k], con["j"][k]
+        D[6 * i:6 * i + 6, k] += con["jac"][k, :6]
+        if j >= 0:
+            D[6 * j:6 * j + 6, k] += con["jac"][k, 6:]
+    pos, quat = sysO.get_rods()
+    return con, D
+
+
+def _mobility_matrix(quat_before, rods, mu, mono=False):
+    a = workloads.quat_to_axis(quat_before)
+    n = rods.n
+    M = np.zeros((6 * n, 6 * n))
+    for i in range(n):
+        m = O.mobility(rods.length[i], rods.radius[i], mu)
+        sphere = rods.length[i] < 2 * rods.radius[i]
+        if sphere:
+            Mt = m[0] * np.eye(3)
+            Mr = m[2] * np.eye(3)
+        else:
+            aa = np.outer(a[i], a[i])
+            Mt = m[0] * aa + m[1] * (np.eye(3) - aa)
+            Mr = m[2] * (np.eye(3) - aa)
+        M[6 * i:6 * i + 3, 6 * i:6 * i + 3] = Mt
+        M[6 * i + 3:6 * i + 6, 6 * i + 3:6 * i + 6] = Mr
+    return M
+
+
+def test_bbpgd_kkt_independent():
+    w = workloads.small_periodic(n=400, box=2.6, seed=11)
+    sysO = O.OracleSystem(w.cfg)
+    sysO.set_rods(w.rods)
+    sysO.detect()
+    unc = sysO.known_velocity().ravel()
+    st = sysO.solve(allow_not_converged=False)
+    con, D = _assemble(sysO, w.rods, w.cfg)
+    M = _mobility_matrix(w.rods.quat, w.rods, w.cfg.viscosity)
+    dt = w.cfg.dt
+    gam = con["gamma"]
+    q = con["delta0"] + dt * (D.T @ unc)
+    g = dt * (D.T @ (M @ (D @ gam))) + q
+    tol = w.cfg.conResTol
+    assert st["nCollision"] > 20
+    assert np.all(gam >= 0)
+    assert np.all(g >= -tol * 1.0001 - 1e-12)
+    res = np.max(np.abs(gam - np.maximum(gam - g, 0.0)))
+    assert res <= tol * 1.0001 + 1e-12
+    assert abs(res - st["residual"]) <= 1e-9
+
+
+def test_step_translation_invariance():
+    w = workloads.small_periodic(n=300, box=2.5, seed=4, kbt=-1.0)
+    a = O.OracleSystem(w.cfg)
+    a.set_rods(w.rods)
+    r2 = w.rods.copy()
+    r2.pos = (r2.pos + np.array([2.5, -2.5, 5.0])).copy()  # whole box periods
+    b = O.OracleSystem(w.cfg)
+    b.set_rods(r2)
+    sa, sb = a.detect(), b.detect()
+    ca, cb = a.constraints(), b.constraints()
+    assert sa["nCollision"] == sb["nCollision"]
+    assert np.array_equal(ca["i"], cb["i"]) and np.array_equal(ca["j"], cb["j"])
+    assert np.allclose(ca["delta0"], cb["delta0"], atol=1e-12)
+
+
+def test_pair_set_permutation_invariance():
+    w = workloads.small_periodic(n=300, box=2.5, seed=5, kbt=-1.0)
+    perm = np.random.default_rng(0).permutation(w.rods.n)
+    r2 = capi.RodState(w.rods.gid[perm], w.rods.pos[perm], w.rods.quat[perm], w.rods.length[perm],
+                       w.rods.radius[perm])
+    a, b = O.OracleSystem(w.cfg), O.OracleSystem(w.cfg)
+    a.set_rods(w.rods)
+    b.set_rods(r2)
+    a.detect()
+    b.detect()
+    ca, cb = a.constraints(), b.constraints()
+
+    def gidpairs(c, rods):
+        out = set()
+        for i, j, m in zip(c["i"], c["j"], c["image"]):
+            gi, gj = rods.gid[i], rods.gid[j]
+            sx, sy, sz = m // 9 - 1, (m // 3) % 3 - 1, m % 3 - 1
+            if gi > gj or (gi == gj and m < 13):
+                gi, gj, sx, sy, sz = gj, gi, -sx, -sy, -sz
+            out.add((int(gi), int(gj), sx, sy, sz))
+        return out
+
+    assert gidpairs(ca, w.rods) == gidpairs(cb, r2)
+
+
+def test_oracle_fault_handling():
+    w = workloads.small_periodic(n=100, box=2.0, seed=1)
+    s = O.OracleSystem(w.cfg)
+    bad = w.rods.copy()
+    bad.pos[5, 1] = np.nan
+    s.set_rods(bad)
+    with pytest.raises(capi.AlensError) as e:
+        s.step()
+    assert e.value.status == capi.ALENS_NAN_DETECTED
+    cfg = workloads.config_with(w.cfg, conMaxIte=1)
+    s2 = O.OracleSystem(cfg)
+    dense = workloads.small_periodic(n=200, box=1.2, seed=2)
+    s2.set_rods(dense.rods)
+    st = s2.step()
+    assert st["rc"] == capi.ALENS_NOT_CONVERGED and st["iterations"] == 1
+    tiny = workloads.config_with(w.cfg)
+    tiny.simBoxHigh[0] = 0.5
+    s3 = O.OracleSystem(tiny)
+    with pytest.raises(capi.AlensError) as e:
+        s3.set_rods(w.rods)
+    assert e.value.status == capi.ALENS_INVALID_ARG
+
+
+def test_bilateral_spring_oracle():
+    """Two parallel rods tied by a stretched bilateral spring move toward
+    each other by the amount the implicit spring predicts."""
+    cfg = capi.make_config(box_high=(10, 10, 10), pbc=(0, 0, 0), kbt=-1.0, col_buf=0.0, tol=1e-10)
+    rods = capi.RodState([0, 1], [[5, 5, 5], [5, 5.3, 5]], workloads.axis_to_quat([[1, 0, 0], [1, 0, 0]]),
+                         [1.0, 1.0], [0.0125, 0.0125])
+    s = O.OracleSystem(cfg)
+    s.set_rods(rods)
+    kappa, ell0 = 100.0, 0.1
+    blk = capi.AlensBlock()
+    blk.delta0 = 0.3 - ell0
+    blk.gamma = -blk.delta0 * kappa
+    blk.globalIndexI, blk.globalIndexJ = 0, 1
+    for d, v in enumerate([0, -1, 0]):
+        blk.normI[d] = v
+        blk.normJ[d] = -v
+    blk.bilateral = 1
+    blk.kappa = kappa
+    s.add_bilateral([blk])
+    st = s.step(allow_not_converged=False)
+    pos, _ = s.get_rods()
+    m_perp = O.mobility(1.0, 0.0125, cfg.viscosity)[1]
+    # implicit spring: gamma = -kappa (delta0 + dt * 2 m_perp gamma)
+    gam = -kappa * blk.delta0 / (1 + kappa * cfg.dt * 2 * m_perp)
+    dy = cfg.dt * m_perp * gam
+    assert st["nBilateral"] == 1
+    assert pos[0, 1] == pytest.approx(5 - dy, abs=1e-9)
+    assert pos[1, 1] == pytest.approx(5.3 + dy, abs=1e-9)
+
+
+def test_library_exports_header_symbols():
+    """The C ABI library loads and exports every function of include/*.h
+    (no CUDA call is made)."""
+    import ctypes
+
+    from alens_gb300 import build
+    path = build.build_lib()
+    lib = ctypes.CDLL(str(path))
+    names = capi.exported_symbols_from_header()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    lib.alens_status_str.restype = ctypes.c_char_p
+    assert lib.alens_status_str(4) == b"constraint capacity exceeded"
