@@ -35,10 +35,10 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units of the GPU library.  Files listed in FP_STRICT hold the
 # FP64 path that must match the oracle bit for bit: they are compiled without
 # FMA contraction.
-CU_SOURCES = ["engine.cu", "kernels_detect.cu", "kernels_solve.cu",
+CU_SOURCES = ["engine.cu", "kernels_detect.cu", "kernels_assemble.cu", "kernels_solve.cu",
               "kernels_mixed.cu", "kernels_mlp.cu", "capi.cu"]
 CXX_SOURCES: list[str] = []
-FP_STRICT = {"kernels_detect.cu", "kernels_solve.cu", "engine.cu", "capi.cu"}
+FP_STRICT = {"kernels_detect.cu", "kernels_assemble.cu", "kernels_solve.cu", "engine.cu", "capi.cu"}
 
 
 def _run(cmd: list[str]) -> None:

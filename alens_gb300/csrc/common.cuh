@@ -18,7 +18,7 @@ constexpr double kPi = 3.141592653589793;
 constexpr double kTwoPi = 6.283185307179586;
 constexpr double kLn2 = 0.6931471805599453;
 constexpr double kParallelEps = 1e-12;
-constexpr int kTile = 256;        // level-1 reduction tile (= solver block size)
+constexpr int kTile = 64;         // level-1 reduction tile (constraints)
 constexpr int kChunk = 2048;      // level-2+ reduction chunk
 constexpr int kImageNone = 13;    // image code of the zero periodic shift
 
@@ -347,6 +347,16 @@ __device__ __forceinline__ double warp_tree_sum(double v) {
     return v;
 }
 
+template <class T>
+__device__ __forceinline__ T warp_tree_sum_t(T v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const T o = __shfl_down_sync(0xffffffffu, v, off);
+        v = v + o;
+    }
+    return v;
+}
+
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
@@ -450,9 +460,13 @@ __device__ inline void chunk_reduce(const double *const (&src)[NV], int m, doubl
 }
 
 // ------------------------------------------------------------ grid barrier
+// Arrival counter and release flag live on separate 128-byte lines so that
+// spinning readers do not contend with arriving atomics.
 struct GridBarrier {
     unsigned int count;
+    unsigned int pad0[31];
     unsigned int gen;
+    unsigned int pad1[31];
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -467,13 +481,30 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
     return v;
 }
 
+__device__ __forceinline__ unsigned int atom_add_release_u32(unsigned int *p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.release.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ unsigned int atom_add_acqrel_u32(unsigned int *p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ void st_relaxed_u32(unsigned int *p, unsigned int v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ int ld_volatile_i32(const int *p) {
     return *(const volatile int *)p;
 }
 
-// Barrier over all blocks of a cooperative launch.  The wait is bounded:
-// after `timeout_ns` (or when another block has already given up) the block
-// sets kErrTimeout in *err and returns false; callers then leave the kernel.
+// Barrier over all blocks of a cooperative launch (release/acquire at GPU
+// scope).  The wait is bounded: after `timeout_ns` (or when another block
+// has already given up) the block sets kErrTimeout in *err and returns
+// false; callers then leave the kernel.
 __device__ inline bool grid_sync(GridBarrier *bar, unsigned int nblocks, int *err,
                                  unsigned long long timeout_ns) {
     __shared__ int s_ok;
@@ -481,28 +512,31 @@ __device__ inline bool grid_sync(GridBarrier *bar, unsigned int nblocks, int *er
     if (threadIdx.x == 0) {
         int ok = 1;
         const unsigned int g = ld_acquire_u32(&bar->gen);
-        __threadfence();
-        const unsigned int arrived = atomicAdd(&bar->count, 1u);
+        const unsigned int arrived = atom_add_acqrel_u32(&bar->count, 1u);
         if (arrived == nblocks - 1) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->gen, 1u);
+            st_relaxed_u32(&bar->count, 0u);
+            atom_add_release_u32(&bar->gen, 1u);
         } else {
-            const unsigned long long t0 = global_ns();
+            unsigned long long t0 = 0;
+            unsigned int spins = 0;
             while (ld_acquire_u32(&bar->gen) == g) {
-                __nanosleep(32);
-                if (ld_volatile_i32(err) & kErrTimeout) {
-                    ok = 0;
-                    break;
-                }
-                if (global_ns() - t0 > timeout_ns) {
-                    atomicOr(err, kErrTimeout);
-                    ok = 0;
-                    break;
+                if (++spins > 64) {
+                    __nanosleep(spins > 1024 ? 256 : 32);
+                    if ((spins & 255) == 0) {
+                        if (t0 == 0) t0 = global_ns();
+                        if (ld_volatile_i32(err) & kErrTimeout) {
+                            ok = 0;
+                            break;
+                        }
+                        if (global_ns() - t0 > timeout_ns) {
+                            atomicOr(err, kErrTimeout);
+                            ok = 0;
+                            break;
+                        }
+                    }
                 }
             }
         }
-        __threadfence();
         s_ok = ok;
     }
     __syncthreads();

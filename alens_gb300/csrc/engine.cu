@@ -80,6 +80,7 @@ Engine::~Engine() {
     freeGroup(conAllocs_);
     freeGroup(blockAllocs_);
     freeGroup(fixedAllocs_);
+    freeGroup(opAllocs_);
     if (hCtl_) cudaFreeHost(hCtl_);
     if (hDyn_) cudaFreeHost(hDyn_);
     if (hBilPrefix_) cudaFreeHost(hBilPrefix_);
@@ -183,6 +184,7 @@ void Engine::finalize() {
     freeGroup(conAllocs_);
     freeGroup(fixedAllocs_);
     freeGroup(blockAllocs_);
+    freeGroup(opAllocs_);
     blockCap_ = 0;
     hostPar_.resize(R_);
     int rodOff = 0, cellOff = 0;
@@ -231,8 +233,7 @@ void Engine::finalize() {
     S.sph = alloc<unsigned char>(G, N);
     S.unc = alloc<double>(G, 6 * (size_t)N);
     S.vel = alloc<double>(G, 6 * (size_t)N);
-    S.U = alloc<double>(G, 6 * (size_t)N);
-    S.U32 = alloc<float>(G, 6 * (size_t)N);
+    S.alphaBuf = alloc<double>(G, 2 * (size_t)R_);
     S.stage = alloc<double>(G, 7 * (size_t)N);
     S.cellOf = alloc<int>(G, N);
     S.sidx = alloc<int>(G, N);
@@ -279,7 +280,8 @@ void Engine::finalize() {
     }
     // constraints
     int want = fixedCap_ > 0 ? fixedCap_ : std::max(4096, 4 * N + 1024);
-    allocConstraints(want, false);
+    nnzCap_ = 0;
+    allocConstraints(std::min(want, kMaxConstraints), false);
     solverGrid_ = 0;
     dirty_ = false;
     haveDetect_ = false;
@@ -297,7 +299,7 @@ void Engine::allocConstraints(int cap, bool keepPrev) {
     auto &G = conAllocs_;
     S.cap = cap;
     S.tileCap = cap / kTile + R_ + 2;
-    S.workCap = S.tileCap / kChunk + 2;
+    S.workCap = S.tileCap / kChunk + R_ + 2;
     S.rawKeys = alloc<unsigned long long>(G, cap);
     S.keys = alloc<unsigned long long>(G, cap);
     S.prevKeys = alloc<unsigned long long>(G, cap);
@@ -306,17 +308,19 @@ void Engine::allocConstraints(int cap, bool keepPrev) {
     S.conJ = alloc<int>(G, cap);
     S.conImg = alloc<int>(G, cap);
     S.jac = alloc<double>(G, 12 * (size_t)cap);
-    double **cd[] = {&S.phi0, &S.q, &S.gamma, &S.g, &S.lb, &S.cinv};
+    S.W = alloc<double>(G, 12 * (size_t)cap);
+    double **cd[] = {&S.phi0, &S.q, &S.gamma, &S.lb, &S.cinv, &S.sgam[0], &S.sgam[1], &S.sg[0], &S.sg[1]};
     for (double **p : cd) *p = alloc<double>(G, cap);
     S.lab = alloc<double>(G, 6 * (size_t)cap);
     S.rowEnt = alloc<int>(G, 2 * (size_t)cap);
+    S.annz = alloc<int>(G, cap);
+    S.aptr = alloc<int>(G, cap + 1);
     if (precision_ == ALENS_PREC_MIXED) {
-        S.jac32 = alloc<float>(G, 12 * (size_t)cap);
-        float **fd[] = {&S.gamma32, &S.g32, &S.q32, &S.lb32, &S.cinv32};
+        float **fd[] = {&S.q32, &S.lb32, &S.cinv32, &S.sgam32[0], &S.sgam32[1], &S.sg32[0], &S.sg32[1]};
         for (float **p : fd) *p = alloc<float>(G, cap);
     }
     S.part = alloc<double>(G, 9 * (size_t)S.tileCap);
-    S.work = alloc<double>(G, 9 * (size_t)S.workCap);
+    S.work = alloc<double>(G, (size_t)kMaxSolverGrid * 3 * S.workCap);
     S.tileRep = alloc<int>(G, S.tileCap);
     if (keepPrev && prevN > 0 && oldKeys) {
         const int n = std::min(prevN, cap);
@@ -325,6 +329,17 @@ void Engine::allocConstraints(int cap, bool keepPrev) {
         CK(cudaStreamSynchronize(stream_));
     }
     freeGroup(old);
+    allocOperator(std::max<long long>(nnzCap_, 10LL * cap));
+}
+
+void Engine::allocOperator(long long nnz) {
+    if (nnz >= (1LL << 31) - 1) throw ApiError(ALENS_CAPACITY);
+    freeGroup(opAllocs_);
+    nnzCap_ = nnz;
+    S_.nnzCap = (int)nnz;
+    S_.acol = alloc<int>(opAllocs_, (size_t)nnz);
+    S_.aval = alloc<double>(opAllocs_, (size_t)nnz);
+    S_.aval32 = precision_ == ALENS_PREC_MIXED ? alloc<float>(opAllocs_, (size_t)nnz) : nullptr;
 }
 
 void Engine::updateRods(int rep, int n, const double *pos, const double *quat) {
@@ -444,6 +459,7 @@ int Engine::enqueueDetect() {
     launch_build(S, stream_);
     n += 2;
     n += launch_rows(S, stream_);
+    n += launch_assemble(S, stream_);
     CK(cudaGetLastError());
     return n;
 }
@@ -520,12 +536,19 @@ bool Engine::handleOverflow() {
     const long long needColl = std::max<long long>(hCtl_->rawCount, hCtl_->totalColl);
     const long long need = needColl + nBilQueued_;
     lastNeeded_ = need;
-    if (fixedCap_ > 0) throw ApiError(ALENS_CAPACITY);
-    if (need >= (1LL << 30)) throw ApiError(ALENS_CAPACITY);
     CK(cudaStreamSynchronize(stream_));
-    invalidateGraph();
-    allocConstraints((int)std::min<long long>(need + need / 2 + 1024, (1LL << 30) - 1), true);
-    return true;
+    if (need > S_.cap || hCtl_->nTiles > S_.tileCap) {
+        if (fixedCap_ > 0 || need > kMaxConstraints) throw ApiError(ALENS_CAPACITY);
+        invalidateGraph();
+        allocConstraints((int)std::min<long long>(need + need / 2 + 1024, kMaxConstraints), true);
+        return true;
+    }
+    if (hCtl_->totalNnz > S_.nnzCap) {
+        invalidateGraph();
+        allocOperator((long long)hCtl_->totalNnz * 3 / 2 + 4096);
+        return true;
+    }
+    throw ApiError(ALENS_CAPACITY);
 }
 
 int Engine::collectStats(int stage) {

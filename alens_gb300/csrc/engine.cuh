@@ -8,11 +8,15 @@
 //               geometry (centre, axis, half-length, radius, rod index)
 //   pairs       raw 64-bit keys (i<<32 | j<<5 | image), per-rod counts and
 //               offsets, canonical keys sorted by (i, j, image)
-//   constraints AoS Jacobian 12 x FP64 (96 B) [+ 12 x FP32 copy for the
-//               mixed solver], rod indices I/J, phi0, q, gamma, g, lower
-//               bound, compliance, lab points
+//   constraints AoS Jacobian 12 x FP64 (96 B), mobility-weighted Jacobian
+//               W = M J (96 B), rod indices I/J, phi0, q, final gamma,
+//               solver iterates gamma/g by pass parity, lower bound,
+//               compliance, lab points (+ FP32 copies for the mixed solver)
 //   rod rows    rod-major rows of D: entries 2k+side, ascending (CSR)
-//   reduction   level-1 tile partials (4 kinds) + chunk work space
+//   operator    Delassus rows A = dt D^T M D (CSR: aptr, acol, aval FP64
+//               [+ aval32]); ~4-20 nonzeros per row
+//   reduction   level-1 tile partials (64-constraint tiles) + per-block
+//               chunk work space
 #pragma once
 
 #include <cstdint>
@@ -54,14 +58,16 @@ struct DevCtl {
     int rawCount;     // collision pairs found (may exceed capacity)
     int errFlags;     // kErr* bits
     int totalColl, totalBil, totalCon, nTiles;
-    int activeCount;
+    int totalNnz;     // nonzeros of the Delassus operator
     int maxIte;       // max over replicas
+    int activeCnt[3]; // replicas active per solver pass (mod 3)
+    int finalParity;  // buffer holding the solver's last iterate
     GridBarrier bar;
 };
 
 // Device pointers and sizes of one context; passed to kernels by value.
 struct DevState {
-    int R, nRods, cap, nCells, tileCap, workCap, blockCap;
+    int R, nRods, cap, nCells, tileCap, workCap, blockCap, nnzCap;
     int warm, precision;
     RepParams *par;
     RepDyn *dyn;
@@ -73,8 +79,7 @@ struct DevState {
     int *imm, *rodRep;
     double *ax, *ay, *az, *hcol, *rcol, *m0, *m1, *m2;
     unsigned char *sph;
-    double *unc, *vel, *U;  // 6 x nRods SoA each
-    float *U32;             // 6 x nRods SoA (mixed solver)
+    double *unc, *vel;      // 6 x nRods SoA each
     double *stage;          // 7 x nRods host-transfer staging (interleaved)
     // cells
     int *cellOf, *cellCount, *cellStart, *cellCursor;
@@ -86,9 +91,16 @@ struct DevState {
     // constraints
     int *conI, *conJ, *conImg;
     double *jac;
-    float *jac32;
-    double *phi0, *q, *gamma, *g, *lb, *cinv, *lab;
-    float *gamma32, *g32, *q32, *lb32, *cinv32;
+    double *phi0, *q, *gamma, *lb, *cinv, *lab;
+    float *q32, *lb32, *cinv32;
+    double *sgam[2], *sg[2];   // solver iterates by pass parity (FP64)
+    float *sgam32[2], *sg32[2];
+    double *alphaBuf;          // 2 x R step sizes by pass parity
+    // Delassus operator A = dt D^T M D (rows ascending in column)
+    double *W;                 // 12 x cap: M J per constraint side
+    int *annz, *aptr, *acol;
+    double *aval;
+    float *aval32;
     int *rowCount, *rowPtr, *rowCursor, *rowEnt;
     unsigned long long *prevKeys;
     double *prevGamma;
@@ -96,8 +108,8 @@ struct DevState {
     AlensBlock *blocks;
     int *blockRep;
     // reductions
-    double *part;   // 4 x tileCap
-    double *work;   // 4 x workCap
+    double *part;   // 9 x tileCap (solver: 2 parities x 4 kinds; stress: 9)
+    double *work;   // per block 9 x workCap
     int *tileRep;   // tileCap
     double *stress; // 9 x R outputs
     // scan scratch
@@ -113,14 +125,13 @@ int launch_pair_sort(const DevState &S, cudaStream_t st);
 void launch_ranges(const DevState &S, cudaStream_t st);
 void launch_build(const DevState &S, cudaStream_t st);
 int launch_rows(const DevState &S, cudaStream_t st);
+// ---- Delassus operator (kernels_assemble.cu)
+int launch_assemble(const DevState &S, cudaStream_t st);
 void launch_unpack_rods(const DevState &S, int rodOffset, int n, cudaStream_t st);
 void launch_pack_rods(const DevState &S, int rodOffset, int n, int what, cudaStream_t st);
 
 // ---- solve / advance (kernels_solve.cu)
-struct SolveLaunch {
-    int grid;
-    int block;
-};
+constexpr int kMaxSolverGrid = 152 * 8;  // work space is sized for this
 int solver_max_grid(int precision);  // cooperative residency limit
 // precision == MIXED: FP32 kernel, state reset, FP64 refinement kernel
 // (events ev[0..3] recorded around the two kernels when non-null).

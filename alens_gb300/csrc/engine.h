@@ -8,6 +8,9 @@
 
 namespace alens {
 
+// the three-pass scan covers up to 4096 x 1024 elements
+constexpr int kMaxConstraints = 4096 * 1024;
+
 struct ApiError {
     int status;
     explicit ApiError(int s) : status(s) {}
@@ -61,6 +64,7 @@ class Engine {
     void makeParams(int rep, const HostRods &h, RepParams &P) const;
     void finalize();
     void allocConstraints(int cap, bool keepPrev);
+    void allocOperator(long long nnz);
     void uploadBlocks();
     int enqueueDetect();
     int enqueueSolve(cudaEvent_t *ev);
@@ -93,7 +97,8 @@ class Engine {
     bool dirty_ = true;
     bool haveDetect_ = false, haveSolve_ = false;
     DevState S_{};
-    std::vector<void *> rodAllocs_, conAllocs_, blockAllocs_, fixedAllocs_;
+    std::vector<void *> rodAllocs_, conAllocs_, blockAllocs_, fixedAllocs_, opAllocs_;
+    long long nnzCap_ = 0;
     int blockCap_ = 0;
     int nBilQueued_ = 0;
     AlensBlock *hBlocks_ = nullptr;

@@ -404,13 +404,15 @@ __global__ void k_ranges(DevState S) {
             d.alpha = 0.0;
             d.res = 0.0;
             active += d.active;
+            (void)active;
             maxIte = P.maxIte > maxIte ? P.maxIte : maxIte;
         }
         c->totalColl = totalColl;
         c->totalBil = S.bilPrefix[S.R];
         c->totalCon = totalColl + S.bilPrefix[S.R];
         c->nTiles = tile;
-        c->activeCount = active;
+        c->activeCnt[0] = c->activeCnt[1] = c->activeCnt[2] = 0;
+        c->finalParity = 1;
         c->maxIte = maxIte;
         c->bar.count = 0;
         c->bar.gen = 0;
@@ -444,6 +446,7 @@ __device__ void finish_constraint(const DevState &S, int k, const RepParams &P, 
     const double q = phi0 + P.dt * (dI + dJ);
     const double g0 = gamma0 < lb ? lb : gamma0;
     S.q[k] = q;
+    S.sgam[1][k] = g0;  // the solver starts from the parity-1 buffer
     S.gamma[k] = g0;
     S.lb[k] = lb;
     S.cinv[k] = cinv;
@@ -451,10 +454,8 @@ __device__ void finish_constraint(const DevState &S, int k, const RepParams &P, 
     atomicAdd(&S.rowCount[I], 1);
     if (J >= 0) atomicAdd(&S.rowCount[J], 1);
     if (S.precision == ALENS_PREC_MIXED) {
-#pragma unroll
-        for (int c = 0; c < 12; c++) S.jac32[12 * (size_t)k + c] = (float)jac[c];
         S.q32[k] = (float)q;
-        S.gamma32[k] = (float)g0;
+        S.sgam32[1][k] = (float)g0;
         S.lb32[k] = (float)lb;
         S.cinv32[k] = (float)cinv;
     }

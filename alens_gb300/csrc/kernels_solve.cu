@@ -1,5 +1,6 @@
-// kernels_solve.cu - FP64 BBPGD (bit-compatible with the oracle), solver
-// state reset, velocity write-back + Euler update (SimToolbox
+// kernels_solve.cu - FP64 BBPGD launch (bit-compatible with the oracle),
+// the hand-over from the FP32 solver to the FP64 refinement sweeps, the
+// final gamma gather, velocity write-back + Euler update (SimToolbox
 // SylinderSystem::stepEuler, SRC/TubuleSystem.cpp:55) and the constraint
 // stress sum (calcConStress, SRC/TubuleSystem.cpp:224).
 //
@@ -12,36 +13,47 @@ namespace {
 
 __device__ __forceinline__ int flags(const DevState &S) { return ld_volatile_i32(&S.ctl->errFlags); }
 
-// Re-arm the solver state of every replica; with from32, gamma starts from
-// the FP32 solution (refinement sweeps of the mixed solver).
-__global__ void k_solver_reset(DevState S, int from32) {
+// Start of the FP64 refinement: gamma0 = the FP32 solution, solver state
+// re-armed; the FP32 iteration count is kept in refineIter.
+__global__ void k_refine_setup(DevState S) {
     if (flags(S) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
+    const int par = S.ctl->finalParity;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int active = 0;
         for (int r = 0; r < S.R; r++) {
             RepDyn &d = S.dyn[r];
-            d.refineIter = d.iter;  // iterations of the previous (FP32) solve
+            d.refineIter = d.iter;
             d.iter = 0;
             d.active = d.nCon > 0 ? 1 : 0;
             d.converged = d.nCon > 0 ? 0 : 1;
             d.status = 0;
-            d.counter = 0;
-            d.alpha = 0.0;
             d.res = 0.0;
-            active += d.active;
-        }
-        S.ctl->activeCount = active;
-        S.ctl->bar.count = 0;
-        S.ctl->bar.gen = 0;
-    }
-    if (from32) {
-        const int nc = S.ctl->totalCon;
-        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) {
-            const double g = (double)S.gamma32[k];
-            const double lb = S.lb[k];
-            S.gamma[k] = g < lb ? lb : g;
         }
     }
+    const int nc = S.ctl->totalCon;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) {
+        const double g = (double)S.sgam32[par][k];
+        const double lb = S.lb[k];
+        S.sgam[1][k] = g < lb ? lb : g;
+    }
+}
+
+// Barrier and pass counters are re-armed by a separate single-thread
+// kernel so that no block of the next solver launch can observe them
+// half-written.
+__global__ void k_solver_arm(DevState S) {
+    DevCtl *c = S.ctl;
+    c->activeCnt[0] = c->activeCnt[1] = c->activeCnt[2] = 0;
+    c->bar.count = 0;
+    c->bar.gen = 0;
+    c->finalParity = 1;
+}
+
+__global__ void k_solver_finish(DevState S) {
+    if (flags(S) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
+    const int par = S.ctl->finalParity;
+    const int nc = S.ctl->totalCon;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x)
+        S.gamma[k] = S.sgam[par][k];
 }
 
 __global__ void k_advance(DevState S) {
@@ -130,32 +142,43 @@ __global__ void k_advance(DevState S) {
     }
 }
 
-// Pair virial sum_k gamma_k (labI - labJ)_a n_b per replica, canonical tree.
+// Pair virial sum_k gamma_k (labI - labJ)_a n_b per replica with the
+// canonical tree: 64-constraint tiles (two warp trees, then warp0 + warp1),
+// then chunk reduction per replica.
 __global__ void __launch_bounds__(256) k_stress_tiles(DevState S) {
-    __shared__ double scr[9][8];
+    __shared__ double tv[4][2][9];
     const int nTiles = S.ctl->nTiles;
     const size_t tc = (size_t)S.tileCap;
-    for (int T = blockIdx.x; T < nTiles; T += gridDim.x) {
-        const int rep = S.tileRep[T];
-        const RepDyn &d = S.dyn[rep];
-        const int local = (T - d.tileStart) * kTile + (int)threadIdx.x;
+    const int group = threadIdx.x >> 6, lane64 = threadIdx.x & 63, w = (threadIdx.x >> 5) & 1;
+    for (int base = blockIdx.x * 4; base < nTiles; base += gridDim.x * 4) {
+        const int T = base + group;
         double v[9];
 #pragma unroll
         for (int q = 0; q < 9; q++) v[q] = 0.0;
-        if (local < d.nCon) {
-            const int k = d.conStart + local;
-            const double gk = S.gamma[k];
+        if (T < nTiles) {
+            const RepDyn &d = S.dyn[S.tileRep[T]];
+            const int local = (T - d.tileStart) * kTile + lane64;
+            if (local < d.nCon) {
+                const int k = d.conStart + local;
+                const double gk = S.gamma[k];
 #pragma unroll
-            for (int a = 0; a < 3; a++) {
-                const double r = S.lab[6 * (size_t)k + a] - S.lab[6 * (size_t)k + 3 + a];
+                for (int a = 0; a < 3; a++) {
+                    const double r = S.lab[6 * (size_t)k + a] - S.lab[6 * (size_t)k + 3 + a];
 #pragma unroll
-                for (int b = 0; b < 3; b++) v[3 * a + b] = gk * r * S.jac[12 * (size_t)k + b];
+                    for (int b = 0; b < 3; b++) v[3 * a + b] = gk * r * S.jac[12 * (size_t)k + b];
+                }
             }
         }
-        block_tree_sum256<9>(v, scr);
-        if (threadIdx.x == 0)
 #pragma unroll
-            for (int q = 0; q < 9; q++) S.part[q * tc + T] = v[q];
+        for (int q = 0; q < 9; q++) v[q] = warp_tree_sum_t<double>(v[q]);
+        if ((threadIdx.x & 31) == 0)
+#pragma unroll
+            for (int q = 0; q < 9; q++) tv[group][w][q] = v[q];
+        __syncthreads();
+        if (threadIdx.x < 4 && base + (int)threadIdx.x < nTiles) {
+            const int g = threadIdx.x;
+            for (int q = 0; q < 9; q++) S.part[q * tc + base + g] = tv[g][0][q] + tv[g][1][q];
+        }
         __syncthreads();
     }
 }
@@ -163,7 +186,6 @@ __global__ void __launch_bounds__(256) k_stress_tiles(DevState S) {
 __global__ void __launch_bounds__(256) k_stress_final(DevState S) {
     __shared__ double scr[9][8];
     const size_t tc = (size_t)S.tileCap, wc = (size_t)S.workCap;
-    // replicas one after another: they share the chunk work space
     for (int r = 0; r < S.R; r++) {
         const RepDyn &d = S.dyn[r];
         const double *src[9];
@@ -182,13 +204,27 @@ __global__ void __launch_bounds__(256) k_stress_final(DevState S) {
     }
 }
 
-template <class Real>
-int max_grid_for(void (*kernel)(DevState, SolveView<Real>, unsigned long long)) {
+int occupancy_grid(const void *kernel) {
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kSolveThreads, 0);
     return nsm * (per > 0 ? per : 0);
+}
+
+template <class Real>
+cudaError_t launch_coop(const DevState &S, const SolveView<Real> &V, int grid,
+                        unsigned long long timeout_ns, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kSolveThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_solve<Real>, S, V, timeout_ns);
 }
 
 }  // namespace
@@ -198,56 +234,59 @@ cudaError_t launch_solve_fp32(const DevState &S, int grid, unsigned long long ti
 int solver_max_grid_fp32();
 
 int solver_max_grid(int precision) {
+    int g = occupancy_grid((const void *)k_solve<double>);
     if (precision == ALENS_PREC_MIXED) {
         const int a = solver_max_grid_fp32();
-        const int b = max_grid_for<double>(k_solve<double>);
-        return a < b ? a : b;
+        g = a < g ? a : g;
     }
-    return max_grid_for<double>(k_solve<double>);
-}
-
-static cudaError_t launch_coop_fp64(const DevState &S, int grid, unsigned long long timeout_ns,
-                                    cudaStream_t st) {
-    SolveView<double> V{S.jac, S.gamma, S.g, S.q, S.lb, S.cinv, S.U};
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(256);
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_solve<double>, S, V, timeout_ns);
+    return g < kMaxSolverGrid ? g : kMaxSolverGrid;
 }
 
 cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned long long timeout_ns,
                          cudaStream_t st, cudaEvent_t *ev, int *launches) {
     int n = 0;
     cudaError_t e;
+    SolveView<double> V{};
+    V.aptr = S.aptr;
+    V.acol = S.acol;
+    V.aval = S.aval;
+    V.gam[0] = S.sgam[0];
+    V.gam[1] = S.sgam[1];
+    V.g[0] = S.sg[0];
+    V.g[1] = S.sg[1];
+    V.q = S.q;
+    V.lb = S.lb;
+    V.cinv = S.cinv;
+    V.alphaBuf = S.alphaBuf;
+    V.fp64 = 1;
     if (ev) cudaEventRecord(ev[0], st);
     if (precision == ALENS_PREC_MIXED) {
         e = launch_solve_fp32(S, grid, timeout_ns, st);
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[1], st);
-        k_solver_reset<<<256, 256, 0, st>>>(S, 1);
+        k_refine_setup<<<256, 256, 0, st>>>(S);
+        k_solver_arm<<<1, 1, 0, st>>>(S);
+        n += 3;
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[2], st);
-        e = launch_coop_fp64(S, grid, timeout_ns, st);
+        e = launch_coop<double>(S, V, grid, timeout_ns, st);
+        n++;
         if (ev) cudaEventRecord(ev[3], st);
-        n = 3;
     } else {
-        e = launch_coop_fp64(S, grid, timeout_ns, st);
+        e = launch_coop<double>(S, V, grid, timeout_ns, st);
+        n++;
         if (ev) {
             cudaEventRecord(ev[1], st);
             cudaEventRecord(ev[2], st);
             cudaEventRecord(ev[3], st);
         }
-        n = 1;
     }
+    if (e != cudaSuccess) return e;
+    k_solver_finish<<<512, 256, 0, st>>>(S);
+    n++;
     if (launches) *launches += n;
-    return e;
+    return cudaGetLastError();
 }
 
 void launch_advance(const DevState &S, cudaStream_t st) {

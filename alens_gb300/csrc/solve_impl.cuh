@@ -1,42 +1,53 @@
-// solve_impl.cuh - persistent BBPGD kernel (the role of SimToolbox
-// BCQPSolver's BBPGD, conSolverChoice 0, docs/source/quickstart.md:356-358;
-// method: Yan, Zhang, Shelley, J. Chem. Phys. 150:064109 (2019) with
-// Barzilai-Borwein steps, IMA J. Numer. Anal. 8:141 (1988)).
+// solve_impl.cuh - persistent BBPGD kernel over the explicit Delassus
+// operator (the role of SimToolbox BCQPSolver's BBPGD, conSolverChoice 0,
+// docs/source/quickstart.md:356-358; method: Yan, Zhang, Shelley, J. Chem.
+// Phys. 150:064109 (2019) with alternating Barzilai-Borwein steps, IMA J.
+// Numer. Anal. 8:141 (1988)).
 //
-// Problem per replica: min 1/2 g^T A g + q^T g  s.t.  gamma_k >= lb_k
-// (lb = -inf for bilateral rows), A = dt D^T M D + diag(cinv).
+// Problem per replica: min 1/2 x^T A x + q^T x  s.t.  x_k >= lb_k
+// (lb = -inf on bilateral rows), A = dt D^T M D + diag(cinv).
 //
-// One cooperative launch runs every iteration of every replica.  Each pass is
-//   phase A (per rod):        x = source vector, F = D x, U = M F
-//   grid barrier
-//   phase B (per 256-tile):   (A x)_k = dt (D_I.U_I + D_J.U_J) + cinv_k x_k,
-//                             per-constraint update, tile partial sums
-//   last block of a replica:  canonical reduction of its tiles -> step size,
-//                             residual, convergence
-//   grid barrier
-// Passes: G0 (x = gamma0: g0 = A gamma0 + q, residual), AG (x = g0: initial
-// step g.g / g.Ag), then iterations x = P(gamma - alpha g).
+// One cooperative launch runs every iteration of every replica, one grid
+// barrier per pass.  Pass p:
+//   1. decision (every block, for the replicas of its tiles): canonical
+//      reduction of the pass p-1 tile partials -> residual test, step size;
+//      the block holding a replica's first tile records its state
+//   2. rows (64-constraint tiles, contiguous per block): row k forms
+//      x_l for its columns, (A x)_k, the update and the tile partials
+//   3. grid barrier
+// Passes: 0 = G0 (x = gamma0, g = A x + q, residual), 1 = AG (x = g: step
+// g.g / g.Ag), 2.. = iterations x = P(gamma - alpha g).  gamma and g
+// ping-pong between two buffers by pass parity; retired replicas copy their
+// values forward and mark their partials, so the last buffer always holds
+// every replica's final state.
 //
-// Real = double: the oracle's arithmetic bit for bit (compiled without FMA).
-// Real = float: FP32 Jacobian, velocities, gamma and g; FP64 dot products,
-// residual and step sizes.
+// Real = double reproduces the oracle bit for bit (compiled without FMA).
+// Real = float: FP32 operator, gamma and g, products and per-warp sums;
+// FP64 tile/chunk accumulation of the dot products and step sizes; the
+// residual min(g, x - lb) is exact for lb = 0 and bilateral rows.
 #pragma once
 
 #include "engine.cuh"
 
 namespace alens {
 
-enum SolveMode { kModeG0 = 0, kModeAG = 1, kModeIter = 2 };
+enum SolveMode { kModeCopy = 0, kModeG0 = 1, kModeAG = 2, kModeIter = 3 };
+constexpr int kSolveThreads = 256;
+constexpr int kRowTile = 64;         // level-1 reduction tile
+constexpr int kWindow = 64;          // replicas decided per block window
 
 template <class Real>
 struct SolveView {
-    const Real *jac;
-    Real *gamma;
-    Real *g;
+    const int *aptr;
+    const int *acol;
+    const Real *aval;
+    Real *gam[2];
+    Real *g[2];
     const Real *q;
     const Real *lb;
     const Real *cinv;
-    Real *U;
+    double *alphaBuf;   // 2 x R, by pass parity
+    int fp64;           // 1: exact oracle arithmetic
 };
 
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
@@ -48,48 +59,8 @@ __device__ __forceinline__ Real projlb(Real v, Real lb) {
     return v < lb ? lb : v;
 }
 
-template <class Real>
-__device__ __forceinline__ Real dot6u(const Real *J, const Real *U, size_t st, int r) {
-    return J[0] * ldcg(U + r) + J[1] * ldcg(U + st + r) + J[2] * ldcg(U + 2 * st + r) +
-           J[3] * ldcg(U + 3 * st + r) + J[4] * ldcg(U + 4 * st + r) + J[5] * ldcg(U + 5 * st + r);
-}
-
-template <class Real>
-__device__ __forceinline__ Real source_x(int mode, Real gam, Real gold, Real alpha, Real lb) {
-    if (mode == kModeG0) return gam;
-    if (mode == kModeAG) return gold;
-    return projlb<Real>(gam - alpha * gold, lb);
-}
-
-template <class Real>
-__device__ void phase_rods(const DevState &S, const SolveView<Real> &V, int mode) {
-    const size_t st = (size_t)S.nRods;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
-        const int rep = __ldg(S.rodRep + r);
-        if (!ldcg(&S.dyn[rep].active)) continue;
-        const Real alpha = (Real)ldcg(&S.dyn[rep].alpha);
-        Real F[6] = {Real(0), Real(0), Real(0), Real(0), Real(0), Real(0)};
-        const int e1 = __ldg(S.rowPtr + r + 1);
-        for (int e = __ldg(S.rowPtr + r); e < e1; e++) {
-            const int ent = __ldg(S.rowEnt + e);
-            const int k = ent >> 1;
-            const Real x = source_x<Real>(mode, ldcg(V.gamma + k), ldcg(V.g + k), alpha, __ldg(V.lb + k));
-            const Real *J = V.jac + 12 * (size_t)k + 6 * (ent & 1);
-#pragma unroll
-            for (int c = 0; c < 6; c++) F[c] = F[c] + x * __ldg(J + c);
-        }
-        Real Uo[6] = {Real(0), Real(0), Real(0), Real(0), Real(0), Real(0)};
-        if (!__ldg(S.imm + r)) {
-            const Real a[3] = {(Real)__ldg(S.ax + r), (Real)__ldg(S.ay + r), (Real)__ldg(S.az + r)};
-            const Real m[3] = {(Real)__ldg(S.m0 + r), (Real)__ldg(S.m1 + r), (Real)__ldg(S.m2 + r)};
-            mobility_apply<Real>(a, m, __ldg(S.sph + r) != 0, S.par[rep].mono != 0, F, Uo);
-        }
-#pragma unroll
-        for (int c = 0; c < 6; c++) V.U[c * st + r] = Uo[c];
-    }
-}
-
-// chunk reduction of tile partials with L2-coherent loads
+// chunk reduction (levels >= 2) of m tile partials with L2-coherent loads;
+// result valid in thread 0; all threads must call.
 template <int NV>
 __device__ void chunk_reduce_cg(const double *const (&src)[NV], int m, double *const (&work)[NV],
                                 double (&out)[NV], double (*scratch)[8]) {
@@ -125,6 +96,7 @@ __device__ void chunk_reduce_cg(const double *const (&src)[NV], int m, double *c
         if (mc == 1) {
 #pragma unroll
             for (int q = 0; q < NV; q++) out[q] = __ldcg(work[q]);
+            __syncthreads();
             return;
         }
 #pragma unroll
@@ -133,155 +105,248 @@ __device__ void chunk_reduce_cg(const double *const (&src)[NV], int m, double *c
     }
 }
 
-__device__ __forceinline__ void retire(DevCtl *ctl, RepDyn *d, int status, int converged) {
-    d->status = status;
-    d->converged = converged;
-    d->active = 0;
-    atomicSub(&ctl->activeCount, 1);
-}
+struct SolveShared {
+    double scr[3][8];
+    double scrmax[8];
+    double alpha[kWindow];
+    int mode[kWindow];
+    double tileVal[4][2][4];  // [group][warp][kind]
+};
 
-// Final reduction and state update of replica `rep`, run by its last block.
+// Decision of replica r at pass p from the pass p-1 partials; identical in
+// every block that evaluates it.
 template <class Real>
-__device__ void replica_update(const DevState &S, int rep, int mode, int it, double (*scr)[8],
-                              double *scrmax) {
-    RepDyn *d = &S.dyn[rep];
-    const int t0 = d->tileStart, nt = d->nTiles;
+__device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r, int t0, int t1,
+                       SolveShared &sh, int slot) {
+    const RepDyn &d = S.dyn[r];
+    const RepParams &P = S.par[r];
+    if (p == 0) {
+        if (threadIdx.x == 0) {
+            sh.mode[slot] = kModeG0;
+            sh.alpha[slot] = 0.0;
+            if (d.nCon > 0 && d.tileStart >= t0 && d.tileStart < t1) atomicAdd(&S.ctl->activeCnt[0], 1);
+        }
+        __syncthreads();
+        return;
+    }
+    const int par = (p - 1) & 1;
     const size_t tc = (size_t)S.tileCap, wc = (size_t)S.workCap;
-    const double *const src[3] = {S.part + t0, S.part + tc + t0, S.part + 2 * tc + t0};
-    double *const work[3] = {S.work, S.work + wc, S.work + 2 * wc};
+    const double *base = S.part + (size_t)par * 4 * tc;
+    const double *const src[3] = {base + d.tileStart, base + tc + d.tileStart, base + 2 * tc + d.tileStart};
+    // each block uses its own chunk work space
+    double *wb = S.work + (size_t)blockIdx.x * 3 * wc;
+    double *const work[3] = {wb, wb + wc, wb + 2 * wc};
     double sums[3];
-    chunk_reduce_cg<3>(src, nt, work, sums, scr);
-    double mx = 0.0;
-    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        const double v = __ldcg(S.part + 3 * tc + t0 + i);
+    chunk_reduce_cg<3>(src, d.nTiles, work, sums, sh.scr);
+    // max over tiles (order-free); retired replicas carry -1
+    double mx = -2.0;
+    for (int i = threadIdx.x; i < d.nTiles; i += blockDim.x) {
+        const double v = __ldcg(base + 3 * tc + d.tileStart + i);
         mx = v > mx ? v : mx;
     }
-    mx = block_max256(mx, scrmax);
+    mx = block_max256(mx, sh.scrmax);
     if (threadIdx.x == 0) {
-        const RepParams &P = S.par[rep];
-        DevCtl *ctl = S.ctl;
-        if (mode == kModeG0) {
-            d->res = mx;
+        const bool owner = d.tileStart >= t0 && d.tileStart < t1;
+        int mode = kModeCopy;
+        double alpha = 0.0;
+        int status = -1, iter = 0;
+        if (mx < 0.0) {
+            mode = kModeCopy;  // retired in an earlier pass
+        } else if (p == 1) {
             if (isinf(mx))
-                retire(ctl, d, ALENS_NAN_DETECTED, 0);
+                status = ALENS_NAN_DETECTED;
             else if (mx <= P.tol)
-                retire(ctl, d, ALENS_OK, 1);
+                status = ALENS_OK;
             else if (P.maxIte <= 0)
-                retire(ctl, d, ALENS_NOT_CONVERGED, 0);
-        } else if (mode == kModeAG) {
+                status = ALENS_NOT_CONVERGED;
+            else
+                mode = kModeAG;
+        } else if (p == 2) {
             const double gg = sums[0], gAg = sums[1];
-            double alpha = (gAg > 0.0) ? gg / gAg : 1.0;
+            alpha = (gAg > 0.0) ? gg / gAg : 1.0;
             if (!(alpha > 0.0) || isinf(alpha)) alpha = 1.0;
-            d->alpha = alpha;
+            mode = kModeIter;
         } else {
-            d->iter = it;
-            d->res = mx;
+            const int itp = p - 2;
+            iter = itp;
             if (isinf(mx)) {
-                retire(ctl, d, ALENS_NAN_DETECTED, 0);
+                status = ALENS_NAN_DETECTED;
             } else if (mx <= P.tol) {
-                retire(ctl, d, ALENS_OK, 1);
+                status = ALENS_OK;
             } else {
+                alpha = __ldcg(V.alphaBuf + (size_t)((p - 1) & 1) * S.R + r);
                 const double ss = sums[0], sy = sums[1], yy = sums[2];
                 if (sy > 0.0) {
-                    const double a = (it & 1) ? ss / sy : sy / yy;
-                    if (a > 0.0 && !isinf(a)) d->alpha = a;
+                    const double a = (itp & 1) ? ss / sy : sy / yy;
+                    if (a > 0.0 && !isinf(a)) alpha = a;
                 }
-                if (it >= P.maxIte) retire(ctl, d, ALENS_NOT_CONVERGED, 0);
+                if (itp >= P.maxIte)
+                    status = ALENS_NOT_CONVERGED;
+                else
+                    mode = kModeIter;
             }
         }
-        d->counter = 0;
-        __threadfence();
+        sh.mode[slot] = mode;
+        sh.alpha[slot] = alpha;
+        if (owner) {
+            if (status >= 0) {
+                RepDyn *dw = &S.dyn[r];
+                dw->status = status;
+                dw->converged = status == ALENS_OK ? 1 : 0;
+                dw->iter = iter;
+                dw->res = mx;
+                dw->active = 0;
+            }
+            if (mode != kModeCopy) {
+                atomicAdd(&S.ctl->activeCnt[p % 3], 1);
+                __stcg(V.alphaBuf + (size_t)(p & 1) * S.R + r, alpha);
+            }
+        }
     }
     __syncthreads();
 }
 
+// One 64-constraint tile processed by a 64-thread group (two warps).
 template <class Real>
-__device__ void phase_tiles(const DevState &S, const SolveView<Real> &V, int mode, int it,
-                            double (*scr)[8], double *scrmax, int *s_last) {
-    const size_t st = (size_t)S.nRods;
-    const size_t tc = (size_t)S.tileCap;
-    const int nTiles = S.ctl->nTiles;
-    for (int T = blockIdx.x; T < nTiles; T += gridDim.x) {
-        const int rep = __ldg(S.tileRep + T);
-        RepDyn *d = &S.dyn[rep];
-        if (!ldcg(&d->active)) continue;
-        const int local = (T - d->tileStart) * kTile + (int)threadIdx.x;
-        const int k = d->conStart + local;
-        double v[3] = {0.0, 0.0, 0.0};
-        double r = 0.0;
-        if (local < d->nCon) {
-            const Real alpha = (Real)ldcg(&d->alpha);
-            const Real *J = V.jac + 12 * (size_t)k;
-            const int I = __ldg(S.conI + k), Jr = __ldg(S.conJ + k);
-            const Real dI = dot6u<Real>(J, V.U, st, I);
-            const Real dJ = Jr >= 0 ? dot6u<Real>(J + 6, V.U, st, Jr) : Real(0);
-            const Real gam = ldcg(V.gamma + k), gold = ldcg(V.g + k);
-            const Real lbk = __ldg(V.lb + k);
-            const Real x = source_x<Real>(mode, gam, gold, alpha, lbk);
-            Real Ax = (Real)S.par[rep].dt * (dI + dJ);
-            Ax = Ax + __ldg(V.cinv + k) * x;
-            if (mode == kModeAG) {
-                const double gd = (double)gold;
-                v[0] = gd * gd;
-                v[1] = gd * (double)Ax;
+__device__ void process_tile(const DevState &S, const SolveView<Real> &V, int p, int T, int mode,
+                             Real alpha, SolveShared &sh, int group) {
+    const int lane64 = threadIdx.x & 63;
+    const int warpInGroup = (threadIdx.x >> 5) & 1;
+    const int r = __ldg(S.tileRep + T);
+    const RepDyn &d = S.dyn[r];
+    const int local = (T - d.tileStart) * kRowTile + lane64;
+    const bool valid = local < d.nCon;
+    const int k = d.conStart + local;
+    const int inB = (p + 1) & 1, outB = p & 1;
+    Real v0 = Real(0), v1 = Real(0), v2 = Real(0);
+    double rmax = 0.0;
+    if (mode == kModeCopy) {
+        rmax = -1.0;
+        if (valid) {
+            V.gam[outB][k] = ldcg(V.gam[inB] + k);
+            V.g[outB][k] = ldcg(V.g[inB] + k);
+        }
+    } else if (valid) {
+        const Real gam = ldcg(V.gam[inB] + k);
+        const Real gold = mode == kModeG0 ? Real(0) : ldcg(V.g[inB] + k);
+        const Real lbk = __ldg(V.lb + k);
+        Real xk;
+        if (mode == kModeG0)
+            xk = gam;
+        else if (mode == kModeAG)
+            xk = gold;
+        else
+            xk = projlb<Real>(gam - alpha * gold, lbk);
+        Real acc = Real(0);
+        const int e1 = __ldg(V.aptr + k + 1);
+        for (int e = __ldg(V.aptr + k); e < e1; e++) {
+            const int l = __ldg(V.acol + e);
+            Real xl;
+            if (mode == kModeG0) {
+                xl = ldcg(V.gam[inB] + l);
+            } else if (mode == kModeAG) {
+                xl = ldcg(V.g[inB] + l);
             } else {
-                const Real gn = Ax + __ldg(V.q + k);
-                const double xd = (double)x, gnd = (double)gn, lbd = (double)lbk;
-                r = fabs(xd - projlb<double>(xd - gnd, lbd));
-                if (mode == kModeIter) {
-                    const double s = xd - (double)gam;
-                    const double y = gnd - (double)gold;
-                    v[0] = s * s;
-                    v[1] = s * y;
-                    v[2] = y * y;
-                    V.gamma[k] = x;
-                }
-                V.g[k] = gn;
-                if (r != r) {
-                    atomicOr(&S.ctl->errFlags, kErrNaN);
-                    r = INFINITY;
-                }
+                xl = projlb<Real>(ldcg(V.gam[inB] + l) - alpha * ldcg(V.g[inB] + l), __ldg(V.lb + l));
             }
+            acc = acc + __ldg(V.aval + e) * xl;
         }
-        block_tree_sum256<3>(v, scr);
-        r = block_max256(r, scrmax);
-        if (threadIdx.x == 0) {
-            __stcg(S.part + T, v[0]);
-            __stcg(S.part + tc + T, v[1]);
-            __stcg(S.part + 2 * tc + T, v[2]);
-            __stcg(S.part + 3 * tc + T, r);
-            __threadfence();
-            const int ticket = atomicAdd(&d->counter, 1);
-            *s_last = (ticket == d->nTiles - 1);
+        acc = acc + __ldg(V.cinv + k) * xk;
+        if (mode == kModeAG) {
+            v0 = gold * gold;
+            v1 = gold * acc;
+            V.gam[outB][k] = gam;
+            V.g[outB][k] = gold;
+        } else {
+            const Real gn = acc + __ldg(V.q + k);
+            if (V.fp64) {
+                const double xd = (double)xk;
+                const double gd = (double)gn;
+                rmax = fabs(xd - projlb<double>(xd - gd, (double)lbk));
+            } else {
+                // x - P(x - g) = min(g, x - lb): exact for lb = 0 and lb = -inf
+                const Real m = gn < xk - lbk ? gn : xk - lbk;
+                rmax = fabs((double)m);
+            }
+            if (rmax != rmax) {
+                atomicOr(&S.ctl->errFlags, kErrNaN);
+                rmax = INFINITY;
+            }
+            if (mode == kModeIter) {
+                const Real s = xk - gam;
+                const Real y = gn - gold;
+                v0 = s * s;
+                v1 = s * y;
+                v2 = y * y;
+            }
+            V.gam[outB][k] = xk;
+            V.g[outB][k] = gn;
         }
-        __syncthreads();
-        if (*s_last) {
-            __threadfence();
-            replica_update<Real>(S, rep, mode, it, scr, scrmax);
-        }
-        __syncthreads();
+    }
+    // warp trees in Real, tile = warp0 + warp1 in FP64
+    Real w0 = warp_tree_sum_t<Real>(v0);
+    Real w1 = warp_tree_sum_t<Real>(v1);
+    Real w2 = warp_tree_sum_t<Real>(v2);
+    double wm = warp_max(rmax);
+    if ((threadIdx.x & 31) == 0) {
+        sh.tileVal[group][warpInGroup][0] = (double)w0;
+        sh.tileVal[group][warpInGroup][1] = (double)w1;
+        sh.tileVal[group][warpInGroup][2] = (double)w2;
+        sh.tileVal[group][warpInGroup][3] = wm;
     }
 }
 
 template <class Real>
-__global__ void __launch_bounds__(256) k_solve(DevState S, SolveView<Real> V,
-                                               unsigned long long timeout_ns) {
-    __shared__ double scr[3][8];
-    __shared__ double scrmax[8];
-    __shared__ int s_last;
+__global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<Real> V,
+                                                         unsigned long long timeout_ns) {
+    __shared__ SolveShared sh;
     if (ld_volatile_i32(&S.ctl->errFlags) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
     const unsigned int nb = gridDim.x;
-    const int maxIte = S.ctl->maxIte;
-    for (int pass = 0;; pass++) {
-        const int mode = pass == 0 ? kModeG0 : (pass == 1 ? kModeAG : kModeIter);
-        const int it = pass - 1;
-        if (mode == kModeIter && it > maxIte) break;
-        if (ldcg(&S.ctl->activeCount) <= 0) break;
-        phase_rods<Real>(S, V, mode);
+    const int nTiles = S.ctl->nTiles;
+    const int tpb = (nTiles + (int)nb - 1) / (int)nb;
+    const int t0 = min((int)blockIdx.x * tpb, nTiles);
+    const int t1 = min(t0 + tpb, nTiles);
+    const int maxPass = S.ctl->maxIte + 3;
+    const size_t tc = (size_t)S.tileCap;
+    const int group = threadIdx.x >> 6;
+    int lastPass = 0;
+    for (int p = 0; p <= maxPass; p++) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl->activeCnt[(p + 1) % 3] = 0;
+        double *partBase = S.part + (size_t)(p & 1) * 4 * tc;
+        // replica windows of this block's tile range
+        int T = t0;
+        while (T < t1) {
+            const int rFirst = __ldg(S.tileRep + T);
+            const int rLast = min(__ldg(S.tileRep + t1 - 1), rFirst + kWindow - 1);
+            for (int r = rFirst; r <= rLast; r++) decide<Real>(S, V, p, r, t0, t1, sh, r - rFirst);
+            // tiles of the window, four per round
+            int Tend = T;
+            while (Tend < t1 && __ldg(S.tileRep + Tend) <= rLast) Tend++;
+            for (int base = T; base < Tend; base += 4) {
+                const int Tg = base + group;
+                if (Tg < Tend) {
+                    const int slot = __ldg(S.tileRep + Tg) - rFirst;
+                    process_tile<Real>(S, V, p, Tg, sh.mode[slot], (Real)sh.alpha[slot], sh, group);
+                }
+                __syncthreads();
+                if (threadIdx.x < 4 && base + (int)threadIdx.x < Tend) {
+                    const int g = threadIdx.x;
+                    const int Tw = base + g;
+#pragma unroll
+                    for (int q = 0; q < 3; q++)
+                        __stcg(partBase + q * tc + Tw, sh.tileVal[g][0][q] + sh.tileVal[g][1][q]);
+                    const double a = sh.tileVal[g][0][3], b = sh.tileVal[g][1][3];
+                    __stcg(partBase + 3 * tc + Tw, a > b ? a : b);
+                }
+                __syncthreads();
+            }
+            T = Tend;
+        }
+        lastPass = p;
         if (!grid_sync(&S.ctl->bar, nb, &S.ctl->errFlags, timeout_ns)) return;
-        phase_tiles<Real>(S, V, mode, it, scr, scrmax, &s_last);
-        if (!grid_sync(&S.ctl->bar, nb, &S.ctl->errFlags, timeout_ns)) return;
+        if (ldcg(&S.ctl->activeCnt[p % 3]) == 0) break;
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl->finalParity = lastPass & 1;
 }
 
 }  // namespace alens

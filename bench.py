@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="bounded CPU-oracle sample for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="print per-stage CUDA-event times of both solver forms (direct launches) "
+                         "for profiling; no JSON line")
     return ap.parse_args()
 
 
@@ -277,8 +280,43 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_case(args):
+    """Direct-launch steps with stage timing: per-stage ms and ms per BBPGD
+    pass for both forms (the command profiled under ncu)."""
+    import torch
+    from alens_gb300 import capi, workloads
+    w = workload(args, 0)
+    rods = relaxed_state(w, args.pre_steps, capi.GpuSystem)
+    stream = torch.cuda.Stream()
+    for name, prec, warm in (("plain_fp64", capi.PREC_FP64, capi.WARM_ZERO),
+                             ("mixed_warm", capi.PREC_MIXED, capi.WARM_PREV)):
+        c = workloads.config_with(w.cfg, precision=prec, warmStart=warm, stageTiming=1, useGraph=0)
+        c.stream = stream.cuda_stream
+        g = capi.GpuSystem(c)
+        g.set_rods(rods)
+        g.step()
+        acc = np.zeros(5)
+        passes = 0
+        for _ in range(args.steps):
+            st = g.step()
+            acc += g.stage_times()
+            it = st["iterations"]
+            passes += 1 + (1 + it if it > 0 else 0)
+        acc /= args.steps
+        print(json.dumps({"form": name, "ms_detect": acc[0], "ms_solve_main": acc[1], "ms_refine": acc[2],
+                          "ms_advance": acc[3], "ms_step": acc[4],
+                          "us_per_pass": 1e3 * acc[1] * args.steps / max(passes, 1),
+                          "passes_per_step": passes / args.steps,
+                          "blocks_per_sm": os.environ.get("ALENS_SOLVER_BLOCKS_PER_SM", "default")}),
+              flush=True)
+        g.close()
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -16,7 +16,9 @@
 //     parallel-overlap case resolved at the overlap midpoint);
 //   * the complementarity formulation and BBPGD with alternating
 //     Barzilai-Borwein steps (Yan, Zhang, Shelley, J. Chem. Phys. 150:064109
-//     (2019); Barzilai & Borwein, IMA J. Numer. Anal. 8:141 (1988));
+//     (2019); Barzilai & Borwein, IMA J. Numer. Anal. 8:141 (1988)); the
+//     operator dt D^T M D is assembled explicitly once per step (the
+//     Delassus matrix of contact mechanics) and applied as a sparse product;
 //   * slender-body drag of a straight rod from the local slender-body
 //     operator of Tornberg & Shelley, J. Comput. Phys. 196:8 (2004):
 //     b = -(1 + 2 ln(r/L)), zeta_par = 4 pi mu L / b,
@@ -184,18 +186,20 @@ void normals6(uint64_t seed, int64_t gid, int64_t step, double z[6]) {
 }
 
 // ------------------------------------------------------- canonical reduction
-// Level 1: tiles of 256 elements, one per lane of 8 warps; warp tree with
-// offsets 16..1 (v[l] = v[l] + v[l+off]), then the same tree over the 8 warp
-// sums with offsets 4,2,1.  Level 2+: chunks of 2048 partials, lane t adds
-// partials t, t+256, ..., t+1792 in order, then the same two trees.
+// Level 1: tiles of 64 elements held by two warps; in each warp the tree
+// v[l] = v[l] + v[l+off] for off = 16..1, then tile = warp0 + warp1.
+// Level 2+: chunks of 2048 partials over 256 lanes: lane t adds partials
+// t, t+256, ..., t+1792 in order, warp trees as above, then the 8 warp sums
+// with offsets 4,2,1; repeated until one value remains.
+double warp_tree(double *v) {
+    for (int off = 16; off >= 1; off >>= 1)
+        for (int l = 0; l < off; l++) v[l] = v[l] + v[l + off];
+    return v[0];
+}
+
 double tree256(double *lanes) {
-    for (int w = 0; w < 8; w++) {
-        double *v = lanes + 32 * w;
-        for (int off = 16; off >= 1; off >>= 1)
-            for (int l = 0; l < off; l++) v[l] = v[l] + v[l + off];
-    }
     double ws[8];
-    for (int w = 0; w < 8; w++) ws[w] = lanes[32 * w];
+    for (int w = 0; w < 8; w++) ws[w] = warp_tree(lanes + 32 * w);
     for (int off = 4; off >= 1; off >>= 1)
         for (int i = 0; i < off; i++) ws[i] = ws[i] + ws[i + off];
     return ws[0];
@@ -203,12 +207,14 @@ double tree256(double *lanes) {
 
 template <class F>
 double tile_sum(F &&val, int64_t base, int64_t n) {
-    double lanes[256];
-    for (int l = 0; l < 256; l++) {
+    double lanes[64];
+    for (int l = 0; l < 64; l++) {
         const int64_t i = base + l;
         lanes[l] = (i < n) ? val(i) : 0.0;
     }
-    return tree256(lanes);
+    const double w0 = warp_tree(lanes);
+    const double w1 = warp_tree(lanes + 32);
+    return w0 + w1;
 }
 
 double chunk_sum(const double *T, int64_t base, int64_t m) {
@@ -239,10 +245,10 @@ double reduce_partials(std::vector<double> T) {
 
 template <class F>
 double canon_sum_f(F &&val, int64_t n) {
-    const int64_t m = (n + 255) / 256;
+    const int64_t m = (n + 63) / 64;
     std::vector<double> T(m);
 #pragma omp parallel for schedule(static)
-    for (int64_t t = 0; t < m; t++) T[t] = tile_sum(val, 256 * t, n);
+    for (int64_t t = 0; t < m; t++) T[t] = tile_sum(val, 64 * t, n);
     return reduce_partials(std::move(T));
 }
 
@@ -421,6 +427,10 @@ struct OrcCtx {
     // rod-major rows: entries 2k+side, ascending
     std::vector<int64_t> rowptr;
     std::vector<int64_t> rowent;
+    // Delassus operator rows (ascending column)
+    std::vector<int64_t> aptr;
+    std::vector<int> acol;
+    std::vector<double> aval;
     // warm start
     std::vector<uint64_t> prevKeys;
     std::vector<double> prevGamma;
@@ -762,35 +772,78 @@ void build_constraints(OrcCtx *x) {
     }
 }
 
-// y = A x  (without q): F = D x, U = M F, y_k = dt*(J_I.U_I + J_J.U_J) + cinv_k x_k
-void apply_A(OrcCtx *x, const std::vector<double> &xin, std::vector<double> &y,
-             std::vector<double> &U) {
-    const int n = x->n;
+// Delassus operator A = dt D^T M D, assembled explicitly per step.
+// W_k,side = M_rod J_k,side (mobility-weighted Jacobian).  Row k lists the
+// constraints l that share a rod with k, in ascending l; its value is
+// dt * (sum of J_k,sk . W_l,sl over shared rods), contributions ordered by
+// k's side (rod I first), then by the rod row (entry 2l+sl ascending).
+void build_delassus(OrcCtx *x) {
     const int nc = x->ncoll + x->nbil;
     const bool mono = x->cfg.monolayer != 0;
-    U.assign(6 * (size_t)n, 0.0);
-#pragma omp parallel for schedule(static)
-    for (int r = 0; r < n; r++) {
-        double F[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        for (int64_t e = x->rowptr[r]; e < x->rowptr[r + 1]; e++) {
-            const int64_t ent = x->rowent[e];
-            const int64_t k = ent >> 1;
-            const double *J = &x->jac[12 * k + 6 * (ent & 1)];
-            const double g = xin[k];
-            for (int cc = 0; cc < 6; cc++) F[cc] = F[cc] + g * J[cc];
-        }
-        if (x->imm[r]) continue;
-        mobility_apply(&x->axis[3 * r], &x->mob[3 * r], x->sph[r], mono, F, &U[6 * (size_t)r]);
-    }
-    y.assign(nc, 0.0);
     const double dt = x->cfg.dt;
+    std::vector<double> W(12 * (size_t)nc, 0.0);
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < nc; k++) {
-        const double *J = &x->jac[12 * (size_t)k];
-        const double dI = dot6(J, &U[6 * (size_t)x->ci[k]]);
-        const double dJ = x->cj[k] >= 0 ? dot6(J + 6, &U[6 * (size_t)x->cj[k]]) : 0.0;
-        double v = dt * (dI + dJ);
+        for (int side = 0; side < 2; side++) {
+            const int r = side == 0 ? x->ci[k] : x->cj[k];
+            if (r < 0 || x->imm[r]) continue;
+            mobility_apply(&x->axis[3 * r], &x->mob[3 * r], x->sph[r], mono,
+                           &x->jac[12 * (size_t)k + 6 * side], &W[12 * (size_t)k + 6 * side]);
+        }
+    }
+    std::vector<std::vector<std::pair<int, double>>> rows(nc);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int k = 0; k < nc; k++) {
+        const int rI = x->ci[k], rJ = x->cj[k];
+        const int64_t *LI = &x->rowent[x->rowptr[rI]];
+        const int64_t nI = x->rowptr[rI + 1] - x->rowptr[rI];
+        const int64_t *LJ = rJ >= 0 ? &x->rowent[x->rowptr[rJ]] : nullptr;
+        const int64_t nJ = rJ >= 0 ? x->rowptr[rJ + 1] - x->rowptr[rJ] : 0;
+        const double *JkI = &x->jac[12 * (size_t)k];
+        const double *JkJ = JkI + 6;
+        int64_t a = 0, b = 0;
+        auto &row = rows[k];
+        while (a < nI || b < nJ) {
+            const int64_t la = a < nI ? (LI[a] >> 1) : INT64_MAX;
+            const int64_t lb = b < nJ ? (LJ[b] >> 1) : INT64_MAX;
+            const int64_t l = la < lb ? la : lb;
+            double acc = 0.0;
+            while (a < nI && (LI[a] >> 1) == l) {
+                acc = acc + dot6(JkI, &W[12 * (size_t)l + 6 * (LI[a] & 1)]);
+                a++;
+            }
+            while (b < nJ && (LJ[b] >> 1) == l) {
+                acc = acc + dot6(JkJ, &W[12 * (size_t)l + 6 * (LJ[b] & 1)]);
+                b++;
+            }
+            row.emplace_back((int)l, dt * acc);
+        }
+    }
+    x->aptr.assign(nc + 1, 0);
+    for (int k = 0; k < nc; k++) x->aptr[k + 1] = x->aptr[k] + (int64_t)rows[k].size();
+    x->acol.resize(x->aptr[nc]);
+    x->aval.resize(x->aptr[nc]);
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < nc; k++) {
+        int64_t o = x->aptr[k];
+        for (auto &e : rows[k]) {
+            x->acol[o] = e.first;
+            x->aval[o] = e.second;
+            o++;
+        }
+    }
+}
+
+// y_k = sum_l A_kl x_l (ascending l) + cinv_k x_k  (+ q_k when withQ)
+void spmv_A(OrcCtx *x, const std::vector<double> &xin, std::vector<double> &y, bool withQ) {
+    const int nc = x->ncoll + x->nbil;
+    y.assign(nc, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < nc; k++) {
+        double v = 0.0;
+        for (int64_t e = x->aptr[k]; e < x->aptr[k + 1]; e++) v = v + x->aval[e] * xin[x->acol[e]];
         v = v + x->cinv[k] * xin[k];
+        if (withQ) v = v + x->q[k];
         y[k] = v;
     }
 }
@@ -809,9 +862,9 @@ int solve_bbpgd(OrcCtx *x, AlensStepStats *st) {
     st->residual = 0.0;
     st->converged = 1;
     if (nc == 0) return ALENS_OK;
-    std::vector<double> g, Ag, U, gn, gamn(nc);
-    apply_A(x, gam, g, U);
-    for (int k = 0; k < nc; k++) g[k] = g[k] + x->q[k];
+    build_delassus(x);
+    std::vector<double> g, Ag, gn, gamn(nc);
+    spmv_A(x, gam, g, true);
     auto residual = [&](const std::vector<double> &gm, const std::vector<double> &gg) {
         double res = 0.0;
         bool bad = false;
@@ -833,7 +886,7 @@ int solve_bbpgd(OrcCtx *x, AlensStepStats *st) {
         st->residual = res;
         return ALENS_OK;
     }
-    apply_A(x, g, Ag, U);
+    spmv_A(x, g, Ag, false);
     const double gg = canon_sum_f([&](int64_t k) { return g[k] * g[k]; }, nc);
     const double gAg = canon_sum_f([&](int64_t k) { return g[k] * Ag[k]; }, nc);
     double alpha = (gAg > 0.0) ? gg / gAg : 1.0;
@@ -844,8 +897,7 @@ int solve_bbpgd(OrcCtx *x, AlensStepStats *st) {
 #pragma omp parallel for schedule(static)
         for (int k = 0; k < nc; k++)
             gamn[k] = proj(gam[k] - alpha * g[k], x->unil[k], x->lb[k]);
-        apply_A(x, gamn, gn, U);
-        for (int k = 0; k < nc; k++) gn[k] = gn[k] + x->q[k];
+        spmv_A(x, gamn, gn, true);
         const double ss = canon_sum_f(
             [&](int64_t k) { const double s = gamn[k] - gam[k]; return s * s; }, nc);
         const double sy = canon_sum_f(

@@ -119,17 +119,18 @@ def test_dcp_random_against_brute_force():
 
 
 # ------------------------------------------------- canonical reduction
+def _warp(v):
+    v = list(v)
+    off = 16
+    while off >= 1:
+        for l in range(off):
+            v[l] = v[l] + v[l + off]
+        off //= 2
+    return v[0]
+
+
 def _tree256(lanes):
-    lanes = list(lanes)
-    for w in range(8):
-        v = lanes[32 * w:32 * w + 32]
-        off = 16
-        while off >= 1:
-            for l in range(off):
-                v[l] = v[l] + v[l + off]
-            off //= 2
-        lanes[32 * w] = v[0]
-    ws = [lanes[32 * w] for w in range(8)]
+    ws = [_warp(lanes[32 * w:32 * w + 32]) for w in range(8)]
     for off in (4, 2, 1):
         for i in range(off):
             ws[i] = ws[i] + ws[i + off]
@@ -141,7 +142,10 @@ def _canon_py(v):
     n = len(v)
     if n == 0:
         return 0.0
-    T = [_tree256([v[b + l] if b + l < n else 0.0 for l in range(256)]) for b in range(0, n, 256)]
+    def tile64(b):
+        lanes = [v[b + l] if b + l < n else 0.0 for l in range(64)]
+        return _warp(lanes[:32]) + _warp(lanes[32:])
+    T = [tile64(b) for b in range(0, n, 64)]
     while True:
         m = len(T)
         R = []
@@ -160,7 +164,7 @@ def _canon_py(v):
         T = R
 
 
-@pytest.mark.parametrize("n", [0, 1, 255, 256, 257, 5000, 70000])
+@pytest.mark.parametrize("n", [0, 1, 63, 64, 65, 5000, 140000])
 def test_canonical_sum_tree(n):
     rng = np.random.default_rng(n)
     v = rng.normal(size=n) * 10.0 ** rng.uniform(-8, 8, size=n)
