@@ -135,8 +135,11 @@ def make_config(box_low=(0.0, 0.0, 0.0), box_high=(5.0, 5.0, 5.0), pbc=(1, 1, 1)
 
 
 class AlensError(RuntimeError):
-    def __init__(self, status: int, where: str):
-        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} ({status})")
+    def __init__(self, status: int, where: str, detail: str = ""):
+        msg = f"{where}: {STATUS_NAMES.get(status, status)} ({status})"
+        if detail:
+            msg += f" [{detail}]"
+        super().__init__(msg)
         self.status = status
 
 
@@ -183,6 +186,7 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_step_count": (C.c_int, [vp, _PI64]),
         "alens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "alens_get_launch_count": (C.c_int, [vp, _PI64]),
+        "alens_get_last_error": (C.c_char_p, [vp]),
         "alens_get_stage_times": (C.c_int, [vp, _PD]),
     }
     for name, (res, args) in sigs.items():
@@ -238,6 +242,15 @@ class RodState:
 class GpuSystem:
     """One context of the CUDA library (``nrep`` replicas, default 1)."""
 
+    def _ck(self, rc, where, ok=(ALENS_OK,)):
+        if rc not in ok:
+            detail = ""
+            if self.h:
+                d = self.lib.alens_get_last_error(self.h)
+                detail = d.decode() if d else ""
+            raise AlensError(rc, where, detail)
+        return rc
+
     def __init__(self, cfg: AlensConfig | list[AlensConfig], lib: C.CDLL | None = None):
         self.lib = lib or load_library()
         self.h = C.c_void_p()
@@ -268,7 +281,7 @@ class GpuSystem:
         self.close()
 
     def set_rods(self, rods: RodState, replica: int = 0):
-        _ck(self.lib.alens_set_rods(self.h, replica, rods.n, _p(rods.gid, C.c_int64), _p(rods.pos, C.c_double),
+        self._ck(self.lib.alens_set_rods(self.h, replica, rods.n, _p(rods.gid, C.c_int64), _p(rods.pos, C.c_double),
                                     _p(rods.quat, C.c_double), _p(rods.length, C.c_double),
                                     _p(rods.radius, C.c_double), _p(rods.immovable, C.c_int32)),
             "alens_set_rods")
@@ -277,13 +290,13 @@ class GpuSystem:
     def update_rods(self, pos, quat, replica: int = 0):
         pos = np.ascontiguousarray(pos, dtype=np.float64)
         quat = np.ascontiguousarray(quat, dtype=np.float64)
-        _ck(self.lib.alens_update_rods(self.h, replica, self.n[replica], _p(pos, C.c_double),
+        self._ck(self.lib.alens_update_rods(self.h, replica, self.n[replica], _p(pos, C.c_double),
                                        _p(quat, C.c_double)), "alens_update_rods")
 
     def get_rods(self, replica: int = 0, out=None):
         n = self.n[replica]
         pos, quat = out if out is not None else (np.empty((n, 3)), np.empty((n, 4)))
-        _ck(self.lib.alens_get_rods(self.h, replica, n, _p(pos, C.c_double), _p(quat, C.c_double)),
+        self._ck(self.lib.alens_get_rods(self.h, replica, n, _p(pos, C.c_double), _p(quat, C.c_double)),
             "alens_get_rods")
         return pos, quat
 
@@ -291,18 +304,18 @@ class GpuSystem:
         n = self.n[replica]
         v = np.empty((n, 3))
         w = np.empty((n, 3))
-        _ck(self.lib.alens_get_velocity(self.h, replica, n, _p(v, C.c_double), _p(w, C.c_double)),
+        self._ck(self.lib.alens_get_velocity(self.h, replica, n, _p(v, C.c_double), _p(w, C.c_double)),
             "alens_get_velocity")
         return v, w
 
     def add_bilateral(self, blocks, replica: int = 0):
         arr = (AlensBlock * len(blocks))(*blocks)
-        _ck(self.lib.alens_add_bilateral(self.h, replica, len(blocks), arr), "alens_add_bilateral")
+        self._ck(self.lib.alens_add_bilateral(self.h, replica, len(blocks), arr), "alens_add_bilateral")
 
     def _stage(self, fn, name, ok=(ALENS_OK,)):
         st = AlensStepStats()
         rc = fn(self.h, C.byref(st))
-        _ck(rc, name, ok)
+        self._ck(rc, name, ok)
         d = st.as_dict()
         d["rc"] = rc
         return d
@@ -323,13 +336,13 @@ class GpuSystem:
 
     def replica_stats(self, replica: int):
         st = AlensStepStats()
-        _ck(self.lib.alens_get_replica_stats(self.h, replica, C.byref(st)), "alens_get_replica_stats")
+        self._ck(self.lib.alens_get_replica_stats(self.h, replica, C.byref(st)), "alens_get_replica_stats")
         return st.as_dict()
 
     def num_constraints(self, replica: int = 0):
         a = C.c_int32()
         b = C.c_int32()
-        _ck(self.lib.alens_get_num_constraints(self.h, replica, C.byref(a), C.byref(b)),
+        self._ck(self.lib.alens_get_num_constraints(self.h, replica, C.byref(a), C.byref(b)),
             "alens_get_num_constraints")
         return a.value, b.value
 
@@ -342,32 +355,32 @@ class GpuSystem:
         d0 = np.empty(n)
         g = np.empty(n)
         jac = np.empty((n, 12))
-        _ck(self.lib.alens_get_constraints(self.h, replica, n, _p(ii, C.c_int32), _p(jj, C.c_int32),
+        self._ck(self.lib.alens_get_constraints(self.h, replica, n, _p(ii, C.c_int32), _p(jj, C.c_int32),
                                            _p(im, C.c_int32), _p(d0, C.c_double), _p(g, C.c_double),
                                            _p(jac, C.c_double)), "alens_get_constraints")
         return dict(i=ii, j=jj, image=im, delta0=d0, gamma=g, jac=jac, ncoll=nc, nbil=nb)
 
     def con_stress(self, replica: int = 0):
         s = np.empty(9)
-        _ck(self.lib.alens_get_con_stress(self.h, replica, _p(s, C.c_double)), "alens_get_con_stress")
+        self._ck(self.lib.alens_get_con_stress(self.h, replica, _p(s, C.c_double)), "alens_get_con_stress")
         return s.reshape(3, 3)
 
     def step_count(self) -> int:
         c = C.c_int64()
-        _ck(self.lib.alens_get_step_count(self.h, C.byref(c)), "alens_get_step_count")
+        self._ck(self.lib.alens_get_step_count(self.h, C.byref(c)), "alens_get_step_count")
         return c.value
 
     def launch_count(self) -> int:
         c = C.c_int64()
-        _ck(self.lib.alens_get_launch_count(self.h, C.byref(c)), "alens_get_launch_count")
+        self._ck(self.lib.alens_get_launch_count(self.h, C.byref(c)), "alens_get_launch_count")
         return c.value
 
     def stage_times(self):
         t = np.zeros(5)
-        _ck(self.lib.alens_get_stage_times(self.h, _p(t, C.c_double)), "alens_get_stage_times")
+        self._ck(self.lib.alens_get_stage_times(self.h, _p(t, C.c_double)), "alens_get_stage_times")
         return t
 
     def stream_handle(self) -> int:
         s = C.c_void_p()
-        _ck(self.lib.alens_get_stream(self.h, C.byref(s)), "alens_get_stream")
+        self._ck(self.lib.alens_get_stream(self.h, C.byref(s)), "alens_get_stream")
         return s.value or 0

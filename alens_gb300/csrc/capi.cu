@@ -5,26 +5,39 @@
 
 #include "engine.h"
 
+#include <string>
+
 struct AlensCtx {
     alens::Engine *eng;
+    std::string lastError;
 };
 
 namespace {
 
 template <class F>
-int guarded(F &&f) {
+int guarded_ctx(AlensCtx *ctx, F &&f) {
     try {
-        return f();
+        const int rc = f();
+        return rc;
     } catch (const alens::ApiError &e) {
+        if (ctx) ctx->lastError = alens_status_str(e.status);
         return e.status;
     } catch (const alens::CudaFailure &e) {
+        if (ctx) ctx->lastError = std::string(e.where) + ": " + cudaGetErrorString(e.err);
         cudaGetLastError();
         return ALENS_CUDA_ERROR;
     } catch (const std::bad_alloc &) {
+        if (ctx) ctx->lastError = "host allocation failed";
         return ALENS_CUDA_ERROR;
     } catch (...) {
+        if (ctx) ctx->lastError = "unknown exception";
         return ALENS_CUDA_ERROR;
     }
+}
+
+template <class F>
+int guarded(F &&f) {
+    return guarded_ctx(nullptr, f);
 }
 
 }  // namespace
@@ -79,7 +92,7 @@ int alens_create_ensemble(const AlensConfig *cfgs, int nReplica, AlensCtx **out)
     if (!cfgs || !out || nReplica < 1) return ALENS_INVALID_ARG;
     *out = nullptr;
     return guarded([&] {
-        AlensCtx *c = new AlensCtx{new alens::Engine(cfgs, nReplica)};
+        AlensCtx *c = new AlensCtx{new alens::Engine(cfgs, nReplica), std::string()};
         *out = c;
         return (int)ALENS_OK;
     });
@@ -98,7 +111,7 @@ int alens_set_rods(AlensCtx *ctx, int replica, int n, const int64_t *gid, const 
                    const double *orientation, const double *length, const double *radius,
                    const int32_t *immovable) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->setRods(replica, n, gid, pos, orientation, length, radius, immovable);
         return (int)ALENS_OK;
     });
@@ -106,7 +119,7 @@ int alens_set_rods(AlensCtx *ctx, int replica, int n, const int64_t *gid, const 
 
 int alens_update_rods(AlensCtx *ctx, int replica, int n, const double *pos, const double *orientation) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->updateRods(replica, n, pos, orientation);
         return (int)ALENS_OK;
     });
@@ -114,7 +127,7 @@ int alens_update_rods(AlensCtx *ctx, int replica, int n, const double *pos, cons
 
 int alens_get_rods(AlensCtx *ctx, int replica, int n, double *pos, double *orientation) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->getRods(replica, n, pos, orientation);
         return (int)ALENS_OK;
     });
@@ -122,7 +135,7 @@ int alens_get_rods(AlensCtx *ctx, int replica, int n, double *pos, double *orien
 
 int alens_get_velocity(AlensCtx *ctx, int replica, int n, double *vel, double *omega) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->getVelocity(replica, n, vel, omega);
         return (int)ALENS_OK;
     });
@@ -130,7 +143,7 @@ int alens_get_velocity(AlensCtx *ctx, int replica, int n, double *vel, double *o
 
 int alens_add_bilateral(AlensCtx *ctx, int replica, int n, const AlensBlock *blocks) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->addBilateral(replica, n, blocks);
         return (int)ALENS_OK;
     });
@@ -138,27 +151,27 @@ int alens_add_bilateral(AlensCtx *ctx, int replica, int n, const AlensBlock *blo
 
 int alens_step(AlensCtx *ctx, AlensStepStats *stats) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] { return ctx->eng->step(stats); });
+    return guarded_ctx(ctx, [&] { return ctx->eng->step(stats); });
 }
 
 int alens_detect(AlensCtx *ctx, AlensStepStats *stats) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] { return ctx->eng->detect(stats); });
+    return guarded_ctx(ctx, [&] { return ctx->eng->detect(stats); });
 }
 
 int alens_solve(AlensCtx *ctx, AlensStepStats *stats) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] { return ctx->eng->solve(stats); });
+    return guarded_ctx(ctx, [&] { return ctx->eng->solve(stats); });
 }
 
 int alens_advance(AlensCtx *ctx, AlensStepStats *stats) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] { return ctx->eng->advance(stats); });
+    return guarded_ctx(ctx, [&] { return ctx->eng->advance(stats); });
 }
 
 int alens_get_replica_stats(AlensCtx *ctx, int replica, AlensStepStats *stats) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->replicaStats(replica, stats);
         return (int)ALENS_OK;
     });
@@ -166,7 +179,7 @@ int alens_get_replica_stats(AlensCtx *ctx, int replica, AlensStepStats *stats) {
 
 int alens_get_num_constraints(AlensCtx *ctx, int replica, int *nCollision, int *nBilateral) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->numConstraints(replica, nCollision, nBilateral);
         return (int)ALENS_OK;
     });
@@ -175,7 +188,7 @@ int alens_get_num_constraints(AlensCtx *ctx, int replica, int *nCollision, int *
 int alens_get_constraints(AlensCtx *ctx, int replica, int cap, int32_t *indexI, int32_t *indexJ,
                           int32_t *image, double *delta0, double *gamma, double *jac) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->getConstraints(replica, cap, indexI, indexJ, image, delta0, gamma, jac);
         return (int)ALENS_OK;
     });
@@ -183,7 +196,7 @@ int alens_get_constraints(AlensCtx *ctx, int replica, int cap, int32_t *indexI, 
 
 int alens_get_con_stress(AlensCtx *ctx, int replica, double *stress9) {
     if (!ctx) return ALENS_INVALID_ARG;
-    return guarded([&] {
+    return guarded_ctx(ctx, [&] {
         ctx->eng->conStress(replica, stress9);
         return (int)ALENS_OK;
     });
@@ -193,6 +206,11 @@ int alens_get_step_count(AlensCtx *ctx, int64_t *count) {
     if (!ctx || !count) return ALENS_INVALID_ARG;
     *count = ctx->eng->stepCount();
     return ALENS_OK;
+}
+
+const char *alens_get_last_error(AlensCtx *ctx) {
+    if (!ctx) return "";
+    return ctx->lastError.c_str();
 }
 
 int alens_get_launch_count(AlensCtx *ctx, int64_t *count) {

@@ -19,7 +19,7 @@ constexpr double kTwoPi = 6.283185307179586;
 constexpr double kLn2 = 0.6931471805599453;
 constexpr double kParallelEps = 1e-12;
 constexpr int kTile = 64;         // level-1 reduction tile (constraints)
-constexpr int kChunk = 2048;      // level-2+ reduction chunk
+constexpr int kChunk = 1024;      // level-2+ reduction chunk (one warp)
 constexpr int kImageNone = 13;    // image code of the zero periodic shift
 
 // error flag bits (DevCtl::errFlags)

@@ -224,9 +224,10 @@ void Engine::finalize() {
     // rods
     auto &G = rodAllocs_;
     double **rodD[] = {&S.px, &S.py, &S.pz, &S.qx, &S.qy, &S.qz, &S.qw, &S.len, &S.rad,
-                       &S.ax, &S.ay, &S.az, &S.hcol, &S.rcol, &S.m0, &S.m1, &S.m2,
-                       &S.sx, &S.sy, &S.sz, &S.sax, &S.say, &S.saz, &S.sh, &S.sr};
+                       &S.ax, &S.ay, &S.az, &S.hcol, &S.rcol, &S.m0, &S.m1, &S.m2};
     for (double **p : rodD) *p = alloc<double>(G, N);
+    S.sA = alloc<float4>(G, N);
+    S.sB = alloc<float4>(G, N);
     S.gid = alloc<long long>(G, N);
     S.imm = alloc<int>(G, N);
     S.rodRep = alloc<int>(G, N);
@@ -284,6 +285,7 @@ void Engine::finalize() {
     allocConstraints(std::min(want, kMaxConstraints), false);
     solverGrid_ = 0;
     dirty_ = false;
+    prevCountHost_ = 0;
     haveDetect_ = false;
     haveSolve_ = false;
     CK(cudaStreamSynchronize(stream_));
@@ -295,7 +297,7 @@ void Engine::allocConstraints(int cap, bool keepPrev) {
     double *oldGamma = S.prevGamma;
     std::vector<void *> old;
     old.swap(conAllocs_);
-    const int prevN = keepPrev ? hCtl_->totalColl : 0;
+    const int prevN = keepPrev ? prevCountHost_ : 0;
     auto &G = conAllocs_;
     S.cap = cap;
     S.tileCap = cap / kTile + R_ + 2;
@@ -648,6 +650,7 @@ int Engine::step(AlensStepStats *out) {
             for (auto &q : queue_) q.clear();
             stepCount_++;
             last_.step = stepCount_ - 1;
+            prevCountHost_ = hCtl_->totalColl;
         }
         haveDetect_ = haveSolve_ = false;
         if (out) *out = last_;
@@ -688,6 +691,7 @@ int Engine::advance(AlensStepStats *out) {
     readBack();
     for (auto &q : queue_) q.clear();
     stepCount_++;
+    prevCountHost_ = hCtl_->totalColl;
     haveDetect_ = haveSolve_ = false;
     if (out) *out = last_;
     return ALENS_OK;

@@ -83,7 +83,7 @@ struct DevState {
     double *stage;          // 7 x nRods host-transfer staging (interleaved)
     // cells
     int *cellOf, *cellCount, *cellStart, *cellCursor;
-    double *sx, *sy, *sz, *sax, *say, *saz, *sh, *sr;
+    float4 *sA, *sB;   // cell-sorted FP32 search geometry
     int *sidx;
     // pairs
     int *pairCount, *pairOff, *pairCursor;

@@ -89,7 +89,8 @@ class Engine {
     int precision_ = 0, warm_ = 0;
     bool useGraph_ = true, graphFailed_ = false;
     int fixedCap_ = 0;
-    int solverBlocksPerSM_ = 2;
+    int solverBlocksPerSM_ = 1;
+    int prevCountHost_ = 0;  // valid warm-start keys on the device
     int solverGrid_ = 0;
     std::vector<HostRods> rods_;
     std::vector<std::vector<AlensBlock>> queue_;

@@ -206,19 +206,23 @@ __global__ void k_scan_add(int *out, int n, const int *tmp) {
 }
 
 // ------------------------------------------------------------- scatter
+// Cell-sorted FP32 search geometry: centre relative to its cell origin and
+// half-length (sA), axis and collision radius (sB).  Relative coordinates
+// keep the FP32 screen accurate whatever the box size.
 __global__ void k_scatter(DevState S) {
     if (flags(S) & kErrNaN) return;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const int cid = S.cellOf[r];
         const int slot = S.cellStart[cid] + atomicAdd(&S.cellCursor[cid], 1);
-        S.sx[slot] = S.px[r];
-        S.sy[slot] = S.py[r];
-        S.sz[slot] = S.pz[r];
-        S.sax[slot] = S.ax[r];
-        S.say[slot] = S.ay[r];
-        S.saz[slot] = S.az[r];
-        S.sh[slot] = S.hcol[r];
-        S.sr[slot] = S.rcol[r];
+        const RepParams &P = S.par[S.rodRep[r]];
+        const int lc = cid - P.cellOffset;
+        const int cx = lc % P.ncell[0], cy = (lc / P.ncell[0]) % P.ncell[1], cz = lc / (P.ncell[0] * P.ncell[1]);
+        const double ox = P.lo[0] + (double)cx * P.cellsz[0];
+        const double oy = P.lo[1] + (double)cy * P.cellsz[1];
+        const double oz = P.lo[2] + (double)cz * P.cellsz[2];
+        S.sA[slot] = make_float4((float)(S.px[r] - ox), (float)(S.py[r] - oy), (float)(S.pz[r] - oz),
+                                 (float)S.hcol[r]);
+        S.sB[slot] = make_float4((float)S.ax[r], (float)S.ay[r], (float)S.az[r], (float)S.rcol[r]);
         S.sidx[slot] = r;
     }
 }
@@ -226,6 +230,11 @@ __global__ void k_scatter(DevState S) {
 // ---------------------------------------------------------- pair search
 constexpr int kPairBuf = 16;
 constexpr int kPairThreads = 128;
+// Screening margin (um) between the FP32 separation and the FP64 decision:
+// candidates with |sep32 - colBuf| < margin are decided in FP64 with the
+// oracle's arithmetic, all others by the FP32 value.  FP32 errors on
+// cell-relative coordinates are below 1e-5 um.
+constexpr float kScreenMargin = 1e-3f;
 
 __device__ __forceinline__ void flush_keys(const DevState &S, const unsigned long long *buf, int nb) {
     const int base = atomicAdd(&S.ctl->rawCount, nb);
@@ -238,8 +247,56 @@ __device__ __forceinline__ void flush_keys(const DevState &S, const unsigned lon
     }
 }
 
+__device__ __forceinline__ float clampf_(float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+// segment distance in FP32 (screen only)
+__device__ __forceinline__ float dcp_dist32(float3 c1, float3 u1, float h1, float3 c2, float3 u2, float h2) {
+    const float w0 = c1.x - c2.x, w1 = c1.y - c2.y, w2 = c1.z - c2.z;
+    const float b = u1.x * u2.x + u1.y * u2.y + u1.z * u2.z;
+    const float d = u1.x * w0 + u1.y * w1 + u1.z * w2;
+    const float e = u2.x * w0 + u2.y * w1 + u2.z * w2;
+    const float det = 1.0f - b * b;
+    float s;
+    if (det > 1e-6f) {
+        s = clampf_((b * e - d) / det, -h1, h1);
+    } else {
+        const float ab = fabsf(b);
+        const float lo = fmaxf(-h1, -d - ab * h2), hi = fminf(h1, -d + ab * h2);
+        s = lo <= hi ? 0.5f * (lo + hi) : clampf_(-d, -h1, h1);
+    }
+    float t = b * s + e;
+    if (t < -h2) {
+        t = -h2;
+        s = clampf_(b * t - d, -h1, h1);
+    } else if (t > h2) {
+        t = h2;
+        s = clampf_(b * t - d, -h1, h1);
+    }
+    const float x0 = w0 + s * u1.x - t * u2.x, x1 = w1 + s * u1.y - t * u2.y, x2 = w2 + s * u1.z - t * u2.z;
+    return sqrtf(x0 * x0 + x1 * x1 + x2 * x2);
+}
+
+// exact decision (the oracle's arithmetic) for a borderline candidate
+__device__ __noinline__ bool exact_pair(const DevState &S, int i, int j, const RepParams &P, int sx, int sy,
+                                        int sz) {
+    const double pi[3] = {S.px[i], S.py[i], S.pz[i]};
+    const double ai[3] = {S.ax[i], S.ay[i], S.az[i]};
+    const double c2[3] = {S.px[j] + (double)sx * P.L[0], S.py[j] + (double)sy * P.L[1],
+                          S.pz[j] + (double)sz * P.L[2]};
+    const double aj[3] = {S.ax[j], S.ay[j], S.az[j]};
+    const double hi_ = S.hcol[i], hj = S.hcol[j], ri = S.rcol[i], rj = S.rcol[j];
+    const double d0 = pi[0] - c2[0], d1 = pi[1] - c2[1], d2 = pi[2] - c2[2];
+    const double dd = d0 * d0 + d1 * d1 + d2 * d2;
+    const double lim = hi_ + hj + ri + rj + P.colBuf;
+    if (dd > lim * lim * (1.0 + 1e-10) + 1e-300) return false;
+    const DcpResult R = dcp_segseg(pi, ai, hi_, c2, aj, hj);
+    const double sep = R.dist - ri - rj;
+    return sep < P.colBuf;
+}
+
 // One thread per cell-sorted slot; the warp walks neighbour cells mostly in
-// lockstep, so candidate loads are broadcasts.
+// lockstep, so candidate loads are broadcasts.  FP32 screen, FP64 decision
+// only within the screening margin.
 __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = t < S.nRods && !(flags(S) & kErrNaN);
@@ -249,11 +306,14 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
         int cnt = 0;
         const int i = S.sidx[t];
         const RepParams &P = S.par[S.rodRep[i]];
-        const double pi[3] = {S.sx[t], S.sy[t], S.sz[t]};
-        const double ai[3] = {S.sax[t], S.say[t], S.saz[t]};
-        const double hi_ = S.sh[t], ri = S.sr[t];
-        const double colBuf = P.colBuf;
+        const float4 Ai = S.sA[t], Bi = S.sB[t];
+        const float3 ci = make_float3(Ai.x, Ai.y, Ai.z);
+        const float3 ui = make_float3(Bi.x, Bi.y, Bi.z);
+        const float hi_ = Ai.w, ri = Bi.w;
+        const float colBuf = (float)P.colBuf;
+        const float cutLo = colBuf - kScreenMargin, cutHi = colBuf + kScreenMargin;
         const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
+        const float csx = (float)P.cellsz[0], csy = (float)P.cellsz[1], csz = (float)P.cellsz[2];
         const int lc = S.cellOf[i] - P.cellOffset;
         const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
         for (int oz = -1; oz <= 1; oz++) {
@@ -293,32 +353,29 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
                         }
                     }
                     const int img = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
-                    const double S0 = (double)sx * P.L[0];
-                    const double S1 = (double)sy * P.L[1];
-                    const double S2 = (double)sz * P.L[2];
+                    // the neighbour cell's origin relative to ours
+                    const float3 off = make_float3((float)ox * csx, (float)oy * csy, (float)oz * csz);
                     const int cell = P.cellOffset + (z * ny + y) * nx + xx;
                     const int m1 = S.cellStart[cell + 1];
                     for (int m = S.cellStart[cell]; m < m1; m++) {
                         const int j = S.sidx[m];
                         if (j < i) continue;
                         if (j == i && img <= kImageNone) continue;
-                        const double c2[3] = {S.sx[m] + S0, S.sy[m] + S1, S.sz[m] + S2};
-                        const double d0 = pi[0] - c2[0], d1 = pi[1] - c2[1], d2 = pi[2] - c2[2];
-                        const double dd = d0 * d0 + d1 * d1 + d2 * d2;
-                        const double hj = S.sh[m], rj = S.sr[m];
-                        const double lim = hi_ + hj + ri + rj + colBuf;
-                        if (dd > lim * lim * (1.0 + 1e-10) + 1e-300) continue;
-                        const double aj[3] = {S.sax[m], S.say[m], S.saz[m]};
-                        const DcpResult R = dcp_segseg(pi, ai, hi_, c2, aj, hj);
-                        const double sep = R.dist - ri - rj;
-                        if (sep < colBuf) {
-                            if (nb == kPairBuf) {
-                                flush_keys(S, buf, nb);
-                                nb = 0;
-                            }
-                            buf[nb++] = pair_key(i, j, img);
-                            cnt++;
+                        const float4 Aj = S.sA[m];
+                        const float3 cj = make_float3(Aj.x + off.x, Aj.y + off.y, Aj.z + off.z);
+                        const float d0 = ci.x - cj.x, d1 = ci.y - cj.y, d2 = ci.z - cj.z;
+                        const float4 Bj = S.sB[m];
+                        const float lim = hi_ + Aj.w + ri + Bj.w + cutHi;
+                        if (d0 * d0 + d1 * d1 + d2 * d2 > lim * lim) continue;
+                        const float sep = dcp_dist32(ci, ui, hi_, cj, make_float3(Bj.x, Bj.y, Bj.z), Aj.w) - ri - Bj.w;
+                        if (sep >= cutHi) continue;
+                        if (sep >= cutLo && !exact_pair(S, i, j, P, sx, sy, sz)) continue;
+                        if (nb == kPairBuf) {
+                            flush_keys(S, buf, nb);
+                            nb = 0;
                         }
+                        buf[nb++] = pair_key(i, j, img);
+                        cnt++;
                     }
                 }
             }

@@ -183,24 +183,19 @@ __global__ void __launch_bounds__(256) k_stress_tiles(DevState S) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_stress_final(DevState S) {
-    __shared__ double scr[9][8];
-    const size_t tc = (size_t)S.tileCap, wc = (size_t)S.workCap;
+__global__ void k_stress_final(DevState S) {
+    __shared__ double chunk[9][64];
+    const size_t tc = (size_t)S.tileCap;
     for (int r = 0; r < S.R; r++) {
         const RepDyn &d = S.dyn[r];
         const double *src[9];
-        double *work[9];
-        for (int q = 0; q < 9; q++) {
-            src[q] = S.part + q * tc + d.tileStart;
-            work[q] = S.work + q * wc;
-        }
+        for (int q = 0; q < 9; q++) src[q] = S.part + q * tc + d.tileStart;
         const double *const(&srcr)[9] = src;
-        double *const(&workr)[9] = work;
         double out[9];
-        chunk_reduce_cg<9>(srcr, d.nTiles, workr, out, scr);
+        warp_chunk_reduce<9>(srcr, d.nTiles, chunk, out, nullptr, nullptr);
         if (threadIdx.x == 0)
             for (int q = 0; q < 9; q++) S.stress[9 * r + q] = out[q];
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -298,7 +293,7 @@ void launch_advance(const DevState &S, cudaStream_t st) {
 
 void launch_stress(const DevState &S, cudaStream_t st) {
     k_stress_tiles<<<1024, 256, 0, st>>>(S);
-    k_stress_final<<<1, 256, 0, st>>>(S);
+    k_stress_final<<<1, 32, 0, st>>>(S);
 }
 
 }  // namespace alens

@@ -21,7 +21,9 @@
 // values forward and mark their partials, so the last buffer always holds
 // every replica's final state.
 //
-// Real = double reproduces the oracle bit for bit (compiled without FMA).
+// Real = double reproduces the oracle bit for bit (compiled without FMA
+// contraction; the fused multiply-adds of the row product are explicit on
+// both sides).
 // Real = float: FP32 operator, gamma and g, products and per-warp sums;
 // FP64 tile/chunk accumulation of the dot products and step sizes; the
 // residual min(g, x - lb) is exact for lb = 0 and bilateral rows.
@@ -35,6 +37,7 @@ enum SolveMode { kModeCopy = 0, kModeG0 = 1, kModeAG = 2, kModeIter = 3 };
 constexpr int kSolveThreads = 256;
 constexpr int kRowTile = 64;         // level-1 reduction tile
 constexpr int kWindow = 64;          // replicas decided per block window
+constexpr int kRowPrefetch = 8;      // row entries loaded together
 
 template <class Real>
 struct SolveView {
@@ -59,55 +62,71 @@ __device__ __forceinline__ Real projlb(Real v, Real lb) {
     return v < lb ? lb : v;
 }
 
-// chunk reduction (levels >= 2) of m tile partials with L2-coherent loads;
-// result valid in thread 0; all threads must call.
+// Levels >= 2 of the canonical reduction, run by one warp: chunks of 1024
+// partials, lane l adds partials l, l+32, ..., l+992 in order, then the warp
+// tree; chunk sums are kept in shared memory (up to 64 chunks) and reduced
+// the same way until one value remains.  Loads bypass L1 (the partials are
+// written by other SMs).  The max over all partials of kind `maxKind`
+// (-1: none) is returned in *mx (order-free).  Result valid in lane 0.
 template <int NV>
-__device__ void chunk_reduce_cg(const double *const (&src)[NV], int m, double *const (&work)[NV],
-                                double (&out)[NV], double (*scratch)[8]) {
-    if (m <= 0) {
+__device__ void warp_chunk_reduce(const double *const (&src)[NV], int m, double (*chunk)[64],
+                                  double (&out)[NV], const double *maxSrc, double *mx) {
+    const int lane = threadIdx.x & 31;
+    double lmax = -2.0;
+    int mc = (m + kChunk - 1) / kChunk;
+    for (int c = 0; c < mc; c++) {
+        double acc[NV];
 #pragma unroll
-        for (int q = 0; q < NV; q++) out[q] = 0.0;
-        return;
+        for (int q = 0; q < NV; q++) acc[q] = 0.0;
+#pragma unroll 4
+        for (int j = 0; j < 32; j++) {
+            const int i = c * kChunk + lane + 32 * j;
+            if (i < m) {
+#pragma unroll
+                for (int q = 0; q < NV; q++) acc[q] = acc[q] + __ldcg(src[q] + i);
+                if (maxSrc) {
+                    const double v = __ldcg(maxSrc + i);
+                    lmax = v > lmax ? v : lmax;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            acc[q] = warp_tree_sum_t<double>(acc[q]);
+            if (lane == 0) chunk[q][c] = acc[q];
+        }
     }
-    const double *cur[NV];
-#pragma unroll
-    for (int q = 0; q < NV; q++) cur[q] = src[q];
-    while (true) {
-        const int mc = (m + kChunk - 1) / kChunk;
+    __syncwarp();
+    while (mc > 1) {
+        const int m2 = mc;
+        mc = (m2 + kChunk - 1) / kChunk;  // == 1 while m2 <= 1024
         for (int c = 0; c < mc; c++) {
-            double v[NV];
+            double acc[NV];
+#pragma unroll
+            for (int q = 0; q < NV; q++) acc[q] = 0.0;
+            for (int j = 0; j < 32; j++) {
+                const int i = c * kChunk + lane + 32 * j;
+                if (i < m2) {
+#pragma unroll
+                    for (int q = 0; q < NV; q++) acc[q] = acc[q] + chunk[q][i];
+                }
+            }
+            __syncwarp();
 #pragma unroll
             for (int q = 0; q < NV; q++) {
-                double acc = 0.0;
-#pragma unroll
-                for (int k = 0; k < 8; k++) {
-                    const int i = c * kChunk + (int)threadIdx.x + 256 * k;
-                    if (i < m) acc = acc + __ldcg(cur[q] + i);
-                }
-                v[q] = acc;
+                acc[q] = warp_tree_sum_t<double>(acc[q]);
+                if (lane == 0) chunk[q][c] = acc[q];
             }
-            block_tree_sum256<NV>(v, scratch);
-            if (threadIdx.x == 0) {
-#pragma unroll
-                for (int q = 0; q < NV; q++) __stcg(work[q] + c, v[q]);
-            }
-            __syncthreads();
+            __syncwarp();
         }
-        if (mc == 1) {
-#pragma unroll
-            for (int q = 0; q < NV; q++) out[q] = __ldcg(work[q]);
-            __syncthreads();
-            return;
-        }
-#pragma unroll
-        for (int q = 0; q < NV; q++) cur[q] = work[q];
-        m = mc;
     }
+#pragma unroll
+    for (int q = 0; q < NV; q++) out[q] = m > 0 ? chunk[q][0] : 0.0;
+    if (mx) *mx = warp_max(lmax);
 }
 
 struct SolveShared {
-    double scr[3][8];
-    double scrmax[8];
+    double chunk[3][64];
     double alpha[kWindow];
     int mode[kWindow];
     double tileVal[4][2][4];  // [group][warp][kind]
@@ -130,22 +149,13 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
         return;
     }
     const int par = (p - 1) & 1;
-    const size_t tc = (size_t)S.tileCap, wc = (size_t)S.workCap;
+    const size_t tc = (size_t)S.tileCap;
     const double *base = S.part + (size_t)par * 4 * tc;
-    const double *const src[3] = {base + d.tileStart, base + tc + d.tileStart, base + 2 * tc + d.tileStart};
-    // each block uses its own chunk work space
-    double *wb = S.work + (size_t)blockIdx.x * 3 * wc;
-    double *const work[3] = {wb, wb + wc, wb + 2 * wc};
-    double sums[3];
-    chunk_reduce_cg<3>(src, d.nTiles, work, sums, sh.scr);
-    // max over tiles (order-free); retired replicas carry -1
-    double mx = -2.0;
-    for (int i = threadIdx.x; i < d.nTiles; i += blockDim.x) {
-        const double v = __ldcg(base + 3 * tc + d.tileStart + i);
-        mx = v > mx ? v : mx;
-    }
-    mx = block_max256(mx, sh.scrmax);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
+        const double *const src[3] = {base + d.tileStart, base + tc + d.tileStart, base + 2 * tc + d.tileStart};
+        double sums[3], mx;
+        warp_chunk_reduce<3>(src, d.nTiles, sh.chunk, sums, base + 3 * tc + d.tileStart, &mx);
+        if (threadIdx.x == 0) {
         const bool owner = d.tileStart >= t0 && d.tileStart < t1;
         int mode = kModeCopy;
         double alpha = 0.0;
@@ -202,6 +212,7 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
                 __stcg(V.alphaBuf + (size_t)(p & 1) * S.R + r, alpha);
             }
         }
+        }
     }
     __syncthreads();
 }
@@ -236,22 +247,44 @@ __device__ void process_tile(const DevState &S, const SolveView<Real> &V, int p,
         else if (mode == kModeAG)
             xk = gold;
         else
-            xk = projlb<Real>(gam - alpha * gold, lbk);
+            xk = projlb<Real>(fma(-alpha, gold, gam), lbk);
+        // row k of A: columns and values first, then the column iterates,
+        // so that each group of loads is independent
         Real acc = Real(0);
-        const int e1 = __ldg(V.aptr + k + 1);
-        for (int e = __ldg(V.aptr + k); e < e1; e++) {
-            const int l = __ldg(V.acol + e);
-            Real xl;
-            if (mode == kModeG0) {
-                xl = ldcg(V.gam[inB] + l);
-            } else if (mode == kModeAG) {
-                xl = ldcg(V.g[inB] + l);
-            } else {
-                xl = projlb<Real>(ldcg(V.gam[inB] + l) - alpha * ldcg(V.g[inB] + l), __ldg(V.lb + l));
+        const int e0 = __ldg(V.aptr + k), e1 = __ldg(V.aptr + k + 1);
+        for (int eb = e0; eb < e1; eb += kRowPrefetch) {
+            int cols[kRowPrefetch];
+            Real vals[kRowPrefetch];
+#pragma unroll
+            for (int j = 0; j < kRowPrefetch; j++) {
+                cols[j] = eb + j < e1 ? __ldg(V.acol + eb + j) : k;
+                vals[j] = eb + j < e1 ? __ldg(V.aval + eb + j) : Real(0);
             }
-            acc = acc + __ldg(V.aval + e) * xl;
+            Real xa[kRowPrefetch], xb[kRowPrefetch], xc[kRowPrefetch];
+#pragma unroll
+            for (int j = 0; j < kRowPrefetch; j++) {
+                if (eb + j < e1) {
+                    const int l = cols[j];
+                    if (mode == kModeG0) {
+                        xa[j] = ldcg(V.gam[inB] + l);
+                    } else if (mode == kModeAG) {
+                        xa[j] = ldcg(V.g[inB] + l);
+                    } else {
+                        xa[j] = ldcg(V.gam[inB] + l);
+                        xb[j] = ldcg(V.g[inB] + l);
+                        xc[j] = __ldg(V.lb + l);
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kRowPrefetch; j++) {
+                if (eb + j < e1) {
+                    const Real xl = mode == kModeIter ? projlb<Real>(fma(-alpha, xb[j], xa[j]), xc[j]) : xa[j];
+                    acc = fma(vals[j], xl, acc);
+                }
+            }
         }
-        acc = acc + __ldg(V.cinv + k) * xk;
+        acc = fma(__ldg(V.cinv + k), xk, acc);
         if (mode == kModeAG) {
             v0 = gold * gold;
             v1 = gold * acc;

@@ -140,6 +140,12 @@ void alens_config_default(AlensConfig *cfg);
 /* Text of a status code. */
 const char *alens_status_str(int status);
 
+/* Message of the last failed call on this context (the failing CUDA call
+ * and its error string for ALENS_CUDA_ERROR); "" when none.  The reference
+ * reports such failures through exceptions and spdlog
+ * (SRC/TubuleSystem.cpp:500,642). */
+const char *alens_get_last_error(AlensCtx *ctx);
+
 /* Create a context for one system (replaces SylinderSystem::initialize's
  * configuration part, SRC/TubuleSystem.cpp:79).  Returns ALENS_NO_DEVICE
  * when no CUDA device is usable. */

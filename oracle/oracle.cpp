@@ -188,21 +188,13 @@ void normals6(uint64_t seed, int64_t gid, int64_t step, double z[6]) {
 // ------------------------------------------------------- canonical reduction
 // Level 1: tiles of 64 elements held by two warps; in each warp the tree
 // v[l] = v[l] + v[l+off] for off = 16..1, then tile = warp0 + warp1.
-// Level 2+: chunks of 2048 partials over 256 lanes: lane t adds partials
-// t, t+256, ..., t+1792 in order, warp trees as above, then the 8 warp sums
-// with offsets 4,2,1; repeated until one value remains.
+// Level 2+: chunks of 1024 partials reduced by one warp: lane l adds
+// partials l, l+32, ..., l+992 in order (from 0.0), then the warp tree;
+// repeated until one value remains.
 double warp_tree(double *v) {
     for (int off = 16; off >= 1; off >>= 1)
         for (int l = 0; l < off; l++) v[l] = v[l] + v[l + off];
     return v[0];
-}
-
-double tree256(double *lanes) {
-    double ws[8];
-    for (int w = 0; w < 8; w++) ws[w] = warp_tree(lanes + 32 * w);
-    for (int off = 4; off >= 1; off >>= 1)
-        for (int i = 0; i < off; i++) ws[i] = ws[i] + ws[i + off];
-    return ws[0];
 }
 
 template <class F>
@@ -218,25 +210,25 @@ double tile_sum(F &&val, int64_t base, int64_t n) {
 }
 
 double chunk_sum(const double *T, int64_t base, int64_t m) {
-    double lanes[256];
-    for (int l = 0; l < 256; l++) {
+    double lanes[32];
+    for (int l = 0; l < 32; l++) {
         double acc = 0.0;
-        for (int k = 0; k < 8; k++) {
-            const int64_t i = base + l + 256 * k;
+        for (int j = 0; j < 32; j++) {
+            const int64_t i = base + l + 32 * j;
             if (i < m) acc = acc + T[i];
         }
         lanes[l] = acc;
     }
-    return tree256(lanes);
+    return warp_tree(lanes);
 }
 
 double reduce_partials(std::vector<double> T) {
     int64_t m = (int64_t)T.size();
     if (m == 0) return 0.0;
     while (true) {
-        const int64_t mc = (m + 2047) / 2048;
+        const int64_t mc = (m + 1023) / 1024;
         std::vector<double> R(mc);
-        for (int64_t c = 0; c < mc; c++) R[c] = chunk_sum(T.data(), 2048 * c, m);
+        for (int64_t c = 0; c < mc; c++) R[c] = chunk_sum(T.data(), 1024 * c, m);
         if (mc == 1) return R[0];
         T.swap(R);
         m = mc;
@@ -834,15 +826,16 @@ void build_delassus(OrcCtx *x) {
     }
 }
 
-// y_k = sum_l A_kl x_l (ascending l) + cinv_k x_k  (+ q_k when withQ)
+// y_k = sum_l A_kl x_l (ascending l, fused multiply-adds) + cinv_k x_k
+// (+ q_k when withQ)
 void spmv_A(OrcCtx *x, const std::vector<double> &xin, std::vector<double> &y, bool withQ) {
     const int nc = x->ncoll + x->nbil;
     y.assign(nc, 0.0);
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < nc; k++) {
         double v = 0.0;
-        for (int64_t e = x->aptr[k]; e < x->aptr[k + 1]; e++) v = v + x->aval[e] * xin[x->acol[e]];
-        v = v + x->cinv[k] * xin[k];
+        for (int64_t e = x->aptr[k]; e < x->aptr[k + 1]; e++) v = std::fma(x->aval[e], xin[x->acol[e]], v);
+        v = std::fma(x->cinv[k], xin[k], v);
         if (withQ) v = v + x->q[k];
         y[k] = v;
     }
@@ -896,7 +889,7 @@ int solve_bbpgd(OrcCtx *x, AlensStepStats *st) {
     for (it = 1; it <= x->cfg.conMaxIte; it++) {
 #pragma omp parallel for schedule(static)
         for (int k = 0; k < nc; k++)
-            gamn[k] = proj(gam[k] - alpha * g[k], x->unil[k], x->lb[k]);
+            gamn[k] = proj(std::fma(-alpha, g[k], gam[k]), x->unil[k], x->lb[k]);
         spmv_A(x, gamn, gn, true);
         const double ss = canon_sum_f(
             [&](int64_t k) { const double s = gamn[k] - gam[k]; return s * s; }, nc);

@@ -129,14 +129,6 @@ def _warp(v):
     return v[0]
 
 
-def _tree256(lanes):
-    ws = [_warp(lanes[32 * w:32 * w + 32]) for w in range(8)]
-    for off in (4, 2, 1):
-        for i in range(off):
-            ws[i] = ws[i] + ws[i + off]
-    return ws[0]
-
-
 def _canon_py(v):
     v = [float(x) for x in v]
     n = len(v)
@@ -149,16 +141,16 @@ def _canon_py(v):
     while True:
         m = len(T)
         R = []
-        for c in range(0, m, 2048):
+        for c in range(0, m, 1024):
             lanes = []
-            for l in range(256):
+            for l in range(32):
                 acc = 0.0
-                for k in range(8):
-                    i = c + l + 256 * k
+                for j in range(32):
+                    i = c + l + 32 * j
                     if i < m:
                         acc = acc + T[i]
                 lanes.append(acc)
-            R.append(_tree256(lanes))
+            R.append(_warp(lanes))
         if len(R) == 1:
             return R[0]
         T = R
