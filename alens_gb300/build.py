@@ -84,6 +84,9 @@ def _compile_cu(src: str) -> Path:
         flags.insert(3, "--fmad=false")
     if os.environ.get("ALENS_PTXAS_VERBOSE"):
         flags += ["-Xptxas", "-v"]
+    extra = os.environ.get("ALENS_NVCC_FLAGS", "").split()
+    if extra:
+        flags += extra
     _run(flags)
     return obj
 

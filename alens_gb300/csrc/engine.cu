@@ -63,6 +63,9 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     fixedCap_ = cfg_[0].maxConstraints;
     stageTiming_ = cfg_[0].stageTiming != 0;
     if (const char *e = std::getenv("ALENS_SOLVER_BLOCKS_PER_SM")) solverBlocksPerSM_ = std::max(1, atoi(e));
+    // FP32 solver form: -1 = cluster form with the largest cluster size,
+    // 0 = grid form, N = cluster form with clusters of N CTAs
+    if (const char *e = std::getenv("ALENS_CLUSTER_SIZE")) clusterSize_ = atoi(e);
     CK(cudaMallocHost(&hCtl_, sizeof(DevCtl)));
     CK(cudaMallocHost(&hDyn_, sizeof(RepDyn) * R_));
     CK(cudaMallocHost(&hBilPrefix_, sizeof(int) * (R_ + 1)));
@@ -279,6 +282,8 @@ void Engine::finalize() {
         CK(cudaMemcpy(S.imm, ibuf.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S.rodRep, rbuf.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     }
+    launch_mobility(S, stream_);
+    CK(cudaGetLastError());
     // constraints
     int want = fixedCap_ > 0 ? fixedCap_ : std::max(4096, 4 * N + 1024);
     nnzCap_ = 0;
@@ -311,15 +316,20 @@ void Engine::allocConstraints(int cap, bool keepPrev) {
     S.conImg = alloc<int>(G, cap);
     S.jac = alloc<double>(G, 12 * (size_t)cap);
     S.W = alloc<double>(G, 12 * (size_t)cap);
-    double **cd[] = {&S.phi0, &S.q, &S.gamma, &S.lb, &S.cinv, &S.sgam[0], &S.sgam[1], &S.sg[0], &S.sg[1]};
+    double **cd[] = {&S.phi0, &S.q, &S.gamma, &S.lb, &S.cinv};
     for (double **p : cd) *p = alloc<double>(G, cap);
+    S.lbKind = alloc<int>(G, cap);
+    S.qc = alloc<double2>(G, cap);
+    S.st[0] = alloc<double2>(G, cap);
+    S.st[1] = alloc<double2>(G, cap);
     S.lab = alloc<double>(G, 6 * (size_t)cap);
     S.rowEnt = alloc<int>(G, 2 * (size_t)cap);
     S.annz = alloc<int>(G, cap);
     S.aptr = alloc<int>(G, cap + 1);
     if (precision_ == ALENS_PREC_MIXED) {
-        float **fd[] = {&S.q32, &S.lb32, &S.cinv32, &S.sgam32[0], &S.sgam32[1], &S.sg32[0], &S.sg32[1]};
-        for (float **p : fd) *p = alloc<float>(G, cap);
+        S.qc32 = alloc<float2>(G, cap);
+        S.st32[0] = alloc<float2>(G, cap);
+        S.st32[1] = alloc<float2>(G, cap);
     }
     S.part = alloc<double>(G, 9 * (size_t)S.tileCap);
     S.work = alloc<double>(G, (size_t)kMaxSolverGrid * 3 * S.workCap);
@@ -339,9 +349,8 @@ void Engine::allocOperator(long long nnz) {
     freeGroup(opAllocs_);
     nnzCap_ = nnz;
     S_.nnzCap = (int)nnz;
-    S_.acol = alloc<int>(opAllocs_, (size_t)nnz);
-    S_.aval = alloc<double>(opAllocs_, (size_t)nnz);
-    S_.aval32 = precision_ == ALENS_PREC_MIXED ? alloc<float>(opAllocs_, (size_t)nnz) : nullptr;
+    S_.aent = alloc<int4>(opAllocs_, (size_t)nnz);
+    S_.aent32 = precision_ == ALENS_PREC_MIXED ? alloc<int4>(opAllocs_, (size_t)nnz) : nullptr;
 }
 
 void Engine::updateRods(int rep, int n, const double *pos, const double *quat) {
@@ -447,6 +456,7 @@ int Engine::enqueueDetect() {
     CK(cudaMemsetAsync(S.cellCount, 0, sizeof(int) * S.nCells, stream_));
     CK(cudaMemsetAsync(S.cellCursor, 0, sizeof(int) * S.nCells, stream_));
     CK(cudaMemsetAsync(S.pairCursor, 0, sizeof(int) * S.nRods, stream_));
+    CK(cudaMemsetAsync(S.pairCount, 0, sizeof(int) * S.nRods, stream_));
     CK(cudaMemsetAsync(S.rowCount, 0, sizeof(int) * S.nRods, stream_));
     CK(cudaMemsetAsync(S.rowCursor, 0, sizeof(int) * S.nRods, stream_));
     launch_prep(S, stream_);
@@ -471,12 +481,24 @@ void Engine::ensureSolverGrid() {
     const int maxg = solver_max_grid(precision_);
     solverGrid_ = std::min(maxg, numSM_ * solverBlocksPerSM_);
     if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "solver occupancy");
+    if (precision_ == ALENS_PREC_MIXED && clusterSize_ != 0) {
+        const int maxCs = cluster_max_size();
+        int cs = clusterSize_ > 0 ? std::min(clusterSize_, maxCs) : maxCs;
+        // ensembles: one cluster per replica, at most the co-resident count
+        if (R_ > 1) {
+            while (cs > 1 && cluster_max_active(cs) < R_) cs /= 2;
+        }
+        const int act = cluster_max_active(cs);
+        clusterSize_ = cs;
+        nClusters_ = std::max(1, std::min(R_, act > 0 ? act : 1));
+    }
 }
 
 int Engine::enqueueSolve(cudaEvent_t *ev) {
     ensureSolverGrid();
     int n = 0;
-    CK(launch_solve(S_, solverGrid_, precision_, kBarrierTimeoutNs, stream_, ev, &n));
+    CK(launch_solve(S_, solverGrid_, precision_, kBarrierTimeoutNs, stream_, ev, &n,
+                    clusterSize_ > 0 ? clusterSize_ : 0, nClusters_));
     return n;
 }
 

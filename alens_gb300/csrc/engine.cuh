@@ -50,6 +50,8 @@ struct RepDyn {
     int iter, active, converged, status;
     int counter;              // last-arriver ticket of the current pass
     int refineIter;
+    int finalPar;             // solver buffer holding this replica's result
+    int pad;
     double alpha, res;
 };
 
@@ -92,15 +94,17 @@ struct DevState {
     int *conI, *conJ, *conImg;
     double *jac;
     double *phi0, *q, *gamma, *lb, *cinv, *lab;
-    float *q32, *lb32, *cinv32;
-    double *sgam[2], *sg[2];   // solver iterates by pass parity (FP64)
-    float *sgam32[2], *sg32[2];
+    int *lbKind;               // 0: lb = 0, 1: bilateral, 2: general lb
+    double2 *qc;               // (q, cinv) FP64
+    float2 *qc32;              // (q, cinv) FP32
+    double2 *st[2];            // solver iterates (gamma, g) by pass parity
+    float2 *st32[2];
     double *alphaBuf;          // 2 x R step sizes by pass parity
     // Delassus operator A = dt D^T M D (rows ascending in column)
     double *W;                 // 12 x cap: M J per constraint side
-    int *annz, *aptr, *acol;
-    double *aval;
-    float *aval32;
+    int *annz, *aptr;
+    int4 *aent;                // {col, kind, lo(val), hi(val)}
+    int4 *aent32;              // {col, kind, bits(val32), bits(lb32)}
     int *rowCount, *rowPtr, *rowCursor, *rowEnt;
     unsigned long long *prevKeys;
     double *prevGamma;
@@ -118,6 +122,7 @@ struct DevState {
 
 // ---- detect stage (kernels_detect.cu)
 void launch_prep(const DevState &S, cudaStream_t st);
+void launch_mobility(const DevState &S, cudaStream_t st);  // once per rod set
 int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st);  // returns kernels launched
 void launch_scatter(const DevState &S, cudaStream_t st);
 void launch_pairs(const DevState &S, cudaStream_t st);
@@ -135,8 +140,11 @@ constexpr int kMaxSolverGrid = 152 * 8;  // work space is sized for this
 int solver_max_grid(int precision);  // cooperative residency limit
 // precision == MIXED: FP32 kernel, state reset, FP64 refinement kernel
 // (events ev[0..3] recorded around the two kernels when non-null).
+// clusterSize > 0 selects the cluster form of the FP32 solver.
 cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned long long timeout_ns,
-                         cudaStream_t st, cudaEvent_t *ev, int *launches);
+                         cudaStream_t st, cudaEvent_t *ev, int *launches, int clusterSize, int nClusters);
+int cluster_max_size();            // largest cluster the FP32 solver can use
+int cluster_max_active(int cs);    // co-resident clusters of that size
 void launch_advance(const DevState &S, cudaStream_t st);
 void launch_stress(const DevState &S, cudaStream_t st);
 

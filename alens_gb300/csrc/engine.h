@@ -90,6 +90,8 @@ class Engine {
     bool useGraph_ = true, graphFailed_ = false;
     int fixedCap_ = 0;
     int solverBlocksPerSM_ = 1;
+    int clusterSize_ = -1;   // FP32 solver: -1 largest cluster, 0 grid form
+    int nClusters_ = 1;
     int prevCountHost_ = 0;  // valid warm-start keys on the device
     int solverGrid_ = 0;
     std::vector<HostRods> rods_;

@@ -76,9 +76,10 @@ __device__ int merge_row(const DevState &S, int k, int out0) {
         if (fill) {
             const int o = out0 + cnt;
             const double v = dt * acc;
-            S.acol[o] = l;
-            S.aval[o] = v;
-            if (S.precision == ALENS_PREC_MIXED) S.aval32[o] = (float)v;
+            const int kind = S.lbKind[l];
+            S.aent[o] = make_int4(l, kind, __double2loint(v), __double2hiint(v));
+            if (S.precision == ALENS_PREC_MIXED)
+                S.aent32[o] = make_int4(l, kind, __float_as_int((float)v), __float_as_int((float)S.lb[l]));
         }
         cnt++;
     }

@@ -67,12 +67,8 @@ __global__ void k_prep(DevState S) {
         S.sph[r] = sphere ? 1 : 0;
         S.hcol[r] = sphere ? 0.0 : 0.5 * (L * P.colRatioL);
         S.rcol[r] = rad * P.colRatioD;
-        double m[3] = {0.0, 0.0, 0.0};
         const bool imm = S.imm[r] != 0;
-        if (!imm) mobility_coeffs(L, rad, P.mu, sphere, m);
-        S.m0[r] = m[0];
-        S.m1[r] = m[1];
-        S.m2[r] = m[2];
+        const double m[3] = {S.m0[r], S.m1[r], S.m2[r]};
         double u[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         if (P.kT > 0.0 && !imm) {
             const double bc = sqrt(2.0 * P.kT / P.dt);
@@ -119,6 +115,19 @@ __global__ void k_prep(DevState S) {
         const int cid = P.cellOffset + (cz * P.ncell[1] + cy) * P.ncell[0] + cx;
         S.cellOf[r] = cid;
         atomicAdd(&S.cellCount[cid], 1);
+    }
+}
+
+// Drag mobilities depend only on the rod geometry: computed once per rod set.
+__global__ void k_mobility(DevState S) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
+        const RepParams &P = S.par[S.rodRep[r]];
+        const double L = S.len[r], rad = S.rad[r];
+        double m[3] = {0.0, 0.0, 0.0};
+        if (!S.imm[r]) mobility_coeffs(L, rad, P.mu, L < 2.0 * rad, m);
+        S.m0[r] = m[0];
+        S.m1[r] = m[1];
+        S.m2[r] = m[2];
     }
 }
 
@@ -294,93 +303,79 @@ __device__ __noinline__ bool exact_pair(const DevState &S, int i, int j, const R
     return sep < P.colBuf;
 }
 
-// One thread per cell-sorted slot; the warp walks neighbour cells mostly in
-// lockstep, so candidate loads are broadcasts.  FP32 screen, FP64 decision
-// only within the screening margin.
+// One thread per (neighbour cell, cell-sorted slot) item, slot-fastest: the
+// lanes of a warp hold consecutive rods of (mostly) one home cell looking
+// at the same neighbour offset, so candidate loads are broadcasts.  FP32
+// screen, FP64 decision only within the screening margin.
 __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = t < S.nRods && !(flags(S) & kErrNaN);
+    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nb27 = 27;
+    const bool valid = item < (long long)nb27 * S.nRods && !(flags(S) & kErrNaN);
     unsigned long long buf[kPairBuf];
     int nb = 0;
     if (valid) {
-        int cnt = 0;
+        const int t = (int)(item % S.nRods);
+        const int nbr = (int)(item / S.nRods);
+        const int ox = nbr % 3 - 1, oy = (nbr / 3) % 3 - 1, oz = nbr / 9 - 1;
         const int i = S.sidx[t];
         const RepParams &P = S.par[S.rodRep[i]];
-        const float4 Ai = S.sA[t], Bi = S.sB[t];
-        const float3 ci = make_float3(Ai.x, Ai.y, Ai.z);
-        const float3 ui = make_float3(Bi.x, Bi.y, Bi.z);
-        const float hi_ = Ai.w, ri = Bi.w;
-        const float colBuf = (float)P.colBuf;
-        const float cutLo = colBuf - kScreenMargin, cutHi = colBuf + kScreenMargin;
         const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
-        const float csx = (float)P.cellsz[0], csy = (float)P.cellsz[1], csz = (float)P.cellsz[2];
         const int lc = S.cellOf[i] - P.cellOffset;
         const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
-        for (int oz = -1; oz <= 1; oz++) {
-            int z = cz + oz, sz = 0;
-            if (z < 0 || z >= nz) {
-                if (!P.pbc[2]) continue;
-                if (z < 0) {
-                    z += nz;
-                    sz = -1;
-                } else {
-                    z -= nz;
-                    sz = 1;
+        int xx = cx + ox, y = cy + oy, z = cz + oz;
+        int sx = 0, sy = 0, sz = 0;
+        bool ok = true;
+        if (xx < 0 || xx >= nx) {
+            if (!P.pbc[0]) ok = false;
+            else if (xx < 0) { xx += nx; sx = -1; }
+            else { xx -= nx; sx = 1; }
+        }
+        if (y < 0 || y >= ny) {
+            if (!P.pbc[1]) ok = false;
+            else if (y < 0) { y += ny; sy = -1; }
+            else { y -= ny; sy = 1; }
+        }
+        if (z < 0 || z >= nz) {
+            if (!P.pbc[2]) ok = false;
+            else if (z < 0) { z += nz; sz = -1; }
+            else { z -= nz; sz = 1; }
+        }
+        int cnt = 0;
+        if (ok) {
+            const float4 Ai = S.sA[t], Bi = S.sB[t];
+            const float3 ci = make_float3(Ai.x, Ai.y, Ai.z);
+            const float3 ui = make_float3(Bi.x, Bi.y, Bi.z);
+            const float hi_ = Ai.w, ri = Bi.w;
+            const float colBuf = (float)P.colBuf;
+            const float cutLo = colBuf - kScreenMargin, cutHi = colBuf + kScreenMargin;
+            const int img = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
+            // the neighbour cell's origin relative to ours
+            const float3 off = make_float3((float)ox * (float)P.cellsz[0], (float)oy * (float)P.cellsz[1],
+                                           (float)oz * (float)P.cellsz[2]);
+            const int cell = P.cellOffset + (z * ny + y) * nx + xx;
+            const int m1 = S.cellStart[cell + 1];
+            for (int m = S.cellStart[cell]; m < m1; m++) {
+                const int j = S.sidx[m];
+                if (j < i) continue;
+                if (j == i && img <= kImageNone) continue;
+                const float4 Aj = S.sA[m];
+                const float3 cj = make_float3(Aj.x + off.x, Aj.y + off.y, Aj.z + off.z);
+                const float d0 = ci.x - cj.x, d1 = ci.y - cj.y, d2 = ci.z - cj.z;
+                const float4 Bj = S.sB[m];
+                const float lim = hi_ + Aj.w + ri + Bj.w + cutHi;
+                if (d0 * d0 + d1 * d1 + d2 * d2 > lim * lim) continue;
+                const float sep = dcp_dist32(ci, ui, hi_, cj, make_float3(Bj.x, Bj.y, Bj.z), Aj.w) - ri - Bj.w;
+                if (sep >= cutHi) continue;
+                if (sep >= cutLo && !exact_pair(S, i, j, P, sx, sy, sz)) continue;
+                if (nb == kPairBuf) {
+                    flush_keys(S, buf, nb);
+                    nb = 0;
                 }
-            }
-            for (int oy = -1; oy <= 1; oy++) {
-                int y = cy + oy, sy = 0;
-                if (y < 0 || y >= ny) {
-                    if (!P.pbc[1]) continue;
-                    if (y < 0) {
-                        y += ny;
-                        sy = -1;
-                    } else {
-                        y -= ny;
-                        sy = 1;
-                    }
-                }
-                for (int ox = -1; ox <= 1; ox++) {
-                    int xx = cx + ox, sx = 0;
-                    if (xx < 0 || xx >= nx) {
-                        if (!P.pbc[0]) continue;
-                        if (xx < 0) {
-                            xx += nx;
-                            sx = -1;
-                        } else {
-                            xx -= nx;
-                            sx = 1;
-                        }
-                    }
-                    const int img = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
-                    // the neighbour cell's origin relative to ours
-                    const float3 off = make_float3((float)ox * csx, (float)oy * csy, (float)oz * csz);
-                    const int cell = P.cellOffset + (z * ny + y) * nx + xx;
-                    const int m1 = S.cellStart[cell + 1];
-                    for (int m = S.cellStart[cell]; m < m1; m++) {
-                        const int j = S.sidx[m];
-                        if (j < i) continue;
-                        if (j == i && img <= kImageNone) continue;
-                        const float4 Aj = S.sA[m];
-                        const float3 cj = make_float3(Aj.x + off.x, Aj.y + off.y, Aj.z + off.z);
-                        const float d0 = ci.x - cj.x, d1 = ci.y - cj.y, d2 = ci.z - cj.z;
-                        const float4 Bj = S.sB[m];
-                        const float lim = hi_ + Aj.w + ri + Bj.w + cutHi;
-                        if (d0 * d0 + d1 * d1 + d2 * d2 > lim * lim) continue;
-                        const float sep = dcp_dist32(ci, ui, hi_, cj, make_float3(Bj.x, Bj.y, Bj.z), Aj.w) - ri - Bj.w;
-                        if (sep >= cutHi) continue;
-                        if (sep >= cutLo && !exact_pair(S, i, j, P, sx, sy, sz)) continue;
-                        if (nb == kPairBuf) {
-                            flush_keys(S, buf, nb);
-                            nb = 0;
-                        }
-                        buf[nb++] = pair_key(i, j, img);
-                        cnt++;
-                    }
-                }
+                buf[nb++] = pair_key(i, j, img);
+                cnt++;
             }
         }
-        S.pairCount[i] = cnt;
+        if (cnt) atomicAdd(&S.pairCount[i], cnt);
     }
     // warp-aggregated append of the remaining keys
     const int lane = threadIdx.x & 31;
@@ -503,18 +498,18 @@ __device__ void finish_constraint(const DevState &S, int k, const RepParams &P, 
     const double q = phi0 + P.dt * (dI + dJ);
     const double g0 = gamma0 < lb ? lb : gamma0;
     S.q[k] = q;
-    S.sgam[1][k] = g0;  // the solver starts from the parity-1 buffer
+    S.st[1][k] = make_double2(g0, 0.0);  // the solver starts from the parity-1 buffer
+    S.qc[k] = make_double2(q, cinv);
     S.gamma[k] = g0;
     S.lb[k] = lb;
+    S.lbKind[k] = lb == 0.0 ? 0 : (lb == -INFINITY ? 1 : 2);
     S.cinv[k] = cinv;
     S.phi0[k] = phi0;
     atomicAdd(&S.rowCount[I], 1);
     if (J >= 0) atomicAdd(&S.rowCount[J], 1);
     if (S.precision == ALENS_PREC_MIXED) {
-        S.q32[k] = (float)q;
-        S.sgam32[1][k] = (float)g0;
-        S.lb32[k] = (float)lb;
-        S.cinv32[k] = (float)cinv;
+        S.qc32[k] = make_float2((float)q, (float)cinv);
+        S.st32[1][k] = make_float2((float)g0, 0.0f);
     }
 }
 
@@ -689,7 +684,11 @@ int grid_for(int n, int block, int maxBlocks = 4096) {
 }  // namespace
 
 void launch_prep(const DevState &S, cudaStream_t st) {
-    k_prep<<<grid_for(S.nRods, 256), 256, 0, st>>>(S);
+    k_prep<<<grid_for(S.nRods, 64), 64, 0, st>>>(S);
+}
+
+void launch_mobility(const DevState &S, cudaStream_t st) {
+    k_mobility<<<grid_for(S.nRods, 64), 64, 0, st>>>(S);
 }
 
 int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st) {
@@ -705,8 +704,9 @@ void launch_scatter(const DevState &S, cudaStream_t st) {
 }
 
 void launch_pairs(const DevState &S, cudaStream_t st) {
-    const int g = (S.nRods + kPairThreads - 1) / kPairThreads;
-    k_pairs<<<g > 0 ? g : 1, kPairThreads, 0, st>>>(S);
+    const long long items = 27LL * S.nRods;
+    const long long g = (items + kPairThreads - 1) / kPairThreads;
+    k_pairs<<<(unsigned)(g > 0 ? g : 1), kPairThreads, 0, st>>>(S);
 }
 
 int launch_pair_sort(const DevState &S, cudaStream_t st) {

@@ -18,6 +18,7 @@ __device__ __forceinline__ int flags(const DevState &S) { return ld_volatile_i32
 __global__ void k_refine_setup(DevState S) {
     if (flags(S) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
     const int par = S.ctl->finalParity;
+    __syncthreads();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int r = 0; r < S.R; r++) {
             RepDyn &d = S.dyn[r];
@@ -29,11 +30,16 @@ __global__ void k_refine_setup(DevState S) {
             d.res = 0.0;
         }
     }
-    const int nc = S.ctl->totalCon;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) {
-        const double g = (double)S.sgam32[par][k];
-        const double lb = S.lb[k];
-        S.sgam[1][k] = g < lb ? lb : g;
+    (void)par;
+    for (int r = 0; r < S.R; r++) {
+        const RepDyn &d = S.dyn[r];
+        const float2 *src = d.finalPar ? S.st32[1] : S.st32[0];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nCon; i += gridDim.x * blockDim.x) {
+            const int k = d.conStart + i;
+            const double g = (double)src[k].x;
+            const double lb = S.lb[k];
+            S.st[1][k] = make_double2(g < lb ? lb : g, 0.0);
+        }
     }
 }
 
@@ -52,8 +58,9 @@ __global__ void k_solver_finish(DevState S) {
     if (flags(S) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
     const int par = S.ctl->finalParity;
     const int nc = S.ctl->totalCon;
+    const double2 *src = par ? S.st[1] : S.st[0];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x)
-        S.gamma[k] = S.sgam[par][k];
+        S.gamma[k] = src[k].x;
 }
 
 __global__ void k_advance(DevState S) {
@@ -226,6 +233,7 @@ cudaError_t launch_coop(const DevState &S, const SolveView<Real> &V, int grid,
 
 // defined in kernels_mixed.cu
 cudaError_t launch_solve_fp32(const DevState &S, int grid, unsigned long long timeout_ns, cudaStream_t st);
+cudaError_t launch_solve_fp32_cluster(const DevState &S, int clusterSize, int nClusters, cudaStream_t st);
 int solver_max_grid_fp32();
 
 int solver_max_grid(int precision) {
@@ -238,25 +246,22 @@ int solver_max_grid(int precision) {
 }
 
 cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned long long timeout_ns,
-                         cudaStream_t st, cudaEvent_t *ev, int *launches) {
+                         cudaStream_t st, cudaEvent_t *ev, int *launches, int clusterSize, int nClusters) {
     int n = 0;
     cudaError_t e;
     SolveView<double> V{};
     V.aptr = S.aptr;
-    V.acol = S.acol;
-    V.aval = S.aval;
-    V.gam[0] = S.sgam[0];
-    V.gam[1] = S.sgam[1];
-    V.g[0] = S.sg[0];
-    V.g[1] = S.sg[1];
-    V.q = S.q;
-    V.lb = S.lb;
-    V.cinv = S.cinv;
+    V.aent = S.aent;
+    V.st[0] = S.st[0];
+    V.st[1] = S.st[1];
+    V.qc = S.qc;
+    V.lbGeneral = S.lb;
     V.alphaBuf = S.alphaBuf;
     V.fp64 = 1;
     if (ev) cudaEventRecord(ev[0], st);
     if (precision == ALENS_PREC_MIXED) {
-        e = launch_solve_fp32(S, grid, timeout_ns, st);
+        e = clusterSize > 0 ? launch_solve_fp32_cluster(S, clusterSize, nClusters, st)
+                            : launch_solve_fp32(S, grid, timeout_ns, st);
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[1], st);
         k_refine_setup<<<256, 256, 0, st>>>(S);

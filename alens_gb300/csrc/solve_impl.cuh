@@ -29,6 +29,8 @@
 // residual min(g, x - lb) is exact for lb = 0 and bilateral rows.
 #pragma once
 
+#include <cstdio>
+
 #include "engine.cuh"
 
 namespace alens {
@@ -40,15 +42,33 @@ constexpr int kWindow = 64;          // replicas decided per block window
 constexpr int kRowPrefetch = 8;      // row entries loaded together
 
 template <class Real>
+struct Vec2;
+template <>
+struct Vec2<double> {
+    using T = double2;
+};
+template <>
+struct Vec2<float> {
+    using T = float2;
+};
+
+// Packed solver data (one memory request per operator entry and per
+// neighbour):
+//  st[parity][k] = (gamma, g) of constraint k,
+//  qc[k]         = (q, cinv),
+//  aent[e]       = (column, lower-bound kind, value) of row entries:
+//                  FP64 {col, kind, lo32(val), hi32(val)},
+//                  FP32 {col, kind, bits(val), bits(lb)};
+//  lower-bound kind 0: lb = 0 (collisions), 1: bilateral (no bound),
+//  2: general (FP64 value in lbGeneral).
+template <class Real>
 struct SolveView {
+    using V2 = typename Vec2<Real>::T;
     const int *aptr;
-    const int *acol;
-    const Real *aval;
-    Real *gam[2];
-    Real *g[2];
-    const Real *q;
-    const Real *lb;
-    const Real *cinv;
+    const int4 *aent;
+    V2 *st[2];
+    const V2 *qc;
+    const double *lbGeneral;
     double *alphaBuf;   // 2 x R, by pass parity
     int fp64;           // 1: exact oracle arithmetic
 };
@@ -56,77 +76,108 @@ struct SolveView {
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
 __device__ __forceinline__ float ldcg(const float *p) { return __ldcg(p); }
 __device__ __forceinline__ int ldcg(const int *p) { return __ldcg(p); }
+__device__ __forceinline__ double2 ldcg(const double2 *p) { return __ldcg(p); }
+__device__ __forceinline__ float2 ldcg(const float2 *p) { return __ldcg(p); }
+
+template <class Real>
+__device__ __forceinline__ void decode_entry(const int4 &e, const double *lbGeneral, int &col, Real &val, Real &lb);
+
+template <>
+__device__ __forceinline__ void decode_entry<double>(const int4 &e, const double *lbGeneral, int &col, double &val,
+                                                     double &lb) {
+    col = e.x;
+    val = __hiloint2double(e.w, e.z);
+    lb = e.y == 0 ? 0.0 : (e.y == 1 ? -INFINITY : lbGeneral[e.x]);
+}
+
+template <>
+__device__ __forceinline__ void decode_entry<float>(const int4 &e, const double *, int &col, float &val,
+                                                    float &lb) {
+    col = e.x;
+    val = __int_as_float(e.z);
+    lb = __int_as_float(e.w);
+}
 
 template <class Real>
 __device__ __forceinline__ Real projlb(Real v, Real lb) {
     return v < lb ? lb : v;
 }
 
-// Levels >= 2 of the canonical reduction, run by one warp: chunks of 1024
-// partials, lane l adds partials l, l+32, ..., l+992 in order, then the warp
-// tree; chunk sums are kept in shared memory (up to 64 chunks) and reduced
-// the same way until one value remains.  Loads bypass L1 (the partials are
-// written by other SMs).  The max over all partials of kind `maxKind`
-// (-1: none) is returned in *mx (order-free).  Result valid in lane 0.
-template <int NV>
-__device__ void warp_chunk_reduce(const double *const (&src)[NV], int m, double (*chunk)[64],
-                                  double (&out)[NV], const double *maxSrc, double *mx) {
+// Levels >= 2 of the canonical reduction for one kind, run by one warp:
+// chunks of 1024 partials, lane l adds partials l, l+32, ..., l+992 in
+// order, then the warp tree; chunk sums are kept in shared memory (up to 64
+// chunks) and reduced the same way until one value remains.  All loads of a
+// chunk are issued before the adds; they bypass L1 (the partials are
+// written by other SMs).  Result valid in lane 0.
+__device__ inline double warp_chunk_sum(const double *src, int m, double *chunk) {
     const int lane = threadIdx.x & 31;
-    double lmax = -2.0;
     int mc = (m + kChunk - 1) / kChunk;
     for (int c = 0; c < mc; c++) {
-        double acc[NV];
+        double v[32];
 #pragma unroll
-        for (int q = 0; q < NV; q++) acc[q] = 0.0;
-#pragma unroll 4
         for (int j = 0; j < 32; j++) {
             const int i = c * kChunk + lane + 32 * j;
-            if (i < m) {
-#pragma unroll
-                for (int q = 0; q < NV; q++) acc[q] = acc[q] + __ldcg(src[q] + i);
-                if (maxSrc) {
-                    const double v = __ldcg(maxSrc + i);
-                    lmax = v > lmax ? v : lmax;
-                }
-            }
+            v[j] = i < m ? __ldcg(src + i) : 0.0;
         }
+        double acc = 0.0;
 #pragma unroll
-        for (int q = 0; q < NV; q++) {
-            acc[q] = warp_tree_sum_t<double>(acc[q]);
-            if (lane == 0) chunk[q][c] = acc[q];
-        }
+        for (int j = 0; j < 32; j++)
+            if (c * kChunk + lane + 32 * j < m) acc = acc + v[j];
+        acc = warp_tree_sum_t<double>(acc);
+        if (lane == 0) chunk[c] = acc;
     }
     __syncwarp();
     while (mc > 1) {
         const int m2 = mc;
-        mc = (m2 + kChunk - 1) / kChunk;  // == 1 while m2 <= 1024
+        mc = (m2 + kChunk - 1) / kChunk;
         for (int c = 0; c < mc; c++) {
-            double acc[NV];
-#pragma unroll
-            for (int q = 0; q < NV; q++) acc[q] = 0.0;
+            double acc = 0.0;
             for (int j = 0; j < 32; j++) {
                 const int i = c * kChunk + lane + 32 * j;
-                if (i < m2) {
-#pragma unroll
-                    for (int q = 0; q < NV; q++) acc[q] = acc[q] + chunk[q][i];
-                }
+                if (i < m2) acc = acc + chunk[i];
             }
             __syncwarp();
-#pragma unroll
-            for (int q = 0; q < NV; q++) {
-                acc[q] = warp_tree_sum_t<double>(acc[q]);
-                if (lane == 0) chunk[q][c] = acc[q];
-            }
+            acc = warp_tree_sum_t<double>(acc);
+            if (lane == 0) chunk[c] = acc;
             __syncwarp();
         }
     }
+    return m > 0 ? chunk[0] : 0.0;
+}
+
+// Max of m non-negative doubles (or all equal negative markers) through
+// their bit patterns as signed 64-bit integers: no FP64 instructions.
+__device__ __forceinline__ long long warp_max_bits(long long v) {
 #pragma unroll
-    for (int q = 0; q < NV; q++) out[q] = m > 0 ? chunk[q][0] : 0.0;
-    if (mx) *mx = warp_max(lmax);
+    for (int off = 16; off >= 1; off >>= 1) {
+        const long long o = __shfl_down_sync(0xffffffffu, v, off);
+        v = o > v ? o : v;
+    }
+    return v;
+}
+
+__device__ inline double warp_max_of(const double *src, int m) {
+    const int lane = threadIdx.x & 31;
+    long long mx = __double_as_longlong(-2.0);
+    for (int i = lane; i < m; i += 32) {
+        const long long b = __double_as_longlong(__ldcg(src + i));
+        mx = b > mx ? b : mx;
+    }
+    mx = warp_max_bits(mx);
+    return __longlong_as_double(mx);
+}
+
+// Multi-kind form used by the stress sum (one warp does every kind).
+template <int NV>
+__device__ void warp_chunk_reduce(const double *const (&src)[NV], int m, double (*chunk)[64],
+                                  double (&out)[NV], const double *, double *) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) out[q] = warp_chunk_sum(src[q], m, chunk[q]);
 }
 
 struct SolveShared {
     double chunk[3][64];
+    double red[4];
     double alpha[kWindow];
     int mode[kWindow];
     double tileVal[4][2][4];  // [group][warp][kind]
@@ -151,10 +202,19 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
     const int par = (p - 1) & 1;
     const size_t tc = (size_t)S.tileCap;
     const double *base = S.part + (size_t)par * 4 * tc;
-    if (threadIdx.x < 32) {
-        const double *const src[3] = {base + d.tileStart, base + tc + d.tileStart, base + 2 * tc + d.tileStart};
-        double sums[3], mx;
-        warp_chunk_reduce<3>(src, d.nTiles, sh.chunk, sums, base + 3 * tc + d.tileStart, &mx);
+    // warps 0-2: the three dot products, warp 3: the residual max
+    const int warp = threadIdx.x >> 5;
+    if (warp < 3) {
+        const double v = warp_chunk_sum(base + (size_t)warp * tc + d.tileStart, d.nTiles, sh.chunk[warp]);
+        if ((threadIdx.x & 31) == 0) sh.red[warp] = v;
+    } else if (warp == 3) {
+        const double v = warp_max_of(base + 3 * tc + d.tileStart, d.nTiles);
+        if ((threadIdx.x & 31) == 0) sh.red[3] = v;
+    }
+    __syncthreads();
+    {
+        const double sums[3] = {sh.red[0], sh.red[1], sh.red[2]};
+        const double mx = sh.red[3];
         if (threadIdx.x == 0) {
         const bool owner = d.tileStart >= t0 && d.tileStart < t1;
         int mode = kModeCopy;
@@ -217,6 +277,90 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
     __syncthreads();
 }
 
+// Update of constraint k at pass p in `mode`: reads the previous iterates,
+// forms x_k and (A x)_k, writes the new iterates, returns the dot-product
+// terms (v0, v1, v2) and the residual term.  Row k always holds its own
+// diagonal entry, which supplies gamma_k, g_k and the bound of k.
+template <class Real>
+__device__ __forceinline__ void row_update(const SolveView<Real> &V, int k, int mode, Real alpha,
+                                           const typename Vec2<Real>::T *stIn, typename Vec2<Real>::T *stOut,
+                                           Real &v0, Real &v1, Real &v2, Real &rmax, int *errFlags) {
+    using V2 = typename Vec2<Real>::T;
+    if (mode == kModeCopy) {
+        stOut[k] = ldcg(stIn + k);
+        return;
+    }
+    const V2 qc = __ldg(V.qc + k);
+    Real acc = Real(0);
+    Real gam = Real(0), gold = Real(0), lbk = Real(0), xk = Real(0);
+    const int e0 = __ldg(V.aptr + k), e1 = __ldg(V.aptr + k + 1);
+    for (int eb = e0; eb < e1; eb += kRowPrefetch) {
+        int4 ent[kRowPrefetch];
+#pragma unroll
+        for (int j = 0; j < kRowPrefetch; j++)
+            ent[j] = eb + j < e1 ? __ldg(V.aent + eb + j) : make_int4(k, 1, 0, 0);
+        V2 sv[kRowPrefetch];
+#pragma unroll
+        for (int j = 0; j < kRowPrefetch; j++)
+            if (eb + j < e1) sv[j] = ldcg(stIn + ent[j].x);
+#pragma unroll
+        for (int j = 0; j < kRowPrefetch; j++) {
+            if (eb + j < e1) {
+                int l;
+                Real val, lbl;
+                decode_entry<Real>(ent[j], V.lbGeneral, l, val, lbl);
+                Real xl;
+                if (mode == kModeG0)
+                    xl = sv[j].x;
+                else if (mode == kModeAG)
+                    xl = sv[j].y;
+                else
+                    xl = projlb<Real>(fma(-alpha, sv[j].y, sv[j].x), lbl);
+                if (l == k) {
+                    gam = sv[j].x;
+                    gold = sv[j].y;
+                    lbk = lbl;
+                    xk = xl;
+                }
+                acc = fma(val, xl, acc);
+            }
+        }
+    }
+    acc = fma(qc.y, xk, acc);
+    if (mode == kModeAG) {
+        v0 = gold * gold;
+        v1 = gold * acc;
+        V2 o;
+        o.x = gam;
+        o.y = gold;
+        stOut[k] = o;
+        return;
+    }
+    const Real gn = acc + qc.x;
+    if (V.fp64) {
+        rmax = fabs(xk - projlb<Real>(xk - gn, lbk));
+    } else {
+        // x - P(x - g) = min(g, x - lb): exact for lb = 0 and lb = -inf
+        const Real m = gn < xk - lbk ? gn : xk - lbk;
+        rmax = fabs(m);
+    }
+    if (rmax != rmax) {
+        atomicOr(errFlags, kErrNaN);
+        rmax = Real(INFINITY);
+    }
+    if (mode == kModeIter) {
+        const Real s = xk - gam;
+        const Real y = gn - gold;
+        v0 = s * s;
+        v1 = s * y;
+        v2 = y * y;
+    }
+    V2 o;
+    o.x = xk;
+    o.y = gn;
+    stOut[k] = o;
+}
+
 // One 64-constraint tile processed by a 64-thread group (two warps).
 template <class Real>
 __device__ void process_tile(const DevState &S, const SolveView<Real> &V, int p, int T, int mode,
@@ -228,99 +372,24 @@ __device__ void process_tile(const DevState &S, const SolveView<Real> &V, int p,
     const int local = (T - d.tileStart) * kRowTile + lane64;
     const bool valid = local < d.nCon;
     const int k = d.conStart + local;
-    const int inB = (p + 1) & 1, outB = p & 1;
+    // select the ping-pong buffers without indexing the parameter arrays
+    // (a runtime index would copy the view to local memory)
+    const bool odd = (p & 1) != 0;
+    using V2 = typename Vec2<Real>::T;
+    const V2 *const stIn = odd ? V.st[0] : V.st[1];
+    V2 *const stOut = odd ? V.st[1] : V.st[0];
     Real v0 = Real(0), v1 = Real(0), v2 = Real(0);
-    double rmax = 0.0;
-    if (mode == kModeCopy) {
-        rmax = -1.0;
-        if (valid) {
-            V.gam[outB][k] = ldcg(V.gam[inB] + k);
-            V.g[outB][k] = ldcg(V.g[inB] + k);
-        }
-    } else if (valid) {
-        const Real gam = ldcg(V.gam[inB] + k);
-        const Real gold = mode == kModeG0 ? Real(0) : ldcg(V.g[inB] + k);
-        const Real lbk = __ldg(V.lb + k);
-        Real xk;
-        if (mode == kModeG0)
-            xk = gam;
-        else if (mode == kModeAG)
-            xk = gold;
-        else
-            xk = projlb<Real>(fma(-alpha, gold, gam), lbk);
-        // row k of A: columns and values first, then the column iterates,
-        // so that each group of loads is independent
-        Real acc = Real(0);
-        const int e0 = __ldg(V.aptr + k), e1 = __ldg(V.aptr + k + 1);
-        for (int eb = e0; eb < e1; eb += kRowPrefetch) {
-            int cols[kRowPrefetch];
-            Real vals[kRowPrefetch];
-#pragma unroll
-            for (int j = 0; j < kRowPrefetch; j++) {
-                cols[j] = eb + j < e1 ? __ldg(V.acol + eb + j) : k;
-                vals[j] = eb + j < e1 ? __ldg(V.aval + eb + j) : Real(0);
-            }
-            Real xa[kRowPrefetch], xb[kRowPrefetch], xc[kRowPrefetch];
-#pragma unroll
-            for (int j = 0; j < kRowPrefetch; j++) {
-                if (eb + j < e1) {
-                    const int l = cols[j];
-                    if (mode == kModeG0) {
-                        xa[j] = ldcg(V.gam[inB] + l);
-                    } else if (mode == kModeAG) {
-                        xa[j] = ldcg(V.g[inB] + l);
-                    } else {
-                        xa[j] = ldcg(V.gam[inB] + l);
-                        xb[j] = ldcg(V.g[inB] + l);
-                        xc[j] = __ldg(V.lb + l);
-                    }
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < kRowPrefetch; j++) {
-                if (eb + j < e1) {
-                    const Real xl = mode == kModeIter ? projlb<Real>(fma(-alpha, xb[j], xa[j]), xc[j]) : xa[j];
-                    acc = fma(vals[j], xl, acc);
-                }
-            }
-        }
-        acc = fma(__ldg(V.cinv + k), xk, acc);
-        if (mode == kModeAG) {
-            v0 = gold * gold;
-            v1 = gold * acc;
-            V.gam[outB][k] = gam;
-            V.g[outB][k] = gold;
-        } else {
-            const Real gn = acc + __ldg(V.q + k);
-            if (V.fp64) {
-                const double xd = (double)xk;
-                const double gd = (double)gn;
-                rmax = fabs(xd - projlb<double>(xd - gd, (double)lbk));
-            } else {
-                // x - P(x - g) = min(g, x - lb): exact for lb = 0 and lb = -inf
-                const Real m = gn < xk - lbk ? gn : xk - lbk;
-                rmax = fabs((double)m);
-            }
-            if (rmax != rmax) {
-                atomicOr(&S.ctl->errFlags, kErrNaN);
-                rmax = INFINITY;
-            }
-            if (mode == kModeIter) {
-                const Real s = xk - gam;
-                const Real y = gn - gold;
-                v0 = s * s;
-                v1 = s * y;
-                v2 = y * y;
-            }
-            V.gam[outB][k] = xk;
-            V.g[outB][k] = gn;
-        }
+    Real rmax = mode == kModeCopy ? Real(-1) : Real(0);
+    if (valid) row_update<Real>(V, k, mode, alpha, stIn, stOut, v0, v1, v2, rmax, &S.ctl->errFlags);
+    // warp trees in Real (modes that need them), tile = warp0 + warp1 in
+    // FP64; the max through integer bit patterns
+    Real w0 = Real(0), w1 = Real(0), w2 = Real(0);
+    if (mode == kModeAG || mode == kModeIter) {
+        w0 = warp_tree_sum_t<Real>(v0);
+        w1 = warp_tree_sum_t<Real>(v1);
     }
-    // warp trees in Real, tile = warp0 + warp1 in FP64
-    Real w0 = warp_tree_sum_t<Real>(v0);
-    Real w1 = warp_tree_sum_t<Real>(v1);
-    Real w2 = warp_tree_sum_t<Real>(v2);
-    double wm = warp_max(rmax);
+    if (mode == kModeIter) w2 = warp_tree_sum_t<Real>(v2);
+    const double wm = __longlong_as_double(warp_max_bits(__double_as_longlong((double)rmax)));
     if ((threadIdx.x & 31) == 0) {
         sh.tileVal[group][warpInGroup][0] = (double)w0;
         sh.tileVal[group][warpInGroup][1] = (double)w1;
@@ -343,7 +412,14 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
     const size_t tc = (size_t)S.tileCap;
     const int group = threadIdx.x >> 6;
     int lastPass = 0;
+#ifdef ALENS_TRACE
+    unsigned long long trDecide = 0, trTiles = 0, trBar = 0, trT0 = 0, trT1 = 0;
+#endif
     for (int p = 0; p <= maxPass; p++) {
+#ifdef ALENS_TRACE
+        trT0 = global_ns();
+        trT1 = 0;
+#endif
         if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl->activeCnt[(p + 1) % 3] = 0;
         double *partBase = S.part + (size_t)(p & 1) * 4 * tc;
         // replica windows of this block's tile range
@@ -352,6 +428,9 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
             const int rFirst = __ldg(S.tileRep + T);
             const int rLast = min(__ldg(S.tileRep + t1 - 1), rFirst + kWindow - 1);
             for (int r = rFirst; r <= rLast; r++) decide<Real>(S, V, p, r, t0, t1, sh, r - rFirst);
+#ifdef ALENS_TRACE
+            if (trT1 == 0) trT1 = global_ns();
+#endif
             // tiles of the window, four per round
             int Tend = T;
             while (Tend < t1 && __ldg(S.tileRep + Tend) <= rLast) Tend++;
@@ -376,10 +455,29 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
             T = Tend;
         }
         lastPass = p;
+#ifdef ALENS_TRACE
+        const unsigned long long trT2 = global_ns();
+        if (trT1 == 0) trT1 = trT2;
+#endif
         if (!grid_sync(&S.ctl->bar, nb, &S.ctl->errFlags, timeout_ns)) return;
+#ifdef ALENS_TRACE
+        const unsigned long long trT3 = global_ns();
+        trDecide += trT1 - trT0;
+        trTiles += trT2 - trT1;
+        trBar += trT3 - trT2;
+#endif
         if (ldcg(&S.ctl->activeCnt[p % 3]) == 0) break;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl->finalParity = lastPass & 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S.ctl->finalParity = lastPass & 1;
+        for (int r = 0; r < S.R; r++) S.dyn[r].finalPar = lastPass & 1;
+    }
+#ifdef ALENS_TRACE
+    if (threadIdx.x == 0 && (blockIdx.x == 0 || blockIdx.x == gridDim.x / 2 || blockIdx.x == gridDim.x - 1))
+        printf("trace block %d passes %d: decide %.2f us, tiles %.2f us, barrier %.2f us per pass (tiles %d)\n",
+               blockIdx.x, lastPass + 1, 1e-3 * trDecide / (lastPass + 1), 1e-3 * trTiles / (lastPass + 1),
+               1e-3 * trBar / (lastPass + 1), t1 - t0);
+#endif
 }
 
 }  // namespace alens

@@ -47,6 +47,7 @@ def load_oracle(rebuild: bool = True) -> C.CDLL:
         "orc_get_constraints": (C.c_int, [vp, C.c_int, _PI32, _PI32, _PI32, _PD, _PD, _PD]),
         "orc_get_con_stress": (C.c_int, [vp, _PD]),
         "orc_get_step_count": (C.c_int, [vp, _PI64]),
+        "orc_get_solver_data": (C.c_int, [vp, C.c_int, _PD, _PD]),
         "orc_set_threads": (C.c_int, [C.c_int]),
         "orc_dcp": (None, [_PD, _PD, C.c_double, _PD, _PD, C.c_double, _PD, _PD, _PD, _PD, _PD]),
         "orc_log": (C.c_double, [C.c_double]),
@@ -236,3 +237,12 @@ class OracleSystem:
         c = C.c_int64()
         _ck(self.lib.orc_get_step_count(self.h, C.byref(c)), "orc_get_step_count")
         return c.value
+
+    def solver_data(self):
+        """q and diag(A) of the current constraints (after detect)."""
+        nc, nb = self.num_constraints()
+        q = np.empty(nc + nb)
+        d = np.empty(nc + nb)
+        _ck(self.lib.orc_get_solver_data(self.h, nc + nb, _p(q, C.c_double), _p(d, C.c_double)),
+            "orc_get_solver_data")
+        return q, d

@@ -1187,6 +1187,23 @@ int orc_get_con_stress(OrcCtx *x, double *stress9) {
     return ALENS_OK;
 }
 
+int orc_get_solver_data(OrcCtx *x, int cap, double *q, double *diag) {
+    if (!x) return ALENS_INVALID_ARG;
+    const int nc = x->ncoll + x->nbil;
+    if (cap < nc) return ALENS_CAPACITY;
+    if ((int)x->aptr.size() != nc + 1) build_delassus(x);
+    for (int k = 0; k < nc; k++) {
+        if (q) q[k] = x->q[k];
+        if (diag) {
+            double d = 0.0;
+            for (int64_t e = x->aptr[k]; e < x->aptr[k + 1]; e++)
+                if (x->acol[e] == k) d = x->aval[e];
+            diag[k] = d + x->cinv[k];
+        }
+    }
+    return ALENS_OK;
+}
+
 int orc_get_step_count(OrcCtx *x, int64_t *count) {
     if (!x || !count) return ALENS_INVALID_ARG;
     *count = x->step;

@@ -47,6 +47,8 @@ int orc_get_constraints(OrcCtx *ctx, int cap, int32_t *indexI,
 int orc_get_con_stress(OrcCtx *ctx, double *stress9);
 int orc_get_known_velocity(OrcCtx *ctx, int n, double *vel6);
 int orc_get_step_count(OrcCtx *ctx, int64_t *count);
+/* q and diag(A) of the current constraints (after detect). */
+int orc_get_solver_data(OrcCtx *ctx, int cap, double *q, double *diag);
 int orc_set_threads(int nthreads);
 
 /* Building blocks exposed for known-answer tests. */
