@@ -183,11 +183,7 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_num_constraints": (C.c_int, [vp, C.c_int, _PI32, _PI32]),
         "alens_get_constraints": (C.c_int, [vp, C.c_int, C.c_int, _PI32, _PI32, _PI32, _PD, _PD, _PD]),
         "alens_get_con_stress": (C.c_int, [vp, C.c_int, _PD]),
-        "alens_get_step_count": (C.c_int, [vp, _PI64]),
-        "alens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
-        "alens_get_launch_count": (C.c_int, [vp, _PI64]),
-        "alens_get_last_error": (C.c_char_p, [vp]),
-        "alens_get_stage_times": (C.c_int, [vp, _PD]),
+        "alens_get_operator": (C.c_int, [vp, C.c_int, C.c_int, _PI32, _PI32, _PI32, _PD, _PD, _PD, _PD, _PD]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -359,6 +355,28 @@ class GpuSystem:
                                            _p(im, C.c_int32), _p(d0, C.c_double), _p(g, C.c_double),
                                            _p(jac, C.c_double)), "alens_get_constraints")
         return dict(i=ii, j=jj, image=im, delta0=d0, gamma=g, jac=jac, ncoll=nc, nbil=nb)
+
+    def operator(self, replica: int = 0):
+        """Delassus operator of one replica (CSR, local columns) and the QP
+        vectors; gamma0 is the current gamma."""
+        nc, nb = self.num_constraints(replica)
+        n = nc + nb
+        nnz = C.c_int()
+        self._ck(self.lib.alens_get_operator(self.h, replica, 0, C.byref(nnz), None, None, None, None, None,
+                                             None, None), "alens_get_operator")
+        ptr = np.empty(n + 1, np.int32)
+        cols = np.empty(max(nnz.value, 1), np.int32)
+        vals = np.empty(max(nnz.value, 1))
+        q = np.empty(n)
+        cinv = np.empty(n)
+        lb = np.empty(n)
+        g0 = np.empty(n)
+        self._ck(self.lib.alens_get_operator(self.h, replica, cols.shape[0], C.byref(nnz), _p(ptr, C.c_int32),
+                                             _p(cols, C.c_int32), _p(vals, C.c_double), _p(q, C.c_double),
+                                             _p(cinv, C.c_double), _p(lb, C.c_double), _p(g0, C.c_double)),
+                 "alens_get_operator")
+        m = nnz.value
+        return dict(rowPtr=ptr, cols=cols[:m], vals=vals[:m], q=q, cinv=cinv, lb=lb, gamma0=g0)
 
     def con_stress(self, replica: int = 0):
         s = np.empty(9)

@@ -202,6 +202,15 @@ int alens_get_con_stress(AlensCtx *ctx, int replica, double *stress9) {
     });
 }
 
+int alens_get_operator(AlensCtx *ctx, int replica, int capNnz, int *nnz, int32_t *rowPtr, int32_t *cols,
+                       double *vals, double *q, double *cinv, double *lowerBound, double *gamma0) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->getOperator(replica, capNnz, nnz, rowPtr, cols, vals, q, cinv, lowerBound, gamma0);
+        return (int)ALENS_OK;
+    });
+}
+
 int alens_get_step_count(AlensCtx *ctx, int64_t *count) {
     if (!ctx || !count) return ALENS_INVALID_ARG;
     *count = ctx->eng->stepCount();

@@ -756,6 +756,40 @@ void Engine::getConstraints(int rep, int cap, int32_t *ii, int32_t *jj, int32_t 
     }
 }
 
+void Engine::getOperator(int rep, int capNnz, int *nnz, int32_t *rowPtr, int32_t *cols, double *vals,
+                         double *q, double *cinv, double *lowerBound, double *gamma0) {
+    if (rep < 0 || rep >= R_) throw ApiError(ALENS_INVALID_ARG);
+    if (dirty_) throw ApiError(ALENS_NOT_READY);
+    const RepDyn &d = hDyn_[rep];
+    const int n = d.nCon, k0 = d.conStart;
+    std::vector<int> ptr(n + 1);
+    if (n > 0) CK(cudaMemcpy(ptr.data(), S_.aptr + k0, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    else ptr[0] = 0;
+    const int e0 = ptr[0], total = ptr[n] - ptr[0];
+    if (nnz) *nnz = total;
+    if ((cols || vals) && capNnz < total) throw ApiError(ALENS_CAPACITY);
+    if (rowPtr)
+        for (int k = 0; k <= n; k++) rowPtr[k] = ptr[k] - e0;
+    if ((cols || vals) && total > 0) {
+        std::vector<int4> ent(total);
+        CK(cudaMemcpy(ent.data(), S_.aent + e0, sizeof(int4) * total, cudaMemcpyDeviceToHost));
+        for (int e = 0; e < total; e++) {
+            if (cols) cols[e] = ent[e].x - k0;
+            if (vals) {
+                const unsigned long long bits =
+                    ((unsigned long long)(unsigned)ent[e].w << 32) | (unsigned long long)(unsigned)ent[e].z;
+                std::memcpy(&vals[e], &bits, 8);
+            }
+        }
+    }
+    if (n > 0) {
+        if (q) CK(cudaMemcpy(q, S_.q + k0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (cinv) CK(cudaMemcpy(cinv, S_.cinv + k0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (lowerBound) CK(cudaMemcpy(lowerBound, S_.lb + k0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (gamma0) CK(cudaMemcpy(gamma0, S_.gamma + k0, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    }
+}
+
 void Engine::conStress(int rep, double *out9) {
     if (rep < 0 || rep >= R_ || !out9) throw ApiError(ALENS_INVALID_ARG);
     if (dirty_) throw ApiError(ALENS_NOT_READY);

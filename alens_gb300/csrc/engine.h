@@ -44,6 +44,8 @@ class Engine {
     void getConstraints(int rep, int cap, int32_t *ii, int32_t *jj, int32_t *img, double *d0,
                         double *gam, double *jac);
     void conStress(int rep, double *out9);
+    void getOperator(int rep, int capNnz, int *nnz, int32_t *rowPtr, int32_t *cols, double *vals,
+                     double *q, double *cinv, double *lowerBound, double *gamma0);
     long long stepCount() const { return stepCount_; }
     cudaStream_t stream() const { return stream_; }
     long long lastNeeded() const { return lastNeeded_; }

@@ -48,6 +48,7 @@ def load_oracle(rebuild: bool = True) -> C.CDLL:
         "orc_get_con_stress": (C.c_int, [vp, _PD]),
         "orc_get_step_count": (C.c_int, [vp, _PI64]),
         "orc_get_solver_data": (C.c_int, [vp, C.c_int, _PD, _PD]),
+        "orc_get_operator": (C.c_int, [vp, C.c_int, _PI32, _PI32, _PI32, _PD]),
         "orc_set_threads": (C.c_int, [C.c_int]),
         "orc_dcp": (None, [_PD, _PD, C.c_double, _PD, _PD, C.c_double, _PD, _PD, _PD, _PD, _PD]),
         "orc_log": (C.c_double, [C.c_double]),
@@ -237,6 +238,19 @@ class OracleSystem:
         c = C.c_int64()
         _ck(self.lib.orc_get_step_count(self.h, C.byref(c)), "orc_get_step_count")
         return c.value
+
+    def operator(self):
+        """Delassus operator (CSR) of the current constraints."""
+        nc, nb = self.num_constraints()
+        nnz = C.c_int()
+        _ck(self.lib.orc_get_operator(self.h, 0, C.byref(nnz), None, None, None), "orc_get_operator")
+        ptr = np.empty(nc + nb + 1, np.int32)
+        cols = np.empty(max(nnz.value, 1), np.int32)
+        vals = np.empty(max(nnz.value, 1))
+        _ck(self.lib.orc_get_operator(self.h, cols.shape[0], C.byref(nnz), _p(ptr, C.c_int32), _p(cols, C.c_int32),
+                                      _p(vals, C.c_double)), "orc_get_operator")
+        m = nnz.value
+        return dict(rowPtr=ptr, cols=cols[:m], vals=vals[:m])
 
     def solver_data(self):
         """q and diag(A) of the current constraints (after detect)."""

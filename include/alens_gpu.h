@@ -220,6 +220,19 @@ int alens_get_constraints(AlensCtx *ctx, int replica, int cap,
                           int32_t *indexI, int32_t *indexJ, int32_t *image,
                           double *delta0, double *gamma, double *jac);
 
+/* The Delassus operator A = dt D^T M D of one replica after detect (the
+ * operator SimToolbox's ConstraintOperator applies, CMakeLists.txt:111), in
+ * CSR form over the replica's constraints (canonical order, local column
+ * indices), with the vectors of the QP min 1/2 x^T (A + diag(cinv)) x + q^T x,
+ * x >= lowerBound (-inf on bilateral rows).  gamma0 receives the current
+ * gamma: the initial guess after alens_detect, the solution after
+ * alens_solve.  Pass NULL for any output that is not wanted;
+ * *nnz receives the number of nonzeros; ALENS_CAPACITY if capNnz is too
+ * small for cols/vals. */
+int alens_get_operator(AlensCtx *ctx, int replica, int capNnz, int *nnz, int32_t *rowPtr,
+                       int32_t *cols, double *vals, double *q, double *cinv,
+                       double *lowerBound, double *gamma0);
+
 /* Sum over the constraints of one replica of the pair virial
  * gamma * (lab_I - lab_J) (x) n  (3x3 row-major); the role of
  * SylinderSystem::calcConStress (SRC/TubuleSystem.cpp:224). */

@@ -855,7 +855,6 @@ int solve_bbpgd(OrcCtx *x, AlensStepStats *st) {
     st->residual = 0.0;
     st->converged = 1;
     if (nc == 0) return ALENS_OK;
-    build_delassus(x);
     std::vector<double> g, Ag, gn, gamn(nc);
     spmv_A(x, gam, g, true);
     auto residual = [&](const std::vector<double> &gm, const std::vector<double> &gg) {
@@ -1108,6 +1107,7 @@ int orc_detect(OrcCtx *x, AlensStepStats *st) {
     wrap_positions(x);
     rod_prepare(x);
     build_constraints(x);
+    build_delassus(x);
     x->detected = true;
     x->solved = false;
     x->last = AlensStepStats{};
@@ -1191,7 +1191,6 @@ int orc_get_solver_data(OrcCtx *x, int cap, double *q, double *diag) {
     if (!x) return ALENS_INVALID_ARG;
     const int nc = x->ncoll + x->nbil;
     if (cap < nc) return ALENS_CAPACITY;
-    if ((int)x->aptr.size() != nc + 1) build_delassus(x);
     for (int k = 0; k < nc; k++) {
         if (q) q[k] = x->q[k];
         if (diag) {
@@ -1200,6 +1199,22 @@ int orc_get_solver_data(OrcCtx *x, int cap, double *q, double *diag) {
                 if (x->acol[e] == k) d = x->aval[e];
             diag[k] = d + x->cinv[k];
         }
+    }
+    return ALENS_OK;
+}
+
+int orc_get_operator(OrcCtx *x, int capNnz, int *nnz, int32_t *rowPtr, int32_t *cols, double *vals) {
+    if (!x) return ALENS_INVALID_ARG;
+    const int nc = x->ncoll + x->nbil;
+    if (!x->detected && !x->solved) return ALENS_NOT_READY;
+    const int64_t total = x->aptr[nc];
+    if (nnz) *nnz = (int)total;
+    if ((cols || vals) && capNnz < total) return ALENS_CAPACITY;
+    if (rowPtr)
+        for (int k = 0; k <= nc; k++) rowPtr[k] = (int32_t)x->aptr[k];
+    for (int64_t e = 0; e < total; e++) {
+        if (cols) cols[e] = x->acol[e];
+        if (vals) vals[e] = x->aval[e];
     }
     return ALENS_OK;
 }

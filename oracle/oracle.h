@@ -49,6 +49,7 @@ int orc_get_known_velocity(OrcCtx *ctx, int n, double *vel6);
 int orc_get_step_count(OrcCtx *ctx, int64_t *count);
 /* q and diag(A) of the current constraints (after detect). */
 int orc_get_solver_data(OrcCtx *ctx, int cap, double *q, double *diag);
+int orc_get_operator(OrcCtx *ctx, int capNnz, int *nnz, int32_t *rowPtr, int32_t *cols, double *vals);
 int orc_set_threads(int nthreads);
 
 /* Building blocks exposed for known-answer tests. */

@@ -321,3 +321,24 @@ def test_mixed_precision_close_to_fp64(gpu_lib):
     p64, _ = g64.get_rods()
     pmx, _ = gmx.get_rods()
     assert rel_err(pmx, p64) <= 1e-6
+
+
+def test_delassus_operator_bit_exact(gpu_lib):
+    """The assembled operator A = dt D^T M D and the QP vectors equal the
+    oracle's bit for bit (bilateral rows included)."""
+    w = workloads.small_periodic(n=600, box=3.5, seed=8)
+    g, o = pair(w.cfg, w.rods)
+    blocks = make_links(w.rods, 200, 3.5, seed=5)
+    g.add_bilateral(blocks)
+    o.add_bilateral(blocks)
+    g.detect()
+    o.detect()
+    opg = g.operator()
+    opo = o.operator()
+    assert np.array_equal(opg["rowPtr"], opo["rowPtr"])
+    assert np.array_equal(opg["cols"], opo["cols"])
+    assert np.array_equal(opg["vals"], opo["vals"])
+    q, diag = o.solver_data()
+    assert np.array_equal(opg["q"], q)
+    assert np.all(opg["lb"][: opg["q"].shape[0] - len(blocks)] == 0.0)
+    assert np.all(np.isneginf(opg["lb"][-len(blocks):]))
