@@ -184,6 +184,13 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_constraints": (C.c_int, [vp, C.c_int, C.c_int, _PI32, _PI32, _PI32, _PD, _PD, _PD]),
         "alens_get_con_stress": (C.c_int, [vp, C.c_int, _PD]),
         "alens_get_operator": (C.c_int, [vp, C.c_int, C.c_int, _PI32, _PI32, _PI32, _PD, _PD, _PD, _PD, _PD]),
+        "alens_bbpgd_solve_noalloc": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_int, vp,
+                                                C.POINTER(C.c_int), _PD, C.POINTER(C.c_int)]),
+        "alens_get_step_count": (C.c_int, [vp, _PI64]),
+        "alens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
+        "alens_get_launch_count": (C.c_int, [vp, _PI64]),
+        "alens_get_last_error": (C.c_char_p, [vp]),
+        "alens_get_stage_times": (C.c_int, [vp, _PD]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

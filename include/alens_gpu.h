@@ -238,6 +238,30 @@ int alens_get_operator(AlensCtx *ctx, int replica, int capNnz, int *nnz, int32_t
  * SylinderSystem::calcConStress (SRC/TubuleSystem.cpp:224). */
 int alens_get_con_stress(AlensCtx *ctx, int replica, double *stress9);
 
+/* BBPGD solve that allocates no memory, for callers that cannot call
+ * cudaMalloc where they solve (a step recorded into a CUDA graph, or GPU
+ * memory held by a pool or budget the caller must not disturb).  No
+ * counterpart in the reference: SimToolbox's solver allocates its Tpetra
+ * vectors per solve.
+ * Solves min 1/2 x^T (A + diag(cinv)) x + q^T x, x >= lowerBound (-inf for
+ * bilateral rows) with the library's FP64 BBPGD, starting from gamma0; all
+ * array arguments are DEVICE pointers to the caller's memory: A as CSR
+ * (rowPtr[n+1], cols, vals; the layout alens_get_operator returns), q, cinv,
+ * lowerBound, gamma0 and the output gamma (n each).  iterations, residual
+ * and solveStatus (nullable) are host pointers.  stream may be NULL.
+ * Scratch lives in one fixed __device__ array of about 2.1 MB per GPU that
+ * loads the library: n is limited to 65,536 rows (larger: ALENS_INVALID_ARG).
+ * The first call on a device looks up the array's address; make it before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race.  Returns the solve's status (ALENS_OK or ALENS_NOT_CONVERGED) or an
+ * error. */
+int alens_bbpgd_solve_noalloc(int n, const int32_t *rowPtr, const int32_t *cols,
+                              const double *vals, const double *q,
+                              const double *cinv, const double *lowerBound,
+                              const double *gamma0, double *gamma, double tol,
+                              int maxIte, void *stream, int *iterations,
+                              double *residual, int *solveStatus);
+
 /* Steps executed so far (SylinderSystem::getStepCount). */
 int alens_get_step_count(AlensCtx *ctx, int64_t *count);
 
