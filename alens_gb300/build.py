@@ -116,7 +116,7 @@ def build_facade_driver(force: bool = False) -> Path:
     if not force and _newer(out, deps):
         return out
     cxx = os.environ.get("CXX", "g++")
-    _run([cxx, "-O2", "-std=c++17", "-I", str(ROOT / "include"), "-I", str(CSRC / "facade"),
+    _run([cxx, "-O2", "-std=c++17", "-fopenmp", "-Wall", "-I", str(ROOT / "include"), "-I", str(CSRC / "facade"),
           str(src), str(CSRC / "facade" / "SylinderSystem.cpp"),
           "-L", str(LIBDIR), "-lalens_gpu", "-Wl,-rpath," + str(LIBDIR), "-o", str(out)])
     return out

@@ -1,0 +1,356 @@
+// SylinderSystem.cpp - facade over the C ABI (see SylinderSystem.hpp).
+#include "SylinderSystem.hpp"
+
+#include <omp.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
+
+namespace gpu {
+
+namespace {
+
+std::string trim(const std::string &s) {
+    const size_t a = s.find_first_not_of(" \t\r\n");
+    if (a == std::string::npos) return "";
+    const size_t b = s.find_last_not_of(" \t\r\n");
+    return s.substr(a, b - a + 1);
+}
+
+bool parseBool(const std::string &v) {
+    std::string t;
+    for (char c : v) t += (char)std::tolower((unsigned char)c);
+    return t == "true" || t == "1" || t == "yes";
+}
+
+std::vector<std::string> parseList(const std::string &v) {
+    std::vector<std::string> out;
+    const size_t a = v.find('['), b = v.find(']');
+    if (a == std::string::npos || b == std::string::npos) return out;
+    std::stringstream ss(v.substr(a + 1, b - a - 1));
+    std::string item;
+    while (std::getline(ss, item, ',')) out.push_back(trim(item));
+    return out;
+}
+
+// rotation taking +z onto the unit vector d, as an (x,y,z,w) quaternion
+void quatFromDirection(const double d[3], double q[4]) {
+    double x = -d[1], y = d[0], z = 0.0, w = 1.0 + d[2];
+    if (w < 1e-8) {
+        x = 1.0;
+        y = 0.0;
+        z = 0.0;
+        w = 0.0;
+    }
+    const double n = std::sqrt(x * x + y * y + z * z + w * w);
+    q[0] = x / n;
+    q[1] = y / n;
+    q[2] = z / n;
+    q[3] = w / n;
+}
+
+void directionFromQuat(const double q[4], double d[3]) {
+    const double x = q[0], y = q[1], z = q[2], w = q[3];
+    d[0] = 2.0 * (x * z + w * y);
+    d[1] = 2.0 * (y * z - w * x);
+    d[2] = 1.0 - 2.0 * (x * x + y * y);
+}
+
+}  // namespace
+
+bool SylinderConfig::readYaml(const std::string &path, std::string *err) {
+    std::ifstream f(path);
+    if (!f) {
+        if (err) *err = "cannot open " + path;
+        return false;
+    }
+    std::string line;
+    while (std::getline(f, line)) {
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line = line.substr(0, hash);
+        if (line.empty() || line[0] == ' ' || line[0] == '\t' || line[0] == '-') continue;  // nested
+        const size_t colon = line.find(':');
+        if (colon == std::string::npos) continue;
+        const std::string key = trim(line.substr(0, colon));
+        const std::string val = trim(line.substr(colon + 1));
+        if (val.empty()) continue;
+        auto vec3 = [&](double *dst) {
+            auto items = parseList(val);
+            for (int d = 0; d < 3 && d < (int)items.size(); d++) dst[d] = std::stod(items[d]);
+        };
+        if (key == "rngSeed") rngSeed = std::stoull(val);
+        else if (key == "simBoxLow") vec3(simBoxLow);
+        else if (key == "simBoxHigh") vec3(simBoxHigh);
+        else if (key == "simBoxPBC") {
+            auto items = parseList(val);
+            for (int d = 0; d < 3 && d < (int)items.size(); d++) simBoxPBC[d] = parseBool(items[d]);
+        } else if (key == "monolayer") monolayer = parseBool(val);
+        else if (key == "viscosity") viscosity = std::stod(val);
+        else if (key == "KBT") KBT = std::stod(val);
+        else if (key == "linkKappa") linkKappa = std::stod(val);
+        else if (key == "sylinderDiameter") sylinderDiameter = std::stod(val);
+        else if (key == "sylinderDiameterColRatio") sylinderDiameterColRatio = std::stod(val);
+        else if (key == "sylinderLengthColRatio") sylinderLengthColRatio = std::stod(val);
+        else if (key == "sylinderColBuf") sylinderColBuf = std::stod(val);
+        else if (key == "dt") dt = std::stod(val);
+        else if (key == "timeTotal") timeTotal = std::stod(val);
+        else if (key == "timeSnap") timeSnap = std::stod(val);
+        else if (key == "conResTol") conResTol = std::stod(val);
+        else if (key == "conMaxIte") conMaxIte = (int)std::min(std::stod(val), 2.0e9);
+        else if (key == "conSolverChoice") conSolverChoice = std::stoi(val);
+    }
+    return true;
+}
+
+AlensConfig SylinderConfig::toAlens() const {
+    AlensConfig c;
+    alens_config_default(&c);
+    for (int d = 0; d < 3; d++) {
+        c.simBoxLow[d] = simBoxLow[d];
+        c.simBoxHigh[d] = simBoxHigh[d];
+        c.simBoxPBC[d] = simBoxPBC[d] ? 1 : 0;
+    }
+    c.monolayer = monolayer ? 1 : 0;
+    c.viscosity = viscosity;
+    c.KBT = KBT;
+    c.dt = dt;
+    c.sylinderDiameterColRatio = sylinderDiameterColRatio;
+    c.sylinderLengthColRatio = sylinderLengthColRatio;
+    c.sylinderColBuf = sylinderColBuf;
+    c.conResTol = conResTol;
+    c.conMaxIte = conMaxIte;
+    c.conSolverChoice = conSolverChoice;
+    c.rngSeed = rngSeed;
+    return c;
+}
+
+ConstraintBlock::ConstraintBlock(double delta0, double gamma, int64_t gidI, int64_t gidJ, int globalIndexI,
+                                 int globalIndexJ, const double normI[3], const double normJ[3],
+                                 const double posI[3], const double posJ[3], const double labI[3],
+                                 const double labJ[3], bool oneSide, bool bilateral, double kappa,
+                                 double gammaLB) {
+    std::memset(&blk, 0, sizeof(blk));
+    blk.delta0 = delta0;
+    blk.gamma = gamma;
+    blk.gidI = gidI;
+    blk.gidJ = gidJ;
+    blk.globalIndexI = globalIndexI;
+    blk.globalIndexJ = globalIndexJ;
+    for (int d = 0; d < 3; d++) {
+        blk.normI[d] = normI[d];
+        blk.normJ[d] = normJ[d];
+        blk.posI[d] = posI[d];
+        blk.posJ[d] = posJ[d];
+        blk.labI[d] = labI[d];
+        blk.labJ[d] = labJ[d];
+    }
+    blk.oneSide = oneSide ? 1 : 0;
+    blk.bilateral = bilateral ? 1 : 0;
+    blk.kappa = kappa;
+    blk.gammaLB = gammaLB;
+}
+
+void ConstraintBlock::setStress(const double stress9[9]) {
+    for (int i = 0; i < 9; i++) blk.stress[i] = stress9[i];
+}
+
+std::vector<Sylinder> readSylinderAscii(const std::string &path, std::vector<std::array<int64_t, 2>> *links,
+                                        std::string *err) {
+    std::vector<Sylinder> rods;
+    std::ifstream f(path);
+    if (!f) {
+        if (err) *err = "cannot open " + path;
+        return rods;
+    }
+    std::string line;
+    while (std::getline(f, line)) {
+        std::stringstream ss(line);
+        std::string type;
+        if (!(ss >> type)) continue;
+        if (type == "L") {
+            int64_t a, b;
+            if ((ss >> a >> b) && links) links->push_back({a, b});
+            continue;
+        }
+        if (type != "C" && type != "S") continue;
+        Sylinder s;
+        double m[3], p[3];
+        if (!(ss >> s.gid >> s.radius >> m[0] >> m[1] >> m[2] >> p[0] >> p[1] >> p[2])) continue;
+        if (!(ss >> s.group)) s.group = -1;
+        s.isImmovable = type == "S";
+        double d[3] = {p[0] - m[0], p[1] - m[1], p[2] - m[2]};
+        s.length = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int k = 0; k < 3; k++) s.pos[k] = 0.5 * (m[k] + p[k]);
+        if (s.length > 0) {
+            for (int k = 0; k < 3; k++) d[k] /= s.length;
+        } else {
+            d[0] = 0;
+            d[1] = 0;
+            d[2] = 1;
+        }
+        quatFromDirection(d, s.orientation);
+        s.globalIndex = (int)rods.size();
+        rods.push_back(s);
+    }
+    return rods;
+}
+
+SylinderSystem::~SylinderSystem() {
+    if (ctx_) alens_destroy(ctx_);
+}
+
+void SylinderSystem::check(int rc, const char *where) const {
+    if (rc == ALENS_OK || rc == ALENS_NOT_CONVERGED) return;
+    std::string msg = std::string(where) + ": " + alens_status_str(rc);
+    if (ctx_) msg += std::string(" [") + alens_get_last_error(ctx_) + "]";
+    throw std::runtime_error(msg);
+}
+
+void SylinderSystem::create() {
+    if (ctx_) alens_destroy(ctx_);
+    ctx_ = nullptr;
+    const AlensConfig c = runConfig.toAlens();
+    check(alens_create(&c, &ctx_), "alens_create");
+    const int n = (int)rods_.size();
+    std::vector<int64_t> gid(n);
+    std::vector<double> pos(3 * (size_t)n), quat(4 * (size_t)n), len(n), rad(n);
+    std::vector<int32_t> imm(n);
+    for (int i = 0; i < n; i++) {
+        gid[i] = rods_[i].gid;
+        for (int d = 0; d < 3; d++) pos[3 * i + d] = rods_[i].pos[d];
+        for (int d = 0; d < 4; d++) quat[4 * i + d] = rods_[i].orientation[d];
+        len[i] = rods_[i].length;
+        rad[i] = rods_[i].radius;
+        imm[i] = rods_[i].isImmovable ? 1 : 0;
+    }
+    check(alens_set_rods(ctx_, 0, n, gid.data(), pos.data(), quat.data(), len.data(), rad.data(), imm.data()),
+          "alens_set_rods");
+    conPool_.assign(std::max(1, omp_get_max_threads()), ConstraintBlockQue());
+    rodsStale_ = false;
+}
+
+void SylinderSystem::initialize(const std::string &configFile, const std::string &posFile, int, char **) {
+    std::string err;
+    if (!runConfig.readYaml(configFile, &err)) throw std::runtime_error(err);
+    rods_ = readSylinderAscii(posFile, nullptr, &err);
+    if (rods_.empty() && !err.empty()) throw std::runtime_error(err);
+    create();
+}
+
+void SylinderSystem::reinitialize(const std::string &configFile, const std::string &restartFile, int argc,
+                                  char **argv, bool) {
+    initialize(configFile, restartFile, argc, argv);
+}
+
+void SylinderSystem::initialize(const SylinderConfig &cfg, const std::vector<Sylinder> &rods) {
+    runConfig = cfg;
+    rods_ = rods;
+    for (size_t i = 0; i < rods_.size(); i++) rods_[i].globalIndex = (int)i;
+    create();
+}
+
+void SylinderSystem::prepareStep() {}
+
+void SylinderSystem::flushPool() {
+    std::vector<AlensBlock> all;
+    for (auto &q : conPool_) {
+        for (auto &b : q) all.push_back(b.blk);
+        q.clear();
+    }
+    if (!all.empty()) check(alens_add_bilateral(ctx_, 0, (int)all.size(), all.data()), "alens_add_bilateral");
+}
+
+void SylinderSystem::runStep() {
+    if (!ctx_) throw std::runtime_error("SylinderSystem::runStep before initialize");
+    flushPool();
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = alens_step(ctx_, &stats_);
+    lastStepMs_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    check(rc, "alens_step");
+    rodsStale_ = true;
+}
+
+void SylinderSystem::stepEuler() {
+    // a solve prepared through the staged C ABI (alens_detect/alens_solve)
+    // is applied; without one there is nothing to move
+    if (!ctx_) return;
+    AlensStepStats st;
+    const int rc = alens_advance(ctx_, &st);
+    if (rc == ALENS_NOT_READY) return;
+    check(rc, "alens_advance");
+    rodsStale_ = true;
+}
+
+void SylinderSystem::calcConStress() {
+    if (!ctx_) return;
+    check(alens_get_con_stress(ctx_, 0, stress_.data()), "alens_get_con_stress");
+}
+
+void SylinderSystem::calcOrderParameter() {
+    const auto &rods = getContainer();
+    polar_ = {0, 0, 0};
+    nematic_ = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (rods.empty()) return;
+    for (const auto &r : rods) {
+        double d[3];
+        directionFromQuat(r.orientation, d);
+        for (int a = 0; a < 3; a++) {
+            polar_[a] += d[a];
+            for (int b = 0; b < 3; b++) nematic_[3 * a + b] += d[a] * d[b] - (a == b ? 1.0 / 3.0 : 0.0);
+        }
+    }
+    const double inv = 1.0 / (double)rods.size();
+    for (auto &v : polar_) v *= inv;
+    for (auto &v : nematic_) v *= inv;
+}
+
+const std::vector<Sylinder> &SylinderSystem::getContainer() {
+    if (ctx_ && rodsStale_) {
+        const int n = (int)rods_.size();
+        std::vector<double> pos(3 * (size_t)n), quat(4 * (size_t)n);
+        check(alens_get_rods(ctx_, 0, n, pos.data(), quat.data()), "alens_get_rods");
+        for (int i = 0; i < n; i++) {
+            for (int d = 0; d < 3; d++) rods_[i].pos[d] = pos[3 * i + d];
+            for (int d = 0; d < 4; d++) rods_[i].orientation[d] = quat[4 * i + d];
+        }
+        rodsStale_ = false;
+    }
+    return rods_;
+}
+
+long SylinderSystem::getStepCount() const {
+    int64_t c = 0;
+    if (ctx_) alens_get_step_count(ctx_, &c);
+    return (long)c;
+}
+
+void SylinderSystem::writeResult(const std::string &path) const {
+    auto *self = const_cast<SylinderSystem *>(this);
+    const auto &rods = self->getContainer();
+    std::FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) throw std::runtime_error("cannot write " + path);
+    std::fprintf(f, "%zu\n%.17g\n", rods.size(), runConfig.dt * (double)getStepCount());
+    for (const auto &r : rods) {
+        double d[3];
+        directionFromQuat(r.orientation, d);
+        const double h = 0.5 * r.length;
+        std::fprintf(f, "%c %lld %.17g %.17g %.17g %.17g %.17g %.17g %.17g %d\n", r.isImmovable ? 'S' : 'C',
+                     (long long)r.gid, r.radius, r.pos[0] - h * d[0], r.pos[1] - h * d[1], r.pos[2] - h * d[2],
+                     r.pos[0] + h * d[0], r.pos[1] + h * d[1], r.pos[2] + h * d[2], r.group);
+    }
+    std::fclose(f);
+}
+
+void SylinderSystem::printTimingSummary() const {
+    if (!timerOn_) return;
+    std::printf("rodSystem step %ld: %d collisions, %d bilateral, %d BBPGD iterations, residual %.3e, %.3f ms\n",
+                (long)stats_.step, stats_.nCollision, stats_.nBilateral, stats_.iterations, stats_.residual,
+                lastStepMs_);
+}
+
+}  // namespace gpu

@@ -1,0 +1,134 @@
+// SylinderSystem.hpp - C++ facade with the call surface aLENS's TubuleSystem
+// uses on SimToolbox's SylinderSystem (SRC/TubuleSystem.cpp:38,55,79,100,105,
+// 120,176,223,224,229,697), implemented over the C ABI of include/alens_gpu.h.
+//
+// One system on one GPU: the MPI/FDPS getters of the reference
+// (getDomainInfo, getCommRcp, ...) have no counterpart; prepareStep() has no
+// repartitioning to do.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "alens_gpu.h"
+
+namespace gpu {
+
+// Hot-path subset of SylinderConfig (RunConfig.yaml keys,
+// docs/source/quickstart.md:316-358) plus the keys TubuleSystem reads.
+struct SylinderConfig {
+    unsigned long long rngSeed = 1234;
+    double simBoxLow[3] = {0, 0, 0};
+    double simBoxHigh[3] = {1, 1, 1};
+    bool simBoxPBC[3] = {false, false, false};
+    bool monolayer = false;
+    double viscosity = 0.01;
+    double KBT = 0.00411;
+    double linkKappa = 1000.0;
+    double sylinderDiameter = 0.025;
+    double sylinderDiameterColRatio = 1.0;
+    double sylinderLengthColRatio = 1.0;
+    double sylinderColBuf = 0.025;
+    double dt = 1e-4;
+    double timeTotal = 1.0;
+    double timeSnap = 1.0;
+    double conResTol = 1e-5;
+    int conMaxIte = 2000;
+    int conSolverChoice = 0;
+
+    // Reads the flat "key: value" / "key: [a, b, c]" lines of RunConfig.yaml;
+    // unknown keys and nested blocks are ignored.
+    bool readYaml(const std::string &path, std::string *err = nullptr);
+    AlensConfig toAlens() const;
+};
+
+// Host record of one rod (the fields of Sylinder that TubuleSystem reads,
+// SRC/TubuleBind.hpp:54-67).
+struct Sylinder {
+    int64_t gid = 0;
+    int globalIndex = 0;
+    double radius = 0.0125;
+    double length = 1.0;
+    double pos[3] = {0, 0, 0};
+    double orientation[4] = {0, 0, 0, 1};  // Eigen order (x, y, z, w)
+    bool isImmovable = false;
+    int group = -1;
+};
+
+// Constraint block with SimToolbox's ConstraintBlock constructor signature
+// (SRC/TubuleSystem.cpp:727-736) and setStress (:742).
+struct ConstraintBlock {
+    AlensBlock blk;
+    ConstraintBlock(double delta0, double gamma, int64_t gidI, int64_t gidJ, int globalIndexI, int globalIndexJ,
+                    const double normI[3], const double normJ[3], const double posI[3], const double posJ[3],
+                    const double labI[3], const double labJ[3], bool oneSide, bool bilateral, double kappa,
+                    double gammaLB);
+    void setStress(const double stress9[9]);
+};
+
+using ConstraintBlockQue = std::vector<ConstraintBlock>;
+using ConstraintBlockPool = std::vector<ConstraintBlockQue>;
+
+class SylinderSystem {
+  public:
+    SylinderConfig runConfig;
+
+    SylinderSystem() = default;
+    ~SylinderSystem();
+    SylinderSystem(const SylinderSystem &) = delete;
+    SylinderSystem &operator=(const SylinderSystem &) = delete;
+
+    // RunConfig.yaml + TubuleInitial.dat ("C|S gid radius mx my mz px py pz
+    // [group]" lines, docs/source/quickstart.md:211-218); throws
+    // std::runtime_error on failure.
+    void initialize(const std::string &configFile, const std::string &posFile, int argc = 0,
+                    char **argv = nullptr);
+    // Restart from a SylinderAscii snapshot written by writeResult().
+    void reinitialize(const std::string &configFile, const std::string &restartFile, int argc = 0,
+                      char **argv = nullptr, bool eulerStep = false);
+    void initialize(const SylinderConfig &cfg, const std::vector<Sylinder> &rods);
+
+    void prepareStep();           // nothing to repartition on one GPU
+    void runStep();               // one full step (alens_step)
+    void stepEuler();             // apply a solve prepared by detect/solve (restart path)
+    void calcConStress();         // pair virial of the last step
+    void calcOrderParameter();    // polar and nematic order of the rod axes
+    void writeResult(const std::string &path) const;  // SylinderAscii text
+    void setTimer(bool on) { timerOn_ = on; }
+    void printTimingSummary() const;
+
+    ConstraintBlockPool &getConstraintPoolNonConst() { return conPool_; }
+    const std::vector<Sylinder> &getContainer();  // host copy, refreshed after steps
+    long getStepCount() const;
+    int getSnapID() const { return snapID_; }
+    const AlensStepStats &lastStats() const { return stats_; }
+    std::array<double, 9> conStress() const { return stress_; }
+    std::array<double, 3> polarOrder() const { return polar_; }
+    std::array<double, 9> nematicOrder() const { return nematic_; }
+
+  private:
+    void create();
+    void flushPool();
+    void check(int rc, const char *where) const;
+
+    AlensCtx *ctx_ = nullptr;
+    std::vector<Sylinder> rods_;
+    bool rodsStale_ = false;
+    ConstraintBlockPool conPool_;
+    AlensStepStats stats_{};
+    std::array<double, 9> stress_{};
+    std::array<double, 3> polar_{};
+    std::array<double, 9> nematic_{};
+    int snapID_ = 0;
+    bool timerOn_ = false;
+    double lastStepMs_ = 0.0;
+};
+
+// Read TubuleInitial.dat / SylinderAscii lines; 'L' link lines are returned
+// in links (pairs of gids).
+std::vector<Sylinder> readSylinderAscii(const std::string &path, std::vector<std::array<int64_t, 2>> *links,
+                                        std::string *err);
+
+}  // namespace gpu

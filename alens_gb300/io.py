@@ -1,0 +1,82 @@
+"""aLENS text formats: TubuleInitial.dat / SylinderAscii rod lines
+("C|S gid radius mx my mz px py pz [group]", docs/source/quickstart.md:211-218;
+'L a b' link lines as in Utils/gen_flexible_init.py) and the flat keys of
+RunConfig.yaml (docs/source/quickstart.md:316-358)."""
+from __future__ import annotations
+
+import numpy as np
+
+from .capi import AlensConfig, RodState, make_config
+from .workloads import axis_to_quat, quat_to_axis
+
+
+def read_sylinder_ascii(path):
+    """Rods and links of a TubuleInitial.dat / SylinderAscii file."""
+    gid, pos, axis, length, radius, imm, group, links = [], [], [], [], [], [], [], []
+    with open(path) as f:
+        for line in f:
+            t = line.split()
+            if not t:
+                continue
+            if t[0] == "L" and len(t) >= 3:
+                links.append((int(t[1]), int(t[2])))
+                continue
+            if t[0] not in ("C", "S") or len(t) < 9:
+                continue
+            m = np.array(t[3:6], float)
+            p = np.array(t[6:9], float)
+            d = p - m
+            L = float(np.linalg.norm(d))
+            gid.append(int(t[1]))
+            radius.append(float(t[2]))
+            pos.append(0.5 * (m + p))
+            axis.append(d / L if L > 0 else np.array([0.0, 0.0, 1.0]))
+            length.append(L)
+            imm.append(1 if t[0] == "S" else 0)
+            group.append(int(t[9]) if len(t) > 9 else -1)
+    n = len(gid)
+    rods = RodState(np.array(gid, np.int64), np.array(pos).reshape(n, 3), axis_to_quat(np.array(axis).reshape(n, 3)),
+                    np.array(length), np.array(radius), np.array(imm, np.int32))
+    return rods, links
+
+
+def write_sylinder_ascii(path, rods: RodState, time: float = 0.0, group=None):
+    a = quat_to_axis(rods.quat)
+    h = 0.5 * rods.length[:, None]
+    m = rods.pos - h * a
+    p = rods.pos + h * a
+    imm = rods.immovable if rods.immovable is not None else np.zeros(rods.n, np.int32)
+    with open(path, "w") as f:
+        f.write(f"{rods.n}\n{time:.17g}\n")
+        for i in range(rods.n):
+            g = -1 if group is None else int(group[i])
+            f.write("%s %d %.17g %.17g %.17g %.17g %.17g %.17g %.17g %d\n" % (
+                "S" if imm[i] else "C", rods.gid[i], rods.radius[i], *m[i], *p[i], g))
+
+
+def read_run_config(path, **overrides) -> AlensConfig:
+    vals = {}
+    with open(path) as f:
+        for line in f:
+            line = line.split("#", 1)[0]
+            if not line.strip() or line[0] in " \t-" or ":" not in line:
+                continue
+            k, v = line.split(":", 1)
+            vals[k.strip()] = v.strip()
+
+    def vec(v, conv=float):
+        return [conv(x.strip()) for x in v.strip("[] ").split(",")]
+
+    def b(x):
+        return str(x).strip().lower() in ("true", "1", "yes")
+
+    cfg = make_config(
+        box_low=vec(vals.get("simBoxLow", "[0,0,0]")), box_high=vec(vals.get("simBoxHigh", "[1,1,1]")),
+        pbc=[b(x) for x in vals.get("simBoxPBC", "[false,false,false]").strip("[] ").split(",")],
+        monolayer=b(vals.get("monolayer", "false")), viscosity=float(vals.get("viscosity", 0.01)),
+        kbt=float(vals.get("KBT", 0.00411)), dt=float(vals.get("dt", 1e-4)),
+        col_ratio_d=float(vals.get("sylinderDiameterColRatio", 1.0)),
+        col_ratio_l=float(vals.get("sylinderLengthColRatio", 1.0)),
+        col_buf=float(vals.get("sylinderColBuf", 0.025)), tol=float(vals.get("conResTol", 1e-5)),
+        max_ite=int(float(vals.get("conMaxIte", 2000))), seed=int(vals.get("rngSeed", 1234)), **overrides)
+    return cfg

@@ -1,0 +1,59 @@
+"""CPU tests of the committed fixtures (derived from the reference's
+Examples/DenseMonoLayer data by tests/golden/make_fixtures.py), the aLENS
+text formats and the oracle's regression pin on them."""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+sys.path.insert(0, GOLDEN)
+
+import make_fixtures  # noqa: E402
+
+from alens_gb300 import io  # noqa: E402
+
+
+def test_fixture_files_parse():
+    cfg, rods = make_fixtures.load_fixture()
+    assert rods.n == 1277
+    assert cfg.monolayer == 1 and cfg.dt == 1e-5 and cfg.conMaxIte == 3000
+    assert np.allclose(rods.pos[:, 2], 5.5)
+    assert np.all(rods.radius == 0.0125)
+    assert np.allclose(rods.length, 0.25, atol=1e-6)
+
+
+def test_sylinder_ascii_round_trip(tmp_path):
+    _, rods = make_fixtures.load_fixture()
+    p = tmp_path / "out.dat"
+    io.write_sylinder_ascii(str(p), rods, time=0.5)
+    back, links = io.read_sylinder_ascii(str(p))
+    assert links == []
+    assert np.array_equal(back.gid, rods.gid)
+    assert np.allclose(back.pos, rods.pos, atol=1e-14)
+    assert np.allclose(back.length, rods.length, atol=1e-14)
+    assert np.allclose(back.quat, rods.quat, atol=1e-12)
+
+
+def test_links_and_stationary_lines(tmp_path):
+    p = tmp_path / "in.dat"
+    p.write_text("3\n0\nS 0 0.0125 0 0.5 0.5 20 0.5 0.5\nC 1 0.0125 0 0.5 0.57 20 0.5 0.57 3\nL 0 1\n")
+    rods, links = io.read_sylinder_ascii(str(p))
+    assert rods.n == 2 and links == [(0, 1)]
+    assert list(rods.immovable) == [1, 0]
+    assert np.allclose(rods.length, 20.0)
+    assert np.allclose(rods.pos[1], [10.0, 0.5, 0.57])
+
+
+def test_oracle_reproduces_golden():
+    """Regression pin of the oracle on the monolayer window."""
+    with open(os.path.join(GOLDEN, "monolayer_window_golden.json")) as f:
+        gold = json.load(f)
+    g = make_fixtures.golden(steps=gold["steps"])
+    assert g["iterations"] == gold["iterations"]
+    assert g["collisions"] == gold["collisions"]
+    assert g["rod0"] == gold["rod0"]
+    assert g["pos_head"] == gold["pos_head"] and g["quat_head"] == gold["quat_head"]
+    assert g["stress_trace"] == gold["stress_trace"]
