@@ -116,7 +116,10 @@ def build_facade_driver(force: bool = False) -> Path:
     if not force and _newer(out, deps):
         return out
     cxx = os.environ.get("CXX", "g++")
-    _run([cxx, "-O2", "-std=c++17", "-fopenmp", "-Wall", "-I", str(ROOT / "include"), "-I", str(CSRC / "facade"),
+    # no FMA contraction: aarch64 g++ contracts a*b+c by default, which would
+    # round the reader's lengths and quaternions differently from the oracle
+    _run([cxx, "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-Wall", "-I", str(ROOT / "include"),
+          "-I", str(CSRC / "facade"),
           str(src), str(CSRC / "facade" / "SylinderSystem.cpp"),
           "-L", str(LIBDIR), "-lalens_gpu", "-Wl,-rpath," + str(LIBDIR), "-o", str(out)])
     return out

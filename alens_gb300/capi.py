@@ -175,6 +175,7 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_rods": (C.c_int, [vp, C.c_int, C.c_int, _PD, _PD]),
         "alens_get_velocity": (C.c_int, [vp, C.c_int, C.c_int, _PD, _PD]),
         "alens_add_bilateral": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(AlensBlock)]),
+        "alens_set_links": (C.c_int, [vp, C.c_int, C.c_int, _PI32, _PI32, _PD, _PD, _PD, _PD]),
         "alens_step": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
         "alens_detect": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
         "alens_solve": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
@@ -314,6 +315,16 @@ class GpuSystem:
     def add_bilateral(self, blocks, replica: int = 0):
         arr = (AlensBlock * len(blocks))(*blocks)
         self._ck(self.lib.alens_add_bilateral(self.h, replica, len(blocks), arr), "alens_add_bilateral")
+
+    def set_links(self, links, replica: int = 0):
+        """links: dict of arrays i, j (rod indices), si, sj (arc positions),
+        rest, kappa."""
+        a = [np.ascontiguousarray(links[k], dtype=t) for k, t in
+             (("i", np.int32), ("j", np.int32), ("si", np.float64), ("sj", np.float64), ("rest", np.float64),
+              ("kappa", np.float64))]
+        self._ck(self.lib.alens_set_links(self.h, replica, int(a[0].shape[0]), _p(a[0], C.c_int32),
+                                          _p(a[1], C.c_int32), _p(a[2], C.c_double), _p(a[3], C.c_double),
+                                          _p(a[4], C.c_double), _p(a[5], C.c_double)), "alens_set_links")
 
     def _stage(self, fn, name, ok=(ALENS_OK,)):
         st = AlensStepStats()

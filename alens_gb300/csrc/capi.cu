@@ -149,6 +149,15 @@ int alens_add_bilateral(AlensCtx *ctx, int replica, int n, const AlensBlock *blo
     });
 }
 
+int alens_set_links(AlensCtx *ctx, int replica, int n, const int32_t *indexI, const int32_t *indexJ,
+                    const double *sI, const double *sJ, const double *restLength, const double *kappa) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->setLinks(replica, n, indexI, indexJ, sI, sJ, restLength, kappa);
+        return (int)ALENS_OK;
+    });
+}
+
 int alens_step(AlensCtx *ctx, AlensStepStats *stats) {
     if (!ctx) return ALENS_INVALID_ARG;
     return guarded_ctx(ctx, [&] { return ctx->eng->step(stats); });

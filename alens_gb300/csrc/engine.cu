@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
+#include <type_traits>
 
 namespace alens {
 
@@ -49,6 +50,7 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     R_ = nrep;
     rods_.resize(R_);
     queue_.resize(R_);
+    links_.resize(R_);
     repStats_.assign(R_, AlensStepStats{});
     if (cfg_[0].stream) {
         stream_ = (cudaStream_t)cfg_[0].stream;
@@ -63,12 +65,14 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     fixedCap_ = cfg_[0].maxConstraints;
     stageTiming_ = cfg_[0].stageTiming != 0;
     if (const char *e = std::getenv("ALENS_SOLVER_BLOCKS_PER_SM")) solverBlocksPerSM_ = std::max(1, atoi(e));
-    // FP32 solver form: -1 = cluster form with the largest cluster size,
-    // 0 = grid form, N = cluster form with clusters of N CTAs
+    // FP32 solver form: -1 = automatic (grid form for one replica, where all
+    // SMs share one system; cluster form for ensembles), 0 = grid form,
+    // N = cluster form with clusters of N CTAs
     if (const char *e = std::getenv("ALENS_CLUSTER_SIZE")) clusterSize_ = atoi(e);
     CK(cudaMallocHost(&hCtl_, sizeof(DevCtl)));
     CK(cudaMallocHost(&hDyn_, sizeof(RepDyn) * R_));
     CK(cudaMallocHost(&hBilPrefix_, sizeof(int) * (R_ + 1)));
+    CK(cudaMallocHost(&hLinkSlot0_, sizeof(int) * R_));
     std::memset(hCtl_, 0, sizeof(DevCtl));
     std::memset(hDyn_, 0, sizeof(RepDyn) * R_);
     std::memset(hBilPrefix_, 0, sizeof(int) * (R_ + 1));
@@ -89,6 +93,8 @@ Engine::~Engine() {
     if (hBilPrefix_) cudaFreeHost(hBilPrefix_);
     if (hBlocks_) cudaFreeHost(hBlocks_);
     if (hBlockRep_) cudaFreeHost(hBlockRep_);
+    if (hLinkSlot0_) cudaFreeHost(hLinkSlot0_);
+    freeGroup(linkAllocs_);
     if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -189,6 +195,8 @@ void Engine::finalize() {
     freeGroup(blockAllocs_);
     freeGroup(opAllocs_);
     blockCap_ = 0;
+    freeGroup(linkAllocs_);
+    S_.nLinks = 0;
     hostPar_.resize(R_);
     int rodOff = 0, cellOff = 0;
     for (int r = 0; r < R_; r++) {
@@ -217,6 +225,8 @@ void Engine::finalize() {
     S.stress = alloc<double>(fixedAllocs_, 9 * (size_t)R_);
     S.scanTmp = alloc<int>(fixedAllocs_, 4096);
     S.prevCount = alloc<int>(fixedAllocs_, 1);
+    S.linkSlot0 = alloc<int>(fixedAllocs_, R_);
+    linksDirty_ = true;
     CK(cudaMemcpyAsync(S.par, hostPar_.data(), sizeof(RepParams) * R_, cudaMemcpyHostToDevice, stream_));
     CK(cudaMemsetAsync(S.dyn, 0, sizeof(RepDyn) * R_, stream_));
     CK(cudaMemsetAsync(S.bilPrefix, 0, sizeof(int) * (R_ + 1), stream_));
@@ -411,12 +421,80 @@ void Engine::addBilateral(int rep, int n, const AlensBlock *blocks) {
     queue_[rep].insert(queue_[rep].end(), blocks, blocks + n);
 }
 
+void Engine::setLinks(int rep, int n, const int32_t *idxI, const int32_t *idxJ, const double *sI,
+                      const double *sJ, const double *rest, const double *kappa) {
+    if (rep < 0 || rep >= R_ || n < 0) throw ApiError(ALENS_INVALID_ARG);
+    if (n > 0 && (!idxI || !idxJ || !sI || !sJ || !rest || !kappa)) throw ApiError(ALENS_INVALID_ARG);
+    const int nr = rods_[rep].n;
+    for (int k = 0; k < n; k++) {
+        if (idxI[k] < 0 || idxI[k] >= nr || idxJ[k] < 0 || idxJ[k] >= nr) throw ApiError(ALENS_INVALID_ARG);
+        if (!(kappa[k] > 0.0) || !std::isfinite(sI[k]) || !std::isfinite(sJ[k]) || !std::isfinite(rest[k]))
+            throw ApiError(ALENS_INVALID_ARG);
+    }
+    HostLinks &h = links_[rep];
+    h.I.assign(idxI, idxI + n);
+    h.J.assign(idxJ, idxJ + n);
+    h.sI.assign(sI, sI + n);
+    h.sJ.assign(sJ, sJ + n);
+    h.rest.assign(rest, rest + n);
+    h.kappa.assign(kappa, kappa + n);
+    linksDirty_ = true;
+}
+
+// Concatenated device copy of every replica's links (rod indices made
+// global).  Invalidates the captured graph: the link count is part of it.
+void Engine::uploadLinks() {
+    if (!linksDirty_) return;
+    CK(cudaStreamSynchronize(stream_));
+    invalidateGraph();
+    freeGroup(linkAllocs_);
+    int total = 0;
+    for (int r = 0; r < R_; r++) total += (int)links_[r].I.size();
+    S_.nLinks = total;
+    if (total > 0) {
+        std::vector<int> I(total), J(total), rep(total), loc(total);
+        std::vector<double> a(total), b(total), rest(total), kap(total);
+        int o = 0;
+        for (int r = 0; r < R_; r++) {
+            const HostLinks &h = links_[r];
+            const int off = hostPar_[r].rodOffset;
+            for (size_t k = 0; k < h.I.size(); k++, o++) {
+                I[o] = h.I[k] + off;
+                J[o] = h.J[k] + off;
+                rep[o] = r;
+                loc[o] = (int)k;
+                a[o] = h.sI[k];
+                b[o] = h.sJ[k];
+                rest[o] = h.rest[k];
+                kap[o] = h.kappa[k];
+            }
+        }
+        auto up = [&](auto *&dst, const auto &src) {
+            using T = typename std::remove_reference<decltype(src[0])>::type;
+            dst = alloc<typename std::remove_const<T>::type>(linkAllocs_, total);
+            CK(cudaMemcpy(dst, src.data(), sizeof(T) * total, cudaMemcpyHostToDevice));
+        };
+        up(S_.linkI, I);
+        up(S_.linkJ, J);
+        up(S_.linkRep, rep);
+        up(S_.linkLocal, loc);
+        up(S_.linkSI, a);
+        up(S_.linkSJ, b);
+        up(S_.linkRest, rest);
+        up(S_.linkKappa, kap);
+    }
+    linksDirty_ = false;
+}
+
 // --------------------------------------------------------------- blocks
+// Per replica the blocks are [queued by alens_add_bilateral..., links...].
 void Engine::uploadBlocks() {
+    uploadLinks();
     int total = 0;
     hBilPrefix_[0] = 0;
     for (int r = 0; r < R_; r++) {
-        total += (int)queue_[r].size();
+        hLinkSlot0_[r] = total + (int)queue_[r].size();
+        total += (int)queue_[r].size() + (int)links_[r].I.size();
         hBilPrefix_[r + 1] = total;
     }
     if (total > blockCap_) {
@@ -432,19 +510,19 @@ void Engine::uploadBlocks() {
         CK(cudaMallocHost(&hBlockRep_, sizeof(int) * blockCap_));
     }
     S_.blockCap = blockCap_;
-    if (total > 0) {
-        // the previous step's copies out of the pinned buffers are complete:
-        // every step ends with a stream synchronisation
-        int o = 0;
-        for (int r = 0; r < R_; r++) {
-            std::memcpy(hBlocks_ + o, queue_[r].data(), sizeof(AlensBlock) * queue_[r].size());
-            for (size_t b = 0; b < queue_[r].size(); b++) hBlockRep_[o + b] = r;
-            o += (int)queue_[r].size();
-        }
-        CK(cudaMemcpyAsync(S_.blocks, hBlocks_, sizeof(AlensBlock) * total, cudaMemcpyHostToDevice, stream_));
-        CK(cudaMemcpyAsync(S_.blockRep, hBlockRep_, sizeof(int) * total, cudaMemcpyHostToDevice, stream_));
+    // the previous step's copies out of the pinned buffers are complete:
+    // every step ends with a stream synchronisation
+    for (int r = 0; r < R_; r++) {
+        const int o = hBilPrefix_[r];
+        const size_t nq = queue_[r].size();
+        if (nq == 0) continue;
+        std::memcpy(hBlocks_ + o, queue_[r].data(), sizeof(AlensBlock) * nq);
+        for (size_t b = 0; b < nq; b++) hBlockRep_[o + b] = r;
+        CK(cudaMemcpyAsync(S_.blocks + o, hBlocks_ + o, sizeof(AlensBlock) * nq, cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync(S_.blockRep + o, hBlockRep_ + o, sizeof(int) * nq, cudaMemcpyHostToDevice, stream_));
     }
     CK(cudaMemcpyAsync(S_.bilPrefix, hBilPrefix_, sizeof(int) * (R_ + 1), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(S_.linkSlot0, hLinkSlot0_, sizeof(int) * R_, cudaMemcpyHostToDevice, stream_));
     nBilQueued_ = total;
 }
 
@@ -461,6 +539,10 @@ int Engine::enqueueDetect() {
     CK(cudaMemsetAsync(S.rowCursor, 0, sizeof(int) * S.nRods, stream_));
     launch_prep(S, stream_);
     n += 1;
+    if (S.nLinks > 0) {
+        launch_link_blocks(S, stream_);
+        n += 1;
+    }
     n += launch_scan(S.cellCount, S.cellStart, S.nCells, S.scanTmp, stream_);
     launch_scatter(S, stream_);
     launch_pairs(S, stream_);
@@ -481,6 +563,7 @@ void Engine::ensureSolverGrid() {
     const int maxg = solver_max_grid(precision_);
     solverGrid_ = std::min(maxg, numSM_ * solverBlocksPerSM_);
     if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "solver occupancy");
+    if (clusterSize_ < 0 && R_ == 1) clusterSize_ = 0;
     if (precision_ == ALENS_PREC_MIXED && clusterSize_ != 0) {
         const int maxCs = cluster_max_size();
         int cs = clusterSize_ > 0 ? std::min(clusterSize_, maxCs) : maxCs;

@@ -111,6 +111,11 @@ struct DevState {
     int *prevCount;
     AlensBlock *blocks;
     int *blockRep;
+    // pre-bound crosslinkers (blocks built on the device every step)
+    int nLinks;
+    int *linkI, *linkJ, *linkRep, *linkLocal;  // global rod indices, replica, index in replica
+    double *linkSI, *linkSJ, *linkRest, *linkKappa;
+    int *linkSlot0;  // [R] block slot of each replica's first link (host-written)
     // reductions
     double *part;   // 9 x tileCap (solver: 2 parities x 4 kinds; stress: 9)
     double *work;   // per block 9 x workCap
@@ -125,6 +130,7 @@ void launch_prep(const DevState &S, cudaStream_t st);
 void launch_mobility(const DevState &S, cudaStream_t st);  // once per rod set
 int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st);  // returns kernels launched
 void launch_scatter(const DevState &S, cudaStream_t st);
+void launch_link_blocks(const DevState &S, cudaStream_t st);
 void launch_pairs(const DevState &S, cudaStream_t st);
 int launch_pair_sort(const DevState &S, cudaStream_t st);
 void launch_ranges(const DevState &S, cudaStream_t st);

@@ -35,6 +35,8 @@ class Engine {
     void getRods(int rep, int n, double *pos, double *quat);
     void getVelocity(int rep, int n, double *vel, double *omega);
     void addBilateral(int rep, int n, const AlensBlock *blocks);
+    void setLinks(int rep, int n, const int32_t *idxI, const int32_t *idxJ, const double *sI, const double *sJ,
+                  const double *rest, const double *kappa);
     int step(AlensStepStats *out);
     int detect(AlensStepStats *out);
     int solve(AlensStepStats *out);
@@ -92,12 +94,21 @@ class Engine {
     bool useGraph_ = true, graphFailed_ = false;
     int fixedCap_ = 0;
     int solverBlocksPerSM_ = 1;
-    int clusterSize_ = -1;   // FP32 solver: -1 largest cluster, 0 grid form
+    int clusterSize_ = -1;   // FP32 solver: -1 automatic, 0 grid form, N cluster size
     int nClusters_ = 1;
     int prevCountHost_ = 0;  // valid warm-start keys on the device
     int solverGrid_ = 0;
     std::vector<HostRods> rods_;
     std::vector<std::vector<AlensBlock>> queue_;
+    struct HostLinks {
+        std::vector<int> I, J;
+        std::vector<double> sI, sJ, rest, kappa;
+    };
+    std::vector<HostLinks> links_;
+    bool linksDirty_ = false;
+    std::vector<void *> linkAllocs_;
+    int *hLinkSlot0_ = nullptr;
+    void uploadLinks();
     std::vector<RepParams> hostPar_;
     bool dirty_ = true;
     bool haveDetect_ = false, haveSolve_ = false;

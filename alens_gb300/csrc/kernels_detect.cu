@@ -214,6 +214,59 @@ __global__ void k_scan_add(int *out, int n, const int *tmp) {
         if (base + k < n) out[base + k] += add;
 }
 
+// ------------------------------------------------------------- links
+// Bilateral block of every pre-bound link from the current rod state:
+// anchors P = c_I + sI a_I, Q = c_J + sJ a_J, d = P - Q reduced to the
+// minimum image, spring extension |d| - rest (SRC/TubuleSystem.cpp:714-736).
+__global__ void k_link_blocks(DevState S) {
+    if (flags(S) & kErrNaN) return;
+    for (int L = blockIdx.x * blockDim.x + threadIdx.x; L < S.nLinks; L += gridDim.x * blockDim.x) {
+        const int rep = S.linkRep[L];
+        const RepParams &P = S.par[rep];
+        const int I = S.linkI[L], J = S.linkJ[L];
+        const double sI = S.linkSI[L], sJ = S.linkSJ[L];
+        const double aI[3] = {S.ax[I], S.ay[I], S.az[I]};
+        const double aJ[3] = {S.ax[J], S.ay[J], S.az[J]};
+        const double pI[3] = {S.px[I] + sI * aI[0], S.py[I] + sI * aI[1], S.pz[I] + sI * aI[2]};
+        const double pJ[3] = {S.px[J] + sJ * aJ[0], S.py[J] + sJ * aJ[1], S.pz[J] + sJ * aJ[2]};
+        double d[3];
+        for (int c = 0; c < 3; c++) {
+            d[c] = pI[c] - pJ[c];
+            if (P.pbc[c]) d[c] = d[c] - P.L[c] * floor(d[c] / P.L[c] + 0.5);
+        }
+        const double len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        double n[3] = {0.0, 0.0, 1.0};
+        if (len > 0.0) {
+            n[0] = d[0] / len;
+            n[1] = d[1] / len;
+            n[2] = d[2] / len;
+        }
+        const int slot = S.linkSlot0[rep] + S.linkLocal[L];
+        AlensBlock &B = S.blocks[slot];
+        const double delta0 = len - S.linkRest[L];
+        B.delta0 = delta0;
+        B.gamma = -delta0 * S.linkKappa[L];
+        B.gidI = S.gid[I];
+        B.gidJ = S.gid[J];
+        B.globalIndexI = I - P.rodOffset;
+        B.globalIndexJ = J - P.rodOffset;
+        for (int c = 0; c < 3; c++) {
+            B.normI[c] = n[c];
+            B.normJ[c] = -n[c];
+            B.posI[c] = sI * aI[c];
+            B.posJ[c] = sJ * aJ[c];
+            B.labI[c] = pI[c];
+            B.labJ[c] = pI[c] - d[c];
+        }
+        B.oneSide = 0;
+        B.bilateral = 1;
+        B.kappa = S.linkKappa[L];
+        B.gammaLB = 0.0;
+        for (int c = 0; c < 9; c++) B.stress[c] = 0.0;
+        S.blockRep[slot] = rep;
+    }
+}
+
 // ------------------------------------------------------------- scatter
 // Cell-sorted FP32 search geometry: centre relative to its cell origin and
 // half-length (sA), axis and collision radius (sB).  Relative coordinates
@@ -697,6 +750,10 @@ int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st) {
     k_scan_top<<<1, 1024, 0, st>>>(tmp, nb, out, n);
     if (nb > 0) k_scan_add<<<nb, kScanBlock, 0, st>>>(out, n, tmp);
     return nb > 0 ? 3 : 1;
+}
+
+void launch_link_blocks(const DevState &S, cudaStream_t st) {
+    if (S.nLinks > 0) k_link_blocks<<<grid_for(S.nLinks, 128), 128, 0, st>>>(S);
 }
 
 void launch_scatter(const DevState &S, cudaStream_t st) {

@@ -4,15 +4,28 @@
 RunConfig.yaml (docs/source/quickstart.md:316-358)."""
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 from .capi import AlensConfig, RodState, make_config
-from .workloads import axis_to_quat, quat_to_axis
+from .workloads import quat_to_axis
+
+
+def _quat_from_direction(d0, d1, d2):
+    """Rotation of +z onto (d0, d1, d2) as (x, y, z, w), with the operation
+    order of the C++ facade's reader (gpu::readSylinderAscii), so both
+    readers produce bit-identical rods."""
+    x, y, z, w = -d1, d0, 0.0, 1.0 + d2
+    if w < 1e-8:
+        x, y, z, w = 1.0, 0.0, 0.0, 0.0
+    n = math.sqrt(x * x + y * y + z * z + w * w)
+    return [x / n, y / n, z / n, w / n]
 
 
 def read_sylinder_ascii(path):
     """Rods and links of a TubuleInitial.dat / SylinderAscii file."""
-    gid, pos, axis, length, radius, imm, group, links = [], [], [], [], [], [], [], []
+    gid, pos, quat, length, radius, imm, group, links = [], [], [], [], [], [], [], []
     with open(path) as f:
         for line in f:
             t = line.split()
@@ -23,19 +36,23 @@ def read_sylinder_ascii(path):
                 continue
             if t[0] not in ("C", "S") or len(t) < 9:
                 continue
-            m = np.array(t[3:6], float)
-            p = np.array(t[6:9], float)
-            d = p - m
-            L = float(np.linalg.norm(d))
+            m = [float(v) for v in t[3:6]]
+            p = [float(v) for v in t[6:9]]
+            d = [p[k] - m[k] for k in range(3)]
+            L = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+            if L > 0:
+                d = [d[k] / L for k in range(3)]
+            else:
+                d = [0.0, 0.0, 1.0]
             gid.append(int(t[1]))
             radius.append(float(t[2]))
-            pos.append(0.5 * (m + p))
-            axis.append(d / L if L > 0 else np.array([0.0, 0.0, 1.0]))
+            pos.append([0.5 * (m[k] + p[k]) for k in range(3)])
+            quat.append(_quat_from_direction(*d))
             length.append(L)
             imm.append(1 if t[0] == "S" else 0)
             group.append(int(t[9]) if len(t) > 9 else -1)
     n = len(gid)
-    rods = RodState(np.array(gid, np.int64), np.array(pos).reshape(n, 3), axis_to_quat(np.array(axis).reshape(n, 3)),
+    rods = RodState(np.array(gid, np.int64), np.array(pos).reshape(n, 3), np.array(quat).reshape(n, 4),
                     np.array(length), np.array(radius), np.array(imm, np.int32))
     return rods, links
 

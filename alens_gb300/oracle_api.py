@@ -39,6 +39,7 @@ def load_oracle(rebuild: bool = True) -> C.CDLL:
         "orc_get_known_velocity": (C.c_int, [vp, C.c_int, _PD]),
         "orc_add_bilateral": (C.c_int, [vp, C.c_int, C.POINTER(AlensBlock)]),
         "orc_set_initial_gamma": (C.c_int, [vp, C.c_int, _PD]),
+        "orc_set_links": (C.c_int, [vp, C.c_int, _PI32, _PI32, _PD, _PD, _PD, _PD]),
         "orc_step": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
         "orc_detect": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
         "orc_solve": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
@@ -181,6 +182,14 @@ class OracleSystem:
     def add_bilateral(self, blocks):
         arr = (AlensBlock * len(blocks))(*blocks)
         _ck(self.lib.orc_add_bilateral(self.h, len(blocks), arr), "orc_add_bilateral")
+
+    def set_links(self, links):
+        a = [np.ascontiguousarray(links[k], dtype=t) for k, t in
+             (("i", np.int32), ("j", np.int32), ("si", np.float64), ("sj", np.float64), ("rest", np.float64),
+              ("kappa", np.float64))]
+        _ck(self.lib.orc_set_links(self.h, int(a[0].shape[0]), _p(a[0], C.c_int32), _p(a[1], C.c_int32),
+                                   _p(a[2], C.c_double), _p(a[3], C.c_double), _p(a[4], C.c_double),
+                                   _p(a[5], C.c_double)), "orc_set_links")
 
     def set_initial_gamma(self, gamma):
         g = np.ascontiguousarray(gamma, dtype=np.float64)

@@ -139,6 +139,59 @@ def ensemble(nrep: int = 64, nmin: int = 500, nmax: int = 8000, phi: float = 0.0
     return out
 
 
+def segment_closest_params(c1, u1, h1, c2, u2, h2):
+    """Closest-point parameters (s, t) of segment pairs c1 + s u1, c2 + t u2
+    (|s| <= h1, |t| <= h2), vectorised over pairs; used to place crosslinker
+    anchors."""
+    w = c1 - c2
+    b = np.einsum("ij,ij->i", u1, u2)
+    d = np.einsum("ij,ij->i", u1, w)
+    e = np.einsum("ij,ij->i", u2, w)
+    det = 1.0 - b * b
+    par = det <= 1e-12
+    s = np.where(par, 0.0, (b * e - d) / np.where(par, 1.0, det))
+    lo = np.maximum(-h1, -d - np.abs(b) * h2)
+    hi = np.minimum(h1, -d + np.abs(b) * h2)
+    s = np.where(par, np.where(lo <= hi, 0.5 * (lo + hi), np.clip(-d, -h1, h1)), np.clip(s, -h1, h1))
+    t = b * s + e
+    tc = np.clip(t, -h2, h2)
+    s = np.where(t != tc, np.clip(b * tc - d, -h1, h1), s)
+    return s, tc
+
+
+def pair_list(system, cfg, rods, sep):
+    """(i, j, image) of rod pairs with separation < sep, found with a detect
+    pass of `system` (a GpuSystem or OracleSystem class) whose collision
+    buffer is sep."""
+    c = config_with(cfg, sylinderColBuf=float(sep), KBT=-1.0)
+    s = system(c)
+    s.set_rods(rods)
+    s.detect()
+    con = s.constraints()
+    s.close() if hasattr(s, "close") else None
+    return con["i"].copy(), con["j"].copy(), con["image"].copy()
+
+
+def make_links(cfg, rods, pairs, nlinks: int, seed: int = 0, kappa: float = 100.0, rest: float = 0.05,
+               jitter: float = 0.05) -> dict:
+    """Pre-bound crosslinkers on random near pairs: anchors at the pair's
+    closest points, moved along each rod by U(-jitter, jitter) and kept on
+    the rod."""
+    rng = np.random.default_rng(seed)
+    pi, pj, pimg = pairs
+    pick = rng.integers(0, pi.shape[0], nlinks)
+    i, j, img = pi[pick], pj[pick], pimg[pick]
+    box = np.array([cfg.simBoxHigh[d] - cfg.simBoxLow[d] for d in range(3)])
+    shift = np.stack([img // 9 - 1, (img // 3) % 3 - 1, img % 3 - 1], axis=1) * box
+    a = quat_to_axis(rods.quat)
+    hI, hJ = 0.5 * rods.length[i], 0.5 * rods.length[j]
+    s, t = segment_closest_params(rods.pos[i], a[i], hI, rods.pos[j] + shift, a[j], hJ)
+    s = np.clip(s + rng.uniform(-jitter, jitter, nlinks), -hI, hI)
+    t = np.clip(t + rng.uniform(-jitter, jitter, nlinks), -hJ, hJ)
+    return {"i": i.astype(np.int32), "j": j.astype(np.int32), "si": s, "sj": t,
+            "rest": np.full(nlinks, rest), "kappa": np.full(nlinks, kappa)}
+
+
 def nematic_order_2d(quat: np.ndarray) -> float:
     a = quat_to_axis(quat)
     phi = np.arctan2(a[:, 1], a[:, 0])
@@ -162,5 +215,5 @@ def config_with(cfg: AlensConfig, **changes) -> AlensConfig:
 
 
 __all__ = ["Workload", "small_periodic", "dense_monolayer", "crosslinked_bundle_rods", "large_eval",
-           "ensemble", "axis_to_quat", "quat_to_axis", "nematic_order_2d", "config_with",
-           "PREC_FP64", "WARM_ZERO"]
+           "ensemble", "axis_to_quat", "quat_to_axis", "nematic_order_2d", "config_with", "pair_list",
+           "make_links", "segment_closest_params", "PREC_FP64", "WARM_ZERO"]

@@ -190,6 +190,18 @@ int alens_get_velocity(AlensCtx *ctx, int replica, int n, double *vel,
 int alens_add_bilateral(AlensCtx *ctx, int replica, int n,
                         const AlensBlock *blocks);
 
+/* Pre-bound two-headed crosslinkers of one replica (the doubly-bound
+ * proteins whose blocks TubuleSystem::setProteinConstraints builds on the
+ * host every step, SRC/TubuleSystem.cpp:694-745).  Link k joins rod
+ * indexI[k] at arc position sI[k] (um from the centre along the axis) and
+ * rod indexJ[k] at sJ[k] with a spring of rest length restLength[k] and
+ * stiffness kappa[k].  Every step the library builds each link's bilateral
+ * block on the device from the current rod state (minimum image across
+ * periodic boundaries), after the blocks queued by alens_add_bilateral.
+ * Replaces the replica's link set; n = 0 removes it. */
+int alens_set_links(AlensCtx *ctx, int replica, int n, const int32_t *indexI, const int32_t *indexJ,
+                    const double *sI, const double *sJ, const double *restLength, const double *kappa);
+
 /* One full step (replaces SylinderSystem::runStep, SRC/TubuleSystem.cpp:223).
  * Returns ALENS_OK, ALENS_NOT_CONVERGED (step completed with the last
  * iterate), or an error; *stats (nullable) receives the summary. */

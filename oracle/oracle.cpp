@@ -416,6 +416,9 @@ struct OrcCtx {
     std::vector<double> jac, phi0, q, gamma, cinv, lb, lab;
     std::vector<uint8_t> unil;
     std::vector<AlensBlock> queue, blocks;
+    // pre-bound crosslinkers: blocks built from the rod state every step
+    std::vector<int> linkI, linkJ;
+    std::vector<double> linkSI, linkSJ, linkRest, linkKappa;
     // rod-major rows: entries 2k+side, ascending
     std::vector<int64_t> rowptr;
     std::vector<int64_t> rowent;
@@ -652,6 +655,52 @@ void build_constraints(OrcCtx *x) {
     x->ncoll = (int)keys.size();
     x->blocks = x->queue;
     x->queue.clear();
+    // link blocks after the queued ones: anchors P = c_I + sI a_I,
+    // Q = c_J + sJ a_J, d = P - Q reduced to the minimum image
+    for (size_t L = 0; L < x->linkI.size(); L++) {
+        const int I = x->linkI[L], J = x->linkJ[L];
+        const double sI = x->linkSI[L], sJ = x->linkSJ[L];
+        const double *aI = &x->axis[3 * I], *aJ = &x->axis[3 * J];
+        const double pI[3] = {x->pos[3 * I] + sI * aI[0], x->pos[3 * I + 1] + sI * aI[1],
+                              x->pos[3 * I + 2] + sI * aI[2]};
+        const double pJ[3] = {x->pos[3 * J] + sJ * aJ[0], x->pos[3 * J + 1] + sJ * aJ[1],
+                              x->pos[3 * J + 2] + sJ * aJ[2]};
+        double d[3];
+        for (int cc = 0; cc < 3; cc++) {
+            d[cc] = pI[cc] - pJ[cc];
+            if (c.simBoxPBC[cc]) {
+                const double Lb = c.simBoxHigh[cc] - c.simBoxLow[cc];
+                d[cc] = d[cc] - Lb * std::floor(d[cc] / Lb + 0.5);
+            }
+        }
+        const double len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        double nn[3] = {0.0, 0.0, 1.0};
+        if (len > 0.0) {
+            nn[0] = d[0] / len;
+            nn[1] = d[1] / len;
+            nn[2] = d[2] / len;
+        }
+        AlensBlock B;
+        std::memset(&B, 0, sizeof(B));
+        const double delta0 = len - x->linkRest[L];
+        B.delta0 = delta0;
+        B.gamma = -delta0 * x->linkKappa[L];
+        B.gidI = x->gid[I];
+        B.gidJ = x->gid[J];
+        B.globalIndexI = I;
+        B.globalIndexJ = J;
+        for (int cc = 0; cc < 3; cc++) {
+            B.normI[cc] = nn[cc];
+            B.normJ[cc] = -nn[cc];
+            B.posI[cc] = sI * aI[cc];
+            B.posJ[cc] = sJ * aJ[cc];
+            B.labI[cc] = pI[cc];
+            B.labJ[cc] = pI[cc] - d[cc];
+        }
+        B.bilateral = 1;
+        B.kappa = x->linkKappa[L];
+        x->blocks.push_back(B);
+    }
     x->nbil = (int)x->blocks.size();
     const int nc = x->ncoll + x->nbil;
     x->ci.assign(nc, -1);
@@ -1089,6 +1138,21 @@ int orc_add_bilateral(OrcCtx *x, int n, const AlensBlock *blocks) {
             return ALENS_INVALID_ARG;
     }
     x->queue.insert(x->queue.end(), blocks, blocks + n);
+    return ALENS_OK;
+}
+
+int orc_set_links(OrcCtx *x, int n, const int32_t *idxI, const int32_t *idxJ, const double *sI,
+                  const double *sJ, const double *rest, const double *kappa) {
+    if (!x || n < 0) return ALENS_INVALID_ARG;
+    for (int k = 0; k < n; k++)
+        if (idxI[k] < 0 || idxI[k] >= x->n || idxJ[k] < 0 || idxJ[k] >= x->n || !(kappa[k] > 0.0))
+            return ALENS_INVALID_ARG;
+    x->linkI.assign(idxI, idxI + n);
+    x->linkJ.assign(idxJ, idxJ + n);
+    x->linkSI.assign(sI, sI + n);
+    x->linkSJ.assign(sJ, sJ + n);
+    x->linkRest.assign(rest, rest + n);
+    x->linkKappa.assign(kappa, kappa + n);
     return ALENS_OK;
 }
 

@@ -342,3 +342,23 @@ def test_delassus_operator_bit_exact(gpu_lib):
     assert np.array_equal(opg["q"], q)
     assert np.all(opg["lb"][: opg["q"].shape[0] - len(blocks)] == 0.0)
     assert np.all(np.isneginf(opg["lb"][-len(blocks):]))
+
+
+def test_device_crosslinks(gpu_lib):
+    """Pre-bound crosslinkers: blocks built on the device every step equal
+    the oracle's, and the trajectory stays bit-identical."""
+    from alens_gb300.oracle_api import OracleSystem as Orc
+    w = workloads.crosslinked_bundle_rods(n=1500, box=5.0, seed=3)
+    pairs = workloads.pair_list(Orc, w.cfg, w.rods, 0.05)
+    links = workloads.make_links(w.cfg, w.rods, pairs, 3000, seed=1)
+    g, o = pair(w.cfg, w.rods)
+    g.set_links(links)
+    o.set_links(links)
+    for _ in range(4):
+        sg, so = g.step(), o.step()
+        assert sg["nBilateral"] == so["nBilateral"] == 3000
+        assert sg["iterations"] == so["iterations"]
+    compare_state(g, o)
+    cg, co = g.constraints(), o.constraints()
+    assert np.array_equal(cg["gamma"], co["gamma"])
+    assert np.array_equal(cg["delta0"], co["delta0"])
