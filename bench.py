@@ -151,9 +151,11 @@ def relaxed_state(w, pre_steps, make_sys):
     return RodState(w.rods.gid, pos, quat, w.rods.length, w.rods.radius)
 
 
-def run_arm(torch, stream, cfg, rods, warmup, steps, flush, e2e=False):
+def run_arm(torch, stream, cfg, rods, warmup, steps, flush, e2e=False, mark=False):
     """Time `steps` steps with CUDA events on the library stream; L2 flushed
-    (256 MB write) before every step, outside the timed interval."""
+    (256 MB write) before every step, outside the timed interval.  With
+    `mark`, the timed loop sits between cudaProfilerStart/Stop so that
+    `ncu --profile-from-start off` lists exactly its launches."""
     from alens_gb300 import capi
     cfg.stream = stream.cuda_stream
     sysg = capi.GpuSystem(cfg)
@@ -167,6 +169,9 @@ def run_arm(torch, stream, cfg, rods, warmup, steps, flush, e2e=False):
     l0 = sysg.launch_count()
     times, iters, refine, ncon, resid = [], [], [], [], []
     conv = True
+    if mark:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
     for _ in range(steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -186,6 +191,8 @@ def run_arm(torch, stream, cfg, rods, warmup, steps, flush, e2e=False):
         ncon.append(st["nCollision"] + st["nBilateral"])
         resid.append(st["residual"])
         conv = conv and bool(st["converged"])
+    if mark:
+        torch.cuda.profiler.stop()
     launches = sysg.launch_count() - l0
     sysg.close()
     return dict(ms=times, iters=iters, refine=refine, ncon=ncon, resid=resid, converged=conv,
@@ -224,6 +231,18 @@ def solver_roofline(torch, stream, cfg, rods, steps, peak):
             "refine_gbs": (ref_b / (ref_ms * 1e-3) / 1e9) if ref_ms > 0 else None}
 
 
+def solver_traffic():
+    """DRAM bytes (read + write) of one k_solve<float> launch on this
+    workload, from the committed ncu summary (profiles/k_solve_monolayer20k.md)."""
+    import re
+    p = os.path.join(ROOT, "profiles", "k_solve_monolayer20k.md")
+    try:
+        m = re.search(r"traffic_bytes_per_launch: (\d+)", open(p).read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
 def cpu_baseline(w_cfg, rods, seconds, threads):
     """The oracle (FP64, OpenMP) on the same relaxed workload, bounded to
     about `seconds` of CPU time."""
@@ -238,7 +257,7 @@ def cpu_baseline(w_cfg, rods, seconds, threads):
         o.step()
         n += 1
         el = time.perf_counter() - t0
-        if el >= seconds or n >= 200:
+        if el >= seconds:
             break
     o.close()
     return rods.n * n / el, n, el
@@ -350,7 +369,7 @@ def main():
     with Clocks(local) as clk:
         barrier()
         plain = run_arm(torch, stream, cfg_plain, rods, args.warmup, args.steps, flush)
-        fast = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush)
+        fast = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush, mark=True)
         e2e = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush, e2e=True)
         barrier()
     clocks = clk.summary()
@@ -378,13 +397,7 @@ def main():
         cv, csteps, cel = cpu_baseline(w.cfg, rods, args.cpu_seconds, threads)
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{csteps} FP64 oracle steps ({cel:.1f} s) of the same relaxed {nr}-rod layer"}
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "solver_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("bytes_per_launch_scaled")
-        except Exception:
-            traffic = None
+    traffic = solver_traffic()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum(fast["ms"]) / args.steps, "higher_is_better": True,
