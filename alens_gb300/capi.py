@@ -150,6 +150,10 @@ def _p(a, ctype):
 _PD = C.POINTER(C.c_double)
 _PI32 = C.POINTER(C.c_int32)
 _PI64 = C.POINTER(C.c_int64)
+_PF = C.POINTER(C.c_float)
+
+MLP_NUM_FEATURES = 12
+MLP_NUM_PARAMS = 5057
 
 _LIB = None
 
@@ -192,6 +196,20 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_launch_count": (C.c_int, [vp, _PI64]),
         "alens_get_last_error": (C.c_char_p, [vp]),
         "alens_get_stage_times": (C.c_int, [vp, _PD]),
+        "alens_mlp_create": (C.c_int, [C.c_uint64, C.c_int64, C.POINTER(vp)]),
+        "alens_mlp_destroy": (C.c_int, [vp]),
+        "alens_mlp_get_params": (C.c_int, [vp, _PF]),
+        "alens_mlp_set_params": (C.c_int, [vp, _PF]),
+        "alens_mlp_add_samples": (C.c_int, [vp, C.c_int, _PF, _PF]),
+        "alens_mlp_dataset_size": (C.c_int, [vp, _PI64]),
+        "alens_mlp_clear_dataset": (C.c_int, [vp]),
+        "alens_mlp_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_float, C.c_uint64, _PF]),
+        "alens_mlp_predict": (C.c_int, [vp, C.c_int, _PF, _PF]),
+        "alens_mlp_gradient": (C.c_int, [vp, C.c_int, _PF, _PF, _PF, _PF]),
+        "alens_attach_mlp": (C.c_int, [vp, vp]),
+        "alens_set_feature_capture": (C.c_int, [vp, C.c_int]),
+        "alens_mlp_collect": (C.c_int, [vp, vp, _PI64]),
+        "alens_get_features": (C.c_int, [vp, C.c_int, C.c_int, _PF, _PF, _PI32]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -416,7 +434,101 @@ class GpuSystem:
         self._ck(self.lib.alens_get_stage_times(self.h, _p(t, C.c_double)), "alens_get_stage_times")
         return t
 
+    # ---- learned warm start
+    def attach_mlp(self, mlp: "Mlp | None"):
+        self._ck(self.lib.alens_attach_mlp(self.h, mlp.h if mlp is not None else None), "alens_attach_mlp")
+        self._mlp = mlp  # keep the model alive while attached
+
+    def set_feature_capture(self, on: bool = True):
+        self._ck(self.lib.alens_set_feature_capture(self.h, int(bool(on))), "alens_set_feature_capture")
+
+    def collect(self, mlp: "Mlp") -> int:
+        """Append the last step's (features, converged multiplier) rows to
+        the model's dataset; returns the rows added."""
+        added = C.c_int64()
+        self._ck(self.lib.alens_mlp_collect(self.h, mlp.h, C.byref(added)), "alens_mlp_collect")
+        return added.value
+
+    def features(self, replica: int = 0):
+        """Features (n x 12) and overlap-unit scales A_kk/d (n) of the last
+        step's collision constraints, canonical order."""
+        nc, _ = self.num_constraints(replica)
+        f = np.empty((max(nc, 1), MLP_NUM_FEATURES), np.float32)
+        sc = np.empty(max(nc, 1), np.float32)
+        n = C.c_int32()
+        self._ck(self.lib.alens_get_features(self.h, replica, nc, _p(f, C.c_float), _p(sc, C.c_float),
+                                             C.byref(n)), "alens_get_features")
+        return f[: n.value], sc[: n.value]
+
     def stream_handle(self) -> int:
         s = C.c_void_p()
         self._ck(self.lib.alens_get_stream(self.h, C.byref(s)), "alens_get_stream")
         return s.value or 0
+
+
+class Mlp:
+    """The learned warm-start model (``AlensMlp``): BF16 12-64-64-1 SiLU
+    network trained with the library's tensor-core kernels and Adam."""
+
+    def __init__(self, seed: int = 0, capacity: int = 0, lib: C.CDLL | None = None):
+        self.lib = lib or load_library()
+        self.h = C.c_void_p()
+        _ck(self.lib.alens_mlp_create(int(seed) & 0xFFFFFFFFFFFFFFFF, int(capacity), C.byref(self.h)),
+            "alens_mlp_create")
+
+    def close(self):
+        if self.h:
+            self.lib.alens_mlp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        p = np.empty(MLP_NUM_PARAMS, np.float32)
+        _ck(self.lib.alens_mlp_get_params(self.h, _p(p, C.c_float)), "alens_mlp_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (MLP_NUM_PARAMS,)
+        _ck(self.lib.alens_mlp_set_params(self.h, _p(p, C.c_float)), "alens_mlp_set_params")
+
+    def add_samples(self, feat, target):
+        feat = np.ascontiguousarray(feat, dtype=np.float32).reshape(-1, MLP_NUM_FEATURES)
+        target = np.ascontiguousarray(target, dtype=np.float32).reshape(-1)
+        _ck(self.lib.alens_mlp_add_samples(self.h, feat.shape[0], _p(feat, C.c_float), _p(target, C.c_float)),
+            "alens_mlp_add_samples")
+
+    def dataset_size(self) -> int:
+        n = C.c_int64()
+        _ck(self.lib.alens_mlp_dataset_size(self.h, C.byref(n)), "alens_mlp_dataset_size")
+        return n.value
+
+    def clear_dataset(self):
+        _ck(self.lib.alens_mlp_clear_dataset(self.h), "alens_mlp_clear_dataset")
+
+    def train(self, epochs: int, batch: int = 65536, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
+        loss = np.zeros(max(epochs, 1), np.float32)
+        _ck(self.lib.alens_mlp_train(self.h, int(epochs), int(batch), float(lr), int(seed), _p(loss, C.c_float)),
+            "alens_mlp_train")
+        return loss[:epochs]
+
+    def predict(self, feat) -> np.ndarray:
+        feat = np.ascontiguousarray(feat, dtype=np.float32).reshape(-1, MLP_NUM_FEATURES)
+        out = np.empty(feat.shape[0], np.float32)
+        _ck(self.lib.alens_mlp_predict(self.h, feat.shape[0], _p(feat, C.c_float), _p(out, C.c_float)),
+            "alens_mlp_predict")
+        return out
+
+    def gradient(self, feat, target):
+        feat = np.ascontiguousarray(feat, dtype=np.float32).reshape(-1, MLP_NUM_FEATURES)
+        target = np.ascontiguousarray(target, dtype=np.float32).reshape(-1)
+        g = np.empty(MLP_NUM_PARAMS, np.float32)
+        loss = C.c_float()
+        _ck(self.lib.alens_mlp_gradient(self.h, feat.shape[0], _p(feat, C.c_float), _p(target, C.c_float),
+                                        _p(g, C.c_float), C.byref(loss)), "alens_mlp_gradient")
+        return g, loss.value

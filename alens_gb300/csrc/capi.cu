@@ -12,6 +12,10 @@ struct AlensCtx {
     std::string lastError;
 };
 
+struct AlensMlp {
+    alens::MlpModel *model;
+};
+
 namespace {
 
 template <class F>
@@ -216,6 +220,130 @@ int alens_get_operator(AlensCtx *ctx, int replica, int capNnz, int *nnz, int32_t
     if (!ctx) return ALENS_INVALID_ARG;
     return guarded_ctx(ctx, [&] {
         ctx->eng->getOperator(replica, capNnz, nnz, rowPtr, cols, vals, q, cinv, lowerBound, gamma0);
+        return (int)ALENS_OK;
+    });
+}
+
+// ------------------------------------------------------ learned warm start
+static_assert(alens::kMlpParams == ALENS_MLP_NUM_PARAMS, "parameter count");
+static_assert(alens::kMlpIn == ALENS_MLP_NUM_FEATURES, "feature count");
+
+int alens_mlp_create(uint64_t seed, int64_t datasetCapacity, AlensMlp **out) {
+    if (!out) return ALENS_INVALID_ARG;
+    *out = nullptr;
+    return guarded([&] {
+        AlensMlp *m = new AlensMlp{nullptr};
+        try {
+            m->model = new alens::MlpModel(seed, datasetCapacity);
+        } catch (...) {
+            delete m;
+            throw;
+        }
+        *out = m;
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_mlp_destroy(AlensMlp *mlp) {
+    if (!mlp) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        delete mlp->model;
+        delete mlp;
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_mlp_get_params(AlensMlp *mlp, float *params) {
+    if (!mlp || !params) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        mlp->model->getParams(params);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_mlp_set_params(AlensMlp *mlp, const float *params) {
+    if (!mlp || !params) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        mlp->model->setParams(params);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_mlp_add_samples(AlensMlp *mlp, int n, const float *features, const float *targets) {
+    if (!mlp) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        mlp->model->uploadDataset(features, targets, n);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_mlp_dataset_size(AlensMlp *mlp, int64_t *n) {
+    if (!mlp || !n) return ALENS_INVALID_ARG;
+    *n = mlp->model->datasetSize();
+    return ALENS_OK;
+}
+
+int alens_mlp_clear_dataset(AlensMlp *mlp) {
+    if (!mlp) return ALENS_INVALID_ARG;
+    mlp->model->clearDataset();
+    return ALENS_OK;
+}
+
+int alens_mlp_train(AlensMlp *mlp, int epochs, int batch, float lr, uint64_t seed, float *lossPerEpoch) {
+    if (!mlp) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        mlp->model->train(epochs, batch, lr, seed, lossPerEpoch);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_mlp_predict(AlensMlp *mlp, int n, const float *features, float *out) {
+    if (!mlp) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        mlp->model->predict(n, features, out);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_mlp_gradient(AlensMlp *mlp, int n, const float *features, const float *targets, float *grad,
+                       float *loss) {
+    if (!mlp) return ALENS_INVALID_ARG;
+    return guarded([&] {
+        mlp->model->gradient(n, features, targets, grad, loss);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_attach_mlp(AlensCtx *ctx, AlensMlp *mlp) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->attachMlp(mlp ? mlp->model : nullptr);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_set_feature_capture(AlensCtx *ctx, int enable) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->setFeatureCapture(enable != 0);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_mlp_collect(AlensCtx *ctx, AlensMlp *mlp, int64_t *added) {
+    if (!ctx || !mlp) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        const long long a = ctx->eng->collect(mlp->model);
+        if (added) *added = a;
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_features(AlensCtx *ctx, int replica, int cap, float *features, float *scale, int *n) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        const int m = ctx->eng->getFeatures(replica, cap, features, scale);
+        if (n) *n = m;
         return (int)ALENS_OK;
     });
 }

@@ -324,6 +324,14 @@ void Engine::allocConstraints(int cap, bool keepPrev) {
     S.conI = alloc<int>(G, cap);
     S.conJ = alloc<int>(G, cap);
     S.conImg = alloc<int>(G, cap);
+    S.conST = alloc<float2>(G, cap);
+    if (capture_) {
+        S.feat = alloc<float>(G, (size_t)kMlpIn * cap);
+        S.fscale = alloc<float>(G, cap);
+    } else {
+        S.feat = nullptr;
+        S.fscale = nullptr;
+    }
     S.jac = alloc<double>(G, 12 * (size_t)cap);
     S.W = alloc<double>(G, 12 * (size_t)cap);
     double **cd[] = {&S.phi0, &S.q, &S.gamma, &S.lb, &S.cinv};
@@ -554,7 +562,72 @@ int Engine::enqueueDetect() {
     n += 2;
     n += launch_rows(S, stream_);
     n += launch_assemble(S, stream_);
+    if (warm_ == ALENS_WARM_MLP && mlp_) {
+        launch_mlp_warm(S, mlp_->view(), stream_);
+        n += 1;
+    } else if (S.feat) {
+        launch_mlp_features(S, stream_);
+        n += 1;
+    }
     CK(cudaGetLastError());
+    return n;
+}
+
+// ------------------------------------------------------ learned warm start
+void Engine::attachMlp(MlpModel *m) {
+    CK(cudaStreamSynchronize(stream_));
+    invalidateGraph();
+    mlp_ = m;
+}
+
+void Engine::setFeatureCapture(bool on) {
+    if (on == capture_) return;
+    CK(cudaStreamSynchronize(stream_));
+    invalidateGraph();
+    capture_ = on;
+    captured_ = false;
+    if (!dirty_) {
+        // the constraint buffers are reallocated with (or without) the
+        // feature rows; warm-start keys of the last step are kept
+        allocConstraints(S_.cap, true);
+    }
+}
+
+// Appends the last completed step's collision constraints (features and
+// converged multipliers in overlap units) to the model's dataset.
+long long Engine::collect(MlpModel *m) {
+    if (!m) throw ApiError(ALENS_INVALID_ARG);
+    if (!captured_ || !S_.feat) throw ApiError(ALENS_NOT_READY);
+    long long total = 0;
+    for (int r = 0; r < R_; r++) {
+        const RepDyn &d = hDyn_[r];
+        const long long n = d.collEnd - d.collStart;
+        const long long add = m->reserve(n);
+        if (add <= 0) break;
+        launch_mlp_append(S_, d.conStart, (int)add, m->dsFeatAt(m->datasetSize()), m->dsLabelAt(m->datasetSize()),
+                          stream_);
+        CK(cudaGetLastError());
+        m->commitRows(add);
+        total += add;
+    }
+    CK(cudaStreamSynchronize(stream_));
+    return total;
+}
+
+int Engine::getFeatures(int rep, int cap, float *feat, float *scale) {
+    if (rep < 0 || rep >= R_) throw ApiError(ALENS_INVALID_ARG);
+    if (!captured_ || !S_.feat) throw ApiError(ALENS_NOT_READY);
+    const RepDyn &d = hDyn_[rep];
+    const int n = d.collEnd - d.collStart;
+    if (cap < n) throw ApiError(ALENS_CAPACITY);
+    if (n > 0) {
+        if (feat)
+            CK(cudaMemcpyAsync(feat, S_.feat + (size_t)kMlpIn * d.conStart, sizeof(float) * kMlpIn * n,
+                               cudaMemcpyDeviceToHost, stream_));
+        if (scale)
+            CK(cudaMemcpyAsync(scale, S_.fscale + d.conStart, sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
     return n;
 }
 
@@ -753,6 +826,7 @@ int Engine::step(AlensStepStats *out) {
         const int status = collectStats(2);
         if (status == ALENS_OK || status == ALENS_NOT_CONVERGED) {
             for (auto &q : queue_) q.clear();
+            captured_ = S_.feat != nullptr;
             stepCount_++;
             last_.step = stepCount_ - 1;
             prevCountHost_ = hCtl_->totalColl;
@@ -795,6 +869,7 @@ int Engine::advance(AlensStepStats *out) {
     launches_ += enqueueAdvance();
     readBack();
     for (auto &q : queue_) q.clear();
+    captured_ = S_.feat != nullptr;
     stepCount_++;
     prevCountHost_ = hCtl_->totalColl;
     haveDetect_ = haveSolve_ = false;

@@ -92,6 +92,9 @@ struct DevState {
     unsigned long long *rawKeys, *keys;
     // constraints
     int *conI, *conJ, *conImg;
+    float2 *conST;             // contact parameters (s / h_I, t / h_J) of collisions
+    float *feat, *fscale;      // learned warm start: 12 features and A_kk / d per
+                               // constraint (allocated while features are recorded)
     double *jac;
     double *phi0, *q, *gamma, *lb, *cinv, *lab;
     int *lbKind;               // 0: lb = 0, 1: bilateral, 2: general lb

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "mlp.h"
 
 namespace alens {
 
@@ -48,6 +49,13 @@ class Engine {
     void conStress(int rep, double *out9);
     void getOperator(int rep, int capNnz, int *nnz, int32_t *rowPtr, int32_t *cols, double *vals,
                      double *q, double *cinv, double *lowerBound, double *gamma0);
+    // learned warm start (kernels_mlp.cu): the attached model seeds the
+    // collision multipliers when warmStart == ALENS_WARM_MLP; with feature
+    // capture on, every step records the features of its constraints
+    void attachMlp(MlpModel *m);
+    void setFeatureCapture(bool on);
+    long long collect(MlpModel *m);
+    int getFeatures(int rep, int cap, float *feat, float *scale);
     long long stepCount() const { return stepCount_; }
     cudaStream_t stream() const { return stream_; }
     long long lastNeeded() const { return lastNeeded_; }
@@ -98,6 +106,9 @@ class Engine {
     int nClusters_ = 1;
     int prevCountHost_ = 0;  // valid warm-start keys on the device
     int solverGrid_ = 0;
+    MlpModel *mlp_ = nullptr;
+    bool capture_ = false;
+    bool captured_ = false;  // the last completed step recorded its features
     std::vector<HostRods> rods_;
     std::vector<std::vector<AlensBlock>> queue_;
     struct HostLinks {

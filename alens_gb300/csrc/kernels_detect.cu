@@ -604,6 +604,8 @@ __global__ void k_build(DevState S) {
         S.conI[k] = i;
         S.conJ[k] = j;
         S.conImg[k] = img;
+        S.conST[k] = make_float2(S.hcol[i] > 0.0 ? (float)(R.s / S.hcol[i]) : 0.0f,
+                                 S.hcol[j] > 0.0 ? (float)(R.t / S.hcol[j]) : 0.0f);
 #pragma unroll
         for (int d = 0; d < 3; d++) {
             S.lab[6 * (size_t)k + d] = R.P[d];

@@ -274,6 +274,71 @@ int alens_bbpgd_solve_noalloc(int n, const int32_t *rowPtr, const int32_t *cols,
                               int maxIte, void *stream, int *iterations,
                               double *residual, int *solveStatus);
 
+/* ---- Learned warm start ------------------------------------------------
+ * A 12 -> 64 -> 64 -> 1 SiLU network (BF16 weights, FP32 accumulation on
+ * the tensor cores) that predicts each collision constraint's initial
+ * multiplier for BBPGD.  SimToolbox's solver starts from the gamma stored
+ * in each ConstraintBlock (SRC/TubuleSystem.cpp:727-736, zero for
+ * collisions); with warmStart = ALENS_WARM_MLP and a model attached, the
+ * network supplies that start instead.  The solve still has to reach
+ * conResTol, so the prediction changes iteration counts, never the
+ * tolerance of the answer.  No counterpart in the reference.
+ *
+ * Features (per collision constraint, FP32): current separation, predicted
+ * end-of-step overlap and signed separation (from q = phi0 + dt D^T U), the
+ * cosine of the rod axes, both rod lengths, the contact parameters s/h_I
+ * and t/h_J, the constraint counts of both rods, the previous step's
+ * multiplier of the same pair and image, and the coupling-weighted
+ * predicted overlap of the neighbouring constraints; lengths in units of
+ * the pair's collision diameter, multipliers in "overlap units"
+ * u = gamma * A_kk / d (A_kk = diagonal of the Delassus operator).
+ * Parameters (ALENS_MLP_NUM_PARAMS floats): W1[64][12], b1[64],
+ * W2[64][64], b2[64], w3[64], b3, weights stored [out][in]. */
+#define ALENS_MLP_NUM_FEATURES 12
+#define ALENS_MLP_NUM_PARAMS 5057
+
+typedef struct AlensMlp AlensMlp;
+
+/* Model with seeded initial weights and room for datasetCapacity
+ * (feature, target) rows on the device. */
+int alens_mlp_create(uint64_t seed, int64_t datasetCapacity, AlensMlp **out);
+int alens_mlp_destroy(AlensMlp *mlp);
+/* FP32 master parameters (host arrays of ALENS_MLP_NUM_PARAMS floats);
+ * set also resets the Adam state. */
+int alens_mlp_get_params(AlensMlp *mlp, float *params);
+int alens_mlp_set_params(AlensMlp *mlp, const float *params);
+/* Dataset: rows added from host arrays (features[n*12], targets[n] in
+ * overlap units), current size, clear. */
+int alens_mlp_add_samples(AlensMlp *mlp, int n, const float *features, const float *targets);
+int alens_mlp_dataset_size(AlensMlp *mlp, int64_t *n);
+int alens_mlp_clear_dataset(AlensMlp *mlp);
+/* Adam (beta 0.9/0.999, eps 1e-8) on the mean squared error over the
+ * dataset, `epochs` passes in a seeded random order, minibatches of
+ * `batch` rows; lossPerEpoch[epochs] (nullable) receives each pass's mean
+ * loss.  Forward, backward and the update run in the library's kernels. */
+int alens_mlp_train(AlensMlp *mlp, int epochs, int batch, float lr, uint64_t seed, float *lossPerEpoch);
+/* Network outputs for n feature rows (host arrays). */
+int alens_mlp_predict(AlensMlp *mlp, int n, const float *features, float *out);
+/* Gradient of the mean squared error over n rows with respect to every
+ * parameter (grad[ALENS_MLP_NUM_PARAMS]) and the loss; no update. */
+int alens_mlp_gradient(AlensMlp *mlp, int n, const float *features, const float *targets, float *grad,
+                       float *loss);
+/* Use `mlp` (NULL detaches) for the warm start of this context's steps when
+ * warmStart = ALENS_WARM_MLP.  The model must outlive its attachment;
+ * training it while attached is allowed between steps. */
+int alens_attach_mlp(AlensCtx *ctx, AlensMlp *mlp);
+/* Record the features of every constraint during each step (needed by
+ * alens_mlp_collect and alens_get_features). */
+int alens_set_feature_capture(AlensCtx *ctx, int enable);
+/* Append the last step's collision constraints of every replica to the
+ * model's dataset: features and the converged multiplier in overlap units
+ * (stops at the dataset capacity); *added (nullable) receives the rows. */
+int alens_mlp_collect(AlensCtx *ctx, AlensMlp *mlp, int64_t *added);
+/* Features (features[12*n]) and overlap-unit scale A_kk/d (scale[n]) of the
+ * last step's collision constraints of one replica, canonical order;
+ * *n receives the count; ALENS_CAPACITY if cap < n. */
+int alens_get_features(AlensCtx *ctx, int replica, int cap, float *features, float *scale, int *n);
+
 /* Steps executed so far (SylinderSystem::getStepCount). */
 int alens_get_step_count(AlensCtx *ctx, int64_t *count);
 
