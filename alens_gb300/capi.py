@@ -210,6 +210,7 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_set_feature_capture": (C.c_int, [vp, C.c_int]),
         "alens_mlp_collect": (C.c_int, [vp, vp, _PI64]),
         "alens_get_features": (C.c_int, [vp, C.c_int, C.c_int, _PF, _PF, _PI32]),
+        "alens_autotune": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -433,6 +434,14 @@ class GpuSystem:
         t = np.zeros(5)
         self._ck(self.lib.alens_get_stage_times(self.h, _p(t, C.c_double)), "alens_get_stage_times")
         return t
+
+    def autotune(self, reps: int = 5) -> dict:
+        """Time the solver configurations on the next step's problem and keep
+        the fastest (the rods do not move); returns the report."""
+        import json
+        buf = C.create_string_buffer(16384)
+        self._ck(self.lib.alens_autotune(self.h, int(reps), buf, len(buf)), "alens_autotune")
+        return json.loads(buf.value.decode())
 
     # ---- learned warm start
     def attach_mlp(self, mlp: "Mlp | None"):

@@ -1,5 +1,6 @@
 // capi.cu - the C ABI of include/alens_gpu.h.  Every entry point converts
 // exceptions into status codes; nothing crosses the ABI as a C++ exception.
+#include <algorithm>
 #include <cstring>
 #include <new>
 
@@ -344,6 +345,19 @@ int alens_get_features(AlensCtx *ctx, int replica, int cap, float *features, flo
     return guarded_ctx(ctx, [&] {
         const int m = ctx->eng->getFeatures(replica, cap, features, scale);
         if (n) *n = m;
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_autotune(AlensCtx *ctx, int reps, char *report, int reportCap) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        const std::string js = ctx->eng->autotune(reps);
+        if (report && reportCap > 0) {
+            const size_t n = std::min<size_t>(js.size(), (size_t)reportCap - 1);
+            std::memcpy(report, js.data(), n);
+            report[n] = 0;
+        }
         return (int)ALENS_OK;
     });
 }

@@ -26,6 +26,10 @@ constexpr int kImageNone = 13;    // image code of the zero periodic shift
 constexpr int kErrOverflow = 1;
 constexpr int kErrNaN = 2;
 constexpr int kErrTimeout = 4;
+constexpr int kErrSolverFit = 8;  // the cluster-resident solver could not hold the
+                                  // problem; the host reruns the step in grid form
+// flags after which the solve and the update of a step are skipped
+constexpr int kErrStepAbort = kErrOverflow | kErrNaN | kErrTimeout | kErrSolverFit;
 
 // ------------------------------------------------------------------ math
 // Natural logarithm: x = m 2^e, m in [sqrt(1/2), sqrt(2)),

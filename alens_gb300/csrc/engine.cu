@@ -5,9 +5,11 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
+#include <string>
 #include <type_traits>
 
 namespace alens {
@@ -69,6 +71,11 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     // SMs share one system; cluster form for ensembles), 0 = grid form,
     // N = cluster form with clusters of N CTAs
     if (const char *e = std::getenv("ALENS_CLUSTER_SIZE")) clusterSize_ = atoi(e);
+    if (const char *e = std::getenv("ALENS_CSM_THREADS")) csm_set_threads(atoi(e));
+    if (const char *e = std::getenv("ALENS_SOLVER_FORM")) {
+        const std::string f(e);
+        formRequest_ = f == "grid" ? kFormGrid : (f == "cluster" ? kFormCluster : (f == "resident" ? kFormResident : -1));
+    }
     CK(cudaMallocHost(&hCtl_, sizeof(DevCtl)));
     CK(cudaMallocHost(&hDyn_, sizeof(RepDyn) * R_));
     CK(cudaMallocHost(&hBilPrefix_, sizeof(int) * (R_ + 1)));
@@ -573,6 +580,128 @@ int Engine::enqueueDetect() {
     return n;
 }
 
+// ------------------------------------------------------------- autotuner
+void Engine::applySolverConfig(int form, int clusterSize, int threads, int blocksPerSM) {
+    invalidateGraph();
+    solverBlocksPerSM_ = std::max(1, blocksPerSM);
+    solverGrid_ = std::min(solver_max_grid(precision_), numSM_ * solverBlocksPerSM_);
+    if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "solver occupancy");
+    solverForm_ = form;
+    clusterSize_ = form == kFormGrid ? 0 : clusterSize;
+    if (form == kFormResident) {
+        csm_set_threads(threads);
+        nClusters_ = R_;
+    } else if (form == kFormCluster) {
+        const int act = cluster_max_active(clusterSize);
+        nClusters_ = std::max(1, std::min(R_, act > 0 ? act : 1));
+    } else {
+        nClusters_ = 1;
+    }
+}
+
+std::string Engine::autotune(int reps) {
+    if (reps < 1) throw ApiError(ALENS_INVALID_ARG);
+    AlensStepStats st{};
+    const int rc = detect(&st);
+    if (rc != ALENS_OK) throw ApiError(rc);
+    // snapshot of the detected problem: every trial starts from it
+    const int nc = hCtl_->totalCon;
+    std::vector<void *> tmp;
+    auto snap = [&](const void *src, size_t bytes) {
+        void *p = nullptr;
+        CK(cudaMalloc(&p, std::max<size_t>(bytes, 1)));
+        tmp.push_back(p);
+        CK(cudaMemcpyAsync(p, src, bytes, cudaMemcpyDeviceToDevice, stream_));
+        return p;
+    };
+    void *sDyn = snap(S_.dyn, sizeof(RepDyn) * R_);
+    void *sCtl = snap(S_.ctl, sizeof(DevCtl));
+    void *sSt = snap(S_.st[1], sizeof(double2) * (size_t)nc);
+    void *sSt32 = precision_ == ALENS_PREC_MIXED ? snap(S_.st32[1], sizeof(float2) * (size_t)nc) : nullptr;
+    auto restore = [&]() {
+        CK(cudaMemcpyAsync(S_.dyn, sDyn, sizeof(RepDyn) * R_, cudaMemcpyDeviceToDevice, stream_));
+        CK(cudaMemcpyAsync(S_.ctl, sCtl, sizeof(DevCtl), cudaMemcpyDeviceToDevice, stream_));
+        CK(cudaMemcpyAsync(S_.st[1], sSt, sizeof(double2) * (size_t)nc, cudaMemcpyDeviceToDevice, stream_));
+        if (sSt32)
+            CK(cudaMemcpyAsync(S_.st32[1], sSt32, sizeof(float2) * (size_t)nc, cudaMemcpyDeviceToDevice, stream_));
+    };
+    struct Cand {
+        int form, cs, threads, bps;
+        double ms;
+        bool ok;
+    };
+    std::vector<Cand> cands;
+    for (int bps : {1, 2}) cands.push_back({kFormGrid, 0, 256, bps, 0.0, false});
+    if (precision_ == ALENS_PREC_MIXED) {
+        const int maxCs = cluster_max_size();
+        for (int cs : {16, 8, 4, 2})
+            if (cs <= maxCs) cands.push_back({kFormCluster, cs, 512, 1, 0.0, false});
+        const int csmMax = csm_cluster_size(nullptr);
+        for (int cs : {16, 8, 4, 2})
+            for (int th : {256, 512})
+                if (cs <= csmMax) cands.push_back({kFormResident, cs, th, 1, 0.0, false});
+    }
+    ensureEvents();
+    const int saveForm = solverForm_, saveCs = clusterSize_, saveBps = solverBlocksPerSM_, saveTh = csm_threads();
+    const int saveNcl = nClusters_, saveGrid = solverGrid_;
+    for (Cand &c : cands) {
+        applySolverConfig(c.form, c.cs, c.threads, c.bps);
+        std::vector<double> t;
+        bool ok = true;
+        for (int r = 0; r < reps + 1 && ok; r++) {
+            restore();
+            CK(cudaEventRecord(events_[0], stream_));
+            enqueueSolve(nullptr);
+            CK(cudaEventRecord(events_[1], stream_));
+            readBack();
+            if (hCtl_->errFlags & (kErrSolverFit | kErrTimeout | kErrNaN)) ok = false;
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, events_[0], events_[1]));
+            if (r > 0) t.push_back(ms);  // first run warms up
+        }
+        c.ok = ok && !t.empty();
+        if (c.ok) {
+            std::sort(t.begin(), t.end());
+            c.ms = t[t.size() / 2];
+        }
+    }
+    int best = -1;
+    for (size_t i = 0; i < cands.size(); i++)
+        if (cands[i].ok && (best < 0 || cands[i].ms < cands[best].ms)) best = (int)i;
+    if (best >= 0) {
+        const Cand &b = cands[best];
+        applySolverConfig(b.form, b.cs, b.threads, b.bps);
+    } else {
+        solverForm_ = saveForm;
+        clusterSize_ = saveCs;
+        solverBlocksPerSM_ = saveBps;
+        csm_set_threads(saveTh);
+        nClusters_ = saveNcl;
+        solverGrid_ = saveGrid;
+    }
+    restore();
+    CK(cudaStreamSynchronize(stream_));
+    for (void *p : tmp) cudaFree(p);
+    // the detected problem stands; the next step detects again (the step is
+    // repeatable: noise is keyed by the step index)
+    haveDetect_ = true;
+    haveSolve_ = false;
+    static const char *names[] = {"grid", "cluster", "resident"};
+    std::string js = "{\"constraints\": " + std::to_string(nc) + ", \"candidates\": [";
+    for (size_t i = 0; i < cands.size(); i++) {
+        const Cand &c = cands[i];
+        char buf[256];
+        snprintf(buf, sizeof(buf),
+                 "%s{\"form\": \"%s\", \"cluster\": %d, \"threads\": %d, \"blocks_per_sm\": %d, "
+                 "\"ms\": %s}",
+                 i ? ", " : "", names[c.form], c.cs, c.form == kFormResident ? c.threads : (c.form == kFormCluster ? 512 : 256),
+                 c.bps, c.ok ? std::to_string(c.ms).c_str() : "null");
+        js += buf;
+    }
+    js += "], \"chosen\": " + std::to_string(best) + "}";
+    return js;
+}
+
 // ------------------------------------------------------ learned warm start
 void Engine::attachMlp(MlpModel *m) {
     CK(cudaStreamSynchronize(stream_));
@@ -636,8 +765,34 @@ void Engine::ensureSolverGrid() {
     const int maxg = solver_max_grid(precision_);
     solverGrid_ = std::min(maxg, numSM_ * solverBlocksPerSM_);
     if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "solver occupancy");
-    if (clusterSize_ < 0 && R_ == 1) clusterSize_ = 0;
-    if (precision_ == ALENS_PREC_MIXED && clusterSize_ != 0) {
+    solverForm_ = kFormGrid;
+    if (precision_ != ALENS_PREC_MIXED) return;
+    // FP32 solver form.  Measured on GB300 (20,000-rod layer, ~21,000
+    // constraints): grid 9.6 us per pass, cluster-resident 14 us (random
+    // 8-byte distributed-shared-memory gathers sustain ~0.4 loads per cycle
+    // per SM), cluster with global iterates 16 us; so the grid form is the
+    // default and the cluster forms are chosen on request (autotuner)
+    const int csmCs = csm_cluster_size(nullptr);
+    const bool residentOk = csmCs > 0 && !residentFailed_;
+    if (formRequest_ == kFormResident && residentOk) {
+        int cs = clusterSize_ > 0 ? std::min(clusterSize_, csmCs) : csmCs;
+        // ensembles: clusters of 4 CTAs, as many as can be co-resident
+        if (R_ > 1 && clusterSize_ <= 0) cs = std::min(cs, 4);
+        // clusters never wait on one another: one per replica, the hardware
+        // schedules them as SMs free up
+        solverForm_ = kFormResident;
+        clusterSize_ = cs;
+        nClusters_ = R_;
+        return;
+    }
+    if (formRequest_ == kFormGrid) {
+        clusterSize_ = 0;
+        return;
+    }
+    if (formRequest_ == kFormCluster && clusterSize_ == 0) clusterSize_ = -1;
+    if (clusterSize_ < 0 && R_ == 1 && formRequest_ != kFormCluster) clusterSize_ = 0;
+    if (clusterSize_ != 0) {
+        solverForm_ = kFormCluster;
         const int maxCs = cluster_max_size();
         int cs = clusterSize_ > 0 ? std::min(clusterSize_, maxCs) : maxCs;
         // ensembles: one cluster per replica, at most the co-resident count
@@ -653,7 +808,7 @@ void Engine::ensureSolverGrid() {
 int Engine::enqueueSolve(cudaEvent_t *ev) {
     ensureSolverGrid();
     int n = 0;
-    CK(launch_solve(S_, solverGrid_, precision_, kBarrierTimeoutNs, stream_, ev, &n,
+    CK(launch_solve(S_, solverGrid_, precision_, kBarrierTimeoutNs, stream_, ev, &n, solverForm_,
                     clusterSize_ > 0 ? clusterSize_ : 0, nClusters_));
     return n;
 }
@@ -729,6 +884,18 @@ bool Engine::handleOverflow() {
         return true;
     }
     throw ApiError(ALENS_CAPACITY);
+}
+
+// A step that outgrew the cluster-resident solver: use the grid form from
+// now on for this context.  Returns true if the step must be rerun.
+bool Engine::handleSolverFit() {
+    if (!(hCtl_->errFlags & kErrSolverFit)) return false;
+    CK(cudaStreamSynchronize(stream_));
+    invalidateGraph();
+    residentFailed_ = true;
+    solverGrid_ = 0;
+    clusterSize_ = -1;
+    return true;
 }
 
 int Engine::collectStats(int stage) {
@@ -822,6 +989,7 @@ int Engine::step(AlensStepStats *out) {
         }
         readBack();
         if (handleOverflow()) continue;
+        if (handleSolverFit()) continue;
         if (stageTiming_ && !launched) recordStageTimes();
         const int status = collectStats(2);
         if (status == ALENS_OK || status == ALENS_NOT_CONVERGED) {
@@ -858,6 +1026,12 @@ int Engine::solve(AlensStepStats *out) {
     if (!haveDetect_) throw ApiError(ALENS_NOT_READY);
     launches_ += enqueueSolve(nullptr);
     readBack();
+    if (handleSolverFit()) {
+        // the detect results are intact: clear the flag and solve in grid form
+        CK(cudaMemsetAsync(&S_.ctl->errFlags, 0, sizeof(int), stream_));
+        launches_ += enqueueSolve(nullptr);
+        readBack();
+    }
     const int status = collectStats(1);
     haveSolve_ = (status == ALENS_OK || status == ALENS_NOT_CONVERGED);
     if (out) *out = last_;

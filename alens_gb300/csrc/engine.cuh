@@ -51,7 +51,8 @@ struct RepDyn {
     int counter;              // last-arriver ticket of the current pass
     int refineIter;
     int finalPar;             // solver buffer holding this replica's result
-    int pad;
+    int refined;              // 1: the cluster-resident solver verified the FP32
+                              // solution's FP64 residual (no refinement needed)
     double alpha, res;
 };
 
@@ -147,13 +148,22 @@ void launch_pack_rods(const DevState &S, int rodOffset, int n, int what, cudaStr
 // ---- solve / advance (kernels_solve.cu)
 constexpr int kMaxSolverGrid = 152 * 8;  // work space is sized for this
 int solver_max_grid(int precision);  // cooperative residency limit
+// Forms of the FP32 (mixed-precision) solver
+enum SolverForm {
+    kFormGrid = 0,      // cooperative grid over all SMs, software grid barrier
+    kFormCluster = 1,   // one cluster per replica, iterates in global memory
+    kFormResident = 2   // one cluster per replica, problem held in shared memory
+};
 // precision == MIXED: FP32 kernel, state reset, FP64 refinement kernel
 // (events ev[0..3] recorded around the two kernels when non-null).
-// clusterSize > 0 selects the cluster form of the FP32 solver.
 cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned long long timeout_ns,
-                         cudaStream_t st, cudaEvent_t *ev, int *launches, int clusterSize, int nClusters);
+                         cudaStream_t st, cudaEvent_t *ev, int *launches, int form, int clusterSize,
+                         int nClusters);
 int cluster_max_size();            // largest cluster the FP32 solver can use
 int cluster_max_active(int cs);    // co-resident clusters of that size
+int csm_cluster_size(int *maxActive);  // cluster-resident form: largest cluster, 0 if unusable
+void csm_set_threads(int threads);     // cluster-resident form: threads per CTA (256/512/1024)
+int csm_threads();
 void launch_advance(const DevState &S, cudaStream_t st);
 void launch_stress(const DevState &S, cudaStream_t st);
 

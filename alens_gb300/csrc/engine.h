@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "engine.cuh"
@@ -56,6 +57,9 @@ class Engine {
     void setFeatureCapture(bool on);
     long long collect(MlpModel *m);
     int getFeatures(int rep, int cap, float *feat, float *scale);
+    // Times the solver configurations on this step's detected problem and
+    // keeps the fastest; returns a JSON report.  The rods do not move.
+    std::string autotune(int reps);
     long long stepCount() const { return stepCount_; }
     cudaStream_t stream() const { return stream_; }
     long long lastNeeded() const { return lastNeeded_; }
@@ -88,6 +92,8 @@ class Engine {
     void invalidateGraph();
     void readBack();
     bool handleOverflow();
+    bool handleSolverFit();
+    void applySolverConfig(int form, int clusterSize, int threads, int blocksPerSM);
     int collectStats(int stage);
     void freeGroup(std::vector<void *> &g);
     template <class T>
@@ -104,6 +110,9 @@ class Engine {
     int solverBlocksPerSM_ = 1;
     int clusterSize_ = -1;   // FP32 solver: -1 automatic, 0 grid form, N cluster size
     int nClusters_ = 1;
+    int solverForm_ = -1;    // SolverForm of the FP32 solver (-1: not chosen yet)
+    int formRequest_ = -1;   // ALENS_SOLVER_FORM override (-1 automatic)
+    bool residentFailed_ = false;  // a step did not fit the cluster-resident form
     int prevCountHost_ = 0;  // valid warm-start keys on the device
     int solverGrid_ = 0;
     MlpModel *mlp_ = nullptr;

@@ -502,6 +502,7 @@ __global__ void k_ranges(DevState S) {
             tile += d.nTiles;
             d.iter = 0;
             d.refineIter = 0;
+            d.refined = 0;
             d.active = d.nCon > 0 ? 1 : 0;
             d.converged = d.nCon > 0 ? 0 : 1;
             d.status = 0;

@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_solve_cluster(DevState S, S
     const int nClusters = (int)gridDim.x / CS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __shared__ ClusterShared sh;
-    const bool skip = (ld_volatile_i32(&S.ctl->errFlags) & (kErrOverflow | kErrNaN | kErrTimeout)) != 0;
+    const bool skip = (ld_volatile_i32(&S.ctl->errFlags) & kErrStepAbort) != 0;
     for (int r = cid; r < S.R && !skip; r += nClusters) {
         const RepDyn &d = S.dyn[r];
         const RepParams &P = S.par[r];

@@ -16,7 +16,7 @@ __device__ __forceinline__ int flags(const DevState &S) { return ld_volatile_i32
 // Start of the FP64 refinement: gamma0 = the FP32 solution, solver state
 // re-armed; the FP32 iteration count is kept in refineIter.
 __global__ void k_refine_setup(DevState S) {
-    if (flags(S) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
+    if (flags(S) & kErrStepAbort) return;
     const int par = S.ctl->finalParity;
     __syncthreads();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -24,6 +24,12 @@ __global__ void k_refine_setup(DevState S) {
             RepDyn &d = S.dyn[r];
             d.refineIter = d.iter;
             d.iter = 0;
+            if (d.refined) {
+                // FP64 residual already verified: the FP64 pass copies the
+                // replica's values through (status, residual kept)
+                d.active = 0;
+                continue;
+            }
             d.active = d.nCon > 0 ? 1 : 0;
             d.converged = d.nCon > 0 ? 0 : 1;
             d.status = 0;
@@ -55,7 +61,7 @@ __global__ void k_solver_arm(DevState S) {
 }
 
 __global__ void k_solver_finish(DevState S) {
-    if (flags(S) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
+    if (flags(S) & kErrStepAbort) return;
     const int par = S.ctl->finalParity;
     const int nc = S.ctl->totalCon;
     const double2 *src = par ? S.st[1] : S.st[0];
@@ -64,7 +70,7 @@ __global__ void k_solver_finish(DevState S) {
 }
 
 __global__ void k_advance(DevState S) {
-    if (flags(S) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
+    if (flags(S) & kErrStepAbort) return;
     const size_t st = (size_t)S.nRods;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const int rep = S.rodRep[r];
@@ -235,6 +241,8 @@ cudaError_t launch_coop(const DevState &S, const SolveView<Real> &V, int grid,
 cudaError_t launch_solve_fp32(const DevState &S, int grid, unsigned long long timeout_ns, cudaStream_t st);
 cudaError_t launch_solve_fp32_cluster(const DevState &S, int clusterSize, int nClusters, cudaStream_t st);
 int solver_max_grid_fp32();
+// defined in kernels_csm.cu
+cudaError_t launch_solve_fp32_csm(const DevState &S, int clusterSize, int nClusters, cudaStream_t st);
 
 int solver_max_grid(int precision) {
     int g = occupancy_grid((const void *)k_solve<double>);
@@ -246,7 +254,8 @@ int solver_max_grid(int precision) {
 }
 
 cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned long long timeout_ns,
-                         cudaStream_t st, cudaEvent_t *ev, int *launches, int clusterSize, int nClusters) {
+                         cudaStream_t st, cudaEvent_t *ev, int *launches, int form, int clusterSize,
+                         int nClusters) {
     int n = 0;
     cudaError_t e;
     SolveView<double> V{};
@@ -260,8 +269,12 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
     V.fp64 = 1;
     if (ev) cudaEventRecord(ev[0], st);
     if (precision == ALENS_PREC_MIXED) {
-        e = clusterSize > 0 ? launch_solve_fp32_cluster(S, clusterSize, nClusters, st)
-                            : launch_solve_fp32(S, grid, timeout_ns, st);
+        if (form == kFormResident)
+            e = launch_solve_fp32_csm(S, clusterSize, nClusters, st);
+        else if (form == kFormCluster)
+            e = launch_solve_fp32_cluster(S, clusterSize, nClusters, st);
+        else
+            e = launch_solve_fp32(S, grid, timeout_ns, st);
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[1], st);
         k_refine_setup<<<256, 256, 0, st>>>(S);

@@ -192,9 +192,10 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
     const RepParams &P = S.par[r];
     if (p == 0) {
         if (threadIdx.x == 0) {
-            sh.mode[slot] = kModeG0;
+            const bool done = d.refined != 0;
+            sh.mode[slot] = done ? kModeCopy : kModeG0;
             sh.alpha[slot] = 0.0;
-            if (d.nCon > 0 && d.tileStart >= t0 && d.tileStart < t1) atomicAdd(&S.ctl->activeCnt[0], 1);
+            if (!done && d.nCon > 0 && d.tileStart >= t0 && d.tileStart < t1) atomicAdd(&S.ctl->activeCnt[0], 1);
         }
         __syncthreads();
         return;
@@ -402,7 +403,7 @@ template <class Real>
 __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<Real> V,
                                                          unsigned long long timeout_ns) {
     __shared__ SolveShared sh;
-    if (ld_volatile_i32(&S.ctl->errFlags) & (kErrOverflow | kErrNaN | kErrTimeout)) return;
+    if (ld_volatile_i32(&S.ctl->errFlags) & kErrStepAbort) return;
     const unsigned int nb = gridDim.x;
     const int nTiles = S.ctl->nTiles;
     const int tpb = (nTiles + (int)nb - 1) / (int)nb;

