@@ -26,7 +26,8 @@ int solver_max_grid_fp32() {
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve<float>, kSolveThreads, 0);
+    cudaFuncSetAttribute(k_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSolveDynSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve<float>, kSolveThreads, kSolveDynSmem);
     return nsm * (per > 0 ? per : 0);
 }
 
@@ -43,6 +44,7 @@ cudaError_t launch_solve_fp32(const DevState &S, int grid, unsigned long long ti
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kSolveThreads);
+    cfg.dynamicSmemBytes = kSolveDynSmem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -95,7 +97,8 @@ __global__ void __launch_bounds__(kClusterThreads) k_solve_cluster(DevState S, S
             float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, am = 0.0f;
             for (int i = lo + (int)threadIdx.x; i < hi; i += kClusterThreads) {
                 float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f, rm = 0.0f;
-                row_update<float>(V, d.conStart + i, mode, alpha, stIn, stOut, v0, v1, v2, rm, &S.ctl->errFlags);
+                row_update<float>(V, d.conStart + i, mode, alpha, stIn, stOut, v0, v1, v2, rm, &S.ctl->errFlags,
+                                  RowCache{});
                 a0 += v0;
                 a1 += v1;
                 a2 += v2;

@@ -216,7 +216,8 @@ int occupancy_grid(const void *kernel) {
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kSolveThreads, 0);
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSolveDynSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kSolveThreads, kSolveDynSmem);
     return nsm * (per > 0 ? per : 0);
 }
 
@@ -226,6 +227,7 @@ cudaError_t launch_coop(const DevState &S, const SolveView<Real> &V, int grid,
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kSolveThreads);
+    cfg.dynamicSmemBytes = kSolveDynSmem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

@@ -159,9 +159,16 @@ __device__ __forceinline__ long long warp_max_bits(long long v) {
 __device__ inline double warp_max_of(const double *src, int m) {
     const int lane = threadIdx.x & 31;
     long long mx = __double_as_longlong(-2.0);
-    for (int i = lane; i < m; i += 32) {
-        const long long b = __double_as_longlong(__ldcg(src + i));
-        mx = b > mx ? b : mx;
+    // all loads of a 1024-partial chunk are issued before the compares
+    for (int c = 0; c < m; c += kChunk) {
+        long long b[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int i = c + lane + 32 * j;
+            b[j] = i < m ? __double_as_longlong(__ldcg(src + i)) : mx;
+        }
+#pragma unroll
+        for (int j = 0; j < 32; j++) mx = b[j] > mx ? b[j] : mx;
     }
     mx = warp_max_bits(mx);
     return __longlong_as_double(mx);
@@ -188,10 +195,15 @@ struct SolveShared {
 template <class Real>
 __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r, int t0, int t1,
                        SolveShared &sh, int slot) {
-    const RepDyn &d = S.dyn[r];
-    const RepParams &P = S.par[r];
+    // fields that do not change while the solver runs go through the
+    // read-only cache (hits after the first pass)
+    const RepDyn *dr = S.dyn + r;
+    const int dTileStart = __ldg(&dr->tileStart), dNTiles = __ldg(&dr->nTiles);
+    const double Ptol = __ldg(&S.par[r].tol);
+    const int PmaxIte = __ldg(&S.par[r].maxIte);
     if (p == 0) {
         if (threadIdx.x == 0) {
+            const RepDyn &d = *dr;
             const bool done = d.refined != 0;
             sh.mode[slot] = done ? kModeCopy : kModeG0;
             sh.alpha[slot] = 0.0;
@@ -203,13 +215,16 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
     const int par = (p - 1) & 1;
     const size_t tc = (size_t)S.tileCap;
     const double *base = S.part + (size_t)par * 4 * tc;
+    // the previous step size (written before the last barrier), loaded
+    // while the partials are reduced
+    const double alphaPrev = (threadIdx.x == 0 && p > 2) ? __ldcg(V.alphaBuf + (size_t)((p - 1) & 1) * S.R + r) : 0.0;
     // warps 0-2: the three dot products, warp 3: the residual max
     const int warp = threadIdx.x >> 5;
     if (warp < 3) {
-        const double v = warp_chunk_sum(base + (size_t)warp * tc + d.tileStart, d.nTiles, sh.chunk[warp]);
+        const double v = warp_chunk_sum(base + (size_t)warp * tc + dTileStart, dNTiles, sh.chunk[warp]);
         if ((threadIdx.x & 31) == 0) sh.red[warp] = v;
     } else if (warp == 3) {
-        const double v = warp_max_of(base + 3 * tc + d.tileStart, d.nTiles);
+        const double v = warp_max_of(base + 3 * tc + dTileStart, dNTiles);
         if ((threadIdx.x & 31) == 0) sh.red[3] = v;
     }
     __syncthreads();
@@ -217,7 +232,11 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
         const double sums[3] = {sh.red[0], sh.red[1], sh.red[2]};
         const double mx = sh.red[3];
         if (threadIdx.x == 0) {
-        const bool owner = d.tileStart >= t0 && d.tileStart < t1;
+        const struct {
+            double tol;
+            int maxIte;
+        } P{Ptol, PmaxIte};
+        const bool owner = dTileStart >= t0 && dTileStart < t1;
         int mode = kModeCopy;
         double alpha = 0.0;
         int status = -1, iter = 0;
@@ -245,7 +264,7 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
             } else if (mx <= P.tol) {
                 status = ALENS_OK;
             } else {
-                alpha = __ldcg(V.alphaBuf + (size_t)((p - 1) & 1) * S.R + r);
+                alpha = alphaPrev;
                 const double ss = sums[0], sy = sums[1], yy = sums[2];
                 if (sy > 0.0) {
                     const double a = (itp & 1) ? ss / sy : sy / yy;
@@ -278,6 +297,21 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
     __syncthreads();
 }
 
+// Operator rows of one block cached in shared memory for the whole solve
+// (the rows a block owns do not change between passes): entries
+// [entBase, entBase + nEnt) and row pointers of rows [rowBase, rowBase +
+// nRow].  Entries or rows outside are read from global memory.
+struct RowCache {
+    const int4 *ent;
+    const int *rptr;
+    int entBase, nEnt;
+    int rowBase, nRow;
+};
+
+constexpr int kRowCacheRows = 1024;                  // row pointers cached per block
+constexpr int kSolveDynSmem = 64 * 1024;             // dynamic shared memory of k_solve
+constexpr int kRowCacheEnts = (kSolveDynSmem - 4 * (kRowCacheRows + 4)) / 16;
+
 // Update of constraint k at pass p in `mode`: reads the previous iterates,
 // forms x_k and (A x)_k, writes the new iterates, returns the dot-product
 // terms (v0, v1, v2) and the residual term.  Row k always holds its own
@@ -285,7 +319,8 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
 template <class Real>
 __device__ __forceinline__ void row_update(const SolveView<Real> &V, int k, int mode, Real alpha,
                                            const typename Vec2<Real>::T *stIn, typename Vec2<Real>::T *stOut,
-                                           Real &v0, Real &v1, Real &v2, Real &rmax, int *errFlags) {
+                                           Real &v0, Real &v1, Real &v2, Real &rmax, int *errFlags,
+                                           const RowCache &C) {
     using V2 = typename Vec2<Real>::T;
     if (mode == kModeCopy) {
         stOut[k] = ldcg(stIn + k);
@@ -294,12 +329,17 @@ __device__ __forceinline__ void row_update(const SolveView<Real> &V, int k, int 
     const V2 qc = __ldg(V.qc + k);
     Real acc = Real(0);
     Real gam = Real(0), gold = Real(0), lbk = Real(0), xk = Real(0);
-    const int e0 = __ldg(V.aptr + k), e1 = __ldg(V.aptr + k + 1);
+    const int kr = k - C.rowBase;
+    const bool rc = kr >= 0 && kr < C.nRow;
+    const int e0 = rc ? C.rptr[kr] : __ldg(V.aptr + k), e1 = rc ? C.rptr[kr + 1] : __ldg(V.aptr + k + 1);
     for (int eb = e0; eb < e1; eb += kRowPrefetch) {
         int4 ent[kRowPrefetch];
 #pragma unroll
-        for (int j = 0; j < kRowPrefetch; j++)
-            ent[j] = eb + j < e1 ? __ldg(V.aent + eb + j) : make_int4(k, 1, 0, 0);
+        for (int j = 0; j < kRowPrefetch; j++) {
+            const int ce = eb + j - C.entBase;
+            ent[j] = eb + j < e1 ? ((ce >= 0 && ce < C.nEnt) ? C.ent[ce] : __ldg(V.aent + eb + j))
+                                 : make_int4(k, 1, 0, 0);
+        }
         V2 sv[kRowPrefetch];
 #pragma unroll
         for (int j = 0; j < kRowPrefetch; j++)
@@ -365,14 +405,15 @@ __device__ __forceinline__ void row_update(const SolveView<Real> &V, int k, int 
 // One 64-constraint tile processed by a 64-thread group (two warps).
 template <class Real>
 __device__ void process_tile(const DevState &S, const SolveView<Real> &V, int p, int T, int mode,
-                             Real alpha, SolveShared &sh, int group) {
+                             Real alpha, SolveShared &sh, int group, const RowCache &C) {
     const int lane64 = threadIdx.x & 63;
     const int warpInGroup = (threadIdx.x >> 5) & 1;
     const int r = __ldg(S.tileRep + T);
-    const RepDyn &d = S.dyn[r];
-    const int local = (T - d.tileStart) * kRowTile + lane64;
-    const bool valid = local < d.nCon;
-    const int k = d.conStart + local;
+    // constraint range of the replica: fixed while the solver runs
+    const RepDyn *d = S.dyn + r;
+    const int local = (T - __ldg(&d->tileStart)) * kRowTile + lane64;
+    const bool valid = local < __ldg(&d->nCon);
+    const int k = __ldg(&d->conStart) + local;
     // select the ping-pong buffers without indexing the parameter arrays
     // (a runtime index would copy the view to local memory)
     const bool odd = (p & 1) != 0;
@@ -381,7 +422,7 @@ __device__ void process_tile(const DevState &S, const SolveView<Real> &V, int p,
     V2 *const stOut = odd ? V.st[1] : V.st[0];
     Real v0 = Real(0), v1 = Real(0), v2 = Real(0);
     Real rmax = mode == kModeCopy ? Real(-1) : Real(0);
-    if (valid) row_update<Real>(V, k, mode, alpha, stIn, stOut, v0, v1, v2, rmax, &S.ctl->errFlags);
+    if (valid) row_update<Real>(V, k, mode, alpha, stIn, stOut, v0, v1, v2, rmax, &S.ctl->errFlags, C);
     // warp trees in Real (modes that need them), tile = warp0 + warp1 in
     // FP64; the max through integer bit patterns
     Real w0 = Real(0), w1 = Real(0), w2 = Real(0);
@@ -403,12 +444,36 @@ template <class Real>
 __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<Real> V,
                                                          unsigned long long timeout_ns) {
     __shared__ SolveShared sh;
+    extern __shared__ int4 dynCache[];
     if (ld_volatile_i32(&S.ctl->errFlags) & kErrStepAbort) return;
     const unsigned int nb = gridDim.x;
     const int nTiles = S.ctl->nTiles;
     const int tpb = (nTiles + (int)nb - 1) / (int)nb;
     const int t0 = min((int)blockIdx.x * tpb, nTiles);
     const int t1 = min(t0 + tpb, nTiles);
+    // this block's operator rows, cached for every pass: the rows of tiles
+    // [t0, t1) are one contiguous range of constraints
+    RowCache C{};
+    {
+        int* rptr = reinterpret_cast<int *>(dynCache + kRowCacheEnts);
+        C.ent = dynCache;
+        C.rptr = rptr;
+        if (t0 < t1) {
+            const RepDyn &da = S.dyn[__ldg(S.tileRep + t0)];
+            const RepDyn &db = S.dyn[__ldg(S.tileRep + t1 - 1)];
+            const int rowBeg = da.conStart + (t0 - da.tileStart) * kRowTile;
+            const int rowEnd = min(db.conStart + (t1 - db.tileStart) * kRowTile, db.conStart + db.nCon);
+            const int eBeg = __ldg(V.aptr + rowBeg), eEnd = __ldg(V.aptr + rowEnd);
+            C.entBase = eBeg;
+            C.nEnt = min(eEnd - eBeg, kRowCacheEnts);
+            C.rowBase = rowBeg;
+            C.nRow = rowEnd - rowBeg <= kRowCacheRows ? rowEnd - rowBeg : 0;
+            for (int e = threadIdx.x; e < C.nEnt; e += blockDim.x) dynCache[e] = __ldg(V.aent + eBeg + e);
+            if (C.nRow > 0)
+                for (int i = threadIdx.x; i <= C.nRow; i += blockDim.x) rptr[i] = __ldg(V.aptr + rowBeg + i);
+        }
+        __syncthreads();
+    }
     const int maxPass = S.ctl->maxIte + 3;
     const size_t tc = (size_t)S.tileCap;
     const int group = threadIdx.x >> 6;
@@ -439,7 +504,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
                 const int Tg = base + group;
                 if (Tg < Tend) {
                     const int slot = __ldg(S.tileRep + Tg) - rFirst;
-                    process_tile<Real>(S, V, p, Tg, sh.mode[slot], (Real)sh.alpha[slot], sh, group);
+                    process_tile<Real>(S, V, p, Tg, sh.mode[slot], (Real)sh.alpha[slot], sh, group, C);
                 }
                 __syncthreads();
                 if (threadIdx.x < 4 && base + (int)threadIdx.x < Tend) {
