@@ -8,7 +8,8 @@ slab of thickness 0.1 um, von Mises kappa = 5 about x; seeded synthetic
 data).  Two GPU forms run from the same relaxed state:
   plain : FP64 solve, zero initial gamma
   fast  : FP32-bulk / FP64-reduction solve with FP64 refinement, warm start
-          from the previous step's gamma  (the reported `value`)
+          from the learned network (trained in the untimed set-up on FP64
+          runs; the reported `value`)
 
 `value` is device time (CUDA events on the library's stream, L2 flushed
 between steps, inputs resident in HBM).  `e2e` runs the same steps through
@@ -52,6 +53,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="bounded CPU-oracle sample for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mlp-samples", type=int, default=2_000_000,
+                    help="training rows of the learned warm start")
+    ap.add_argument("--mlp-epochs", type=int, default=20)
+    ap.add_argument("--no-extras", action="store_true", help="skip the other workload shapes")
+    ap.add_argument("--extra-steps", type=int, default=10)
     ap.add_argument("--profile-case", action="store_true",
                     help="print per-stage CUDA-event times of both solver forms (direct launches) "
                          "for profiling; no JSON line")
@@ -151,15 +157,23 @@ def relaxed_state(w, pre_steps, make_sys):
     return RodState(w.rods.gid, pos, quat, w.rods.length, w.rods.radius)
 
 
-def run_arm(torch, stream, cfg, rods, warmup, steps, flush, e2e=False, mark=False):
+def run_arm(torch, stream, cfg, rods, warmup, steps, flush, e2e=False, mark=False, mlp=None, links=None,
+            tune=False):
     """Time `steps` steps with CUDA events on the library stream; L2 flushed
     (256 MB write) before every step, outside the timed interval.  With
     `mark`, the timed loop sits between cudaProfilerStart/Stop so that
-    `ncu --profile-from-start off` lists exactly its launches."""
+    `ncu --profile-from-start off` lists exactly its launches.  `mlp` is
+    attached for the learned warm start; `tune` runs the solver autotuner
+    before the warm-up."""
     from alens_gb300 import capi
     cfg.stream = stream.cuda_stream
     sysg = capi.GpuSystem(cfg)
     sysg.set_rods(rods)
+    if links is not None:
+        sysg.set_links(links)
+    if mlp is not None:
+        sysg.attach_mlp(mlp)
+    tuned = sysg.autotune(reps=3) if tune else None
     n = rods.n
     pos_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     quat_h = torch.empty((n, 4), dtype=torch.float64, pin_memory=True).numpy()
@@ -196,10 +210,10 @@ def run_arm(torch, stream, cfg, rods, warmup, steps, flush, e2e=False, mark=Fals
     launches = sysg.launch_count() - l0
     sysg.close()
     return dict(ms=times, iters=iters, refine=refine, ncon=ncon, resid=resid, converged=conv,
-                launches=launches)
+                launches=launches, tuned=tuned)
 
 
-def solver_roofline(torch, stream, cfg, rods, steps, peak):
+def solver_roofline(torch, stream, cfg, rods, steps, peak, mlp=None):
     """Per-launch time of the main BBPGD kernel from the library's stage
     events (direct launches) and its algorithmic bytes."""
     from alens_gb300 import capi, workloads
@@ -207,6 +221,8 @@ def solver_roofline(torch, stream, cfg, rods, steps, peak):
     c.stream = stream.cuda_stream
     sysg = capi.GpuSystem(c)
     sysg.set_rods(rods)
+    if mlp is not None:
+        sysg.attach_mlp(mlp)
     sysg.step()
     nr = rods.n
     s = 4 if cfg.precision == capi.PREC_MIXED else 8
@@ -299,20 +315,185 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------- other workloads
+def gamma_error(cfg_a, cfg_b, rods, mlp=None, links=None):
+    """One step of two forms from the same state: relative L2 distance of
+    their multipliers, the largest position difference after the step, and
+    both solves' distance to a tightly converged FP64 solution (tolerance
+    1e-10) of the same problem."""
+    from alens_gb300 import capi, workloads
+
+    def one(cfg, attach=False):
+        g = capi.GpuSystem(cfg)
+        g.set_rods(rods)
+        if links is not None:
+            g.set_links(links)
+        if attach and mlp is not None:
+            g.attach_mlp(mlp)
+        st = g.step()
+        gam = g.constraints()["gamma"]
+        pos, _ = g.get_rods()
+        g.close()
+        return gam, pos, st
+
+    ga, pa, _ = one(cfg_a)
+    gb, pb, stb = one(cfg_b, attach=True)
+    gt, _, _ = one(workloads.config_with(cfg_a, conResTol=1e-10, conMaxIte=100000))
+    rel = lambda x, y: float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+    return {"gamma_rel_l2_vs_fp64": rel(gb, ga), "pos_max_abs_diff_um": float(np.max(np.abs(pb - pa))),
+            "fp64_gamma_rel_l2_vs_tight": rel(ga, gt), "fast_gamma_rel_l2_vs_tight": rel(gb, gt),
+            "fast_residual": float(stb["residual"])}
+
+
+def timed_steps(torch, stream, make, steps, flush):
+    """Device time of `steps` steps of the system made by `make()` (CUDA
+    events on the library stream, L2 flushed before each step)."""
+    g = make()
+    g.step()
+    ms, iters = [], []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = g.step()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        iters.append(st["iterations"])
+        if st["converged"] != 1:
+            raise RuntimeError(f"step did not converge: {st}")
+    g.close()
+    return float(np.sum(ms)), float(np.mean(iters))
+
+
+def other_workloads(torch, stream, flush, mlp, steps):
+    """The other benchmark shapes, briefly: rod-steps/s of the plain FP64 and
+    the fast (mixed precision + learned warm start) forms, iterations per
+    step, and the fast form's multiplier error against the FP64 solve."""
+    from alens_gb300 import capi, warmstart, workloads
+    out = {}
+
+    def relax(w, n, links=None):
+        g = capi.GpuSystem(w.cfg)
+        g.set_rods(w.rods)
+        if links is not None:
+            g.set_links(links)
+        for _ in range(n):
+            g.step()
+        pos, quat = g.get_rods()
+        g.close()
+        return capi.RodState(w.rods.gid, pos, quat, w.rods.length, w.rods.radius)
+
+    def maker(cfg, rods, links=None, attach=False):
+        def make():
+            c = workloads.config_with(cfg)
+            c.stream = stream.cuda_stream
+            g = capi.GpuSystem(c)
+            g.set_rods(rods)
+            if links is not None:
+                g.set_links(links)
+            if attach:
+                g.attach_mlp(mlp)
+            return g
+        return make
+
+    def pair_of_forms(name, w, rods, links=None, nsteps=steps):
+        plain = workloads.config_with(w.cfg, precision=capi.PREC_FP64, warmStart=capi.WARM_ZERO)
+        fast = workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_MLP)
+        tp, ip = timed_steps(torch, stream, maker(plain, rods, links), nsteps, flush)
+        tf, itf = timed_steps(torch, stream, maker(fast, rods, links, attach=True), nsteps, flush)
+        r = {"rods": rods.n, "steps": nsteps,
+             "plain_fp64_rod_steps_per_s": rods.n * nsteps / (tp * 1e-3),
+             "fast_rod_steps_per_s": rods.n * nsteps / (tf * 1e-3),
+             "plain_iterations_per_step": ip, "fast_iterations_per_step": itf,
+             "speedup_fast_vs_plain": tp / tf}
+        r.update(gamma_error(plain, fast, rods, mlp=mlp, links=links))
+        out[name] = r
+
+    # plain method, small: 1,000 rods in a 5 um periodic cube
+    w1 = workloads.small_periodic(n=1000, box=5.0, seed=0)
+    pair_of_forms("periodic_1000_rods_5um_cube", w1, relax(w1, 5))
+    # 3D crosslinked bundle: 50,000 rods, 200,000 pre-bound crosslinkers
+    w3 = workloads.crosslinked_bundle_rods(n=50000, box=20.0, seed=0)
+    pairs = workloads.pair_list(capi.GpuSystem, w3.cfg, w3.rods, 0.05)
+    links = workloads.make_links(w3.cfg, w3.rods, pairs, 200000, seed=1)
+    rods3 = relax(w3, 5, links)
+    pair_of_forms("bundle_50000_rods_200000_links", w3, rods3, links=links)
+    out["bundle_50000_rods_200000_links"]["near_pairs_within_0.05um"] = int(pairs[0].shape[0])
+    # learned warm start at scale: 200,000 rods in a 40 um cube
+    w4 = workloads.large_eval(n=200000, box=40.0, seed=0)
+    rods4 = relax(w4, 3)
+    r4 = {}
+    for lab, warm, prec, attach in (("zero_fp64", capi.WARM_ZERO, capi.PREC_FP64, False),
+                                    ("previous_gamma_fp64", capi.WARM_PREV, capi.PREC_FP64, False),
+                                    ("learned_fp64", capi.WARM_MLP, capi.PREC_FP64, True),
+                                    ("learned_mixed", capi.WARM_MLP, capi.PREC_MIXED, True)):
+        cfg = workloads.config_with(w4.cfg, warmStart=warm, precision=prec)
+        t, it = timed_steps(torch, stream, maker(cfg, rods4, attach=attach), steps, flush)
+        r4[lab] = {"iterations_per_step": it, "ms_per_step": t / steps}
+    out["eval_200000_rods_40um_cube"] = r4
+    # batched ensemble: 64 replicas in one launch sequence vs 64 sequential systems
+    reps = workloads.ensemble(nrep=64, nmin=500, nmax=8000, seed=0)
+    reps_rods = [relax(w, 3) for w in reps]
+    cfgs = [workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_MLP) for w in reps]
+    for c in cfgs:
+        c.stream = stream.cuda_stream
+    nr = sum(r.n for r in reps_rods)
+
+    def make_ens():
+        g = capi.GpuSystem(cfgs)
+        for i, r in enumerate(reps_rods):
+            g.set_rods(r, replica=i)
+        g.attach_mlp(mlp)
+        make_ens.tuned = g.autotune(reps=3)
+        return g
+    te, ite = timed_steps(torch, stream, make_ens, steps, flush)
+    singles = [maker(cfgs[i], reps_rods[i], attach=True)() for i in range(len(reps))]
+    for g in singles:
+        g.step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        for g in singles:
+            g.step()
+    e1.record(stream)
+    e1.synchronize()
+    ts = e0.elapsed_time(e1)
+    for g in singles:
+        g.close()
+    chosen = make_ens.tuned["candidates"][make_ens.tuned["chosen"]] if make_ens.tuned["chosen"] >= 0 else None
+    out["ensemble_64_replicas"] = {
+        "rods_total": nr, "replica_rods_min": min(r.n for r in reps_rods),
+        "replica_rods_max": max(r.n for r in reps_rods), "steps": steps,
+        "one_context_rod_steps_per_s": nr * steps / (te * 1e-3),
+        "sequential_64_contexts_rod_steps_per_s": nr * steps / (ts * 1e-3),
+        "speedup_vs_sequential": ts / te, "max_iterations_per_step": ite,
+        "autotuned_solver": chosen}
+    return out
+
+
 def profile_case(args):
     """Direct-launch steps with stage timing: per-stage ms and ms per BBPGD
     pass for both forms (the command profiled under ncu)."""
     import torch
     from alens_gb300 import capi, workloads
+    from alens_gb300 import warmstart
     w = workload(args, 0)
     rods = relaxed_state(w, args.pre_steps, capi.GpuSystem)
     stream = torch.cuda.Stream()
+    mlp, _ = warmstart.build_model(samples=500_000, epochs=10, seed=0)
     for name, prec, warm in (("plain_fp64", capi.PREC_FP64, capi.WARM_ZERO),
-                             ("mixed_warm", capi.PREC_MIXED, capi.WARM_PREV)):
+                             ("mixed_warm", capi.PREC_MIXED, capi.WARM_MLP)):
         c = workloads.config_with(w.cfg, precision=prec, warmStart=warm, stageTiming=1, useGraph=0)
         c.stream = stream.cuda_stream
         g = capi.GpuSystem(c)
         g.set_rods(rods)
+        if warm == capi.WARM_MLP:
+            g.attach_mlp(mlp)
         g.step()
         acc = np.zeros(5)
         passes = 0
@@ -329,6 +510,12 @@ def profile_case(args):
                           "blocks_per_sm": os.environ.get("ALENS_SOLVER_BLOCKS_PER_SM", "default")}),
               flush=True)
         g.close()
+
+
+def _chosen(rep):
+    if not rep or rep.get("chosen", -1) < 0:
+        return None
+    return rep["candidates"][rep["chosen"]]
 
 
 def main():
@@ -357,8 +544,13 @@ def main():
     stream = torch.cuda.Stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     rods = relaxed_state(w, args.pre_steps, capi.GpuSystem)
+    # learned warm start: FP64 runs of 20,000-rod config-1-shaped systems
+    # give the (features, converged multiplier) pairs; the library's own
+    # tensor-core kernels train the network (untimed set-up)
+    from alens_gb300 import warmstart
+    mlp, mlp_info = warmstart.build_model(samples=args.mlp_samples, epochs=args.mlp_epochs, seed=0)
     cfg_plain = workloads.config_with(w.cfg, precision=capi.PREC_FP64, warmStart=capi.WARM_ZERO)
-    cfg_fast = workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_PREV)
+    cfg_fast = workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_MLP)
 
     def barrier():
         torch.cuda.synchronize()
@@ -368,9 +560,11 @@ def main():
 
     with Clocks(local) as clk:
         barrier()
-        plain = run_arm(torch, stream, cfg_plain, rods, args.warmup, args.steps, flush)
-        fast = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush, mark=True)
-        e2e = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush, e2e=True)
+        plain = run_arm(torch, stream, cfg_plain, rods, args.warmup, args.steps, flush, tune=True)
+        fast = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush, mark=True, mlp=mlp,
+                       tune=True)
+        e2e = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush, e2e=True, mlp=mlp,
+                      tune=True)
         barrier()
     clocks = clk.summary()
 
@@ -389,7 +583,7 @@ def main():
             dist.destroy_process_group()
         return
     peak, peak_kind = measured_peaks()
-    roof_fast = solver_roofline(torch, stream, cfg_fast, rods, 10, peak)
+    roof_fast = solver_roofline(torch, stream, cfg_fast, rods, 10, peak, mlp=mlp)
     roof_plain = solver_roofline(torch, stream, cfg_plain, rods, 10, peak)
     cpu = None
     if not args.no_cpu_baseline:
@@ -398,13 +592,15 @@ def main():
         cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{csteps} FP64 oracle steps ({cel:.1f} s) of the same relaxed {nr}-rod layer"}
     traffic = solver_traffic()
+    extras = None if args.no_extras else other_workloads(torch, stream, flush, mlp, args.extra_steps)
+    err = gamma_error(cfg_plain, cfg_fast, rods, mlp=mlp)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum(fast["ms"]) / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk / f64 dots+residual+refine",
         "data": "synthetic (seeded)",
         "config": {"workload": w.name, "rods": nr, "box_um": [args.side, args.side, 0.1],
-                   "pre_steps": args.pre_steps, "form": "mixed precision + previous-gamma warm start",
+                   "pre_steps": args.pre_steps, "form": "mixed precision + learned warm start",
                    "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": f"replicas x{world}"},
         "plain_fp64": {"value": plain_value, "ms_per_step": sum(plain["ms"]) / args.steps,
@@ -415,6 +611,13 @@ def main():
                  "max_residual": float(np.max(fast["resid"])), "converged": fast["converged"],
                  "constraints_per_step": float(np.mean(fast["ncon"]))},
         "speedup_fast_vs_plain": value / plain_value,
+        "fast_vs_fp64_error": err,
+        "learned_warm_start": {"samples": mlp_info["samples"], "generated_from": "FP64 runs, 4 seeded "
+                               "20,000-rod periodic cubes at the 1,000-rods-in-5^3-um density",
+                               "generate_s": mlp_info["generate"]["seconds"],
+                               "train": mlp_info["train"]},
+        "autotuned_solver": {"plain": _chosen(plain["tuned"]), "fast": _chosen(fast["tuned"])},
+        "other_workloads": extras,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nr * 7 * 8,
                 "d2h_bytes_per_step": nr * 7 * 8 + 64},
         "roofline": {"bound": "hbm", "achieved": roof_fast["achieved"], "peak": peak, "unit": "GB/s",
