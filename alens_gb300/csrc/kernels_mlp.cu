@@ -78,9 +78,13 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
         }
     }
     if (!(akk > 0.0) || !(d > 0.0)) return false;
+    // the previous step's multiplier of this key: the constraint build
+    // already looked it up for the warm-start modes (gamma0 = max(0, prev))
     double gprev = 0.0;
     const int prevN = *S.prevCount;
-    if (prevN > 0) {
+    if (S.warm != ALENS_WARM_ZERO) {
+        gprev = S.gamma[k];
+    } else if (prevN > 0) {
         const int rep = S.rodRep[I];
         const unsigned long long key = S.keys[k - S.bilPrefix[rep]];
         int lo = 0, hi = prevN;

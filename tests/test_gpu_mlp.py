@@ -92,6 +92,11 @@ def test_features_match_oracle(gpu_lib):
     g.set_rods(w.rods)
     o.set_rods(w.rods)
     g.set_feature_capture(True)
+    # the warm-start modes take the previous multiplier from the constraint
+    # build instead of their own search: same features
+    gp = capi.GpuSystem(workloads.config_with(w.cfg, warmStart=capi.WARM_PREV))
+    gp.set_rods(w.rods)
+    gp.set_feature_capture(True)
     prev = None
     for step in range(3):
         pos, quat = o.get_rods()
@@ -107,8 +112,18 @@ def test_features_match_oracle(gpu_lib):
         prev = {(int(a), int(b), int(c)): float(gm) for a, b, c, gm in
                 zip(con2["i"], con2["j"], con2["image"], con2["gamma"])}
         o.advance()
+        pg, qg = g.get_rods()
+        gp.update_rods(pg, qg)
         g.step()
         F, S = g.features()
+        gp.step()
+        Fp, Sp = gp.features()
+        # same state; the previous multipliers differ only at the solver
+        # tolerance (the two systems solved their last step from different
+        # starts)
+        assert np.array_equal(Sp, S)
+        assert np.array_equal(np.delete(Fp, 10, axis=1), np.delete(F, 10, axis=1))
+        assert np.max(np.abs(Fp[:, 10] - F[:, 10])) <= 1e-2 * max(1.0, float(np.max(np.abs(F[:, 10]))))
         assert F.shape == Fr.shape
         np.testing.assert_allclose(S, Sr, rtol=1e-5)
         tol = 1e-4 * np.maximum(1.0, np.abs(Fr))
