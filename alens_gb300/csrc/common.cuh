@@ -547,4 +547,55 @@ __device__ inline bool grid_sync(GridBarrier *bar, unsigned int nblocks, int *er
     return s_ok != 0;
 }
 
+// Barrier ending pass p of the BBPGD kernel.  The generation word counts
+// barriers in its upper bits (gen >> 1 = barriers completed since the
+// solver was armed, target = p + 1) and carries in bit 0 whether the pass
+// left every replica retired: the last block to arrive reads the pass's
+// active count (every arrival's increments are visible to it through the
+// acq_rel chain on the counter) and publishes both in one release, so the
+// other blocks learn "continue or stop" from the same load that releases
+// them.  Bounded like grid_sync.
+__device__ inline bool grid_sync_pass(GridBarrier *bar, unsigned int nblocks, int *err,
+                                      unsigned long long timeout_ns, unsigned int target,
+                                      const int *activeCnt, int &stop) {
+    __shared__ int s_ok, s_stop;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1, st = 0;
+        const unsigned int arrived = atom_add_acqrel_u32(&bar->count, 1u);
+        if (arrived == nblocks - 1) {
+            st_relaxed_u32(&bar->count, 0u);
+            st = ld_acquire_u32(reinterpret_cast<const unsigned int *>(activeCnt)) == 0u ? 1 : 0;
+            atom_add_release_u32(&bar->gen, 2u + (unsigned int)st);
+        } else {
+            unsigned long long t0 = 0;
+            unsigned int spins = 0;
+            unsigned int g;
+            while (((g = ld_acquire_u32(&bar->gen)) >> 1) < target) {
+                if (++spins > 64) {
+                    __nanosleep(spins > 1024 ? 256 : 32);
+                    if ((spins & 255) == 0) {
+                        if (t0 == 0) t0 = global_ns();
+                        if (ld_volatile_i32(err) & kErrTimeout) {
+                            ok = 0;
+                            break;
+                        }
+                        if (global_ns() - t0 > timeout_ns) {
+                            atomicOr(err, kErrTimeout);
+                            ok = 0;
+                            break;
+                        }
+                    }
+                }
+            }
+            st = (int)(g & 1u);
+        }
+        s_ok = ok;
+        s_stop = st;
+    }
+    __syncthreads();
+    stop = s_stop;
+    return s_ok != 0;
+}
+
 }  // namespace alens

@@ -119,10 +119,15 @@ __device__ inline double warp_chunk_sum(const double *src, int m, double *chunk)
             const int i = c * kChunk + lane + 32 * j;
             v[j] = i < m ? __ldcg(src + i) : 0.0;
         }
+        // only this lane's valid partials are added (same order as before):
+        // each FP64 add of a full warp occupies the SM's FP64 pipe for 16
+        // cycles on GB300
         double acc = 0.0;
 #pragma unroll
-        for (int j = 0; j < 32; j++)
+        for (int j = 0; j < 32; j++) {
+            if (c * kChunk + 32 * j >= m) break;  // uniform across the warp
             if (c * kChunk + lane + 32 * j < m) acc = acc + v[j];
+        }
         acc = warp_tree_sum_t<double>(acc);
         if (lane == 0) chunk[c] = acc;
     }
@@ -188,6 +193,9 @@ struct SolveShared {
     double alpha[kWindow];
     int mode[kWindow];
     double tileVal[4][2][4];  // [group][warp][kind]
+#ifdef ALENS_TRACE
+    long long trRed;
+#endif
 };
 
 // Decision of replica r at pass p from the pass p-1 partials; identical in
@@ -228,6 +236,9 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
         if ((threadIdx.x & 31) == 0) sh.red[3] = v;
     }
     __syncthreads();
+#ifdef ALENS_TRACE
+    if (threadIdx.x == 0) sh.trRed = clock64();
+#endif
     {
         const double sums[3] = {sh.red[0], sh.red[1], sh.red[2]};
         const double mx = sh.red[3];
@@ -333,6 +344,8 @@ __device__ __forceinline__ void row_update(const SolveView<Real> &V, int k, int 
     const bool rc = kr >= 0 && kr < C.nRow;
     const int e0 = rc ? C.rptr[kr] : __ldg(V.aptr + k), e1 = rc ? C.rptr[kr + 1] : __ldg(V.aptr + k + 1);
     for (int eb = e0; eb < e1; eb += kRowPrefetch) {
+        // entries from the block's shared-memory copy when cached; all
+        // neighbour iterates of the batch are requested before any is used
         int4 ent[kRowPrefetch];
 #pragma unroll
         for (int j = 0; j < kRowPrefetch; j++) {
@@ -343,7 +356,7 @@ __device__ __forceinline__ void row_update(const SolveView<Real> &V, int k, int 
         V2 sv[kRowPrefetch];
 #pragma unroll
         for (int j = 0; j < kRowPrefetch; j++)
-            if (eb + j < e1) sv[j] = ldcg(stIn + ent[j].x);
+            if (eb + j < e1) sv[j] = stIn[ent[j].x];  // L1-cacheable: rows of a block share neighbours
 #pragma unroll
         for (int j = 0; j < kRowPrefetch; j++) {
             if (eb + j < e1) {
@@ -480,11 +493,15 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
     int lastPass = 0;
 #ifdef ALENS_TRACE
     unsigned long long trDecide = 0, trTiles = 0, trBar = 0, trT0 = 0, trT1 = 0;
+    long long cA = 0, cSum[6] = {0, 0, 0, 0, 0, 0};
 #endif
     for (int p = 0; p <= maxPass; p++) {
 #ifdef ALENS_TRACE
         trT0 = global_ns();
         trT1 = 0;
+        cA = clock64();
+        long long cDec = 0, cRow = 0, cStore = 0;
+        sh.trRed = 0;
 #endif
         if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl->activeCnt[(p + 1) % 3] = 0;
         double *partBase = S.part + (size_t)(p & 1) * 4 * tc;
@@ -496,6 +513,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
             for (int r = rFirst; r <= rLast; r++) decide<Real>(S, V, p, r, t0, t1, sh, r - rFirst);
 #ifdef ALENS_TRACE
             if (trT1 == 0) trT1 = global_ns();
+            if (cDec == 0) cDec = clock64();
 #endif
             // tiles of the window, four per round
             int Tend = T;
@@ -506,6 +524,9 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
                     const int slot = __ldg(S.tileRep + Tg) - rFirst;
                     process_tile<Real>(S, V, p, Tg, sh.mode[slot], (Real)sh.alpha[slot], sh, group, C);
                 }
+#ifdef ALENS_TRACE
+                if (cRow == 0) cRow = clock64();
+#endif
                 __syncthreads();
                 if (threadIdx.x < 4 && base + (int)threadIdx.x < Tend) {
                     const int g = threadIdx.x;
@@ -524,15 +545,31 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
 #ifdef ALENS_TRACE
         const unsigned long long trT2 = global_ns();
         if (trT1 == 0) trT1 = trT2;
+        cStore = clock64();
 #endif
-        if (!grid_sync(&S.ctl->bar, nb, &S.ctl->errFlags, timeout_ns)) return;
+        int stop = 0;
+        if (!grid_sync_pass(&S.ctl->bar, nb, &S.ctl->errFlags, timeout_ns, (unsigned int)(p + 1),
+                            &S.ctl->activeCnt[p % 3], stop))
+            return;
 #ifdef ALENS_TRACE
         const unsigned long long trT3 = global_ns();
         trDecide += trT1 - trT0;
         trTiles += trT2 - trT1;
         trBar += trT3 - trT2;
+        {
+            const long long cE = clock64();
+            const long long red = sh.trRed ? sh.trRed : cA;
+            if (cDec && cRow && p > 2) {
+                cSum[0] += red - cA;        // partial reductions
+                cSum[1] += cDec - red;      // decision
+                cSum[2] += cRow - cDec;     // row updates
+                cSum[3] += cStore - cRow;   // tile partial stores + syncs
+                cSum[4] += cE - cStore;     // barrier
+                cSum[5] += 1;
+            }
+        }
 #endif
-        if (ldcg(&S.ctl->activeCnt[p % 3]) == 0) break;
+        if (stop) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         S.ctl->finalParity = lastPass & 1;
@@ -540,9 +577,12 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
     }
 #ifdef ALENS_TRACE
     if (threadIdx.x == 0 && (blockIdx.x == 0 || blockIdx.x == gridDim.x / 2 || blockIdx.x == gridDim.x - 1))
-        printf("trace block %d passes %d: decide %.2f us, tiles %.2f us, barrier %.2f us per pass (tiles %d)\n",
+        printf("trace block %d passes %d: decide %.2f us, tiles %.2f us, barrier %.2f us per pass (tiles %d) | "
+               "cycles/pass: reduce %lld decide %lld rows %lld store %lld barrier %lld\n",
                blockIdx.x, lastPass + 1, 1e-3 * trDecide / (lastPass + 1), 1e-3 * trTiles / (lastPass + 1),
-               1e-3 * trBar / (lastPass + 1), t1 - t0);
+               1e-3 * trBar / (lastPass + 1), t1 - t0, cSum[5] ? cSum[0] / cSum[5] : 0LL,
+               cSum[5] ? cSum[1] / cSum[5] : 0LL, cSum[5] ? cSum[2] / cSum[5] : 0LL,
+               cSum[5] ? cSum[3] / cSum[5] : 0LL, cSum[5] ? cSum[4] / cSum[5] : 0LL);
 #endif
 }
 
