@@ -188,6 +188,7 @@ void Engine::makeParams(int rep, const HostRods &h, RepParams &P) const {
     P.mono = c.monolayer ? 1 : 0;
     P.maxIte = c.conMaxIte;
     P.nRods = h.n;
+    P.halfReachMax = 0.5 * mx;
 }
 
 void Engine::finalize() {

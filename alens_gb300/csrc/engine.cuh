@@ -40,6 +40,7 @@ struct RepParams {
     int nRods;
     int maxIte;
     int pad;
+    double halfReachMax;  // max over rods of collision half-length + radius
 };
 
 // per-replica state produced on the device

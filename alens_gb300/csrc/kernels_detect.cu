@@ -405,9 +405,19 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
             // the neighbour cell's origin relative to ours
             const float3 off = make_float3((float)ox * (float)P.cellsz[0], (float)oy * (float)P.cellsz[1],
                                            (float)oz * (float)P.cellsz[2]);
+            // skip the whole cell when its box lies beyond any partner's reach
+            // (exact: every rod centre of that cell is at least this far)
+            {
+                const float csx = (float)P.cellsz[0], csy = (float)P.cellsz[1], csz = (float)P.cellsz[2];
+                const float bx = fmaxf(fmaxf(off.x - ci.x, ci.x - (off.x + csx)), 0.0f);
+                const float by = fmaxf(fmaxf(off.y - ci.y, ci.y - (off.y + csy)), 0.0f);
+                const float bz = fmaxf(fmaxf(off.z - ci.z, ci.z - (off.z + csz)), 0.0f);
+                const float thr = hi_ + ri + (float)P.halfReachMax + cutHi + kScreenMargin;
+                if (bx * bx + by * by + bz * bz > thr * thr) ok = false;
+            }
             const int cell = P.cellOffset + (z * ny + y) * nx + xx;
-            const int m1 = S.cellStart[cell + 1];
-            for (int m = S.cellStart[cell]; m < m1; m++) {
+            const int m1 = ok ? S.cellStart[cell + 1] : 0;
+            for (int m = ok ? S.cellStart[cell] : 0; m < m1; m++) {
                 const int j = S.sidx[m];
                 if (j < i) continue;
                 if (j == i && img <= kImageNone) continue;

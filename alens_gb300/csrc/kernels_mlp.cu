@@ -58,32 +58,34 @@ __device__ __forceinline__ float dsiluf_(float a) {
 // Features of constraint k; false when k is not a collision constraint or
 // its operator diagonal is not positive (immovable rods).
 __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], float &scale) {
+    // FP32 arithmetic on the FP64 state (the FP64 pipe of GB300 issues two
+    // lanes per cycle per SM; the features only need FP32)
 #pragma unroll
     for (int c = 0; c < kMlpInPad; c++) f[c] = 0.0f;
     scale = 0.0f;
     if (S.conImg[k] < 0) return false;
     const int I = S.conI[k], J = S.conJ[k];
-    const double q = S.q[k];
-    const double d = S.rcol[I] + S.rcol[J];
-    double akk = 0.0, nb = 0.0;
+    const float q = (float)S.q[k];
+    const float d = (float)S.rcol[I] + (float)S.rcol[J];
+    float akk = 0.0f, nb = 0.0f;
     const int e0 = S.aptr[k], e1 = S.aptr[k + 1];
     for (int e = e0; e < e1; e++) {
         const int4 en = __ldg(S.aent + e);
-        const double v = __hiloint2double(en.w, en.z);
+        const float v = (float)__hiloint2double(en.w, en.z);
         if (en.x == k) {
             akk = v;
         } else if (en.y == 0) {
-            const double ql = S.q[en.x];
-            if (ql < 0.0) nb += v * (-ql);
+            const float ql = (float)S.q[en.x];
+            if (ql < 0.0f) nb = fmaf(v, -ql, nb);
         }
     }
-    if (!(akk > 0.0) || !(d > 0.0)) return false;
+    if (!(akk > 0.0f) || !(d > 0.0f)) return false;
     // the previous step's multiplier of this key: the constraint build
     // already looked it up for the warm-start modes (gamma0 = max(0, prev))
-    double gprev = 0.0;
+    float gprev = 0.0f;
     const int prevN = *S.prevCount;
     if (S.warm != ALENS_WARM_ZERO) {
-        gprev = S.gamma[k];
+        gprev = (float)S.gamma[k];
     } else if (prevN > 0) {
         const int rep = S.rodRep[I];
         const unsigned long long key = S.keys[k - S.bilPrefix[rep]];
@@ -95,24 +97,25 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
             else
                 hi = mid;
         }
-        if (lo < prevN && S.prevKeys[lo] == key) gprev = S.prevGamma[lo];
+        if (lo < prevN && S.prevKeys[lo] == key) gprev = (float)S.prevGamma[lo];
     }
-    const double cosab = S.ax[I] * S.ax[J] + S.ay[I] * S.ay[J] + S.az[I] * S.az[J];
+    const float cosab = (float)S.ax[I] * (float)S.ax[J] + (float)S.ay[I] * (float)S.ay[J] +
+                        (float)S.az[I] * (float)S.az[J];
     const float2 st = S.conST[k];
-    const double invd = 1.0 / d;
-    f[0] = (float)(S.phi0[k] * invd);
-    f[1] = (float)((q < 0.0 ? -q : 0.0) * invd);
-    f[2] = (float)(q * invd);
-    f[3] = (float)fabs(cosab);
+    const float invd = 1.0f / d;
+    f[0] = (float)S.phi0[k] * invd;
+    f[1] = (q < 0.0f ? -q : 0.0f) * invd;
+    f[2] = q * invd;
+    f[3] = fabsf(cosab);
     f[4] = (float)S.len[I];
     f[5] = (float)S.len[J];
     f[6] = st.x;
     f[7] = st.y;
     f[8] = (float)(S.rowPtr[I + 1] - S.rowPtr[I]) * 0.125f;
     f[9] = (float)(S.rowPtr[J + 1] - S.rowPtr[J]) * 0.125f;
-    f[10] = (float)(gprev * akk * invd);
-    f[11] = (float)(nb / akk * invd);
-    scale = (float)(akk * invd);
+    f[10] = gprev * akk * invd;
+    f[11] = nb / akk * invd;
+    scale = akk * invd;
     return true;
 }
 
@@ -271,7 +274,7 @@ __global__ void __launch_bounds__(kMlpTile) k_mlp_warm(DevState S, MlpView V) {
         float y = 0.0f;
         if (!infer_tile(sh, tbase, phase, &S.ctl->errFlags, y)) break;
         if (ok) {
-            const double g0 = y > 0.0f ? (double)y / (double)scale : 0.0;
+            const double g0 = y > 0.0f ? (double)(y / scale) : 0.0;
             S.gamma[k] = g0;
             S.st[1][k] = make_double2(g0, 0.0);
             if (S.precision == ALENS_PREC_MIXED) S.st32[1][k] = make_float2((float)g0, 0.0f);
