@@ -157,31 +157,85 @@ void philox(const uint32_t ctr_in[4], const uint32_t key_in[2],
     out[3] = c3;
 }
 
-// Six standard normals for (seed, gid, step): three Philox blocks, six
-// 53-bit uniforms in (0,1), three Box-Muller pairs.
+// FP32 natural log of a normal x > 0: x = m 2^e, m in [sqrt(1/2), sqrt(2)),
+// log m = 2 atanh(u), u = (m-1)/(m+1), atanh series to u^13.
+float det_logf(float x) {
+    uint32_t bits;
+    std::memcpy(&bits, &x, 4);
+    int e = (int)((bits >> 23) & 0xffu) - 127;
+    bits = (bits & 0x807fffffu) | (127u << 23);
+    float m;
+    std::memcpy(&m, &bits, 4);  // m in [1, 2)
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float u = (m - 1.0f) / (m + 1.0f);
+    const float u2 = u * u;
+    float p = 1.0f / 13.0f;
+    p = p * u2 + 1.0f / 11.0f;
+    p = p * u2 + 1.0f / 9.0f;
+    p = p * u2 + 1.0f / 7.0f;
+    p = p * u2 + 1.0f / 5.0f;
+    p = p * u2 + 1.0f / 3.0f;
+    p = p * u2 + 1.0f;
+    return (float)e * 0.693147181f + 2.0f * u * p;
+}
+
+// FP32 sin and cos for |x| <= pi: halve until |x| <= 1, Taylor polynomials
+// to x^11 / x^12, then double-angle formulas.
+void det_sincosf(float x, float *s_out, float *c_out) {
+    int k = 0;
+    while ((x < 0.0f ? -x : x) > 1.0f && k < 8) {
+        x = x * 0.5f;
+        k++;
+    }
+    const float x2 = x * x;
+    float s = -1.0f / 39916800.0f;
+    s = s * x2 + 1.0f / 362880.0f;
+    s = s * x2 - 1.0f / 5040.0f;
+    s = s * x2 + 1.0f / 120.0f;
+    s = s * x2 - 1.0f / 6.0f;
+    s = s * x2 + 1.0f;
+    s = s * x;
+    float c = 1.0f / 479001600.0f;
+    c = c * x2 - 1.0f / 3628800.0f;
+    c = c * x2 + 1.0f / 40320.0f;
+    c = c * x2 - 1.0f / 720.0f;
+    c = c * x2 + 1.0f / 24.0f;
+    c = c * x2 - 0.5f;
+    c = c * x2 + 1.0f;
+    for (int i = 0; i < k; i++) {
+        const float s2 = 2.0f * s * c;
+        const float c2 = c * c - s * s;
+        s = s2;
+        c = c2;
+    }
+    *s_out = s;
+    *c_out = c;
+}
+
+// Six standard normals for (seed, gid, step): two Philox blocks, six
+// 24-bit uniforms in (0,1), three Box-Muller pairs in FP32.
 void normals6(uint64_t seed, int64_t gid, int64_t step, double z[6]) {
     const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    uint32_t w[12];
-    for (uint32_t b = 0; b < 3; b++) {
+    uint32_t w[8];
+    for (uint32_t b = 0; b < 2; b++) {
         const uint32_t ctr[4] = {(uint32_t)(uint64_t)gid,
                                  (uint32_t)((uint64_t)gid >> 32),
                                  (uint32_t)(uint64_t)step, b};
         philox(ctr, key, w + 4 * b);
     }
-    double u[6];
-    for (int i = 0; i < 6; i++) {
-        const double hi = (double)(w[2 * i] >> 5);
-        const double lo = (double)(w[2 * i + 1] >> 6);
-        u[i] = (hi * 67108864.0 + lo + 0.5) * (1.0 / 9007199254740992.0);
-    }
+    float u[6];
+    for (int i = 0; i < 6; i++) u[i] = ((float)(w[i] >> 8) + 0.5f) * 5.9604644775390625e-08f;  // 2^-24
     for (int p = 0; p < 3; p++) {
-        const double r = std::sqrt(-2.0 * det_log(u[2 * p]));
-        const double ang = u[2 * p + 1] * kTwoPi - kPi;
-        double sn, cs;
-        det_sincos(ang, &sn, &cs);
+        const float r = std::sqrt(-2.0f * det_logf(u[2 * p]));
+        const float ang = u[2 * p + 1] * 6.28318531f - 3.14159265f;
+        float sn, cs;
+        det_sincosf(ang, &sn, &cs);
         // angle + pi: cos -> -cos, sin -> -sin
-        z[2 * p] = r * (-cs);
-        z[2 * p + 1] = r * (-sn);
+        z[2 * p] = (double)(r * -cs);
+        z[2 * p + 1] = (double)(r * -sn);
     }
 }
 
