@@ -53,9 +53,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="bounded CPU-oracle sample for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mlp-samples", type=int, default=2_000_000,
+    ap.add_argument("--mlp-samples", type=int, default=10_000_000,
                     help="training rows of the learned warm start")
-    ap.add_argument("--mlp-epochs", type=int, default=20)
+    ap.add_argument("--mlp-epochs", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="skip the other workload shapes")
     ap.add_argument("--extra-steps", type=int, default=10)
     ap.add_argument("--profile-case", action="store_true",
