@@ -40,6 +40,18 @@ constexpr int kSolveThreads = 256;
 constexpr int kRowTile = 64;         // level-1 reduction tile
 constexpr int kWindow = 64;          // replicas decided per block window
 constexpr int kRowPrefetch = 8;      // row entries loaded together
+#ifndef ALENS_ROW_PREFETCH_F32
+#define ALENS_ROW_PREFETCH_F32 16
+#endif
+// entries per gather batch of the FP32 form (FP64 keeps 8: register budget)
+template <class Real>
+struct RowBatch {
+    static constexpr int value = kRowPrefetch;
+};
+template <>
+struct RowBatch<float> {
+    static constexpr int value = ALENS_ROW_PREFETCH_F32;
+};
 
 template <class Real>
 struct Vec2;
@@ -343,22 +355,23 @@ __device__ __forceinline__ void row_update(const SolveView<Real> &V, int k, int 
     const int kr = k - C.rowBase;
     const bool rc = kr >= 0 && kr < C.nRow;
     const int e0 = rc ? C.rptr[kr] : __ldg(V.aptr + k), e1 = rc ? C.rptr[kr + 1] : __ldg(V.aptr + k + 1);
-    for (int eb = e0; eb < e1; eb += kRowPrefetch) {
+    constexpr int B = RowBatch<Real>::value;
+    for (int eb = e0; eb < e1; eb += B) {
         // entries from the block's shared-memory copy when cached; all
         // neighbour iterates of the batch are requested before any is used
-        int4 ent[kRowPrefetch];
+        int4 ent[B];
 #pragma unroll
-        for (int j = 0; j < kRowPrefetch; j++) {
+        for (int j = 0; j < B; j++) {
             const int ce = eb + j - C.entBase;
             ent[j] = eb + j < e1 ? ((ce >= 0 && ce < C.nEnt) ? C.ent[ce] : __ldg(V.aent + eb + j))
                                  : make_int4(k, 1, 0, 0);
         }
-        V2 sv[kRowPrefetch];
+        V2 sv[B];
 #pragma unroll
-        for (int j = 0; j < kRowPrefetch; j++)
+        for (int j = 0; j < B; j++)
             if (eb + j < e1) sv[j] = stIn[ent[j].x];  // L1-cacheable: rows of a block share neighbours
 #pragma unroll
-        for (int j = 0; j < kRowPrefetch; j++) {
+        for (int j = 0; j < B; j++) {
             if (eb + j < e1) {
                 int l;
                 Real val, lbl;
