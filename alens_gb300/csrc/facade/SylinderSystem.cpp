@@ -10,6 +10,7 @@
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
+#include <unordered_map>
 
 namespace gpu {
 
@@ -93,6 +94,7 @@ bool SylinderConfig::readYaml(const std::string &path, std::string *err) {
         else if (key == "viscosity") viscosity = std::stod(val);
         else if (key == "KBT") KBT = std::stod(val);
         else if (key == "linkKappa") linkKappa = std::stod(val);
+        else if (key == "linkGap") linkGap = std::stod(val);
         else if (key == "sylinderDiameter") sylinderDiameter = std::stod(val);
         else if (key == "sylinderDiameterColRatio") sylinderDiameterColRatio = std::stod(val);
         else if (key == "sylinderLengthColRatio") sylinderLengthColRatio = std::stod(val);
@@ -232,12 +234,43 @@ void SylinderSystem::create() {
           "alens_set_rods");
     conPool_.assign(std::max(1, omp_get_max_threads()), ConstraintBlockQue());
     rodsStale_ = false;
+    applyLinks();
+}
+
+// Links of a flexible filament ('L a b' lines of TubuleInitial.dat, as
+// Utils/gen_flexible_init.py writes them; linkKappa / linkGap of
+// RunConfig.yaml, Examples/FlexibleFilament/RunConfig.yaml:19-20): a spring
+// of stiffness linkKappa from the plus end of rod a (centre + L/2 axis) to
+// the minus end of rod b (centre - L/2 axis), rest length linkGap plus both
+// radii (surfaces linkGap apart).  Built on the device every step
+// (alens_set_links).
+void SylinderSystem::applyLinks() {
+    if (links_.empty()) return;
+    std::unordered_map<int64_t, int> index;
+    for (size_t i = 0; i < rods_.size(); i++) index[rods_[i].gid] = (int)i;
+    std::vector<int32_t> I, J;
+    std::vector<double> sI, sJ, rest, kap;
+    for (const auto &l : links_) {
+        auto a = index.find(l[0]), b = index.find(l[1]);
+        if (a == index.end() || b == index.end()) throw std::runtime_error("link to an unknown rod gid");
+        const Sylinder &ra = rods_[a->second];
+        const Sylinder &rb = rods_[b->second];
+        I.push_back(a->second);
+        J.push_back(b->second);
+        sI.push_back(0.5 * ra.length);
+        sJ.push_back(-0.5 * rb.length);
+        rest.push_back(runConfig.linkGap + ra.radius + rb.radius);
+        kap.push_back(runConfig.linkKappa);
+    }
+    check(alens_set_links(ctx_, 0, (int)I.size(), I.data(), J.data(), sI.data(), sJ.data(), rest.data(), kap.data()),
+          "alens_set_links");
 }
 
 void SylinderSystem::initialize(const std::string &configFile, const std::string &posFile, int, char **) {
     std::string err;
     if (!runConfig.readYaml(configFile, &err)) throw std::runtime_error(err);
-    rods_ = readSylinderAscii(posFile, nullptr, &err);
+    links_.clear();
+    rods_ = readSylinderAscii(posFile, &links_, &err);
     if (rods_.empty() && !err.empty()) throw std::runtime_error(err);
     create();
 }

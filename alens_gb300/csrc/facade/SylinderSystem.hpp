@@ -27,6 +27,7 @@ struct SylinderConfig {
     double viscosity = 0.01;
     double KBT = 0.00411;
     double linkKappa = 1000.0;
+    double linkGap = 0.0;           // gap between the surfaces of linked rods (um)
     double sylinderDiameter = 0.025;
     double sylinderDiameterColRatio = 1.0;
     double sylinderLengthColRatio = 1.0;
@@ -115,6 +116,8 @@ class SylinderSystem {
 
     AlensCtx *ctx_ = nullptr;
     std::vector<Sylinder> rods_;
+    std::vector<std::array<int64_t, 2>> links_;  // 'L a b' lines (gids): plus end of a to minus end of b
+    void applyLinks();
     bool rodsStale_ = false;
     ConstraintBlockPool conPool_;
     AlensStepStats stats_{};

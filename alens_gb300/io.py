@@ -97,3 +97,30 @@ def read_run_config(path, **overrides) -> AlensConfig:
         col_buf=float(vals.get("sylinderColBuf", 0.025)), tol=float(vals.get("conResTol", 1e-5)),
         max_ite=int(float(vals.get("conMaxIte", 2000))), seed=int(vals.get("rngSeed", 1234)), **overrides)
     return cfg
+
+
+def read_link_params(path):
+    """linkKappa and linkGap of a RunConfig.yaml (defaults 1000 pN/um, 0)."""
+    kappa, gap = 1000.0, 0.0
+    with open(path) as f:
+        for line in f:
+            line = line.split("#", 1)[0]
+            if ":" not in line:
+                continue
+            k, v = (x.strip() for x in line.split(":", 1))
+            if k == "linkKappa":
+                kappa = float(v)
+            elif k == "linkGap":
+                gap = float(v)
+    return kappa, gap
+
+
+def filament_links(rods: RodState, pairs, kappa: float, gap: float) -> dict:
+    """Spring links of 'L a b' lines (rod gids) for GpuSystem.set_links: plus
+    end of a (centre + L/2 axis) to minus end of b, rest length gap plus both
+    radii, stiffness kappa (the C++ facade builds the same set)."""
+    index = {int(g): i for i, g in enumerate(rods.gid)}
+    I = np.array([index[a] for a, _ in pairs], np.int32)
+    J = np.array([index[b] for _, b in pairs], np.int32)
+    return {"i": I, "j": J, "si": 0.5 * rods.length[I], "sj": -0.5 * rods.length[J],
+            "rest": gap + rods.radius[I] + rods.radius[J], "kappa": np.full(len(pairs), float(kappa))}
