@@ -86,6 +86,33 @@ class AlensBlock(C.Structure):
     ]
 
 
+BOUNDARY_WALL = 0
+BOUNDARY_SPHERE = 1
+BOUNDARY_TUBE = 2
+
+
+class AlensBoundary(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("inside", C.c_int32),
+        ("center", C.c_double * 3),
+        ("axis", C.c_double * 3),
+        ("radius", C.c_double),
+    ]
+
+
+def make_boundary(kind: int, center=(0.0, 0.0, 0.0), axis=(0.0, 0.0, 1.0), radius: float = 1.0,
+                  inside: bool = True) -> AlensBoundary:
+    b = AlensBoundary()
+    b.type = int(kind)
+    b.inside = int(bool(inside))
+    for d in range(3):
+        b.center[d] = float(center[d])
+        b.axis[d] = float(axis[d])
+    b.radius = float(radius)
+    return b
+
+
 class AlensStepStats(C.Structure):
     _fields_ = [
         ("step", C.c_int64),
@@ -180,6 +207,7 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_velocity": (C.c_int, [vp, C.c_int, C.c_int, _PD, _PD]),
         "alens_add_bilateral": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(AlensBlock)]),
         "alens_set_links": (C.c_int, [vp, C.c_int, C.c_int, _PI32, _PI32, _PD, _PD, _PD, _PD]),
+        "alens_set_boundaries": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(AlensBoundary)]),
         "alens_step": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
         "alens_detect": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
         "alens_solve": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
@@ -344,6 +372,10 @@ class GpuSystem:
         self._ck(self.lib.alens_set_links(self.h, replica, int(a[0].shape[0]), _p(a[0], C.c_int32),
                                           _p(a[1], C.c_int32), _p(a[2], C.c_double), _p(a[3], C.c_double),
                                           _p(a[4], C.c_double), _p(a[5], C.c_double)), "alens_set_links")
+
+    def set_boundaries(self, boundaries, replica: int = 0):
+        arr = (AlensBoundary * max(len(boundaries), 1))(*boundaries)
+        self._ck(self.lib.alens_set_boundaries(self.h, replica, len(boundaries), arr), "alens_set_boundaries")
 
     def _stage(self, fn, name, ok=(ALENS_OK,)):
         st = AlensStepStats()

@@ -163,6 +163,14 @@ int alens_set_links(AlensCtx *ctx, int replica, int n, const int32_t *indexI, co
     });
 }
 
+int alens_set_boundaries(AlensCtx *ctx, int replica, int n, const AlensBoundary *boundaries) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->setBoundaries(replica, n, boundaries);
+        return (int)ALENS_OK;
+    });
+}
+
 int alens_step(AlensCtx *ctx, AlensStepStats *stats) {
     if (!ctx) return ALENS_INVALID_ARG;
     return guarded_ctx(ctx, [&] { return ctx->eng->step(stats); });

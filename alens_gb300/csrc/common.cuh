@@ -21,6 +21,7 @@ constexpr double kParallelEps = 1e-12;
 constexpr int kTile = 64;         // level-1 reduction tile (constraints)
 constexpr int kChunk = 1024;      // level-2+ reduction chunk (one warp)
 constexpr int kImageNone = 13;    // image code of the zero periodic shift
+constexpr int kImageBoundary = 27; // keys (i, b, 27 + point): rod i against boundary b
 
 // error flag bits (DevCtl::errFlags)
 constexpr int kErrOverflow = 1;
@@ -240,6 +241,76 @@ __host__ __device__ inline void normals6(unsigned long long seed, long long gid,
         // angle + pi: cos -> -cos, sin -> -sin
         z[2 * p] = (double)(r * -cs);
         z[2 * p + 1] = (double)(r * -sn);
+    }
+}
+
+// ------------------------------------------------------------ boundaries
+// Boundary with a unit axis (normalised on the host); the oracle states the
+// same arithmetic.
+struct BoundaryDev {
+    int type, inside;
+    double c[3], a[3], R;
+};
+
+// Contact points of a rod with a boundary: both ends for walls and for
+// inside spheres/tubes (one point, the centre, for sphere-shaped rods); the
+// point nearest the centre for outside spheres.
+__host__ __device__ inline int boundary_npoints(const BoundaryDev &B, double h) {
+    if (B.type == 1 && !B.inside) return 1;
+    return h > 0.0 ? 2 : 1;
+}
+
+// Contact point e of rod (centre x, unit axis u, collision half-length h):
+// Q, the signed distance s of Q to the boundary (positive on the allowed
+// side) and the unit normal n pointing into the allowed region.
+__host__ __device__ inline void boundary_contact(const BoundaryDev &B, const double x[3], const double u[3],
+                                                 double h, int e, double Q[3], double &s, double n[3]) {
+    double t;
+    if (B.type == 1 && !B.inside) {
+        t = (B.c[0] - x[0]) * u[0] + (B.c[1] - x[1]) * u[1] + (B.c[2] - x[2]) * u[2];
+        t = t < -h ? -h : (t > h ? h : t);
+    } else {
+        t = e == 0 ? -h : h;
+    }
+    Q[0] = x[0] + t * u[0];
+    Q[1] = x[1] + t * u[1];
+    Q[2] = x[2] + t * u[2];
+    const double v[3] = {Q[0] - B.c[0], Q[1] - B.c[1], Q[2] - B.c[2]};
+    if (B.type == 0) {  // wall
+        s = v[0] * B.a[0] + v[1] * B.a[1] + v[2] * B.a[2];
+        n[0] = B.a[0];
+        n[1] = B.a[1];
+        n[2] = B.a[2];
+        return;
+    }
+    double w[3];
+    if (B.type == 2) {  // tube: radial part of v
+        const double p = v[0] * B.a[0] + v[1] * B.a[1] + v[2] * B.a[2];
+        w[0] = v[0] - p * B.a[0];
+        w[1] = v[1] - p * B.a[1];
+        w[2] = v[2] - p * B.a[2];
+    } else {
+        w[0] = v[0];
+        w[1] = v[1];
+        w[2] = v[2];
+    }
+    const double rho = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    double d[3] = {1.0, 0.0, 0.0};
+    if (rho > 0.0) {
+        d[0] = w[0] / rho;
+        d[1] = w[1] / rho;
+        d[2] = w[2] / rho;
+    }
+    if (B.inside) {
+        s = B.R - rho;
+        n[0] = -d[0];
+        n[1] = -d[1];
+        n[2] = -d[2];
+    } else {
+        s = rho - B.R;
+        n[0] = d[0];
+        n[1] = d[1];
+        n[2] = d[2];
     }
 }
 

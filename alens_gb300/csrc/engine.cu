@@ -53,6 +53,7 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     rods_.resize(R_);
     queue_.resize(R_);
     links_.resize(R_);
+    bnd_.resize(R_);
     repStats_.assign(R_, AlensStepStats{});
     if (cfg_[0].stream) {
         stream_ = (cudaStream_t)cfg_[0].stream;
@@ -102,6 +103,7 @@ Engine::~Engine() {
     if (hBlockRep_) cudaFreeHost(hBlockRep_);
     if (hLinkSlot0_) cudaFreeHost(hLinkSlot0_);
     freeGroup(linkAllocs_);
+    freeGroup(bndAllocs_);
     if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -205,6 +207,7 @@ void Engine::finalize() {
     blockCap_ = 0;
     freeGroup(linkAllocs_);
     S_.nLinks = 0;
+    freeGroup(bndAllocs_);
     hostPar_.resize(R_);
     int rodOff = 0, cellOff = 0;
     for (int r = 0; r < R_; r++) {
@@ -235,6 +238,7 @@ void Engine::finalize() {
     S.prevCount = alloc<int>(fixedAllocs_, 1);
     S.linkSlot0 = alloc<int>(fixedAllocs_, R_);
     linksDirty_ = true;
+    bndDirty_ = true;
     CK(cudaMemcpyAsync(S.par, hostPar_.data(), sizeof(RepParams) * R_, cudaMemcpyHostToDevice, stream_));
     CK(cudaMemsetAsync(S.dyn, 0, sizeof(RepDyn) * R_, stream_));
     CK(cudaMemsetAsync(S.bilPrefix, 0, sizeof(int) * (R_ + 1), stream_));
@@ -457,6 +461,53 @@ void Engine::setLinks(int rep, int n, const int32_t *idxI, const int32_t *idxJ, 
     linksDirty_ = true;
 }
 
+void Engine::setBoundaries(int rep, int n, const AlensBoundary *b) {
+    if (rep < 0 || rep >= R_ || n < 0 || n > ALENS_MAX_BOUNDARIES || (n > 0 && !b)) throw ApiError(ALENS_INVALID_ARG);
+    std::vector<BoundaryDev> v;
+    for (int k = 0; k < n; k++) {
+        const AlensBoundary &B = b[k];
+        BoundaryDev d{};
+        d.type = B.type;
+        d.inside = B.inside ? 1 : 0;
+        if (B.type < ALENS_BOUNDARY_WALL || B.type > ALENS_BOUNDARY_TUBE) throw ApiError(ALENS_INVALID_ARG);
+        if (B.type == ALENS_BOUNDARY_TUBE && !d.inside) throw ApiError(ALENS_INVALID_ARG);
+        const double an = std::sqrt(B.axis[0] * B.axis[0] + B.axis[1] * B.axis[1] + B.axis[2] * B.axis[2]);
+        if (B.type != ALENS_BOUNDARY_SPHERE && !(an > 0.0)) throw ApiError(ALENS_INVALID_ARG);
+        if (B.type != ALENS_BOUNDARY_WALL && !(B.radius > 0.0)) throw ApiError(ALENS_INVALID_ARG);
+        for (int c = 0; c < 3; c++) {
+            if (!std::isfinite(B.center[c]) || !std::isfinite(B.axis[c])) throw ApiError(ALENS_INVALID_ARG);
+            d.c[c] = B.center[c];
+            d.a[c] = an > 0.0 ? B.axis[c] / an : 0.0;
+        }
+        d.R = B.radius;
+        v.push_back(d);
+    }
+    bnd_[rep] = std::move(v);
+    bndDirty_ = true;
+}
+
+// Device copy of every replica's boundaries.  Invalidates the captured
+// graph: whether the boundary kernel runs is part of it.
+void Engine::uploadBoundaries() {
+    if (!bndDirty_) return;
+    CK(cudaStreamSynchronize(stream_));
+    invalidateGraph();
+    freeGroup(bndAllocs_);
+    std::vector<BoundaryDev> all;
+    std::vector<int> start(R_ + 1, 0);
+    for (int r = 0; r < R_; r++) {
+        all.insert(all.end(), bnd_[r].begin(), bnd_[r].end());
+        start[r + 1] = (int)all.size();
+    }
+    S_.nBnd = (int)all.size();
+    S_.bnd = alloc<BoundaryDev>(bndAllocs_, all.size());
+    S_.bndStart = alloc<int>(bndAllocs_, R_ + 1);
+    if (!all.empty())
+        CK(cudaMemcpy(S_.bnd, all.data(), sizeof(BoundaryDev) * all.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(S_.bndStart, start.data(), sizeof(int) * (R_ + 1), cudaMemcpyHostToDevice));
+    bndDirty_ = false;
+}
+
 // Concatenated device copy of every replica's links (rod indices made
 // global).  Invalidates the captured graph: the link count is part of it.
 void Engine::uploadLinks() {
@@ -506,6 +557,7 @@ void Engine::uploadLinks() {
 // Per replica the blocks are [queued by alens_add_bilateral..., links...].
 void Engine::uploadBlocks() {
     uploadLinks();
+    uploadBoundaries();
     int total = 0;
     hBilPrefix_[0] = 0;
     for (int r = 0; r < R_; r++) {
@@ -563,6 +615,10 @@ int Engine::enqueueDetect() {
     launch_scatter(S, stream_);
     launch_pairs(S, stream_);
     n += 2;
+    if (S.nBnd > 0) {
+        launch_boundary_pairs(S, stream_);
+        n += 1;
+    }
     n += launch_scan(S.pairCount, S.pairOff, S.nRods, S.scanTmp, stream_);
     n += launch_pair_sort(S, stream_);
     launch_ranges(S, stream_);

@@ -121,6 +121,10 @@ struct DevState {
     int *linkI, *linkJ, *linkRep, *linkLocal;  // global rod indices, replica, index in replica
     double *linkSI, *linkSJ, *linkRest, *linkKappa;
     int *linkSlot0;  // [R] block slot of each replica's first link (host-written)
+    // confinement boundaries (unit axes), replica r owns [bndStart[r], bndStart[r+1])
+    int nBnd;
+    BoundaryDev *bnd;
+    int *bndStart;
     // reductions
     double *part;   // 9 x tileCap (solver: 2 parities x 4 kinds; stress: 9)
     double *work;   // per block 9 x workCap
@@ -137,6 +141,7 @@ int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st);  // 
 void launch_scatter(const DevState &S, cudaStream_t st);
 void launch_link_blocks(const DevState &S, cudaStream_t st);
 void launch_pairs(const DevState &S, cudaStream_t st);
+void launch_boundary_pairs(const DevState &S, cudaStream_t st);  // only when S.nBnd > 0
 int launch_pair_sort(const DevState &S, cudaStream_t st);
 void launch_ranges(const DevState &S, cudaStream_t st);
 void launch_build(const DevState &S, cudaStream_t st);

@@ -39,6 +39,7 @@ class Engine {
     void addBilateral(int rep, int n, const AlensBlock *blocks);
     void setLinks(int rep, int n, const int32_t *idxI, const int32_t *idxJ, const double *sI, const double *sJ,
                   const double *rest, const double *kappa);
+    void setBoundaries(int rep, int n, const AlensBoundary *b);
     int step(AlensStepStats *out);
     int detect(AlensStepStats *out);
     int solve(AlensStepStats *out);
@@ -126,6 +127,10 @@ class Engine {
     };
     std::vector<HostLinks> links_;
     bool linksDirty_ = false;
+    std::vector<std::vector<BoundaryDev>> bnd_;  // per replica, unit axes
+    bool bndDirty_ = false;
+    std::vector<void *> bndAllocs_;
+    void uploadBoundaries();
     std::vector<void *> linkAllocs_;
     int *hLinkSlot0_ = nullptr;
     void uploadLinks();

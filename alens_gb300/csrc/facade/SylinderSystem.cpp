@@ -3,6 +3,7 @@
 
 #include <omp.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -71,10 +72,51 @@ bool SylinderConfig::readYaml(const std::string &path, std::string *err) {
         return false;
     }
     std::string line;
+    bool inBoundaries = false;
+    boundaries.clear();
     while (std::getline(f, line)) {
         const size_t hash = line.find('#');
         if (hash != std::string::npos) line = line.substr(0, hash);
-        if (line.empty() || line[0] == ' ' || line[0] == '\t' || line[0] == '-') continue;  // nested
+        if (trim(line).empty()) continue;
+        const bool nested = line[0] == ' ' || line[0] == '\t' || line[0] == '-';
+        if (inBoundaries && nested) {
+            // "- type: ..." starts an entry; "key: value" lines fill the last one
+            std::string t = trim(line);
+            if (t[0] == '-') {
+                AlensBoundary b;
+                std::memset(&b, 0, sizeof(b));
+                b.inside = 1;
+                b.axis[2] = 1.0;
+                boundaries.push_back(b);
+                t = trim(t.substr(1));
+            }
+            const size_t c2 = t.find(':');
+            if (c2 == std::string::npos || boundaries.empty()) continue;
+            const std::string k = trim(t.substr(0, c2));
+            std::string v = trim(t.substr(c2 + 1));
+            AlensBoundary &b = boundaries.back();
+            auto vec3b = [&](double *dst) {
+                auto items = parseList(v);
+                for (int d = 0; d < 3 && d < (int)items.size(); d++) dst[d] = std::stod(items[d]);
+            };
+            if (k == "type") {
+                v.erase(std::remove(v.begin(), v.end(), '"'), v.end());
+                v.erase(std::remove(v.begin(), v.end(), '\''), v.end());
+                b.type = v == "sphere" ? ALENS_BOUNDARY_SPHERE : (v == "tube" ? ALENS_BOUNDARY_TUBE : ALENS_BOUNDARY_WALL);
+            } else if (k == "center") {
+                vec3b(b.center);
+            } else if (k == "axis" || k == "norm") {
+                vec3b(b.axis);
+            } else if (k == "radius") {
+                b.radius = std::stod(v);
+            } else if (k == "inside") {
+                b.inside = parseBool(v) ? 1 : 0;
+            }
+            continue;
+        }
+        if (nested) continue;  // other nested blocks
+        inBoundaries = trim(line.substr(0, line.find(':'))) == "boundaries";
+        if (inBoundaries) continue;
         const size_t colon = line.find(':');
         if (colon == std::string::npos) continue;
         const std::string key = trim(line.substr(0, colon));
@@ -235,6 +277,9 @@ void SylinderSystem::create() {
     conPool_.assign(std::max(1, omp_get_max_threads()), ConstraintBlockQue());
     rodsStale_ = false;
     applyLinks();
+    if (!runConfig.boundaries.empty())
+        check(alens_set_boundaries(ctx_, 0, (int)runConfig.boundaries.size(), runConfig.boundaries.data()),
+              "alens_set_boundaries");
 }
 
 // Links of a flexible filament ('L a b' lines of TubuleInitial.dat, as

@@ -41,6 +41,10 @@ struct SylinderConfig {
 
     // Reads the flat "key: value" / "key: [a, b, c]" lines of RunConfig.yaml;
     // unknown keys and nested blocks are ignored.
+    // `boundaries:` list (type "wall" | "sphere" | "tube"; center, radius,
+    // axis (or norm for walls), inside), as in
+    // Examples/DenseStrainingMotion/RunConfig.yaml:36-41
+    std::vector<AlensBoundary> boundaries;
     bool readYaml(const std::string &path, std::string *err = nullptr);
     AlensConfig toAlens() const;
 };

@@ -462,6 +462,40 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
     }
 }
 
+// Rod-boundary contacts: every contact point of a rod closer to a boundary
+// of its replica than sylinderColBuf (surface distance, FP64, the oracle's
+// arithmetic) gives a key (i, b, 27 + point) in the rod's pair segment.
+__global__ void k_boundary_pairs(DevState S) {
+    if (flags(S) & kErrNaN) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nRods; i += gridDim.x * blockDim.x) {
+        const int rep = S.rodRep[i];
+        const int b0 = S.bndStart[rep], b1 = S.bndStart[rep + 1];
+        if (b0 == b1) continue;
+        const double colBuf = S.par[rep].colBuf;
+        const double x[3] = {S.px[i], S.py[i], S.pz[i]};
+        const double a[3] = {S.ax[i], S.ay[i], S.az[i]};
+        const double h = S.hcol[i], rc = S.rcol[i];
+        int cnt = 0;
+        for (int b = b0; b < b1; b++) {
+            const BoundaryDev &B = S.bnd[b];
+            const int np = boundary_npoints(B, h);
+            for (int e = 0; e < np; e++) {
+                double Q[3], sd, n[3];
+                boundary_contact(B, x, a, h, e, Q, sd, n);
+                if (sd - rc < colBuf) {
+                    const int pos = atomicAdd(&S.ctl->rawCount, 1);
+                    if (pos < S.cap)
+                        S.rawKeys[pos] = pair_key(i, b - b0, kImageBoundary + e);
+                    else
+                        atomicOr(&S.ctl->errFlags, kErrOverflow);
+                    cnt++;
+                }
+            }
+        }
+        if (cnt) atomicAdd(&S.pairCount[i], cnt);
+    }
+}
+
 // Place raw keys into their rod's segment, then sort each segment: the
 // canonical order is (i, j, image) ascending.
 __global__ void k_pair_bucket(DevState S) {
@@ -588,6 +622,48 @@ __global__ void k_build(DevState S) {
         const int rep = S.rodRep[i];
         const RepParams &P = S.par[rep];
         const int k = p + S.bilPrefix[rep];
+        double g0 = 0.0;
+        if (warmPrev && prevN > 0) {
+            int lo = 0, hi = prevN;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (S.prevKeys[mid] < key)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            if (lo < prevN && S.prevKeys[lo] == key) g0 = S.prevGamma[lo];
+        }
+        if (img >= kImageBoundary) {
+            // rod i against boundary j of its replica, contact point img - 27
+            const BoundaryDev &B = S.bnd[S.bndStart[rep] + j];
+            const double x[3] = {S.px[i], S.py[i], S.pz[i]};
+            const double a[3] = {S.ax[i], S.ay[i], S.az[i]};
+            double Q[3], sd, n[3];
+            boundary_contact(B, x, a, S.hcol[i], img - kImageBoundary, Q, sd, n);
+            const double sep = sd - S.rcol[i];
+            const double r[3] = {Q[0] - x[0], Q[1] - x[1], Q[2] - x[2]};
+            double J[12];
+            J[0] = n[0];
+            J[1] = n[1];
+            J[2] = n[2];
+            cross3(r, n, J + 3);
+#pragma unroll
+            for (int c = 6; c < 12; c++) J[c] = 0.0;
+#pragma unroll
+            for (int c = 0; c < 12; c++) S.jac[12 * (size_t)k + c] = J[c];
+            S.conI[k] = i;
+            S.conJ[k] = -1;
+            S.conImg[k] = img;
+            S.conST[k] = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                S.lab[6 * (size_t)k + d] = Q[d];
+                S.lab[6 * (size_t)k + 3 + d] = Q[d] - sd * n[d];
+            }
+            finish_constraint(S, k, P, i, -1, J, sep, g0, 0.0, 0.0);
+            continue;
+        }
         const int sv[3] = {img / 9 - 1, (img / 3) % 3 - 1, img % 3 - 1};
         const double c1[3] = {S.px[i], S.py[i], S.pz[i]};
         const double c2[3] = {S.px[j] + (double)sv[0] * P.L[0], S.py[j] + (double)sv[1] * P.L[1],
@@ -621,18 +697,6 @@ __global__ void k_build(DevState S) {
         for (int d = 0; d < 3; d++) {
             S.lab[6 * (size_t)k + d] = R.P[d];
             S.lab[6 * (size_t)k + 3 + d] = R.Q[d];
-        }
-        double g0 = 0.0;
-        if (warmPrev && prevN > 0) {
-            int lo = 0, hi = prevN;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (S.prevKeys[mid] < key)
-                    lo = mid + 1;
-                else
-                    hi = mid;
-            }
-            if (lo < prevN && S.prevKeys[lo] == key) g0 = S.prevGamma[lo];
         }
         finish_constraint(S, k, P, i, j, J, sep, g0, 0.0, 0.0);
     }
@@ -777,6 +841,10 @@ void launch_pairs(const DevState &S, cudaStream_t st) {
     const long long items = 27LL * S.nRods;
     const long long g = (items + kPairThreads - 1) / kPairThreads;
     k_pairs<<<(unsigned)(g > 0 ? g : 1), kPairThreads, 0, st>>>(S);
+}
+
+void launch_boundary_pairs(const DevState &S, cudaStream_t st) {
+    k_boundary_pairs<<<grid_for(S.nRods, 256), 256, 0, st>>>(S);
 }
 
 int launch_pair_sort(const DevState &S, cudaStream_t st) {

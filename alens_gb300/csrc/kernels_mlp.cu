@@ -63,7 +63,7 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
 #pragma unroll
     for (int c = 0; c < kMlpInPad; c++) f[c] = 0.0f;
     scale = 0.0f;
-    if (S.conImg[k] < 0) return false;
+    if (S.conImg[k] < 0 || S.conImg[k] >= kImageBoundary) return false;  // blocks, boundary contacts
     const int I = S.conI[k], J = S.conJ[k];
     const float q = (float)S.q[k];
     const float d = (float)S.rcol[I] + (float)S.rcol[J];

@@ -124,3 +124,41 @@ def filament_links(rods: RodState, pairs, kappa: float, gap: float) -> dict:
     J = np.array([index[b] for _, b in pairs], np.int32)
     return {"i": I, "j": J, "si": 0.5 * rods.length[I], "sj": -0.5 * rods.length[J],
             "rest": gap + rods.radius[I] + rods.radius[J], "kappa": np.full(len(pairs), float(kappa))}
+
+
+def read_boundaries(path):
+    """The `boundaries:` list of a RunConfig.yaml as AlensBoundary structs
+    (type "wall" | "sphere" | "tube"; center, radius, axis or norm, inside),
+    parsed as the C++ facade parses it."""
+    from .capi import BOUNDARY_SPHERE, BOUNDARY_TUBE, BOUNDARY_WALL, make_boundary
+    out, cur, inside = [], None, False
+    with open(path) as f:
+        for raw in f:
+            line = raw.split("#", 1)[0]
+            if not line.strip():
+                continue
+            nested = line[0] in " \t-"
+            if inside and nested:
+                t = line.strip()
+                if t.startswith("-"):
+                    cur = {"type": "wall", "center": (0, 0, 0), "axis": (0, 0, 1), "radius": 0.0, "inside": True}
+                    out.append(cur)
+                    t = t[1:].strip()
+                if ":" not in t or cur is None:
+                    continue
+                k, v = (x.strip() for x in t.split(":", 1))
+                if k == "type":
+                    cur["type"] = v.strip("\"'")
+                elif k in ("center", "axis", "norm"):
+                    cur["axis" if k == "norm" else k] = [float(x) for x in v.strip("[] ").split(",")]
+                elif k == "radius":
+                    cur["radius"] = float(v)
+                elif k == "inside":
+                    cur["inside"] = v.lower() in ("true", "1", "yes")
+                continue
+            if nested:
+                continue
+            inside = line.split(":", 1)[0].strip() == "boundaries"
+    kinds = {"wall": BOUNDARY_WALL, "sphere": BOUNDARY_SPHERE, "tube": BOUNDARY_TUBE}
+    return [make_boundary(kinds.get(b["type"], BOUNDARY_WALL), b["center"], b["axis"], b["radius"], b["inside"])
+            for b in out]

@@ -11,7 +11,7 @@ import ctypes as C
 import numpy as np
 
 from . import build as _build
-from .capi import (ALENS_NOT_CONVERGED, ALENS_OK, AlensBlock, AlensConfig, AlensError,
+from .capi import (ALENS_NOT_CONVERGED, ALENS_OK, AlensBlock, AlensBoundary, AlensConfig, AlensError,
                    AlensStepStats, RodState, _p)
 
 _PD = C.POINTER(C.c_double)
@@ -39,6 +39,7 @@ def load_oracle(rebuild: bool = True) -> C.CDLL:
         "orc_get_known_velocity": (C.c_int, [vp, C.c_int, _PD]),
         "orc_add_bilateral": (C.c_int, [vp, C.c_int, C.POINTER(AlensBlock)]),
         "orc_set_initial_gamma": (C.c_int, [vp, C.c_int, _PD]),
+        "orc_set_boundaries": (C.c_int, [vp, C.c_int, C.POINTER(AlensBoundary)]),
         "orc_set_links": (C.c_int, [vp, C.c_int, _PI32, _PI32, _PD, _PD, _PD, _PD]),
         "orc_step": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
         "orc_detect": (C.c_int, [vp, C.POINTER(AlensStepStats)]),
@@ -190,6 +191,10 @@ class OracleSystem:
         _ck(self.lib.orc_set_links(self.h, int(a[0].shape[0]), _p(a[0], C.c_int32), _p(a[1], C.c_int32),
                                    _p(a[2], C.c_double), _p(a[3], C.c_double), _p(a[4], C.c_double),
                                    _p(a[5], C.c_double)), "orc_set_links")
+
+    def set_boundaries(self, boundaries):
+        arr = (AlensBoundary * max(len(boundaries), 1))(*boundaries)
+        _ck(self.lib.orc_set_boundaries(self.h, len(boundaries), arr), "orc_set_boundaries")
 
     def set_initial_gamma(self, gamma):
         g = np.ascontiguousarray(gamma, dtype=np.float64)

@@ -202,6 +202,40 @@ int alens_add_bilateral(AlensCtx *ctx, int replica, int n,
 int alens_set_links(AlensCtx *ctx, int replica, int n, const int32_t *indexI, const int32_t *indexJ,
                     const double *sI, const double *sJ, const double *restLength, const double *kappa);
 
+/* Confinement boundaries of one replica (the role of SimToolbox's Boundary
+ * objects listed under `boundaries:` in RunConfig.yaml,
+ * Examples/DenseStrainingMotion/RunConfig.yaml:36-41, and projected on by
+ * Boundary::project, SRC/TubuleSystem.cpp:285-305).  Every step, each rod
+ * contact point within sylinderColBuf of a boundary becomes a one-sided
+ * unilateral constraint (force along the boundary normal into the allowed
+ * region, gamma >= 0) in the same solve as the collisions:
+ *   wall   : plane through center with unit normal axis; allowed side +axis;
+ *            contact points: both rod ends
+ *   sphere : center, radius; inside = 1 keeps rods inside (both rod ends),
+ *            inside = 0 keeps them outside (the rod point nearest center)
+ *   tube   : infinite cylinder (center, axis, radius), inside = 1 only
+ *            (both rod ends)
+ * Spheres (length < 2 radius) have one contact point, the centre.  These
+ * constraints are reported by alens_get_constraints among the collisions
+ * with indexJ = -1 and image 27 (first point) or 28 (second point).
+ * Up to ALENS_MAX_BOUNDARIES per replica; n = 0 removes them. */
+#define ALENS_MAX_BOUNDARIES 8
+typedef enum AlensBoundaryType {
+    ALENS_BOUNDARY_WALL = 0,
+    ALENS_BOUNDARY_SPHERE = 1,
+    ALENS_BOUNDARY_TUBE = 2
+} AlensBoundaryType;
+
+typedef struct AlensBoundary {
+    int32_t type;       /* AlensBoundaryType                              */
+    int32_t inside;     /* sphere/tube: 1 keep inside, 0 keep outside     */
+    double center[3];   /* um                                             */
+    double axis[3];     /* tube axis or wall normal (normalised here)     */
+    double radius;      /* sphere/tube radius (um)                        */
+} AlensBoundary;
+
+int alens_set_boundaries(AlensCtx *ctx, int replica, int n, const AlensBoundary *boundaries);
+
 /* One full step (replaces SylinderSystem::runStep, SRC/TubuleSystem.cpp:223).
  * Returns ALENS_OK, ALENS_NOT_CONVERGED (step completed with the last
  * iterate), or an error; *stats (nullable) receives the summary. */

@@ -470,6 +470,12 @@ struct OrcCtx {
     std::vector<double> jac, phi0, q, gamma, cinv, lb, lab;
     std::vector<uint8_t> unil;
     std::vector<AlensBlock> queue, blocks;
+    // confinement boundaries (unit axes)
+    struct Bnd {
+        int type, inside;
+        double c[3], a[3], R;
+    };
+    std::vector<Bnd> bnd;
     // pre-bound crosslinkers: blocks built from the rod state every step
     std::vector<int> linkI, linkJ;
     std::vector<double> linkSI, linkSJ, linkRest, linkKappa;
@@ -624,6 +630,52 @@ void image_shift(const OrcCtx *x, int img, double S[3]) {
         S[d] = (double)sv[d] * (x->cfg.simBoxHigh[d] - x->cfg.simBoxLow[d]);
 }
 
+// Rod-boundary contact points: both rod ends for walls and inside
+// spheres/tubes (the centre alone for sphere-shaped rods); the point
+// nearest the centre for outside spheres.  Q, the signed distance s to the
+// boundary (positive on the allowed side) and the unit normal n into the
+// allowed region.
+int boundary_npoints(const OrcCtx::Bnd &B, double h) {
+    if (B.type == 1 && !B.inside) return 1;
+    return h > 0.0 ? 2 : 1;
+}
+
+void boundary_contact(const OrcCtx::Bnd &B, const double x[3], const double u[3], double h, int e,
+                      double Q[3], double &s, double n[3]) {
+    double t;
+    if (B.type == 1 && !B.inside) {
+        t = (B.c[0] - x[0]) * u[0] + (B.c[1] - x[1]) * u[1] + (B.c[2] - x[2]) * u[2];
+        t = t < -h ? -h : (t > h ? h : t);
+    } else {
+        t = e == 0 ? -h : h;
+    }
+    for (int d = 0; d < 3; d++) Q[d] = x[d] + t * u[d];
+    const double v[3] = {Q[0] - B.c[0], Q[1] - B.c[1], Q[2] - B.c[2]};
+    if (B.type == 0) {
+        s = v[0] * B.a[0] + v[1] * B.a[1] + v[2] * B.a[2];
+        for (int d = 0; d < 3; d++) n[d] = B.a[d];
+        return;
+    }
+    double w[3];
+    if (B.type == 2) {
+        const double p = v[0] * B.a[0] + v[1] * B.a[1] + v[2] * B.a[2];
+        for (int d = 0; d < 3; d++) w[d] = v[d] - p * B.a[d];
+    } else {
+        for (int d = 0; d < 3; d++) w[d] = v[d];
+    }
+    const double rho = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    double dir[3] = {1.0, 0.0, 0.0};
+    if (rho > 0.0)
+        for (int d = 0; d < 3; d++) dir[d] = w[d] / rho;
+    if (B.inside) {
+        s = B.R - rho;
+        for (int d = 0; d < 3; d++) n[d] = -dir[d];
+    } else {
+        s = rho - B.R;
+        for (int d = 0; d < 3; d++) n[d] = dir[d];
+    }
+}
+
 void find_pairs(OrcCtx *x, std::vector<std::vector<uint64_t>> &perRod) {
     const int n = x->n;
     const AlensConfig &c = x->cfg;
@@ -693,6 +745,15 @@ void find_pairs(OrcCtx *x, std::vector<std::vector<uint64_t>> &perRod) {
                         if (sep < colBuf) out.push_back(pair_key(i, j, img));
                     }
                 }
+            }
+        }
+        // contacts with the boundaries: keys (i, b, 27 + point)
+        for (size_t b = 0; b < x->bnd.size(); b++) {
+            const int np = boundary_npoints(x->bnd[b], hi_);
+            for (int e = 0; e < np; e++) {
+                double Q[3], sd, nn[3];
+                boundary_contact(x->bnd[b], pi, ai, hi_, e, Q, sd, nn);
+                if (sd - ri < colBuf) out.push_back(pair_key(i, (int64_t)b, 27 + e));
             }
         }
         std::sort(out.begin(), out.end());
@@ -774,6 +835,34 @@ void build_constraints(OrcCtx *x) {
         const uint64_t key = keys[k];
         const int i = (int)(key >> 32), j = (int)((key >> 5) & 0x7ffffff),
                   img = (int)(key & 31);
+        double g0 = 0.0;
+        if (warmPrev && !x->prevKeys.empty()) {
+            auto it = std::lower_bound(x->prevKeys.begin(), x->prevKeys.end(), key);
+            if (it != x->prevKeys.end() && *it == key)
+                g0 = x->prevGamma[it - x->prevKeys.begin()];
+        }
+        if (img >= 27) {
+            // rod i against boundary j: one-sided, force along the normal
+            const double *xi = &x->pos[3 * i], *ai = &x->axis[3 * i];
+            double Q[3], sd, nn[3];
+            boundary_contact(x->bnd[j], xi, ai, x->hcol[i], img - 27, Q, sd, nn);
+            double *J = &x->jac[12 * (size_t)k];
+            const double r[3] = {Q[0] - xi[0], Q[1] - xi[1], Q[2] - xi[2]};
+            J[0] = nn[0];
+            J[1] = nn[1];
+            J[2] = nn[2];
+            cross3(r, nn, J + 3);
+            x->ci[k] = i;
+            x->cj[k] = -1;
+            x->cimg[k] = img;
+            x->phi0[k] = sd - x->rcol[i];
+            for (int d = 0; d < 3; d++) {
+                x->lab[6 * (size_t)k + d] = Q[d];
+                x->lab[6 * (size_t)k + 3 + d] = Q[d] - sd * nn[d];
+            }
+            x->gamma[k] = g0;
+            continue;
+        }
         double S[3];
         image_shift(x, img, S);
         const double *pj = &x->pos[3 * j];
@@ -802,12 +891,6 @@ void build_constraints(OrcCtx *x) {
         for (int d = 0; d < 3; d++) {
             x->lab[6 * (size_t)k + d] = P[d];
             x->lab[6 * (size_t)k + 3 + d] = Q[d];
-        }
-        double g0 = 0.0;
-        if (warmPrev && !x->prevKeys.empty()) {
-            auto it = std::lower_bound(x->prevKeys.begin(), x->prevKeys.end(), key);
-            if (it != x->prevKeys.end() && *it == key)
-                g0 = x->prevGamma[it - x->prevKeys.begin()];
         }
         x->gamma[k] = g0;
     }
@@ -1207,6 +1290,29 @@ int orc_set_links(OrcCtx *x, int n, const int32_t *idxI, const int32_t *idxJ, co
     x->linkSJ.assign(sJ, sJ + n);
     x->linkRest.assign(rest, rest + n);
     x->linkKappa.assign(kappa, kappa + n);
+    return ALENS_OK;
+}
+
+int orc_set_boundaries(OrcCtx *x, int n, const AlensBoundary *b) {
+    if (!x || n < 0 || n > ALENS_MAX_BOUNDARIES || (n > 0 && !b)) return ALENS_INVALID_ARG;
+    std::vector<OrcCtx::Bnd> v;
+    for (int k = 0; k < n; k++) {
+        OrcCtx::Bnd d{};
+        d.type = b[k].type;
+        d.inside = b[k].inside ? 1 : 0;
+        if (d.type < 0 || d.type > 2 || (d.type == 2 && !d.inside)) return ALENS_INVALID_ARG;
+        const double an = std::sqrt(b[k].axis[0] * b[k].axis[0] + b[k].axis[1] * b[k].axis[1] +
+                                    b[k].axis[2] * b[k].axis[2]);
+        if (d.type != 1 && !(an > 0.0)) return ALENS_INVALID_ARG;
+        if (d.type != 0 && !(b[k].radius > 0.0)) return ALENS_INVALID_ARG;
+        for (int c = 0; c < 3; c++) {
+            d.c[c] = b[k].center[c];
+            d.a[c] = an > 0.0 ? b[k].axis[c] / an : 0.0;
+        }
+        d.R = b[k].radius;
+        v.push_back(d);
+    }
+    x->bnd = v;
     return ALENS_OK;
 }
 

@@ -36,6 +36,7 @@ int orc_get_rods(OrcCtx *ctx, int n, double *pos, double *orientation);
 int orc_get_velocity(OrcCtx *ctx, int n, double *vel, double *omega);
 int orc_add_bilateral(OrcCtx *ctx, int n, const AlensBlock *blocks);
 int orc_set_initial_gamma(OrcCtx *ctx, int n, const double *gamma);
+int orc_set_boundaries(OrcCtx *ctx, int n, const AlensBoundary *boundaries);
 int orc_set_links(OrcCtx *ctx, int n, const int32_t *indexI, const int32_t *indexJ, const double *sI,
                   const double *sJ, const double *restLength, const double *kappa);
 int orc_step(OrcCtx *ctx, AlensStepStats *stats);
