@@ -162,3 +162,47 @@ def read_boundaries(path):
     kinds = {"wall": BOUNDARY_WALL, "sphere": BOUNDARY_SPHERE, "tube": BOUNDARY_TUBE}
     return [make_boundary(kinds.get(b["type"], BOUNDARY_WALL), b["center"], b["axis"], b["radius"], b["inside"])
             for b in out]
+
+
+def write_vtp(path, rods: RodState, gamma_sum=None):
+    """Rods as a VTK XML PolyData file (.vtp, ASCII): two points per rod (its
+    segment ends) joined by one line cell, with per-rod cell data gid,
+    length, radius and, when given, the summed constraint force magnitude.
+    The role of the snapshot writer the reference's ParaView states read
+    (Examples/*/ *.pvsm load SylinderAscii / VTK output)."""
+    a = quat_to_axis(rods.quat)
+    h = 0.5 * rods.length[:, None]
+    pts = np.empty((2 * rods.n, 3))
+    pts[0::2] = rods.pos - h * a
+    pts[1::2] = rods.pos + h * a
+
+    def arr(name, typ, vals, ncomp=1):
+        body = " ".join(repr(float(v)) if typ.startswith("Float") else str(int(v)) for v in np.ravel(vals))
+        return (f'<DataArray type="{typ}" Name="{name}" NumberOfComponents="{ncomp}" format="ascii">'
+                f"{body}</DataArray>\n")
+
+    with open(path, "w") as f:
+        f.write('<?xml version="1.0"?>\n<VTKFile type="PolyData" version="0.1" byte_order="LittleEndian">\n')
+        f.write(f'<PolyData>\n<Piece NumberOfPoints="{2 * rods.n}" NumberOfVerts="0" NumberOfLines="{rods.n}" '
+                'NumberOfStrips="0" NumberOfPolys="0">\n')
+        f.write("<Points>\n" + arr("Points", "Float64", pts, 3) + "</Points>\n")
+        f.write("<Lines>\n" + arr("connectivity", "Int64", np.arange(2 * rods.n))
+                + arr("offsets", "Int64", 2 * np.arange(1, rods.n + 1)) + "</Lines>\n")
+        f.write("<CellData>\n" + arr("gid", "Int64", rods.gid) + arr("length", "Float64", rods.length)
+                + arr("radius", "Float64", rods.radius))
+        if gamma_sum is not None:
+            f.write(arr("force", "Float64", gamma_sum))
+        f.write("</CellData>\n</Piece>\n</PolyData>\n</VTKFile>\n")
+
+
+def write_time_step_info(path, step: int, snap_id: int, time: float):
+    """Restart bookkeeping next to a snapshot (the role of TimeStepInfo.txt,
+    whose presence makes aLENS restart, SRC/main.cpp:28-37)."""
+    with open(path, "w") as f:
+        f.write(f"{int(step)}\n{int(snap_id)}\n{time:.17g}\n")
+
+
+def read_time_step_info(path):
+    with open(path) as f:
+        vals = f.read().split()
+    return int(vals[0]), int(vals[1]), float(vals[2])

@@ -57,3 +57,21 @@ def test_oracle_reproduces_golden():
     assert g["rod0"] == gold["rod0"]
     assert g["pos_head"] == gold["pos_head"] and g["quat_head"] == gold["quat_head"]
     assert g["stress_trace"] == gold["stress_trace"]
+
+
+def test_vtp_and_restart_info(tmp_path):
+    import xml.etree.ElementTree as ET
+    _, rods = make_fixtures.load_fixture()
+    p = tmp_path / "snap.vtp"
+    io.write_vtp(str(p), rods, gamma_sum=np.arange(rods.n, dtype=float))
+    root = ET.parse(str(p)).getroot()
+    piece = root.find("PolyData/Piece")
+    assert int(piece.get("NumberOfPoints")) == 2 * rods.n and int(piece.get("NumberOfLines")) == rods.n
+    pts = np.array(piece.find("Points/DataArray").text.split(), float).reshape(-1, 3)
+    mid = 0.5 * (pts[0::2] + pts[1::2])
+    assert np.allclose(mid, rods.pos, atol=1e-12)
+    assert np.allclose(np.linalg.norm(pts[1::2] - pts[0::2], axis=1), rods.length, atol=1e-12)
+    names = [d.get("Name") for d in piece.find("CellData")]
+    assert names == ["gid", "length", "radius", "force"]
+    io.write_time_step_info(str(tmp_path / "TimeStepInfo.txt"), 1200, 12, 0.12)
+    assert io.read_time_step_info(str(tmp_path / "TimeStepInfo.txt")) == (1200, 12, 0.12)
