@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--mlp-epochs", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="skip the other workload shapes")
     ap.add_argument("--extra-steps", type=int, default=10)
+    ap.add_argument("--profile-step", action="store_true",
+                    help="one step of each form (direct launches) between cudaProfilerStart/Stop, for an ncu "
+                         "launch list with --profile-from-start off; no JSON line")
     ap.add_argument("--profile-case", action="store_true",
                     help="print per-stage CUDA-event times of both solver forms (direct launches) "
                          "for profiling; no JSON line")
@@ -433,6 +436,9 @@ def other_workloads(torch, stream, flush, mlp, steps):
         cfg = workloads.config_with(w4.cfg, warmStart=warm, precision=prec)
         t, it = timed_steps(torch, stream, maker(cfg, rods4, attach=attach), steps, flush)
         r4[lab] = {"iterations_per_step": it, "ms_per_step": t / steps}
+    r4.update(gamma_error(workloads.config_with(w4.cfg, precision=capi.PREC_FP64, warmStart=capi.WARM_ZERO),
+                          workloads.config_with(w4.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_MLP),
+                          rods4, mlp=mlp))
     out["eval_200000_rods_40um_cube"] = r4
     # batched ensemble: 64 replicas in one launch sequence vs 64 sequential systems
     reps = workloads.ensemble(nrep=64, nmin=500, nmax=8000, seed=0)
@@ -518,10 +524,37 @@ def _chosen(rep):
     return rep["candidates"][rep["chosen"]]
 
 
+def profile_step(args):
+    """One step of the fast and of the plain form, each after 3 warm-up steps,
+    inside cudaProfilerStart/Stop (direct launches)."""
+    import torch
+    from alens_gb300 import capi, warmstart, workloads
+    w = workload(args, 0)
+    rods = relaxed_state(w, args.pre_steps, capi.GpuSystem)
+    mlp, _ = warmstart.build_model(samples=300_000, epochs=3, seed=0)
+    for prec, warm in ((capi.PREC_MIXED, capi.WARM_MLP), (capi.PREC_FP64, capi.WARM_ZERO)):
+        c = workloads.config_with(w.cfg, precision=prec, warmStart=warm, useGraph=0)
+        g = capi.GpuSystem(c)
+        g.set_rods(rods)
+        if warm == capi.WARM_MLP:
+            g.attach_mlp(mlp)
+        for _ in range(3):
+            g.step()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        g.step()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        g.close()
+
+
 def main():
     args = parse()
     if args.profile_case:
         profile_case(args)
+        return
+    if args.profile_step:
+        profile_step(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
