@@ -477,6 +477,10 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
     const int tpb = (nTiles + (int)nb - 1) / (int)nb;
     const int t0 = min((int)blockIdx.x * tpb, nTiles);
     const int t1 = min(t0 + tpb, nTiles);
+    // blocks without tiles leave at once; the barrier counts the others
+    // (block 0 always stays: it arms the pass counters)
+    const int nActive = nTiles > 0 ? (nTiles + tpb - 1) / tpb : 1;
+    if ((int)blockIdx.x >= nActive) return;
     // this block's operator rows, cached for every pass: the rows of tiles
     // [t0, t1) are one contiguous range of constraints
     RowCache C{};
@@ -561,7 +565,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
         cStore = clock64();
 #endif
         int stop = 0;
-        if (!grid_sync_pass(&S.ctl->bar, nb, &S.ctl->errFlags, timeout_ns, (unsigned int)(p + 1),
+        if (!grid_sync_pass(&S.ctl->bar, (unsigned int)nActive, &S.ctl->errFlags, timeout_ns, (unsigned int)(p + 1),
                             &S.ctl->activeCnt[p % 3], stop))
             return;
 #ifdef ALENS_TRACE
