@@ -68,6 +68,7 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     fixedCap_ = cfg_[0].maxConstraints;
     stageTiming_ = cfg_[0].stageTiming != 0;
     if (const char *e = std::getenv("ALENS_SOLVER_BLOCKS_PER_SM")) solverBlocksPerSM_ = std::max(1, atoi(e));
+    if (const char *e = std::getenv("ALENS_SOLVER_MIN_TILES")) solverMinTiles_ = std::max(1, atoi(e));
     // FP32 solver form: -1 = automatic (grid form for one replica, where all
     // SMs share one system; cluster form for ensembles), 0 = grid form,
     // N = cluster form with clusters of N CTAs
@@ -228,6 +229,7 @@ void Engine::finalize() {
     S.nCells = C;
     S.warm = warm_;
     S.precision = precision_;
+    S.solveMinTiles = solverMinTiles_;
     // fixed-size control
     S.par = alloc<RepParams>(fixedAllocs_, R_);
     S.dyn = alloc<RepDyn>(fixedAllocs_, R_);
@@ -638,9 +640,11 @@ int Engine::enqueueDetect() {
 }
 
 // ------------------------------------------------------------- autotuner
-void Engine::applySolverConfig(int form, int clusterSize, int threads, int blocksPerSM) {
+void Engine::applySolverConfig(int form, int clusterSize, int threads, int blocksPerSM, int minTiles) {
     invalidateGraph();
     solverBlocksPerSM_ = std::max(1, blocksPerSM);
+    solverMinTiles_ = std::max(1, minTiles);
+    S_.solveMinTiles = solverMinTiles_;
     solverGrid_ = std::min(solver_max_grid(precision_), numSM_ * solverBlocksPerSM_);
     if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "solver occupancy");
     solverForm_ = form;
@@ -683,26 +687,30 @@ std::string Engine::autotune(int reps) {
             CK(cudaMemcpyAsync(S_.st32[1], sSt32, sizeof(float2) * (size_t)nc, cudaMemcpyDeviceToDevice, stream_));
     };
     struct Cand {
-        int form, cs, threads, bps;
+        int form, cs, threads, bps, mt;
         double ms;
         bool ok;
     };
     std::vector<Cand> cands;
-    for (int bps : {1, 2}) cands.push_back({kFormGrid, 0, 256, bps, 0.0, false});
+    // grid form: blocks per SM x minimum tiles per block (fewer, fuller
+    // blocks make the per-pass barrier and the redundant reductions cheaper)
+    for (int bps : {1, 2})
+        for (int mt : {1, 2, 4, 8}) cands.push_back({kFormGrid, 0, 256, bps, mt, 0.0, false});
     if (precision_ == ALENS_PREC_MIXED) {
         const int maxCs = cluster_max_size();
         for (int cs : {16, 8, 4, 2})
-            if (cs <= maxCs) cands.push_back({kFormCluster, cs, 512, 1, 0.0, false});
+            if (cs <= maxCs) cands.push_back({kFormCluster, cs, 512, 1, 1, 0.0, false});
         const int csmMax = csm_cluster_size(nullptr);
         for (int cs : {16, 8, 4, 2})
             for (int th : {256, 512})
-                if (cs <= csmMax) cands.push_back({kFormResident, cs, th, 1, 0.0, false});
+                if (cs <= csmMax) cands.push_back({kFormResident, cs, th, 1, 1, 0.0, false});
     }
     ensureEvents();
     const int saveForm = solverForm_, saveCs = clusterSize_, saveBps = solverBlocksPerSM_, saveTh = csm_threads();
+    const int saveMt = solverMinTiles_;
     const int saveNcl = nClusters_, saveGrid = solverGrid_;
     for (Cand &c : cands) {
-        applySolverConfig(c.form, c.cs, c.threads, c.bps);
+        applySolverConfig(c.form, c.cs, c.threads, c.bps, c.mt);
         std::vector<double> t;
         bool ok = true;
         for (int r = 0; r < reps + 1 && ok; r++) {
@@ -727,11 +735,13 @@ std::string Engine::autotune(int reps) {
         if (cands[i].ok && (best < 0 || cands[i].ms < cands[best].ms)) best = (int)i;
     if (best >= 0) {
         const Cand &b = cands[best];
-        applySolverConfig(b.form, b.cs, b.threads, b.bps);
+        applySolverConfig(b.form, b.cs, b.threads, b.bps, b.mt);
     } else {
         solverForm_ = saveForm;
         clusterSize_ = saveCs;
         solverBlocksPerSM_ = saveBps;
+        solverMinTiles_ = saveMt;
+        S_.solveMinTiles = saveMt;
         csm_set_threads(saveTh);
         nClusters_ = saveNcl;
         solverGrid_ = saveGrid;
@@ -750,9 +760,9 @@ std::string Engine::autotune(int reps) {
         char buf[256];
         snprintf(buf, sizeof(buf),
                  "%s{\"form\": \"%s\", \"cluster\": %d, \"threads\": %d, \"blocks_per_sm\": %d, "
-                 "\"ms\": %s}",
+                 "\"min_tiles\": %d, \"ms\": %s}",
                  i ? ", " : "", names[c.form], c.cs, c.form == kFormResident ? c.threads : (c.form == kFormCluster ? 512 : 256),
-                 c.bps, c.ok ? std::to_string(c.ms).c_str() : "null");
+                 c.bps, c.mt, c.ok ? std::to_string(c.ms).c_str() : "null");
         js += buf;
     }
     js += "], \"chosen\": " + std::to_string(best) + "}";

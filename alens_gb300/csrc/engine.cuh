@@ -52,8 +52,9 @@ struct RepDyn {
     int counter;              // last-arriver ticket of the current pass
     int refineIter;
     int finalPar;             // solver buffer holding this replica's result
-    int refined;              // 1: the cluster-resident solver verified the FP32
-                              // solution's FP64 residual (no refinement needed)
+    int refined;              // 1: the FP32 solution's FP64 residual is within
+                              // tolerance (no FP64 refinement sweep needed)
+    unsigned long long res64bits;  // FP64 residual of the FP32 solution (max, bits)
     double alpha, res;
 };
 
@@ -66,6 +67,8 @@ struct DevCtl {
     int maxIte;       // max over replicas
     int activeCnt[3]; // replicas active per solver pass (mod 3)
     int finalParity;  // buffer holding the solver's last iterate
+    int allRefined;   // every replica's FP32 solution met the FP64 tolerance
+    unsigned int setupDone;  // blocks of the refinement set-up that finished
     GridBarrier bar;
 };
 
@@ -73,6 +76,7 @@ struct DevCtl {
 struct DevState {
     int R, nRods, cap, nCells, tileCap, workCap, blockCap, nnzCap;
     int warm, precision;
+    int solveMinTiles;         // BBPGD: at least this many 64-row tiles per solver block
     RepParams *par;
     RepDyn *dyn;
     DevCtl *ctl;

@@ -94,7 +94,7 @@ class Engine {
     void readBack();
     bool handleOverflow();
     bool handleSolverFit();
-    void applySolverConfig(int form, int clusterSize, int threads, int blocksPerSM);
+    void applySolverConfig(int form, int clusterSize, int threads, int blocksPerSM, int minTiles = 1);
     int collectStats(int stage);
     void freeGroup(std::vector<void *> &g);
     template <class T>
@@ -109,6 +109,7 @@ class Engine {
     bool useGraph_ = true, graphFailed_ = false;
     int fixedCap_ = 0;
     int solverBlocksPerSM_ = 1;
+    int solverMinTiles_ = 1;  // at least this many tiles per grid-form solver block
     int clusterSize_ = -1;   // FP32 solver: -1 automatic, 0 grid form, N cluster size
     int nClusters_ = 1;
     int solverForm_ = -1;    // SolverForm of the FP32 solver (-1: not chosen yet)

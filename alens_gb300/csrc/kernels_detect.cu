@@ -547,6 +547,7 @@ __global__ void k_ranges(DevState S) {
             d.iter = 0;
             d.refineIter = 0;
             d.refined = 0;
+            d.res64bits = 0ULL;
             d.active = d.nCon > 0 ? 1 : 0;
             d.converged = d.nCon > 0 ? 0 : 1;
             d.status = 0;
@@ -563,6 +564,8 @@ __global__ void k_ranges(DevState S) {
         c->nTiles = tile;
         c->activeCnt[0] = c->activeCnt[1] = c->activeCnt[2] = 0;
         c->finalParity = 1;
+        c->allRefined = 0;
+        c->setupDone = 0u;
         c->maxIte = maxIte;
         c->bar.count = 0;
         c->bar.gen = 0;

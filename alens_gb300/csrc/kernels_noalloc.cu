@@ -86,6 +86,8 @@ __global__ void k_noalloc_setup(NoAllocScratch *sc, PlainOperator op, const doub
         c.maxIte = maxIte;
         c.activeCnt[0] = c.activeCnt[1] = c.activeCnt[2] = 0;
         c.finalParity = 1;
+        c.allRefined = 0;
+        c.setupDone = 0u;
         c.bar.count = 0;
         c.bar.gen = 0;
         RepDyn &d = sc->dyn;
@@ -102,6 +104,8 @@ __global__ void k_noalloc_setup(NoAllocScratch *sc, PlainOperator op, const doub
         d.counter = 0;
         d.refineIter = 0;
         d.finalPar = 1;
+        d.refined = 0;
+        d.res64bits = 0ULL;
         d.alpha = 0.0;
         d.res = 0.0;
         RepParams &P = sc->par;

@@ -13,40 +13,87 @@ namespace {
 
 __device__ __forceinline__ int flags(const DevState &S) { return ld_volatile_i32(&S.ctl->errFlags); }
 
-// Start of the FP64 refinement: gamma0 = the FP32 solution, solver state
-// re-armed; the FP32 iteration count is kept in refineIter.
+// Start of the FP64 refinement: gamma0 = the FP32 solution promoted and
+// projected, and the FP64 residual of that point computed as the FP64
+// solver's first pass would (the same entries, order and operations), max
+// per replica.  The last block to finish (ticket counter, no waiting)
+// re-arms the replicas: those within tolerance are marked refined and keep
+// the FP32 status; when all are, the FP64 launch returns at once.  The FP32
+// iteration count is kept in refineIter.
 __global__ void k_refine_setup(DevState S) {
+    __shared__ int s_last;
     if (flags(S) & kErrStepAbort) return;
-    const int par = S.ctl->finalParity;
-    __syncthreads();
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        for (int r = 0; r < S.R; r++) {
-            RepDyn &d = S.dyn[r];
-            d.refineIter = d.iter;
-            d.iter = 0;
-            if (d.refined) {
-                // FP64 residual already verified: the FP64 pass copies the
-                // replica's values through (status, residual kept)
-                d.active = 0;
-                continue;
-            }
-            d.active = d.nCon > 0 ? 1 : 0;
-            d.converged = d.nCon > 0 ? 0 : 1;
-            d.status = 0;
-            d.res = 0.0;
-        }
-    }
-    (void)par;
-    for (int r = 0; r < S.R; r++) {
-        const RepDyn &d = S.dyn[r];
+    const int nIdx = S.ctl->nTiles * kRowTile;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nIdx; idx += gridDim.x * blockDim.x) {
+        const int T = idx / kRowTile;
+        RepDyn &d = S.dyn[S.tileRep[T]];
+        const int local = (T - d.tileStart) * kRowTile + idx % kRowTile;
+        if (local >= d.nCon) continue;
+        const int k = d.conStart + local;
         const float2 *src = d.finalPar ? S.st32[1] : S.st32[0];
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nCon; i += gridDim.x * blockDim.x) {
-            const int k = d.conStart + i;
-            const double g = (double)src[k].x;
-            const double lb = S.lb[k];
-            S.st[1][k] = make_double2(g < lb ? lb : g, 0.0);
+        const double lbk = S.lb[k];
+        double xk = (double)src[k].x;
+        xk = xk < lbk ? lbk : xk;
+        S.st[1][k] = make_double2(xk, 0.0);
+        if (d.refined || d.status != ALENS_OK) continue;
+        double acc = 0.0;
+        const int e0 = S.aptr[k], e1 = S.aptr[k + 1];
+        for (int eb = e0; eb < e1; eb += kRowPrefetch) {
+            int4 en[kRowPrefetch];
+            float xs[kRowPrefetch];
+#pragma unroll
+            for (int j = 0; j < kRowPrefetch; j++) en[j] = eb + j < e1 ? __ldg(S.aent + eb + j) : make_int4(k, 1, 0, 0);
+#pragma unroll
+            for (int j = 0; j < kRowPrefetch; j++) xs[j] = src[en[j].x].x;
+#pragma unroll
+            for (int j = 0; j < kRowPrefetch; j++) {
+                if (eb + j < e1) {
+                    const double lbl = en[j].y == 0 ? 0.0 : (en[j].y == 1 ? -INFINITY : S.lb[en[j].x]);
+                    double xl = (double)xs[j];
+                    xl = xl < lbl ? lbl : xl;
+                    acc = fma(__hiloint2double(en[j].w, en[j].z), xl, acc);
+                }
+            }
         }
+        acc = fma(S.qc[k].y, xk, acc);
+        const double gn = acc + S.qc[k].x;
+        const double pr = xk - gn < lbk ? lbk : xk - gn;
+        const double rr = fabs(xk - pr);
+        atomicMax(&d.res64bits, (unsigned long long)__double_as_longlong(rr == rr ? rr : INFINITY));
     }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&S.ctl->setupDone, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last || threadIdx.x != 0) return;
+    __threadfence();
+    int all = 1;
+    for (int r = 0; r < S.R; r++) {
+        RepDyn &d = S.dyn[r];
+        d.refineIter = d.iter;
+        d.iter = 0;
+        if (d.nCon <= 0) continue;
+        if (!d.refined && d.status == ALENS_OK) {
+            const double res = __longlong_as_double((long long)ld_acquire_u64(&d.res64bits));
+            if (res <= S.par[r].tol) {
+                d.refined = 1;
+                d.res = res;
+            }
+        }
+        if (d.refined) {
+            // FP64 residual verified: the FP64 pass copies the replica's
+            // values through (status, residual kept)
+            d.active = 0;
+            continue;
+        }
+        all = 0;
+        d.active = 1;
+        d.converged = 0;
+        d.status = 0;
+        d.res = 0.0;
+    }
+    S.ctl->allRefined = all;
+    S.ctl->setupDone = 0u;
 }
 
 // Barrier and pass counters are re-armed by a separate single-thread
@@ -279,7 +326,7 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
             e = launch_solve_fp32(S, grid, timeout_ns, st);
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[1], st);
-        k_refine_setup<<<256, 256, 0, st>>>(S);
+        k_refine_setup<<<2 * (grid > 0 ? grid : 1), 128, 0, st>>>(S);
         k_solver_arm<<<1, 1, 0, st>>>(S);
         n += 3;
         e = cudaGetLastError();
@@ -305,10 +352,12 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
 }
 
 void launch_advance(const DevState &S, cudaStream_t st) {
-    int g = (S.nRods + 255) / 256;
+    // small blocks: the update is FP64-pipe bound (2 lanes/clk/SM on GB300),
+    // so the rods are spread over every SM rather than packed into a few
+    int g = (S.nRods + 63) / 64;
     if (g < 1) g = 1;
-    if (g > 4096) g = 4096;
-    k_advance<<<g, 256, 0, st>>>(S);
+    if (g > 8192) g = 8192;
+    k_advance<<<g, 64, 0, st>>>(S);
 }
 
 void launch_stress(const DevState &S, cudaStream_t st) {

@@ -323,17 +323,50 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
 // Operator rows of one block cached in shared memory for the whole solve
 // (the rows a block owns do not change between passes): entries
 // [entBase, entBase + nEnt) and row pointers of rows [rowBase, rowBase +
-// nRow].  Entries or rows outside are read from global memory.
+// nRow].  Entries or rows outside are read from global memory.  gv holds,
+// per cached entry, the previous iterate (gamma, g) of the entry's column,
+// gathered at the start of each pass (see gather_columns).
 struct RowCache {
     const int4 *ent;
     const int *rptr;
+    const void *gv;
     int entBase, nEnt;
     int rowBase, nRow;
 };
 
 constexpr int kRowCacheRows = 1024;                  // row pointers cached per block
-constexpr int kSolveDynSmem = 64 * 1024;             // dynamic shared memory of k_solve
-constexpr int kRowCacheEnts = (kSolveDynSmem - 4 * (kRowCacheRows + 4)) / 16;
+constexpr int kSolveDynSmem = 96 * 1024;             // dynamic shared memory of k_solve
+// entries cached per block: an int4 entry plus its gathered column iterate
+template <class Real>
+__host__ __device__ constexpr int row_cache_ents() {
+    return (kSolveDynSmem - 4 * (kRowCacheRows + 4)) / (16 + (int)sizeof(typename Vec2<Real>::T));
+}
+constexpr int kGatherWarp0 = 4;                      // warps kGatherWarp0.. gather
+
+// Start of a pass: the upper warps copy the previous iterate of every
+// cached entry's column into shared memory (asynchronous copies, all in
+// flight together, no registers held) while the lower warps reduce the
+// previous pass's partials (decide); the row updates then read their
+// neighbours from shared memory.  Each gathering thread waits for its own
+// copies; the __syncthreads that follows publishes them to the block.
+template <class Real>
+__device__ __forceinline__ void gather_columns(const RowCache &C, const typename Vec2<Real>::T *stIn) {
+    using V2 = typename Vec2<Real>::T;
+    const int nt = (int)blockDim.x - 32 * kGatherWarp0;
+    const int t = (int)threadIdx.x - 32 * kGatherWarp0;
+    if (t < 0 || C.nEnt <= 0) return;
+    const unsigned int gvBase = (unsigned int)__cvta_generic_to_shared(C.gv);
+#pragma unroll 4
+    for (int e = t; e < C.nEnt; e += nt) {
+        const V2 *src = stIn + C.ent[e].x;  // L1-cacheable: written before the last barrier
+        const unsigned int dst = gvBase + (unsigned int)(e * (int)sizeof(V2));
+        if constexpr (sizeof(V2) == 16)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
 
 // Update of constraint k at pass p in `mode`: reads the previous iterates,
 // forms x_k and (A x)_k, writes the new iterates, returns the dot-product
@@ -356,40 +389,69 @@ __device__ __forceinline__ void row_update(const SolveView<Real> &V, int k, int 
     const bool rc = kr >= 0 && kr < C.nRow;
     const int e0 = rc ? C.rptr[kr] : __ldg(V.aptr + k), e1 = rc ? C.rptr[kr + 1] : __ldg(V.aptr + k + 1);
     constexpr int B = RowBatch<Real>::value;
-    for (int eb = e0; eb < e1; eb += B) {
-        // entries from the block's shared-memory copy when cached; all
-        // neighbour iterates of the batch are requested before any is used
-        int4 ent[B];
-#pragma unroll
-        for (int j = 0; j < B; j++) {
-            const int ce = eb + j - C.entBase;
-            ent[j] = eb + j < e1 ? ((ce >= 0 && ce < C.nEnt) ? C.ent[ce] : __ldg(V.aent + eb + j))
-                                 : make_int4(k, 1, 0, 0);
+    const int ce0 = e0 - C.entBase, ce1 = e1 - C.entBase;
+    if (ce0 >= 0 && ce1 <= C.nEnt) {
+        // whole row cached: entries and their column iterates from shared
+        // memory, one at a time (same operations, same order)
+        const V2 *gv = reinterpret_cast<const V2 *>(C.gv);
+        for (int ce = ce0; ce < ce1; ce++) {
+            const int4 en = C.ent[ce];
+            const V2 sv = gv[ce];
+            int l;
+            Real val, lbl;
+            decode_entry<Real>(en, V.lbGeneral, l, val, lbl);
+            Real xl;
+            if (mode == kModeG0)
+                xl = sv.x;
+            else if (mode == kModeAG)
+                xl = sv.y;
+            else
+                xl = projlb<Real>(fma(-alpha, sv.y, sv.x), lbl);
+            if (l == k) {
+                gam = sv.x;
+                gold = sv.y;
+                lbk = lbl;
+                xk = xl;
+            }
+            acc = fma(val, xl, acc);
         }
-        V2 sv[B];
+    } else {
+        for (int eb = e0; eb < e1; eb += B) {
+            // entries from the block's shared-memory copy when cached; all
+            // neighbour iterates of the batch are requested before any is
+            // used
+            int4 ent[B];
 #pragma unroll
-        for (int j = 0; j < B; j++)
-            if (eb + j < e1) sv[j] = stIn[ent[j].x];  // L1-cacheable: rows of a block share neighbours
+            for (int j = 0; j < B; j++) {
+                const int ce = eb + j - C.entBase;
+                ent[j] = eb + j < e1 ? ((ce >= 0 && ce < C.nEnt) ? C.ent[ce] : __ldg(V.aent + eb + j))
+                                     : make_int4(k, 1, 0, 0);
+            }
+            V2 sv[B];
 #pragma unroll
-        for (int j = 0; j < B; j++) {
-            if (eb + j < e1) {
-                int l;
-                Real val, lbl;
-                decode_entry<Real>(ent[j], V.lbGeneral, l, val, lbl);
-                Real xl;
-                if (mode == kModeG0)
-                    xl = sv[j].x;
-                else if (mode == kModeAG)
-                    xl = sv[j].y;
-                else
-                    xl = projlb<Real>(fma(-alpha, sv[j].y, sv[j].x), lbl);
-                if (l == k) {
-                    gam = sv[j].x;
-                    gold = sv[j].y;
-                    lbk = lbl;
-                    xk = xl;
+            for (int j = 0; j < B; j++)
+                if (eb + j < e1) sv[j] = stIn[ent[j].x];  // L1-cacheable: rows of a block share neighbours
+#pragma unroll
+            for (int j = 0; j < B; j++) {
+                if (eb + j < e1) {
+                    int l;
+                    Real val, lbl;
+                    decode_entry<Real>(ent[j], V.lbGeneral, l, val, lbl);
+                    Real xl;
+                    if (mode == kModeG0)
+                        xl = sv[j].x;
+                    else if (mode == kModeAG)
+                        xl = sv[j].y;
+                    else
+                        xl = projlb<Real>(fma(-alpha, sv[j].y, sv[j].x), lbl);
+                    if (l == k) {
+                        gam = sv[j].x;
+                        gold = sv[j].y;
+                        lbk = lbl;
+                        xk = xl;
+                    }
+                    acc = fma(val, xl, acc);
                 }
-                acc = fma(val, xl, acc);
             }
         }
     }
@@ -467,14 +529,20 @@ __device__ void process_tile(const DevState &S, const SolveView<Real> &V, int p,
 }
 
 template <class Real>
-__global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<Real> V,
+__global__ void __launch_bounds__(kSolveThreads, 2) k_solve(DevState S, SolveView<Real> V,
                                                          unsigned long long timeout_ns) {
     __shared__ SolveShared sh;
     extern __shared__ int4 dynCache[];
     if (ld_volatile_i32(&S.ctl->errFlags) & kErrStepAbort) return;
+    // FP64 refinement after an FP32 solve whose result already met the FP64
+    // tolerance (checked by the refinement set-up, which left the promoted
+    // solution in buffer 1): nothing to do
+    if constexpr (sizeof(Real) == 8) {
+        if (S.precision == ALENS_PREC_MIXED && ld_volatile_i32(&S.ctl->allRefined)) return;
+    }
     const unsigned int nb = gridDim.x;
     const int nTiles = S.ctl->nTiles;
-    const int tpb = (nTiles + (int)nb - 1) / (int)nb;
+    const int tpb = max(S.solveMinTiles, (nTiles + (int)nb - 1) / (int)nb);
     const int t0 = min((int)blockIdx.x * tpb, nTiles);
     const int t1 = min(t0 + tpb, nTiles);
     // blocks without tiles leave at once; the barrier counts the others
@@ -484,10 +552,14 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
     // this block's operator rows, cached for every pass: the rows of tiles
     // [t0, t1) are one contiguous range of constraints
     RowCache C{};
+    constexpr int kEnts = row_cache_ents<Real>();
     {
-        int* rptr = reinterpret_cast<int *>(dynCache + kRowCacheEnts);
+        using V2 = typename Vec2<Real>::T;
+        V2 *gv = reinterpret_cast<V2 *>(dynCache + kEnts);
+        int *rptr = reinterpret_cast<int *>(gv + kEnts);
         C.ent = dynCache;
         C.rptr = rptr;
+        C.gv = gv;
         if (t0 < t1) {
             const RepDyn &da = S.dyn[__ldg(S.tileRep + t0)];
             const RepDyn &db = S.dyn[__ldg(S.tileRep + t1 - 1)];
@@ -495,7 +567,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
             const int rowEnd = min(db.conStart + (t1 - db.tileStart) * kRowTile, db.conStart + db.nCon);
             const int eBeg = __ldg(V.aptr + rowBeg), eEnd = __ldg(V.aptr + rowEnd);
             C.entBase = eBeg;
-            C.nEnt = min(eEnd - eBeg, kRowCacheEnts);
+            C.nEnt = min(eEnd - eBeg, kEnts);
             C.rowBase = rowBeg;
             C.nRow = rowEnd - rowBeg <= kRowCacheRows ? rowEnd - rowBeg : 0;
             for (int e = threadIdx.x; e < C.nEnt; e += blockDim.x) dynCache[e] = __ldg(V.aent + eBeg + e);
@@ -522,6 +594,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevState S, SolveView<R
 #endif
         if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl->activeCnt[(p + 1) % 3] = 0;
         double *partBase = S.part + (size_t)(p & 1) * 4 * tc;
+        // completes before the first decide()'s __syncthreads
+        gather_columns<Real>(C, (p & 1) ? V.st[0] : V.st[1]);
         // replica windows of this block's tile range
         int T = t0;
         while (T < t1) {

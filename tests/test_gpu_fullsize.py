@@ -39,6 +39,14 @@ def test_layer_20000(gpu_lib):
     assert st["nCollision"] > 10000
 
 
+def test_layer_20000_fuller_blocks(gpu_lib, monkeypatch):
+    """At least 24 tiles (1,536 rows) per solver block: each block's rows
+    overflow its shared-memory row cache, so cached and uncached rows mix."""
+    monkeypatch.setenv("ALENS_SOLVER_MIN_TILES", "24")
+    w = workloads.dense_monolayer(n=20000, side=40.0, seed=0)
+    run_pair(w.cfg, w.rods, 3)
+
+
 def test_bundle_50000_with_200000_links(gpu_lib):
     w = workloads.crosslinked_bundle_rods(n=50000, box=20.0, seed=0)
     pairs = workloads.pair_list(capi.GpuSystem, w.cfg, w.rods, 0.05)

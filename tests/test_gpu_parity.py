@@ -487,6 +487,20 @@ def test_autotune_keeps_fp64_parity(gpu_lib):
     compare_state(g, o)
 
 
+@pytest.mark.parametrize("min_tiles", [2, 3, 8])
+def test_min_tiles_per_block_keeps_fp64_parity(gpu_lib, monkeypatch, min_tiles):
+    """Fewer, fuller solver blocks (a minimum number of 64-row tiles per
+    block) change only which block updates which rows: the FP64 trajectory
+    equals the oracle's bit for bit, single system and ensemble."""
+    monkeypatch.setenv("ALENS_SOLVER_MIN_TILES", str(min_tiles))
+    w = workloads.small_periodic(n=1000, box=5.0, seed=0)
+    g, o = pair(w.cfg, w.rods)
+    for _ in range(4):
+        sg, so = g.step(), o.step()
+        assert sg["iterations"] == so["iterations"]
+    compare_state(g, o)
+
+
 def test_autotune_mixed_ensemble(gpu_lib):
     reps = workloads.ensemble(nrep=8, nmin=300, nmax=3000, seed=8)
     cfgs = [workloads.config_with(w.cfg, precision=capi.PREC_MIXED) for w in reps]
