@@ -49,51 +49,129 @@ __global__ void k_weights(DevState S) {
     }
 }
 
-// Merge of the rod rows of k's two rods; with fill == false only counts.
-template <bool fill>
-__device__ int merge_row(const DevState &S, int k, int out0) {
+// Row k of A is the merge of the rod rows of k's two rods (entries 2l+s,
+// ascending): one output per distinct l, in ascending l.  The structure is
+// found by one warp per row (integer work only): lane a holds entry a of
+// rod I's row and of rod J's row; a lane is the leader of its l when the
+// previous entry of its row has another l; an output's position is the
+// number of distinct l below it in the union (leaders before it in its own
+// row, leaders below it in the other row, less the values counted twice),
+// found with ballots and a lower bound over the other row's lanes.  Rows
+// with more than 32 entries on either rod are merged by lane 0 alone.
+// The values are then formed by one thread per output (full warps for the
+// FP64 pipe).
+constexpr int kArowWarps = 8;  // rows per 256-thread block
+
+__device__ __forceinline__ unsigned int lowmask(int n) { return n >= 32 ? 0xffffffffu : ((1u << n) - 1u); }
+
+// First lane index in [0, 32) whose value (ascending over lanes, padded
+// with large values) is >= x; 32 when none.
+__device__ __forceinline__ int lane_lower_bound(int vals, int x) {
+    int lo = 0, hi = 32;
+#pragma unroll
+    for (int it = 0; it < 6; it++) {
+        const int mid = (lo + hi) >> 1;
+        const int v = __shfl_sync(0xffffffffu, vals, mid & 31);
+        const bool go = lo < hi && v < x;
+        lo = go ? mid + 1 : lo;
+        hi = (lo < hi && !go) ? mid : hi;
+    }
+    return lo;
+}
+
+struct RowLists {
+    int aI0, nI, aJ0, nJ;
+};
+
+__device__ __forceinline__ RowLists row_lists(const DevState &S, int k) {
+    RowLists L;
     const int rI = S.conI[k], rJ = S.conJ[k];
-    const int aI0 = S.rowPtr[rI], nI = S.rowPtr[rI + 1] - aI0;
-    const int aJ0 = rJ >= 0 ? S.rowPtr[rJ] : 0;
-    const int nJ = rJ >= 0 ? S.rowPtr[rJ + 1] - aJ0 : 0;
-    const double *JkI = S.jac + 12 * (size_t)k;
-    const double *JkJ = JkI + 6;
-    const double dt = S.par[S.rodRep[rI]].dt;
+    L.aI0 = S.rowPtr[rI];
+    L.nI = S.rowPtr[rI + 1] - L.aI0;
+    L.aJ0 = rJ >= 0 ? S.rowPtr[rJ] : 0;
+    L.nJ = rJ >= 0 ? S.rowPtr[rJ + 1] - L.aJ0 : 0;
+    return L;
+}
+
+// Serial merge (lane 0, long rows): count, or write (k, eI, eJ, l) per
+// output at out0 (eI/eJ: index into rowEnt of the first entry of l in
+// rod I's / rod J's row, -1 when absent).
+template <bool fill>
+__device__ int merge_serial(const DevState &S, int k, const RowLists &L, int out0) {
     int a = 0, b = 0, cnt = 0;
-    while (a < nI || b < nJ) {
-        const int la = a < nI ? (S.rowEnt[aI0 + a] >> 1) : 0x7fffffff;
-        const int lb = b < nJ ? (S.rowEnt[aJ0 + b] >> 1) : 0x7fffffff;
+    while (a < L.nI || b < L.nJ) {
+        const int la = a < L.nI ? (S.rowEnt[L.aI0 + a] >> 1) : 0x7fffffff;
+        const int lb = b < L.nJ ? (S.rowEnt[L.aJ0 + b] >> 1) : 0x7fffffff;
         const int l = la < lb ? la : lb;
-        double acc = 0.0;
-        while (a < nI && (S.rowEnt[aI0 + a] >> 1) == l) {
-            if (fill) acc = acc + dot6d(JkI, S.W + 12 * (size_t)l + 6 * (S.rowEnt[aI0 + a] & 1));
-            a++;
-        }
-        while (b < nJ && (S.rowEnt[aJ0 + b] >> 1) == l) {
-            if (fill) acc = acc + dot6d(JkJ, S.W + 12 * (size_t)l + 6 * (S.rowEnt[aJ0 + b] & 1));
-            b++;
-        }
-        if (fill) {
-            const int o = out0 + cnt;
-            const double v = dt * acc;
-            const int kind = S.lbKind[l];
-            S.aent[o] = make_int4(l, kind, __double2loint(v), __double2hiint(v));
-            if (S.precision == ALENS_PREC_MIXED)
-                S.aent32[o] = make_int4(l, kind, __float_as_int((float)v), __float_as_int((float)S.lb[l]));
-        }
+        const int eI = la == l ? L.aI0 + a : -1, eJ = lb == l ? L.aJ0 + b : -1;
+        while (a < L.nI && (S.rowEnt[L.aI0 + a] >> 1) == l) a++;
+        while (b < L.nJ && (S.rowEnt[L.aJ0 + b] >> 1) == l) b++;
+        if (fill) S.aent[out0 + cnt] = make_int4(k, eI, eJ, l);
         cnt++;
     }
     return cnt;
 }
 
+// One warp per row: the number of outputs (fill == false) or their
+// structure records written to aent (fill == true).
+template <bool fill>
+__device__ void arow_warp(const DevState &S, int k) {
+    const int lane = threadIdx.x & 31;
+    const RowLists L = row_lists(S, k);
+    if (L.nI > 32 || L.nJ > 32) {
+        if (lane == 0) {
+            if (fill)
+                merge_serial<true>(S, k, L, S.aptr[k]);
+            else
+                S.annz[k] = merge_serial<false>(S, k, L, 0);
+        }
+        __syncwarp();
+        return;
+    }
+    constexpr int kPad = 0x3fffffff;
+    const int lI = lane < L.nI ? (S.rowEnt[L.aI0 + lane] >> 1) : kPad;
+    const int lJ = lane < L.nJ ? (S.rowEnt[L.aJ0 + lane] >> 1) : kPad;
+    const int pI = __shfl_up_sync(0xffffffffu, lI, 1), pJ = __shfl_up_sync(0xffffffffu, lJ, 1);
+    const bool leadI = lane < L.nI && (lane == 0 || pI != lI);
+    const bool leadJ = lane < L.nJ && (lane == 0 || pJ != lJ);
+    const int jInI = lane_lower_bound(lI, lJ);  // position of this lane's J value among I
+    const int lIat = __shfl_sync(0xffffffffu, lI, jInI & 31);  // every lane takes part
+    const bool inI = jInI < L.nI && lIat == lJ;
+    const unsigned int mI = __ballot_sync(0xffffffffu, leadI);
+    const unsigned int mJ = __ballot_sync(0xffffffffu, leadJ);
+    const unsigned int mBoth = __ballot_sync(0xffffffffu, leadJ && inI);
+    if (!fill) {
+        if (lane == 0) S.annz[k] = __popc(mI) + __popc(mJ) - __popc(mBoth);
+        return;
+    }
+    const int iInJ = lane_lower_bound(lJ, lI);  // position of this lane's I value among J
+    const int out0 = S.aptr[k];
+    // the J entry of an I value: lane iInJ of the J row when its value matches
+    const int lJat = __shfl_sync(0xffffffffu, lJ, iInJ & 31);
+    if (leadI) {
+        const int rank = __popc(mI & lowmask(lane)) + __popc(mJ & lowmask(iInJ)) - __popc(mBoth & lowmask(iInJ));
+        const int eJ = (iInJ < L.nJ && lJat == lI) ? L.aJ0 + iInJ : -1;
+        S.aent[out0 + rank] = make_int4(k, L.aI0 + lane, eJ, lI);
+    }
+    if (leadJ && !inI) {
+        const int rank = __popc(mJ & lowmask(lane)) + __popc(mI & lowmask(jInI)) - __popc(mBoth & lowmask(lane));
+        S.aent[out0 + rank] = make_int4(k, -1, L.aJ0 + lane, lJ);
+    }
+}
+
 __global__ void k_arow_count(DevState S) {
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < S.cap; k += gridDim.x * blockDim.x)
-        S.annz[k] = k < nc ? merge_row<false>(S, k, 0) : 0;
+    const int w = blockIdx.x * kArowWarps + (threadIdx.x >> 5);
+    for (int k = w; k < S.cap; k += gridDim.x * kArowWarps) {
+        if (k < nc)
+            arow_warp<false>(S, k);
+        else if ((threadIdx.x & 31) == 0)
+            S.annz[k] = 0;
+    }
 }
 
-__global__ void k_arow_fill(DevState S) {
+__global__ void k_arow_struct(DevState S) {
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
     const int nnz = S.aptr[nc];
@@ -102,8 +180,40 @@ __global__ void k_arow_fill(DevState S) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&S.ctl->errFlags, kErrOverflow);
         return;
     }
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x)
-        merge_row<true>(S, k, S.aptr[k]);
+    const int w = blockIdx.x * kArowWarps + (threadIdx.x >> 5);
+    for (int k = w; k < nc; k += gridDim.x * kArowWarps) arow_warp<true>(S, k);
+}
+
+// A_kl = dt * (sum over l's entries in rod I's row of J_k,I . W_l,s, then
+// over its entries in rod J's row of J_k,J . W_l,s), in entry order.
+__global__ void k_arow_values(DevState S) {
+    if (flags(S) & (kErrNaN | kErrOverflow)) return;
+    const int nc = S.ctl->totalCon;
+    const int nnz = S.aptr[nc];
+    if (nnz > S.nnzCap) return;
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < nnz; o += gridDim.x * blockDim.x) {
+        const int4 rec = S.aent[o];
+        const int k = rec.x, l = rec.w;
+        const int rI = S.conI[k], rJ = S.conJ[k];
+        const double *JkI = S.jac + 12 * (size_t)k;
+        const double *JkJ = JkI + 6;
+        double acc = 0.0;
+        if (rec.y >= 0) {
+            const int end = S.rowPtr[rI + 1];
+            for (int e = rec.y; e < end && (S.rowEnt[e] >> 1) == l; e++)
+                acc = acc + dot6d(JkI, S.W + 12 * (size_t)l + 6 * (S.rowEnt[e] & 1));
+        }
+        if (rec.z >= 0) {
+            const int end = S.rowPtr[rJ + 1];
+            for (int e = rec.z; e < end && (S.rowEnt[e] >> 1) == l; e++)
+                acc = acc + dot6d(JkJ, S.W + 12 * (size_t)l + 6 * (S.rowEnt[e] & 1));
+        }
+        const double v = S.par[S.rodRep[rI]].dt * acc;
+        const int kind = S.lbKind[l];
+        S.aent[o] = make_int4(l, kind, __double2loint(v), __double2hiint(v));
+        if (S.precision == ALENS_PREC_MIXED)
+            S.aent32[o] = make_int4(l, kind, __float_as_int((float)v), __float_as_int((float)S.lb[l]));
+    }
 }
 
 int grid_for(int n, int block) {
@@ -115,10 +225,12 @@ int grid_for(int n, int block) {
 
 int launch_assemble(const DevState &S, cudaStream_t st) {
     k_weights<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
-    k_arow_count<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
+    const int rowBlocks = grid_for(S.cap, kArowWarps);
+    k_arow_count<<<rowBlocks, 32 * kArowWarps, 0, st>>>(S);
     const int n = launch_scan(S.annz, S.aptr, S.cap, S.scanTmp, st);
-    k_arow_fill<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
-    return n + 3;
+    k_arow_struct<<<rowBlocks, 32 * kArowWarps, 0, st>>>(S);
+    k_arow_values<<<grid_for(S.nnzCap, 256), 256, 0, st>>>(S);
+    return n + 4;
 }
 
 }  // namespace alens

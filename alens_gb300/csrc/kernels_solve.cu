@@ -26,40 +26,55 @@ __global__ void k_refine_setup(DevState S) {
     const int nIdx = S.ctl->nTiles * kRowTile;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nIdx; idx += gridDim.x * blockDim.x) {
         const int T = idx / kRowTile;
-        RepDyn &d = S.dyn[S.tileRep[T]];
+        const int rep = S.tileRep[T];
+        RepDyn &d = S.dyn[rep];
         const int local = (T - d.tileStart) * kRowTile + idx % kRowTile;
-        if (local >= d.nCon) continue;
-        const int k = d.conStart + local;
-        const float2 *src = d.finalPar ? S.st32[1] : S.st32[0];
-        const double lbk = S.lb[k];
-        double xk = (double)src[k].x;
-        xk = xk < lbk ? lbk : xk;
-        S.st[1][k] = make_double2(xk, 0.0);
-        if (d.refined || d.status != ALENS_OK) continue;
-        double acc = 0.0;
-        const int e0 = S.aptr[k], e1 = S.aptr[k + 1];
-        for (int eb = e0; eb < e1; eb += kRowPrefetch) {
-            int4 en[kRowPrefetch];
-            float xs[kRowPrefetch];
+        unsigned long long bits = 0ULL;  // residual of this row (0: not counted)
+        if (local < d.nCon) {
+            const int k = d.conStart + local;
+            const float2 *src = d.finalPar ? S.st32[1] : S.st32[0];
+            const double lbk = S.lb[k];
+            double xk = (double)src[k].x;
+            xk = xk < lbk ? lbk : xk;
+            S.st[1][k] = make_double2(xk, 0.0);
+            if (!d.refined && d.status == ALENS_OK) {
+                double acc = 0.0;
+                const int e0 = S.aptr[k], e1 = S.aptr[k + 1];
+                for (int eb = e0; eb < e1; eb += kRowPrefetch) {
+                    int4 en[kRowPrefetch];
+                    float xs[kRowPrefetch];
 #pragma unroll
-            for (int j = 0; j < kRowPrefetch; j++) en[j] = eb + j < e1 ? __ldg(S.aent + eb + j) : make_int4(k, 1, 0, 0);
+                    for (int j = 0; j < kRowPrefetch; j++)
+                        en[j] = eb + j < e1 ? __ldg(S.aent + eb + j) : make_int4(k, 1, 0, 0);
 #pragma unroll
-            for (int j = 0; j < kRowPrefetch; j++) xs[j] = src[en[j].x].x;
+                    for (int j = 0; j < kRowPrefetch; j++) xs[j] = src[en[j].x].x;
 #pragma unroll
-            for (int j = 0; j < kRowPrefetch; j++) {
-                if (eb + j < e1) {
-                    const double lbl = en[j].y == 0 ? 0.0 : (en[j].y == 1 ? -INFINITY : S.lb[en[j].x]);
-                    double xl = (double)xs[j];
-                    xl = xl < lbl ? lbl : xl;
-                    acc = fma(__hiloint2double(en[j].w, en[j].z), xl, acc);
+                    for (int j = 0; j < kRowPrefetch; j++) {
+                        if (eb + j < e1) {
+                            const double lbl = en[j].y == 0 ? 0.0 : (en[j].y == 1 ? -INFINITY : S.lb[en[j].x]);
+                            double xl = (double)xs[j];
+                            xl = xl < lbl ? lbl : xl;
+                            acc = fma(__hiloint2double(en[j].w, en[j].z), xl, acc);
+                        }
+                    }
                 }
+                acc = fma(S.qc[k].y, xk, acc);
+                const double gn = acc + S.qc[k].x;
+                const double pr = xk - gn < lbk ? lbk : xk - gn;
+                const double rr = fabs(xk - pr);
+                bits = (unsigned long long)__double_as_longlong(rr == rr ? rr : INFINITY);
             }
         }
-        acc = fma(S.qc[k].y, xk, acc);
-        const double gn = acc + S.qc[k].x;
-        const double pr = xk - gn < lbk ? lbk : xk - gn;
-        const double rr = fabs(xk - pr);
-        atomicMax(&d.res64bits, (unsigned long long)__double_as_longlong(rr == rr ? rr : INFINITY));
+        // max over the warp's lanes of the same replica (non-negative
+        // doubles order like their bit patterns), one atomic per group: a
+        // per-row atomic on the replica's word serialises at one L2 slice
+        const unsigned int act = __activemask();
+        const unsigned int grp = __match_any_sync(act, rep);
+        const unsigned int hi = (unsigned int)(bits >> 32);
+        const unsigned int hiMax = __reduce_max_sync(grp, hi);
+        const unsigned int loMax = __reduce_max_sync(grp, hi == hiMax ? (unsigned int)bits : 0u);
+        if ((threadIdx.x & 31) == __ffs(grp) - 1 && (hiMax | loMax) != 0u)
+            atomicMax(&d.res64bits, ((unsigned long long)hiMax << 32) | loMax);
     }
     __threadfence();
     __syncthreads();
