@@ -693,22 +693,26 @@ __device__ inline bool grid_sync(GridBarrier *bar, unsigned int nblocks, int *er
 // Barrier ending pass p of the BBPGD kernel.  The generation word counts
 // barriers in its upper bits (gen >> 1 = barriers completed since the
 // solver was armed, target = p + 1) and carries in bit 0 whether the pass
-// left every replica retired: the last block to arrive reads the pass's
-// active count (every arrival's increments are visible to it through the
-// acq_rel chain on the counter) and publishes both in one release, so the
-// other blocks learn "continue or stop" from the same load that releases
-// them.  Bounded like grid_sync.
+// left every replica retired.  Each block's arrival adds
+// 1 + (act << kBarActShift) to the counter, act = the replicas it owns
+// that iterated in this pass, so the last block to arrive reads the pass's
+// total active count from its own atomic's return value and publishes
+// "continue or stop" in the same release that frees the others (no
+// further load on the critical path).  Bounded like grid_sync.
+constexpr int kBarActShift = 12;  // arrivals in the low 12 bits (up to 4095 blocks)
+
 __device__ inline bool grid_sync_pass(GridBarrier *bar, unsigned int nblocks, int *err,
-                                      unsigned long long timeout_ns, unsigned int target,
-                                      const int *activeCnt, int &stop) {
+                                      unsigned long long timeout_ns, unsigned int target, int act,
+                                      int &stop) {
     __shared__ int s_ok, s_stop;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1, st = 0;
-        const unsigned int arrived = atom_add_acqrel_u32(&bar->count, 1u);
-        if (arrived == nblocks - 1) {
+        const unsigned int add = 1u + ((unsigned int)act << kBarActShift);
+        const unsigned int old = atom_add_acqrel_u32(&bar->count, add);
+        if ((old & ((1u << kBarActShift) - 1u)) == nblocks - 1) {
             st_relaxed_u32(&bar->count, 0u);
-            st = ld_acquire_u32(reinterpret_cast<const unsigned int *>(activeCnt)) == 0u ? 1 : 0;
+            st = ((old + add) >> kBarActShift) == 0u ? 1 : 0;
             atom_add_release_u32(&bar->gen, 2u + (unsigned int)st);
         } else {
             unsigned long long t0 = 0;

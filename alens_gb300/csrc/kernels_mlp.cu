@@ -47,7 +47,9 @@ namespace {
 
 constexpr unsigned long long kMmaTimeoutNs = 1000000000ULL;  // 1 s
 
-__device__ __forceinline__ float sigmoidf_(float a) { return 1.0f / (1.0f + expf(-a)); }
+// fast exponential and divide (a few instructions each): the activations
+// are rounded to BF16 before the next layer, far coarser than their error
+__device__ __forceinline__ float sigmoidf_(float a) { return __fdividef(1.0f, 1.0f + __expf(-a)); }
 __device__ __forceinline__ float siluf_(float a) { return a * sigmoidf_(a); }
 __device__ __forceinline__ float dsiluf_(float a) {
     const float s = sigmoidf_(a);
@@ -69,14 +71,26 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
     const float d = (float)S.rcol[I] + (float)S.rcol[J];
     float akk = 0.0f, nb = 0.0f;
     const int e0 = S.aptr[k], e1 = S.aptr[k + 1];
-    for (int e = e0; e < e1; e++) {
-        const int4 en = __ldg(S.aent + e);
-        const float v = (float)__hiloint2double(en.w, en.z);
-        if (en.x == k) {
-            akk = v;
-        } else if (en.y == 0) {
-            const float ql = (float)S.q[en.x];
-            if (ql < 0.0f) nb = fmaf(v, -ql, nb);
+    constexpr int kB = 8;
+    for (int eb = e0; eb < e1; eb += kB) {
+        // the batch's entries, then all their neighbours' q, are requested
+        // before any is used; the sum keeps the entry order
+        int4 en[kB];
+#pragma unroll
+        for (int j = 0; j < kB; j++) en[j] = eb + j < e1 ? __ldg(S.aent + eb + j) : make_int4(k, 1, 0, 0);
+        float ql[kB];
+#pragma unroll
+        for (int j = 0; j < kB; j++) ql[j] = (en[j].x != k && en[j].y == 0) ? (float)S.q[en[j].x] : 0.0f;
+#pragma unroll
+        for (int j = 0; j < kB; j++) {
+            if (eb + j < e1) {
+                const float v = (float)__hiloint2double(en[j].w, en[j].z);
+                if (en[j].x == k) {
+                    akk = v;
+                } else if (en[j].y == 0) {
+                    if (ql[j] < 0.0f) nb = fmaf(v, -ql[j], nb);
+                }
+            }
         }
     }
     if (!(akk > 0.0f) || !(d > 0.0f)) return false;

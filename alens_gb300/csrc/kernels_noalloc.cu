@@ -210,8 +210,11 @@ __global__ void __launch_bounds__(kSolveThreads) k_noalloc_solve(DevState S, Sol
     int lastPass = 0;
     for (int p = 0; p <= maxPass; p++) {
         if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl->activeCnt[(p + 1) % 3] = 0;
+        if (threadIdx.x == 0) sh.act = 0;
         double *partBase = S.part + (size_t)(p & 1) * 4 * tc;
         if (t0 < t1) decide<double>(S, V, p, 0, t0, t1, sh, 0);
+        // the block owning the replica counts it active for this pass
+        if (threadIdx.x == 0 && sh.act) atomicAdd(&S.ctl->activeCnt[p % 3], sh.act);
         const int mode = sh.mode[0];
         const double alpha = sh.alpha[0];
         const bool odd = (p & 1) != 0;

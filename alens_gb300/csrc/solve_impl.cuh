@@ -205,6 +205,7 @@ struct SolveShared {
     double alpha[kWindow];
     int mode[kWindow];
     double tileVal[4][2][4];  // [group][warp][kind]
+    int act;                  // replicas owned by this block iterating in this pass
 #ifdef ALENS_TRACE
     long long trRed;
 #endif
@@ -227,7 +228,7 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
             const bool done = d.refined != 0;
             sh.mode[slot] = done ? kModeCopy : kModeG0;
             sh.alpha[slot] = 0.0;
-            if (!done && d.nCon > 0 && d.tileStart >= t0 && d.tileStart < t1) atomicAdd(&S.ctl->activeCnt[0], 1);
+            if (!done && d.nCon > 0 && d.tileStart >= t0 && d.tileStart < t1) sh.act++;
         }
         __syncthreads();
         return;
@@ -311,7 +312,7 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
                 dw->active = 0;
             }
             if (mode != kModeCopy) {
-                atomicAdd(&S.ctl->activeCnt[p % 3], 1);
+                sh.act++;
                 __stcg(V.alphaBuf + (size_t)(p & 1) * S.R + r, alpha);
             }
         }
@@ -342,6 +343,7 @@ __host__ __device__ constexpr int row_cache_ents() {
     return (kSolveDynSmem - 4 * (kRowCacheRows + 4)) / (16 + (int)sizeof(typename Vec2<Real>::T));
 }
 constexpr int kGatherWarp0 = 4;                      // warps kGatherWarp0.. gather
+static_assert(kMaxSolverGrid < (1 << kBarActShift), "barrier arrival field too narrow");
 
 // Start of a pass: the upper warps copy the previous iterate of every
 // cached entry's column into shared memory (asynchronous copies, all in
@@ -592,7 +594,7 @@ __global__ void __launch_bounds__(kSolveThreads, 2) k_solve(DevState S, SolveVie
         long long cDec = 0, cRow = 0, cStore = 0;
         sh.trRed = 0;
 #endif
-        if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl->activeCnt[(p + 1) % 3] = 0;
+        if (threadIdx.x == 0) sh.act = 0;
         double *partBase = S.part + (size_t)(p & 1) * 4 * tc;
         // completes before the first decide()'s __syncthreads
         gather_columns<Real>(C, (p & 1) ? V.st[0] : V.st[1]);
@@ -640,7 +642,7 @@ __global__ void __launch_bounds__(kSolveThreads, 2) k_solve(DevState S, SolveVie
 #endif
         int stop = 0;
         if (!grid_sync_pass(&S.ctl->bar, (unsigned int)nActive, &S.ctl->errFlags, timeout_ns, (unsigned int)(p + 1),
-                            &S.ctl->activeCnt[p % 3], stop))
+                            sh.act, stop))
             return;
 #ifdef ALENS_TRACE
         const unsigned long long trT3 = global_ns();
