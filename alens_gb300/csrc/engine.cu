@@ -192,6 +192,8 @@ void Engine::makeParams(int rep, const HostRods &h, RepParams &P) const {
     P.maxIte = c.conMaxIte;
     P.nRods = h.n;
     P.halfReachMax = 0.5 * mx;
+    // the same IEEE operations as the per-rod expression it replaces
+    P.bcoef = c.KBT > 0.0 ? std::sqrt(2.0 * c.KBT / c.dt) : 0.0;
 }
 
 void Engine::finalize() {
@@ -251,7 +253,8 @@ void Engine::finalize() {
     // rods
     auto &G = rodAllocs_;
     double **rodD[] = {&S.px, &S.py, &S.pz, &S.qx, &S.qy, &S.qz, &S.qw, &S.len, &S.rad,
-                       &S.ax, &S.ay, &S.az, &S.hcol, &S.rcol, &S.m0, &S.m1, &S.m2};
+                       &S.ax, &S.ay, &S.az, &S.hcol, &S.rcol, &S.m0, &S.m1, &S.m2,
+                       &S.sm0, &S.sm1, &S.sm2};
     for (double **p : rodD) *p = alloc<double>(G, N);
     S.sA = alloc<float4>(G, N);
     S.sB = alloc<float4>(G, N);

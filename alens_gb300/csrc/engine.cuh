@@ -41,6 +41,7 @@ struct RepParams {
     int maxIte;
     int pad;
     double halfReachMax;  // max over rods of collision half-length + radius
+    double bcoef;         // sqrt(2 kT / dt), Brownian velocity scale (kT > 0)
 };
 
 // per-replica state produced on the device
@@ -86,6 +87,7 @@ struct DevState {
     long long *gid;
     int *imm, *rodRep;
     double *ax, *ay, *az, *hcol, *rcol, *m0, *m1, *m2;
+    double *sm0, *sm1, *sm2;   // square roots of the mobilities (Brownian noise)
     unsigned char *sph;
     double *unc, *vel;      // 6 x nRods SoA each
     double *stage;          // 7 x nRods host-transfer staging (interleaved)

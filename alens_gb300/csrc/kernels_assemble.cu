@@ -26,13 +26,14 @@ __device__ __forceinline__ double dot6d(const double *a, const double *b) {
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3] + a[4] * b[4] + a[5] * b[5];
 }
 
-// W = M J for both sides of every constraint.
+// W = M J for both sides of every constraint, one thread per side
+// (adjacent lanes: the two sides of a constraint).
 __global__ void k_weights(DevState S) {
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) {
-#pragma unroll
-        for (int side = 0; side < 2; side++) {
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < 2 * nc; it += gridDim.x * blockDim.x) {
+        const int k = it >> 1, side = it & 1;
+        {
             const int r = side == 0 ? S.conI[k] : S.conJ[k];
             double U[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
             if (r >= 0 && !S.imm[r]) {
@@ -224,7 +225,7 @@ int grid_for(int n, int block) {
 }  // namespace
 
 int launch_assemble(const DevState &S, cudaStream_t st) {
-    k_weights<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
+    k_weights<<<grid_for(2 * S.cap, 128), 128, 0, st>>>(S);
     const int rowBlocks = grid_for(S.cap, kArowWarps);
     k_arow_count<<<rowBlocks, 32 * kArowWarps, 0, st>>>(S);
     const int n = launch_scan(S.annz, S.aptr, S.cap, S.scanTmp, st);

@@ -68,10 +68,9 @@ __global__ void k_prep(DevState S) {
         S.hcol[r] = sphere ? 0.0 : 0.5 * (L * P.colRatioL);
         S.rcol[r] = rad * P.colRatioD;
         const bool imm = S.imm[r] != 0;
-        const double m[3] = {S.m0[r], S.m1[r], S.m2[r]};
         double u[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         if (P.kT > 0.0 && !imm) {
-            const double bc = sqrt(2.0 * P.kT / P.dt);
+            const double bc = P.bcoef;
             double z[6];
             normals6(P.seed, S.gid[r], step, z);
             if (P.mono) {
@@ -81,7 +80,7 @@ __global__ void k_prep(DevState S) {
             }
             double w[6];
             if (sphere) {
-                const double st = sqrt(m[0]), sr = sqrt(m[2]);
+                const double st = S.sm0[r], sr = S.sm2[r];
                 w[0] = st * z[0];
                 w[1] = st * z[1];
                 w[2] = st * z[2];
@@ -89,7 +88,7 @@ __global__ void k_prep(DevState S) {
                 w[4] = sr * z[4];
                 w[5] = sr * z[5];
             } else {
-                const double sp = sqrt(m[0]), sq = sqrt(m[1]), sr = sqrt(m[2]);
+                const double sp = S.sm0[r], sq = S.sm1[r], sr = S.sm2[r];
                 const double za = a[0] * z[0] + a[1] * z[1] + a[2] * z[2];
                 w[0] = sp * za * a[0] + sq * (z[0] - za * a[0]);
                 w[1] = sp * za * a[1] + sq * (z[1] - za * a[1]);
@@ -128,6 +127,9 @@ __global__ void k_mobility(DevState S) {
         S.m0[r] = m[0];
         S.m1[r] = m[1];
         S.m2[r] = m[2];
+        S.sm0[r] = sqrt(m[0]);
+        S.sm1[r] = sqrt(m[1]);
+        S.sm2[r] = sqrt(m[2]);
     }
 }
 
@@ -202,6 +204,83 @@ __global__ void k_scan_top(int *tmp, int nb, int *out, int n) {
     for (int k = 0; k < 4; k++) {
         if (base + k < nb) tmp[base + k] = ex;
         ex += v[k];
+    }
+    if (threadIdx.x == 0) out[n] = tot;
+}
+
+// Exclusive scan of up to kScanSingleMax ints by one 1024-thread block,
+// one launch instead of three for the per-rod and per-cell counts.  Warp w owns the contiguous segment [w G, (w + 1) G) (G a
+// multiple of 128); its lanes read consecutive int4 (coalesced), a round's
+// loads all in flight together.  Pass 1 sums each segment, one block scan
+// over the 32 segment totals gives the offsets, pass 2 re-reads the
+// segment and writes the prefixes (warp scan per 128 elements plus a
+// running carry).
+constexpr int kScanSingleThreads = 1024;
+constexpr int kScanSingleMax = 32768;  // above this the three-pass scan is faster
+constexpr int kScanRound = 4;  // int4 loads per lane per round
+
+__device__ __forceinline__ int4 scan_load4(const int *in, int i, int end, bool vec) {
+    if (vec && i + 3 < end) return *reinterpret_cast<const int4 *>(in + i);
+    int4 q;
+    q.x = i < end ? in[i] : 0;
+    q.y = i + 1 < end ? in[i + 1] : 0;
+    q.z = i + 2 < end ? in[i + 2] : 0;
+    q.w = i + 3 < end ? in[i + 3] : 0;
+    return q;
+}
+
+__global__ void __launch_bounds__(kScanSingleThreads) k_scan_single(const int *in, int *out, int n, int vec) {
+    __shared__ int sm[33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int G = (((n + 31) / 32) + 127) & ~127;
+    const int s0 = min(warp * G, n), s1 = min(s0 + G, n);
+    int s = 0;
+    for (int r = s0; r < s1; r += 128 * kScanRound) {
+        int4 q[kScanRound];
+#pragma unroll
+        for (int j = 0; j < kScanRound; j++) q[j] = scan_load4(in, r + 128 * j + 4 * lane, s1, vec != 0);
+#pragma unroll
+        for (int j = 0; j < kScanRound; j++) s += q[j].x + q[j].y + q[j].z + q[j].w;
+    }
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    int tot;
+    // every lane of a warp holds the same s: the block scan sees it once
+    const int segOff = block_exclusive_scan(lane == 0 ? s : 0, sm, &tot);
+    int carry = __shfl_sync(0xffffffffu, segOff, 0);
+    for (int r = s0; r < s1; r += 128 * kScanRound) {
+        int4 q[kScanRound];
+#pragma unroll
+        for (int j = 0; j < kScanRound; j++) q[j] = scan_load4(in, r + 128 * j + 4 * lane, s1, vec != 0);
+#pragma unroll
+        for (int j = 0; j < kScanRound; j++) {
+            const int i = r + 128 * j + 4 * lane;
+            const int t = q[j].x + q[j].y + q[j].z + q[j].w;
+            int inc = t;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int o = __shfl_up_sync(0xffffffffu, inc, off);
+                if (lane >= off) inc += o;
+            }
+            int ex = carry + inc - t;
+            int4 o;
+            o.x = ex;
+            ex += q[j].x;
+            o.y = ex;
+            ex += q[j].y;
+            o.z = ex;
+            ex += q[j].z;
+            o.w = ex;
+            if (vec && i + 3 < s1) {
+                *reinterpret_cast<int4 *>(out + i) = o;
+            } else {
+                if (i < s1) out[i] = o.x;
+                if (i + 1 < s1) out[i + 1] = o.y;
+                if (i + 2 < s1) out[i + 2] = o.z;
+                if (i + 3 < s1) out[i + 3] = o.w;
+            }
+            carry += __shfl_sync(0xffffffffu, inc, 31);
+        }
     }
     if (threadIdx.x == 0) out[n] = tot;
 }
@@ -825,6 +904,11 @@ void launch_mobility(const DevState &S, cudaStream_t st) {
 }
 
 int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st) {
+    if (n <= kScanSingleMax) {
+        const int vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0 ? 1 : 0;
+        k_scan_single<<<1, kScanSingleThreads, 0, st>>>(in, out, n, vec);
+        return 1;
+    }
     const int nb = (n + kScanSpan - 1) / kScanSpan;
     if (nb > 0) k_scan_block<<<nb, kScanBlock, 0, st>>>(in, out, n, tmp);
     k_scan_top<<<1, 1024, 0, st>>>(tmp, nb, out, n);
