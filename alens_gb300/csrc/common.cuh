@@ -608,6 +608,7 @@ struct GridBarrier {
     unsigned int pad0[31];
     unsigned int gen;
     unsigned int pad1[31];
+    unsigned int pass[3][32];  // BBPGD pass counters (pass p uses pass[p % 3][0])
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -690,55 +691,50 @@ __device__ inline bool grid_sync(GridBarrier *bar, unsigned int nblocks, int *er
     return s_ok != 0;
 }
 
-// Barrier ending pass p of the BBPGD kernel.  The generation word counts
-// barriers in its upper bits (gen >> 1 = barriers completed since the
-// solver was armed, target = p + 1) and carries in bit 0 whether the pass
-// left every replica retired.  Each block's arrival adds
-// 1 + (act << kBarActShift) to the counter, act = the replicas it owns
-// that iterated in this pass, so the last block to arrive reads the pass's
-// total active count from its own atomic's return value and publishes
-// "continue or stop" in the same release that frees the others (no
-// further load on the critical path).  Bounded like grid_sync.
+// Barrier ending pass p of the BBPGD kernel.  Pass p has its own counter
+// (three in rotation); each block adds 1 + (act << kBarActShift) to it with
+// one release reduction (act = the replicas it owns that iterated in this
+// pass) and then polls it until all nblocks arrivals are in.  The final
+// value also gives the pass's total active count, hence "continue or
+// stop", so no block waits on a last arriver's second store.  Block 0
+// clears the counter of pass p + 1 during pass p (its last use was pass
+// p - 2, which every block has left).  Bounded like grid_sync.
 constexpr int kBarActShift = 12;  // arrivals in the low 12 bits (up to 4095 blocks)
 
+__device__ __forceinline__ void red_add_release_u32(unsigned int *p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ inline bool grid_sync_pass(GridBarrier *bar, unsigned int nblocks, int *err,
-                                      unsigned long long timeout_ns, unsigned int target, int act,
-                                      int &stop) {
+                                      unsigned long long timeout_ns, int p, int act, int &stop) {
     __shared__ int s_ok, s_stop;
     __syncthreads();
     if (threadIdx.x == 0) {
-        int ok = 1, st = 0;
-        const unsigned int add = 1u + ((unsigned int)act << kBarActShift);
-        const unsigned int old = atom_add_acqrel_u32(&bar->count, add);
-        if ((old & ((1u << kBarActShift) - 1u)) == nblocks - 1) {
-            st_relaxed_u32(&bar->count, 0u);
-            st = ((old + add) >> kBarActShift) == 0u ? 1 : 0;
-            atom_add_release_u32(&bar->gen, 2u + (unsigned int)st);
-        } else {
-            unsigned long long t0 = 0;
-            unsigned int spins = 0;
-            unsigned int g;
-            while (((g = ld_acquire_u32(&bar->gen)) >> 1) < target) {
-                if (++spins > 64) {
-                    __nanosleep(spins > 1024 ? 256 : 32);
-                    if ((spins & 255) == 0) {
-                        if (t0 == 0) t0 = global_ns();
-                        if (ld_volatile_i32(err) & kErrTimeout) {
-                            ok = 0;
-                            break;
-                        }
-                        if (global_ns() - t0 > timeout_ns) {
-                            atomicOr(err, kErrTimeout);
-                            ok = 0;
-                            break;
-                        }
+        int ok = 1;
+        unsigned int *c = &bar->pass[p % 3][0];
+        red_add_release_u32(c, 1u + ((unsigned int)act << kBarActShift));
+        unsigned long long t0 = 0;
+        unsigned int spins = 0;
+        unsigned int v;
+        while (((v = ld_acquire_u32(c)) & ((1u << kBarActShift) - 1u)) < nblocks) {
+            if (++spins > 64) {
+                __nanosleep(spins > 1024 ? 256 : 32);
+                if ((spins & 255) == 0) {
+                    if (t0 == 0) t0 = global_ns();
+                    if (ld_volatile_i32(err) & kErrTimeout) {
+                        ok = 0;
+                        break;
+                    }
+                    if (global_ns() - t0 > timeout_ns) {
+                        atomicOr(err, kErrTimeout);
+                        ok = 0;
+                        break;
                     }
                 }
             }
-            st = (int)(g & 1u);
         }
         s_ok = ok;
-        s_stop = st;
+        s_stop = (v >> kBarActShift) == 0u ? 1 : 0;
     }
     __syncthreads();
     stop = s_stop;

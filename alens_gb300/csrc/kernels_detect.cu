@@ -648,6 +648,7 @@ __global__ void k_ranges(DevState S) {
         c->maxIte = maxIte;
         c->bar.count = 0;
         c->bar.gen = 0;
+        c->bar.pass[0][0] = c->bar.pass[1][0] = c->bar.pass[2][0] = 0u;
         int ok = 1;
         if (c->totalCon > S.cap || tile > S.tileCap) {
             atomicOr(&c->errFlags, kErrOverflow);

@@ -90,6 +90,7 @@ __global__ void k_noalloc_setup(NoAllocScratch *sc, PlainOperator op, const doub
         c.setupDone = 0u;
         c.bar.count = 0;
         c.bar.gen = 0;
+        c.bar.pass[0][0] = c.bar.pass[1][0] = c.bar.pass[2][0] = 0u;
         RepDyn &d = sc->dyn;
         d.collStart = 0;
         d.collEnd = n;

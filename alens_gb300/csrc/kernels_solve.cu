@@ -119,6 +119,7 @@ __global__ void k_solver_arm(DevState S) {
     c->activeCnt[0] = c->activeCnt[1] = c->activeCnt[2] = 0;
     c->bar.count = 0;
     c->bar.gen = 0;
+    c->bar.pass[0][0] = c->bar.pass[1][0] = c->bar.pass[2][0] = 0u;
     c->finalParity = 1;
 }
 

@@ -595,6 +595,7 @@ __global__ void __launch_bounds__(kSolveThreads, 2) k_solve(DevState S, SolveVie
         sh.trRed = 0;
 #endif
         if (threadIdx.x == 0) sh.act = 0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) st_relaxed_u32(&S.ctl->bar.pass[(p + 1) % 3][0], 0u);
         double *partBase = S.part + (size_t)(p & 1) * 4 * tc;
         // completes before the first decide()'s __syncthreads
         gather_columns<Real>(C, (p & 1) ? V.st[0] : V.st[1]);
@@ -641,8 +642,7 @@ __global__ void __launch_bounds__(kSolveThreads, 2) k_solve(DevState S, SolveVie
         cStore = clock64();
 #endif
         int stop = 0;
-        if (!grid_sync_pass(&S.ctl->bar, (unsigned int)nActive, &S.ctl->errFlags, timeout_ns, (unsigned int)(p + 1),
-                            sh.act, stop))
+        if (!grid_sync_pass(&S.ctl->bar, (unsigned int)nActive, &S.ctl->errFlags, timeout_ns, p, sh.act, stop))
             return;
 #ifdef ALENS_TRACE
         const unsigned long long trT3 = global_ns();
