@@ -51,35 +51,10 @@ __global__ void k_weights(DevState S) {
 }
 
 // Row k of A is the merge of the rod rows of k's two rods (entries 2l+s,
-// ascending): one output per distinct l, in ascending l.  The structure is
-// found by one warp per row (integer work only): lane a holds entry a of
-// rod I's row and of rod J's row; a lane is the leader of its l when the
-// previous entry of its row has another l; an output's position is the
-// number of distinct l below it in the union (leaders before it in its own
-// row, leaders below it in the other row, less the values counted twice),
-// found with ballots and a lower bound over the other row's lanes.  Rows
-// with more than 32 entries on either rod are merged by lane 0 alone.
-// The values are then formed by one thread per output (full warps for the
-// FP64 pipe).
-constexpr int kArowWarps = 8;  // rows per 256-thread block
-
-__device__ __forceinline__ unsigned int lowmask(int n) { return n >= 32 ? 0xffffffffu : ((1u << n) - 1u); }
-
-// First lane index in [0, 32) whose value (ascending over lanes, padded
-// with large values) is >= x; 32 when none.
-__device__ __forceinline__ int lane_lower_bound(int vals, int x) {
-    int lo = 0, hi = 32;
-#pragma unroll
-    for (int it = 0; it < 6; it++) {
-        const int mid = (lo + hi) >> 1;
-        const int v = __shfl_sync(0xffffffffu, vals, mid & 31);
-        const bool go = lo < hi && v < x;
-        lo = go ? mid + 1 : lo;
-        hi = (lo < hi && !go) ? mid : hi;
-    }
-    return lo;
-}
-
+// ascending): one output per distinct l, in ascending l.  The structure
+// (which entries of the two rod rows feed each output) is found by one
+// thread per row with integer work only; the values are then formed by one
+// thread per output (full warps for the FP64 pipe).
 struct RowLists {
     int aI0, nI, aJ0, nJ;
 };
@@ -94,11 +69,11 @@ __device__ __forceinline__ RowLists row_lists(const DevState &S, int k) {
     return L;
 }
 
-// Serial merge (lane 0, long rows): count, or write (k, eI, eJ, l) per
-// output at out0 (eI/eJ: index into rowEnt of the first entry of l in
-// rod I's / rod J's row, -1 when absent).
+// Merge of the two rod rows: the number of outputs, or (fill) the record
+// (k, eI, eJ, l) of each output written to aent at out0 (eI/eJ: index into
+// rowEnt of the first entry of l in rod I's / rod J's row, -1 when absent).
 template <bool fill>
-__device__ int merge_serial(const DevState &S, int k, const RowLists &L, int out0) {
+__device__ int merge_rows(const DevState &S, int k, const RowLists &L, int out0) {
     int a = 0, b = 0, cnt = 0;
     while (a < L.nI || b < L.nJ) {
         const int la = a < L.nI ? (S.rowEnt[L.aI0 + a] >> 1) : 0x7fffffff;
@@ -113,63 +88,11 @@ __device__ int merge_serial(const DevState &S, int k, const RowLists &L, int out
     return cnt;
 }
 
-// One warp per row: the number of outputs (fill == false) or their
-// structure records written to aent (fill == true).
-template <bool fill>
-__device__ void arow_warp(const DevState &S, int k) {
-    const int lane = threadIdx.x & 31;
-    const RowLists L = row_lists(S, k);
-    if (L.nI > 32 || L.nJ > 32) {
-        if (lane == 0) {
-            if (fill)
-                merge_serial<true>(S, k, L, S.aptr[k]);
-            else
-                S.annz[k] = merge_serial<false>(S, k, L, 0);
-        }
-        __syncwarp();
-        return;
-    }
-    constexpr int kPad = 0x3fffffff;
-    const int lI = lane < L.nI ? (S.rowEnt[L.aI0 + lane] >> 1) : kPad;
-    const int lJ = lane < L.nJ ? (S.rowEnt[L.aJ0 + lane] >> 1) : kPad;
-    const int pI = __shfl_up_sync(0xffffffffu, lI, 1), pJ = __shfl_up_sync(0xffffffffu, lJ, 1);
-    const bool leadI = lane < L.nI && (lane == 0 || pI != lI);
-    const bool leadJ = lane < L.nJ && (lane == 0 || pJ != lJ);
-    const int jInI = lane_lower_bound(lI, lJ);  // position of this lane's J value among I
-    const int lIat = __shfl_sync(0xffffffffu, lI, jInI & 31);  // every lane takes part
-    const bool inI = jInI < L.nI && lIat == lJ;
-    const unsigned int mI = __ballot_sync(0xffffffffu, leadI);
-    const unsigned int mJ = __ballot_sync(0xffffffffu, leadJ);
-    const unsigned int mBoth = __ballot_sync(0xffffffffu, leadJ && inI);
-    if (!fill) {
-        if (lane == 0) S.annz[k] = __popc(mI) + __popc(mJ) - __popc(mBoth);
-        return;
-    }
-    const int iInJ = lane_lower_bound(lJ, lI);  // position of this lane's I value among J
-    const int out0 = S.aptr[k];
-    // the J entry of an I value: lane iInJ of the J row when its value matches
-    const int lJat = __shfl_sync(0xffffffffu, lJ, iInJ & 31);
-    if (leadI) {
-        const int rank = __popc(mI & lowmask(lane)) + __popc(mJ & lowmask(iInJ)) - __popc(mBoth & lowmask(iInJ));
-        const int eJ = (iInJ < L.nJ && lJat == lI) ? L.aJ0 + iInJ : -1;
-        S.aent[out0 + rank] = make_int4(k, L.aI0 + lane, eJ, lI);
-    }
-    if (leadJ && !inI) {
-        const int rank = __popc(mJ & lowmask(lane)) + __popc(mI & lowmask(jInI)) - __popc(mBoth & lowmask(lane));
-        S.aent[out0 + rank] = make_int4(k, -1, L.aJ0 + lane, lJ);
-    }
-}
-
 __global__ void k_arow_count(DevState S) {
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
-    const int w = blockIdx.x * kArowWarps + (threadIdx.x >> 5);
-    for (int k = w; k < S.cap; k += gridDim.x * kArowWarps) {
-        if (k < nc)
-            arow_warp<false>(S, k);
-        else if ((threadIdx.x & 31) == 0)
-            S.annz[k] = 0;
-    }
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < S.cap; k += gridDim.x * blockDim.x)
+        S.annz[k] = k < nc ? merge_rows<false>(S, k, row_lists(S, k), 0) : 0;
 }
 
 __global__ void k_arow_struct(DevState S) {
@@ -181,8 +104,8 @@ __global__ void k_arow_struct(DevState S) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&S.ctl->errFlags, kErrOverflow);
         return;
     }
-    const int w = blockIdx.x * kArowWarps + (threadIdx.x >> 5);
-    for (int k = w; k < nc; k += gridDim.x * kArowWarps) arow_warp<true>(S, k);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x)
+        merge_rows<true>(S, k, row_lists(S, k), S.aptr[k]);
 }
 
 // A_kl = dt * (sum over l's entries in rod I's row of J_k,I . W_l,s, then
@@ -226,10 +149,9 @@ int grid_for(int n, int block) {
 
 int launch_assemble(const DevState &S, cudaStream_t st) {
     k_weights<<<grid_for(2 * S.cap, 128), 128, 0, st>>>(S);
-    const int rowBlocks = grid_for(S.cap, kArowWarps);
-    k_arow_count<<<rowBlocks, 32 * kArowWarps, 0, st>>>(S);
+    k_arow_count<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
     const int n = launch_scan(S.annz, S.aptr, S.cap, S.scanTmp, st);
-    k_arow_struct<<<rowBlocks, 32 * kArowWarps, 0, st>>>(S);
+    k_arow_struct<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
     k_arow_values<<<grid_for(S.nnzCap, 256), 256, 0, st>>>(S);
     return n + 4;
 }
