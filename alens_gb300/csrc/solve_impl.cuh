@@ -41,9 +41,10 @@ constexpr int kRowTile = 64;         // level-1 reduction tile
 constexpr int kWindow = 64;          // replicas decided per block window
 constexpr int kRowPrefetch = 8;      // row entries loaded together
 #ifndef ALENS_ROW_PREFETCH_F32
-#define ALENS_ROW_PREFETCH_F32 16
+#define ALENS_ROW_PREFETCH_F32 8
 #endif
-// entries per gather batch of the FP32 form (FP64 keeps 8: register budget)
+// entries per gather batch of the FP32 form (8: with 16 the kernel spills
+// past its 128-register budget and runs ~5 % slower)
 template <class Real>
 struct RowBatch {
     static constexpr int value = kRowPrefetch;
