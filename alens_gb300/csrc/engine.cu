@@ -78,6 +78,11 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
         const std::string f(e);
         formRequest_ = f == "grid" ? kFormGrid : (f == "cluster" ? kFormCluster : (f == "resident" ? kFormResident : -1));
     }
+    CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; i++) {
+        CK(cudaEventCreateWithFlags(&forkEv_[i], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&joinEv_[i], cudaEventDisableTiming));
+    }
     CK(cudaMallocHost(&hCtl_, sizeof(DevCtl)));
     CK(cudaMallocHost(&hDyn_, sizeof(RepDyn) * R_));
     CK(cudaMallocHost(&hBilPrefix_, sizeof(int) * (R_ + 1)));
@@ -105,6 +110,11 @@ Engine::~Engine() {
     if (hLinkSlot0_) cudaFreeHost(hLinkSlot0_);
     freeGroup(linkAllocs_);
     freeGroup(bndAllocs_);
+    for (int i = 0; i < 2; i++) {
+        if (forkEv_[i]) cudaEventDestroy(forkEv_[i]);
+        if (joinEv_[i]) cudaEventDestroy(joinEv_[i]);
+    }
+    if (side_) cudaStreamDestroy(side_);
     if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -194,6 +204,10 @@ void Engine::makeParams(int rep, const HostRods &h, RepParams &P) const {
     P.halfReachMax = 0.5 * mx;
     // the same IEEE operations as the per-rod expression it replaces
     P.bcoef = c.KBT > 0.0 ? std::sqrt(2.0 * c.KBT / c.dt) : 0.0;
+    for (int d = 0; d < 3; d++) P.cellsz32[d] = (float)P.cellsz[d];
+    P.colBuf32 = (float)P.colBuf;
+    P.halfReach32 = (float)P.halfReachMax;
+    P.pad32 = 0.0f;
 }
 
 void Engine::finalize() {
@@ -603,15 +617,14 @@ void Engine::uploadBlocks() {
 int Engine::enqueueDetect() {
     DevState &S = S_;
     int n = 0;
-    CK(cudaMemsetAsync(&S.ctl->rawCount, 0, 2 * sizeof(int), stream_));  // rawCount, errFlags
-    CK(cudaMemsetAsync(S.cellCount, 0, sizeof(int) * S.nCells, stream_));
-    CK(cudaMemsetAsync(S.cellCursor, 0, sizeof(int) * S.nCells, stream_));
-    CK(cudaMemsetAsync(S.pairCursor, 0, sizeof(int) * S.nRods, stream_));
-    CK(cudaMemsetAsync(S.pairCount, 0, sizeof(int) * S.nRods, stream_));
-    CK(cudaMemsetAsync(S.rowCount, 0, sizeof(int) * S.nRods, stream_));
-    CK(cudaMemsetAsync(S.rowCursor, 0, sizeof(int) * S.nRods, stream_));
+    launch_step_clear(S, stream_);  // rawCount, errFlags and the per-cell / per-rod counters
     launch_prep(S, stream_);
-    n += 1;
+    // branch 0: the Brownian velocities beside the binning and pair search
+    CK(cudaEventRecord(forkEv_[0], stream_));
+    CK(cudaStreamWaitEvent(side_, forkEv_[0], 0));
+    launch_noise(S, side_);
+    CK(cudaEventRecord(joinEv_[0], side_));
+    n += 3;
     if (S.nLinks > 0) {
         launch_link_blocks(S, stream_);
         n += 1;
@@ -627,10 +640,16 @@ int Engine::enqueueDetect() {
     n += launch_scan(S.pairCount, S.pairOff, S.nRods, S.scanTmp, stream_);
     n += launch_pair_sort(S, stream_);
     launch_ranges(S, stream_);
+    CK(cudaStreamWaitEvent(stream_, joinEv_[0], 0));
     launch_build(S, stream_);
-    n += 2;
+    // branch 1: the mobility-weighted Jacobian beside the rod rows and the
+    // operator structure
+    CK(cudaEventRecord(forkEv_[1], stream_));
+    CK(cudaStreamWaitEvent(side_, forkEv_[1], 0));
+    launch_weights(S, side_);
+    n += 3;
     n += launch_rows(S, stream_);
-    n += launch_assemble(S, stream_);
+    n += launch_assemble(S, stream_, side_, joinEv_[1]);
     if (warm_ == ALENS_WARM_MLP && mlp_) {
         launch_mlp_warm(S, mlp_->view(), stream_);
         n += 1;

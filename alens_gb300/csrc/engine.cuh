@@ -42,6 +42,9 @@ struct RepParams {
     int pad;
     double halfReachMax;  // max over rods of collision half-length + radius
     double bcoef;         // sqrt(2 kT / dt), Brownian velocity scale (kT > 0)
+    // FP32 copies for the pair screen (conversions from FP64 issue on the
+    // FP64 pipe, 2 lanes/clk/SM on GB300)
+    float cellsz32[3], colBuf32, halfReach32, pad32;
 };
 
 // per-replica state produced on the device
@@ -141,7 +144,9 @@ struct DevState {
 };
 
 // ---- detect stage (kernels_detect.cu)
+void launch_step_clear(const DevState &S, cudaStream_t st);
 void launch_prep(const DevState &S, cudaStream_t st);
+void launch_noise(const DevState &S, cudaStream_t st);
 void launch_mobility(const DevState &S, cudaStream_t st);  // once per rod set
 int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st);  // returns kernels launched
 void launch_scatter(const DevState &S, cudaStream_t st);
@@ -153,7 +158,8 @@ void launch_ranges(const DevState &S, cudaStream_t st);
 void launch_build(const DevState &S, cudaStream_t st);
 int launch_rows(const DevState &S, cudaStream_t st);
 // ---- Delassus operator (kernels_assemble.cu)
-int launch_assemble(const DevState &S, cudaStream_t st);
+void launch_weights(const DevState &S, cudaStream_t st);
+int launch_assemble(const DevState &S, cudaStream_t st, cudaStream_t side, cudaEvent_t join);
 void launch_unpack_rods(const DevState &S, int rodOffset, int n, cudaStream_t st);
 void launch_pack_rods(const DevState &S, int rodOffset, int n, int what, cudaStream_t st);
 

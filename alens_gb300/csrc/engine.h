@@ -104,6 +104,8 @@ class Engine {
     int R_ = 0;
     int device_ = 0, numSM_ = 0;
     cudaStream_t stream_ = nullptr;
+    cudaStream_t side_ = nullptr;  // concurrent branch of the detect stage
+    cudaEvent_t forkEv_[2] = {nullptr, nullptr}, joinEv_[2] = {nullptr, nullptr};
     bool ownStream_ = false;
     int precision_ = 0, warm_ = 0;
     bool useGraph_ = true, graphFailed_ = false;

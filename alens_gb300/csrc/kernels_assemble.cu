@@ -147,13 +147,18 @@ int grid_for(int n, int block) {
 
 }  // namespace
 
-int launch_assemble(const DevState &S, cudaStream_t st) {
-    k_weights<<<grid_for(2 * S.cap, 128), 128, 0, st>>>(S);
+void launch_weights(const DevState &S, cudaStream_t st) { k_weights<<<grid_for(2 * S.cap, 128), 128, 0, st>>>(S); }
+
+// Row structure on `st`; the values need the weights, which the caller
+// launched on `side` (recorded in `join`) while the rows were sorted.
+int launch_assemble(const DevState &S, cudaStream_t st, cudaStream_t side, cudaEvent_t join) {
     k_arow_count<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
     const int n = launch_scan(S.annz, S.aptr, S.cap, S.scanTmp, st);
     k_arow_struct<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
+    cudaEventRecord(join, side);
+    cudaStreamWaitEvent(st, join, 0);
     k_arow_values<<<grid_for(S.nnzCap, 256), 256, 0, st>>>(S);
-    return n + 4;
+    return n + 3;
 }
 
 }  // namespace alens

@@ -27,7 +27,6 @@ __device__ __forceinline__ int cell_coord(double v, double lo, double cs, int n)
 
 // ------------------------------------------------------------------ prep
 __global__ void k_prep(DevState S) {
-    const long long step = S.ctl->step;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const int rep = S.rodRep[r];
         const RepParams &P = S.par[rep];
@@ -67,6 +66,26 @@ __global__ void k_prep(DevState S) {
         S.sph[r] = sphere ? 1 : 0;
         S.hcol[r] = sphere ? 0.0 : 0.5 * (L * P.colRatioL);
         S.rcol[r] = rad * P.colRatioD;
+        const int cx = cell_coord(p[0], P.lo[0], P.cellsz[0], P.ncell[0]);
+        const int cy = cell_coord(p[1], P.lo[1], P.cellsz[1], P.ncell[1]);
+        const int cz = cell_coord(p[2], P.lo[2], P.cellsz[2], P.ncell[2]);
+        const int cid = P.cellOffset + (cz * P.ncell[1] + cy) * P.ncell[0] + cx;
+        S.cellOf[r] = cid;
+        atomicAdd(&S.cellCount[cid], 1);
+    }
+}
+
+// Known (Brownian) velocity of every rod: U_B = sqrt(2 kT / dt) M^(1/2) xi
+// with xi from Philox keyed by (seed, gid, step).  Runs beside the pair
+// search (it needs only the axes and flags that k_prep wrote); the
+// constraint build consumes it.
+__global__ void k_noise(DevState S) {
+    if (flags(S) & kErrNaN) return;
+    const long long step = S.ctl->step;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
+        const RepParams &P = S.par[S.rodRep[r]];
+        const double a[3] = {S.ax[r], S.ay[r], S.az[r]};
+        const bool sphere = S.sph[r] != 0;
         const bool imm = S.imm[r] != 0;
         double u[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         if (P.kT > 0.0 && !imm) {
@@ -108,12 +127,27 @@ __global__ void k_prep(DevState S) {
         }
 #pragma unroll
         for (int k = 0; k < 6; k++) S.unc[(size_t)k * S.nRods + r] = u[k];
-        const int cx = cell_coord(p[0], P.lo[0], P.cellsz[0], P.ncell[0]);
-        const int cy = cell_coord(p[1], P.lo[1], P.cellsz[1], P.ncell[1]);
-        const int cz = cell_coord(p[2], P.lo[2], P.cellsz[2], P.ncell[2]);
-        const int cid = P.cellOffset + (cz * P.ncell[1] + cy) * P.ncell[0] + cx;
-        S.cellOf[r] = cid;
-        atomicAdd(&S.cellCount[cid], 1);
+    }
+}
+
+// Start of a step: the counters the detect stage accumulates into (one
+// launch instead of a memset per array).
+__global__ void k_step_clear(DevState S) {
+    const int stride = gridDim.x * blockDim.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) {
+        S.ctl->rawCount = 0;
+        S.ctl->errFlags = 0;
+    }
+    for (int c = t; c < S.nCells; c += stride) {
+        S.cellCount[c] = 0;
+        S.cellCursor[c] = 0;
+    }
+    for (int r = t; r < S.nRods; r += stride) {
+        S.pairCursor[r] = 0;
+        S.pairCount[r] = 0;
+        S.rowCount[r] = 0;
+        S.rowCursor[r] = 0;
     }
 }
 
@@ -478,20 +512,20 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
             const float3 ci = make_float3(Ai.x, Ai.y, Ai.z);
             const float3 ui = make_float3(Bi.x, Bi.y, Bi.z);
             const float hi_ = Ai.w, ri = Bi.w;
-            const float colBuf = (float)P.colBuf;
+            const float colBuf = P.colBuf32;
             const float cutLo = colBuf - kScreenMargin, cutHi = colBuf + kScreenMargin;
             const int img = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
             // the neighbour cell's origin relative to ours
-            const float3 off = make_float3((float)ox * (float)P.cellsz[0], (float)oy * (float)P.cellsz[1],
-                                           (float)oz * (float)P.cellsz[2]);
+            const float3 off = make_float3((float)ox * P.cellsz32[0], (float)oy * P.cellsz32[1],
+                                           (float)oz * P.cellsz32[2]);
             // skip the whole cell when its box lies beyond any partner's reach
             // (exact: every rod centre of that cell is at least this far)
             {
-                const float csx = (float)P.cellsz[0], csy = (float)P.cellsz[1], csz = (float)P.cellsz[2];
+                const float csx = P.cellsz32[0], csy = P.cellsz32[1], csz = P.cellsz32[2];
                 const float bx = fmaxf(fmaxf(off.x - ci.x, ci.x - (off.x + csx)), 0.0f);
                 const float by = fmaxf(fmaxf(off.y - ci.y, ci.y - (off.y + csy)), 0.0f);
                 const float bz = fmaxf(fmaxf(off.z - ci.z, ci.z - (off.z + csz)), 0.0f);
-                const float thr = hi_ + ri + (float)P.halfReachMax + cutHi + kScreenMargin;
+                const float thr = hi_ + ri + P.halfReach32 + cutHi + kScreenMargin;
                 if (bx * bx + by * by + bz * bz > thr * thr) ok = false;
             }
             const int cell = P.cellOffset + (z * ny + y) * nx + xx;
@@ -896,8 +930,16 @@ int grid_for(int n, int block, int maxBlocks = 4096) {
 
 }  // namespace
 
+void launch_step_clear(const DevState &S, cudaStream_t st) {
+    k_step_clear<<<grid_for(S.nRods > S.nCells ? S.nRods : S.nCells, 256), 256, 0, st>>>(S);
+}
+
 void launch_prep(const DevState &S, cudaStream_t st) {
     k_prep<<<grid_for(S.nRods, 64), 64, 0, st>>>(S);
+}
+
+void launch_noise(const DevState &S, cudaStream_t st) {
+    k_noise<<<grid_for(S.nRods, 64), 64, 0, st>>>(S);
 }
 
 void launch_mobility(const DevState &S, cudaStream_t st) {
