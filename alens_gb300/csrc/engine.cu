@@ -894,11 +894,11 @@ void Engine::ensureSolverGrid() {
     }
 }
 
-int Engine::enqueueSolve(cudaEvent_t *ev) {
+int Engine::enqueueSolve(cudaEvent_t *ev, bool finish) {
     ensureSolverGrid();
     int n = 0;
     CK(launch_solve(S_, solverGrid_, precision_, kBarrierTimeoutNs, stream_, ev, &n, solverForm_,
-                    clusterSize_ > 0 ? clusterSize_ : 0, nClusters_));
+                    clusterSize_ > 0 ? clusterSize_ : 0, nClusters_, finish));
     return n;
 }
 
@@ -1113,12 +1113,12 @@ int Engine::detect(AlensStepStats *out) {
 
 int Engine::solve(AlensStepStats *out) {
     if (!haveDetect_) throw ApiError(ALENS_NOT_READY);
-    launches_ += enqueueSolve(nullptr);
+    launches_ += enqueueSolve(nullptr, true);
     readBack();
     if (handleSolverFit()) {
         // the detect results are intact: clear the flag and solve in grid form
         CK(cudaMemsetAsync(&S_.ctl->errFlags, 0, sizeof(int), stream_));
-        launches_ += enqueueSolve(nullptr);
+        launches_ += enqueueSolve(nullptr, true);
         readBack();
     }
     const int status = collectStats(1);

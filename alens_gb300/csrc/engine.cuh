@@ -176,7 +176,7 @@ enum SolverForm {
 // (events ev[0..3] recorded around the two kernels when non-null).
 cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned long long timeout_ns,
                          cudaStream_t st, cudaEvent_t *ev, int *launches, int form, int clusterSize,
-                         int nClusters);
+                         int nClusters, bool finish);
 int cluster_max_size();            // largest cluster the FP32 solver can use
 int cluster_max_active(int cs);    // co-resident clusters of that size
 int csm_cluster_size(int *maxActive);  // cluster-resident form: largest cluster, 0 if unusable

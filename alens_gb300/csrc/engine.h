@@ -84,7 +84,8 @@ class Engine {
     void allocOperator(long long nnz);
     void uploadBlocks();
     int enqueueDetect();
-    int enqueueSolve(cudaEvent_t *ev);
+    // finish: copy the solution into gamma (a full step leaves it to the update)
+    int enqueueSolve(cudaEvent_t *ev, bool finish = false);
     void ensureSolverGrid();
     int enqueueAdvance();
     void ensureEvents();

@@ -109,12 +109,7 @@ __global__ void k_refine_setup(DevState S) {
     }
     S.ctl->allRefined = all;
     S.ctl->setupDone = 0u;
-}
-
-// Barrier and pass counters are re-armed by a separate single-thread
-// kernel so that no block of the next solver launch can observe them
-// half-written.
-__global__ void k_solver_arm(DevState S) {
+    // re-arm the barrier and pass counters for the FP64 launch that follows
     DevCtl *c = S.ctl;
     c->activeCnt[0] = c->activeCnt[1] = c->activeCnt[2] = 0;
     c->bar.count = 0;
@@ -123,11 +118,12 @@ __global__ void k_solver_arm(DevState S) {
     c->finalParity = 1;
 }
 
+// The solution into gamma (alens_solve reports it before the update; a
+// full step leaves the copy to k_advance).
 __global__ void k_solver_finish(DevState S) {
     if (flags(S) & kErrStepAbort) return;
-    const int par = S.ctl->finalParity;
     const int nc = S.ctl->totalCon;
-    const double2 *src = par ? S.st[1] : S.st[0];
+    const double2 *src = S.ctl->finalParity ? S.st[1] : S.st[0];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x)
         S.gamma[k] = src[k].x;
 }
@@ -135,6 +131,8 @@ __global__ void k_solver_finish(DevState S) {
 __global__ void k_advance(DevState S) {
     if (flags(S) & kErrStepAbort) return;
     const size_t st = (size_t)S.nRods;
+    // the solver's last iterate (the solution)
+    const double2 *fin = S.ctl->finalParity ? S.st[1] : S.st[0];
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const int rep = S.rodRep[r];
         const RepParams &P = S.par[rep];
@@ -149,7 +147,7 @@ __global__ void k_advance(DevState S) {
             const int ent = S.rowEnt[e];
             const int k = ent >> 1;
             const double *J = S.jac + 12 * (size_t)k + 6 * (ent & 1);
-            const double gk = S.gamma[k];
+            const double gk = fin[k].x;
 #pragma unroll
             for (int c = 0; c < 6; c++) F[c] = F[c] + gk * J[c];
         }
@@ -204,13 +202,16 @@ __global__ void k_advance(DevState S) {
         S.py[r] = p[1];
         S.pz[r] = p[2];
     }
-    // collision keys and gamma of this step for the next warm start
+    // the solution into gamma, and the collision keys and multipliers of
+    // this step for the next warm start
+    const int nc = S.ctl->totalCon;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) S.gamma[k] = fin[k].x;
     const int totalColl = S.ctl->totalColl;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < totalColl; p += gridDim.x * blockDim.x) {
         const unsigned long long key = S.keys[p];
         const int rep = S.rodRep[(int)(key >> 32)];
         S.prevKeys[p] = key;
-        S.prevGamma[p] = S.gamma[p + S.bilPrefix[rep]];
+        S.prevGamma[p] = fin[p + S.bilPrefix[rep]].x;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *S.prevCount = totalColl;
@@ -320,7 +321,7 @@ int solver_max_grid(int precision) {
 
 cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned long long timeout_ns,
                          cudaStream_t st, cudaEvent_t *ev, int *launches, int form, int clusterSize,
-                         int nClusters) {
+                         int nClusters, bool finish) {
     int n = 0;
     cudaError_t e;
     SolveView<double> V{};
@@ -343,8 +344,7 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[1], st);
         k_refine_setup<<<2 * (grid > 0 ? grid : 1), 128, 0, st>>>(S);
-        k_solver_arm<<<1, 1, 0, st>>>(S);
-        n += 3;
+        n += 2;
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[2], st);
@@ -361,8 +361,10 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
         }
     }
     if (e != cudaSuccess) return e;
-    k_solver_finish<<<512, 256, 0, st>>>(S);
-    n++;
+    if (finish) {
+        k_solver_finish<<<512, 256, 0, st>>>(S);
+        n++;
+    }
     if (launches) *launches += n;
     return cudaGetLastError();
 }
