@@ -212,6 +212,18 @@ struct SolveShared {
 #endif
 };
 
+// Step-size quotient: the FP32 form uses its step in FP32, so its quotient
+// is formed in FP32 (a few cycles instead of a dependent FP64 divide
+// sequence on the 2-lane FP64 pipe); the FP64 form keeps the oracle's FP64
+// divide.
+template <class Real>
+__device__ __forceinline__ double step_quot(double num, double den) {
+    if constexpr (sizeof(Real) == 4)
+        return (double)__fdiv_rn((float)num, (float)den);
+    else
+        return num / den;
+}
+
 // Decision of replica r at pass p from the pass p-1 partials; identical in
 // every block that evaluates it.
 template <class Real>
@@ -278,7 +290,7 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
                 mode = kModeAG;
         } else if (p == 2) {
             const double gg = sums[0], gAg = sums[1];
-            alpha = (gAg > 0.0) ? gg / gAg : 1.0;
+            alpha = (gAg > 0.0) ? step_quot<Real>(gg, gAg) : 1.0;
             if (!(alpha > 0.0) || isinf(alpha)) alpha = 1.0;
             mode = kModeIter;
         } else {
@@ -292,7 +304,7 @@ __device__ void decide(const DevState &S, const SolveView<Real> &V, int p, int r
                 alpha = alphaPrev;
                 const double ss = sums[0], sy = sums[1], yy = sums[2];
                 if (sy > 0.0) {
-                    const double a = (itp & 1) ? ss / sy : sy / yy;
+                    const double a = (itp & 1) ? step_quot<Real>(ss, sy) : step_quot<Real>(sy, yy);
                     if (a > 0.0 && !isinf(a)) alpha = a;
                 }
                 if (itp >= P.maxIte)
