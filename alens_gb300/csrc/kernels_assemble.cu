@@ -147,7 +147,7 @@ int grid_for(int n, int block) {
 
 }  // namespace
 
-void launch_weights(const DevState &S, cudaStream_t st) { k_weights<<<grid_for(2 * S.cap, 128), 128, 0, st>>>(S); }
+void launch_weights(const DevState &S, cudaStream_t st) { k_weights<<<grid_for(2 * S.cap, 32), 32, 0, st>>>(S); }
 
 // Row structure on `st`; the values need the weights, which the caller
 // launched on `side` (recorded in `join`) while the rows were sorted.

@@ -939,7 +939,7 @@ void launch_prep(const DevState &S, cudaStream_t st) {
 }
 
 void launch_noise(const DevState &S, cudaStream_t st) {
-    k_noise<<<grid_for(S.nRods, 64), 64, 0, st>>>(S);
+    k_noise<<<grid_for(S.nRods, 32), 32, 0, st>>>(S);
 }
 
 void launch_mobility(const DevState &S, cudaStream_t st) {
@@ -986,7 +986,7 @@ int launch_pair_sort(const DevState &S, cudaStream_t st) {
 void launch_ranges(const DevState &S, cudaStream_t st) { k_ranges<<<1, 256, 0, st>>>(S); }
 
 void launch_build(const DevState &S, cudaStream_t st) {
-    k_build<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
+    k_build<<<grid_for(S.cap, 32, 8192), 32, 0, st>>>(S);
 }
 
 int launch_rows(const DevState &S, cudaStream_t st) {

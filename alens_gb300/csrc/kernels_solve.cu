@@ -370,12 +370,12 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
 }
 
 void launch_advance(const DevState &S, cudaStream_t st) {
-    // small blocks: the update is FP64-pipe bound (2 lanes/clk/SM on GB300),
-    // so the rods are spread over every SM rather than packed into a few
-    int g = (S.nRods + 63) / 64;
+    // one-warp blocks: the update is FP64-pipe bound (2 lanes/clk/SM on
+    // GB300), so the rods are spread evenly over every SM
+    int g = (S.nRods + 31) / 32;
     if (g < 1) g = 1;
-    if (g > 8192) g = 8192;
-    k_advance<<<g, 64, 0, st>>>(S);
+    if (g > 16384) g = 16384;
+    k_advance<<<g, 32, 0, st>>>(S);
 }
 
 void launch_stress(const DevState &S, cudaStream_t st) {
