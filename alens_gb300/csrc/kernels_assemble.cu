@@ -152,12 +152,12 @@ void launch_weights(const DevState &S, cudaStream_t st) { k_weights<<<grid_for(2
 // Row structure on `st`; the values need the weights, which the caller
 // launched on `side` (recorded in `join`) while the rows were sorted.
 int launch_assemble(const DevState &S, cudaStream_t st, cudaStream_t side, cudaEvent_t join) {
-    k_arow_count<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
+    k_arow_count<<<grid_for(S.cap, 32), 32, 0, st>>>(S);
     const int n = launch_scan(S.annz, S.aptr, S.cap, S.scanTmp, st);
-    k_arow_struct<<<grid_for(S.cap, 128), 128, 0, st>>>(S);
+    k_arow_struct<<<grid_for(S.cap, 32), 32, 0, st>>>(S);
     cudaEventRecord(join, side);
     cudaStreamWaitEvent(st, join, 0);
-    k_arow_values<<<grid_for(S.nnzCap, 256), 256, 0, st>>>(S);
+    k_arow_values<<<grid_for(S.nnzCap, 64), 64, 0, st>>>(S);
     return n + 3;
 }
 

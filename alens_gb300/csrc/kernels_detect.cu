@@ -935,7 +935,7 @@ void launch_step_clear(const DevState &S, cudaStream_t st) {
 }
 
 void launch_prep(const DevState &S, cudaStream_t st) {
-    k_prep<<<grid_for(S.nRods, 64), 64, 0, st>>>(S);
+    k_prep<<<grid_for(S.nRods, 32), 32, 0, st>>>(S);
 }
 
 void launch_noise(const DevState &S, cudaStream_t st) {
@@ -979,7 +979,7 @@ void launch_boundary_pairs(const DevState &S, cudaStream_t st) {
 
 int launch_pair_sort(const DevState &S, cudaStream_t st) {
     k_pair_bucket<<<grid_for(S.cap, 256), 256, 0, st>>>(S);
-    k_pair_segsort<<<grid_for(S.nRods, 128), 128, 0, st>>>(S);
+    k_pair_segsort<<<grid_for(S.nRods, 32), 32, 0, st>>>(S);
     return 2;
 }
 
@@ -992,7 +992,7 @@ void launch_build(const DevState &S, cudaStream_t st) {
 int launch_rows(const DevState &S, cudaStream_t st) {
     const int n = launch_scan(S.rowCount, S.rowPtr, S.nRods, S.scanTmp, st);
     k_rows_fill<<<grid_for(S.cap, 256), 256, 0, st>>>(S);
-    k_rows_sort<<<grid_for(S.nRods, 128), 128, 0, st>>>(S);
+    k_rows_sort<<<grid_for(S.nRods, 32), 32, 0, st>>>(S);
     return n + 2;
 }
 

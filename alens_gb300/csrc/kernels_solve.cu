@@ -343,7 +343,7 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
             e = launch_solve_fp32(S, grid, timeout_ns, st);
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[1], st);
-        k_refine_setup<<<2 * (grid > 0 ? grid : 1), 128, 0, st>>>(S);
+        k_refine_setup<<<8 * (grid > 0 ? grid : 1), 32, 0, st>>>(S);
         n += 2;
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
