@@ -350,6 +350,7 @@ void Engine::allocConstraints(int cap, bool keepPrev) {
     S.workCap = S.tileCap / kChunk + R_ + 2;
     S.rawKeys = alloc<unsigned long long>(G, cap);
     S.keys = alloc<unsigned long long>(G, cap);
+    S.border = alloc<int4>(G, cap);
     S.prevKeys = alloc<unsigned long long>(G, cap);
     S.prevGamma = alloc<double>(G, cap);
     S.conI = alloc<int>(G, cap);
@@ -631,8 +632,8 @@ int Engine::enqueueDetect() {
     }
     n += launch_scan(S.cellCount, S.cellStart, S.nCells, S.scanTmp, stream_);
     launch_scatter(S, stream_);
-    launch_pairs(S, stream_);
-    n += 2;
+    launch_pairs(S, stream_);  // screen + FP64 decision of the borderline candidates
+    n += 3;
     if (S.nBnd > 0) {
         launch_boundary_pairs(S, stream_);
         n += 1;
@@ -957,7 +958,8 @@ void Engine::readBack() {
 // Returns true if the constraint buffers were grown (the step must rerun).
 bool Engine::handleOverflow() {
     if (!(hCtl_->errFlags & kErrOverflow)) return false;
-    const long long needColl = std::max<long long>(hCtl_->rawCount, hCtl_->totalColl);
+    const long long needColl =
+        std::max<long long>(std::max<long long>(hCtl_->rawCount, hCtl_->borderCount), hCtl_->totalColl);
     const long long need = needColl + nBilQueued_;
     lastNeeded_ = need;
     CK(cudaStreamSynchronize(stream_));

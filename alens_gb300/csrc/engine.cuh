@@ -66,6 +66,7 @@ struct DevCtl {
     long long step;
     int rawCount;     // collision pairs found (may exceed capacity)
     int errFlags;     // kErr* bits
+    int borderCount;  // pair candidates left to the FP64 decision
     int totalColl, totalBil, totalCon, nTiles;
     int totalNnz;     // nonzeros of the Delassus operator
     int maxIte;       // max over replicas
@@ -101,6 +102,7 @@ struct DevState {
     // pairs
     int *pairCount, *pairOff, *pairCursor;
     unsigned long long *rawKeys, *keys;
+    int4 *border;              // pair candidates within the FP32 screen's margin: (i, j, image)
     // constraints
     int *conI, *conJ, *conImg;
     float2 *conST;             // contact parameters (s / h_I, t / h_J) of collisions

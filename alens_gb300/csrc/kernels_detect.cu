@@ -138,6 +138,7 @@ __global__ void k_step_clear(DevState S) {
     if (t == 0) {
         S.ctl->rawCount = 0;
         S.ctl->errFlags = 0;
+        S.ctl->borderCount = 0;
     }
     for (int c = t; c < S.nCells; c += stride) {
         S.cellCount[c] = 0;
@@ -542,7 +543,17 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
                 if (d0 * d0 + d1 * d1 + d2 * d2 > lim * lim) continue;
                 const float sep = dcp_dist32(ci, ui, hi_, cj, make_float3(Bj.x, Bj.y, Bj.z), Aj.w) - ri - Bj.w;
                 if (sep >= cutHi) continue;
-                if (sep >= cutLo && !exact_pair(S, i, j, P, sx, sy, sz)) continue;
+                if (sep >= cutLo) {
+                    // within the screen's margin: decided in FP64 by
+                    // k_pairs_exact, with full warps (here one lane's FP64
+                    // segment distance would hold its whole warp)
+                    const int slot = atomicAdd(&S.ctl->borderCount, 1);
+                    if (slot < S.cap)
+                        S.border[slot] = make_int4(i, j, img, 0);
+                    else
+                        atomicOr(&S.ctl->errFlags, kErrOverflow);
+                    continue;
+                }
                 if (nb == kPairBuf) {
                     flush_keys(S, buf, nb);
                     nb = 0;
@@ -572,6 +583,25 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
             S.rawKeys[pos] = buf[e];
         else
             atomicOr(&S.ctl->errFlags, kErrOverflow);
+    }
+}
+
+// The FP64 decision (the oracle's arithmetic) for the candidates the FP32
+// screen left within its margin; accepted pairs are appended like k_pairs'.
+__global__ void k_pairs_exact(DevState S) {
+    if (flags(S) & (kErrNaN | kErrOverflow)) return;
+    const int n = min(S.ctl->borderCount, S.cap);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+        const int4 e = S.border[b];
+        const int i = e.x, j = e.y, img = e.z;
+        const RepParams &P = S.par[S.rodRep[i]];
+        if (!exact_pair(S, i, j, P, img / 9 - 1, (img / 3) % 3 - 1, img % 3 - 1)) continue;
+        const int pos = atomicAdd(&S.ctl->rawCount, 1);
+        if (pos < S.cap)
+            S.rawKeys[pos] = pair_key(i, j, img);
+        else
+            atomicOr(&S.ctl->errFlags, kErrOverflow);
+        atomicAdd(&S.pairCount[i], 1);
     }
 }
 
@@ -967,10 +997,22 @@ void launch_scatter(const DevState &S, cudaStream_t st) {
     k_scatter<<<grid_for(S.nRods, 256), 256, 0, st>>>(S);
 }
 
+int sm_count_detect() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
 void launch_pairs(const DevState &S, cudaStream_t st) {
     const long long items = 27LL * S.nRods;
     const long long g = (items + kPairThreads - 1) / kPairThreads;
     k_pairs<<<(unsigned)(g > 0 ? g : 1), kPairThreads, 0, st>>>(S);
+    k_pairs_exact<<<2 * sm_count_detect(), 64, 0, st>>>(S);
 }
 
 void launch_boundary_pairs(const DevState &S, cudaStream_t st) {
