@@ -79,7 +79,7 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
         formRequest_ = f == "grid" ? kFormGrid : (f == "cluster" ? kFormCluster : (f == "resident" ? kFormResident : -1));
     }
     CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < 3; i++) {
         CK(cudaEventCreateWithFlags(&forkEv_[i], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&joinEv_[i], cudaEventDisableTiming));
     }
@@ -110,7 +110,7 @@ Engine::~Engine() {
     if (hLinkSlot0_) cudaFreeHost(hLinkSlot0_);
     freeGroup(linkAllocs_);
     freeGroup(bndAllocs_);
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < 3; i++) {
         if (forkEv_[i]) cudaEventDestroy(forkEv_[i]);
         if (joinEv_[i]) cudaEventDestroy(joinEv_[i]);
     }
@@ -624,7 +624,6 @@ int Engine::enqueueDetect() {
     CK(cudaEventRecord(forkEv_[0], stream_));
     CK(cudaStreamWaitEvent(side_, forkEv_[0], 0));
     launch_noise(S, side_);
-    CK(cudaEventRecord(joinEv_[0], side_));
     n += 3;
     if (S.nLinks > 0) {
         launch_link_blocks(S, stream_);
@@ -639,8 +638,13 @@ int Engine::enqueueDetect() {
         n += 1;
     }
     n += launch_scan(S.pairCount, S.pairOff, S.nRods, S.scanTmp, stream_);
+    // the per-replica ranges (from the pair offsets) on the same branch,
+    // beside the canonical sort of the keys
+    CK(cudaEventRecord(forkEv_[2], stream_));
+    CK(cudaStreamWaitEvent(side_, forkEv_[2], 0));
+    launch_ranges(S, side_);
+    CK(cudaEventRecord(joinEv_[0], side_));
     n += launch_pair_sort(S, stream_);
-    launch_ranges(S, stream_);
     CK(cudaStreamWaitEvent(stream_, joinEv_[0], 0));
     launch_build(S, stream_);
     // branch 1: the mobility-weighted Jacobian beside the rod rows and the

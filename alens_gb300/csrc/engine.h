@@ -106,7 +106,7 @@ class Engine {
     int device_ = 0, numSM_ = 0;
     cudaStream_t stream_ = nullptr;
     cudaStream_t side_ = nullptr;  // concurrent branch of the detect stage
-    cudaEvent_t forkEv_[2] = {nullptr, nullptr}, joinEv_[2] = {nullptr, nullptr};
+    cudaEvent_t forkEv_[3] = {nullptr, nullptr, nullptr}, joinEv_[3] = {nullptr, nullptr, nullptr};
     bool ownStream_ = false;
     int precision_ = 0, warm_ = 0;
     bool useGraph_ = true, graphFailed_ = false;

@@ -141,9 +141,15 @@ struct InferSmem {
     alignas(1024) uint8_t w2[kW2Bytes];                  // 8 KB
     float b1[kMlpHid], b2[kMlpHid], w3[kMlpHid];
     float b3;
+    float ypart[kMlpTile];  // output-layer partial sums of the upper column half
     alignas(8) unsigned long long mbar;
     uint32_t tmem;
 };
+
+// Inference CTAs have 256 threads: thread t serves row t & 127 (its TMEM
+// lane, 32 x32b lanes per warp quadrant) and column half t >> 7 of each
+// hidden layer, so every epilogue is split over two threads per row.
+constexpr int kInferThreads = 2 * kMlpTile;
 
 __device__ void copy16(uint8_t *dst, const uint8_t *src, int bytes) {
     for (int o = (int)threadIdx.x * 16; o < bytes; o += (int)blockDim.x * 16)
@@ -205,13 +211,15 @@ __device__ __forceinline__ bool wait_mma(uint32_t mbar, uint32_t &phase, int *er
 }
 
 // Forward pass of one tile whose features are already in sh.x; returns the
-// network output of this thread's row.  False on timeout.
+// network output of this thread's row in the threads of column half 0.
+// False on timeout.
 template <class Sm>
 __device__ bool infer_tile(Sm &sh, uint32_t tbase, uint32_t &phase, int *err, float &y) {
     constexpr uint32_t idesc = tc::idesc_bf16(kMlpTile, kMlpHid);
     const uint32_t mbar = tc::smem_addr(&sh.mbar);
     const int tid = threadIdx.x;
-    const uint32_t lane_base = tbase + ((uint32_t)((tid >> 5) * 32) << 16);
+    const int row = tid & (kMlpTile - 1), c0 = 32 * (tid >> 7);
+    const uint32_t lane_base = tbase + ((uint32_t)(((tid >> 5) & 3) * 32) << 16);
     handoff_to_mma();
     if (tid == 0) {
         const uint64_t a = tc::smem_desc(tc::smem_addr(sh.x), 128, 256);
@@ -220,16 +228,15 @@ __device__ bool infer_tile(Sm &sh, uint32_t tbase, uint32_t &phase, int *err, fl
         tc::commit(mbar);
     }
     if (!wait_mma(mbar, phase, err)) return false;
-#pragma unroll
-    for (int c = 0; c < kMlpHid; c += 32) {
+    {
         float v[32];
-        tc::tmem_ld32(lane_base + c, v);
+        tc::tmem_ld32(lane_base + c0, v);
 #pragma unroll
         for (int g = 0; g < 32; g += 8) {
             float h[8];
 #pragma unroll
-            for (int e = 0; e < 8; e++) h[e] = siluf_(v[g + e] + sh.b1[c + g + e]);
-            tc::st_bf16x8(sh.h1, tc::core_off(tid, c + g, kMlpHid), h);
+            for (int e = 0; e < 8; e++) h[e] = siluf_(v[g + e] + sh.b1[c0 + g + e]);
+            tc::st_bf16x8(sh.h1, tc::core_off(row, c0 + g, kMlpHid), h);
         }
     }
     handoff_to_mma();
@@ -243,19 +250,20 @@ __device__ bool infer_tile(Sm &sh, uint32_t tbase, uint32_t &phase, int *err, fl
         tc::commit(mbar);
     }
     if (!wait_mma(mbar, phase, err)) return false;
-    float acc = sh.b3;
-#pragma unroll
-    for (int c = 0; c < kMlpHid; c += 32) {
+    float acc = 0.0f;
+    {
         float v[32];
-        tc::tmem_ld32(lane_base + kMlpHid + c, v);
+        tc::tmem_ld32(lane_base + kMlpHid + c0, v);
 #pragma unroll
-        for (int e = 0; e < 32; e++) acc = fmaf(siluf_(v[e] + sh.b2[c + e]), sh.w3[c + e], acc);
+        for (int e = 0; e < 32; e++) acc = fmaf(siluf_(v[e] + sh.b2[c0 + e]), sh.w3[c0 + e], acc);
     }
-    y = acc;
-    // every lane's TMEM reads are complete before the next tile's MMA
+    if (c0 != 0) sh.ypart[row] = acc;
+    // the partial sums are in place and every lane's TMEM reads are
+    // complete before the next tile's MMA
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
+    if (c0 == 0) y = (sh.b3 + acc) + sh.ypart[row];
     return true;
 }
 
@@ -266,7 +274,7 @@ __device__ __forceinline__ void store_features(uint8_t *x, int row, const float 
 
 // Warm start of every collision constraint of the step (after the
 // operator assembly, before the solve).  Optionally records the features.
-__global__ void __launch_bounds__(kMlpTile) k_mlp_warm(DevState S, MlpView V) {
+__global__ void __launch_bounds__(kInferThreads) k_mlp_warm(DevState S, MlpView V) {
     __shared__ InferSmem sh;
     if (ld_volatile_i32(&S.ctl->errFlags) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
@@ -274,20 +282,24 @@ __global__ void __launch_bounds__(kMlpTile) k_mlp_warm(DevState S, MlpView V) {
     if ((int)blockIdx.x >= nTiles) return;
     const uint32_t tbase = infer_setup(sh, V, 128);
     uint32_t phase = 0;
+    const bool lead = threadIdx.x < kMlpTile;  // the row's features and output
     for (int t = blockIdx.x; t < nTiles; t += gridDim.x) {
         const int k = t * kMlpTile + (int)threadIdx.x;
-        float f[kMlpInPad];
         float scale = 0.0f;
-        const bool ok = k < nc && mlp_features(S, k, f, scale);
-        if (S.feat && k < nc) {
+        bool ok = false;
+        if (lead) {
+            float f[kMlpInPad];
+            ok = k < nc && mlp_features(S, k, f, scale);
+            if (S.feat && k < nc) {
 #pragma unroll
-            for (int c = 0; c < kMlpIn; c++) S.feat[(size_t)k * kMlpIn + c] = f[c];
-            S.fscale[k] = scale;
+                for (int c = 0; c < kMlpIn; c++) S.feat[(size_t)k * kMlpIn + c] = f[c];
+                S.fscale[k] = scale;
+            }
+            store_features(sh.x, threadIdx.x, f);
         }
-        store_features(sh.x, threadIdx.x, f);
         float y = 0.0f;
         if (!infer_tile(sh, tbase, phase, &S.ctl->errFlags, y)) break;
-        if (ok) {
+        if (lead && ok) {
             const double g0 = y > 0.0f ? (double)(y / scale) : 0.0;
             S.gamma[k] = g0;
             S.st[1][k] = make_double2(g0, 0.0);
@@ -322,21 +334,24 @@ __global__ void k_mlp_append(DevState S, int k0, int n, float *dsFeat, float *ds
 }
 
 // Network output for rows of a feature matrix (n x 12, FP32).
-__global__ void __launch_bounds__(kMlpTile) k_mlp_predict(MlpView V, const float *feat, int n, float *out) {
+__global__ void __launch_bounds__(kInferThreads) k_mlp_predict(MlpView V, const float *feat, int n, float *out) {
     __shared__ InferSmem sh;
     const int nTiles = (n + kMlpTile - 1) / kMlpTile;
     if ((int)blockIdx.x >= nTiles) return;
     const uint32_t tbase = infer_setup(sh, V, 128);
     uint32_t phase = 0;
+    const bool lead = threadIdx.x < kMlpTile;
     for (int t = blockIdx.x; t < nTiles; t += gridDim.x) {
         const int r = t * kMlpTile + (int)threadIdx.x;
-        float f[kMlpInPad];
+        if (lead) {
+            float f[kMlpInPad];
 #pragma unroll
-        for (int c = 0; c < kMlpInPad; c++) f[c] = (r < n && c < kMlpIn) ? feat[(size_t)r * kMlpIn + c] : 0.0f;
-        store_features(sh.x, threadIdx.x, f);
+            for (int c = 0; c < kMlpInPad; c++) f[c] = (r < n && c < kMlpIn) ? feat[(size_t)r * kMlpIn + c] : 0.0f;
+            store_features(sh.x, threadIdx.x, f);
+        }
         float y = 0.0f;
         if (!infer_tile(sh, tbase, phase, V.err, y)) break;
-        if (r < n) out[r] = y;
+        if (lead && r < n) out[r] = y;
     }
     tmem_release(tbase, 128);
 }
@@ -656,7 +671,7 @@ void launch_mlp_warm(const DevState &S, const MlpView &V, cudaStream_t st) {
     // a tile return at once
     const int tiles = (S.cap + kMlpTile - 1) / kMlpTile;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-    k_mlp_warm<<<grid > 0 ? grid : 1, kMlpTile, 0, st>>>(S, V);
+    k_mlp_warm<<<grid > 0 ? grid : 1, kInferThreads, 0, st>>>(S, V);
 }
 
 void launch_mlp_features(const DevState &S, cudaStream_t st) {
@@ -673,7 +688,7 @@ void launch_mlp_predict(const MlpView &V, const float *feat, int n, float *out, 
     if (n <= 0) return;
     const int tiles = (n + kMlpTile - 1) / kMlpTile;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-    k_mlp_predict<<<grid, kMlpTile, 0, st>>>(V, feat, n, out);
+    k_mlp_predict<<<grid, kInferThreads, 0, st>>>(V, feat, n, out);
 }
 
 cudaError_t launch_mlp_train(const MlpView &V, const float *feat, const float *label, long long nData,
