@@ -180,6 +180,20 @@ void Engine::makeParams(int rep, const HostRods &h, RepParams &P) const {
         nc = std::max(1, std::min(nc, 1024));
         P.ncell[d] = nc;
     }
+    // dense systems (many rods per cutoff-sized cell) use cells of half the
+    // cutoff and a 5-cell stencil: the candidates then cover about a third
+    // of the volume of the 27 full cells
+    P.stencil = 3;
+    {
+        const long long cells = (long long)P.ncell[0] * P.ncell[1] * P.ncell[2];
+        if (cutoff > 0 && (double)h.n > 24.0 * (double)cells) {
+            P.stencil = 5;
+            for (int d = 0; d < 3; d++) {
+                int nc = (int)std::floor(P.L[d] / (0.5 * cutoff));
+                P.ncell[d] = std::max(1, std::min(nc, 1024));
+            }
+        }
+    }
     // keep the cell count proportional to the rod count (the grid only
     // affects the candidate enumeration, never the result)
     const long long limit = std::max<long long>(64, 2LL * h.n);
@@ -241,6 +255,8 @@ void Engine::finalize() {
     DevState &S = S_;
     std::memset(&S, 0, sizeof(S));
     S.R = R_;
+    S.pairStencil = 3;
+    for (int r = 0; r < R_; r++) S.pairStencil = std::max(S.pairStencil, hostPar_[r].stencil);
     S.nRods = N;
     S.nCells = C;
     S.warm = warm_;

@@ -39,7 +39,7 @@ struct RepParams {
     int rodOffset;
     int nRods;
     int maxIte;
-    int pad;
+    int stencil;          // pair-search cells per dimension around a rod's cell (3 or 5)
     double halfReachMax;  // max over rods of collision half-length + radius
     double bcoef;         // sqrt(2 kT / dt), Brownian velocity scale (kT > 0)
     // FP32 copies for the pair screen (conversions from FP64 issue on the
@@ -82,6 +82,7 @@ struct DevState {
     int R, nRods, cap, nCells, tileCap, workCap, blockCap, nnzCap;
     int warm, precision;
     int solveMinTiles;         // BBPGD: at least this many 64-row tiles per solver block
+    int pairStencil;           // pair search: max over replicas of RepParams::stencil
     RepParams *par;
     RepDyn *dyn;
     DevCtl *ctl;

@@ -476,14 +476,14 @@ __device__ __noinline__ bool exact_pair(const DevState &S, int i, int j, const R
 // screen, FP64 decision only within the screening margin.
 __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
     const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int nb27 = 27;
-    const bool valid = item < (long long)nb27 * S.nRods && !(flags(S) & kErrNaN);
+    const int W = S.pairStencil, Rw = W >> 1;  // stencil of W^3 cells (W = 3 or 5)
+    const bool valid = item < (long long)(W * W * W) * S.nRods && !(flags(S) & kErrNaN);
     unsigned long long buf[kPairBuf];
     int nb = 0;
     if (valid) {
         const int t = (int)(item % S.nRods);
         const int nbr = (int)(item / S.nRods);
-        const int ox = nbr % 3 - 1, oy = (nbr / 3) % 3 - 1, oz = nbr / 9 - 1;
+        const int ox = nbr % W - Rw, oy = (nbr / W) % W - Rw, oz = nbr / (W * W) - Rw;
         const int i = S.sidx[t];
         const RepParams &P = S.par[S.rodRep[i]];
         const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
@@ -491,21 +491,28 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
         const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
         int xx = cx + ox, y = cy + oy, z = cz + oz;
         int sx = 0, sy = 0, sz = 0;
-        bool ok = true;
+        // offsets beyond this replica's own stencil are not needed
+        const int Rp = P.stencil >> 1;
+        bool ok = abs(ox) <= Rp && abs(oy) <= Rp && abs(oz) <= Rp;
+        // one periodic wrap (shift of one box length); a cell still outside
+        // is beyond the cutoff (the box is at least one cutoff long)
         if (xx < 0 || xx >= nx) {
             if (!P.pbc[0]) ok = false;
             else if (xx < 0) { xx += nx; sx = -1; }
             else { xx -= nx; sx = 1; }
+            if (xx < 0 || xx >= nx) ok = false;
         }
         if (y < 0 || y >= ny) {
             if (!P.pbc[1]) ok = false;
             else if (y < 0) { y += ny; sy = -1; }
             else { y -= ny; sy = 1; }
+            if (y < 0 || y >= ny) ok = false;
         }
         if (z < 0 || z >= nz) {
             if (!P.pbc[2]) ok = false;
             else if (z < 0) { z += nz; sz = -1; }
             else { z -= nz; sz = 1; }
+            if (z < 0 || z >= nz) ok = false;
         }
         int cnt = 0;
         if (ok) {
@@ -1009,7 +1016,7 @@ int sm_count_detect() {
 }
 
 void launch_pairs(const DevState &S, cudaStream_t st) {
-    const long long items = 27LL * S.nRods;
+    const long long items = (long long)S.pairStencil * S.pairStencil * S.pairStencil * S.nRods;
     const long long g = (items + kPairThreads - 1) / kPairThreads;
     k_pairs<<<(unsigned)(g > 0 ? g : 1), kPairThreads, 0, st>>>(S);
     k_pairs_exact<<<2 * sm_count_detect(), 64, 0, st>>>(S);
