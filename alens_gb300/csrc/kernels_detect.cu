@@ -676,14 +676,21 @@ __global__ void k_pair_segsort(DevState S) {
 }
 
 // ---------------------------------------------------------------- ranges
-// One block: per-replica constraint/tile ranges, totals, solver state.
+// Per-replica constraint and tile ranges from the pair offsets, one thread
+// per replica (a block scan gives the tile starts), then the step's totals
+// and the solver's counters.
 __global__ void k_ranges(DevState S) {
-    __shared__ int s_ok;
+    __shared__ int sm[33];
+    __shared__ int s_tile, s_maxIte, s_ok;
     if (threadIdx.x == 0) {
-        DevCtl *c = S.ctl;
-        int tile = 0, active = 0, maxIte = 0;
-        const int totalColl = S.pairOff[S.nRods];
-        for (int r = 0; r < S.R; r++) {
+        s_tile = 0;
+        s_maxIte = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < S.R; base += blockDim.x) {
+        const int r = base + (int)threadIdx.x;
+        int nTiles = 0;
+        if (r < S.R) {
             const RepParams &P = S.par[r];
             RepDyn &d = S.dyn[r];
             d.collStart = S.pairOff[P.rodOffset];
@@ -692,8 +699,6 @@ __global__ void k_ranges(DevState S) {
             d.conStart = d.collStart + S.bilPrefix[r];
             d.nCon = (d.collEnd - d.collStart) + nBil;
             d.nTiles = (d.nCon + kTile - 1) / kTile;
-            d.tileStart = tile;
-            tile += d.nTiles;
             d.iter = 0;
             d.refineIter = 0;
             d.refined = 0;
@@ -704,10 +709,20 @@ __global__ void k_ranges(DevState S) {
             d.counter = 0;
             d.alpha = 0.0;
             d.res = 0.0;
-            active += d.active;
-            (void)active;
-            maxIte = P.maxIte > maxIte ? P.maxIte : maxIte;
+            nTiles = d.nTiles;
+            atomicMax(&s_maxIte, P.maxIte);
         }
+        int tot;
+        const int ex = block_exclusive_scan(nTiles, sm, &tot);
+        if (r < S.R) S.dyn[r].tileStart = s_tile + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        DevCtl *c = S.ctl;
+        const int tile = s_tile;
+        const int totalColl = S.pairOff[S.nRods];
         c->totalColl = totalColl;
         c->totalBil = S.bilPrefix[S.R];
         c->totalCon = totalColl + S.bilPrefix[S.R];
@@ -716,7 +731,7 @@ __global__ void k_ranges(DevState S) {
         c->finalParity = 1;
         c->allRefined = 0;
         c->setupDone = 0u;
-        c->maxIte = maxIte;
+        c->maxIte = s_maxIte;
         c->bar.count = 0;
         c->bar.gen = 0;
         c->bar.pass[0][0] = c->bar.pass[1][0] = c->bar.pass[2][0] = 0u;
@@ -729,9 +744,11 @@ __global__ void k_ranges(DevState S) {
     }
     __syncthreads();
     if (!s_ok || (flags(S) & (kErrNaN | kErrOverflow))) return;
-    for (int r = 0; r < S.R; r++) {
+    // tile -> replica map, one warp per replica
+    const int lane = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < S.R; r += blockDim.x >> 5) {
         const RepDyn &d = S.dyn[r];
-        for (int t = threadIdx.x; t < d.nTiles; t += blockDim.x) S.tileRep[d.tileStart + t] = r;
+        for (int t = lane; t < d.nTiles; t += 32) S.tileRep[d.tileStart + t] = r;
     }
 }
 
@@ -1032,7 +1049,7 @@ int launch_pair_sort(const DevState &S, cudaStream_t st) {
     return 2;
 }
 
-void launch_ranges(const DevState &S, cudaStream_t st) { k_ranges<<<1, 256, 0, st>>>(S); }
+void launch_ranges(const DevState &S, cudaStream_t st) { k_ranges<<<1, 1024, 0, st>>>(S); }
 
 void launch_build(const DevState &S, cudaStream_t st) {
     k_build<<<grid_for(S.cap, 32, 8192), 32, 0, st>>>(S);
