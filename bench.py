@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--profile-case", action="store_true",
                     help="print per-stage CUDA-event times of both solver forms (direct launches) "
                          "for profiling; no JSON line")
+    ap.add_argument("--profile-ensemble", action="store_true",
+                    help="one step of the 64-replica ensemble (mixed precision, direct launches) "
+                         "between cudaProfilerStart/Stop, after 3 warm-up steps; no JSON line")
     return ap.parse_args()
 
 
@@ -548,6 +551,27 @@ def profile_step(args):
         g.close()
 
 
+def profile_ensemble(args):
+    """One step of the 64-replica ensemble inside cudaProfilerStart/Stop."""
+    import torch
+    from alens_gb300 import capi, workloads
+    reps = workloads.ensemble(nrep=64, nmin=500, nmax=8000, seed=0)
+    cfgs = [workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_ZERO, useGraph=0)
+            for w in reps]
+    g = capi.GpuSystem(cfgs)
+    for r, w in enumerate(reps):
+        g.set_rods(w.rods, replica=r)
+    g.autotune(reps=2)
+    for _ in range(3):
+        g.step()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    g.step()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    g.close()
+
+
 def main():
     args = parse()
     if args.profile_case:
@@ -555,6 +579,9 @@ def main():
         return
     if args.profile_step:
         profile_step(args)
+        return
+    if args.profile_ensemble:
+        profile_ensemble(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
