@@ -19,6 +19,8 @@
 //               chunk work space
 #pragma once
 
+#include <utility>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -76,6 +78,34 @@ struct DevCtl {
     unsigned int setupDone;  // blocks of the refinement set-up that finished
     GridBarrier bar;
 };
+
+// Programmatic dependent launch.  A kernel launched with launch_pdl may be
+// scheduled while the previous kernel of its stream is still running: it
+// first waits (griddepcontrol.wait) until that kernel has completed and its
+// writes are visible, then lets its own dependents be scheduled.  Every
+// kernel of the step starts with ALENS_PDL_PROLOGUE (a no-op when the
+// kernel was launched normally).
+#define ALENS_PDL_PROLOGUE()                                        \
+    do {                                                            \
+        asm volatile("griddepcontrol.wait;" ::: "memory");          \
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); \
+    } while (0)
+
+template <class... KArgs, class... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Device pointers and sizes of one context; passed to kernels by value.
 struct DevState {

@@ -29,6 +29,7 @@ __device__ __forceinline__ double dot6d(const double *a, const double *b) {
 // W = M J for both sides of every constraint, one thread per side
 // (adjacent lanes: the two sides of a constraint).
 __global__ void k_weights(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
     for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < 2 * nc; it += gridDim.x * blockDim.x) {
@@ -89,6 +90,7 @@ __device__ int merge_rows(const DevState &S, int k, const RowLists &L, int out0)
 }
 
 __global__ void k_arow_count(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < S.cap; k += gridDim.x * blockDim.x)
@@ -96,6 +98,7 @@ __global__ void k_arow_count(DevState S) {
 }
 
 __global__ void k_arow_struct(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
     const int nnz = S.aptr[nc];
@@ -111,6 +114,7 @@ __global__ void k_arow_struct(DevState S) {
 // A_kl = dt * (sum over l's entries in rod I's row of J_k,I . W_l,s, then
 // over its entries in rod J's row of J_k,J . W_l,s), in entry order.
 __global__ void k_arow_values(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
     const int nnz = S.aptr[nc];
@@ -152,9 +156,9 @@ void launch_weights(const DevState &S, cudaStream_t st) { k_weights<<<grid_for(2
 // Row structure on `st`; the values need the weights, which the caller
 // launched on `side` (recorded in `join`) while the rows were sorted.
 int launch_assemble(const DevState &S, cudaStream_t st, cudaStream_t side, cudaEvent_t join) {
-    k_arow_count<<<grid_for(S.cap, 32), 32, 0, st>>>(S);
+    launch_pdl(k_arow_count, dim3(grid_for(S.cap, 32)), dim3(32), 0, st, S);
     const int n = launch_scan(S.annz, S.aptr, S.cap, S.scanTmp, st);
-    k_arow_struct<<<grid_for(S.cap, 32), 32, 0, st>>>(S);
+    launch_pdl(k_arow_struct, dim3(grid_for(S.cap, 32)), dim3(32), 0, st, S);
     cudaEventRecord(join, side);
     cudaStreamWaitEvent(st, join, 0);
     k_arow_values<<<grid_for(S.nnzCap, 64), 64, 0, st>>>(S);

@@ -27,6 +27,7 @@ __device__ __forceinline__ int cell_coord(double v, double lo, double cs, int n)
 
 // ------------------------------------------------------------------ prep
 __global__ void k_prep(DevState S) {
+    ALENS_PDL_PROLOGUE();
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const int rep = S.rodRep[r];
         const RepParams &P = S.par[rep];
@@ -80,6 +81,7 @@ __global__ void k_prep(DevState S) {
 // search (it needs only the axes and flags that k_prep wrote); the
 // constraint build consumes it.
 __global__ void k_noise(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & kErrNaN) return;
     const long long step = S.ctl->step;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
@@ -133,6 +135,7 @@ __global__ void k_noise(DevState S) {
 // Start of a step: the counters the detect stage accumulates into (one
 // launch instead of a memset per array).
 __global__ void k_step_clear(DevState S) {
+    ALENS_PDL_PROLOGUE();
     const int stride = gridDim.x * blockDim.x;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t == 0) {
@@ -205,6 +208,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *smem32, int *tot
 }
 
 __global__ void k_scan_block(const int *in, int *out, int n, int *tmp) {
+    ALENS_PDL_PROLOGUE();
     __shared__ int sm[33];
     const int base = blockIdx.x * kScanSpan + threadIdx.x * kScanPer;
     int v[kScanPer];
@@ -225,6 +229,7 @@ __global__ void k_scan_block(const int *in, int *out, int n, int *tmp) {
 }
 
 __global__ void k_scan_top(int *tmp, int nb, int *out, int n) {
+    ALENS_PDL_PROLOGUE();
     __shared__ int sm[33];
     // up to 1024 threads x 4 = 4096 block totals
     const int base = threadIdx.x * 4;
@@ -265,6 +270,7 @@ __device__ __forceinline__ int4 scan_load4(const int *in, int i, int end, bool v
 }
 
 __global__ void __launch_bounds__(kScanSingleThreads) k_scan_single(const int *in, int *out, int n, int vec) {
+    ALENS_PDL_PROLOGUE();
     __shared__ int sm[33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = (((n + 31) / 32) + 127) & ~127;
@@ -321,6 +327,7 @@ __global__ void __launch_bounds__(kScanSingleThreads) k_scan_single(const int *i
 }
 
 __global__ void k_scan_add(int *out, int n, const int *tmp) {
+    ALENS_PDL_PROLOGUE();
     const int add = tmp[blockIdx.x];
     const int base = blockIdx.x * kScanSpan + threadIdx.x * kScanPer;
 #pragma unroll
@@ -333,6 +340,7 @@ __global__ void k_scan_add(int *out, int n, const int *tmp) {
 // anchors P = c_I + sI a_I, Q = c_J + sJ a_J, d = P - Q reduced to the
 // minimum image, spring extension |d| - rest (SRC/TubuleSystem.cpp:714-736).
 __global__ void k_link_blocks(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & kErrNaN) return;
     for (int L = blockIdx.x * blockDim.x + threadIdx.x; L < S.nLinks; L += gridDim.x * blockDim.x) {
         const int rep = S.linkRep[L];
@@ -386,6 +394,7 @@ __global__ void k_link_blocks(DevState S) {
 // half-length (sA), axis and collision radius (sB).  Relative coordinates
 // keep the FP32 screen accurate whatever the box size.
 __global__ void k_scatter(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & kErrNaN) return;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const int cid = S.cellOf[r];
@@ -475,6 +484,7 @@ __device__ __noinline__ bool exact_pair(const DevState &S, int i, int j, const R
 // at the same neighbour offset, so candidate loads are broadcasts.  FP32
 // screen, FP64 decision only within the screening margin.
 __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
+    ALENS_PDL_PROLOGUE();
     const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int W = S.pairStencil, Rw = W >> 1;  // stencil of W^3 cells (W = 3 or 5)
     const bool valid = item < (long long)(W * W * W) * S.nRods && !(flags(S) & kErrNaN);
@@ -596,6 +606,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
 // The FP64 decision (the oracle's arithmetic) for the candidates the FP32
 // screen left within its margin; accepted pairs are appended like k_pairs'.
 __global__ void k_pairs_exact(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int n = min(S.ctl->borderCount, S.cap);
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
@@ -616,6 +627,7 @@ __global__ void k_pairs_exact(DevState S) {
 // of its replica than sylinderColBuf (surface distance, FP64, the oracle's
 // arithmetic) gives a key (i, b, 27 + point) in the rod's pair segment.
 __global__ void k_boundary_pairs(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & kErrNaN) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nRods; i += gridDim.x * blockDim.x) {
         const int rep = S.rodRep[i];
@@ -649,6 +661,7 @@ __global__ void k_boundary_pairs(DevState S) {
 // Place raw keys into their rod's segment, then sort each segment: the
 // canonical order is (i, j, image) ascending.
 __global__ void k_pair_bucket(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int n = S.ctl->rawCount;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
@@ -660,6 +673,7 @@ __global__ void k_pair_bucket(DevState S) {
 }
 
 __global__ void k_pair_segsort(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nRods; i += gridDim.x * blockDim.x) {
         const int b = S.pairOff[i], e = S.pairOff[i + 1];
@@ -680,6 +694,7 @@ __global__ void k_pair_segsort(DevState S) {
 // per replica (a block scan gives the tile starts), then the step's totals
 // and the solver's counters.
 __global__ void k_ranges(DevState S) {
+    ALENS_PDL_PROLOGUE();
     __shared__ int sm[33];
     __shared__ int s_tile, s_maxIte, s_ok;
     if (threadIdx.x == 0) {
@@ -783,6 +798,7 @@ __device__ void finish_constraint(const DevState &S, int k, const RepParams &P, 
 }
 
 __global__ void k_build(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int totalColl = S.ctl->totalColl, totalBil = S.ctl->totalBil;
     const bool warmPrev = S.warm == ALENS_WARM_PREV || S.warm == ALENS_WARM_MLP;
@@ -910,6 +926,7 @@ __global__ void k_build(DevState S) {
 
 // ------------------------------------------------------------- rod rows
 __global__ void k_rows_fill(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) {
@@ -920,6 +937,7 @@ __global__ void k_rows_fill(DevState S) {
 }
 
 __global__ void k_rows_sort(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const int b = S.rowPtr[r], e = S.rowPtr[r + 1];
@@ -989,7 +1007,7 @@ void launch_step_clear(const DevState &S, cudaStream_t st) {
 }
 
 void launch_prep(const DevState &S, cudaStream_t st) {
-    k_prep<<<grid_for(S.nRods, 32), 32, 0, st>>>(S);
+    launch_pdl(k_prep, dim3(grid_for(S.nRods, 32)), dim3(32), 0, st, S);
 }
 
 void launch_noise(const DevState &S, cudaStream_t st) {
@@ -1003,22 +1021,22 @@ void launch_mobility(const DevState &S, cudaStream_t st) {
 int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st) {
     if (n <= kScanSingleMax) {
         const int vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0 ? 1 : 0;
-        k_scan_single<<<1, kScanSingleThreads, 0, st>>>(in, out, n, vec);
+        launch_pdl(k_scan_single, dim3(1), dim3(kScanSingleThreads), 0, st, in, out, n, vec);
         return 1;
     }
     const int nb = (n + kScanSpan - 1) / kScanSpan;
-    if (nb > 0) k_scan_block<<<nb, kScanBlock, 0, st>>>(in, out, n, tmp);
-    k_scan_top<<<1, 1024, 0, st>>>(tmp, nb, out, n);
-    if (nb > 0) k_scan_add<<<nb, kScanBlock, 0, st>>>(out, n, tmp);
+    if (nb > 0) launch_pdl(k_scan_block, dim3(nb), dim3(kScanBlock), 0, st, in, out, n, tmp);
+    launch_pdl(k_scan_top, dim3(1), dim3(1024), 0, st, tmp, nb, out, n);
+    if (nb > 0) launch_pdl(k_scan_add, dim3(nb), dim3(kScanBlock), 0, st, out, n, tmp);
     return nb > 0 ? 3 : 1;
 }
 
 void launch_link_blocks(const DevState &S, cudaStream_t st) {
-    if (S.nLinks > 0) k_link_blocks<<<grid_for(S.nLinks, 128), 128, 0, st>>>(S);
+    if (S.nLinks > 0) launch_pdl(k_link_blocks, dim3(grid_for(S.nLinks, 128)), dim3(128), 0, st, S);
 }
 
 void launch_scatter(const DevState &S, cudaStream_t st) {
-    k_scatter<<<grid_for(S.nRods, 256), 256, 0, st>>>(S);
+    launch_pdl(k_scatter, dim3(grid_for(S.nRods, 256)), dim3(256), 0, st, S);
 }
 
 int sm_count_detect() {
@@ -1035,17 +1053,17 @@ int sm_count_detect() {
 void launch_pairs(const DevState &S, cudaStream_t st) {
     const long long items = (long long)S.pairStencil * S.pairStencil * S.pairStencil * S.nRods;
     const long long g = (items + kPairThreads - 1) / kPairThreads;
-    k_pairs<<<(unsigned)(g > 0 ? g : 1), kPairThreads, 0, st>>>(S);
-    k_pairs_exact<<<2 * sm_count_detect(), 64, 0, st>>>(S);
+    launch_pdl(k_pairs, dim3((unsigned)(g > 0 ? g : 1)), dim3(kPairThreads), 0, st, S);
+    launch_pdl(k_pairs_exact, dim3(2 * sm_count_detect()), dim3(64), 0, st, S);
 }
 
 void launch_boundary_pairs(const DevState &S, cudaStream_t st) {
-    k_boundary_pairs<<<grid_for(S.nRods, 256), 256, 0, st>>>(S);
+    launch_pdl(k_boundary_pairs, dim3(grid_for(S.nRods, 256)), dim3(256), 0, st, S);
 }
 
 int launch_pair_sort(const DevState &S, cudaStream_t st) {
-    k_pair_bucket<<<grid_for(S.cap, 256), 256, 0, st>>>(S);
-    k_pair_segsort<<<grid_for(S.nRods, 32), 32, 0, st>>>(S);
+    launch_pdl(k_pair_bucket, dim3(grid_for(S.cap, 256)), dim3(256), 0, st, S);
+    launch_pdl(k_pair_segsort, dim3(grid_for(S.nRods, 32)), dim3(32), 0, st, S);
     return 2;
 }
 
@@ -1057,8 +1075,8 @@ void launch_build(const DevState &S, cudaStream_t st) {
 
 int launch_rows(const DevState &S, cudaStream_t st) {
     const int n = launch_scan(S.rowCount, S.rowPtr, S.nRods, S.scanTmp, st);
-    k_rows_fill<<<grid_for(S.cap, 256), 256, 0, st>>>(S);
-    k_rows_sort<<<grid_for(S.nRods, 32), 32, 0, st>>>(S);
+    launch_pdl(k_rows_fill, dim3(grid_for(S.cap, 256)), dim3(256), 0, st, S);
+    launch_pdl(k_rows_sort, dim3(grid_for(S.nRods, 32)), dim3(32), 0, st, S);
     return n + 2;
 }
 

@@ -275,6 +275,7 @@ __device__ __forceinline__ void store_features(uint8_t *x, int row, const float 
 // Warm start of every collision constraint of the step (after the
 // operator assembly, before the solve).  Optionally records the features.
 __global__ void __launch_bounds__(kInferThreads) k_mlp_warm(DevState S, MlpView V) {
+    ALENS_PDL_PROLOGUE();
     __shared__ InferSmem sh;
     if (ld_volatile_i32(&S.ctl->errFlags) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
@@ -311,6 +312,7 @@ __global__ void __launch_bounds__(kInferThreads) k_mlp_warm(DevState S, MlpView 
 
 // Features only (recording without the learned warm start).
 __global__ void k_mlp_features(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (ld_volatile_i32(&S.ctl->errFlags) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x) {
@@ -671,11 +673,11 @@ void launch_mlp_warm(const DevState &S, const MlpView &V, cudaStream_t st) {
     // a tile return at once
     const int tiles = (S.cap + kMlpTile - 1) / kMlpTile;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-    k_mlp_warm<<<grid > 0 ? grid : 1, kInferThreads, 0, st>>>(S, V);
+    launch_pdl(k_mlp_warm, dim3(grid > 0 ? grid : 1), dim3(kInferThreads), 0, st, S, V);
 }
 
 void launch_mlp_features(const DevState &S, cudaStream_t st) {
-    k_mlp_features<<<2 * sm_count(), 256, 0, st>>>(S);
+    launch_pdl(k_mlp_features, dim3(2 * sm_count()), dim3(256), 0, st, S);
 }
 
 void launch_mlp_append(const DevState &S, int k0, int n, float *dsFeat, float *dsLabel, cudaStream_t st) {

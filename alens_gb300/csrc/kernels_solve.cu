@@ -21,6 +21,7 @@ __device__ __forceinline__ int flags(const DevState &S) { return ld_volatile_i32
 // the FP32 status; when all are, the FP64 launch returns at once.  The FP32
 // iteration count is kept in refineIter.
 __global__ void k_refine_setup(DevState S) {
+    ALENS_PDL_PROLOGUE();
     __shared__ int s_last;
     if (flags(S) & kErrStepAbort) return;
     const int nIdx = S.ctl->nTiles * kRowTile;
@@ -121,6 +122,7 @@ __global__ void k_refine_setup(DevState S) {
 // The solution into gamma (alens_solve reports it before the update; a
 // full step leaves the copy to k_advance).
 __global__ void k_solver_finish(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & kErrStepAbort) return;
     const int nc = S.ctl->totalCon;
     const double2 *src = S.ctl->finalParity ? S.st[1] : S.st[0];
@@ -129,6 +131,7 @@ __global__ void k_solver_finish(DevState S) {
 }
 
 __global__ void k_advance(DevState S) {
+    ALENS_PDL_PROLOGUE();
     if (flags(S) & kErrStepAbort) return;
     const size_t st = (size_t)S.nRods;
     // the solver's last iterate (the solution)
@@ -343,7 +346,7 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
             e = launch_solve_fp32(S, grid, timeout_ns, st);
         if (e != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[1], st);
-        k_refine_setup<<<8 * (grid > 0 ? grid : 1), 32, 0, st>>>(S);
+        launch_pdl(k_refine_setup, dim3(8 * (grid > 0 ? grid : 1)), dim3(32), 0, st, S);
         n += 2;
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -362,7 +365,7 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
     }
     if (e != cudaSuccess) return e;
     if (finish) {
-        k_solver_finish<<<512, 256, 0, st>>>(S);
+        launch_pdl(k_solver_finish, dim3(512), dim3(256), 0, st, S);
         n++;
     }
     if (launches) *launches += n;
@@ -375,7 +378,7 @@ void launch_advance(const DevState &S, cudaStream_t st) {
     int g = (S.nRods + 31) / 32;
     if (g < 1) g = 1;
     if (g > 16384) g = 16384;
-    k_advance<<<g, 32, 0, st>>>(S);
+    launch_pdl(k_advance, dim3(g), dim3(32), 0, st, S);
 }
 
 void launch_stress(const DevState &S, cudaStream_t st) {
