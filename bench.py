@@ -40,6 +40,21 @@ METRIC = "rod-steps/s at BBPGD residual <=1e-5 (warm-start+mixed; plain FP64 alo
 UNIT = "rod-steps/s"
 
 
+def max_over_ranks(torch, dist, world, seconds, device):
+    """The job's time: the largest per-rank time (all-reduce MAX over the
+    ranks; every rank gets it)."""
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, rods_per_rank, steps, seconds):
+    """Whole-job rod-steps/s: every rank steps its own replica of
+    `rods_per_rank` rods (weak scaling), timed by the slowest rank."""
+    return world * rods_per_rank * steps / seconds
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -629,15 +644,12 @@ def main():
     clocks = clk.summary()
 
     def total_s(arm):
-        t = torch.tensor([sum(arm["ms"]) * 1e-3], dtype=torch.float64, device="cuda")
-        if world > 1:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(torch, dist, world, sum(arm["ms"]) * 1e-3, "cuda")
 
     t_fast, t_plain, t_e2e = total_s(fast), total_s(plain), total_s(e2e)
-    value = world * nr * args.steps / t_fast
-    plain_value = world * nr * args.steps / t_plain
-    e2e_value = world * nr * args.steps / t_e2e
+    value = job_throughput(world, nr, args.steps, t_fast)
+    plain_value = job_throughput(world, nr, args.steps, t_plain)
+    e2e_value = job_throughput(world, nr, args.steps, t_e2e)
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
