@@ -39,7 +39,7 @@ def test_max_over_ranks_and_job_throughput_gloo():
     import torch.multiprocessing as mp
     world = 2
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_rank_main, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
