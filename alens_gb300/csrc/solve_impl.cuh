@@ -11,10 +11,13 @@
 // barrier per pass.  Pass p:
 //   1. decision (every block, for the replicas of its tiles): canonical
 //      reduction of the pass p-1 tile partials -> residual test, step size;
-//      the block holding a replica's first tile records its state
+//      the block holding a replica's first tile records its state.  Under
+//      it, the upper warps copy the previous iterates of the columns of the
+//      block's cached operator rows into shared memory (cp.async)
 //   2. rows (64-constraint tiles, contiguous per block): row k forms
 //      x_l for its columns, (A x)_k, the update and the tile partials
-//   3. grid barrier
+//   3. grid barrier (per-pass counter polled by every block; the arrival
+//      word also counts the replicas still iterating, which decides stop)
 // Passes: 0 = G0 (x = gamma0, g = A x + q, residual), 1 = AG (x = g: step
 // g.g / g.Ag), 2.. = iterations x = P(gamma - alpha g).  gamma and g
 // ping-pong between two buffers by pass parity; retired replicas copy their
@@ -25,8 +28,9 @@
 // contraction; the fused multiply-adds of the row product are explicit on
 // both sides).
 // Real = float: FP32 operator, gamma and g, products and per-warp sums;
-// FP64 tile/chunk accumulation of the dot products and step sizes; the
-// residual min(g, x - lb) is exact for lb = 0 and bilateral rows.
+// FP64 tile/chunk accumulation of the dot products; the step-size quotient
+// in FP32 (the step is used in FP32); the residual min(g, x - lb) is exact
+// for lb = 0 and bilateral rows.
 #pragma once
 
 #include <cstdio>
