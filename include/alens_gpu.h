@@ -386,12 +386,16 @@ int alens_get_launch_count(AlensCtx *ctx, int64_t *count);
 
 /* Project autotuner (no counterpart in the reference): detects the next
  * step's constraints, times every applicable configuration of the solver on
- * that problem (grid form with 1 or 2 blocks per SM; for the mixed
- * precision also the cluster forms with 2-16 CTAs per cluster and 256 or
- * 512 threads per CTA), each `reps` times from the same initial iterate,
- * and keeps the fastest for the following steps.  The rods do not move.
- * report (nullable, reportCap bytes) receives a JSON text with every
- * candidate's median solve time and the index of the chosen one. */
+ * that problem (grid form with 1 or 2 blocks per SM and at least 1, 2, 4 or
+ * 8 64-row tiles per block; for the mixed precision also the cluster forms
+ * with 2-16 CTAs per cluster and 256 or 512 threads per CTA), each `reps`
+ * times from the same initial iterate, and keeps the fastest for the
+ * following steps.  The rods do not move.  report (nullable, reportCap
+ * bytes) receives a JSON text with every candidate's median solve time and
+ * the index of the chosen one.  The environment variables
+ * ALENS_SOLVER_FORM (grid | cluster | resident), ALENS_SOLVER_BLOCKS_PER_SM,
+ * ALENS_SOLVER_MIN_TILES, ALENS_CLUSTER_SIZE and ALENS_CSM_THREADS set the
+ * same choices by hand when a context is created. */
 int alens_autotune(AlensCtx *ctx, int reps, char *report, int reportCap);
 
 /* CUDA-event times (ms) of the stages of the last step when stageTiming is
