@@ -487,6 +487,26 @@ def test_autotune_keeps_fp64_parity(gpu_lib):
     compare_state(g, o)
 
 
+@pytest.mark.parametrize("box,n,pbc", [(1.3, 300, (1, 1, 1)), (1.9, 600, (1, 1, 1)), (1.3, 300, (1, 1, 0))])
+def test_dense_pair_search_stencil(gpu_lib, box, n, pbc):
+    """Dense boxes (more than 24 rods per cutoff-sized cell) take the
+    half-cutoff cells and the 5-cell stencil; with 2 or 3 cells per side
+    the +-2 offsets wrap once across the periodic boundary (and are dropped
+    where that still leaves the grid, or where the side is not periodic).
+    The pair sets, multipliers and trajectory equal the oracle's bit for
+    bit."""
+    from alens_gb300 import workloads as wl
+    w = wl.small_periodic(n=n, box=box, seed=3, lmin=0.5, lmax=1.0)
+    cfg = wl.config_with(w.cfg, simBoxPBC=pbc)
+    g, o = pair(cfg, w.rods)
+    for _ in range(3):
+        sg, so = g.step(), o.step()
+        assert sg["nCollision"] == so["nCollision"] > 0
+        assert sg["iterations"] == so["iterations"]
+        compare_constraints(g, o)
+    compare_state(g, o)
+
+
 @pytest.mark.parametrize("min_tiles", [2, 3, 8])
 def test_min_tiles_per_block_keeps_fp64_parity(gpu_lib, monkeypatch, min_tiles):
     """Fewer, fuller solver blocks (a minimum number of 64-row tiles per
