@@ -255,8 +255,15 @@ void Engine::finalize() {
     DevState &S = S_;
     std::memset(&S, 0, sizeof(S));
     S.R = R_;
-    S.pairStencil = 3;
-    for (int r = 0; r < R_; r++) S.pairStencil = std::max(S.pairStencil, hostPar_[r].stencil);
+    for (int d = 0; d < 3; d++) {
+        int rad = 0;
+        for (int r = 0; r < R_; r++) {
+            const RepParams &P = hostPar_[r];
+            // one cell along a closed side: no neighbour cells that way
+            if (!(P.ncell[d] == 1 && !P.pbc[d])) rad = std::max(rad, P.stencil >> 1);
+        }
+        S.pairW[d] = 2 * rad + 1;
+    }
     S.nRods = N;
     S.nCells = C;
     S.warm = warm_;

@@ -112,7 +112,8 @@ struct DevState {
     int R, nRods, cap, nCells, tileCap, workCap, blockCap, nnzCap;
     int warm, precision;
     int solveMinTiles;         // BBPGD: at least this many 64-row tiles per solver block
-    int pairStencil;           // pair search: max over replicas of RepParams::stencil
+    int pairW[3];              // pair search: stencil width per dimension (max over replicas;
+                               // 1 where every replica has one closed cell)
     RepParams *par;
     RepDyn *dyn;
     DevCtl *ctl;

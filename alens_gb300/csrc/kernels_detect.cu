@@ -486,14 +486,15 @@ __device__ __noinline__ bool exact_pair(const DevState &S, int i, int j, const R
 __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
     ALENS_PDL_PROLOGUE();
     const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int W = S.pairStencil, Rw = W >> 1;  // stencil of W^3 cells (W = 3 or 5)
-    const bool valid = item < (long long)(W * W * W) * S.nRods && !(flags(S) & kErrNaN);
+    // stencil of Wx x Wy x Wz cells (widths 1, 3 or 5)
+    const int Wx = S.pairW[0], Wy = S.pairW[1], Wz = S.pairW[2];
+    const bool valid = item < (long long)(Wx * Wy * Wz) * S.nRods && !(flags(S) & kErrNaN);
     unsigned long long buf[kPairBuf];
     int nb = 0;
     if (valid) {
         const int t = (int)(item % S.nRods);
         const int nbr = (int)(item / S.nRods);
-        const int ox = nbr % W - Rw, oy = (nbr / W) % W - Rw, oz = nbr / (W * W) - Rw;
+        const int ox = nbr % Wx - (Wx >> 1), oy = (nbr / Wx) % Wy - (Wy >> 1), oz = nbr / (Wx * Wy) - (Wz >> 1);
         const int i = S.sidx[t];
         const RepParams &P = S.par[S.rodRep[i]];
         const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
@@ -1051,7 +1052,7 @@ int sm_count_detect() {
 }
 
 void launch_pairs(const DevState &S, cudaStream_t st) {
-    const long long items = (long long)S.pairStencil * S.pairStencil * S.pairStencil * S.nRods;
+    const long long items = (long long)S.pairW[0] * S.pairW[1] * S.pairW[2] * S.nRods;
     const long long g = (items + kPairThreads - 1) / kPairThreads;
     launch_pdl(k_pairs, dim3((unsigned)(g > 0 ? g : 1)), dim3(kPairThreads), 0, st, S);
     launch_pdl(k_pairs_exact, dim3(2 * sm_count_detect()), dim3(64), 0, st, S);
