@@ -669,7 +669,9 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum(fast["ms"]) / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk / f64 dots+residual+refine",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "precision": "f32 operator, iterates and row products; f64 dot-product accumulation, "
+                     "residual check and refinement; the plain arm is f64 throughout",
         "data": "synthetic (seeded)",
         "config": {"workload": w.name, "rods": nr, "box_um": [args.side, args.side, 0.1],
                    "pre_steps": args.pre_steps, "form": "mixed precision + learned warm start",
