@@ -183,6 +183,36 @@ def test_mobility_slender_body_and_sphere():
     assert np.allclose(O.mobility(0.15, 0.1, mu), ref, rtol=1e-14)
 
 
+def test_brownian_velocity_fluctuation_dissipation():
+    """Known velocity U_B = sqrt(2 kT/dt) M^1/2 xi has covariance (2 kT/dt) M:
+    along the axis the parallel mobility, across it the perpendicular one,
+    rotation only about axes normal to the rod (20,000 unit rods)."""
+    w = workloads.small_periodic(n=20000, box=30.0, seed=3, lmin=1.0, lmax=1.0)
+    s = O.OracleSystem(w.cfg)
+    s.set_rods(w.rods)
+    s.detect()
+    u = s.known_velocity()
+    a = workloads.quat_to_axis(w.rods.quat)
+    m = O.mobility(1.0, float(w.rods.radius[0]), w.cfg.viscosity)
+    c = 2.0 * w.cfg.KBT / w.cfg.dt
+    ut, om = u[:, :3], u[:, 3:]
+    upar = np.einsum("ij,ij->i", ut, a)
+    uperp = ut - upar[:, None] * a
+    opar = np.einsum("ij,ij->i", om, a)
+    operp = om - opar[:, None] * a
+    z = upar / math.sqrt(c * m[0])
+    assert abs(z.mean()) < 0.03 and abs(z.var() - 1.0) < 0.05
+    assert abs((uperp ** 2).sum(1).mean() / (c * m[1]) - 2.0) < 0.1
+    assert abs((operp ** 2).sum(1).mean() / (c * m[2]) - 2.0) < 0.1
+    assert np.abs(opar).max() <= 1e-12 * math.sqrt(c * m[2])
+    assert abs(np.corrcoef(upar, uperp[:, 0])[0, 1]) < 0.05
+    # a fresh context at the same step draws the same noise (keyed by seed, gid, step)
+    s2 = O.OracleSystem(w.cfg)
+    s2.set_rods(w.rods)
+    s2.detect()
+    assert np.array_equal(s2.known_velocity(), u)
+
+
 # ---------------------------------------------- solve: independent KKT
 def _assemble(sysO, rods, cfg):
     """D (6N x Nc), block mobility M and U_nc rebuilt in numpy."""
