@@ -270,6 +270,27 @@ def test_bbpgd_kkt_independent():
     assert abs(res - st["residual"]) <= 1e-9
 
 
+def test_collision_stress_is_pair_virial():
+    """Collision virial sum_k gamma_k (P_k - Q_k) n_k^T rebuilt in numpy: with
+    n = (P - Q)/|P - Q| it is sum_k gamma_k d_k n_k n_k^T, d_k = phi0_k +
+    rcol_I + rcol_J, symmetric and positive semidefinite (gamma >= 0)."""
+    w = workloads.small_periodic(n=400, box=2.6, seed=11, col_ratio_d=0.8)
+    s = O.OracleSystem(w.cfg)
+    s.set_rods(w.rods)
+    s.detect()
+    s.solve(allow_not_converged=False)
+    con = s.constraints()
+    assert con["nbil"] == 0 and con["ncoll"] > 20
+    rcol = 0.8 * w.rods.radius
+    d = con["delta0"] + rcol[con["i"]] + rcol[con["j"]]
+    n = con["jac"][:, :3]
+    ref = np.einsum("k,ka,kb->ab", con["gamma"] * d, n, n)
+    got = s.con_stress()
+    assert np.allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    assert np.allclose(got, got.T, rtol=0, atol=1e-12 * np.abs(ref).max())
+    assert np.linalg.eigvalsh(0.5 * (got + got.T)).min() >= -1e-12 * np.abs(ref).max()
+
+
 def test_step_translation_invariance():
     w = workloads.small_periodic(n=300, box=2.5, seed=4, kbt=-1.0)
     a = O.OracleSystem(w.cfg)
