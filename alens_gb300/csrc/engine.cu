@@ -169,7 +169,6 @@ void Engine::makeParams(int rep, const HostRods &h, RepParams &P) const {
         mx = std::max(mx, 2.0 * hh + 2.0 * rc);
     }
     const double cutoff = mx + c.sylinderColBuf;
-    long long total = 1;
     for (int d = 0; d < 3; d++) {
         P.lo[d] = c.simBoxLow[d];
         P.hi[d] = c.simBoxHigh[d];
@@ -197,7 +196,7 @@ void Engine::makeParams(int rep, const HostRods &h, RepParams &P) const {
     // keep the cell count proportional to the rod count (the grid only
     // affects the candidate enumeration, never the result)
     const long long limit = std::max<long long>(64, 2LL * h.n);
-    while ((total = (long long)P.ncell[0] * P.ncell[1] * P.ncell[2]) > limit) {
+    while ((long long)P.ncell[0] * P.ncell[1] * P.ncell[2] > limit) {
         int d = 0;
         for (int e = 1; e < 3; e++)
             if (P.ncell[e] > P.ncell[d]) d = e;
