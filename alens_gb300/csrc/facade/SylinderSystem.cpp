@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
@@ -275,6 +276,10 @@ void SylinderSystem::create() {
     check(alens_set_rods(ctx_, 0, n, gid.data(), pos.data(), quat.data(), len.data(), rad.data(), imm.data()),
           "alens_set_rods");
     conPool_.assign(std::max(1, omp_get_max_threads()), ConstraintBlockQue());
+    dinfo_ = DomainInfo::fromConfig(runConfig);
+    rngPool_ = std::make_shared<RngPool>(runConfig.rngSeed, std::max(1, omp_get_max_threads()));
+    snapID_ = 0;
+    stepOffset_ = 0;
     rodsStale_ = false;
     applyLinks();
     if (!runConfig.boundaries.empty())
@@ -322,7 +327,21 @@ void SylinderSystem::initialize(const std::string &configFile, const std::string
 
 void SylinderSystem::reinitialize(const std::string &configFile, const std::string &restartFile, int argc,
                                   char **argv, bool) {
-    initialize(configFile, restartFile, argc, argv);
+    long step = 0;
+    int snap = 0;
+    double time = 0.0;
+    {
+        std::ifstream in(restartFile);
+        if (!in) throw std::runtime_error("cannot read " + restartFile);
+    }
+    if (!readTimeStepInfo(restartFile, &step, &snap, &time)) {
+        initialize(configFile, restartFile, argc, argv);
+        return;
+    }
+    const std::string snapFile = getResultFolderWithID(snap) + "SylinderAscii_" + std::to_string(snap) + ".dat";
+    initialize(configFile, snapFile, argc, argv);
+    snapID_ = snap + 1;
+    stepOffset_ = step;
 }
 
 void SylinderSystem::initialize(const SylinderConfig &cfg, const std::vector<Sylinder> &rods) {
@@ -404,7 +423,92 @@ const std::vector<Sylinder> &SylinderSystem::getContainer() {
 long SylinderSystem::getStepCount() const {
     int64_t c = 0;
     if (ctx_) alens_get_step_count(ctx_, &c);
-    return (long)c;
+    return stepOffset_ + (long)c;
+}
+
+bool SylinderSystem::readTimeStepInfo(const std::string &path, long *step, int *snapID, double *time) {
+    std::ifstream in(path);
+    std::string a, b, c, extra;
+    if (!(in >> a >> b >> c) || (in >> extra)) return false;
+    char *e1 = nullptr, *e2 = nullptr, *e3 = nullptr;
+    const long st = std::strtol(a.c_str(), &e1, 10);
+    const long sn = std::strtol(b.c_str(), &e2, 10);
+    const double t = std::strtod(c.c_str(), &e3);
+    if (*e1 != '\0' || *e2 != '\0' || *e3 != '\0' || st < 0 || sn < 0 || sn > 2147483647L) return false;
+    *step = st;
+    *snapID = (int)sn;
+    *time = t;
+    return true;
+}
+
+bool SylinderSystem::snapshotDue(long step, double timeSnap, double dt) {
+    if (!(dt > 0.0) || !(timeSnap > 0.0)) return false;
+    const long every = std::max(1L, (long)std::llround(timeSnap / dt));
+    return step % every == 0;
+}
+
+std::string SylinderSystem::getResultFolderWithID(int snapID) {
+    constexpr int kPerFolder = 400;
+    const int lo = snapID / kPerFolder * kPerFolder;
+    return "./result/result" + std::to_string(lo) + "-" + std::to_string(lo + kPerFolder - 1) + "/";
+}
+
+void SylinderSystem::writeResult() {
+    if (!getIfWriteResultCurrentStep()) return;
+    const std::string folder = getCurrentResultFolder();
+    std::error_code ec;
+    std::filesystem::create_directories(folder, ec);
+    if (ec) throw std::runtime_error("cannot create " + folder + ": " + ec.message());
+    writeResult(folder + "SylinderAscii_" + std::to_string(snapID_) + ".dat");
+    std::FILE *f = std::fopen("TimeStepInfo.txt", "w");
+    if (!f) throw std::runtime_error("cannot write TimeStepInfo.txt");
+    std::fprintf(f, "%ld\n%d\n%.17g\n", getStepCount(), snapID_, runConfig.dt * (double)getStepCount());
+    std::fclose(f);
+    snapID_++;
+}
+
+DomainInfo DomainInfo::fromConfig(const SylinderConfig &cfg) {
+    DomainInfo d;
+    for (int k = 0; k < 3; k++) {
+        d.low[k] = cfg.simBoxLow[k];
+        d.high[k] = cfg.simBoxHigh[k];
+        d.pbc[k] = cfg.simBoxPBC[k];
+    }
+    return d;
+}
+
+RngPool::RngPool(unsigned long long seed, int nThreads) {
+    streams_.resize(std::max(1, nThreads));
+    for (size_t t = 0; t < streams_.size(); t++) {
+        std::seed_seq seq{(unsigned)(seed & 0xffffffffu), (unsigned)(seed >> 32), (unsigned)t};
+        streams_[t].eng.seed(seq);
+    }
+}
+
+RngPool::Stream &RngPool::at(int threadId) {
+    if (threadId < 0 || threadId >= (int)streams_.size())
+        throw std::out_of_range("RngPool: thread id " + std::to_string(threadId));
+    return streams_[threadId];
+}
+
+double RngPool::getU01(int threadId) {
+    Stream &s = at(threadId);
+    return ((double)(s.eng() >> 11) + 0.5) * 0x1p-53;
+}
+
+double RngPool::getN01(int threadId) {
+    Stream &s = at(threadId);
+    if (s.hasSpare) {
+        s.hasSpare = false;
+        return s.spare;
+    }
+    const double u1 = ((double)(s.eng() >> 11) + 0.5) * 0x1p-53;
+    const double u2 = ((double)(s.eng() >> 11) + 0.5) * 0x1p-53;
+    const double r = std::sqrt(-2.0 * std::log(u1));
+    const double th = 6.283185307179586 * u2;
+    s.spare = r * std::sin(th);
+    s.hasSpare = true;
+    return r * std::cos(th);
 }
 
 void SylinderSystem::writeResult(const std::string &path) const {
@@ -421,6 +525,7 @@ void SylinderSystem::writeResult(const std::string &path) const {
                      (long long)r.gid, r.radius, r.pos[0] - h * d[0], r.pos[1] - h * d[1], r.pos[2] - h * d[2],
                      r.pos[0] + h * d[0], r.pos[1] + h * d[1], r.pos[2] + h * d[2], r.group);
     }
+    for (const auto &l : links_) std::fprintf(f, "L %lld %lld\n", (long long)l[0], (long long)l[1]);
     std::fclose(f);
 }
 

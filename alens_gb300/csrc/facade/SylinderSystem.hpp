@@ -2,13 +2,15 @@
 // uses on SimToolbox's SylinderSystem (SRC/TubuleSystem.cpp:38,55,79,100,105,
 // 120,176,223,224,229,697), implemented over the C ABI of include/alens_gpu.h.
 //
-// One system on one GPU: the MPI/FDPS getters of the reference
-// (getDomainInfo, getCommRcp, ...) have no counterpart; prepareStep() has no
-// repartitioning to do.
+// One system on one GPU and one rank: the MPI/FDPS getters of the reference
+// (getDomainInfo, getCommRcp, getRngPoolPtr) return single-rank values, and
+// prepareStep() has no repartitioning to do.
 #pragma once
 
 #include <array>
 #include <cstdint>
+#include <memory>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -76,6 +78,46 @@ struct ConstraintBlock {
 using ConstraintBlockQue = std::vector<ConstraintBlock>;
 using ConstraintBlockPool = std::vector<ConstraintBlockQue>;
 
+// Root domain of the single rank (the role of FDPS's DomainInfo that
+// TubuleSystem hands to its protein container, SRC/TubuleSystem.cpp:121-125):
+// the simulation box and its periodic axes.
+struct DomainInfo {
+    std::array<double, 3> low{{0, 0, 0}}, high{{1, 1, 1}};
+    std::array<bool, 3> pbc{{false, false, false}};
+    double getLen(int d) const { return high[d] - low[d]; }
+    static DomainInfo fromConfig(const SylinderConfig &cfg);
+};
+
+// Communicator of the single rank (TubuleSystem asks getCommRcp()->getRank(),
+// SRC/TubuleSystem.cpp:812-813).
+struct Comm {
+    int getRank() const { return 0; }
+    int getSize() const { return 1; }
+};
+
+// Per-thread random streams for host-side callers (the role of the pool that
+// TubuleSystem draws from with getU01(threadId) / getN01(threadId),
+// SRC/TubuleSystem.cpp:273-279,381).  Stream t is a 64-bit Mersenne twister
+// seeded with (seed, t); uniforms are (k + 1/2) 2^-53 for the top 53 bits k
+// (open interval), normals come from the Box-Muller pair of two uniforms.
+// A thread uses only its own stream.
+class RngPool {
+  public:
+    RngPool(unsigned long long seed, int nThreads);
+    double getU01(int threadId);
+    double getN01(int threadId);
+    int size() const { return (int)streams_.size(); }
+
+  private:
+    struct Stream {
+        std::mt19937_64 eng;
+        double spare = 0.0;
+        bool hasSpare = false;
+    };
+    Stream &at(int threadId);
+    std::vector<Stream> streams_;
+};
+
 class SylinderSystem {
   public:
     SylinderConfig runConfig;
@@ -90,7 +132,10 @@ class SylinderSystem {
     // std::runtime_error on failure.
     void initialize(const std::string &configFile, const std::string &posFile, int argc = 0,
                     char **argv = nullptr);
-    // Restart from a SylinderAscii snapshot written by writeResult().
+    // Restart from TimeStepInfo.txt written by writeResult() (the rods come
+    // from that snapshot's SylinderAscii file, getSnapID() is its ID + 1 and
+    // getStepCount() continues from its step), or directly from a
+    // SylinderAscii snapshot file.
     void reinitialize(const std::string &configFile, const std::string &restartFile, int argc = 0,
                       char **argv = nullptr, bool eulerStep = false);
     void initialize(const SylinderConfig &cfg, const std::vector<Sylinder> &rods);
@@ -100,7 +145,14 @@ class SylinderSystem {
     void stepEuler();             // apply a solve prepared by detect/solve (restart path)
     void calcConStress();         // pair virial of the last step
     void calcOrderParameter();    // polar and nematic order of the rod axes
-    void writeResult(const std::string &path) const;  // SylinderAscii text
+    void writeResult(const std::string &path) const;  // SylinderAscii text (rods, then link lines)
+    // When a snapshot is due at the current step: SylinderAscii_<snapID>.dat
+    // in the current result folder (created) and ./TimeStepInfo.txt (step,
+    // snapID and time, one per line; its presence is what makes aLENS
+    // restart, SRC/main.cpp:28-37), then snapID + 1.  Called where the
+    // reference calls writeResult() (SRC/TubuleSystem.cpp:100); its runStep
+    // also writes before moving, which a caller does here with one more call.
+    void writeResult();
     void setTimer(bool on) { timerOn_ = on; }
     void printTimingSummary() const;
 
@@ -108,6 +160,24 @@ class SylinderSystem {
     const std::vector<Sylinder> &getContainer();  // host copy, refreshed after steps
     long getStepCount() const;
     int getSnapID() const { return snapID_; }
+
+    // single-rank getters (set up by initialize)
+    const DomainInfo &getDomainInfo() const { return dinfo_; }
+    DomainInfo &getDomainInfoNonConst() { return dinfo_; }
+    const std::shared_ptr<const Comm> &getCommRcp() const { return comm_; }
+    std::shared_ptr<RngPool> getRngPoolPtr() const { return rngPool_; }
+
+    // Snapshot bookkeeping (SRC/TubuleSystem.cpp:50,309-310,321): a snapshot
+    // every round(timeSnap / dt) steps; snapshots grouped 400 to a folder,
+    // ./result/result0-399/, ./result/result400-799/, ... (the layout
+    // docs/source/visualization.md:32 lists).
+    bool getIfWriteResultCurrentStep() const { return snapshotDue(getStepCount(), runConfig.timeSnap, runConfig.dt); }
+    std::string getCurrentResultFolder() const { return getResultFolderWithID(snapID_); }
+    static std::string getResultFolderWithID(int snapID);
+    static bool snapshotDue(long step, double timeSnap, double dt);
+    // TimeStepInfo.txt: exactly three numbers (step, snapID, time); false
+    // for anything else (a SylinderAscii snapshot, say)
+    static bool readTimeStepInfo(const std::string &path, long *step, int *snapID, double *time);
     const AlensStepStats &lastStats() const { return stats_; }
     std::array<double, 9> conStress() const { return stress_; }
     std::array<double, 3> polarOrder() const { return polar_; }
@@ -129,8 +199,12 @@ class SylinderSystem {
     std::array<double, 3> polar_{};
     std::array<double, 9> nematic_{};
     int snapID_ = 0;
+    long stepOffset_ = 0;  // step of the snapshot a restart began from
     bool timerOn_ = false;
     double lastStepMs_ = 0.0;
+    DomainInfo dinfo_;
+    std::shared_ptr<const Comm> comm_ = std::make_shared<const Comm>();
+    std::shared_ptr<RngPool> rngPool_;
 };
 
 // Read TubuleInitial.dat / SylinderAscii lines; 'L' link lines are returned

@@ -8,14 +8,147 @@
 // The bilateral blocks are one spring (kappa = linkKappa) between the first
 // two rods, rebuilt every step from their current geometry.  Prints one JSON
 // line with the run summary.
+//
+// usage: facade_driver --host-checks RunConfig.yaml [restart files...]
+// Prints one JSON line from the single-rank getters that need no device
+// (result folders, snapshot schedule, domain, communicator, random pool)
+// and, per restart file, [is TimeStepInfo, step, snapID, time].
+//
+// usage: facade_driver --restart-check RunConfig.yaml TubuleInitial.dat steps
+// Steps a system, calling writeResult() before each runStep (where the
+// reference's runStep writes its snapshot), then restarts a second system
+// from ./TimeStepInfo.txt and prints one JSON line: snapshot IDs and steps of
+// both, and the largest centre and axis differences between the restarted
+// rods and the first system's rods at its last snapshot.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "SylinderSystem.hpp"
 
+namespace {
+
+int hostChecks(const char *yaml, int nFiles, char **files) {
+    gpu::SylinderConfig cfg;
+    std::string err;
+    if (!cfg.readYaml(yaml, &err)) {
+        std::fprintf(stderr, "facade_driver: %s\n", err.c_str());
+        return 1;
+    }
+    const gpu::DomainInfo d = gpu::DomainInfo::fromConfig(cfg);
+    const gpu::Comm comm;
+    gpu::RngPool pool(cfg.rngSeed, 2), again(cfg.rngSeed, 2);
+    const int n = 200000;
+    double su = 0, suu = 0, sn = 0, snn = 0, umin = 1, umax = 0;
+    for (int i = 0; i < n; i++) {
+        const double u = pool.getU01(0), z = pool.getN01(0);
+        su += u;
+        suu += u * u;
+        sn += z;
+        snn += z * z;
+        umin = u < umin ? u : umin;
+        umax = u > umax ? u : umax;
+    }
+    const double first1 = pool.getU01(1), firstAgain0 = again.getU01(0), firstAgain1 = again.getU01(1);
+    bool outOfRange = false;
+    try {
+        pool.getU01(2);
+    } catch (const std::out_of_range &) {
+        outOfRange = true;
+    }
+    std::string restart = "[";
+    for (int f = 0; f < nFiles; f++) {
+        long step = -1;
+        int snap = -1;
+        double time = -1.0;
+        const bool info = gpu::SylinderSystem::readTimeStepInfo(files[f], &step, &snap, &time);
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "%s[%d, %ld, %d, %.17g]", f ? ", " : "", (int)info, step, snap, time);
+        restart += buf;
+    }
+    restart += "]";
+    const long every = std::lround(cfg.timeSnap / cfg.dt);
+    std::printf("{\"folders\": [\"%s\", \"%s\", \"%s\", \"%s\"], \"snap_every\": %ld, "
+                "\"due\": [%d, %d, %d, %d], \"low\": [%.17g, %.17g, %.17g], \"high\": [%.17g, %.17g, %.17g], "
+                "\"pbc\": [%d, %d, %d], \"len0\": %.17g, \"rank\": %d, \"size\": %d, "
+                "\"u_mean\": %.9g, \"u_var\": %.9g, \"u_min\": %.17g, \"u_max\": %.17g, "
+                "\"n_mean\": %.9g, \"n_var\": %.9g, \"stream1_first\": %.17g, "
+                "\"again0_first\": %.17g, \"again1_first\": %.17g, \"out_of_range\": %d, \"restart\": %s}\n",
+                gpu::SylinderSystem::getResultFolderWithID(0).c_str(),
+                gpu::SylinderSystem::getResultFolderWithID(399).c_str(),
+                gpu::SylinderSystem::getResultFolderWithID(400).c_str(),
+                gpu::SylinderSystem::getResultFolderWithID(1234).c_str(), every,
+                (int)gpu::SylinderSystem::snapshotDue(0, cfg.timeSnap, cfg.dt),
+                (int)gpu::SylinderSystem::snapshotDue(1, cfg.timeSnap, cfg.dt),
+                (int)gpu::SylinderSystem::snapshotDue(every, cfg.timeSnap, cfg.dt),
+                (int)gpu::SylinderSystem::snapshotDue(3 * every + 1, cfg.timeSnap, cfg.dt), d.low[0], d.low[1],
+                d.low[2], d.high[0], d.high[1], d.high[2], (int)d.pbc[0], (int)d.pbc[1], (int)d.pbc[2], d.getLen(0),
+                comm.getRank(), comm.getSize(), su / n, suu / n - (su / n) * (su / n), umin, umax, sn / n,
+                snn / n - (sn / n) * (sn / n), first1, firstAgain0, firstAgain1, (int)outOfRange,
+                restart.c_str());
+    return 0;
+}
+
+void axisOf(const double q[4], double a[3]) {
+    const double x = q[0], y = q[1], z = q[2], w = q[3];
+    a[0] = 2.0 * (x * z + w * y);
+    a[1] = 2.0 * (y * z - w * x);
+    a[2] = 1.0 - 2.0 * (x * x + y * y);
+}
+
+int restartCheck(const char *yaml, const char *dat, int steps) {
+    gpu::SylinderSystem first;
+    first.initialize(yaml, dat);
+    std::vector<gpu::Sylinder> snap;
+    long snapStep = -1;
+    int snapID = -1;
+    for (int s = 0; s < steps; s++) {
+        if (first.getIfWriteResultCurrentStep()) {
+            snap = first.getContainer();
+            snapStep = first.getStepCount();
+            snapID = first.getSnapID();
+        }
+        first.writeResult();
+        first.runStep();
+    }
+    gpu::SylinderSystem again;
+    again.reinitialize(yaml, "TimeStepInfo.txt");
+    const auto &rods = again.getContainer();
+    double dpos = 0.0, daxis = 0.0;
+    const bool same = rods.size() == snap.size();
+    for (size_t i = 0; same && i < rods.size(); i++) {
+        double a[3], b[3];
+        axisOf(rods[i].orientation, a);
+        axisOf(snap[i].orientation, b);
+        for (int d = 0; d < 3; d++) {
+            dpos = std::fmax(dpos, std::fabs(rods[i].pos[d] - snap[i].pos[d]));
+            daxis = std::fmax(daxis, std::fabs(a[d] - b[d]));
+        }
+    }
+    std::printf("{\"snap_id_after\": %d, \"last_snap_id\": %d, \"last_snap_step\": %ld, \"steps\": %ld, "
+                "\"restart_snap_id\": %d, \"restart_step\": %ld, \"same_count\": %d, \"max_dpos\": %.3g, "
+                "\"max_daxis\": %.3g, \"folder\": \"%s\"}\n",
+                first.getSnapID(), snapID, snapStep, first.getStepCount(), again.getSnapID(), again.getStepCount(),
+                (int)same, dpos, daxis, again.getResultFolderWithID(snapID).c_str());
+    return 0;
+}
+
+}  // namespace
+
 int main(int argc, char **argv) {
+    if (argc >= 3 && std::strcmp(argv[1], "--host-checks") == 0) return hostChecks(argv[2], argc - 3, argv + 3);
+    if (argc == 5 && std::strcmp(argv[1], "--restart-check") == 0) {
+        try {
+            return restartCheck(argv[2], argv[3], std::atoi(argv[4]));
+        } catch (const std::exception &e) {
+            std::fprintf(stderr, "facade_driver: %s\n", e.what());
+            return 1;
+        }
+    }
     if (argc < 4) {
         std::fprintf(stderr, "usage: %s RunConfig.yaml TubuleInitial.dat steps [out.dat]\n", argv[0]);
         return 2;

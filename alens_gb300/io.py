@@ -57,7 +57,9 @@ def read_sylinder_ascii(path):
     return rods, links
 
 
-def write_sylinder_ascii(path, rods: RodState, time: float = 0.0, group=None):
+def write_sylinder_ascii(path, rods: RodState, time: float = 0.0, group=None, links=()):
+    """Rods as 'C|S gid radius minus-end plus-end group' lines, then the
+    links as 'L a b' lines (gids), readable by read_sylinder_ascii."""
     a = quat_to_axis(rods.quat)
     h = 0.5 * rods.length[:, None]
     m = rods.pos - h * a
@@ -69,6 +71,8 @@ def write_sylinder_ascii(path, rods: RodState, time: float = 0.0, group=None):
             g = -1 if group is None else int(group[i])
             f.write("%s %d %.17g %.17g %.17g %.17g %.17g %.17g %.17g %d\n" % (
                 "S" if imm[i] else "C", rods.gid[i], rods.radius[i], *m[i], *p[i], g))
+        for la, lb in links:
+            f.write("L %d %d\n" % (int(la), int(lb)))
 
 
 def read_run_config(path, **overrides) -> AlensConfig:

@@ -141,3 +141,26 @@ def test_flexible_filament_links(gpu_lib, tmp_path):
     # the chain holds together: neighbour spacing stays near 2r + gap
     d = np.linalg.norm(np.diff(pg, axis=0), axis=1)
     assert np.all(np.abs(d[1:] - (0.02 + gap)) < 0.01)
+
+
+def test_facade_snapshot_and_restart(gpu_lib, tmp_path):
+    """writeResult() before every runStep writes SylinderAscii_<snapID>.dat
+    into ./result/result0-399/ every round(timeSnap/dt) steps plus
+    ./TimeStepInfo.txt; reinitialize from TimeStepInfo.txt restores the last
+    snapshot's rods, its snapID + 1 and its step."""
+    exe = build.build_facade_driver()
+    with open(os.path.join(GOLDEN, "monolayer_window.yaml")) as f:
+        text = f.read()
+    yml = tmp_path / "RunConfig.yaml"
+    yml.write_text(text + "timeSnap: 0.00002\n")  # every 2 steps (dt = 1e-5)
+    proc = subprocess.run([str(exe), "--restart-check", str(yml), os.path.join(GOLDEN, "monolayer_window.dat"), "5"],
+                          capture_output=True, text=True, timeout=300, cwd=str(tmp_path))
+    assert proc.returncode == 0, proc.stderr
+    r = json.loads(proc.stdout.strip().splitlines()[-1])
+    assert r["steps"] == 5 and r["snap_id_after"] == 3  # steps 0, 2, 4
+    assert r["last_snap_id"] == 2 and r["last_snap_step"] == 4
+    assert r["restart_snap_id"] == 3 and r["restart_step"] == 4
+    assert r["same_count"] == 1 and r["max_dpos"] < 1e-12 and r["max_daxis"] < 1e-12
+    folder = tmp_path / "result" / "result0-399"
+    assert sorted(p.name for p in folder.iterdir()) == [f"SylinderAscii_{i}.dat" for i in range(3)]
+    assert (tmp_path / "TimeStepInfo.txt").read_text().split()[:2] == ["4", "2"]

@@ -1,0 +1,78 @@
+"""CPU tests of the C++ SylinderSystem facade's single-rank getters: result
+folders and snapshot schedule, domain, communicator and the per-thread
+random pool (no device call)."""
+import json
+import subprocess
+
+from alens_gb300 import build
+
+YAML = """rngSeed: 99
+simBoxLow: [0.0, -1.0, 2.0]
+simBoxHigh: [40.0, 39.0, 2.5]
+simBoxPBC: [true, true, false]
+dt: 0.0001
+timeSnap: 0.01
+"""
+
+
+def _host_checks(tmp_path, text=YAML):
+    build.build_lib()
+    exe = build.build_facade_driver()
+    yml = tmp_path / "RunConfig.yaml"
+    yml.write_text(text)
+    proc = subprocess.run([str(exe), "--host-checks", str(yml)], capture_output=True, text=True, timeout=120)
+    assert proc.returncode == 0, proc.stderr
+    return json.loads(proc.stdout.strip().splitlines()[-1])
+
+
+def test_result_folders_and_snapshot_schedule(tmp_path):
+    r = _host_checks(tmp_path)
+    # 400 snapshots per folder: result0-399, result400-799, ...
+    assert r["folders"] == ["./result/result0-399/", "./result/result0-399/", "./result/result400-799/",
+                            "./result/result1200-1599/"]
+    assert r["snap_every"] == 100  # timeSnap / dt
+    assert r["due"] == [1, 0, 1, 0]  # steps 0, 1, 100, 301
+
+
+def test_domain_and_single_rank(tmp_path):
+    r = _host_checks(tmp_path)
+    assert r["low"] == [0.0, -1.0, 2.0] and r["high"] == [40.0, 39.0, 2.5]
+    assert r["pbc"] == [1, 1, 0] and r["len0"] == 40.0
+    assert r["rank"] == 0 and r["size"] == 1
+
+
+def test_random_pool_streams(tmp_path):
+    r = _host_checks(tmp_path)
+    # 200,000 draws: U(0,1) mean 1/2, variance 1/12, open interval; N(0,1)
+    assert abs(r["u_mean"] - 0.5) < 0.005 and abs(r["u_var"] - 1.0 / 12.0) < 0.002
+    assert 0.0 < r["u_min"] and r["u_max"] < 1.0
+    assert abs(r["n_mean"]) < 0.01 and abs(r["n_var"] - 1.0) < 0.02
+    # same seed, same streams; streams of different threads differ
+    assert r["again1_first"] == r["stream1_first"]
+    assert r["again0_first"] != r["again1_first"]
+    assert r["out_of_range"] == 1
+    other = _host_checks(tmp_path, YAML.replace("rngSeed: 99", "rngSeed: 100"))
+    assert other["again0_first"] != r["again0_first"]
+
+
+def test_time_step_info_restart_files(tmp_path):
+    from alens_gb300 import io
+    info = tmp_path / "TimeStepInfo.txt"
+    io.write_time_step_info(info, 1200, 12, 0.12)
+    snap = tmp_path / "SylinderAscii_12.dat"
+    snap.write_text("2\n0.12\nC 0 0.0125 0 0 0 1 0 0 0\nC 1 0.0125 0 1 0 1 1 0 0\n")
+    short = tmp_path / "short.txt"
+    short.write_text("1 2\n")
+    build.build_lib()
+    exe = build.build_facade_driver()
+    yml = tmp_path / "RunConfig.yaml"
+    yml.write_text(YAML)
+    proc = subprocess.run([str(exe), "--host-checks", str(yml), str(info), str(snap), str(short),
+                           str(tmp_path / "absent.txt")], capture_output=True, text=True, timeout=120)
+    assert proc.returncode == 0, proc.stderr
+    r = json.loads(proc.stdout.strip().splitlines()[-1])["restart"]
+    # the Python writer and the facade reader agree; snapshots and anything
+    # else are not taken for restart bookkeeping
+    assert r[0] == [1, 1200, 12, 0.12]
+    assert [x[0] for x in r[1:]] == [0, 0, 0]
+    assert io.read_time_step_info(info) == (1200, 12, 0.12)

@@ -45,6 +45,11 @@ def test_links_and_stationary_lines(tmp_path):
     assert list(rods.immovable) == [1, 0]
     assert np.allclose(rods.length, 20.0)
     assert np.allclose(rods.pos[1], [10.0, 0.5, 0.57])
+    # links survive a write and a read
+    q = tmp_path / "out.dat"
+    io.write_sylinder_ascii(str(q), rods, links=links)
+    back, back_links = io.read_sylinder_ascii(str(q))
+    assert back_links == [(0, 1)] and list(back.immovable) == [1, 0]
 
 
 def test_oracle_reproduces_golden():
