@@ -220,6 +220,7 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_bbpgd_solve_noalloc": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_int, vp,
                                                 C.POINTER(C.c_int), _PD, C.POINTER(C.c_int)]),
         "alens_get_step_count": (C.c_int, [vp, _PI64]),
+        "alens_set_step_count": (C.c_int, [vp, C.c_int64]),
         "alens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "alens_get_launch_count": (C.c_int, [vp, _PI64]),
         "alens_get_last_error": (C.c_char_p, [vp]),
@@ -456,6 +457,9 @@ class GpuSystem:
         c = C.c_int64()
         self._ck(self.lib.alens_get_step_count(self.h, C.byref(c)), "alens_get_step_count")
         return c.value
+
+    def set_step_count(self, count: int):
+        self._ck(self.lib.alens_set_step_count(self.h, int(count)), "alens_set_step_count")
 
     def launch_count(self) -> int:
         c = C.c_int64()

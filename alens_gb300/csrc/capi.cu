@@ -376,6 +376,14 @@ int alens_get_step_count(AlensCtx *ctx, int64_t *count) {
     return ALENS_OK;
 }
 
+int alens_set_step_count(AlensCtx *ctx, int64_t count) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->setStepCount((long long)count);
+        return (int)ALENS_OK;
+    });
+}
+
 const char *alens_get_last_error(AlensCtx *ctx) {
     if (!ctx) return "";
     return ctx->lastError.c_str();

@@ -1155,6 +1155,17 @@ int Engine::solve(AlensStepStats *out) {
     return status;
 }
 
+void Engine::setStepCount(long long s) {
+    if (s < 0) throw ApiError(ALENS_INVALID_ARG);
+    if (haveDetect_ || haveSolve_) throw ApiError(ALENS_NOT_READY);
+    stepCount_ = s;
+    if (dirty_ || !S_.ctl) return;  // finalize() writes it with the device state
+    CK(cudaStreamSynchronize(stream_));
+    hCtl_->step = s;
+    CK(cudaMemcpyAsync(&S_.ctl->step, &hCtl_->step, sizeof(long long), cudaMemcpyHostToDevice, stream_));
+    CK(cudaStreamSynchronize(stream_));
+}
+
 int Engine::advance(AlensStepStats *out) {
     if (!haveSolve_) throw ApiError(ALENS_NOT_READY);
     launches_ += enqueueAdvance();

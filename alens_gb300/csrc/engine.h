@@ -62,6 +62,9 @@ class Engine {
     // keeps the fastest; returns a JSON report.  The rods do not move.
     std::string autotune(int reps);
     long long stepCount() const { return stepCount_; }
+    // Index of the next step (it keys the Brownian noise); not while a
+    // staged step is pending
+    void setStepCount(long long s);
     cudaStream_t stream() const { return stream_; }
     long long lastNeeded() const { return lastNeeded_; }
     long long launches() const { return launches_; }

@@ -279,7 +279,6 @@ void SylinderSystem::create() {
     dinfo_ = DomainInfo::fromConfig(runConfig);
     rngPool_ = std::make_shared<RngPool>(runConfig.rngSeed, std::max(1, omp_get_max_threads()));
     snapID_ = 0;
-    stepOffset_ = 0;
     rodsStale_ = false;
     applyLinks();
     if (!runConfig.boundaries.empty())
@@ -341,7 +340,7 @@ void SylinderSystem::reinitialize(const std::string &configFile, const std::stri
     const std::string snapFile = getResultFolderWithID(snap) + "SylinderAscii_" + std::to_string(snap) + ".dat";
     initialize(configFile, snapFile, argc, argv);
     snapID_ = snap + 1;
-    stepOffset_ = step;
+    check(alens_set_step_count(ctx_, step), "alens_set_step_count");
 }
 
 void SylinderSystem::initialize(const SylinderConfig &cfg, const std::vector<Sylinder> &rods) {
@@ -423,7 +422,7 @@ const std::vector<Sylinder> &SylinderSystem::getContainer() {
 long SylinderSystem::getStepCount() const {
     int64_t c = 0;
     if (ctx_) alens_get_step_count(ctx_, &c);
-    return stepOffset_ + (long)c;
+    return (long)c;
 }
 
 bool SylinderSystem::readTimeStepInfo(const std::string &path, long *step, int *snapID, double *time) {

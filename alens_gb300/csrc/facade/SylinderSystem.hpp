@@ -133,9 +133,9 @@ class SylinderSystem {
     void initialize(const std::string &configFile, const std::string &posFile, int argc = 0,
                     char **argv = nullptr);
     // Restart from TimeStepInfo.txt written by writeResult() (the rods come
-    // from that snapshot's SylinderAscii file, getSnapID() is its ID + 1 and
-    // getStepCount() continues from its step), or directly from a
-    // SylinderAscii snapshot file.
+    // from that snapshot's SylinderAscii file, getSnapID() is its ID + 1, and
+    // the step count, which keys the Brownian noise, continues from its
+    // step), or directly from a SylinderAscii snapshot file.
     void reinitialize(const std::string &configFile, const std::string &restartFile, int argc = 0,
                       char **argv = nullptr, bool eulerStep = false);
     void initialize(const SylinderConfig &cfg, const std::vector<Sylinder> &rods);
@@ -199,7 +199,6 @@ class SylinderSystem {
     std::array<double, 3> polar_{};
     std::array<double, 9> nematic_{};
     int snapID_ = 0;
-    long stepOffset_ = 0;  // step of the snapshot a restart began from
     bool timerOn_ = false;
     double lastStepMs_ = 0.0;
     DomainInfo dinfo_;

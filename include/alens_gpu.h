@@ -376,6 +376,14 @@ int alens_get_features(AlensCtx *ctx, int replica, int cap, float *features, flo
 /* Steps executed so far (SylinderSystem::getStepCount). */
 int alens_get_step_count(AlensCtx *ctx, int64_t *count);
 
+/* Set the step count, i.e. the index of the next step, for a restart
+ * (SylinderSystem::reinitialize from TimeStepInfo.txt, SRC/TubuleSystem.cpp:38).
+ * The step index keys the Brownian noise, so a context restarted at step s
+ * draws the noise an uninterrupted run draws from step s on.  count >= 0
+ * (else ALENS_INVALID_ARG); not between alens_detect and alens_advance
+ * (ALENS_NOT_READY). */
+int alens_set_step_count(AlensCtx *ctx, int64_t count);
+
 /* The CUDA stream of the context (cudaStream_t), for event timing. */
 int alens_get_stream(AlensCtx *ctx, void **stream);
 

@@ -536,3 +536,46 @@ def test_autotune_mixed_ensemble(gpu_lib):
         assert st["converged"] == 1
         for r in range(len(reps)):
             assert fp64_residual(g, r) <= cfgs[r].conResTol * 1.0001
+
+
+def test_restart_step_count_continues_noise(gpu_lib):
+    """A context restarted from the rods after step 3 with the step count set
+    to 3 reproduces steps 3 and 4 of an uninterrupted run bit for bit (the
+    step keys the Brownian noise), whether the count is set before the
+    device state exists or after a step."""
+    w = workloads.small_periodic(n=1000, box=5.0, seed=0)
+    cfg = workloads.config_with(w.cfg, warmStart=capi.WARM_ZERO)
+    a = capi.GpuSystem(cfg)
+    a.set_rods(w.rods)
+    for _ in range(3):
+        a.step()
+    p3, q3 = a.get_rods()
+    for _ in range(2):
+        a.step()
+    p5, q5 = a.get_rods()
+    r3 = w.rods.copy()
+    r3.pos, r3.quat = p3.copy(), q3.copy()
+    b = capi.GpuSystem(cfg)
+    b.set_rods(r3)
+    b.set_step_count(3)
+    c = capi.GpuSystem(cfg)
+    c.set_rods(w.rods)
+    c.step()
+    c.update_rods(p3, q3)
+    c.set_step_count(3)
+    for s in (b, c):
+        s.step()
+        s.step()
+        assert s.step_count() == 5
+        pb, qb = s.get_rods()
+        assert np.array_equal(pb, p5) and np.array_equal(qb, q5)
+    d = capi.GpuSystem(cfg)
+    d.set_rods(r3)
+    d.step()
+    d.step()
+    assert not np.array_equal(d.get_rods()[0], p5)
+    with pytest.raises(capi.AlensError):
+        b.set_step_count(-1)
+    b.detect()
+    with pytest.raises(capi.AlensError):
+        b.set_step_count(7)  # a staged step is pending
