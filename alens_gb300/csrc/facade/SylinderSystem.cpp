@@ -12,6 +12,7 @@
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
+#include <type_traits>
 #include <unordered_map>
 
 namespace gpu {
@@ -459,11 +460,122 @@ void SylinderSystem::writeResult() {
     std::filesystem::create_directories(folder, ec);
     if (ec) throw std::runtime_error("cannot create " + folder + ": " + ec.message());
     writeResult(folder + "SylinderAscii_" + std::to_string(snapID_) + ".dat");
+    writeSylinderVTK(folder, snapID_, getContainer());
     std::FILE *f = std::fopen("TimeStepInfo.txt", "w");
     if (!f) throw std::runtime_error("cannot write TimeStepInfo.txt");
     std::fprintf(f, "%ld\n%d\n%.17g\n", getStepCount(), snapID_, runConfig.dt * (double)getStepCount());
     std::fclose(f);
     snapID_++;
+}
+
+namespace {
+
+// RFC 4648 base64 with padding
+std::string base64(const std::vector<unsigned char> &in) {
+    static const char kAlphabet[] = "ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789+/";
+    std::string out;
+    out.reserve((in.size() + 2) / 3 * 4);
+    size_t i = 0;
+    for (; i + 2 < in.size(); i += 3) {
+        const unsigned v = (unsigned)in[i] << 16 | (unsigned)in[i + 1] << 8 | in[i + 2];
+        out += kAlphabet[v >> 18 & 63];
+        out += kAlphabet[v >> 12 & 63];
+        out += kAlphabet[v >> 6 & 63];
+        out += kAlphabet[v & 63];
+    }
+    if (i + 1 == in.size()) {
+        const unsigned v = (unsigned)in[i] << 16;
+        out += kAlphabet[v >> 18 & 63];
+        out += kAlphabet[v >> 12 & 63];
+        out += "==";
+    } else if (i + 2 == in.size()) {
+        const unsigned v = (unsigned)in[i] << 16 | (unsigned)in[i + 1] << 8;
+        out += kAlphabet[v >> 18 & 63];
+        out += kAlphabet[v >> 12 & 63];
+        out += kAlphabet[v >> 6 & 63];
+        out += '=';
+    }
+    return out;
+}
+
+// little-endian bytes of an integer or IEEE double, independent of the host order
+template <class T>
+void putLE(std::vector<unsigned char> &b, T v) {
+    uint64_t u = 0;
+    if constexpr (std::is_same<T, double>::value) {
+        std::memcpy(&u, &v, 8);
+    } else {
+        u = (uint64_t)(int64_t)v;
+    }
+    for (size_t k = 0; k < sizeof(T); k++) b.push_back((unsigned char)(u >> (8 * k) & 0xff));
+}
+
+template <class T>
+std::string dataArray(const char *name, const char *vtkType, int ncomp, const std::vector<T> &vals) {
+    std::vector<unsigned char> bytes;
+    bytes.reserve(8 + sizeof(T) * vals.size());
+    putLE<uint64_t>(bytes, (uint64_t)(sizeof(T) * vals.size()));
+    for (const T &v : vals) putLE<T>(bytes, v);
+    return std::string("<DataArray type=\"") + vtkType + "\" Name=\"" + name + "\" NumberOfComponents=\"" +
+           std::to_string(ncomp) + "\" format=\"binary\">" + base64(bytes) + "</DataArray>\n";
+}
+
+}  // namespace
+
+void SylinderSystem::writeSylinderVTK(const std::string &folder, int snapID, const std::vector<Sylinder> &rods) {
+    const size_t n = rods.size();
+    std::vector<double> pts(6 * n), radius(n), length(n), dir(3 * n);
+    std::vector<int64_t> gid(n);
+    std::vector<int32_t> conn(2 * n), offs(n), group(n), imm(n);
+    for (size_t i = 0; i < n; i++) {
+        const Sylinder &r = rods[i];
+        double d[3];
+        directionFromQuat(r.orientation, d);
+        const double h = 0.5 * r.length;
+        for (int k = 0; k < 3; k++) {
+            pts[6 * i + k] = r.pos[k] - h * d[k];
+            pts[6 * i + 3 + k] = r.pos[k] + h * d[k];
+            dir[3 * i + k] = d[k];
+        }
+        conn[2 * i] = (int32_t)(2 * i);
+        conn[2 * i + 1] = (int32_t)(2 * i + 1);
+        offs[i] = (int32_t)(2 * i + 2);
+        gid[i] = r.gid;
+        radius[i] = r.radius;
+        length[i] = r.length;
+        group[i] = r.group;
+        imm[i] = r.isImmovable ? 1 : 0;
+    }
+    const std::string sep = (folder.empty() || folder.back() == '/') ? "" : "/";
+    const std::string piece = "Sylinder_r0_" + std::to_string(snapID) + ".vtp";
+    const char *head = "<?xml version=\"1.0\"?>\n";
+    {
+        std::ofstream f(folder + sep + piece, std::ios::binary);
+        if (!f) throw std::runtime_error("cannot write " + folder + sep + piece);
+        f << head << "<VTKFile type=\"PolyData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+          << "<PolyData>\n<Piece NumberOfPoints=\"" << 2 * n << "\" NumberOfVerts=\"0\" NumberOfLines=\"" << n
+          << "\" NumberOfStrips=\"0\" NumberOfPolys=\"0\">\n"
+          << "<Points>\n" << dataArray("position", "Float64", 3, pts) << "</Points>\n"
+          << "<Lines>\n" << dataArray("connectivity", "Int32", 1, conn) << dataArray("offsets", "Int32", 1, offs)
+          << "</Lines>\n<CellData Scalars=\"scalars\">\n"
+          << dataArray("gid", "Int64", 1, gid) << dataArray("radius", "Float64", 1, radius)
+          << dataArray("length", "Float64", 1, length) << dataArray("group", "Int32", 1, group)
+          << dataArray("isImmovable", "Int32", 1, imm) << dataArray("direction", "Float64", 3, dir)
+          << "</CellData>\n</Piece>\n</PolyData>\n</VTKFile>\n";
+    }
+    std::ofstream f(folder + sep + "Sylinder_" + std::to_string(snapID) + ".pvtp", std::ios::binary);
+    if (!f) throw std::runtime_error("cannot write the index of " + piece);
+    f << head << "<VTKFile type=\"PPolyData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+      << "<PPolyData GhostLevel=\"0\">\n<PPoints>\n"
+      << "<PDataArray type=\"Float64\" Name=\"position\" NumberOfComponents=\"3\"/>\n</PPoints>\n"
+      << "<PCellData Scalars=\"scalars\">\n"
+      << "<PDataArray type=\"Int64\" Name=\"gid\" NumberOfComponents=\"1\"/>\n"
+      << "<PDataArray type=\"Float64\" Name=\"radius\" NumberOfComponents=\"1\"/>\n"
+      << "<PDataArray type=\"Float64\" Name=\"length\" NumberOfComponents=\"1\"/>\n"
+      << "<PDataArray type=\"Int32\" Name=\"group\" NumberOfComponents=\"1\"/>\n"
+      << "<PDataArray type=\"Int32\" Name=\"isImmovable\" NumberOfComponents=\"1\"/>\n"
+      << "<PDataArray type=\"Float64\" Name=\"direction\" NumberOfComponents=\"3\"/>\n"
+      << "</PCellData>\n<Piece Source=\"" << piece << "\"/>\n</PPolyData>\n</VTKFile>\n";
 }
 
 DomainInfo DomainInfo::fromConfig(const SylinderConfig &cfg) {

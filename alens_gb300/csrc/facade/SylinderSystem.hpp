@@ -147,7 +147,8 @@ class SylinderSystem {
     void calcOrderParameter();    // polar and nematic order of the rod axes
     void writeResult(const std::string &path) const;  // SylinderAscii text (rods, then link lines)
     // When a snapshot is due at the current step: SylinderAscii_<snapID>.dat
-    // in the current result folder (created) and ./TimeStepInfo.txt (step,
+    // and Sylinder_<snapID>.pvtp (+ piece) in the current result folder
+    // (created) and ./TimeStepInfo.txt (step,
     // snapID and time, one per line; its presence is what makes aLENS
     // restart, SRC/main.cpp:28-37), then snapID + 1.  Called where the
     // reference calls writeResult() (SRC/TubuleSystem.cpp:100); its runStep
@@ -175,6 +176,12 @@ class SylinderSystem {
     std::string getCurrentResultFolder() const { return getResultFolderWithID(snapID_); }
     static std::string getResultFolderWithID(int snapID);
     static bool snapshotDue(long step, double timeSnap, double dt);
+    // Sylinder_<snapID>.pvtp and its one piece Sylinder_r0_<snapID>.vtp in
+    // `folder` (the aLENS snapshot pair, README.md:140-148): two points per
+    // rod (minus end, plus end) joined by a line cell; cell data gid, radius,
+    // length, group, isImmovable, direction; inline binary arrays (base64 of
+    // a UInt64 byte count and the little-endian values).
+    static void writeSylinderVTK(const std::string &folder, int snapID, const std::vector<Sylinder> &rods);
     // TimeStepInfo.txt: exactly three numbers (step, snapID, time); false
     // for anything else (a SylinderAscii snapshot, say)
     static bool readTimeStepInfo(const std::string &path, long *step, int *snapID, double *time);

@@ -14,6 +14,9 @@
 // (result folders, snapshot schedule, domain, communicator, random pool)
 // and, per restart file, [is TimeStepInfo, step, snapID, time].
 //
+// usage: facade_driver --write-vtk TubuleInitial.dat folder snapID
+// Reads the rods and writes Sylinder_<snapID>.pvtp and its piece (no device).
+//
 // usage: facade_driver --restart-check RunConfig.yaml TubuleInitial.dat steps
 // Steps a system, calling writeResult() before each runStep (where the
 // reference's runStep writes its snapshot), then restarts a second system
@@ -141,6 +144,18 @@ int restartCheck(const char *yaml, const char *dat, int steps) {
 
 int main(int argc, char **argv) {
     if (argc >= 3 && std::strcmp(argv[1], "--host-checks") == 0) return hostChecks(argv[2], argc - 3, argv + 3);
+    if (argc == 5 && std::strcmp(argv[1], "--write-vtk") == 0) {
+        try {
+            std::string err;
+            const auto rods = gpu::readSylinderAscii(argv[2], nullptr, &err);
+            if (rods.empty() && !err.empty()) throw std::runtime_error(err);
+            gpu::SylinderSystem::writeSylinderVTK(argv[3], std::atoi(argv[4]), rods);
+            return 0;
+        } catch (const std::exception &e) {
+            std::fprintf(stderr, "facade_driver: %s\n", e.what());
+            return 1;
+        }
+    }
     if (argc == 5 && std::strcmp(argv[1], "--restart-check") == 0) {
         try {
             return restartCheck(argv[2], argv[3], std::atoi(argv[4]));

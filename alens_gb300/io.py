@@ -199,6 +199,99 @@ def write_vtp(path, rods: RodState, gamma_sum=None):
         f.write("</CellData>\n</Piece>\n</PolyData>\n</VTKFile>\n")
 
 
+# --------------------------------------------------------------- snapshots
+# aLENS result layout (docs/source/visualization.md:13,32; README.md:135-148):
+# snapshots grouped 400 to a folder (result/result0-399/, result400-799/, ...),
+# each snapshot a SylinderAscii_<id>.dat text file and a parallel VTK index
+# Sylinder_<id>.pvtp naming one serial piece per rank, Sylinder_r<rank>_<id>.vtp
+# (here one rank).  Data arrays are inline binary: base64 of a UInt64 byte
+# count followed by the little-endian values.  The C++ facade writes the same
+# bytes (gpu::SylinderSystem::writeSylinderVTK).
+
+SNAPSHOTS_PER_FOLDER = 400
+
+# cell data of a rod piece: (name, VTK type, numpy dtype, components)
+_ROD_CELL_FIELDS = [("gid", "Int64", "<i8", 1), ("radius", "Float64", "<f8", 1), ("length", "Float64", "<f8", 1),
+                    ("group", "Int32", "<i4", 1), ("isImmovable", "Int32", "<i4", 1),
+                    ("direction", "Float64", "<f8", 3)]
+
+
+def result_folder(snap_id: int, root: str = "./result") -> str:
+    lo = snap_id // SNAPSHOTS_PER_FOLDER * SNAPSHOTS_PER_FOLDER
+    return f"{root}/result{lo}-{lo + SNAPSHOTS_PER_FOLDER - 1}/"
+
+
+def _b64_array(name, vtk_type, values, ncomp):
+    import base64
+    import struct
+    raw = np.ascontiguousarray(values).tobytes()
+    body = base64.b64encode(struct.pack("<Q", len(raw)) + raw).decode("ascii")
+    return (f'<DataArray type="{vtk_type}" Name="{name}" NumberOfComponents="{ncomp}" format="binary">'
+            f"{body}</DataArray>\n")
+
+
+def write_sylinder_pvtp(folder, snap_id: int, rods: RodState, group=None):
+    """Sylinder_<id>.pvtp and its piece Sylinder_r0_<id>.vtp in `folder`: two
+    points per rod (minus end, plus end) joined by a line cell; cell data gid,
+    radius, length, group, isImmovable and the unit direction."""
+    import os
+    n = rods.n
+    a = quat_to_axis(rods.quat)
+    h = 0.5 * rods.length[:, None]
+    pts = np.empty((2 * n, 3))
+    pts[0::2] = rods.pos - h * a
+    pts[1::2] = rods.pos + h * a
+    imm = rods.immovable if rods.immovable is not None else np.zeros(n, np.int32)
+    grp = np.full(n, -1, np.int32) if group is None else np.asarray(group)
+    cells = {"gid": rods.gid, "radius": rods.radius, "length": rods.length, "group": grp, "isImmovable": imm,
+             "direction": a}
+    piece = f"Sylinder_r0_{snap_id}.vtp"
+    head = '<?xml version="1.0"?>\n'
+    with open(os.path.join(folder, piece), "w") as f:
+        f.write(head + '<VTKFile type="PolyData" version="1.0" byte_order="LittleEndian" header_type="UInt64">\n')
+        f.write(f'<PolyData>\n<Piece NumberOfPoints="{2 * n}" NumberOfVerts="0" NumberOfLines="{n}" '
+                'NumberOfStrips="0" NumberOfPolys="0">\n')
+        f.write("<Points>\n" + _b64_array("position", "Float64", pts.astype("<f8"), 3) + "</Points>\n")
+        f.write("<Lines>\n" + _b64_array("connectivity", "Int32", np.arange(2 * n, dtype="<i4"), 1)
+                + _b64_array("offsets", "Int32", 2 * np.arange(1, n + 1, dtype="<i4"), 1) + "</Lines>\n")
+        f.write('<CellData Scalars="scalars">\n')
+        for name, vt, dt, nc in _ROD_CELL_FIELDS:
+            f.write(_b64_array(name, vt, np.asarray(cells[name]).astype(dt), nc))
+        f.write("</CellData>\n</Piece>\n</PolyData>\n</VTKFile>\n")
+    with open(os.path.join(folder, f"Sylinder_{snap_id}.pvtp"), "w") as f:
+        f.write(head + '<VTKFile type="PPolyData" version="1.0" byte_order="LittleEndian" header_type="UInt64">\n')
+        f.write('<PPolyData GhostLevel="0">\n<PPoints>\n'
+                '<PDataArray type="Float64" Name="position" NumberOfComponents="3"/>\n</PPoints>\n')
+        f.write('<PCellData Scalars="scalars">\n')
+        for name, vt, _, nc in _ROD_CELL_FIELDS:
+            f.write(f'<PDataArray type="{vt}" Name="{name}" NumberOfComponents="{nc}"/>\n')
+        f.write(f'</PCellData>\n<Piece Source="{piece}"/>\n</PPolyData>\n</VTKFile>\n')
+
+
+def write_snapshot(snap_id: int, rods: RodState, step: int, time: float, root: str = "./result", links=(),
+                   group=None, info_path: str = "TimeStepInfo.txt") -> str:
+    """One aLENS snapshot: SylinderAscii_<id>.dat and Sylinder_<id>.pvtp (+ piece)
+    in result_folder(snap_id, root), then the restart bookkeeping file.
+    Returns the folder."""
+    import os
+    folder = result_folder(snap_id, root)
+    os.makedirs(folder, exist_ok=True)
+    write_sylinder_ascii(os.path.join(folder, f"SylinderAscii_{snap_id}.dat"), rods, time=time, group=group,
+                         links=links)
+    write_sylinder_pvtp(folder, snap_id, rods, group=group)
+    write_time_step_info(info_path, step, snap_id, time)
+    return folder
+
+
+def read_vtk_binary_array(text: str, dtype):
+    """Values of one inline binary DataArray body (UInt64 byte-count header)."""
+    import base64
+    import struct
+    raw = base64.b64decode(text.strip())
+    nbytes = struct.unpack("<Q", raw[:8])[0]
+    return np.frombuffer(raw[8:8 + nbytes], dtype=dtype)
+
+
 def write_time_step_info(path, step: int, snap_id: int, time: float):
     """Restart bookkeeping next to a snapshot (the role of TimeStepInfo.txt,
     whose presence makes aLENS restart, SRC/main.cpp:28-37)."""

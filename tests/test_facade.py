@@ -145,7 +145,8 @@ def test_flexible_filament_links(gpu_lib, tmp_path):
 
 def test_facade_snapshot_and_restart(gpu_lib, tmp_path):
     """writeResult() before every runStep writes SylinderAscii_<snapID>.dat
-    into ./result/result0-399/ every round(timeSnap/dt) steps plus
+    and Sylinder_<snapID>.pvtp (+ piece) into ./result/result0-399/ every
+    round(timeSnap/dt) steps plus
     ./TimeStepInfo.txt; reinitialize from TimeStepInfo.txt restores the last
     snapshot's rods, its snapID + 1 and its step."""
     exe = build.build_facade_driver()
@@ -162,5 +163,9 @@ def test_facade_snapshot_and_restart(gpu_lib, tmp_path):
     assert r["restart_snap_id"] == 3 and r["restart_step"] == 4
     assert r["same_count"] == 1 and r["max_dpos"] < 1e-12 and r["max_daxis"] < 1e-12
     folder = tmp_path / "result" / "result0-399"
-    assert sorted(p.name for p in folder.iterdir()) == [f"SylinderAscii_{i}.dat" for i in range(3)]
+    names = sorted(p.name for p in folder.iterdir())
+    assert [x for x in names if x.startswith("SylinderAscii_")] == [f"SylinderAscii_{i}.dat" for i in range(3)]
+    assert [x for x in names if x.endswith(".pvtp")] == [f"Sylinder_{i}.pvtp" for i in range(3)]
+    assert [x for x in names if x.endswith(".vtp")] == [f"Sylinder_r0_{i}.vtp" for i in range(3)]
+    assert len(names) == 9
     assert (tmp_path / "TimeStepInfo.txt").read_text().split()[:2] == ["4", "2"]

@@ -76,3 +76,23 @@ def test_time_step_info_restart_files(tmp_path):
     assert r[0] == [1, 1200, 12, 0.12]
     assert [x[0] for x in r[1:]] == [0, 0, 0]
     assert io.read_time_step_info(info) == (1200, 12, 0.12)
+
+
+def test_facade_vtk_writer_matches_python(tmp_path):
+    """The facade's Sylinder_<id>.pvtp / Sylinder_r0_<id>.vtp writer and the
+    Python one produce the same bytes for the same rods (both read from the
+    same TubuleInitial.dat by bit-identical readers)."""
+    import os
+    from alens_gb300 import io
+    dat = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "monolayer_window.dat")
+    build.build_lib()
+    exe = build.build_facade_driver()
+    cpp, py = tmp_path / "cpp", tmp_path / "py"
+    cpp.mkdir()
+    py.mkdir()
+    proc = subprocess.run([str(exe), "--write-vtk", dat, str(cpp), "7"], capture_output=True, text=True, timeout=120)
+    assert proc.returncode == 0, proc.stderr
+    rods, _ = io.read_sylinder_ascii(dat)
+    io.write_sylinder_pvtp(str(py), 7, rods)
+    for name in ("Sylinder_7.pvtp", "Sylinder_r0_7.vtp"):
+        assert (cpp / name).read_bytes() == (py / name).read_bytes(), name

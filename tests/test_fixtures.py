@@ -13,7 +13,7 @@ sys.path.insert(0, GOLDEN)
 
 import make_fixtures  # noqa: E402
 
-from alens_gb300 import io  # noqa: E402
+from alens_gb300 import io, workloads  # noqa: E402
 
 
 def test_fixture_files_parse():
@@ -80,3 +80,48 @@ def test_vtp_and_restart_info(tmp_path):
     assert names == ["gid", "length", "radius", "force"]
     io.write_time_step_info(str(tmp_path / "TimeStepInfo.txt"), 1200, 12, 0.12)
     assert io.read_time_step_info(str(tmp_path / "TimeStepInfo.txt")) == (1200, 12, 0.12)
+
+
+def test_sylinder_pvtp_snapshot(tmp_path):
+    """aLENS snapshot layout: result/result0-399/ holds SylinderAscii_<id>.dat
+    and Sylinder_<id>.pvtp indexing Sylinder_r0_<id>.vtp; the binary arrays
+    decode to the rods' end points, gids and geometry."""
+    import re
+    import xml.etree.ElementTree as ET
+    _, rods = make_fixtures.load_fixture()
+    info = tmp_path / "TimeStepInfo.txt"
+    folder = io.write_snapshot(12, rods, step=1200, time=0.012, root=str(tmp_path / "result"),
+                               links=[(0, 1)], info_path=str(info))
+    assert folder == str(tmp_path / "result") + "/result0-399/"
+    assert io.result_folder(400) == "./result/result400-799/"
+    assert io.read_time_step_info(info) == (1200, 12, 0.012)
+    back, links = io.read_sylinder_ascii(folder + "SylinderAscii_12.dat")
+    assert links == [(0, 1)] and back.n == rods.n
+    index = ET.parse(folder + "Sylinder_12.pvtp").getroot()
+    assert index.get("type") == "PPolyData"
+    pieces = [p.get("Source") for p in index.iter("Piece")]
+    assert pieces == ["Sylinder_r0_12.vtp"]
+    # the frame number the aLENS .pvd collector takes from the index name
+    assert int(re.search(r"_([^_.]+)(?:\.[^_]*)?$", "Sylinder_12.pvtp").group(1)) == 12
+    declared = [(a.get("Name"), a.get("type")) for a in index.iter("PDataArray")]
+    root = ET.parse(folder + pieces[0]).getroot()
+    piece = root.find("PolyData/Piece")
+    assert int(piece.get("NumberOfPoints")) == 2 * rods.n and int(piece.get("NumberOfLines")) == rods.n
+    arrays = {a.get("Name"): a for a in root.iter("DataArray")}
+    assert [(n, arrays[n].get("type")) for n, _ in declared] == declared
+    types = {"Float64": "<f8", "Int64": "<i8", "Int32": "<i4"}
+
+    def values(name):
+        a = arrays[name]
+        return io.read_vtk_binary_array(a.text, types[a.get("type")])
+
+    pts = values("position").reshape(-1, 2, 3)
+    axis = workloads.quat_to_axis(rods.quat)
+    h = 0.5 * rods.length[:, None]
+    assert np.array_equal(pts[:, 0], rods.pos - h * axis) and np.array_equal(pts[:, 1], rods.pos + h * axis)
+    assert np.array_equal(values("connectivity"), np.arange(2 * rods.n))
+    assert np.array_equal(values("offsets"), 2 * np.arange(1, rods.n + 1))
+    assert np.array_equal(values("gid"), rods.gid)
+    assert np.array_equal(values("length"), rods.length) and np.array_equal(values("radius"), rods.radius)
+    assert np.array_equal(values("direction").reshape(-1, 3), axis)
+    assert np.all(values("group") == -1)
