@@ -291,6 +291,68 @@ def test_collision_stress_is_pair_virial():
     assert np.linalg.eigvalsh(0.5 * (got + got.T)).min() >= -1e-12 * np.abs(ref).max()
 
 
+def test_collision_geometry_independent():
+    """Every collision row of the oracle recomputed in numpy with the
+    package's own clamped closest-point routine (a different formulation of
+    the segment distance): the separation phi0 = |P - Q| - rcol_I - rcol_J,
+    the normal (P - Q)/|P - Q| and the pair's periodic image."""
+    w = workloads.small_periodic(n=1000, box=5.0, seed=0)
+    s = O.OracleSystem(w.cfg)
+    s.set_rods(w.rods)
+    s.detect()
+    con = s.constraints()
+    nc = con["ncoll"]
+    assert nc > 100
+    i, j, img = con["i"][:nc], con["j"][:nc], con["image"][:nc]
+    box = np.array([w.cfg.simBoxHigh[d] - w.cfg.simBoxLow[d] for d in range(3)])
+    shift = np.stack([img // 9 - 1, (img // 3) % 3 - 1, img % 3 - 1], axis=1) * box
+    a = workloads.quat_to_axis(w.rods.quat)
+    hI, hJ = 0.5 * w.rods.length[i], 0.5 * w.rods.length[j]
+    cI, cJ = w.rods.pos[i], w.rods.pos[j] + shift
+    sp, tp = workloads.segment_closest_params(cI, a[i], hI, cJ, a[j], hJ)
+    P = cI + sp[:, None] * a[i]
+    Q = cJ + tp[:, None] * a[j]
+    dist = np.linalg.norm(P - Q, axis=1)
+    sep = dist - w.rods.radius[i] - w.rods.radius[j]
+    assert np.max(np.abs(sep - con["delta0"][:nc])) <= 1e-12
+    assert np.all(sep < w.cfg.sylinderColBuf)
+    n = (P - Q) / dist[:, None]
+    assert np.max(np.abs(n - con["jac"][:nc, :3])) <= 1e-9
+    assert np.array_equal(con["jac"][:nc, 6:9], -con["jac"][:nc, :3])
+
+
+def test_pair_set_complete_brute_force():
+    """The oracle's collision set equals a brute-force scan of all rod pairs
+    (minimum image; the 5 um box is wider than twice the cutoff, so one image
+    per pair) with the numpy closest-point routine: nothing missed, nothing
+    extra, and no pair within rounding distance of the cutoff."""
+    w = workloads.small_periodic(n=1000, box=5.0, seed=0)
+    s = O.OracleSystem(w.cfg)
+    s.set_rods(w.rods)
+    s.detect()
+    con = s.constraints()
+    nc = con["ncoll"]
+    rods = w.rods
+    I, J = np.triu_indices(rods.n, 1)
+    d = rods.pos[J] - rods.pos[I]
+    shift = -np.round(d / 5.0) * 5.0
+    reach = (0.5 * (rods.length[I] + rods.length[J]) + rods.radius[I] + rods.radius[J]
+             + w.cfg.sylinderColBuf)
+    keep = np.linalg.norm(d + shift, axis=1) < reach
+    I, J, shift = I[keep], J[keep], shift[keep]
+    a = workloads.quat_to_axis(rods.quat)
+    cI, cJ = rods.pos[I], rods.pos[J] + shift
+    sp, tp = workloads.segment_closest_params(cI, a[I], 0.5 * rods.length[I], cJ, a[J], 0.5 * rods.length[J])
+    sep = (np.linalg.norm(cI + sp[:, None] * a[I] - cJ - tp[:, None] * a[J], axis=1)
+           - rods.radius[I] - rods.radius[J])
+    hit = sep < w.cfg.sylinderColBuf
+    assert np.min(np.abs(sep - w.cfg.sylinderColBuf)) > 1e-9
+    brute = set(zip(I[hit].tolist(), J[hit].tolist()))
+    found = {(min(x, y), max(x, y)) for x, y in zip(con["i"][:nc].tolist(), con["j"][:nc].tolist())}
+    assert len(found) == nc > 100
+    assert found == brute
+
+
 def test_step_translation_invariance():
     w = workloads.small_periodic(n=300, box=2.5, seed=4, kbt=-1.0)
     a = O.OracleSystem(w.cfg)
