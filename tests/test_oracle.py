@@ -422,6 +422,37 @@ def test_delassus_operator_independent():
     assert np.abs(diag - (np.diag(ref) + comp)).max() <= 1e-12 * np.abs(ref).max()
 
 
+def test_crosslink_blocks_independent():
+    """Crosslinker blocks built from the rod state, recomputed in numpy:
+    anchors c + s a on both rods, separation reduced to the minimum image,
+    phi0 = |d| - rest, normal d/|d| at I and -d/|d| at J, torque arms
+    (s a) x n; every link row follows the collision rows."""
+    w = workloads.small_periodic(n=400, box=2.6, seed=11)
+    links = workloads.make_links(w.cfg, w.rods, workloads.pair_list(O.OracleSystem, w.cfg, w.rods, 0.05), 60,
+                                 seed=2, kappa=100.0)
+    s = O.OracleSystem(w.cfg)
+    s.set_rods(w.rods)
+    s.set_links(links)
+    s.detect()
+    con = s.constraints()
+    nc = con["ncoll"]
+    a = workloads.quat_to_axis(w.rods.quat)
+    i, j = links["i"], links["j"]
+    rI = links["si"][:, None] * a[i]
+    rJ = links["sj"][:, None] * a[j]
+    d = (w.rods.pos[i] + rI) - (w.rods.pos[j] + rJ)
+    d -= 2.6 * np.round(d / 2.6)
+    ln = np.linalg.norm(d, axis=1)
+    n = d / ln[:, None]
+    rows = slice(nc, nc + len(i))
+    assert np.array_equal(con["i"][rows], i) and np.array_equal(con["j"][rows], j)
+    assert np.abs(con["delta0"][rows] - (ln - links["rest"])).max() <= 1e-12
+    jac = con["jac"][rows]
+    assert np.abs(jac[:, 0:3] - n).max() <= 1e-12 and np.abs(jac[:, 6:9] + n).max() <= 1e-12
+    assert np.abs(jac[:, 3:6] - np.cross(rI, n)).max() <= 1e-12
+    assert np.abs(jac[:, 9:12] - np.cross(rJ, -n)).max() <= 1e-12
+
+
 def test_step_translation_invariance():
     w = workloads.small_periodic(n=300, box=2.5, seed=4, kbt=-1.0)
     a = O.OracleSystem(w.cfg)
