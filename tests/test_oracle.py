@@ -453,6 +453,41 @@ def test_crosslink_blocks_independent():
     assert np.abs(jac[:, 9:12] - np.cross(rJ, -n)).max() <= 1e-12
 
 
+def test_pair_set_complete_headline_layer():
+    """The 20,000-rod quasi-2D layer (periodic in x and y, free in z): the
+    oracle's ~59,000 collisions equal a KD-tree scan of all rod pairs within
+    the largest reach, decided with the numpy closest-point routine."""
+    spatial = pytest.importorskip("scipy.spatial")
+    w = workloads.dense_monolayer()
+    s = O.OracleSystem(w.cfg)
+    s.set_rods(w.rods)
+    s.detect()
+    con = s.constraints()
+    nc = con["ncoll"]
+    rods = w.rods
+    L = np.array([w.cfg.simBoxHigh[d] - w.cfg.simBoxLow[d] for d in range(3)])
+    pbc = np.array([bool(w.cfg.simBoxPBC[d]) for d in range(3)])
+    box = np.where(pbc, L, 1e6)
+    pos = rods.pos + np.array([0.0, 0.0, 1000.0])  # free axis: far from the tree's wrap
+    tree = spatial.cKDTree(np.mod(pos, box), boxsize=box)
+    reach = rods.length.max() + 2 * rods.radius.max() + w.cfg.sylinderColBuf
+    pairs = tree.query_pairs(reach, output_type="ndarray")
+    I, J = pairs[:, 0], pairs[:, 1]
+    d = rods.pos[J] - rods.pos[I]
+    shift = np.where(pbc, -np.round(d / L) * L, 0.0)
+    a = workloads.quat_to_axis(rods.quat)
+    cI, cJ = rods.pos[I], rods.pos[J] + shift
+    sp, tp = workloads.segment_closest_params(cI, a[I], 0.5 * rods.length[I], cJ, a[J], 0.5 * rods.length[J])
+    sep = (np.linalg.norm(cI + sp[:, None] * a[I] - cJ - tp[:, None] * a[J], axis=1)
+           - rods.radius[I] - rods.radius[J])
+    hit = sep < w.cfg.sylinderColBuf
+    assert np.min(np.abs(sep - w.cfg.sylinderColBuf)) > 1e-9
+    brute = set(zip(np.minimum(I, J)[hit].tolist(), np.maximum(I, J)[hit].tolist()))
+    found = {(min(x, y), max(x, y)) for x, y in zip(con["i"][:nc].tolist(), con["j"][:nc].tolist())}
+    assert len(found) == nc > 50000
+    assert found == brute
+
+
 def test_step_translation_invariance():
     w = workloads.small_periodic(n=300, box=2.5, seed=4, kbt=-1.0)
     a = O.OracleSystem(w.cfg)
