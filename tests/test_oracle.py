@@ -595,3 +595,27 @@ def test_library_exports_header_symbols():
         assert hasattr(lib, n), n
     lib.alens_status_str.restype = ctypes.c_char_p
     assert lib.alens_status_str(4) == b"constraint capacity exceeded"
+
+
+def test_monolayer_motion_stays_in_plane():
+    """monolayer: true (Examples/DenseMonoLayer/RunConfig.yaml:8) on the
+    window fixture: three steps with collisions move rods in x and y only,
+    with no out-of-plane velocity and rotation about z only, so in-plane
+    axes stay in plane."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_fixtures
+    cfg, rods = make_fixtures.load_fixture()
+    assert cfg.monolayer
+    s = O.OracleSystem(cfg)
+    s.set_rods(rods)
+    for _ in range(3):
+        st = s.step(allow_not_converged=False)
+    assert st["nCollision"] > 1000
+    pos, quat = s.get_rods()
+    vel, omega = s.get_velocity()
+    assert np.array_equal(pos[:, 2], rods.pos[:, 2])
+    assert np.abs(pos[:, :2] - rods.pos[:, :2]).max() > 1e-4
+    assert np.all(vel[:, 2] == 0.0) and np.all(omega[:, :2] == 0.0)
+    assert np.abs(workloads.quat_to_axis(quat)[:, 2]).max() <= 1e-14
