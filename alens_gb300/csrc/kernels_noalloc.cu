@@ -1,11 +1,11 @@
 // kernels_noalloc.cu - BBPGD solve that allocates nothing.
 //
 // Some callers of this library cannot call cudaMalloc at the point where
-// they solve: a caller that records its time step into a CUDA graph
-// (allocation is not a stream operation and synchronises the device), or a
-// caller whose GPU memory is owned by a pool or budget it must not disturb
-// (for instance a host code that hands the constraint problem of a step to
-// the GPU from inside its own time loop).  For them this file provides
+// they solve.  Two kinds are common: a host code whose GPU memory is all
+// owned by another allocator (a framework's caching pool that has reserved
+// the device, or a fixed memory budget that must not be disturbed), and a
+// time loop that must not stall the device, since cudaMalloc and cudaFree
+// may synchronise it.  For them this file provides
 // alens_bbpgd_solve_noalloc: the FP64 BBPGD of the library over an operator
 // the caller already holds in device memory (CSR rows), with every scratch
 // buffer in one file-scope __device__ array of fixed size.
@@ -18,6 +18,10 @@
 // Limits and sharing:
 //  * at most kNoAllocMaxConstraints rows (65,536); larger problems are
 //    rejected with ALENS_INVALID_ARG;
+//  * column indices must lie in [0, n) and rowPtr[0] must be 0; an entry
+//    whose column lies outside is skipped and the call returns
+//    ALENS_INVALID_ARG (the array holds the state of 65,536 rows, so an
+//    unchecked column could read another call's leftovers or past its end);
 //  * the scratch array (about 2.1 MB) lives on every GPU that loads the
 //    library until the process exits;
 //  * every call uses the same array and leaves its contents behind; each
@@ -25,8 +29,11 @@
 //    are independent, but calls that overlap on the GPU (other streams or
 //    threads at the same time) race on it;
 //  * the first call on a device resolves the array's device address
-//    (cudaGetSymbolAddress) and the solver's launch size; make that first
-//    call before any stream capture.
+//    (cudaGetSymbolAddress) and the solver's launch size and keeps them for
+//    the life of the process; cudaDeviceReset after that first call is not
+//    supported;
+//  * before returning, a call waits for its stream and copies the
+//    iteration count, status, residual and error flags into host memory.
 //
 // Compiled with --fmad=false (the FP64 arithmetic matches the oracle).
 #include <mutex>
@@ -39,6 +46,7 @@ namespace {
 
 constexpr int kNoAllocMaxConstraints = 65536;
 constexpr int kNoAllocMaxTiles = kNoAllocMaxConstraints / kTile;
+constexpr int kErrBadColumn = 1 << 8;  // a column index outside [0, n) was skipped
 
 struct NoAllocScratch {
     double2 st[2][kNoAllocMaxConstraints];     // (gamma, g) by pass parity
@@ -118,7 +126,7 @@ __global__ void k_noalloc_setup(NoAllocScratch *sc, PlainOperator op, const doub
 }
 
 // Row update over plain CSR: the operations of row_update<double>.
-__device__ __forceinline__ void row_update_plain(const PlainOperator &op, int k, int mode, double alpha,
+__device__ __forceinline__ void row_update_plain(const PlainOperator &op, int n, int k, int mode, double alpha,
                                                  const double2 *stIn, double2 *stOut, double &v0, double &v1,
                                                  double &v2, double &rmax, int *errFlags) {
     if (mode == kModeCopy) {
@@ -140,23 +148,28 @@ __device__ __forceinline__ void row_update_plain(const PlainOperator &op, int k,
     for (int eb = e0; eb < e1; eb += kRowPrefetch) {
         int cols[kRowPrefetch];
         double vals[kRowPrefetch];
+        bool use[kRowPrefetch];
 #pragma unroll
         for (int j = 0; j < kRowPrefetch; j++) {
             cols[j] = eb + j < e1 ? __ldg(op.cols + eb + j) : k;
             vals[j] = eb + j < e1 ? __ldg(op.vals + eb + j) : 0.0;
+            // a column outside [0, n) is flagged and skipped, never read
+            const bool inRange = cols[j] >= 0 && cols[j] < n;
+            if (eb + j < e1 && !inRange) atomicOr(errFlags, kErrBadColumn);
+            use[j] = eb + j < e1 && inRange;
         }
         double2 sv[kRowPrefetch];
         double lbs[kRowPrefetch];
 #pragma unroll
         for (int j = 0; j < kRowPrefetch; j++) {
-            if (eb + j < e1) {
+            if (use[j]) {
                 sv[j] = ldcg(stIn + cols[j]);
                 lbs[j] = __ldg(op.lb + cols[j]);
             }
         }
 #pragma unroll
         for (int j = 0; j < kRowPrefetch; j++) {
-            if (eb + j < e1) {
+            if (use[j]) {
                 double xl;
                 if (mode == kModeG0)
                     xl = sv[j].x;
@@ -228,7 +241,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_noalloc_solve(DevState S, Sol
                 double v0 = 0.0, v1 = 0.0, v2 = 0.0;
                 double rmax = mode == kModeCopy ? -1.0 : 0.0;
                 if (local < nCon)
-                    row_update_plain(op, local, mode, alpha, stIn, stOut, v0, v1, v2, rmax, &S.ctl->errFlags);
+                    row_update_plain(op, nCon, local, mode, alpha, stIn, stOut, v0, v1, v2, rmax, &S.ctl->errFlags);
                 double w0 = 0.0, w1 = 0.0, w2 = 0.0;
                 if (mode == kModeAG || mode == kModeIter) {
                     w0 = warp_tree_sum_t<double>(v0);
@@ -374,6 +387,7 @@ extern "C" int alens_bbpgd_solve_noalloc(int n, const int32_t *rowPtr, const int
     if (residual) *residual = hostRes;
     if (solveStatus) *solveStatus = hostStatus;
     if (hostErr & kErrTimeout) return ALENS_TIMEOUT;
+    if (hostErr & kErrBadColumn) return ALENS_INVALID_ARG;
     if (hostErr & kErrNaN) return ALENS_NAN_DETECTED;
     return hostStatus;
 }

@@ -285,22 +285,26 @@ int alens_get_operator(AlensCtx *ctx, int replica, int capNnz, int *nnz, int32_t
 int alens_get_con_stress(AlensCtx *ctx, int replica, double *stress9);
 
 /* BBPGD solve that allocates no memory, for callers that cannot call
- * cudaMalloc where they solve (a step recorded into a CUDA graph, or GPU
- * memory held by a pool or budget the caller must not disturb).  No
- * counterpart in the reference: SimToolbox's solver allocates its Tpetra
- * vectors per solve.
+ * cudaMalloc where they solve: a host code whose GPU memory is all owned by
+ * another allocator (a framework's caching pool, a fixed budget), or a time
+ * loop that must not stall the device (cudaMalloc/cudaFree may synchronise
+ * it).  No counterpart in the reference: SimToolbox's solver allocates its
+ * Tpetra vectors per solve.
  * Solves min 1/2 x^T (A + diag(cinv)) x + q^T x, x >= lowerBound (-inf for
  * bilateral rows) with the library's FP64 BBPGD, starting from gamma0; all
  * array arguments are DEVICE pointers to the caller's memory: A as CSR
- * (rowPtr[n+1], cols, vals; the layout alens_get_operator returns), q, cinv,
- * lowerBound, gamma0 and the output gamma (n each).  iterations, residual
- * and solveStatus (nullable) are host pointers.  stream may be NULL.
+ * (rowPtr[n+1] with rowPtr[0] = 0, cols with every column in [0, n), vals;
+ * the layout alens_get_operator returns), q, cinv, lowerBound, gamma0 and
+ * the output gamma (n each).  An entry with a column outside [0, n) is
+ * skipped and the call returns ALENS_INVALID_ARG.  iterations, residual and
+ * solveStatus (nullable) are host pointers; before returning, the call
+ * waits for `stream` (NULL: the default stream) and copies them there.
  * Scratch lives in one fixed __device__ array of about 2.1 MB per GPU that
  * loads the library: n is limited to 65,536 rows (larger: ALENS_INVALID_ARG).
- * The first call on a device looks up the array's address; make it before
- * any stream capture.  Calls share the array: calls that overlap on the GPU
- * race.  Returns the solve's status (ALENS_OK or ALENS_NOT_CONVERGED) or an
- * error. */
+ * The first call on a device looks up the array's address and keeps it for
+ * the life of the process (cudaDeviceReset afterwards is not supported).
+ * Calls share the array: calls that overlap on the GPU race.  Returns the
+ * solve's status (ALENS_OK or ALENS_NOT_CONVERGED) or an error. */
 int alens_bbpgd_solve_noalloc(int n, const int32_t *rowPtr, const int32_t *cols,
                               const double *vals, const double *q,
                               const double *cinv, const double *lowerBound,

@@ -8,7 +8,7 @@ physical settings (Examples/DenseMonoLayer/RunConfig.yaml) on a closed
 (non-periodic) 4 x 4 window.  Golden outputs: five oracle steps with one
 bilateral spring between the first two rods (the facade driver's protocol).
 
-usage: python tests/golden/make_fixtures.py [/path/to/aLENS]
+usage: python tests/golden/make_fixtures.py /path/to/aLENS
 """
 import json
 import os
@@ -110,7 +110,9 @@ def golden(steps=5):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_fixtures.py /path/to/aLENS")
+    ref = sys.argv[1]
     n = write_fixture(ref)
     g = golden()
     with open(os.path.join(HERE, "monolayer_window_golden.json"), "w") as f:
