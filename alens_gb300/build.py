@@ -36,7 +36,7 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # FP64 path that must match the oracle bit for bit: they are compiled without
 # FMA contraction.
 CU_SOURCES = ["engine.cu", "kernels_detect.cu", "kernels_assemble.cu", "kernels_solve.cu",
-              "kernels_mixed.cu", "kernels_csm.cu", "kernels_mlp.cu", "mlp.cu", "kernels_noalloc.cu", "capi.cu"]
+              "kernels_mixed.cu", "kernels_fast.cu", "kernels_csm.cu", "kernels_mlp.cu", "mlp.cu", "kernels_noalloc.cu", "capi.cu"]
 CXX_SOURCES: list[str] = []
 FP_STRICT = {"kernels_detect.cu", "kernels_assemble.cu", "kernels_solve.cu", "kernels_noalloc.cu",
              "engine.cu", "capi.cu"}

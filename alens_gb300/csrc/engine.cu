@@ -76,9 +76,15 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     if (const char *e = std::getenv("ALENS_CSM_THREADS")) csm_set_threads(atoi(e));
     if (const char *e = std::getenv("ALENS_SOLVER_FORM")) {
         const std::string f(e);
-        formRequest_ = f == "grid" ? kFormGrid : (f == "cluster" ? kFormCluster : (f == "resident" ? kFormResident : -1));
+        formRequest_ = f == "grid"       ? kFormGrid
+                       : f == "cluster"  ? kFormCluster
+                       : f == "resident" ? kFormResident
+                       : f == "fast"     ? kFormFast
+                                         : -1;
     }
     CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&side2_, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&orderJoin_, cudaEventDisableTiming));
     for (int i = 0; i < 3; i++) {
         CK(cudaEventCreateWithFlags(&forkEv_[i], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&joinEv_[i], cudaEventDisableTiming));
@@ -115,6 +121,8 @@ Engine::~Engine() {
         if (joinEv_[i]) cudaEventDestroy(joinEv_[i]);
     }
     if (side_) cudaStreamDestroy(side_);
+    if (side2_) cudaStreamDestroy(side2_);
+    if (orderJoin_) cudaEventDestroy(orderJoin_);
     if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -277,6 +285,8 @@ void Engine::finalize() {
     S.scanTmp = alloc<int>(fixedAllocs_, 4096);
     S.prevCount = alloc<int>(fixedAllocs_, 1);
     S.linkSlot0 = alloc<int>(fixedAllocs_, R_);
+    S.fastPart = alloc<double>(fixedAllocs_, 2 * 8 * (size_t)kFastMaxGrid);
+    S.fastScanTmp = alloc<int>(fixedAllocs_, 4096);
     linksDirty_ = true;
     bndDirty_ = true;
     CK(cudaMemcpyAsync(S.par, hostPar_.data(), sizeof(RepParams) * R_, cudaMemcpyHostToDevice, stream_));
@@ -311,6 +321,29 @@ void Engine::finalize() {
     S.rowPtr = alloc<int>(G, N + 1);
     S.rowCursor = alloc<int>(G, N);
     S.cellCount = alloc<int>(G, C);
+    if (R_ == 1 && precision_ == ALENS_PREC_MIXED) {
+        // cells in Morton (bit-interleaved) order of their grid coordinates,
+        // for the single-system solver's spatial row order
+        const RepParams &P0 = hostPar_[0];
+        std::vector<std::pair<unsigned long long, int>> code((size_t)C);
+        for (int c = 0; c < C; c++) {
+            const int cx = c % P0.ncell[0], cy = (c / P0.ncell[0]) % P0.ncell[1], cz = c / (P0.ncell[0] * P0.ncell[1]);
+            unsigned long long m = 0;
+            for (int bit = 0; bit < 21; bit++) {
+                m |= (unsigned long long)((cx >> bit) & 1) << (3 * bit);
+                m |= (unsigned long long)((cy >> bit) & 1) << (3 * bit + 1);
+                m |= (unsigned long long)((cz >> bit) & 1) << (3 * bit + 2);
+            }
+            code[(size_t)c] = {m, c};
+        }
+        std::sort(code.begin(), code.end());
+        std::vector<int> byRank((size_t)C);
+        for (int r = 0; r < C; r++) byRank[(size_t)r] = code[(size_t)r].second;
+        S.cellByRank = alloc<int>(G, C);
+        S.fastCellCnt = alloc<int>(G, C + 1);
+        S.fastCellBase = alloc<int>(G, C + 1);
+        CK(cudaMemcpy(S.cellByRank, byRank.data(), sizeof(int) * (size_t)C, cudaMemcpyHostToDevice));
+    }
     S.cellStart = alloc<int>(G, C + 1);
     S.cellCursor = alloc<int>(G, C);
     CK(cudaMemsetAsync(S.vel, 0, sizeof(double) * 6 * (size_t)N, stream_));
@@ -402,6 +435,10 @@ void Engine::allocConstraints(int cap, bool keepPrev) {
         S.qc32 = alloc<float2>(G, cap);
         S.st32[0] = alloc<float2>(G, cap);
         S.st32[1] = alloc<float2>(G, cap);
+        if (R_ == 1) {
+            S.fastPerm = alloc<int>(G, cap);
+            S.fastInv = alloc<int>(G, cap);
+        }
     }
     S.part = alloc<double>(G, 9 * (size_t)S.tileCap);
     S.work = alloc<double>(G, (size_t)kMaxSolverGrid * 3 * S.workCap);
@@ -640,6 +677,7 @@ void Engine::uploadBlocks() {
 int Engine::enqueueDetect() {
     DevState &S = S_;
     int n = 0;
+    ensureSolverGrid();
     launch_step_clear(S, stream_);  // rawCount, errFlags and the per-cell / per-rod counters
     launch_prep(S, stream_);
     // branch 0: the Brownian velocities beside the binning and pair search
@@ -665,6 +703,16 @@ int Engine::enqueueDetect() {
     CK(cudaEventRecord(forkEv_[2], stream_));
     CK(cudaStreamWaitEvent(side_, forkEv_[2], 0));
     launch_ranges(S, side_);
+    // the single-system solver's spatial row order on a third branch, beside
+    // the pair sort, constraint build and operator assembly (computed
+    // whenever that form may run, so that the autotuner can try it on the
+    // detected problem)
+    const bool order = S.fastPerm && !fastFailed_;
+    if (order) {
+        CK(cudaStreamWaitEvent(side2_, forkEv_[2], 0));
+        n += launch_fast_order(S, side2_);
+        CK(cudaEventRecord(orderJoin_, side2_));
+    }
     CK(cudaEventRecord(joinEv_[0], side_));
     n += launch_pair_sort(S, stream_);
     CK(cudaStreamWaitEvent(stream_, joinEv_[0], 0));
@@ -684,6 +732,7 @@ int Engine::enqueueDetect() {
         launch_mlp_features(S, stream_);
         n += 1;
     }
+    if (order) CK(cudaStreamWaitEvent(stream_, orderJoin_, 0));
     CK(cudaGetLastError());
     return n;
 }
@@ -697,7 +746,13 @@ void Engine::applySolverConfig(int form, int clusterSize, int threads, int block
     solverGrid_ = std::min(solver_max_grid(precision_), numSM_ * solverBlocksPerSM_);
     if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "solver occupancy");
     solverForm_ = form;
-    clusterSize_ = form == kFormGrid ? 0 : clusterSize;
+    clusterSize_ = (form == kFormGrid || form == kFormFast) ? 0 : clusterSize;
+    if (form == kFormFast) {
+        solverGrid_ = fast_solver_grid();
+        if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "fast solver occupancy");
+        nClusters_ = 1;
+        return;
+    }
     if (form == kFormResident) {
         csm_set_threads(threads);
         nClusters_ = R_;
@@ -745,6 +800,9 @@ std::string Engine::autotune(int reps) {
     // blocks make the per-pass barrier and the redundant reductions cheaper)
     for (int bps : {1, 2})
         for (int mt : {1, 2, 4, 8}) cands.push_back({kFormGrid, 0, 256, bps, mt, 0.0, false});
+    if (precision_ == ALENS_PREC_MIXED && R_ == 1 && S_.fastPerm && !fastFailed_ && fast_solver_grid() > 0 &&
+        nc <= fast_solver_capacity())
+        cands.push_back({kFormFast, 0, 256, 1, 1, 0.0, false});
     if (precision_ == ALENS_PREC_MIXED) {
         const int maxCs = cluster_max_size();
         for (int cs : {16, 8, 4, 2})
@@ -802,7 +860,7 @@ std::string Engine::autotune(int reps) {
     // repeatable: noise is keyed by the step index)
     haveDetect_ = true;
     haveSolve_ = false;
-    static const char *names[] = {"grid", "cluster", "resident"};
+    static const char *names[] = {"grid", "cluster", "resident", "fast"};
     std::string js = "{\"constraints\": " + std::to_string(nc) + ", \"candidates\": [";
     for (size_t i = 0; i < cands.size(); i++) {
         const Cand &c = cands[i];
@@ -883,6 +941,17 @@ void Engine::ensureSolverGrid() {
     if (solverGrid_ < 1) throw CudaFailure(cudaErrorLaunchOutOfResources, "solver occupancy");
     solverForm_ = kFormGrid;
     if (precision_ != ALENS_PREC_MIXED) return;
+    // one system: the single-system form unless another form was requested
+    if (R_ == 1 && (formRequest_ < 0 || formRequest_ == kFormFast) && clusterSize_ <= 0 && !fastFailed_ &&
+        S_.fastPerm) {
+        const int fg = fast_solver_grid();
+        if (fg > 0) {
+            solverForm_ = kFormFast;
+            solverGrid_ = fg;
+            clusterSize_ = 0;
+            return;
+        }
+    }
     // FP32 solver form.  Measured on GB300 (20,000-rod layer, ~21,000
     // constraints): grid 9.6 us per pass, cluster-resident 14 us (random
     // 8-byte distributed-shared-memory gathers sustain ~0.4 loads per cycle
@@ -1009,7 +1078,10 @@ bool Engine::handleSolverFit() {
     if (!(hCtl_->errFlags & kErrSolverFit)) return false;
     CK(cudaStreamSynchronize(stream_));
     invalidateGraph();
-    residentFailed_ = true;
+    if (solverForm_ == kFormFast)
+        fastFailed_ = true;
+    else
+        residentFailed_ = true;
     solverGrid_ = 0;
     clusterSize_ = -1;
     return true;

@@ -173,6 +173,13 @@ struct DevState {
     double *work;   // per block 9 x workCap
     int *tileRep;   // tileCap
     double *stress; // 9 x R outputs
+    // single-system solver (kernels_fast.cu): per-block records (2 parities
+    // x kFastMaxGrid blocks x 64 bytes), the spatial row permutation and its
+    // inverse (constraint capacity), constraints per cell in Morton order and
+    // their exclusive scan (nCells + 1 each), scan scratch, and the cells in
+    // Morton order (fixed per context)
+    double *fastPart;
+    int *fastPerm, *fastInv, *fastCellCnt, *fastCellBase, *fastScanTmp, *cellByRank;
     // scan scratch
     int *scanTmp;
 };
@@ -199,12 +206,15 @@ void launch_pack_rods(const DevState &S, int rodOffset, int n, int what, cudaStr
 
 // ---- solve / advance (kernels_solve.cu)
 constexpr int kMaxSolverGrid = 152 * 8;  // work space is sized for this
+constexpr int kFastMaxGrid = 256;        // blocks of the single-system solver (one per SM)
 int solver_max_grid(int precision);  // cooperative residency limit
 // Forms of the FP32 (mixed-precision) solver
 enum SolverForm {
     kFormGrid = 0,      // cooperative grid over all SMs, software grid barrier
     kFormCluster = 1,   // one cluster per replica, iterates in global memory
-    kFormResident = 2   // one cluster per replica, problem held in shared memory
+    kFormResident = 2,  // one cluster per replica, problem held in shared memory
+    kFormFast = 3       // one system: spatial row order, per-block records, FP64 check and refinement
+                        // in the same launch (kernels_fast.cu)
 };
 // precision == MIXED: FP32 kernel, state reset, FP64 refinement kernel
 // (events ev[0..3] recorded around the two kernels when non-null).
@@ -216,6 +226,9 @@ int cluster_max_active(int cs);    // co-resident clusters of that size
 int csm_cluster_size(int *maxActive);  // cluster-resident form: largest cluster, 0 if unusable
 void csm_set_threads(int threads);     // cluster-resident form: threads per CTA (256/512/1024)
 int csm_threads();
+int fast_solver_grid();            // single-system form: blocks (one per SM), 0 if unusable
+long long fast_solver_capacity();  // single-system form: constraints it holds
+int launch_fast_order(const DevState &S, cudaStream_t st);  // its row order (side stream); kernels launched
 void launch_advance(const DevState &S, cudaStream_t st);
 void launch_stress(const DevState &S, cudaStream_t st);
 

@@ -109,6 +109,8 @@ class Engine {
     int device_ = 0, numSM_ = 0;
     cudaStream_t stream_ = nullptr;
     cudaStream_t side_ = nullptr;  // concurrent branch of the detect stage
+    cudaStream_t side2_ = nullptr; // the single-system solver's row order, beside the assembly
+    cudaEvent_t orderJoin_ = nullptr;
     cudaEvent_t forkEv_[3] = {nullptr, nullptr, nullptr}, joinEv_[3] = {nullptr, nullptr, nullptr};
     bool ownStream_ = false;
     int precision_ = 0, warm_ = 0;
@@ -121,6 +123,7 @@ class Engine {
     int solverForm_ = -1;    // SolverForm of the FP32 solver (-1: not chosen yet)
     int formRequest_ = -1;   // ALENS_SOLVER_FORM override (-1 automatic)
     bool residentFailed_ = false;  // a step did not fit the cluster-resident form
+    bool fastFailed_ = false;      // a step did not fit the single-system form
     int prevCountHost_ = 0;  // valid warm-start keys on the device
     int solverGrid_ = 0;
     MlpModel *mlp_ = nullptr;

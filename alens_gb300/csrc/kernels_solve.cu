@@ -312,6 +312,8 @@ cudaError_t launch_solve_fp32_cluster(const DevState &S, int clusterSize, int nC
 int solver_max_grid_fp32();
 // defined in kernels_csm.cu
 cudaError_t launch_solve_fp32_csm(const DevState &S, int clusterSize, int nClusters, cudaStream_t st);
+// defined in kernels_fast.cu
+cudaError_t launch_solve_fast(const DevState &S, int grid, unsigned long long timeout_ns, cudaStream_t st);
 
 int solver_max_grid(int precision) {
     int g = occupancy_grid((const void *)k_solve<double>);
@@ -337,7 +339,16 @@ cudaError_t launch_solve(const DevState &S, int grid, int precision, unsigned lo
     V.alphaBuf = S.alphaBuf;
     V.fp64 = 1;
     if (ev) cudaEventRecord(ev[0], st);
-    if (precision == ALENS_PREC_MIXED) {
+    if (precision == ALENS_PREC_MIXED && form == kFormFast) {
+        // FP32 iterations, FP64 check and refinement in one launch
+        e = launch_solve_fast(S, grid, timeout_ns, st);
+        n++;
+        if (ev) {
+            cudaEventRecord(ev[1], st);
+            cudaEventRecord(ev[2], st);
+            cudaEventRecord(ev[3], st);
+        }
+    } else if (precision == ALENS_PREC_MIXED) {
         if (form == kFormResident)
             e = launch_solve_fp32_csm(S, clusterSize, nClusters, st);
         else if (form == kFormCluster)

@@ -389,7 +389,7 @@ def fp64_residual(system, replica=0):
     return float(np.max(np.abs(x - np.maximum(op["lb"], x - g)))) if n else 0.0
 
 
-@pytest.mark.parametrize("form", ["grid", "cluster", "resident"])
+@pytest.mark.parametrize("form", ["grid", "cluster", "resident", "fast"])
 def test_mixed_forms_match_fp64(gpu_lib, monkeypatch, form):
     """Every form of the FP32-bulk solver reaches the FP64 tolerance and
     stays close to the FP64 solution of the same step (relative L2 of the
