@@ -225,6 +225,10 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_launch_count": (C.c_int, [vp, _PI64]),
         "alens_get_last_error": (C.c_char_p, [vp]),
         "alens_get_stage_times": (C.c_int, [vp, _PD]),
+        "alens_step_batched": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(AlensStepStats)]),
+        "alens_get_gamma": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_int), _PI32, _PD]),
+        "alens_get_pairs": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_int), _PI32, _PI32, _PI32]),
+        "alens_set_wait_limit": (C.c_int, [vp, C.c_uint64, C.c_int]),
         "alens_mlp_create": (C.c_int, [C.c_uint64, C.c_int64, C.POINTER(vp)]),
         "alens_mlp_destroy": (C.c_int, [vp]),
         "alens_mlp_get_params": (C.c_int, [vp, _PF]),

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "engine.h"
 
@@ -214,6 +215,86 @@ int alens_get_constraints(AlensCtx *ctx, int replica, int cap, int32_t *indexI, 
         ctx->eng->getConstraints(replica, cap, indexI, indexJ, image, delta0, gamma, jac);
         return (int)ALENS_OK;
     });
+}
+
+int alens_get_gamma(AlensCtx *ctx, int replica, int cap, int *n, int32_t *pairs, double *gamma) {
+    if (!ctx || !n) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        int nc = 0, nb = 0;
+        ctx->eng->numConstraints(replica, &nc, &nb);
+        *n = nc + nb;
+        if (cap < nc + nb) return (int)ALENS_CAPACITY;
+        std::vector<int32_t> ii((size_t)(nc + nb)), jj((size_t)(nc + nb));
+        ctx->eng->getConstraints(replica, nc + nb, ii.data(), jj.data(), nullptr, nullptr, gamma, nullptr);
+        if (pairs)
+            for (int k = 0; k < nc + nb; k++) {
+                pairs[2 * k] = ii[(size_t)k];
+                pairs[2 * k + 1] = jj[(size_t)k];
+            }
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_pairs(AlensCtx *ctx, int replica, int cap, int *n, int32_t *indexI, int32_t *indexJ,
+                    int32_t *image) {
+    if (!ctx || !n) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        int nc = 0, nb = 0;
+        ctx->eng->numConstraints(replica, &nc, &nb);
+        *n = nc;
+        if (cap < nc) return (int)ALENS_CAPACITY;
+        std::vector<int32_t> ii((size_t)(nc + nb)), jj((size_t)(nc + nb)), im((size_t)(nc + nb));
+        ctx->eng->getConstraints(replica, nc + nb, ii.data(), jj.data(), im.data(), nullptr, nullptr, nullptr);
+        for (int k = 0; k < nc; k++) {
+            if (indexI) indexI[k] = ii[(size_t)k];
+            if (indexJ) indexJ[k] = jj[(size_t)k];
+            if (image) image[k] = im[(size_t)k];
+        }
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_set_wait_limit(AlensCtx *ctx, uint64_t timeoutNs, int stallBarriers) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->setWaitLimit((unsigned long long)timeoutNs, stallBarriers);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_step_batched(AlensCtx **ctxs, int n, AlensStepStats *stats) {
+    if (n < 0 || (n > 0 && !ctxs)) return ALENS_INVALID_ARG;
+    for (int i = 0; i < n; i++)
+        if (!ctxs[i]) return ALENS_INVALID_ARG;
+    std::vector<int> rc((size_t)n, ALENS_OK);
+    std::vector<int> direct((size_t)n, 0), started((size_t)n, 0);
+    // enqueue every context's step first ...
+    for (int i = 0; i < n; i++) {
+        AlensCtx *c = ctxs[i];
+        rc[(size_t)i] = guarded_ctx(c, [&] {
+            c->eng->finalizeForStep();
+            direct[(size_t)i] = c->eng->stepLaunch() ? 1 : 0;
+            started[(size_t)i] = 1;
+            return (int)ALENS_OK;
+        });
+    }
+    // ... then read them back; a step that must be repeated runs alone
+    for (int i = 0; i < n; i++) {
+        if (!started[(size_t)i]) continue;
+        AlensCtx *c = ctxs[i];
+        AlensStepStats *out = stats ? stats + i : nullptr;
+        rc[(size_t)i] = guarded_ctx(c, [&] {
+            const int r = c->eng->stepFinish(out, direct[(size_t)i] != 0);
+            return r == alens::Engine::kStepRetry ? c->eng->step(out) : r;
+        });
+    }
+    int worst = ALENS_OK;
+    for (int i = 0; i < n; i++) {
+        const int r = rc[(size_t)i];
+        if (r != ALENS_OK && r != ALENS_NOT_CONVERGED) return r;
+        if (r == ALENS_NOT_CONVERGED) worst = r;
+    }
+    return worst;
 }
 
 int alens_get_con_stress(AlensCtx *ctx, int replica, double *stress9) {

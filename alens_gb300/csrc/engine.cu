@@ -276,6 +276,7 @@ void Engine::finalize() {
     S.warm = warm_;
     S.precision = precision_;
     S.solveMinTiles = solverMinTiles_;
+    S.barrierExtra = stallBarriers_;
     // fixed-size control
     S.par = alloc<RepParams>(fixedAllocs_, R_);
     S.dyn = alloc<RepDyn>(fixedAllocs_, R_);
@@ -993,7 +994,7 @@ void Engine::ensureSolverGrid() {
 int Engine::enqueueSolve(cudaEvent_t *ev, bool finish) {
     ensureSolverGrid();
     int n = 0;
-    CK(launch_solve(S_, solverGrid_, precision_, kBarrierTimeoutNs, stream_, ev, &n, solverForm_,
+    CK(launch_solve(S_, solverGrid_, precision_, waitTimeoutNs_, stream_, ev, &n, solverForm_,
                     clusterSize_ > 0 ? clusterSize_ : 0, nClusters_, finish));
     return n;
 }
@@ -1146,53 +1147,78 @@ void Engine::recordStageTimes() {
     for (int i = 0; i < 5; i++) stageMs_[i] = t[i];
 }
 
+// Enqueues one attempt of a full step (graph replay or direct launches);
+// returns whether the direct-launch path ran (stage timing).
+bool Engine::stepLaunch() {
+    uploadBlocks();
+    bool launched = false;
+    if (useGraph_ && !stageTiming_) {
+        if (!graphExec_ && !graphFailed_) {
+            if (!buildGraph()) graphFailed_ = true;
+        }
+        if (graphExec_) {
+            CK(cudaGraphLaunch(graphExec_, stream_));
+            launches_ += graphLaunches_;
+            launched = true;
+        }
+    }
+    if (!launched) {
+        if (stageTiming_) {
+            ensureEvents();
+            CK(cudaEventRecord(events_[0], stream_));
+            launches_ += enqueueDetect();
+            // solve records events 1..4 (start, main end, refine start, refine end)
+            launches_ += enqueueSolve(&events_[1]);
+            launches_ += enqueueAdvance();
+            CK(cudaEventRecord(events_[5], stream_));
+        } else {
+            launches_ += enqueueDetect();
+            launches_ += enqueueSolve(nullptr);
+            launches_ += enqueueAdvance();
+        }
+    }
+    return !launched;
+}
+
+// Reads back the attempt's results.  Returns kStepRetry when the buffers
+// were regrown or the solver form changed (the step is repeatable and must
+// be run again), else the step's status.
+int Engine::stepFinish(AlensStepStats *out, bool direct) {
+    readBack();
+    if (handleOverflow()) return kStepRetry;
+    if (handleSolverFit()) return kStepRetry;
+    if (stageTiming_ && direct) recordStageTimes();
+    const int status = collectStats(2);
+    if (status == ALENS_OK || status == ALENS_NOT_CONVERGED) {
+        for (auto &q : queue_) q.clear();
+        captured_ = S_.feat != nullptr;
+        stepCount_++;
+        last_.step = stepCount_ - 1;
+        prevCountHost_ = hCtl_->totalColl;
+    }
+    haveDetect_ = haveSolve_ = false;
+    if (out) *out = last_;
+    return status;
+}
+
 int Engine::step(AlensStepStats *out) {
     finalize();
     for (int attempt = 0; attempt < 8; attempt++) {
-        uploadBlocks();
-        bool launched = false;
-        if (useGraph_ && !stageTiming_) {
-            if (!graphExec_ && !graphFailed_) {
-                if (!buildGraph()) graphFailed_ = true;
-            }
-            if (graphExec_) {
-                CK(cudaGraphLaunch(graphExec_, stream_));
-                launches_ += graphLaunches_;
-                launched = true;
-            }
-        }
-        if (!launched) {
-            if (stageTiming_) {
-                ensureEvents();
-                CK(cudaEventRecord(events_[0], stream_));
-                launches_ += enqueueDetect();
-                // solve records events 1..4 (start, main end, refine start, refine end)
-                launches_ += enqueueSolve(&events_[1]);
-                launches_ += enqueueAdvance();
-                CK(cudaEventRecord(events_[5], stream_));
-            } else {
-                launches_ += enqueueDetect();
-                launches_ += enqueueSolve(nullptr);
-                launches_ += enqueueAdvance();
-            }
-        }
-        readBack();
-        if (handleOverflow()) continue;
-        if (handleSolverFit()) continue;
-        if (stageTiming_ && !launched) recordStageTimes();
-        const int status = collectStats(2);
-        if (status == ALENS_OK || status == ALENS_NOT_CONVERGED) {
-            for (auto &q : queue_) q.clear();
-            captured_ = S_.feat != nullptr;
-            stepCount_++;
-            last_.step = stepCount_ - 1;
-            prevCountHost_ = hCtl_->totalColl;
-        }
-        haveDetect_ = haveSolve_ = false;
-        if (out) *out = last_;
-        return status;
+        const bool direct = stepLaunch();
+        const int rc = stepFinish(out, direct);
+        if (rc != kStepRetry) return rc;
     }
     throw ApiError(ALENS_CAPACITY);
+}
+
+void Engine::setWaitLimit(unsigned long long timeoutNs, int stallBarriers) {
+    if (stallBarriers != 0 && stallBarriers != 1) throw ApiError(ALENS_INVALID_ARG);
+    if (haveDetect_ || haveSolve_) throw ApiError(ALENS_NOT_READY);
+    CK(cudaStreamSynchronize(stream_));
+    invalidateGraph();
+    waitTimeoutNs_ = timeoutNs ? timeoutNs : kBarrierTimeoutNs;
+    stallBarriers_ = stallBarriers;
+    S_.barrierExtra = stallBarriers_;
 }
 
 int Engine::detect(AlensStepStats *out) {

@@ -112,6 +112,8 @@ struct DevState {
     int R, nRods, cap, nCells, tileCap, workCap, blockCap, nnzCap;
     int warm, precision;
     int solveMinTiles;         // BBPGD: at least this many 64-row tiles per solver block
+    int barrierExtra;          // solver grid barriers wait for this many blocks more than launched
+                               // (0; 1 only to test the bounded-wait path: every wait runs out)
     int pairW[3];              // pair search: stencil width per dimension (max over replicas;
                                // 1 where every replica has one closed cell)
     RepParams *par;

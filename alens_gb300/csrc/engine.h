@@ -41,6 +41,16 @@ class Engine {
                   const double *rest, const double *kappa);
     void setBoundaries(int rep, int n, const AlensBoundary *b);
     int step(AlensStepStats *out);
+    // the two halves of a step attempt, for stepping several contexts
+    // together (alens_step_batched): stepLaunch enqueues, stepFinish reads
+    // back and returns kStepRetry when the attempt must be repeated
+    static constexpr int kStepRetry = -1000;
+    bool stepLaunch();
+    int stepFinish(AlensStepStats *out, bool direct);
+    void finalizeForStep() { finalize(); }
+    // bounded device waits: grid-barrier limit (0 = default) and the
+    // barrier stall used to test the timeout path
+    void setWaitLimit(unsigned long long timeoutNs, int stallBarriers);
     int detect(AlensStepStats *out);
     int solve(AlensStepStats *out);
     int advance(AlensStepStats *out);
@@ -124,6 +134,8 @@ class Engine {
     int formRequest_ = -1;   // ALENS_SOLVER_FORM override (-1 automatic)
     bool residentFailed_ = false;  // a step did not fit the cluster-resident form
     bool fastFailed_ = false;      // a step did not fit the single-system form
+    unsigned long long waitTimeoutNs_ = 2000000000ULL;  // grid-barrier wait limit (2 s)
+    int stallBarriers_ = 0;                             // 1: barriers wait for one block more (tests)
     int prevCountHost_ = 0;  // valid warm-start keys on the device
     int solverGrid_ = 0;
     MlpModel *mlp_ = nullptr;

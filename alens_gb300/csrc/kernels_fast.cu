@@ -150,7 +150,8 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float bh, float bl)
 __device__ __forceinline__ bool fast_barrier(const DevState &S, int bi, int G, unsigned long long timeout_ns) {
     if (blockIdx.x == 0 && threadIdx.x == 0) st_relaxed_u32(&S.ctl->bar.pass[(bi + 1) % 3][0], 0u);
     int stopUnused = 0;
-    return grid_sync_pass(&S.ctl->bar, (unsigned int)G, &S.ctl->errFlags, timeout_ns, bi, 1, stopUnused);
+    return grid_sync_pass(&S.ctl->bar, (unsigned int)(G + S.barrierExtra), &S.ctl->errFlags, timeout_ns, bi, 1,
+                          stopUnused);
 }
 
 // Block record: warp sums in Real, then warp 0 adds the eight warp values

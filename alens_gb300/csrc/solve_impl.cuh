@@ -659,7 +659,8 @@ __global__ void __launch_bounds__(kSolveThreads, 2) k_solve(DevState S, SolveVie
         cStore = clock64();
 #endif
         int stop = 0;
-        if (!grid_sync_pass(&S.ctl->bar, (unsigned int)nActive, &S.ctl->errFlags, timeout_ns, p, sh.act, stop))
+        if (!grid_sync_pass(&S.ctl->bar, (unsigned int)(nActive + S.barrierExtra), &S.ctl->errFlags, timeout_ns,
+                            p, sh.act, stop))
             return;
 #ifdef ALENS_TRACE
         const unsigned long long trT3 = global_ns();

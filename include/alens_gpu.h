@@ -241,6 +241,18 @@ int alens_set_boundaries(AlensCtx *ctx, int replica, int n, const AlensBoundary 
  * iterate), or an error; *stats (nullable) receives the summary. */
 int alens_step(AlensCtx *ctx, AlensStepStats *stats);
 
+/* Step several contexts together (the batched call SURVEY's boundary names
+ * for replicas kept in separate contexts; replicas in one context are
+ * stepped together by alens_step already, see alens_create_ensemble).
+ * Every context's step is enqueued on its own stream before any result is
+ * read back, so steps on different streams run concurrently; a context
+ * whose step must be repeated (buffer regrowth) repeats it alone.  stats
+ * (nullable) receives n entries.  Returns the first status that is neither
+ * ALENS_OK nor ALENS_NOT_CONVERGED, else ALENS_NOT_CONVERGED if any step
+ * hit the cap, else ALENS_OK.  Replaces n calls of SylinderSystem::runStep
+ * (SRC/TubuleSystem.cpp:223). */
+int alens_step_batched(AlensCtx **ctxs, int n, AlensStepStats *stats);
+
 /* The three parts of alens_step, for staged use and testing:
  * detect = known velocity + pair search + constraint assembly,
  * solve = BBPGD, advance = velocity write-back + Euler update
@@ -278,6 +290,22 @@ int alens_get_constraints(AlensCtx *ctx, int replica, int cap,
 int alens_get_operator(AlensCtx *ctx, int replica, int capNnz, int *nnz, int32_t *rowPtr,
                        int32_t *cols, double *vals, double *q, double *cinv,
                        double *lowerBound, double *gamma0);
+
+/* The multipliers of one replica's constraints after a solve, with the rod
+ * pair of each (pairs[2k], pairs[2k+1] = indexI, indexJ), canonical order
+ * as alens_get_constraints: the gamma a ConstraintBlock holds after
+ * runStep (SRC/TubuleSystem.cpp:697-743 reads the pool).  *n receives the
+ * count; ALENS_CAPACITY if cap < *n.  pairs and gamma may be NULL. */
+int alens_get_gamma(AlensCtx *ctx, int replica, int cap, int *n, int32_t *pairs, double *gamma);
+
+/* The collision constraints of one replica after detect (the near-pair
+ * search's result: rod pairs with separation below sylinderColBuf, with the
+ * periodic image of rod J, and boundary contacts with indexJ = -1), sorted by
+ * (indexI, indexJ, image).  *n receives the count; ALENS_CAPACITY if
+ * cap < *n.  Any array may be NULL.  The role of the pair list SimToolbox's
+ * near-pair search hands to CalcSylinderNearForce (Protein/ProteinData.hpp:25). */
+int alens_get_pairs(AlensCtx *ctx, int replica, int cap, int *n, int32_t *indexI, int32_t *indexJ,
+                    int32_t *image);
 
 /* Sum over the constraints of one replica of the pair virial
  * gamma * (lab_I - lab_J) (x) n  (3x3 row-major); the role of
@@ -376,6 +404,16 @@ int alens_mlp_collect(AlensCtx *ctx, AlensMlp *mlp, int64_t *added);
  * last step's collision constraints of one replica, canonical order;
  * *n receives the count; ALENS_CAPACITY if cap < n. */
 int alens_get_features(AlensCtx *ctx, int replica, int cap, float *features, float *scale, int *n);
+
+/* Bounded device waits (no counterpart in the reference).  Every grid-wide
+ * wait of the solver gives up after timeoutNs (0 = the default, 2 s), sets
+ * ALENS_TIMEOUT and leaves the rods unmoved.  stallBarriers = 1 makes the
+ * solver's grid barriers wait for one block more than the launch holds, so
+ * that every such wait of the following steps runs out: a test of the
+ * timeout path that faults nothing (the context stays usable); 0 restores
+ * normal operation.  Not between alens_detect and alens_advance
+ * (ALENS_NOT_READY). */
+int alens_set_wait_limit(AlensCtx *ctx, uint64_t timeoutNs, int stallBarriers);
 
 /* Steps executed so far (SylinderSystem::getStepCount). */
 int alens_get_step_count(AlensCtx *ctx, int64_t *count);
