@@ -85,6 +85,7 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&side2_, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&orderJoin_, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&orderFork_, cudaEventDisableTiming));
     for (int i = 0; i < 3; i++) {
         CK(cudaEventCreateWithFlags(&forkEv_[i], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&joinEv_[i], cudaEventDisableTiming));
@@ -123,6 +124,7 @@ Engine::~Engine() {
     if (side_) cudaStreamDestroy(side_);
     if (side2_) cudaStreamDestroy(side2_);
     if (orderJoin_) cudaEventDestroy(orderJoin_);
+    if (orderFork_) cudaEventDestroy(orderFork_);
     if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -461,6 +463,16 @@ void Engine::allocOperator(long long nnz) {
     S_.nnzCap = (int)nnz;
     S_.aent = alloc<int4>(opAllocs_, (size_t)nnz);
     S_.aent32 = precision_ == ALENS_PREC_MIXED ? alloc<int4>(opAllocs_, (size_t)nnz) : nullptr;
+    if (precision_ == ALENS_PREC_MIXED && R_ == 1) {
+        // the streaming layout pads each 32-row slice to its longest row;
+        // rows sorted by length bound the padding by 32 x the longest row
+        // per block
+        S_.fastEntCap = nnz + nnz / 2 + 32LL * 128 * kFastMaxGrid;
+        S_.fastEnt = alloc<int2>(opAllocs_, (size_t)S_.fastEntCap);
+    } else {
+        S_.fastEnt = nullptr;
+        S_.fastEntCap = 0;
+    }
 }
 
 void Engine::updateRods(int rep, int n, const double *pos, const double *quat) {
@@ -704,16 +716,7 @@ int Engine::enqueueDetect() {
     CK(cudaEventRecord(forkEv_[2], stream_));
     CK(cudaStreamWaitEvent(side_, forkEv_[2], 0));
     launch_ranges(S, side_);
-    // the single-system solver's spatial row order on a third branch, beside
-    // the pair sort, constraint build and operator assembly (computed
-    // whenever that form may run, so that the autotuner can try it on the
-    // detected problem)
-    const bool order = S.fastPerm && !fastFailed_;
-    if (order) {
-        CK(cudaStreamWaitEvent(side2_, forkEv_[2], 0));
-        n += launch_fast_order(S, side2_);
-        CK(cudaEventRecord(orderJoin_, side2_));
-    }
+
     CK(cudaEventRecord(joinEv_[0], side_));
     n += launch_pair_sort(S, stream_);
     CK(cudaStreamWaitEvent(stream_, joinEv_[0], 0));
@@ -725,6 +728,17 @@ int Engine::enqueueDetect() {
     launch_weights(S, side_);
     n += 3;
     n += launch_rows(S, stream_);
+    // the single-system solver's spatial row order (from the cell list and
+    // the rod rows) on a third branch, beside the operator assembly;
+    // computed whenever that form may run, so that the autotuner can try it
+    // on the detected problem
+    const bool order = S.fastPerm && !fastFailed_;
+    if (order) {
+        CK(cudaEventRecord(orderFork_, stream_));
+        CK(cudaStreamWaitEvent(side2_, orderFork_, 0));
+        n += launch_fast_order(S, side2_);
+        CK(cudaEventRecord(orderJoin_, side2_));
+    }
     n += launch_assemble(S, stream_, side_, joinEv_[1]);
     if (warm_ == ALENS_WARM_MLP && mlp_) {
         launch_mlp_warm(S, mlp_->view(), stream_);

@@ -182,6 +182,8 @@ struct DevState {
     // Morton order (fixed per context)
     double *fastPart;
     int *fastPerm, *fastInv, *fastCellCnt, *fastCellBase, *fastScanTmp, *cellByRank;
+    int2 *fastEnt;             // streaming layout of the single-system solver (fastEntCap entries,
+    long long fastEntCap;      // an equal region per block)
     // scan scratch
     int *scanTmp;
 };

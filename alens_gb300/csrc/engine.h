@@ -120,7 +120,7 @@ class Engine {
     cudaStream_t stream_ = nullptr;
     cudaStream_t side_ = nullptr;  // concurrent branch of the detect stage
     cudaStream_t side2_ = nullptr; // the single-system solver's row order, beside the assembly
-    cudaEvent_t orderJoin_ = nullptr;
+    cudaEvent_t orderJoin_ = nullptr, orderFork_ = nullptr;
     cudaEvent_t forkEv_[3] = {nullptr, nullptr, nullptr}, joinEv_[3] = {nullptr, nullptr, nullptr};
     bool ownStream_ = false;
     int precision_ = 0, warm_ = 0;

@@ -17,9 +17,9 @@
 //   Ordering (per step, kernels k_order_count / k_order_place on a side
 //     stream beside the operator assembly): constraints are permuted so
 //     that each block owns a compact patch of space.  Cells are walked in
-//     Morton order, the rods of a cell by index, and each rod's collisions
-//     (its canonical run, [pairOff[i], pairOff[i+1])) stay in canonical
-//     order; bilateral rows keep their canonical positions.  Deterministic.
+//     Morton order, the rods of a cell by index, and each rod's constraints
+//     with the rod as I (collisions, then crosslinker and user blocks) in
+//     ascending canonical order, read from the rod rows.  Deterministic.
 //   Rows: block b owns permuted rows [r0, r1) and caches their operator rows
 //     in shared memory (8 bytes per entry).  Each entry's column is either one
 //     of the block's own rows (its iterate is read from the block's own
@@ -44,9 +44,18 @@
 //     The solution is left in canonical order in the FP64 iterate buffer
 //     that the rod update reads.
 //
-// A block whose rows do not fit its shared memory reports it in its first
-// record; every block then stops after the first pass and the context falls
-// back to the grid form (kErrSolverFit).
+// Streaming blocks: a block whose rows hold more entries than its shared
+// memory (the 50,000-rod bundle with 200,000 crosslinks: ~43,000 per block)
+// sorts its rows by length (descending, ties by index) into slices of 32 and
+// writes their entries column-major (entry j of the slice's 32 rows
+// contiguous, short rows padded with zero entries) into its own region of a
+// global buffer, once per solve.  Each pass a warp streams a slice's
+// entries with coalesced loads; own columns come from shared memory, the
+// others straight from the previous pass's global iterates (L1/L2).
+//
+// A block whose rows fit neither form (more than kFastRows rows, or a region
+// too small) reports it in its first record; every block then stops after
+// the first pass and the context falls back to the grid form (kErrSolverFit).
 //
 // Iterations are reported as in the other mixed-precision forms: FP32
 // iterations in refineIter, FP64 refinement iterations in iter.
@@ -60,8 +69,10 @@ namespace {
 
 constexpr int kFastThreads = 256;
 constexpr int kFastWarps = kFastThreads / 32;
-constexpr int kFastRows = 1024;          // own rows per block
-constexpr int kFastEnts = 11000;         // cached operator entries per block
+constexpr int kFastRows = 2048;          // own rows per block
+constexpr int kFastEnts = 8000;          // operator entries per block held in shared memory
+constexpr int kSlice = 32;               // rows per slice of the streaming layout
+constexpr int kMaxSlices = kFastRows / kSlice;
 constexpr int kFastHalo = 3000;          // halo columns per block
 constexpr int kFastCellRods = 256;       // rods per cell staged in shared memory by the ordering
 constexpr int kRowBatch = 8;             // row entries loaded together
@@ -96,6 +107,9 @@ constexpr int kOffGv = kOffHaloCol + kFastHalo * 4;             // float2 [kFast
 constexpr int kFastSmem = kOffGv + kFastHalo * 8;
 static_assert(kOffEnt % 16 == 0 && kOffGv % 8 == 0, "shared-memory alignment");
 static_assert(kFastSmem + 1024 <= 227 * 1024, "shared memory per block");
+// the streaming layout's sort keys, slot order and slice table alias the
+// shared-memory entry region (unused by a streaming block)
+static_assert((2 * kFastRows + 2 * (kMaxSlices + 1)) * 4 <= kFastEnts * 8, "streaming scratch");
 
 enum FastPhase { kPh32 = 0, kPhCheck = 1, kPh64 = 2 };
 constexpr int kStatusMisfit = -1;
@@ -422,6 +436,11 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
     int *haloPos = reinterpret_cast<int *>(smem + kOffHaloPos);
     int *haloCol = reinterpret_cast<int *>(smem + kOffHaloCol);
     float2 *gv = reinterpret_cast<float2 *>(smem + kOffGv);
+    // streaming layout (aliases the entry region)
+    int *sortKey = reinterpret_cast<int *>(smem + kOffEnt);
+    int *slotRow = sortKey + kFastRows;
+    int *sliceBase = slotRow + kFastRows;
+    int *sliceLen = sliceBase + kMaxSlices + 1;
     if (ld_volatile_i32(&S.ctl->errFlags) & kErrStepAbort) return;
     const int G = (int)gridDim.x, b = (int)blockIdx.x;
     const int tid = (int)threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -443,6 +462,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
     const int rpb = (n + G - 1) / G;
     const int r0 = min(b * rpb, n), r1 = min(r0 + rpb, n), nr = r1 - r0;
     int fit = rpb <= kFastRows ? 1 : 0;
+    int big = 0;  // 1: this block streams its entries from global memory
     if (fit) {
         for (int i = tid; i < nr; i += kFastThreads) {
             const int k = __ldcg(perm + r0 + i);
@@ -468,8 +488,8 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
         }
         __syncthreads();
         const int E = nr > 0 ? rowBeg[nr] : 0;
-        if (E > kFastEnts) fit = 0;
-        if (fit) {
+        if (E > kFastEnts) big = 1;
+        if (!big) {
             // entry-parallel: entry e of row i (binary search in rowBeg)
             for (int e = tid; e < E; e += kFastThreads) {
                 int lo = 0, hi = nr - 1;
@@ -500,8 +520,89 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
         }
     }
     __syncthreads();
-    if (sh.haloCount > kFastHalo) fit = 0;
-    const int nHalo = fit ? sh.haloCount : 0;
+    if (fit && !big && sh.haloCount > kFastHalo) big = 1;  // too many halo columns: stream instead
+    int2 *gEnt = S.fastEnt + (S.fastEntCap / G) * (long long)b;  // this block's streaming region
+    int nSlices = 0;
+    if (fit && big) {
+        // rows sorted by length, descending (ties by index): keys in a
+        // power-of-two bitonic network
+        int P = 1;
+        while (P < nr) P <<= 1;
+        for (int i = tid; i < P; i += kFastThreads) {
+            const int len = i < nr ? min(rowBeg[i + 1] - rowBeg[i], 1023) : 0;
+            sortKey[i] = i < nr ? (((1023 - len) << 11) | i) : 0x7fffffff;
+        }
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = tid; i < P; i += kFastThreads) {
+                    const int ij = i ^ j;
+                    if (ij > i) {
+                        const int a = sortKey[i], c = sortKey[ij];
+                        if (((i & k) == 0) == (a > c)) {
+                            sortKey[i] = c;
+                            sortKey[ij] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        nSlices = (nr + kSlice - 1) / kSlice;
+        for (int t = tid; t < nr; t += kFastThreads) slotRow[t] = sortKey[t] & 2047;
+        __syncthreads();
+        if (warp == 0) {  // slice lengths (first row of a slice is its longest) and bases
+            int carry = 0;
+            for (int c0 = 0; c0 < nSlices; c0 += 32) {
+                const int sl = c0 + lane;
+                int len = 0;
+                if (sl < nSlices) {
+                    const int i = slotRow[sl * kSlice];
+                    len = rowBeg[i + 1] - rowBeg[i];
+                    sliceLen[sl] = len;
+                }
+                const int v = kSlice * len;
+                const int incl = warp_incl_scan_i(v);
+                if (sl < nSlices) sliceBase[sl] = carry + incl - v;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
+            }
+            if (lane == 0) sliceBase[nSlices] = carry;
+        }
+        __syncthreads();
+        const int total = sliceBase[nSlices];
+        if ((long long)total > S.fastEntCap / G) {
+            fit = 0;
+        } else {
+            // entries column-major per slice; padding: the row's own column, value 0
+            for (int idx = tid; idx < total; idx += kFastThreads) {
+                int lo = 0, hi = nSlices - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sliceBase[mid] <= idx)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                const int rel = idx - sliceBase[lo];
+                const int j = rel / kSlice, t = lo * kSlice + rel % kSlice;
+                int2 out = make_int2(kEntOwn, 0);
+                if (t < nr) {
+                    const int i = slotRow[t];
+                    out = make_int2(i | kEntOwn, 0);
+                    if (j < rowBeg[i + 1] - rowBeg[i]) {
+                        const int4 en = __ldg(S.aent32 + ownA[i] + j);
+                        const int pc = __ldcg(inv + en.x);
+                        const bool own = (unsigned int)(pc - r0) < (unsigned int)nr;
+                        out = make_int2(((own ? pc - r0 : pc) & kEntSrcMask) | ((en.y & 3) << 28) | (own ? kEntOwn : 0),
+                                        en.z);
+                    }
+                }
+                gEnt[idx] = out;
+            }
+        }
+    }
+    __syncthreads();
+    const int nHalo = (fit && !big) ? sh.haloCount : 0;
 #ifdef ALENS_TRACE_FAST
     tLoad = clock64();
 #endif
@@ -582,7 +683,96 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
             float2 *ownOut = ownSt + (odd ? 0 : kFastRows);
             float2 *gOut = odd ? gst1 : gst0;
             float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, am = 0.0f;
-            for (int i = tid; i < nr && fit; i += kFastThreads) {
+            // iterates of the other blocks' columns (streaming blocks): the
+            // previous pass's permuted buffer, or at pass 0 the canonical
+            // initial guess
+            const float2 *gIn = odd ? gst0 : gst1;
+            // row tail shared by both layouts
+            auto finish_row = [&](int i, float acc, float gam, float gold, float lbk, float xk) {
+                const float2 qc = ownQc[i];
+                acc = fmaf(qc.y, xk, acc);
+                float2 o;
+                if (mode == kModeAG) {
+                    a0 += gold * gold;
+                    a1 += gold * acc;
+                    o = make_float2(gam, gold);
+                } else {
+                    const float gn = acc + qc.x;
+                    // x - P(x - g) = min(g, x - lb)
+                    const float mm = gn < xk - lbk ? gn : xk - lbk;
+                    float rm = fabsf(mm);
+                    if (rm != rm) {
+                        atomicOr(&nanSeen, kErrNaN);
+                        rm = INFINITY;
+                    }
+                    am = rm > am ? rm : am;
+                    if (mode == kModeIter) {
+                        const float s = xk - gam, y = gn - gold;
+                        a0 += s * s;
+                        a1 += s * y;
+                        a2 += y * y;
+                    }
+                    o = make_float2(xk, gn);
+                }
+                ownOut[i] = o;
+                gOut[r0 + i] = o;
+            };
+            if (fit && big) {
+                // a warp per slice, a lane per row; entry j of the slice's rows
+                // is one coalesced load
+                for (int sl = warp; sl < nSlices; sl += kFastWarps) {
+                    const int t = sl * kSlice + lane;
+                    const int i = t < nr ? slotRow[t] : 0;
+                    const float2 own = ownIn[i];
+                    const float gam = own.x, gold = own.y, lbk = ownLb[i];
+                    float xk;
+                    if (mode == kModeG0)
+                        xk = gam;
+                    else if (mode == kModeAG)
+                        xk = gold;
+                    else
+                        xk = projlb<float>(fmaf(-alpha, gold, gam), lbk);
+                    float acc = 0.0f;
+                    const int len = sliceLen[sl];
+                    const int2 *se = gEnt + sliceBase[sl] + lane;
+                    for (int jb = 0; jb < len; jb += kRowBatch) {
+                        int2 en[kRowBatch];
+                        float2 sv[kRowBatch];
+#pragma unroll
+                        for (int j = 0; j < kRowBatch; j++)
+                            en[j] = jb + j < len ? __ldg(se + (jb + j) * kSlice) : make_int2(i | kEntOwn, 0);
+#pragma unroll
+                        for (int j = 0; j < kRowBatch; j++) {
+                            const int src = en[j].x & kEntSrcMask;
+                            if (en[j].x & kEntOwn)
+                                sv[j] = ownIn[src];
+                            else if (p == 0)
+                                sv[j] = make_float2(__ldcg(gst1 + __ldcg(perm + src)).x, 0.0f);
+                            else
+                                sv[j] = gIn[src];
+                        }
+#pragma unroll
+                        for (int j = 0; j < kRowBatch; j++) {
+                            const int kind = (en[j].x >> 28) & 3;
+                            float lbl = 0.0f;
+                            if (kind != 0) {
+                                const int src = en[j].x & kEntSrcMask;
+                                lbl = lb32_of(kind, (en[j].x & kEntOwn) ? ownK[src] : __ldcg(perm + src), S.lb);
+                            }
+                            float xl;
+                            if (mode == kModeG0)
+                                xl = sv[j].x;
+                            else if (mode == kModeAG)
+                                xl = sv[j].y;
+                            else
+                                xl = projlb<float>(fmaf(-alpha, sv[j].y, sv[j].x), lbl);
+                            acc = fmaf(__int_as_float(en[j].y), xl, acc);
+                        }
+                    }
+                    if (t < nr) finish_row(i, acc, gam, gold, lbk, xk);
+                }
+            }
+            for (int i = tid; i < nr && fit && !big; i += kFastThreads) {
                 const int e0 = rowBeg[i], e1 = rowBeg[i + 1];
                 // the row's own iterate and its x (the diagonal entry's column)
                 const float2 own = ownIn[i];
@@ -622,33 +812,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                         acc = fmaf(__int_as_float(en[j].y), xl, acc);
                     }
                 }
-                const float2 qc = ownQc[i];
-                acc = fmaf(qc.y, xk, acc);
-                float2 o;
-                if (mode == kModeAG) {
-                    a0 += gold * gold;
-                    a1 += gold * acc;
-                    o = make_float2(gam, gold);
-                } else {
-                    const float gn = acc + qc.x;
-                    // x - P(x - g) = min(g, x - lb)
-                    const float mm = gn < xk - lbk ? gn : xk - lbk;
-                    float rm = fabsf(mm);
-                    if (rm != rm) {
-                        atomicOr(&nanSeen, kErrNaN);
-                        rm = INFINITY;
-                    }
-                    am = rm > am ? rm : am;
-                    if (mode == kModeIter) {
-                        const float s = xk - gam, y = gn - gold;
-                        a0 += s * s;
-                        a1 += s * y;
-                        a2 += y * y;
-                    }
-                    o = make_float2(xk, gn);
-                }
-                ownOut[i] = o;
-                gOut[r0 + i] = o;
+                finish_row(i, acc, gam, gold, lbk, xk);
             }
 #ifdef ALENS_TRACE_FAST
             __syncthreads();
@@ -663,6 +827,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
             const float2 *ownIn = ownSt + (odd ? kFastRows : 0);
             double2 *stOut = S.st[p & 1];
             double am = 0.0;
+            const float2 *gIn = odd ? gst0 : gst1;  // the last FP32 pass's permuted iterates
             for (int i = tid; i < nr && fit; i += kFastThreads) {
                 const int e0 = rowBeg[i], e1 = rowBeg[i + 1], k = ownK[i], a0 = ownA[i];
                 const double lbk = lb64_of(__ldg(S.lbKind + k), k, S.lb);
@@ -670,13 +835,21 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                 xk = xk < lbk ? lbk : xk;
                 double acc = 0.0;
                 for (int e = e0; e < e1; e++) {
-                    const int2 en = ent[e];
-                    const int src = en.x & kEntSrcMask;
-                    const float xs = (en.x & kEntOwn) ? ownIn[src].x : gv[src].x;
-                    const double lbl = lb64_of((en.x >> 28) & 3, entCol[e], S.lb);
+                    const int4 e64 = __ldg(S.aent + a0 + (e - e0));
+                    float xs;
+                    double lbl;
+                    if (big) {
+                        const int pc = __ldcg(inv + e64.x);
+                        xs = (unsigned int)(pc - r0) < (unsigned int)nr ? ownIn[pc - r0].x : gIn[pc].x;
+                        lbl = lb64_of(e64.y & 3, e64.x, S.lb);
+                    } else {
+                        const int2 en = ent[e];
+                        const int src = en.x & kEntSrcMask;
+                        xs = (en.x & kEntOwn) ? ownIn[src].x : gv[src].x;
+                        lbl = lb64_of((en.x >> 28) & 3, entCol[e], S.lb);
+                    }
                     double xl = (double)xs;
                     xl = xl < lbl ? lbl : xl;
-                    const int4 e64 = __ldg(S.aent + a0 + (e - e0));
                     acc = fma(__hiloint2double(e64.w, e64.z), xl, acc);
                 }
                 const double2 qc = __ldg(S.qc + k);
@@ -753,7 +926,8 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
 }
 
 // ---------------------------------------------------------------- ordering
-// Constraints per cell, one warp per cell in Morton rank order.
+// Constraints whose rod I lies in the cell (a rod's side-I entries of the
+// rod rows), one warp per cell in Morton rank order.
 __global__ void k_order_count(DevState S) {
     if (ld_volatile_i32(&S.ctl->errFlags) & (kErrNaN | kErrOverflow)) return;
     const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
@@ -761,38 +935,40 @@ __global__ void k_order_count(DevState S) {
     const int c = S.cellByRank[w];
     const int s0 = S.cellStart[c], s1 = S.cellStart[c + 1];
     int cnt = 0;
-    for (int s = s0 + lane; s < s1; s += 32) cnt += S.pairCount[S.sidx[s]];
+    for (int s = s0 + lane; s < s1; s += 32) {
+        const int r = S.sidx[s];
+        for (int e = S.rowPtr[r]; e < S.rowPtr[r + 1]; e++) cnt += (S.rowEnt[e] & 1) == 0 ? 1 : 0;
+    }
     cnt = warp_sum_i(cnt);
     if (lane == 0) S.fastCellCnt[w] = cnt;
 }
 
 // Permutation and inverse, one warp per cell (rank order): a rod's
-// collisions start after those of the cell's rods with a smaller index
-// (their counts summed, no sort needed), so the order within a cell is by
-// rod index whatever order the cell list holds them in.  Bilateral rows
-// keep their canonical positions.
+// constraints (those with the rod as I, ascending: its collisions, then its
+// crosslinker and user blocks) start after those of the cell's rods with a
+// smaller index (their counts summed, no sort needed), so the order within a
+// cell is by rod index whatever order the cell list holds them in.
 __global__ void __launch_bounds__(256) k_order_place(DevState S) {
     __shared__ int stage[8][2 * kFastCellRods];  // per warp: the cell's rods and their counts
     if (ld_volatile_i32(&S.ctl->errFlags) & (kErrNaN | kErrOverflow)) return;
-    const int nColl = S.pairOff[S.nRods], n = nColl + S.bilPrefix[1];
-    if (n > S.cap) return;  // the constraint buffers overflowed: the step is rerun
-    const int tidG = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    for (int k = nColl + tidG; k < n; k += (int)(gridDim.x * blockDim.x)) {
-        S.fastPerm[k] = k;
-        S.fastInv[k] = k;
-    }
-    const int gw = tidG >> 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     if (gw >= S.nCells) return;
     const int c = S.cellByRank[gw];
     const int s0 = S.cellStart[c], m = S.cellStart[c + 1] - s0;
     const int base = S.fastCellBase[gw];
     int *rods = stage[warp], *cnts = stage[warp] + kFastCellRods;
+    auto side_i_count = [&](int r) {
+        int n = 0;
+        for (int e = S.rowPtr[r]; e < S.rowPtr[r + 1]; e++) n += (S.rowEnt[e] & 1) == 0 ? 1 : 0;
+        return n;
+    };
     const bool staged = m <= kFastCellRods;
     if (staged) {
         for (int s = lane; s < m; s += 32) {
             const int r = S.sidx[s0 + s];
             rods[s] = r;
-            cnts[s] = S.pairCount[r];
+            cnts[s] = side_i_count(r);
         }
         __syncwarp();
     }
@@ -801,13 +977,16 @@ __global__ void __launch_bounds__(256) k_order_place(DevState S) {
         int off = 0;
         for (int u = 0; u < m; u++) {
             const int ru = staged ? rods[u] : S.sidx[s0 + u];
-            if (ru < r) off += staged ? cnts[u] : S.pairCount[ru];
+            if (ru < r) off += staged ? cnts[u] : side_i_count(ru);
         }
-        const int cnt = staged ? cnts[s] : S.pairCount[r];
-        const int pos = base + off, o0 = S.pairOff[r];
-        for (int t = 0; t < cnt; t++) {
-            S.fastPerm[pos + t] = o0 + t;
-            S.fastInv[o0 + t] = pos + t;
+        int pos = base + off;
+        for (int e = S.rowPtr[r]; e < S.rowPtr[r + 1]; e++) {
+            const int ent = S.rowEnt[e];
+            if (ent & 1) continue;
+            const int k = ent >> 1;
+            S.fastPerm[pos] = k;
+            S.fastInv[k] = pos;
+            pos++;
         }
     }
 }
