@@ -573,31 +573,59 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
         if ((long long)total > S.fastEntCap / G) {
             fit = 0;
         } else {
-            // entries column-major per slice; padding: the row's own column, value 0
-            for (int idx = tid; idx < total; idx += kFastThreads) {
-                int lo = 0, hi = nSlices - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (sliceBase[mid] <= idx)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-                const int rel = idx - sliceBase[lo];
-                const int j = rel / kSlice, t = lo * kSlice + rel % kSlice;
-                int2 out = make_int2(kEntOwn, 0);
-                if (t < nr) {
-                    const int i = slotRow[t];
-                    out = make_int2(i | kEntOwn, 0);
-                    if (j < rowBeg[i + 1] - rowBeg[i]) {
-                        const int4 en = __ldg(S.aent32 + ownA[i] + j);
-                        const int pc = __ldcg(inv + en.x);
-                        const bool own = (unsigned int)(pc - r0) < (unsigned int)nr;
-                        out = make_int2(((own ? pc - r0 : pc) & kEntSrcMask) | ((en.y & 3) << 28) | (own ? kEntOwn : 0),
-                                        en.z);
+            // entries column-major per slice; padding: the row's own column,
+            // value 0.  Eight entries per thread at a time: their operator
+            // entries, then their columns' positions, are all requested
+            // before any is used.
+            constexpr int kFill = 8;
+            for (int base = 0; base < total; base += kFill * kFastThreads) {
+                int slot[kFill], rowI[kFill], jj[kFill];
+                int4 en[kFill];
+                int pc[kFill];
+#pragma unroll
+                for (int u = 0; u < kFill; u++) {
+                    const int idx = base + u * kFastThreads + tid;
+                    slot[u] = -1;
+                    rowI[u] = 0;
+                    jj[u] = 0;
+                    if (idx < total) {
+                        int lo = 0, hi = nSlices - 1;
+                        while (lo < hi) {
+                            const int mid = (lo + hi + 1) >> 1;
+                            if (sliceBase[mid] <= idx)
+                                lo = mid;
+                            else
+                                hi = mid - 1;
+                        }
+                        const int rel = idx - sliceBase[lo];
+                        const int t = lo * kSlice + rel % kSlice;
+                        jj[u] = rel / kSlice;
+                        if (t < nr) {
+                            rowI[u] = slotRow[t];
+                            slot[u] = jj[u] < rowBeg[rowI[u] + 1] - rowBeg[rowI[u]] ? 1 : 0;
+                        } else {
+                            slot[u] = 0;
+                        }
                     }
                 }
-                gEnt[idx] = out;
+#pragma unroll
+                for (int u = 0; u < kFill; u++)
+                    en[u] = slot[u] == 1 ? __ldg(S.aent32 + ownA[rowI[u]] + jj[u]) : make_int4(0, 0, 0, 0);
+#pragma unroll
+                for (int u = 0; u < kFill; u++) pc[u] = slot[u] == 1 ? __ldcg(inv + en[u].x) : 0;
+#pragma unroll
+                for (int u = 0; u < kFill; u++) {
+                    const int idx = base + u * kFastThreads + tid;
+                    if (slot[u] < 0) continue;
+                    int2 out = make_int2(rowI[u] | kEntOwn, 0);
+                    if (slot[u] == 1) {
+                        const bool own = (unsigned int)(pc[u] - r0) < (unsigned int)nr;
+                        out = make_int2(((own ? pc[u] - r0 : pc[u]) & kEntSrcMask) | ((en[u].y & 3) << 28) |
+                                            (own ? kEntOwn : 0),
+                                        en[u].z);
+                    }
+                    gEnt[idx] = out;
+                }
             }
         }
     }
@@ -735,12 +763,21 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                     float acc = 0.0f;
                     const int len = sliceLen[sl];
                     const int2 *se = gEnt + sliceBase[sl] + lane;
+                    // software pipeline: the next batch's entries are requested
+                    // before this batch's iterates
+                    int2 nxt[kRowBatch];
+#pragma unroll
+                    for (int j = 0; j < kRowBatch; j++)
+                        nxt[j] = j < len ? __ldg(se + j * kSlice) : make_int2(i | kEntOwn, 0);
                     for (int jb = 0; jb < len; jb += kRowBatch) {
                         int2 en[kRowBatch];
                         float2 sv[kRowBatch];
 #pragma unroll
+                        for (int j = 0; j < kRowBatch; j++) en[j] = nxt[j];
+#pragma unroll
                         for (int j = 0; j < kRowBatch; j++)
-                            en[j] = jb + j < len ? __ldg(se + (jb + j) * kSlice) : make_int2(i | kEntOwn, 0);
+                            nxt[j] = jb + kRowBatch + j < len ? __ldg(se + (jb + kRowBatch + j) * kSlice)
+                                                              : make_int2(i | kEntOwn, 0);
 #pragma unroll
                         for (int j = 0; j < kRowBatch; j++) {
                             const int src = en[j].x & kEntSrcMask;
@@ -753,11 +790,13 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                         }
 #pragma unroll
                         for (int j = 0; j < kRowBatch; j++) {
+                            // lower bound of the column: 0 (collisions), none (crosslinks);
+                            // only a general bound (kind 2) needs the column's value
                             const int kind = (en[j].x >> 28) & 3;
-                            float lbl = 0.0f;
-                            if (kind != 0) {
+                            float lbl = kind == 0 ? 0.0f : -INFINITY;
+                            if (kind == 2) {
                                 const int src = en[j].x & kEntSrcMask;
-                                lbl = lb32_of(kind, (en[j].x & kEntOwn) ? ownK[src] : __ldcg(perm + src), S.lb);
+                                lbl = (float)S.lb[(en[j].x & kEntOwn) ? ownK[src] : __ldcg(perm + src)];
                             }
                             float xl;
                             if (mode == kModeG0)
@@ -801,7 +840,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
 #pragma unroll
                     for (int j = 0; j < kRowBatch; j++) {
                         const int kind = (en[j].x >> 28) & 3;
-                        const float lbl = kind == 0 ? 0.0f : lb32_of(kind, entCol[eb + j], S.lb);
+                        const float lbl = kind == 0 ? 0.0f : (kind == 1 ? -INFINITY : (float)S.lb[entCol[eb + j]]);
                         float xl;
                         if (mode == kModeG0)
                             xl = sv[j].x;
