@@ -229,6 +229,7 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_gamma": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_int), _PI32, _PD]),
         "alens_get_pairs": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_int), _PI32, _PI32, _PI32]),
         "alens_set_wait_limit": (C.c_int, [vp, C.c_uint64, C.c_int]),
+        "alens_get_constraint_points": (C.c_int, [vp, C.c_int, C.c_int, _PD]),
         "alens_mlp_create": (C.c_int, [C.c_uint64, C.c_int64, C.POINTER(vp)]),
         "alens_mlp_destroy": (C.c_int, [vp]),
         "alens_mlp_get_params": (C.c_int, [vp, _PF]),
@@ -451,6 +452,24 @@ class GpuSystem:
                  "alens_get_operator")
         m = nnz.value
         return dict(rowPtr=ptr, cols=cols[:m], vals=vals[:m], q=q, cinv=cinv, lb=lb, gamma0=g0)
+
+    def constraint_blocks(self, replica: int = 0) -> dict:
+        """The last step's constraint blocks of one replica, canonical order:
+        rod indices, periodic image, separation, multiplier, normal on rod I,
+        lab-frame points, compliance-derived stiffness kappa (0 for
+        collisions), bilateral and one-sided flags."""
+        c = self.constraints(replica)
+        op = self.operator(replica)
+        n = c["i"].shape[0]
+        lab = np.empty((n, 6))
+        self._ck(self.lib.alens_get_constraint_points(self.h, replica, n, _p(lab, C.c_double)),
+                 "alens_get_constraint_points")
+        cinv = op["cinv"]
+        kappa = np.where(cinv > 0.0, 1.0 / np.where(cinv > 0.0, cinv, 1.0), 0.0)
+        return {"i": c["i"], "j": c["j"], "image": c["image"], "delta0": c["delta0"], "gamma": c["gamma"],
+                "normI": c["jac"][:, 0:3].copy(), "labI": lab[:, 0:3].copy(), "labJ": lab[:, 3:6].copy(),
+                "kappa": kappa, "bilateral": np.isneginf(op["lb"]).astype(np.int32),
+                "oneSide": (c["j"] < 0).astype(np.int32)}
 
     def con_stress(self, replica: int = 0):
         s = np.empty(9)

@@ -254,6 +254,14 @@ int alens_get_pairs(AlensCtx *ctx, int replica, int cap, int *n, int32_t *indexI
     });
 }
 
+int alens_get_constraint_points(AlensCtx *ctx, int replica, int cap, double *lab) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->getConstraintPoints(replica, cap, lab);
+        return (int)ALENS_OK;
+    });
+}
+
 int alens_set_wait_limit(AlensCtx *ctx, uint64_t timeoutNs, int stallBarriers) {
     if (!ctx) return ALENS_INVALID_ARG;
     return guarded_ctx(ctx, [&] {

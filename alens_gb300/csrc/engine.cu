@@ -1328,6 +1328,17 @@ void Engine::getConstraints(int rep, int cap, int32_t *ii, int32_t *jj, int32_t 
     }
 }
 
+void Engine::getConstraintPoints(int rep, int cap, double *lab) {
+    if (rep < 0 || rep >= R_) throw ApiError(ALENS_INVALID_ARG);
+    if (dirty_) throw ApiError(ALENS_NOT_READY);
+    const RepDyn &d = hDyn_[rep];
+    if (cap < d.nCon) throw ApiError(ALENS_CAPACITY);
+    if (d.nCon == 0 || !lab) return;
+    CK(cudaMemcpyAsync(lab, S_.lab + 6 * (size_t)d.conStart, sizeof(double) * 6 * (size_t)d.nCon,
+                       cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+}
+
 void Engine::getOperator(int rep, int capNnz, int *nnz, int32_t *rowPtr, int32_t *cols, double *vals,
                          double *q, double *cinv, double *lowerBound, double *gamma0) {
     if (rep < 0 || rep >= R_) throw ApiError(ALENS_INVALID_ARG);

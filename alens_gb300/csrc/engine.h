@@ -51,6 +51,7 @@ class Engine {
     // bounded device waits: grid-barrier limit (0 = default) and the
     // barrier stall used to test the timeout path
     void setWaitLimit(unsigned long long timeoutNs, int stallBarriers);
+    void getConstraintPoints(int rep, int cap, double *lab);
     int detect(AlensStepStats *out);
     int solve(AlensStepStats *out);
     int advance(AlensStepStats *out);

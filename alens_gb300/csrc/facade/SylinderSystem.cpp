@@ -345,6 +345,7 @@ void SylinderSystem::reinitialize(const std::string &configFile, const std::stri
 }
 
 void SylinderSystem::initialize(const SylinderConfig &cfg, const std::vector<Sylinder> &rods) {
+    haveBlocks_ = false;
     runConfig = cfg;
     rods_ = rods;
     for (size_t i = 0; i < rods_.size(); i++) rods_[i].globalIndex = (int)i;
@@ -370,6 +371,7 @@ void SylinderSystem::runStep() {
     lastStepMs_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     check(rc, "alens_step");
     rodsStale_ = true;
+    haveBlocks_ = true;
 }
 
 void SylinderSystem::stepEuler() {
@@ -461,6 +463,7 @@ void SylinderSystem::writeResult() {
     if (ec) throw std::runtime_error("cannot create " + folder + ": " + ec.message());
     writeResult(folder + "SylinderAscii_" + std::to_string(snapID_) + ".dat");
     writeSylinderVTK(folder, snapID_, getContainer());
+    writeConBlockVTK(folder, snapID_, getConBlocks());
     std::FILE *f = std::fopen("TimeStepInfo.txt", "w");
     if (!f) throw std::runtime_error("cannot write TimeStepInfo.txt");
     std::fprintf(f, "%ld\n%d\n%.17g\n", getStepCount(), snapID_, runConfig.dt * (double)getStepCount());
@@ -576,6 +579,111 @@ void SylinderSystem::writeSylinderVTK(const std::string &folder, int snapID, con
       << "<PDataArray type=\"Int32\" Name=\"isImmovable\" NumberOfComponents=\"1\"/>\n"
       << "<PDataArray type=\"Float64\" Name=\"direction\" NumberOfComponents=\"3\"/>\n"
       << "</PCellData>\n<Piece Source=\"" << piece << "\"/>\n</PPolyData>\n</VTKFile>\n";
+}
+
+std::vector<ConBlockRecord> SylinderSystem::getConBlocks() {
+    std::vector<ConBlockRecord> out;
+    if (!ctx_ || !haveBlocks_) return out;
+    int nc = 0, nb = 0;
+    check(alens_get_num_constraints(ctx_, 0, &nc, &nb), "alens_get_num_constraints");
+    const int n = nc + nb;
+    if (n == 0) return out;
+    std::vector<int32_t> ii(n), jj(n), img(n);
+    std::vector<double> d0(n), gam(n), jac(12 * (size_t)n), lab(6 * (size_t)n), cinv(n), lb(n);
+    check(alens_get_constraints(ctx_, 0, n, ii.data(), jj.data(), img.data(), d0.data(), gam.data(), jac.data()),
+          "alens_get_constraints");
+    check(alens_get_constraint_points(ctx_, 0, n, lab.data()), "alens_get_constraint_points");
+    int nnz = 0;
+    check(alens_get_operator(ctx_, 0, 0, &nnz, nullptr, nullptr, nullptr, nullptr, cinv.data(), lb.data(), nullptr),
+          "alens_get_operator");
+    const auto &rods = getContainer();
+    out.resize((size_t)n);
+    for (int k = 0; k < n; k++) {
+        ConBlockRecord &r = out[(size_t)k];
+        r.gamma = gam[k];
+        r.delta0 = d0[k];
+        r.kappa = cinv[k] > 0.0 ? 1.0 / cinv[k] : 0.0;
+        r.bilateral = std::isinf(lb[k]) && lb[k] < 0.0 ? 1 : 0;
+        r.oneSide = jj[k] < 0 ? 1 : 0;
+        r.globalIndexI = ii[k];
+        r.globalIndexJ = jj[k];
+        r.gidI = rods[(size_t)ii[k]].gid;
+        r.gidJ = jj[k] >= 0 ? rods[(size_t)jj[k]].gid : -1;
+        r.image = img[k];
+        for (int d = 0; d < 3; d++) {
+            r.normI[d] = jac[12 * (size_t)k + d];
+            r.labI[d] = lab[6 * (size_t)k + d];
+            r.labJ[d] = lab[6 * (size_t)k + 3 + d];
+        }
+    }
+    return out;
+}
+
+void SylinderSystem::writeConBlockVTK(const std::string &folder, int snapID, const std::vector<ConBlockRecord> &blocks) {
+    const size_t n = blocks.size();
+    std::vector<double> pts(6 * n), gamma(n), delta0(n), kappa(n), norm(3 * n), stress(9 * n);
+    std::vector<int64_t> gidI(n), gidJ(n);
+    std::vector<int32_t> conn(2 * n), offs(n), bil(n), one(n), gI(n), gJ(n), img(n);
+    for (size_t k = 0; k < n; k++) {
+        const ConBlockRecord &b = blocks[k];
+        double r[3];
+        for (int d = 0; d < 3; d++) {
+            pts[6 * k + d] = b.labI[d];
+            pts[6 * k + 3 + d] = b.labJ[d];
+            norm[3 * k + d] = b.normI[d];
+            r[d] = b.labI[d] - b.labJ[d];
+        }
+        for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) stress[9 * k + 3 * a + c] = (b.gamma * r[a]) * b.normI[c];
+        conn[2 * k] = (int32_t)(2 * k);
+        conn[2 * k + 1] = (int32_t)(2 * k + 1);
+        offs[k] = (int32_t)(2 * k + 2);
+        gamma[k] = b.gamma;
+        delta0[k] = b.delta0;
+        kappa[k] = b.kappa;
+        bil[k] = b.bilateral;
+        one[k] = b.oneSide;
+        gidI[k] = b.gidI;
+        gidJ[k] = b.gidJ;
+        gI[k] = b.globalIndexI;
+        gJ[k] = b.globalIndexJ;
+        img[k] = b.image;
+    }
+    const std::string sep = (folder.empty() || folder.back() == '/') ? "" : "/";
+    const std::string piece = "ConBlock_r0_" + std::to_string(snapID) + ".vtp";
+    const char *head = "<?xml version=\"1.0\"?>\n";
+    {
+        std::ofstream f(folder + sep + piece, std::ios::binary);
+        if (!f) throw std::runtime_error("cannot write " + folder + sep + piece);
+        f << head << "<VTKFile type=\"PolyData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+          << "<PolyData>\n<Piece NumberOfPoints=\"" << 2 * n << "\" NumberOfVerts=\"0\" NumberOfLines=\"" << n
+          << "\" NumberOfStrips=\"0\" NumberOfPolys=\"0\">\n"
+          << "<Points>\n" << dataArray("position", "Float64", 3, pts) << "</Points>\n"
+          << "<Lines>\n" << dataArray("connectivity", "Int32", 1, conn) << dataArray("offsets", "Int32", 1, offs)
+          << "</Lines>\n<CellData Scalars=\"scalars\">\n"
+          << dataArray("gamma", "Float64", 1, gamma) << dataArray("delta0", "Float64", 1, delta0)
+          << dataArray("kappa", "Float64", 1, kappa) << dataArray("bilateral", "Int32", 1, bil)
+          << dataArray("oneSide", "Int32", 1, one) << dataArray("gidI", "Int64", 1, gidI)
+          << dataArray("gidJ", "Int64", 1, gidJ) << dataArray("globalIndexI", "Int32", 1, gI)
+          << dataArray("globalIndexJ", "Int32", 1, gJ) << dataArray("image", "Int32", 1, img)
+          << dataArray("normI", "Float64", 3, norm) << dataArray("Stress", "Float64", 9, stress)
+          << "</CellData>\n</Piece>\n</PolyData>\n</VTKFile>\n";
+    }
+    std::ofstream f(folder + sep + "ConBlock_" + std::to_string(snapID) + ".pvtp", std::ios::binary);
+    if (!f) throw std::runtime_error("cannot write the index of " + piece);
+    f << head << "<VTKFile type=\"PPolyData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+      << "<PPolyData GhostLevel=\"0\">\n<PPoints>\n"
+      << "<PDataArray type=\"Float64\" Name=\"position\" NumberOfComponents=\"3\"/>\n</PPoints>\n"
+      << "<PCellData Scalars=\"scalars\">\n";
+    static const char *kFields[][3] = {{"Float64", "gamma", "1"},      {"Float64", "delta0", "1"},
+                                       {"Float64", "kappa", "1"},      {"Int32", "bilateral", "1"},
+                                       {"Int32", "oneSide", "1"},      {"Int64", "gidI", "1"},
+                                       {"Int64", "gidJ", "1"},         {"Int32", "globalIndexI", "1"},
+                                       {"Int32", "globalIndexJ", "1"}, {"Int32", "image", "1"},
+                                       {"Float64", "normI", "3"},      {"Float64", "Stress", "9"}};
+    for (const auto &fl : kFields)
+        f << "<PDataArray type=\"" << fl[0] << "\" Name=\"" << fl[1] << "\" NumberOfComponents=\"" << fl[2] << "\"/>\n";
+    f << "</PCellData>\n<Piece Source=\"" << piece << "\"/>\n</PPolyData>\n</VTKFile>\n";
 }
 
 DomainInfo DomainInfo::fromConfig(const SylinderConfig &cfg) {

@@ -53,6 +53,20 @@ struct SylinderConfig {
 
 // Host record of one rod (the fields of Sylinder that TubuleSystem reads,
 // SRC/TubuleBind.hpp:54-67).
+// One solved constraint block as the ConBlock snapshot draws it (the
+// ConstraintBlock fields of SRC/TubuleSystem.cpp:727-736 that describe it):
+// contact points labI (rod I) and labJ (rod J, or the boundary surface),
+// normal on rod I, separation, multiplier, stiffness (0 for collisions).
+struct ConBlockRecord {
+    double gamma = 0.0, delta0 = 0.0, kappa = 0.0;
+    int bilateral = 0, oneSide = 0;
+    int64_t gidI = 0, gidJ = -1;
+    int globalIndexI = 0, globalIndexJ = -1, image = 13;
+    double normI[3] = {0, 0, 0};
+    double labI[3] = {0, 0, 0};
+    double labJ[3] = {0, 0, 0};
+};
+
 struct Sylinder {
     int64_t gid = 0;
     int globalIndex = 0;
@@ -146,8 +160,9 @@ class SylinderSystem {
     void calcConStress();         // pair virial of the last step
     void calcOrderParameter();    // polar and nematic order of the rod axes
     void writeResult(const std::string &path) const;  // SylinderAscii text (rods, then link lines)
-    // When a snapshot is due at the current step: SylinderAscii_<snapID>.dat
-    // and Sylinder_<snapID>.pvtp (+ piece) in the current result folder
+    // When a snapshot is due at the current step: SylinderAscii_<snapID>.dat,
+    // Sylinder_<snapID>.pvtp (+ piece) and ConBlock_<snapID>.pvtp (+ piece,
+    // the blocks of the last runStep) in the current result folder
     // (created) and ./TimeStepInfo.txt (step,
     // snapID and time, one per line; its presence is what makes aLENS
     // restart, SRC/main.cpp:28-37), then snapID + 1.  Called where the
@@ -182,6 +197,15 @@ class SylinderSystem {
     // length, group, isImmovable, direction; inline binary arrays (base64 of
     // a UInt64 byte count and the little-endian values).
     static void writeSylinderVTK(const std::string &folder, int snapID, const std::vector<Sylinder> &rods);
+    // ConBlock_<snapID>.pvtp and its piece ConBlock_r0_<snapID>.vtp in
+    // `folder` (the constraint-block snapshot of README.md:142): one line
+    // cell per block from labI to labJ; cell data gamma, delta0, kappa,
+    // bilateral, oneSide, gidI, gidJ, globalIndexI, globalIndexJ, image,
+    // normI and the block's pair virial gamma (labI - labJ) (x) normI as
+    // Stress (row-major 3x3).  Same bytes as alens_gb300.io.write_conblock_pvtp.
+    static void writeConBlockVTK(const std::string &folder, int snapID, const std::vector<ConBlockRecord> &blocks);
+    // The blocks of the last runStep (empty before the first one).
+    std::vector<ConBlockRecord> getConBlocks();
     // TimeStepInfo.txt: exactly three numbers (step, snapID, time); false
     // for anything else (a SylinderAscii snapshot, say)
     static bool readTimeStepInfo(const std::string &path, long *step, int *snapID, double *time);
@@ -200,6 +224,7 @@ class SylinderSystem {
     std::vector<std::array<int64_t, 2>> links_;  // 'L a b' lines (gids): plus end of a to minus end of b
     void applyLinks();
     bool rodsStale_ = false;
+    bool haveBlocks_ = false;  // a step has run on the current rods (its blocks are readable)
     ConstraintBlockPool conPool_;
     AlensStepStats stats_{};
     std::array<double, 9> stress_{};

@@ -25,6 +25,7 @@
 // rods and the first system's rods at its last snapshot.
 #include <cmath>
 #include <cstdio>
+#include <fstream>
 #include <cstdlib>
 #include <cstring>
 #include <stdexcept>
@@ -155,6 +156,28 @@ int main(int argc, char **argv) {
             std::fprintf(stderr, "facade_driver: %s\n", e.what());
             return 1;
         }
+    }
+    if (argc == 5 && std::strcmp(argv[1], "--write-conblock") == 0) {
+        // records: one block per line, "gamma delta0 kappa bilateral oneSide
+        // gidI gidJ globalIndexI globalIndexJ image normI(3) labI(3) labJ(3)"
+        std::ifstream in(argv[2]);
+        std::vector<gpu::ConBlockRecord> blocks;
+        gpu::ConBlockRecord b;
+        long long gI = 0, gJ = 0;
+        while (in >> b.gamma >> b.delta0 >> b.kappa >> b.bilateral >> b.oneSide >> gI >> gJ >> b.globalIndexI >>
+               b.globalIndexJ >> b.image >> b.normI[0] >> b.normI[1] >> b.normI[2] >> b.labI[0] >> b.labI[1] >>
+               b.labI[2] >> b.labJ[0] >> b.labJ[1] >> b.labJ[2]) {
+            b.gidI = (int64_t)gI;
+            b.gidJ = (int64_t)gJ;
+            blocks.push_back(b);
+        }
+        try {
+            gpu::SylinderSystem::writeConBlockVTK(argv[3], std::atoi(argv[4]), blocks);
+        } catch (const std::exception &e) {
+            std::fprintf(stderr, "%s\n", e.what());
+            return 1;
+        }
+        return 0;
     }
     if (argc == 5 && std::strcmp(argv[1], "--restart-check") == 0) {
         try {

@@ -268,17 +268,83 @@ def write_sylinder_pvtp(folder, snap_id: int, rods: RodState, group=None):
         f.write(f'</PCellData>\n<Piece Source="{piece}"/>\n</PPolyData>\n</VTKFile>\n')
 
 
+# cell data of a constraint-block piece (ConBlock_<id>.pvtp): the fields of a
+# ConstraintBlock (SRC/TubuleSystem.cpp:727-736) that describe the solved
+# block, and its pair virial gamma (labI - labJ) (x) normI as "Stress"
+_CON_CELL_FIELDS = [("gamma", "Float64", "<f8", 1), ("delta0", "Float64", "<f8", 1), ("kappa", "Float64", "<f8", 1),
+                    ("bilateral", "Int32", "<i4", 1), ("oneSide", "Int32", "<i4", 1), ("gidI", "Int64", "<i8", 1),
+                    ("gidJ", "Int64", "<i8", 1), ("globalIndexI", "Int32", "<i4", 1),
+                    ("globalIndexJ", "Int32", "<i4", 1), ("image", "Int32", "<i4", 1),
+                    ("normI", "Float64", "<f8", 3), ("Stress", "Float64", "<f8", 9)]
+
+
+def conblock_cells(blocks: dict, gid) -> dict:
+    """Cell arrays of a ConBlock piece from GpuSystem.constraint_blocks()
+    and the rods' gids (gidJ = -1 for boundary contacts)."""
+    gid = np.asarray(gid, dtype=np.int64)
+    i = np.asarray(blocks["i"], dtype=np.int64)
+    j = np.asarray(blocks["j"], dtype=np.int64)
+    r = np.asarray(blocks["labI"]) - np.asarray(blocks["labJ"])
+    n = np.asarray(blocks["normI"])
+    g = np.asarray(blocks["gamma"])
+    stress = (g[:, None, None] * r[:, :, None]) * n[:, None, :]
+    return {"gamma": g, "delta0": blocks["delta0"], "kappa": blocks["kappa"], "bilateral": blocks["bilateral"],
+            "oneSide": blocks["oneSide"], "gidI": gid[i] if i.size else i,
+            "gidJ": np.where(j >= 0, gid[np.maximum(j, 0)] if j.size else j, -1),
+            "globalIndexI": i, "globalIndexJ": j, "image": blocks["image"], "normI": n,
+            "Stress": stress.reshape(-1, 9)}
+
+
+def write_conblock_pvtp(folder, snap_id: int, blocks: dict, gid):
+    """ConBlock_<id>.pvtp and its piece ConBlock_r0_<id>.vtp in `folder` (the
+    constraint-block snapshot aLENS lists in README.md:142 and collects with
+    Run/result/Result2PVD.py:26): one line cell per block from its contact
+    point on rod I (labI) to the one on rod J or the boundary (labJ); cell
+    data as _CON_CELL_FIELDS.  The C++ facade writes the same bytes
+    (gpu::SylinderSystem::writeConBlockVTK)."""
+    import os
+    cells = conblock_cells(blocks, gid)
+    n = int(np.asarray(blocks["gamma"]).shape[0])
+    pts = np.empty((2 * n, 3))
+    pts[0::2] = np.asarray(blocks["labI"]).reshape(-1, 3)
+    pts[1::2] = np.asarray(blocks["labJ"]).reshape(-1, 3)
+    piece = f"ConBlock_r0_{snap_id}.vtp"
+    head = '<?xml version="1.0"?>\n'
+    with open(os.path.join(folder, piece), "w") as f:
+        f.write(head + '<VTKFile type="PolyData" version="1.0" byte_order="LittleEndian" header_type="UInt64">\n')
+        f.write(f'<PolyData>\n<Piece NumberOfPoints="{2 * n}" NumberOfVerts="0" NumberOfLines="{n}" '
+                'NumberOfStrips="0" NumberOfPolys="0">\n')
+        f.write("<Points>\n" + _b64_array("position", "Float64", pts.astype("<f8"), 3) + "</Points>\n")
+        f.write("<Lines>\n" + _b64_array("connectivity", "Int32", np.arange(2 * n, dtype="<i4"), 1)
+                + _b64_array("offsets", "Int32", 2 * np.arange(1, n + 1, dtype="<i4"), 1) + "</Lines>\n")
+        f.write('<CellData Scalars="scalars">\n')
+        for name, vt, dt, nc in _CON_CELL_FIELDS:
+            f.write(_b64_array(name, vt, np.asarray(cells[name]).astype(dt), nc))
+        f.write("</CellData>\n</Piece>\n</PolyData>\n</VTKFile>\n")
+    with open(os.path.join(folder, f"ConBlock_{snap_id}.pvtp"), "w") as f:
+        f.write(head + '<VTKFile type="PPolyData" version="1.0" byte_order="LittleEndian" header_type="UInt64">\n')
+        f.write('<PPolyData GhostLevel="0">\n<PPoints>\n'
+                '<PDataArray type="Float64" Name="position" NumberOfComponents="3"/>\n</PPoints>\n')
+        f.write('<PCellData Scalars="scalars">\n')
+        for name, vt, _, nc in _CON_CELL_FIELDS:
+            f.write(f'<PDataArray type="{vt}" Name="{name}" NumberOfComponents="{nc}"/>\n')
+        f.write(f'</PCellData>\n<Piece Source="{piece}"/>\n</PPolyData>\n</VTKFile>\n')
+
+
 def write_snapshot(snap_id: int, rods: RodState, step: int, time: float, root: str = "./result", links=(),
-                   group=None, info_path: str = "TimeStepInfo.txt") -> str:
-    """One aLENS snapshot: SylinderAscii_<id>.dat and Sylinder_<id>.pvtp (+ piece)
-    in result_folder(snap_id, root), then the restart bookkeeping file.
-    Returns the folder."""
+                   group=None, info_path: str = "TimeStepInfo.txt", blocks: dict | None = None) -> str:
+    """One aLENS snapshot: SylinderAscii_<id>.dat, Sylinder_<id>.pvtp (+ piece)
+    and, with `blocks` (GpuSystem.constraint_blocks() of the last step),
+    ConBlock_<id>.pvtp (+ piece) in result_folder(snap_id, root), then the
+    restart bookkeeping file.  Returns the folder."""
     import os
     folder = result_folder(snap_id, root)
     os.makedirs(folder, exist_ok=True)
     write_sylinder_ascii(os.path.join(folder, f"SylinderAscii_{snap_id}.dat"), rods, time=time, group=group,
                          links=links)
     write_sylinder_pvtp(folder, snap_id, rods, group=group)
+    if blocks is not None:
+        write_conblock_pvtp(folder, snap_id, blocks, rods.gid)
     write_time_step_info(info_path, step, snap_id, time)
     return folder
 

@@ -307,6 +307,14 @@ int alens_get_gamma(AlensCtx *ctx, int replica, int cap, int *n, int32_t *pairs,
 int alens_get_pairs(AlensCtx *ctx, int replica, int cap, int *n, int32_t *indexI, int32_t *indexJ,
                     int32_t *image);
 
+/* Lab-frame contact points of one replica's constraints, canonical order:
+ * lab[6k .. 6k+2] = point on rod I, lab[6k+3 .. 6k+5] = point on rod J (for
+ * boundary contacts, the point on the boundary surface).  The labI / labJ
+ * fields of the ConstraintBlocks (SRC/TubuleSystem.cpp:727-736) that the
+ * ConBlock_<id>.pvtp snapshots draw (README.md:142).  ALENS_CAPACITY if
+ * cap is below the constraint count. */
+int alens_get_constraint_points(AlensCtx *ctx, int replica, int cap, double *lab);
+
 /* Sum over the constraints of one replica of the pair virial
  * gamma * (lab_I - lab_J) (x) n  (3x3 row-major); the role of
  * SylinderSystem::calcConStress (SRC/TubuleSystem.cpp:224). */

@@ -144,8 +144,9 @@ def test_flexible_filament_links(gpu_lib, tmp_path):
 
 
 def test_facade_snapshot_and_restart(gpu_lib, tmp_path):
-    """writeResult() before every runStep writes SylinderAscii_<snapID>.dat
-    and Sylinder_<snapID>.pvtp (+ piece) into ./result/result0-399/ every
+    """writeResult() before every runStep writes SylinderAscii_<snapID>.dat,
+    Sylinder_<snapID>.pvtp (+ piece) and ConBlock_<snapID>.pvtp (+ piece)
+    into ./result/result0-399/ every
     round(timeSnap/dt) steps plus
     ./TimeStepInfo.txt; reinitialize from TimeStepInfo.txt restores the last
     snapshot's rods, its snapID + 1 and its step."""
@@ -165,7 +166,15 @@ def test_facade_snapshot_and_restart(gpu_lib, tmp_path):
     folder = tmp_path / "result" / "result0-399"
     names = sorted(p.name for p in folder.iterdir())
     assert [x for x in names if x.startswith("SylinderAscii_")] == [f"SylinderAscii_{i}.dat" for i in range(3)]
-    assert [x for x in names if x.endswith(".pvtp")] == [f"Sylinder_{i}.pvtp" for i in range(3)]
-    assert [x for x in names if x.endswith(".vtp")] == [f"Sylinder_r0_{i}.vtp" for i in range(3)]
-    assert len(names) == 9
+    assert [x for x in names if x.startswith("Sylinder_") and x.endswith(".pvtp")] == \
+        [f"Sylinder_{i}.pvtp" for i in range(3)]
+    assert [x for x in names if x.startswith("Sylinder_r0_")] == [f"Sylinder_r0_{i}.vtp" for i in range(3)]
+    # the constraint blocks of the last runStep beside every rod snapshot (none
+    # before the first step)
+    assert [x for x in names if x.startswith("ConBlock_") and x.endswith(".pvtp")] == \
+        [f"ConBlock_{i}.pvtp" for i in range(3)]
+    assert [x for x in names if x.startswith("ConBlock_r0_")] == [f"ConBlock_r0_{i}.vtp" for i in range(3)]
+    assert 'NumberOfLines="0"' in (folder / "ConBlock_r0_0.vtp").read_text()
+    assert 'NumberOfLines="0"' not in (folder / "ConBlock_r0_2.vtp").read_text()
+    assert len(names) == 15
     assert (tmp_path / "TimeStepInfo.txt").read_text().split()[:2] == ["4", "2"]

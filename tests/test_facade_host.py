@@ -96,3 +96,43 @@ def test_facade_vtk_writer_matches_python(tmp_path):
     io.write_sylinder_pvtp(str(py), 7, rods)
     for name in ("Sylinder_7.pvtp", "Sylinder_r0_7.vtp"):
         assert (cpp / name).read_bytes() == (py / name).read_bytes(), name
+
+
+def test_facade_conblock_writer_matches_python(tmp_path):
+    """The facade's ConBlock_<id>.pvtp / ConBlock_r0_<id>.vtp writer and the
+    Python one produce the same bytes for the same blocks: collisions, a
+    boundary contact (no rod J), crosslinker springs, and an empty set."""
+    import numpy as np
+    from alens_gb300 import io
+    rng = np.random.default_rng(3)
+    n = 40
+    gid = np.arange(100, 160, dtype=np.int64)
+    j = rng.integers(0, 60, n).astype(np.int32)
+    j[5] = -1
+    blocks = {"i": rng.integers(0, 60, n).astype(np.int32), "j": j, "image": rng.integers(0, 27, n).astype(np.int32),
+              "delta0": rng.normal(0, 0.01, n), "gamma": np.abs(rng.normal(0, 0.3, n)), "normI": rng.normal(0, 1, (n, 3)),
+              "labI": rng.uniform(0, 5, (n, 3)), "labJ": rng.uniform(0, 5, (n, 3)),
+              "kappa": np.where(np.arange(n) >= 30, 100.0, 0.0), "bilateral": (np.arange(n) >= 30).astype(np.int32),
+              "oneSide": (j < 0).astype(np.int32)}
+    build.build_lib()
+    exe = build.build_facade_driver()
+    for label, sel in (("some", np.arange(n)), ("none", np.arange(0))):
+        b = {k: np.asarray(v)[sel] for k, v in blocks.items()}
+        cells = io.conblock_cells(b, gid)
+        rec = tmp_path / f"{label}.txt"
+        with open(rec, "w") as f:
+            for k in range(sel.shape[0]):
+                vals = [cells["gamma"][k], cells["delta0"][k], cells["kappa"][k], cells["bilateral"][k],
+                        cells["oneSide"][k], cells["gidI"][k], cells["gidJ"][k], cells["globalIndexI"][k],
+                        cells["globalIndexJ"][k], cells["image"][k], *b["normI"][k], *b["labI"][k], *b["labJ"][k]]
+                f.write(" ".join(repr(float(v)) if isinstance(v, (float, np.floating)) else str(int(v))
+                                 for v in vals) + "\n")
+        cpp, py = tmp_path / f"cpp_{label}", tmp_path / f"py_{label}"
+        cpp.mkdir()
+        py.mkdir()
+        proc = subprocess.run([str(exe), "--write-conblock", str(rec), str(cpp), "4"], capture_output=True,
+                              text=True, timeout=120)
+        assert proc.returncode == 0, proc.stderr
+        io.write_conblock_pvtp(str(py), 4, b, gid)
+        for name in ("ConBlock_4.pvtp", "ConBlock_r0_4.vtp"):
+            assert (cpp / name).read_bytes() == (py / name).read_bytes(), (label, name)

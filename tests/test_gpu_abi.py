@@ -146,3 +146,43 @@ def test_solver_wait_runs_out_then_recovers(gpu_lib, precision):
     assert g.step_count() == 2
     g.close()
     o.close()
+
+
+def test_conblock_snapshot_carries_the_solve(gpu_lib, tmp_path):
+    """write_snapshot(blocks=...) writes ConBlock_<id>.pvtp whose arrays are
+    the step's constraints: multipliers, separations, crosslink stiffness, and
+    per-block stresses that sum to the replica's pair virial."""
+    import re
+    from alens_gb300 import io
+    w = workloads.small_periodic(n=1000, box=5.0, seed=3)
+    pairs_ = workloads.pair_list(capi.GpuSystem, w.cfg, w.rods, 0.05)
+    links = workloads.make_links(w.cfg, w.rods, pairs_, 100, seed=3)
+    g = capi.GpuSystem(w.cfg)
+    g.set_rods(w.rods)
+    g.set_links(links)
+    g.step()
+    blocks = g.constraint_blocks()
+    c = g.constraints()
+    pos, quat = g.get_rods()
+    rods = capi.RodState(w.rods.gid, pos, quat, w.rods.length, w.rods.radius)
+    folder = io.write_snapshot(0, rods, step=1, time=1e-4, root=str(tmp_path / "result"), blocks=blocks,
+                               info_path=str(tmp_path / "TimeStepInfo.txt"))
+    text = open(folder + "ConBlock_r0_0.vtp").read()
+
+    def arr(name, dtype):
+        m = re.search(rf'Name="{name}" NumberOfComponents="\d+" format="binary">([^<]*)<', text)
+        return io.read_vtk_binary_array(m.group(1), dtype)
+
+    n = c["gamma"].shape[0]
+    assert f'NumberOfLines="{n}"' in text
+    assert np.array_equal(arr("gamma", "<f8"), c["gamma"])
+    assert np.array_equal(arr("delta0", "<f8"), c["delta0"])
+    assert np.array_equal(arr("globalIndexI", "<i4"), c["i"])
+    kap = arr("kappa", "<f8")
+    assert np.allclose(kap[c["ncoll"]:], 100.0) and np.all(kap[:c["ncoll"]] == 0.0)
+    assert int(arr("bilateral", "<i4").sum()) == 100
+    stress = arr("Stress", "<f8").reshape(-1, 3, 3).sum(axis=0)
+    assert np.allclose(stress, g.con_stress(), rtol=1e-12, atol=1e-15)
+    pts = arr("position", "<f8").reshape(-1, 3)
+    assert np.array_equal(pts[0::2], blocks["labI"]) and np.array_equal(pts[1::2], blocks["labJ"])
+    g.close()
