@@ -36,10 +36,10 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # FP64 path that must match the oracle bit for bit: they are compiled without
 # FMA contraction.
 CU_SOURCES = ["engine.cu", "kernels_detect.cu", "kernels_assemble.cu", "kernels_solve.cu",
-              "kernels_mixed.cu", "kernels_fast.cu", "kernels_csm.cu", "kernels_mlp.cu", "mlp.cu", "kernels_noalloc.cu", "capi.cu"]
+              "kernels_mixed.cu", "kernels_fast.cu", "kernels_csm.cu", "kernels_mlp.cu", "mlp.cu", "kernels_noalloc.cu", "kernels_kmc.cu", "capi.cu"]
 CXX_SOURCES: list[str] = []
 FP_STRICT = {"kernels_detect.cu", "kernels_assemble.cu", "kernels_solve.cu", "kernels_noalloc.cu",
-             "engine.cu", "capi.cu"}
+             "kernels_kmc.cu", "engine.cu", "capi.cu"}
 
 
 def _run(cmd: list[str]) -> None:
@@ -66,13 +66,14 @@ def oracle_path() -> Path:
 
 def build_oracle(force: bool = False) -> Path:
     out = oracle_path()
-    deps = [ORACLE / "oracle.cpp", ORACLE / "oracle.h", ROOT / "include" / "alens_gpu.h"]
+    deps = [ORACLE / "oracle.cpp", ORACLE / "oracle_kmc.cpp", ORACLE / "oracle.h", ORACLE / "oracle_ctx.h",
+            ROOT / "include" / "alens_gpu.h"]
     if not force and _newer(out, deps):
         return out
     cxx = os.environ.get("CXX", "g++")
     _run([cxx, "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC",
           "-shared", "-Wall", "-Wextra", "-Wno-unused-parameter",
-          "-I", str(ROOT / "include"), str(ORACLE / "oracle.cpp"), "-o", str(out)])
+          "-I", str(ROOT / "include"), str(ORACLE / "oracle.cpp"), str(ORACLE / "oracle_kmc.cpp"), "-o", str(out)])
     return out
 
 

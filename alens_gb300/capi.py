@@ -131,6 +131,64 @@ class AlensStepStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class AlensProteinType(C.Structure):
+    """One protein species (ProteinType of Protein/ProteinType.hpp:24-76),
+    in ProteinConfig.yaml units."""
+    _fields_ = [
+        ("tag", C.c_int32),
+        ("fixedEnd0", C.c_int32),
+        ("useBindVol", C.c_int32),
+        ("lookupType", C.c_int32),
+        ("freeLength", C.c_double),
+        ("kappa", C.c_double),
+        ("lambda_", C.c_double),
+        ("PtoAPratio", C.c_double),
+        ("diffUnbound", C.c_double),
+        ("rc", C.c_double),
+        ("eps", C.c_double),
+        ("ko_s", C.c_double * 2),
+        ("ko_d", C.c_double * 2),
+        ("Ka", C.c_double * 2),
+        ("Ke", C.c_double * 2),
+    ]
+
+
+def make_protein_type(tag=0, freeLength=0.025, rc=0.025, kappa=200.0, lambda_=0.5, diffUnbound=1.0,
+                      useBindVol=False, eps=400.0, Ka=(100.0, 100.0), ko_s=(28.1, 28.1), Ke=(100.0, 100.0),
+                      ko_d=(28.1, 28.1), PtoAPratio=1.0, fixedEnd0=False, lookupType=0) -> AlensProteinType:
+    """A species; the defaults are the symmetric crosslinker of the dense
+    monolayer example (Examples/DenseMonoLayer/ProteinConfig.yaml)."""
+    t = AlensProteinType()
+    t.tag, t.fixedEnd0, t.useBindVol, t.lookupType = int(tag), int(fixedEnd0), int(useBindVol), int(lookupType)
+    t.freeLength, t.kappa, t.lambda_, t.PtoAPratio = float(freeLength), float(kappa), float(lambda_), float(PtoAPratio)
+    t.diffUnbound, t.rc, t.eps = float(diffUnbound), float(rc), float(eps)
+    for e in range(2):
+        t.ko_s[e], t.ko_d[e], t.Ka[e], t.Ke[e] = float(ko_s[e]), float(ko_d[e]), float(Ka[e]), float(Ke[e])
+    return t
+
+
+class AlensKmcStats(C.Structure):
+    _fields_ = [(k, C.c_int32) for k in ("nU", "nS", "nD", "nUS", "nSU", "nSD", "nDS", "maxCandidates")]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# AlensProtein (112 bytes) as a numpy record
+PROTEIN_DTYPE = np.dtype([("gid", "<i8"), ("type", "<i4"), ("idBind", "<i4", (2,)), ("pad", "<i4"),
+                          ("distBind", "<f8", (2,)), ("pos", "<f8", (3,)), ("posEnd", "<f8", (2, 3))])
+assert PROTEIN_DTYPE.itemsize == 112
+
+
+def protein_array(n: int) -> np.ndarray:
+    """n unbound proteins (idBind = -1, NaN geometry) to fill in."""
+    a = np.zeros(n, dtype=PROTEIN_DTYPE)
+    a["idBind"] = -1
+    a["distBind"] = np.nan
+    a["posEnd"] = np.nan
+    return a
+
+
 def make_config(box_low=(0.0, 0.0, 0.0), box_high=(5.0, 5.0, 5.0), pbc=(1, 1, 1),
                 monolayer=False, viscosity=0.01, kbt=0.00411, dt=1e-4,
                 col_ratio_d=1.0, col_ratio_l=1.0, col_buf=0.025, tol=1e-5,
@@ -230,6 +288,10 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_get_pairs": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_int), _PI32, _PI32, _PI32]),
         "alens_set_wait_limit": (C.c_int, [vp, C.c_uint64, C.c_int]),
         "alens_get_constraint_points": (C.c_int, [vp, C.c_int, C.c_int, _PD]),
+        "alens_set_protein_types": (C.c_int, [vp, C.c_int, C.POINTER(AlensProteinType), C.c_double, C.c_double]),
+        "alens_set_proteins": (C.c_int, [vp, C.c_int, C.c_int, vp]),
+        "alens_get_proteins": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_int), vp]),
+        "alens_protein_bind_step": (C.c_int, [vp, C.POINTER(AlensKmcStats)]),
         "alens_mlp_create": (C.c_int, [C.c_uint64, C.c_int64, C.POINTER(vp)]),
         "alens_mlp_destroy": (C.c_int, [vp]),
         "alens_mlp_get_params": (C.c_int, [vp, _PF]),
@@ -378,6 +440,30 @@ class GpuSystem:
         self._ck(self.lib.alens_set_links(self.h, replica, int(a[0].shape[0]), _p(a[0], C.c_int32),
                                           _p(a[1], C.c_int32), _p(a[2], C.c_double), _p(a[3], C.c_double),
                                           _p(a[4], C.c_double), _p(a[5], C.c_double)), "alens_set_links")
+
+    def set_protein_types(self, types, kbt: float = 0.00411, rod_diameter: float = 0.025):
+        arr = (AlensProteinType * max(len(types), 1))(*types)
+        self._ck(self.lib.alens_set_protein_types(self.h, len(types), arr, float(kbt), float(rod_diameter)),
+                 "alens_set_protein_types")
+
+    def set_proteins(self, proteins: np.ndarray, replica: int = 0):
+        a = np.ascontiguousarray(proteins, dtype=PROTEIN_DTYPE)
+        self._ck(self.lib.alens_set_proteins(self.h, replica, int(a.shape[0]), a.ctypes.data if a.size else None),
+                 "alens_set_proteins")
+
+    def get_proteins(self, replica: int = 0) -> np.ndarray:
+        n = C.c_int()
+        self._ck(self.lib.alens_get_proteins(self.h, replica, 0, C.byref(n), None), "alens_get_proteins",
+                 ok=(ALENS_OK, ALENS_CAPACITY))
+        a = np.zeros(n.value, dtype=PROTEIN_DTYPE)
+        self._ck(self.lib.alens_get_proteins(self.h, replica, n.value, C.byref(n), a.ctypes.data if a.size else None),
+                 "alens_get_proteins")
+        return a
+
+    def protein_bind_step(self) -> list[dict]:
+        st = (AlensKmcStats * self.nrep)()
+        self._ck(self.lib.alens_protein_bind_step(self.h, st), "alens_protein_bind_step")
+        return [st[r].as_dict() for r in range(self.nrep)]
 
     def set_boundaries(self, boundaries, replica: int = 0):
         arr = (AlensBoundary * max(len(boundaries), 1))(*boundaries)

@@ -262,6 +262,36 @@ int alens_get_constraint_points(AlensCtx *ctx, int replica, int cap, double *lab
     });
 }
 
+int alens_set_protein_types(AlensCtx *ctx, int n, const AlensProteinType *types, double KBT,
+                            double rodDiameter) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->setProteinTypes(n, types, KBT, rodDiameter);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_set_proteins(AlensCtx *ctx, int replica, int n, const AlensProtein *proteins) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->setProteins(replica, n, proteins);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_get_proteins(AlensCtx *ctx, int replica, int cap, int *n, AlensProtein *proteins) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] {
+        ctx->eng->getProteins(replica, cap, n, proteins);
+        return (int)ALENS_OK;
+    });
+}
+
+int alens_protein_bind_step(AlensCtx *ctx, AlensKmcStats *stats) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] { return ctx->eng->proteinBindStep(stats); });
+}
+
 int alens_set_wait_limit(AlensCtx *ctx, uint64_t timeoutNs, int stallBarriers) {
     if (!ctx) return ALENS_INVALID_ARG;
     return guarded_ctx(ctx, [&] {

@@ -53,6 +53,8 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     rods_.resize(R_);
     queue_.resize(R_);
     links_.resize(R_);
+    prot_.resize(R_);
+    springs_.assign(R_, 0);
     bnd_.resize(R_);
     repStats_.assign(R_, AlensStepStats{});
     if (cfg_[0].stream) {
@@ -94,6 +96,8 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     CK(cudaMallocHost(&hDyn_, sizeof(RepDyn) * R_));
     CK(cudaMallocHost(&hBilPrefix_, sizeof(int) * (R_ + 1)));
     CK(cudaMallocHost(&hLinkSlot0_, sizeof(int) * R_));
+    CK(cudaMallocHost(&hKmc_, sizeof(int) * (9 * R_ + 1)));
+    std::memset(hKmc_, 0, sizeof(int) * (9 * R_ + 1));
     std::memset(hCtl_, 0, sizeof(DevCtl));
     std::memset(hDyn_, 0, sizeof(RepDyn) * R_);
     std::memset(hBilPrefix_, 0, sizeof(int) * (R_ + 1));
@@ -115,7 +119,11 @@ Engine::~Engine() {
     if (hBlocks_) cudaFreeHost(hBlocks_);
     if (hBlockRep_) cudaFreeHost(hBlockRep_);
     if (hLinkSlot0_) cudaFreeHost(hLinkSlot0_);
+    if (hKmc_) cudaFreeHost(hKmc_);
     freeGroup(linkAllocs_);
+    freeGroup(protAllocs_);
+    freeGroup(kmcAllocs_);
+    freeGroup(kmcFixedAllocs_);
     freeGroup(bndAllocs_);
     for (int i = 0; i < 3; i++) {
         if (forkEv_[i]) cudaEventDestroy(forkEv_[i]);
@@ -607,10 +615,17 @@ void Engine::uploadLinks() {
     CK(cudaStreamSynchronize(stream_));
     invalidateGraph();
     freeGroup(linkAllocs_);
-    int total = 0;
-    for (int r = 0; r < R_; r++) total += (int)links_[r].I.size();
+    int total = 0, nprot = 0;
+    for (int r = 0; r < R_; r++) {
+        total += (int)links_[r].I.size();
+        nprot += (int)prot_[r].size();
+        springs_[r] = 0;
+    }
+    userLinkTotal_ = total;
+    // one row more per protein: the doubly bound ones become springs
+    linkCap_ = total + nprot;
     S_.nLinks = total;
-    if (total > 0) {
+    if (linkCap_ > 0) {
         std::vector<int> I(total), J(total), rep(total), loc(total);
         std::vector<double> a(total), b(total), rest(total), kap(total);
         int o = 0;
@@ -630,8 +645,8 @@ void Engine::uploadLinks() {
         }
         auto up = [&](auto *&dst, const auto &src) {
             using T = typename std::remove_reference<decltype(src[0])>::type;
-            dst = alloc<typename std::remove_const<T>::type>(linkAllocs_, total);
-            CK(cudaMemcpy(dst, src.data(), sizeof(T) * total, cudaMemcpyHostToDevice));
+            dst = alloc<typename std::remove_const<T>::type>(linkAllocs_, linkCap_);
+            if (total > 0) CK(cudaMemcpy(dst, src.data(), sizeof(T) * total, cudaMemcpyHostToDevice));
         };
         up(S_.linkI, I);
         up(S_.linkJ, J);
@@ -643,18 +658,21 @@ void Engine::uploadLinks() {
         up(S_.linkKappa, kap);
     }
     linksDirty_ = false;
+    springsDirty_ = nprot > 0;
 }
 
 // --------------------------------------------------------------- blocks
-// Per replica the blocks are [queued by alens_add_bilateral..., links...].
+// Per replica the blocks are [queued by alens_add_bilateral..., links...,
+// protein springs...].
 void Engine::uploadBlocks() {
     uploadLinks();
+    if (springsDirty_) rebuildSprings();
     uploadBoundaries();
     int total = 0;
     hBilPrefix_[0] = 0;
     for (int r = 0; r < R_; r++) {
         hLinkSlot0_[r] = total + (int)queue_[r].size();
-        total += (int)queue_[r].size() + (int)links_[r].I.size();
+        total += (int)queue_[r].size() + (int)links_[r].I.size() + springs_[r];
         hBilPrefix_[r + 1] = total;
     }
     if (total > blockCap_) {
@@ -1380,6 +1398,315 @@ void Engine::conStress(int rep, double *out9) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out9, S_.stress + 9 * (size_t)rep, sizeof(double) * 9, cudaMemcpyDeviceToHost, stream_));
     CK(cudaStreamSynchronize(stream_));
+}
+
+// ------------------------------------------------------ protein kinetics
+namespace {
+
+constexpr double kPiKmc = 3.141592653589793;
+
+bool finite_nonneg(double v) { return std::isfinite(v) && v >= 0.0; }
+
+// 4 pi int_0^inf r^2 exp(-a (r - c)^2) dr in closed form (lookupType 0:
+// c = ell0 + D), the bind volume of Protein/ProteinModel.md
+double bind_volume(double a, double c) {
+    const double G = 0.5 * std::sqrt(kPiKmc / a) * (1.0 + std::erf(c * std::sqrt(a)));
+    const double e = std::exp(-(a * (c * c)));
+    return 4.0 * kPiKmc * ((c * e) / (2.0 * a) + G * (1.0 / (2.0 * a) + c * c));
+}
+
+// The species' rates with dt folded in (ProteinType::readFromYaml unit
+// conversion, Protein/ProteinType.hpp:121-127; fixedEnd0 rule of
+// Protein/ProteinModel.md; factors of Protein/ProteinData.hpp:90-140).
+KmcType make_kmc_type(const AlensProteinType &in, double KBT, double D, double dt) {
+    KmcType T;
+    std::memset(&T, 0, sizeof(T));
+    double koS[2] = {in.ko_s[0], in.ko_s[1]}, koD[2] = {in.ko_d[0], in.ko_d[1]};
+    if (in.fixedEnd0) {
+        koS[0] = 0.0;
+        koD[0] = 0.0;
+    }
+    const double Ka[2] = {in.Ka[0] / 602.0, in.Ka[1] / 602.0};
+    const double Ke[2] = {in.useBindVol ? in.Ke[0] / 602.0 : in.Ke[0], in.useBindVol ? in.Ke[1] / 602.0 : in.Ke[1]};
+    T.ell0 = in.freeLength;
+    T.c = in.freeLength + D;
+    T.A = ((1.0 - in.lambda) * in.kappa) / (2.0 * KBT);
+    T.w = 6.0 / std::sqrt(T.A);
+    T.rOuter = T.c + T.w;
+    T.Ads = (in.lambda * in.kappa) / (2.0 * KBT);
+    const double rd = std::sqrt((6.0 * in.diffUnbound) * dt);
+    T.rcap = in.rc > rd ? in.rc : rd;
+    T.PtoAP = in.PtoAPratio;
+    const double vol = 3.0 / (4.0 * kPiKmc * ((T.rcap * T.rcap) * T.rcap));
+    const double Vb = in.useBindVol ? bind_volume(T.A, T.c) : 1.0;
+    for (int e = 0; e < 2; e++) {
+        T.usCoef[e] = (((koS[e] * Ka[e]) * in.eps) * vol) * dt;
+        T.suProb[e] = koS[e] * dt;
+        T.sdCoef[e] = (((koD[e] * Ke[e]) * in.eps) * dt) / Vb;
+        T.koD[e] = koD[e];
+    }
+    T.dt = dt;
+    T.kappa = in.kappa;
+    return T;
+}
+
+}  // namespace
+
+void Engine::setProteinTypes(int n, const AlensProteinType *t, double KBT, double D) {
+    if (n < 0 || (n > 0 && !t) || !(KBT > 0.0) || !std::isfinite(KBT) || !finite_nonneg(D))
+        throw ApiError(ALENS_INVALID_ARG);
+    for (int k = 0; k < n; k++) {
+        const AlensProteinType &p = t[k];
+        bool ok = p.lookupType == 0 && std::isfinite(p.kappa) && p.kappa > 0.0 && std::isfinite(p.lambda) &&
+                  p.lambda >= 0.0 && p.lambda < 1.0 && finite_nonneg(p.freeLength) && std::isfinite(p.rc) &&
+                  p.rc > 0.0 && finite_nonneg(p.eps) && finite_nonneg(p.diffUnbound) &&
+                  std::isfinite(p.PtoAPratio) && p.PtoAPratio > 0.0;
+        for (int e = 0; e < 2; e++)
+            ok = ok && finite_nonneg(p.ko_s[e]) && finite_nonneg(p.ko_d[e]) && finite_nonneg(p.Ka[e]) &&
+                 finite_nonneg(p.Ke[e]);
+        if (!ok) throw ApiError(ALENS_INVALID_ARG);
+    }
+    syncProteinsToHost();
+    for (const auto &v : prot_)
+        for (const AlensProtein &p : v)
+            if (p.type >= n) throw ApiError(ALENS_INVALID_ARG);
+    ptypes_.assign(t, t + n);
+    kmcKBT_ = KBT;
+    kmcD_ = D;
+    springsDirty_ = nProt_ > 0 || protUpload_;  // rest lengths and stiffness may change
+}
+
+void Engine::setProteins(int rep, int n, const AlensProtein *p) {
+    if (rep < 0 || rep >= R_ || n < 0 || (n > 0 && !p)) throw ApiError(ALENS_INVALID_ARG);
+    if (ptypes_.empty() && n > 0) throw ApiError(ALENS_NOT_READY);
+    if (n > 0 && !rods_[rep].set) throw ApiError(ALENS_NOT_READY);
+    if (haveDetect_ || haveSolve_) throw ApiError(ALENS_NOT_READY);
+    const int nr = rods_[rep].n;
+    for (int k = 0; k < n; k++) {
+        const AlensProtein &q = p[k];
+        if (q.type < 0 || q.type >= (int)ptypes_.size()) throw ApiError(ALENS_INVALID_ARG);
+        int nb = 0;
+        for (int e = 0; e < 2; e++) {
+            if (q.idBind[e] == -1) continue;
+            if (q.idBind[e] < 0 || q.idBind[e] >= nr || !std::isfinite(q.distBind[e])) throw ApiError(ALENS_INVALID_ARG);
+            nb++;
+        }
+        if (nb == 0 && !(std::isfinite(q.pos[0]) && std::isfinite(q.pos[1]) && std::isfinite(q.pos[2])))
+            throw ApiError(ALENS_INVALID_ARG);
+    }
+    int total = 0;
+    for (int r = 0; r < R_; r++) total += r == rep ? n : (int)prot_[r].size();
+    if (total > (4 << 20) - 1) throw ApiError(ALENS_INVALID_ARG);
+    syncProteinsToHost();
+    const size_t before = prot_[rep].size();
+    prot_[rep].assign(p, p + n);
+    protUpload_ = true;
+    if ((size_t)n != before) linksDirty_ = true;  // one link row per protein
+}
+
+void Engine::getProteins(int rep, int cap, int *n, AlensProtein *out) {
+    if (rep < 0 || rep >= R_ || !n || cap < 0) throw ApiError(ALENS_INVALID_ARG);
+    syncProteinsToHost();
+    const int m = (int)prot_[rep].size();
+    *n = m;
+    if (cap < m) throw ApiError(ALENS_CAPACITY);
+    if (m > 0) {
+        if (!out) throw ApiError(ALENS_INVALID_ARG);
+        std::memcpy(out, prot_[rep].data(), sizeof(AlensProtein) * m);
+    }
+}
+
+void Engine::syncProteinsToHost() {
+    if (!protDevNewer_) return;
+    CK(cudaStreamSynchronize(stream_));
+    std::vector<AlensProtein> all(nProt_);
+    if (nProt_ > 0) CK(cudaMemcpy(all.data(), K_.prot, sizeof(AlensProtein) * nProt_, cudaMemcpyDeviceToHost));
+    int o = 0;
+    for (int r = 0; r < R_; r++) {
+        std::copy(all.begin() + o, all.begin() + o + prot_[r].size(), prot_[r].begin());
+        o += (int)prot_[r].size();
+    }
+    protDevNewer_ = false;
+}
+
+void Engine::uploadProteins() {
+    if (!protUpload_) return;
+    CK(cudaStreamSynchronize(stream_));
+    int total = 0;
+    for (int r = 0; r < R_; r++) total += (int)prot_[r].size();
+    freeGroup(protAllocs_);
+    K_.prot = alloc<AlensProtein>(protAllocs_, total);
+    K_.protRep = alloc<int>(protAllocs_, total);
+    K_.dFlag = alloc<int>(protAllocs_, total + 1);
+    K_.dScan = alloc<int>(protAllocs_, total + 1);
+    std::vector<AlensProtein> all;
+    std::vector<int> rep;
+    all.reserve(total);
+    rep.reserve(total);
+    for (int r = 0; r < R_; r++) {
+        all.insert(all.end(), prot_[r].begin(), prot_[r].end());
+        rep.insert(rep.end(), prot_[r].size(), r);
+    }
+    if (total > 0) {
+        CK(cudaMemcpy(K_.prot, all.data(), sizeof(AlensProtein) * total, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(K_.protRep, rep.data(), sizeof(int) * total, cudaMemcpyHostToDevice));
+    }
+    nProt_ = total;
+    K_.nProt = total;
+    protUpload_ = false;
+    protDevNewer_ = false;
+    springsDirty_ = true;
+}
+
+// Species tables per replica, the binding grid of every replica (cell edge
+// at least the largest rod half-length plus the largest capture distance)
+// and the device buffers they size.  Needs the rods on the device.
+void Engine::prepareKmc() {
+    const int nt = (int)ptypes_.size();
+    std::vector<KmcType> types((size_t)R_ * std::max(nt, 1));
+    std::vector<KmcRep> reps(R_);
+    int cells = 0, protOff = 0, userOff = 0;
+    for (int r = 0; r < R_; r++) {
+        const RepParams &P = hostPar_[r];
+        double reachT = 0.0;
+        for (int k = 0; k < nt; k++) {
+            KmcType &T = types[(size_t)r * nt + k];
+            T = make_kmc_type(ptypes_[k], kmcKBT_, kmcD_, cfg_[r].dt);
+            reachT = std::max(reachT, std::max(T.rcap, T.rOuter));
+        }
+        double hl = 0.0;
+        for (double L : rods_[r].len) hl = std::max(hl, 0.5 * L);
+        const double reach = hl + reachT;
+        KmcRep &Q = reps[r];
+        std::memset(&Q, 0, sizeof(Q));
+        for (int d = 0; d < 3; d++) {
+            Q.lo[d] = P.lo[d];
+            Q.hi[d] = P.hi[d];
+            Q.L[d] = P.L[d];
+            Q.pbc[d] = P.pbc[d];
+            // one nearest periodic image within the reach
+            if (P.pbc[d] && !prot_[r].empty() && !(P.L[d] >= 2.0 * reach)) throw ApiError(ALENS_INVALID_ARG);
+            const double f = reach > 0.0 ? std::floor(P.L[d] / reach) : 1.0;
+            Q.ncell[d] = f < 1.0 ? 1 : (f > 512.0 ? 512 : (int)f);
+        }
+        const long long limit = std::max<long long>(64, 2LL * rods_[r].n);
+        while ((long long)Q.ncell[0] * Q.ncell[1] * Q.ncell[2] > limit) {
+            int d = 0;
+            for (int e = 1; e < 3; e++)
+                if (Q.ncell[e] > Q.ncell[d]) d = e;
+            Q.ncell[d] = std::max(1, Q.ncell[d] / 2);
+        }
+        for (int d = 0; d < 3; d++) Q.cellsz[d] = Q.L[d] / Q.ncell[d];
+        Q.cellOffset = cells;
+        cells += Q.ncell[0] * Q.ncell[1] * Q.ncell[2];
+        Q.rodOffset = P.rodOffset;
+        Q.nRods = rods_[r].n;
+        Q.protOffset = protOff;
+        Q.nProt = (int)prot_[r].size();
+        protOff += Q.nProt;
+        Q.userLinks = (int)links_[r].I.size();
+        userOff += Q.userLinks;
+        Q.seed = cfg_[r].rngSeed;
+    }
+    if (cells > (4 << 20) - 1) throw ApiError(ALENS_INVALID_ARG);
+    const int nrod = S_.nRods;
+    if (kmcFixedAllocs_.empty() || kmcTypeCap_ < (int)types.size()) {
+        freeGroup(kmcFixedAllocs_);
+        kmcTypeCap_ = (int)types.size();
+        K_.types = alloc<KmcType>(kmcFixedAllocs_, kmcTypeCap_);
+        K_.rep = alloc<KmcRep>(kmcFixedAllocs_, R_);
+        K_.stats = alloc<int>(kmcFixedAllocs_, 9 * (size_t)R_ + 1);
+        K_.dCount = K_.stats + 8 * R_;
+        K_.err = K_.stats + 9 * R_;
+    }
+    if (cells + 1 > kmcCellCap_ || nrod > kmcRodCap_) {
+        freeGroup(kmcAllocs_);
+        kmcCellCap_ = std::max(cells + 1, kmcCellCap_);
+        kmcRodCap_ = std::max(nrod, kmcRodCap_);
+        K_.cellCount = alloc<int>(kmcAllocs_, kmcCellCap_);
+        K_.cellStart = alloc<int>(kmcAllocs_, kmcCellCap_);
+        K_.cellCursor = alloc<int>(kmcAllocs_, kmcCellCap_);
+        K_.cellRod = alloc<int>(kmcAllocs_, kmcRodCap_);
+        K_.rodC = alloc<double4>(kmcAllocs_, kmcRodCap_);
+        K_.rodA = alloc<double4>(kmcAllocs_, kmcRodCap_);
+    }
+    CK(cudaMemcpyAsync((void *)K_.types, types.data(), sizeof(KmcType) * types.size(), cudaMemcpyHostToDevice,
+                       stream_));
+    CK(cudaMemcpyAsync((void *)K_.rep, reps.data(), sizeof(KmcRep) * R_, cudaMemcpyHostToDevice, stream_));
+    // the host vectors die here: the copies must be done
+    CK(cudaStreamSynchronize(stream_));
+    K_.R = R_;
+    K_.nCells = cells;
+    K_.nTypes = std::max(nt, 1);
+    K_.nProt = nProt_;
+    K_.step = stepCount_;
+    K_.D = kmcD_;
+}
+
+// the springs' counts per replica (and the step's stats) back on the host
+void Engine::readSprings(AlensKmcStats *stats) {
+    CK(cudaMemcpyAsync(hKmc_, K_.stats, sizeof(int) * (9 * R_ + 1), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    const int before = S_.nLinks;
+    int total = userLinkTotal_;
+    for (int r = 0; r < R_; r++) {
+        springs_[r] = hKmc_[8 * R_ + r];
+        total += springs_[r];
+    }
+    S_.nLinks = total;
+    if (S_.nLinks != before) invalidateGraph();
+    if (stats)
+        for (int r = 0; r < R_; r++) {
+            const int *c = hKmc_ + 8 * r;
+            stats[r] = AlensKmcStats{c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7]};
+        }
+    springsDirty_ = false;
+    if (hKmc_[9 * R_] & kKmcErrSpring) throw ApiError(ALENS_CAPACITY);
+}
+
+void Engine::rebuildSprings() {
+    uploadProteins();
+    if (nProt_ == 0) {
+        for (int r = 0; r < R_; r++) springs_[r] = 0;
+        if (S_.nLinks != userLinkTotal_) invalidateGraph();
+        S_.nLinks = userLinkTotal_;
+        springsDirty_ = false;
+        return;
+    }
+    if (ptypes_.empty()) throw ApiError(ALENS_NOT_READY);
+    prepareKmc();
+    CK(cudaMemsetAsync(K_.stats, 0, sizeof(int) * (9 * R_ + 1), stream_));
+    launches_ += launch_kmc_springs(K_, S_, userLinkTotal_, linkCap_, stream_);
+    CK(cudaGetLastError());
+    readSprings(nullptr);
+}
+
+int Engine::proteinBindStep(AlensKmcStats *stats) {
+    if (haveDetect_ || haveSolve_) throw ApiError(ALENS_NOT_READY);
+    finalize();
+    uploadLinks();
+    uploadProteins();
+    if (nProt_ == 0) {
+        rebuildSprings();
+        if (stats) std::memset(stats, 0, sizeof(AlensKmcStats) * R_);
+        return ALENS_OK;
+    }
+    if (ptypes_.empty()) throw ApiError(ALENS_NOT_READY);
+    prepareKmc();
+    CK(cudaMemsetAsync(K_.cellCount, 0, sizeof(int) * (K_.nCells + 1), stream_));
+    CK(cudaMemsetAsync(K_.cellCursor, 0, sizeof(int) * (K_.nCells + 1), stream_));
+    CK(cudaMemsetAsync(K_.stats, 0, sizeof(int) * (9 * R_ + 1), stream_));
+    launch_kmc_bin(K_, S_, stream_);
+    int n = 1 + launch_scan(K_.cellCount, K_.cellStart, K_.nCells + 1, S_.scanTmp, stream_);
+    launch_kmc_scatter(K_, S_, stream_);
+    launch_kmc_bind(K_, stream_);
+    n += 3;
+    n += launch_kmc_springs(K_, S_, userLinkTotal_, linkCap_, stream_);
+    CK(cudaGetLastError());
+    launches_ += n;
+    protDevNewer_ = true;
+    readSprings(stats);
+    return (hKmc_[9 * R_] & kKmcErrCand) ? ALENS_CAPACITY : ALENS_OK;
 }
 
 }  // namespace alens

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "kmc.cuh"
 #include "mlp.h"
 
 namespace alens {
@@ -52,6 +53,11 @@ class Engine {
     // barrier stall used to test the timeout path
     void setWaitLimit(unsigned long long timeoutNs, int stallBarriers);
     void getConstraintPoints(int rep, int cap, double *lab);
+    // protein binding kinetics (engine_kmc.cu)
+    void setProteinTypes(int n, const AlensProteinType *types, double KBT, double D);
+    void setProteins(int rep, int n, const AlensProtein *p);
+    void getProteins(int rep, int cap, int *n, AlensProtein *out);
+    int proteinBindStep(AlensKmcStats *stats);
     int detect(AlensStepStats *out);
     int solve(AlensStepStats *out);
     int advance(AlensStepStats *out);
@@ -156,7 +162,28 @@ class Engine {
     void uploadBoundaries();
     std::vector<void *> linkAllocs_;
     int *hLinkSlot0_ = nullptr;
+    int userLinkTotal_ = 0;  // rows of alens_set_links links (all replicas)
+    int linkCap_ = 0;        // link rows allocated: user links + one per protein
     void uploadLinks();
+    // proteins: host copies per replica, the device state, and the springs
+    // (doubly bound proteins) written after the user links
+    std::vector<AlensProteinType> ptypes_;
+    double kmcKBT_ = 0.0, kmcD_ = 0.0;
+    std::vector<std::vector<AlensProtein>> prot_;
+    bool protUpload_ = false;    // the host copies are newer than the device
+    bool protDevNewer_ = false;  // bind steps advanced the device past the host copies
+    bool springsDirty_ = false;  // the spring rows must be written again
+    std::vector<int> springs_;   // spring rows per replica
+    int nProt_ = 0;
+    KmcDev K_{};
+    std::vector<void *> protAllocs_, kmcAllocs_, kmcFixedAllocs_;
+    int kmcCellCap_ = 0, kmcRodCap_ = 0, kmcTypeCap_ = 0;
+    int *hKmc_ = nullptr;        // pinned: 8 x R stats, R spring counts, error flags
+    void uploadProteins();
+    void syncProteinsToHost();
+    void prepareKmc();
+    void rebuildSprings();
+    void readSprings(AlensKmcStats *stats);
     std::vector<RepParams> hostPar_;
     bool dirty_ = true;
     bool haveDetect_ = false, haveSolve_ = false;

@@ -1,0 +1,75 @@
+// kmc.cuh - device state of the protein binding step (two-stage KMC model:
+// unbound U, singly bound S, doubly bound D).
+//
+// Layout in HBM:
+//   proteins   AoS AlensProtein (112 B) + replica index, all replicas
+//              concatenated in the order they were set
+//   species    KmcType per protein type (rates folded with dt, see below)
+//   rod view   per rod (global index): wrapped centre + half-length, unit
+//              axis + sphere flag (two double4, 64 B), rebuilt each step
+//   cells      uniform grid per replica whose edge is at least the binding
+//              reach (largest rod half-length + largest capture distance):
+//              count / exclusive start / cursor per cell, rod indices by cell
+//   springs    doubly bound flag and its exclusive scan per protein; the
+//              springs are written into the context's link rows
+#pragma once
+
+#include "engine.cuh"
+
+namespace alens {
+
+// Per species: the rates of Protein/ProteinModel.md with dt folded in.
+struct KmcType {
+    double ell0;        // rest length (freeLength)
+    double c;           // head distance of zero stretch: ell0 + D (lookupType 0)
+    double A;           // (1 - lambda) kappa / (2 KBT): S->D Boltzmann exponent
+    double w;           // support half-width of the S->D integrand in head distance
+    double rOuter;      // c + w: farthest head distance with a non-zero S->D rate
+    double Ads;         // lambda kappa / (2 KBT): D->S load sensitivity
+    double rcap;        // U->S capture radius: max(rc, sqrt(6 diffUnbound dt))
+    double PtoAP;       // parallel / antiparallel S->D binding ratio
+    double usCoef[2];   // ko_s Ka eps * 3 / (4 pi rcap^3) * dt  (times L_c)
+    double suProb[2];   // ko_s dt
+    double sdCoef[2];   // ko_d Ke eps dt [/ Vb]               (times the integral)
+    double koD[2];      // ko_d
+    double dt;
+    double kappa;       // spring constant of the D-stage spring
+};
+
+struct KmcRep {
+    double lo[3], hi[3], L[3], cellsz[3];
+    int pbc[3], ncell[3];
+    int cellOffset, rodOffset, nRods, protOffset, nProt;
+    int userLinks;      // links of alens_set_links (their rows come first)
+    unsigned long long seed;
+};
+
+struct KmcDev {
+    int nProt, R, nCells, nTypes;
+    AlensProtein *prot;
+    int *protRep;
+    const KmcType *types;   // nTypes per replica (dt is per replica)
+    const KmcRep *rep;
+    double4 *rodC;      // wrapped centre, half-length
+    double4 *rodA;      // axis, 1 for a sphere-shaped rod
+    int *cellCount, *cellStart, *cellCursor, *cellRod;
+    int *dFlag, *dScan;  // nProt + 1 each
+    int *stats;          // 8 per replica: nU nS nD nUS nSU nSD nDS maxCand
+    int *dCount;         // doubly bound proteins per replica
+    int *err;
+    long long step;
+    double D;
+};
+
+constexpr int kKmcMaxCand = 64;     // candidate rods one protein may weigh in a step
+constexpr int kKmcErrCand = 1;      // a protein had more candidates (its state is kept)
+constexpr int kKmcErrSpring = 2;    // a spring row fell outside the link capacity
+
+void launch_kmc_bin(const KmcDev &K, const DevState &S, cudaStream_t st);
+void launch_kmc_scatter(const KmcDev &K, const DevState &S, cudaStream_t st);
+void launch_kmc_bind(const KmcDev &K, cudaStream_t st);
+// doubly bound flags, their scan and the spring rows at link offset
+// userTotal (capacity linkCap); dCount per replica
+int launch_kmc_springs(const KmcDev &K, const DevState &S, int userTotal, int linkCap, cudaStream_t st);
+
+}  // namespace alens

@@ -11,8 +11,8 @@ import ctypes as C
 import numpy as np
 
 from . import build as _build
-from .capi import (ALENS_NOT_CONVERGED, ALENS_OK, AlensBlock, AlensBoundary, AlensConfig, AlensError,
-                   AlensStepStats, RodState, _p)
+from .capi import (ALENS_CAPACITY, ALENS_NOT_CONVERGED, ALENS_OK, PROTEIN_DTYPE, AlensBlock, AlensBoundary,
+                   AlensConfig, AlensError, AlensKmcStats, AlensProteinType, AlensStepStats, RodState, _p)
 
 _PD = C.POINTER(C.c_double)
 _PI32 = C.POINTER(C.c_int32)
@@ -59,6 +59,18 @@ def load_oracle(rebuild: bool = True) -> C.CDLL:
         "orc_normals6": (None, [C.c_uint64, C.c_int64, C.c_int64, _PD]),
         "orc_canon_sum": (C.c_double, [_PD, C.c_int64]),
         "orc_mobility": (None, [C.c_double, C.c_double, C.c_double, _PD]),
+        "orc_set_protein_types": (C.c_int, [vp, C.c_int, C.POINTER(AlensProteinType), C.c_double, C.c_double]),
+        "orc_set_proteins": (C.c_int, [vp, C.c_int, vp]),
+        "orc_get_proteins": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), vp]),
+        "orc_protein_bind_step": (C.c_int, [vp, C.POINTER(AlensKmcStats)]),
+        "orc_kmc_exp": (C.c_double, [C.c_double]),
+        "orc_kmc_sd_integral": (C.c_double, [C.POINTER(AlensProteinType), C.c_double, C.c_double, C.c_double,
+                                             C.c_double, C.c_double, C.c_double]),
+        "orc_kmc_sd_invert": (C.c_double, [C.POINTER(AlensProteinType), C.c_double, C.c_double, C.c_double,
+                                           C.c_double, C.c_double, C.c_double, C.c_double]),
+        "orc_kmc_bind_volume": (C.c_double, [C.POINTER(AlensProteinType), C.c_double, C.c_double]),
+        "orc_kmc_binding_factor_sd": (C.c_double, [C.POINTER(AlensProteinType), C.c_int, _PD, _PD]),
+        "orc_kmc_type_constants": (None, [C.POINTER(AlensProteinType), C.c_double, C.c_double, C.c_double, _PD]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -120,6 +132,38 @@ def mobility(length: float, radius: float, viscosity: float):
     out = np.empty(3)
     load_oracle().orc_mobility(float(length), float(radius), float(viscosity), _p(out, C.c_double))
     return out
+
+
+def kmc_exp(x: float) -> float:
+    return load_oracle().orc_kmc_exp(float(x))
+
+
+def kmc_sd_integral(ptype: AlensProteinType, kbt: float, d: float, dt: float, d2: float, sA: float,
+                    sB: float) -> float:
+    return load_oracle().orc_kmc_sd_integral(C.byref(ptype), kbt, d, dt, d2, sA, sB)
+
+
+def kmc_sd_invert(ptype: AlensProteinType, kbt: float, d: float, dt: float, d2: float, sA: float, sB: float,
+                  target: float) -> float:
+    return load_oracle().orc_kmc_sd_invert(C.byref(ptype), kbt, d, dt, d2, sA, sB, target)
+
+
+def kmc_bind_volume(ptype: AlensProteinType, kbt: float, d: float) -> float:
+    return load_oracle().orc_kmc_bind_volume(C.byref(ptype), kbt, d)
+
+
+def kmc_binding_factor_sd(ptype: AlensProteinType, end: int, dir_bound, dir_rod) -> float:
+    a = np.ascontiguousarray(dir_bound, dtype=np.float64)
+    b = np.ascontiguousarray(dir_rod, dtype=np.float64)
+    return load_oracle().orc_kmc_binding_factor_sd(C.byref(ptype), int(end), _p(a, C.c_double), _p(b, C.c_double))
+
+
+def kmc_type_constants(ptype: AlensProteinType, kbt: float, d: float, dt: float) -> dict:
+    out = np.zeros(12)
+    load_oracle().orc_kmc_type_constants(C.byref(ptype), kbt, d, dt, _p(out, C.c_double))
+    keys = ("rcap", "rOuter", "A", "w", "usCoef0", "usCoef1", "suProb0", "suProb1", "sdCoef0", "sdCoef1",
+            "koD0", "koD1")
+    return dict(zip(keys, out.tolist()))
 
 
 def _ck(rc, where, ok=(ALENS_OK,)):
@@ -191,6 +235,29 @@ class OracleSystem:
         _ck(self.lib.orc_set_links(self.h, int(a[0].shape[0]), _p(a[0], C.c_int32), _p(a[1], C.c_int32),
                                    _p(a[2], C.c_double), _p(a[3], C.c_double), _p(a[4], C.c_double),
                                    _p(a[5], C.c_double)), "orc_set_links")
+
+    def set_protein_types(self, types, kbt: float = 0.00411, rod_diameter: float = 0.025):
+        arr = (AlensProteinType * max(len(types), 1))(*types)
+        _ck(self.lib.orc_set_protein_types(self.h, len(types), arr, float(kbt), float(rod_diameter)),
+            "orc_set_protein_types")
+
+    def set_proteins(self, proteins: np.ndarray):
+        a = np.ascontiguousarray(proteins, dtype=PROTEIN_DTYPE)
+        _ck(self.lib.orc_set_proteins(self.h, int(a.shape[0]), a.ctypes.data if a.size else None),
+            "orc_set_proteins")
+
+    def get_proteins(self) -> np.ndarray:
+        n = C.c_int()
+        _ck(self.lib.orc_get_proteins(self.h, 0, C.byref(n), None), "orc_get_proteins", ok=(ALENS_OK, ALENS_CAPACITY))
+        a = np.zeros(n.value, dtype=PROTEIN_DTYPE)
+        _ck(self.lib.orc_get_proteins(self.h, n.value, C.byref(n), a.ctypes.data if a.size else None),
+            "orc_get_proteins")
+        return a
+
+    def protein_bind_step(self) -> dict:
+        st = AlensKmcStats()
+        _ck(self.lib.orc_protein_bind_step(self.h, C.byref(st)), "orc_protein_bind_step")
+        return st.as_dict()
 
     def set_boundaries(self, boundaries):
         arr = (AlensBoundary * max(len(boundaries), 1))(*boundaries)

@@ -217,3 +217,54 @@ def config_with(cfg: AlensConfig, **changes) -> AlensConfig:
 __all__ = ["Workload", "small_periodic", "dense_monolayer", "crosslinked_bundle_rods", "large_eval",
            "ensemble", "axis_to_quat", "quat_to_axis", "nematic_order_2d", "config_with", "pair_list",
            "make_links", "segment_closest_params", "PREC_FP64", "WARM_ZERO"]
+
+
+def protein_population(cfg, rods, n: int, frac_single: float = 0.3, frac_double: float = 0.2, seed: int = 0,
+                       pairs=None, ntypes: int = 1, near: float = 0.02) -> np.ndarray:
+    """n proteins over a rod configuration: a fraction singly bound (one head
+    at a random arc position of a random rod), a fraction doubly bound (heads
+    at the closest points of random near pairs, moved along each rod by up
+    to ``near``; needs ``pairs`` from pair_list) and the rest unbound, half
+    of them within ``near`` of a random rod point (so that they can bind)
+    and half uniform in the box.  Types cycle over ``ntypes`` species; gids
+    are 10^6 + index."""
+    from .capi import protein_array
+    rng = np.random.default_rng(seed)
+    a = quat_to_axis(rods.quat)
+    lo = np.array([cfg.simBoxLow[d] for d in range(3)])
+    hi = np.array([cfg.simBoxHigh[d] for d in range(3)])
+    p = protein_array(n)
+    p["gid"] = 1_000_000 + np.arange(n)
+    p["type"] = np.arange(n) % max(ntypes, 1)
+    nd = int(n * frac_double) if pairs is not None and pairs[0].shape[0] > 0 else 0
+    ns = int(n * frac_single)
+    nu = n - nd - ns
+    # unbound
+    half = nu // 2
+    r = rng.integers(0, rods.n, half)
+    s = rng.uniform(-0.5, 0.5, half) * rods.length[r]
+    off = rng.normal(size=(half, 3))
+    off *= (near * rng.uniform(0, 1, half) / np.linalg.norm(off, axis=1))[:, None]
+    p["pos"][:half] = rods.pos[r] + s[:, None] * a[r] + off
+    p["pos"][half:nu] = lo + rng.uniform(0, 1, (nu - half, 3)) * (hi - lo)
+    if cfg.monolayer:
+        p["pos"][:nu, 2] = rods.pos[0, 2] + rng.uniform(-near, near, nu)
+    # singly bound
+    r = rng.integers(0, rods.n, ns)
+    p["idBind"][nu:nu + ns, 0] = r
+    p["distBind"][nu:nu + ns, 0] = rng.uniform(-0.5, 0.5, ns) * rods.length[r]
+    # doubly bound
+    if nd:
+        pi, pj, pimg = pairs
+        pick = rng.integers(0, pi.shape[0], nd)
+        i, j, img = pi[pick], pj[pick], pimg[pick]
+        box = hi - lo
+        shift = np.stack([img // 9 - 1, (img // 3) % 3 - 1, img % 3 - 1], axis=1) * box
+        hI, hJ = 0.5 * rods.length[i], 0.5 * rods.length[j]
+        s, t = segment_closest_params(rods.pos[i], a[i], hI, rods.pos[j] + shift, a[j], hJ)
+        o = nu + ns
+        p["idBind"][o:, 0] = i
+        p["idBind"][o:, 1] = j
+        p["distBind"][o:, 0] = np.clip(s + rng.uniform(-near, near, nd), -hI, hI)
+        p["distBind"][o:, 1] = np.clip(t + rng.uniform(-near, near, nd), -hJ, hJ)
+    return p

@@ -456,6 +456,99 @@ int alens_get_launch_count(AlensCtx *ctx, int64_t *count);
  * same choices by hand when a context is created. */
 int alens_autotune(AlensCtx *ctx, int reps, char *report, int reportCap);
 
+/* ------------------------------------------------------------------------
+ * Protein binding kinetics (the two-stage KMC model: unbound U, singly
+ * bound S, doubly bound D; Protein/ProteinModel.md "The Binding/Unbinding
+ * probabilities and rates in KMC").
+ * ---------------------------------------------------------------------- */
+
+/* One protein species.  Replaces ProteinType (Protein/ProteinType.hpp:24-76)
+ * as read by ProteinType::readFromYaml (:81-129): the same YAML keys, in the
+ * same units (um, pN, s; Ka in (uM)^-1; Ke in (uM)^-1 when useBindVol, else
+ * a number per binding site).  The library applies readFromYaml's
+ * conversion (Ka /= 602, Ke /= 602 when useBindVol) and, for fixedEnd0, the
+ * rule of Protein/ProteinModel.md ("When fixedEnd0==true": ko_s[0] =
+ * ko_d[0] = 0).  Only lookupType 0 (stretch length = head distance - rod
+ * diameter) is supported; lookupType 1 is rejected (the reference marks it
+ * as not to be used, Protein/ProteinType.hpp:162-164).  The walking and
+ * diffusion fields of ProteinType belong to the motion step, which this
+ * library does not run. */
+typedef struct AlensProteinType {
+    int32_t tag;
+    int32_t fixedEnd0;
+    int32_t useBindVol;
+    int32_t lookupType;   /* must be 0 */
+    double freeLength;    /* rest length ell0, um */
+    double kappa;         /* spring constant, pN/um */
+    double lambda;        /* unbinding load sensitivity */
+    double PtoAPratio;    /* parallel / antiparallel S->D binding ratio */
+    double diffUnbound;   /* um^2/s, sets the capture radius floor */
+    double rc;            /* capture radius, um */
+    double eps;           /* binding sites per um of rod */
+    double ko_s[2], ko_d[2], Ka[2], Ke[2];
+} AlensProteinType;
+
+/* One protein (the binding part of ProteinData / ProteinBindStatus,
+ * Protein/ProteinBindStatus.hpp:35-85).  idBind[e] is the index (within the
+ * replica) of the rod head e is bound to, or -1 (ID_UB); distBind[e] is the
+ * head's distance from that rod's centre along its axis, in
+ * [-length/2, length/2].  pos is the protein centre: the free point of an
+ * unbound protein (input and output), the bound head of a singly bound one
+ * and the midpoint of the heads of a doubly bound one (output).  posEnd[e]
+ * is head e's lab-frame position (output; NaN when unbound). */
+typedef struct AlensProtein {
+    int64_t gid;
+    int32_t type;         /* index into the species table */
+    int32_t idBind[2];
+    int32_t pad;
+    double distBind[2];
+    double pos[3];
+    double posEnd[2][3];
+} AlensProtein;
+
+/* Counts of one replica after a binding step: proteins per stage and the
+ * transitions taken in the step. */
+typedef struct AlensKmcStats {
+    int32_t nU, nS, nD;
+    int32_t nUS, nSU, nSD, nDS;
+    int32_t maxCandidates;  /* most rods any protein could bind to this step */
+} AlensKmcStats;
+
+/* The species table of the context (all replicas) with the protein
+ * temperature KBT (ProteinConfig KBT, pN um) and the rod diameter D
+ * (RunConfig sylinderDiameter, um) that the binding rates use.  Replaces
+ * ProteinConfig's type list (Protein/ProteinConfig.cpp:6-45) and
+ * TubuleSystem::buildLookupTable (SRC/TubuleSystem.cpp:583-629): the S->D
+ * binding integral is evaluated by quadrature, not tabulated.  Invalidates
+ * no protein; proteins must refer to existing types at the next step. */
+int alens_set_protein_types(AlensCtx *ctx, int n, const AlensProteinType *types, double KBT,
+                            double rodDiameter);
+
+/* The proteins of one replica (TubuleSystem::setInitialProteinFromFile /
+ * readProteinVTK, SRC/TubuleSystem.cpp:761-872).  Bound heads must name a
+ * rod of the replica (ALENS_INVALID_ARG otherwise); pos of a bound protein
+ * is recomputed from its heads.  Doubly bound proteins are bilateral
+ * springs of the next step (rest length freeLength + rodDiameter, stiffness
+ * kappa), after the replica's alens_set_links links.  n = 0 removes them. */
+int alens_set_proteins(AlensCtx *ctx, int replica, int n, const AlensProtein *proteins);
+
+/* The current proteins of one replica, in the order they were set.  cap too
+ * small: ALENS_CAPACITY with *n set. */
+int alens_get_proteins(AlensCtx *ctx, int replica, int cap, int *n, AlensProtein *proteins);
+
+/* One KMC binding step of every protein of every replica on the current rod
+ * state: U -> S, S -> U, S -> D and D -> S with the rates of
+ * Protein/ProteinModel.md, one event at most per protein (the choice rule
+ * of SRC/kmc_step_funcs.hpp:35-230), then the doubly bound proteins become
+ * the replica's protein springs for the next alens_step.  Replaces
+ * TubuleSystem::calcBindInteraction + setProteinConstraints
+ * (SRC/TubuleSystem.cpp:232-259, 694-745) and CalcProteinBind::operator()
+ * (SRC/CalcProteinBind.hpp:59-173).  The random numbers are Philox4x32-10
+ * keyed by (rngSeed, protein gid, step count), so a step is reproducible
+ * and independent of the device.  stats (nullable) receives one record per
+ * replica.  Not between alens_detect and alens_advance (ALENS_NOT_READY). */
+int alens_protein_bind_step(AlensCtx *ctx, AlensKmcStats *stats);
+
 /* CUDA-event times (ms) of the stages of the last step when stageTiming is
  * on: ms[0] detect, ms[1] main solve kernel (FP32 kernel in mixed mode),
  * ms[2] FP64 refinement (mixed mode; 0 otherwise), ms[3] advance,

@@ -38,6 +38,7 @@
 // so for identical inputs the two agree bit for bit.
 
 #include "oracle.h"
+#include "oracle_ctx.h"
 
 #include <algorithm>
 #include <cmath>
@@ -452,48 +453,7 @@ inline uint64_t pair_key(int64_t i, int64_t j, int img) {
 }  // namespace
 
 // ------------------------------------------------------------------ context
-struct OrcCtx {
-    AlensConfig cfg;
-    int n = 0;
-    std::vector<int64_t> gid;
-    std::vector<double> pos, quat, len, rad;
-    std::vector<int32_t> imm;
-    double cutoff = 0.0;
-    int ncell[3] = {1, 1, 1};
-    double cellsz[3] = {1, 1, 1};
-    // per-step rod data
-    std::vector<double> axis, hcol, rcol, mob, unc, vel;
-    std::vector<uint8_t> sph;
-    // constraints
-    int ncoll = 0, nbil = 0;
-    std::vector<int32_t> ci, cj, cimg;
-    std::vector<double> jac, phi0, q, gamma, cinv, lb, lab;
-    std::vector<uint8_t> unil;
-    std::vector<AlensBlock> queue, blocks;
-    // confinement boundaries (unit axes)
-    struct Bnd {
-        int type, inside;
-        double c[3], a[3], R;
-    };
-    std::vector<Bnd> bnd;
-    // pre-bound crosslinkers: blocks built from the rod state every step
-    std::vector<int> linkI, linkJ;
-    std::vector<double> linkSI, linkSJ, linkRest, linkKappa;
-    // rod-major rows: entries 2k+side, ascending
-    std::vector<int64_t> rowptr;
-    std::vector<int64_t> rowent;
-    // Delassus operator rows (ascending column)
-    std::vector<int64_t> aptr;
-    std::vector<int> acol;
-    std::vector<double> aval;
-    // warm start
-    std::vector<uint64_t> prevKeys;
-    std::vector<double> prevGamma;
-    std::vector<double> initGammaOverride;
-    int64_t step = 0;
-    bool detected = false, solved = false;
-    AlensStepStats last{};
-};
+// struct OrcCtx: oracle_ctx.h
 
 namespace {
 
@@ -770,11 +730,10 @@ void build_constraints(OrcCtx *x) {
     x->ncoll = (int)keys.size();
     x->blocks = x->queue;
     x->queue.clear();
-    // link blocks after the queued ones: anchors P = c_I + sI a_I,
+    // link blocks after the queued ones (the alens_set_links links, then the
+    // springs of doubly bound proteins): anchors P = c_I + sI a_I,
     // Q = c_J + sJ a_J, d = P - Q reduced to the minimum image
-    for (size_t L = 0; L < x->linkI.size(); L++) {
-        const int I = x->linkI[L], J = x->linkJ[L];
-        const double sI = x->linkSI[L], sJ = x->linkSJ[L];
+    auto add_link = [&](int I, int J, double sI, double sJ, double rest, double kappa) {
         const double *aI = &x->axis[3 * I], *aJ = &x->axis[3 * J];
         const double pI[3] = {x->pos[3 * I] + sI * aI[0], x->pos[3 * I + 1] + sI * aI[1],
                               x->pos[3 * I + 2] + sI * aI[2]};
@@ -797,9 +756,9 @@ void build_constraints(OrcCtx *x) {
         }
         AlensBlock B;
         std::memset(&B, 0, sizeof(B));
-        const double delta0 = len - x->linkRest[L];
+        const double delta0 = len - rest;
         B.delta0 = delta0;
-        B.gamma = -delta0 * x->linkKappa[L];
+        B.gamma = -delta0 * kappa;
         B.gidI = x->gid[I];
         B.gidJ = x->gid[J];
         B.globalIndexI = I;
@@ -813,9 +772,15 @@ void build_constraints(OrcCtx *x) {
             B.labJ[cc] = pI[cc] - d[cc];
         }
         B.bilateral = 1;
-        B.kappa = x->linkKappa[L];
+        B.kappa = kappa;
         x->blocks.push_back(B);
-    }
+    };
+    for (size_t L = 0; L < x->linkI.size(); L++)
+        add_link(x->linkI[L], x->linkJ[L], x->linkSI[L], x->linkSJ[L], x->linkRest[L], x->linkKappa[L]);
+    kmc_springs(x);
+    for (size_t L = 0; L < x->springI.size(); L++)
+        add_link(x->springI[L], x->springJ[L], x->springSI[L], x->springSJ[L], x->springRest[L],
+                 x->springKappa[L]);
     x->nbil = (int)x->blocks.size();
     const int nc = x->ncoll + x->nbil;
     x->ci.assign(nc, -1);

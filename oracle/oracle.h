@@ -55,6 +55,22 @@ int orc_get_solver_data(OrcCtx *ctx, int cap, double *q, double *diag);
 int orc_get_operator(OrcCtx *ctx, int capNnz, int *nnz, int32_t *rowPtr, int32_t *cols, double *vals);
 int orc_set_threads(int nthreads);
 
+/* Protein binding step (oracle_kmc.cpp), mirroring alens_set_protein_types,
+ * alens_set_proteins, alens_get_proteins and alens_protein_bind_step. */
+int orc_set_protein_types(OrcCtx *ctx, int n, const AlensProteinType *types, double KBT, double rodDiameter);
+int orc_set_proteins(OrcCtx *ctx, int n, const AlensProtein *proteins);
+int orc_get_proteins(OrcCtx *ctx, int cap, int *n, AlensProtein *proteins);
+int orc_protein_bind_step(OrcCtx *ctx, AlensKmcStats *stats);
+double orc_kmc_exp(double x);
+double orc_kmc_sd_integral(const AlensProteinType *t, double KBT, double D, double dt, double d2, double sA,
+                           double sB);
+double orc_kmc_sd_invert(const AlensProteinType *t, double KBT, double D, double dt, double d2, double sA,
+                         double sB, double target);
+double orc_kmc_bind_volume(const AlensProteinType *t, double KBT, double D);
+double orc_kmc_binding_factor_sd(const AlensProteinType *t, int end, const double dirBound[3],
+                                 const double dirRod[3]);
+void orc_kmc_type_constants(const AlensProteinType *t, double KBT, double D, double dt, double out[12]);
+
 /* Building blocks exposed for known-answer tests. */
 void orc_dcp(const double c1[3], const double u1[3], double h1,
              const double c2[3], const double u2[3], double h2,

@@ -1,0 +1,309 @@
+"""The oracle's restatement of the protein binding step (oracle/oracle_kmc.cpp),
+checked on the CPU.
+
+* The one known answer the reference ships for this path,
+  Protein/ProteinTest.hpp:33-71 ("Parallel to Anti-parallel binding
+  affinity"): with PtoAPratio = 0.5 the S->D binding factor towards a rod
+  parallel to the bound rod, over the factor towards an antiparallel one,
+  is 0.5 within 1e-6 (mock protein of Protein/ProteinType.hpp:171-188).
+* The S->D integral and its inverse against scipy's adaptive quadrature,
+  the bind volume against a numerical integral, the exp against numpy.
+* The event frequencies of whole steps against the rates of
+  Protein/ProteinModel.md (binomial bounds), the binding-point
+  distributions against the chord and the Boltzmann integrand, and the
+  springs the doubly bound proteins become.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from alens_gb300 import capi, workloads
+from alens_gb300 import oracle_api as oa
+
+integrate = pytest.importorskip("scipy.integrate")
+
+KBT = 0.00411
+D = 0.025
+
+
+def mock_type(**kw):
+    """ProteinType::setMockProteinType (Protein/ProteinType.hpp:171-188)."""
+    base = dict(Ka=(1.0, 1.0), Ke=(1.0, 1.0), ko_s=(1.0, 1.0), ko_d=(1.0, 1.0), kappa=1.0, eps=1.0, rc=0.5,
+                freeLength=1.0, lambda_=0.0, PtoAPratio=1.0, diffUnbound=0.0)
+    base.update(kw)
+    return capi.make_protein_type(**base)
+
+
+def test_ptoap_ratio_known_answer():
+    """Protein/ProteinTest.hpp:33-71: bound rod along x (MockSylinder,
+    :19-31), head 0 bound, free end 1; para / antipara factor = PtoAPratio."""
+    t = mock_type(PtoAPratio=0.5)
+    x = np.array([1.0, 0.0, 0.0])
+    para = oa.kmc_binding_factor_sd(t, 1, x, x)
+    anti = oa.kmc_binding_factor_sd(t, 1, x, -x)
+    assert abs(0.5 - para / anti) < 1e-6
+    # the other branch: PtoAPratio > 1 scales the antiparallel factor
+    t2 = mock_type(PtoAPratio=2.0)
+    assert abs(2.0 - oa.kmc_binding_factor_sd(t2, 1, x, x) / oa.kmc_binding_factor_sd(t2, 1, x, -x)) < 1e-6
+    # the prefactor never exceeds 1 (Protein/ProteinData.hpp:123)
+    assert oa.kmc_binding_factor_sd(t2, 1, x, x) == 1.0
+    # fixedEnd0: the end-0 turnover rates are zero
+    t3 = mock_type(fixedEnd0=True)
+    assert oa.kmc_binding_factor_sd(t3, 0, x, x) == 0.0
+
+
+def test_type_constants_follow_the_model():
+    t = capi.make_protein_type(ko_s=(3.0, 4.0), Ka=(60.2, 120.4), Ke=(6.02, 2.0), ko_d=(5.0, 6.0), eps=400.0,
+                               rc=0.03, diffUnbound=1.0, kappa=200.0, lambda_=0.25)
+    dt = 1e-4
+    c = oa.kmc_type_constants(t, KBT, D, dt)
+    rcap = max(0.03, math.sqrt(6 * 1.0 * dt))
+    assert c["rcap"] == pytest.approx(rcap, rel=1e-15)
+    # (Lc / 2rc)(3 Ka / (4 pi rc^3))(2 rc eps) ko_s dt = Lc * usCoef
+    assert c["usCoef0"] == pytest.approx(3.0 * (60.2 / 602) * 400 * 3 / (4 * math.pi * rcap ** 3) * dt, rel=1e-14)
+    assert c["usCoef1"] == pytest.approx(4.0 * (120.4 / 602) * 400 * 3 / (4 * math.pi * rcap ** 3) * dt, rel=1e-14)
+    assert c["suProb0"] == pytest.approx(3.0 * dt, rel=1e-15)
+    # useBindVol false: Ke is a number per site
+    assert c["sdCoef1"] == pytest.approx(6.0 * 2.0 * 400 * dt, rel=1e-14)
+    assert c["A"] == pytest.approx(0.75 * 200.0 / (2 * KBT), rel=1e-15)
+    assert c["rOuter"] == pytest.approx(0.025 + D + 6 / math.sqrt(c["A"]), rel=1e-15)
+
+
+def _integrand(t, d2, s):
+    A = (1 - t.lambda_) * t.kappa / (2 * KBT)
+    return math.exp(-A * (math.sqrt(d2 + s * s) - t.freeLength - D) ** 2)
+
+
+@pytest.mark.parametrize("d,sA,sB", [(0.0, -0.5, 0.5), (0.03, -0.5, 0.5), (0.049, -0.2, 0.7), (0.06, 0.01, 0.4),
+                                     (0.08, -0.3, -0.02), (0.1, -1.0, 1.0), (0.02, 0.05, 0.06), (0.04, -0.02, 0.02)])
+@pytest.mark.parametrize("kappa,lam", [(200.0, 0.5), (300.0, 0.25822), (50.0, 0.0)])
+def test_sd_integral_and_inverse_against_adaptive_quadrature(d, sA, sB, kappa, lam):
+    t = capi.make_protein_type(kappa=kappa, lambda_=lam, freeLength=0.025)
+    d2 = d * d
+    got = oa.kmc_sd_integral(t, KBT, D, 1e-5, d2, sA, sB)
+    pts = [p for p in (-math.sqrt(max((0.05) ** 2 - d2, 0.0)), 0.0, math.sqrt(max(0.05 ** 2 - d2, 0.0)))
+           if sA < p < sB]
+    ref, _ = integrate.quad(lambda s: _integrand(t, d2, s), sA, sB, points=pts or None, epsabs=0.0,
+                            epsrel=1e-13, limit=500)
+    assert abs(got - ref) <= 1e-10 * max(ref, 1e-300) + 1e-16, (got, ref)
+    if ref > 1e-12:
+        for u in (0.0, 0.1, 0.5, 0.9, 0.999):
+            s = oa.kmc_sd_invert(t, KBT, D, 1e-5, d2, sA, sB, u * got)
+            assert sA <= s <= sB
+            part, _ = integrate.quad(lambda x: _integrand(t, d2, x), sA, s, epsabs=0.0, epsrel=1e-13, limit=500)
+            assert abs(part - u * got) <= 1e-9 * got, (u, part, u * got)
+
+
+def test_bind_volume_closed_form():
+    for kappa, lam, ell0 in ((200.0, 0.5, 0.025), (300.0, 0.25822, 0.053), (1.0, 0.0, 1.0)):
+        t = capi.make_protein_type(kappa=kappa, lambda_=lam, freeLength=ell0)
+        a = (1 - lam) * kappa / (2 * KBT)
+        c = ell0 + D
+        ref, _ = integrate.quad(lambda r: 4 * math.pi * r * r * math.exp(-a * (r - c) ** 2), 0, c + 40 / math.sqrt(a),
+                                epsabs=0.0, epsrel=1e-13, limit=500)
+        assert oa.kmc_bind_volume(t, KBT, D) == pytest.approx(ref, rel=1e-12)
+
+
+def test_exp_accuracy():
+    x = np.concatenate([np.linspace(-745.0, 709.0, 20001), np.linspace(-1, 1, 2001), [0.0, -0.0, 1e-300]])
+    got = np.array([oa.kmc_exp(v) for v in x])
+    ref = np.exp(x)
+    normal = ref > 2.3e-308
+    rel = np.abs(got[normal] - ref[normal]) / ref[normal]
+    assert rel.max() <= 4e-16, rel.max()
+    assert oa.kmc_exp(0.0) == 1.0
+    assert oa.kmc_exp(-800.0) == 0.0 and math.isinf(oa.kmc_exp(800.0))
+
+
+# ----------------------------------------------------------- whole steps
+def _one_rod_system(dt=1e-4, length=1.0, extra=None):
+    cfg = capi.make_config(box_high=(4.0, 4.0, 4.0), pbc=(1, 1, 1), dt=dt)
+    pos = [[2.0, 2.0, 2.0]]
+    ax = [[1.0, 0.0, 0.0]]
+    if extra is not None:
+        pos.append(extra[0])
+        ax.append(extra[1])
+    n = len(pos)
+    rods = capi.RodState(np.arange(n, dtype=np.int64), np.array(pos), workloads.axis_to_quat(np.array(ax)),
+                         np.full(n, length), np.full(n, 0.0125))
+    o = oa.OracleSystem(cfg)
+    o.set_rods(rods)
+    return o, cfg
+
+
+def _binom_ok(k, n, p, z=5.0):
+    mu = n * p
+    sd = math.sqrt(max(n * p * (1 - p), 1e-12))
+    return abs(k - mu) <= z * sd + 1
+
+
+def test_unbound_binding_frequency_and_chord():
+    t = capi.make_protein_type(rc=0.05, diffUnbound=0.0, ko_s=(50.0, 30.0), Ka=(0.05, 0.05), eps=400.0)
+    o, cfg = _one_rod_system()
+    o.set_protein_types([t], KBT, D)
+    n = 40000
+    p = capi.protein_array(n)
+    p["gid"] = np.arange(n)
+    d = 0.03                      # distance of the protein from the axis
+    p["pos"] = [2.1, 2.0 + d, 2.0]
+    o.set_proteins(p)
+    st = o.protein_bind_step()
+    c = oa.kmc_type_constants(t, KBT, D, cfg.dt)
+    Lc = 2 * math.sqrt(0.05 ** 2 - d * d)
+    P0, P1 = Lc * c["usCoef0"], Lc * c["usCoef1"]
+    assert P0 + P1 < 1
+    q = o.get_proteins()
+    b0 = int(np.sum(q["idBind"][:, 0] == 0))
+    b1 = int(np.sum(q["idBind"][:, 1] == 0))
+    assert st["nUS"] == b0 + b1 and st["nS"] == b0 + b1
+    assert _binom_ok(b0, n, P0) and _binom_ok(b1, n, P1)
+    # binding points uniform on the chord [0.1 - Lc/2, 0.1 + Lc/2]
+    s = np.concatenate([q["distBind"][q["idBind"][:, 0] == 0, 0], q["distBind"][q["idBind"][:, 1] == 0, 1]])
+    assert s.min() >= 0.1 - Lc / 2 - 1e-12 and s.max() <= 0.1 + Lc / 2 + 1e-12
+    stats = pytest.importorskip("scipy.stats")
+    assert stats.kstest((s - (0.1 - Lc / 2)) / Lc, "uniform").pvalue > 1e-4
+    o.close()
+
+
+def test_single_to_double_frequency_and_positions():
+    """Rod 0 along x at the origin of the box centre; rod 1 parallel at
+    distance 0.06 (the bound head at the centre of rod 0)."""
+    t = capi.make_protein_type(ko_s=(0.0, 0.0), ko_d=(100.0, 100.0), Ke=(0.5, 0.5), eps=400.0, kappa=200.0,
+                               lambda_=0.5, PtoAPratio=0.5)
+    o, cfg = _one_rod_system(extra=([2.1, 2.06, 2.0], [1.0, 0.0, 0.0]))
+    o.set_protein_types([t], KBT, D)
+    n = 40000
+    p = capi.protein_array(n)
+    p["gid"] = np.arange(n)
+    p["idBind"][:, 0] = 0
+    p["distBind"][:, 0] = 0.0
+    o.set_proteins(p)
+    st = o.protein_bind_step()
+    c = oa.kmc_type_constants(t, KBT, D, cfg.dt)
+    # foot of the head on rod 1: t0 = -0.1 from its centre; rod half-length 0.5
+    I = oa.kmc_sd_integral(t, KBT, D, cfg.dt, 0.06 ** 2, -0.5 + 0.1, 0.5 + 0.1)
+    P = 0.5 * c["sdCoef1"] * I      # parallel rods: PtoAPratio prefactor
+    q = o.get_proteins()
+    k = int(np.sum(q["idBind"][:, 1] == 1))
+    assert st["nSD"] == k and st["nSU"] == 0
+    assert _binom_ok(k, n, P), (k, n * P)
+    # the bound points follow the integrand: CDF from scipy
+    s = q["distBind"][q["idBind"][:, 1] == 1, 1] + 0.1     # arc from the foot
+
+    def cdf(x):
+        v, _ = integrate.quad(lambda y: _integrand(t, 0.06 ** 2, y), -0.4, x, epsrel=1e-10, limit=200)
+        return v / I
+
+    stats = pytest.importorskip("scipy.stats")
+    assert stats.kstest(s, np.vectorize(cdf)).pvalue > 1e-4
+    o.close()
+
+
+def test_unbinding_frequencies_and_release():
+    t = capi.make_protein_type(ko_s=(300.0, 100.0), ko_d=(80.0, 40.0), Ka=(0.0, 0.0), Ke=(0.0, 0.0), rc=0.04,
+                               lambda_=0.0, diffUnbound=0.0)
+    o, cfg = _one_rod_system(extra=([2.0, 2.05, 2.0], [1.0, 0.0, 0.0]))
+    o.set_protein_types([t], KBT, D)
+    n = 30000
+    p = capi.protein_array(n)
+    p["gid"] = np.arange(n)
+    p["idBind"][: n // 3, 0] = 0                      # S, head 0
+    p["distBind"][: n // 3, 0] = 0.2
+    p["idBind"][n // 3: 2 * n // 3, 1] = 0            # S, head 1
+    p["distBind"][n // 3: 2 * n // 3, 1] = -0.2
+    p["idBind"][2 * n // 3:, 0] = 0                   # D
+    p["idBind"][2 * n // 3:, 1] = 1
+    p["distBind"][2 * n // 3:, 0] = 0.0
+    p["distBind"][2 * n // 3:, 1] = 0.0
+    o.set_proteins(p)
+    o.protein_bind_step()
+    q = o.get_proteins()
+    m = n // 3
+    su0 = int(np.sum(q["idBind"][:m, 0] == -1))
+    su1 = int(np.sum(q["idBind"][m:2 * m, 1] == -1))
+    assert _binom_ok(su0, m, 300.0 * cfg.dt) and _binom_ok(su1, m, 100.0 * cfg.dt)
+    # released within the capture radius of the head
+    rel = q["pos"][:m][q["idBind"][:m, 0] == -1] - np.array([2.2, 2.0, 2.0])
+    assert np.all(np.linalg.norm(rel, axis=1) <= 0.04 + 1e-12)
+    dd = q[2 * m:]
+    ds0 = int(np.sum((dd["idBind"][:, 0] == -1)))
+    ds1 = int(np.sum((dd["idBind"][:, 1] == -1)))
+    assert _binom_ok(ds0, m, 80.0 * cfg.dt) and _binom_ok(ds1, m, 40.0 * cfg.dt)
+    assert not np.any((dd["idBind"][:, 0] == -1) & (dd["idBind"][:, 1] == -1))
+    o.close()
+
+
+def test_load_dependent_unbinding():
+    """lambda > 0: ko_d exp(lambda kappa (l - D - ell0)^2 / (2 kT))
+    (Protein/ProteinData.hpp:132-140)."""
+    lam, kappa, ell0 = 0.4, 100.0, 0.02
+    t = capi.make_protein_type(ko_s=(0.0, 0.0), ko_d=(5.0, 5.0), Ka=(0.0, 0.0), Ke=(0.0, 0.0), lambda_=lam,
+                               kappa=kappa, freeLength=ell0)
+    sep = 0.07
+    o, cfg = _one_rod_system(extra=([2.0, 2.0 + sep, 2.0], [1.0, 0.0, 0.0]))
+    o.set_protein_types([t], KBT, D)
+    n = 40000
+    p = capi.protein_array(n)
+    p["gid"] = np.arange(n)
+    p["idBind"][:, 0] = 0
+    p["idBind"][:, 1] = 1
+    p["distBind"][:] = 0.0
+    o.set_proteins(p)
+    st = o.protein_bind_step()
+    rate = 5.0 * math.exp(lam * kappa * (sep - D - ell0) ** 2 / (2 * KBT))
+    assert _binom_ok(st["nDS"], n, 2 * rate * cfg.dt)
+    o.close()
+
+
+def test_doubly_bound_proteins_become_springs():
+    w = workloads.small_periodic(n=300, box=3.0, seed=2)
+    pairs = workloads.pair_list(oa.OracleSystem, w.cfg, w.rods, 0.05)
+    t = capi.make_protein_type(kappa=150.0, freeLength=0.03)
+    prots = workloads.protein_population(w.cfg, w.rods, 500, pairs=pairs, seed=2)
+    o = oa.OracleSystem(w.cfg)
+    o.set_rods(w.rods)
+    o.set_protein_types([t], KBT, D)
+    o.set_proteins(prots)
+    o.detect()
+    c = o.constraints()
+    nd = int(np.sum((prots["idBind"][:, 0] >= 0) & (prots["idBind"][:, 1] >= 0)))
+    nb = c["gamma"].shape[0] - c["ncoll"]
+    assert nd > 0 and nb == nd
+    dd = prots[(prots["idBind"][:, 0] >= 0) & (prots["idBind"][:, 1] >= 0)]
+    assert np.array_equal(c["i"][c["ncoll"]:], dd["idBind"][:, 0])
+    assert np.array_equal(c["j"][c["ncoll"]:], dd["idBind"][:, 1])
+    # delta0 = head distance - (freeLength + D), gamma0 = -kappa delta0
+    a = workloads.quat_to_axis(w.rods.quat)
+    box = np.array([w.cfg.simBoxHigh[k] - w.cfg.simBoxLow[k] for k in range(3)])
+    P = w.rods.pos[dd["idBind"][:, 0]] + dd["distBind"][:, :1] * a[dd["idBind"][:, 0]]
+    Q = w.rods.pos[dd["idBind"][:, 1]] + dd["distBind"][:, 1:] * a[dd["idBind"][:, 1]]
+    dv = P - Q
+    dv -= box * np.floor(dv / box + 0.5)
+    assert np.allclose(c["delta0"][c["ncoll"]:], np.linalg.norm(dv, axis=1) - 0.055, atol=1e-12)
+    o.close()
+
+
+def test_invalid_protein_input_is_rejected():
+    o, _ = _one_rod_system()
+    p = capi.protein_array(1)
+    with pytest.raises(capi.AlensError):
+        o.set_proteins(p)                      # no species yet
+    with pytest.raises(capi.AlensError):
+        o.set_protein_types([capi.make_protein_type(lookupType=1)])
+    with pytest.raises(capi.AlensError):
+        o.set_protein_types([capi.make_protein_type(lambda_=1.0)])
+    o.set_protein_types([capi.make_protein_type()])
+    p["pos"] = [1.0, 1.0, 1.0]
+    bad = p.copy()
+    bad["type"] = 1
+    with pytest.raises(capi.AlensError):
+        o.set_proteins(bad)
+    bad = p.copy()
+    bad["idBind"][0, 0] = 5
+    bad["distBind"][0, 0] = 0.0
+    with pytest.raises(capi.AlensError):
+        o.set_proteins(bad)
+    o.set_proteins(p)
+    assert o.protein_bind_step()["nU"] == 1
+    o.close()
