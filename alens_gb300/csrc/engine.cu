@@ -165,6 +165,7 @@ void Engine::setRods(int rep, int n, const int64_t *gid, const double *pos, cons
     h.quat.assign(quat, quat + 4 * (size_t)n);
     h.len.assign(len, len + n);
     h.rad.assign(rad, rad + n);
+    for (int i = 0; i < n; i++) h.hlMax = std::max(h.hlMax, 0.5 * len[i]);
     h.imm.assign(n, 0);
     if (imm)
         for (int i = 0; i < n; i++) h.imm[i] = imm[i] ? 1 : 0;
@@ -1447,6 +1448,19 @@ KmcType make_kmc_type(const AlensProteinType &in, double KBT, double D, double d
     }
     T.dt = dt;
     T.kappa = in.kappa;
+    T.rcapf = (float)T.rcap;
+    T.rOuterf = (float)T.rOuter;
+    T.wf = (float)T.w;
+    T.Af = (float)T.A;
+    T.cf = (float)T.c;
+    for (int e = 0; e < 2; e++) {
+        T.usCoeff[e] = (float)T.usCoef[e];
+        T.suProbf[e] = (float)T.suProb[e];
+        T.sdCoeff[e] = (float)T.sdCoef[e];
+    }
+    const float r = (float)in.PtoAPratio;
+    T.prefPar = r < 1.0f ? r : 1.0f;
+    T.prefAnti = r > 1.0f ? 1.0f / r : 1.0f;
     return T;
 }
 
@@ -1539,6 +1553,7 @@ void Engine::uploadProteins() {
     K_.protRep = alloc<int>(protAllocs_, total);
     K_.dFlag = alloc<int>(protAllocs_, total + 1);
     K_.dScan = alloc<int>(protAllocs_, total + 1);
+    K_.task = alloc<float4>(protAllocs_, 3 * (size_t)total);
     std::vector<AlensProtein> all;
     std::vector<int> rep;
     all.reserve(total);
@@ -1574,9 +1589,7 @@ void Engine::prepareKmc() {
             T = make_kmc_type(ptypes_[k], kmcKBT_, kmcD_, cfg_[r].dt);
             reachT = std::max(reachT, std::max(T.rcap, T.rOuter));
         }
-        double hl = 0.0;
-        for (double L : rods_[r].len) hl = std::max(hl, 0.5 * L);
-        const double reach = hl + reachT;
+        const double reach = rods_[r].hlMax + reachT;
         KmcRep &Q = reps[r];
         std::memset(&Q, 0, sizeof(Q));
         for (int d = 0; d < 3; d++) {
@@ -1589,14 +1602,20 @@ void Engine::prepareKmc() {
             const double f = reach > 0.0 ? std::floor(P.L[d] / reach) : 1.0;
             Q.ncell[d] = f < 1.0 ? 1 : (f > 512.0 ? 512 : (int)f);
         }
+        // at most max(64, 2 n) cells; a periodic side keeps two cells at
+        // least (with one, an offset would not name one image)
         const long long limit = std::max<long long>(64, 2LL * rods_[r].n);
         while ((long long)Q.ncell[0] * Q.ncell[1] * Q.ncell[2] > limit) {
-            int d = 0;
-            for (int e = 1; e < 3; e++)
-                if (Q.ncell[e] > Q.ncell[d]) d = e;
-            Q.ncell[d] = std::max(1, Q.ncell[d] / 2);
+            int d = -1;
+            for (int e = 0; e < 3; e++)
+                if (Q.ncell[e] > (Q.pbc[e] ? 2 : 1) && (d < 0 || Q.ncell[e] > Q.ncell[d])) d = e;
+            if (d < 0) break;
+            Q.ncell[d] = std::max(Q.pbc[d] ? 2 : 1, Q.ncell[d] / 2);
         }
-        for (int d = 0; d < 3; d++) Q.cellsz[d] = Q.L[d] / Q.ncell[d];
+        for (int d = 0; d < 3; d++) {
+            Q.cellsz[d] = Q.L[d] / Q.ncell[d];
+            Q.cellszf[d] = (float)Q.cellsz[d];
+        }
         Q.cellOffset = cells;
         cells += Q.ncell[0] * Q.ncell[1] * Q.ncell[2];
         Q.rodOffset = P.rodOffset;
@@ -1610,7 +1629,10 @@ void Engine::prepareKmc() {
     }
     if (cells > (4 << 20) - 1) throw ApiError(ALENS_INVALID_ARG);
     const int nrod = S_.nRods;
+    bool kmcAllocsFresh = false;
     if (kmcFixedAllocs_.empty() || kmcTypeCap_ < (int)types.size()) {
+        kmcAllocsFresh = true;
+        CK(cudaStreamSynchronize(stream_));
         freeGroup(kmcFixedAllocs_);
         kmcTypeCap_ = (int)types.size();
         K_.types = alloc<KmcType>(kmcFixedAllocs_, kmcTypeCap_);
@@ -1620,6 +1642,7 @@ void Engine::prepareKmc() {
         K_.err = K_.stats + 9 * R_;
     }
     if (cells + 1 > kmcCellCap_ || nrod > kmcRodCap_) {
+        CK(cudaStreamSynchronize(stream_));
         freeGroup(kmcAllocs_);
         kmcCellCap_ = std::max(cells + 1, kmcCellCap_);
         kmcRodCap_ = std::max(nrod, kmcRodCap_);
@@ -1627,14 +1650,25 @@ void Engine::prepareKmc() {
         K_.cellStart = alloc<int>(kmcAllocs_, kmcCellCap_);
         K_.cellCursor = alloc<int>(kmcAllocs_, kmcCellCap_);
         K_.cellRod = alloc<int>(kmcAllocs_, kmcRodCap_);
-        K_.rodC = alloc<double4>(kmcAllocs_, kmcRodCap_);
-        K_.rodA = alloc<double4>(kmcAllocs_, kmcRodCap_);
+        K_.rodC = alloc<KDouble4>(kmcAllocs_, kmcRodCap_);
+        K_.rodA = alloc<KDouble4>(kmcAllocs_, kmcRodCap_);
+        K_.cellRel = alloc<float4>(kmcAllocs_, kmcRodCap_);
+        K_.cellAx = alloc<float4>(kmcAllocs_, kmcRodCap_);
     }
-    CK(cudaMemcpyAsync((void *)K_.types, types.data(), sizeof(KmcType) * types.size(), cudaMemcpyHostToDevice,
-                       stream_));
-    CK(cudaMemcpyAsync((void *)K_.rep, reps.data(), sizeof(KmcRep) * R_, cudaMemcpyHostToDevice, stream_));
-    // the host vectors die here: the copies must be done
-    CK(cudaStreamSynchronize(stream_));
+    // upload the tables when they changed (the host copies stay alive until
+    // the next upload, which first waits for the stream)
+    const bool sameT = kmcTypesUp_.size() == types.size() &&
+                       std::memcmp(kmcTypesUp_.data(), types.data(), sizeof(KmcType) * types.size()) == 0;
+    const bool sameR = kmcRepsUp_.size() == reps.size() &&
+                       std::memcmp(kmcRepsUp_.data(), reps.data(), sizeof(KmcRep) * reps.size()) == 0;
+    if (!sameT || !sameR || kmcAllocsFresh) {
+        CK(cudaStreamSynchronize(stream_));
+        kmcTypesUp_ = std::move(types);
+        kmcRepsUp_ = std::move(reps);
+        CK(cudaMemcpyAsync((void *)K_.types, kmcTypesUp_.data(), sizeof(KmcType) * kmcTypesUp_.size(),
+                           cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync((void *)K_.rep, kmcRepsUp_.data(), sizeof(KmcRep) * R_, cudaMemcpyHostToDevice, stream_));
+    }
     K_.R = R_;
     K_.nCells = cells;
     K_.nTypes = std::max(nt, 1);

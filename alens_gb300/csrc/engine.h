@@ -93,6 +93,7 @@ class Engine {
     struct HostRods {
         int n = 0;
         bool set = false;
+        double hlMax = 0.0;  // largest half-length
         std::vector<long long> gid;
         std::vector<double> pos, quat, len, rad;
         std::vector<int> imm;
@@ -179,6 +180,8 @@ class Engine {
     std::vector<void *> protAllocs_, kmcAllocs_, kmcFixedAllocs_;
     int kmcCellCap_ = 0, kmcRodCap_ = 0, kmcTypeCap_ = 0;
     int *hKmc_ = nullptr;        // pinned: 8 x R stats, R spring counts, error flags
+    std::vector<KmcType> kmcTypesUp_;  // the species and replica tables on the device
+    std::vector<KmcRep> kmcRepsUp_;
     void uploadProteins();
     void syncProteinsToHost();
     void prepareKmc();

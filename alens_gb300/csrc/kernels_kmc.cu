@@ -30,25 +30,28 @@
 // submodule, absent from the checkout).  Here it is evaluated by composite
 // 8-point Gauss-Legendre quadrature over the integrand's support: head
 // distances within w = 6/sqrt(A) of ell0 + D (outside, the integrand is
-// below e^-36), split into at most two arcs and into panels of w/4.
+// below e^-36), split into at most two arcs and into panels of w/4; the
+// integrand in FP32 (relative error of the integral ~1e-6, against ~1e-3
+// for a 256 x 256 table), edges, sums and probabilities in FP64.
 //
-// Arithmetic: FP64 with IEEE +,-,*,/,sqrt only (no FMA contraction: this
-// file is compiled with --fmad=false), the project's own exp (Cody-Waite
-// reduction by ln 2, Taylor polynomial to r^13), Philox4x32-10 rolls keyed
-// by (seed, protein gid, step).  The CPU oracle states the same operations,
+// Arithmetic: IEEE +,-,*,/,sqrt only (no FMA contraction: this file is
+// compiled with --fmad=false) and the project's own exp in FP64 and FP32
+// (Cody-Waite reduction by ln 2, Taylor polynomials to r^13 / r^8),
+// Philox4x32-10 rolls keyed by (seed, protein gid, step).  The CPU oracle states the same operations,
 // so both produce the same protein states bit for bit.
 #include "kmc.cuh"
 
 namespace alens {
 namespace {
 
-// Gauss-Legendre on [-1, 1], 8 points: roots of P_8 and their weights
-__constant__ double kGLx[8] = {-0.9602898564975362, -0.7966664774136267, -0.525532409916329,
-                               -0.18343464249564978, 0.18343464249564978, 0.525532409916329,
-                               0.7966664774136267,  0.9602898564975362};
-__constant__ double kGLw[8] = {0.10122853629037706, 0.22238103445337443, 0.3137066458778869,
-                               0.36268378337836166, 0.36268378337836166, 0.3137066458778869,
-                               0.22238103445337443, 0.10122853629037706};
+// Gauss-Legendre on [-1, 1], 8 points: roots of P_8 and their weights,
+// rounded to FP32
+__constant__ float kGLx[8] = {
+    -0.9602898359298706f, -0.7966665029525757f, -0.5255324244499207f, -0.1834346354007721f,
+    0.1834346354007721f,  0.5255324244499207f,  0.7966665029525757f,  0.9602898359298706f};
+__constant__ float kGLw[8] = {
+    0.10122853517532349f, 0.22238104045391083f, 0.313706636428833f, 0.3626837730407715f,
+    0.3626837730407715f,  0.313706636428833f,   0.22238104045391083f, 0.10122853517532349f};
 
 // e^x: x = k ln2 + r, |r| <= ln2/2, ln2 split into a 24-bit head (k ln2_hi
 // exact) and the tail; e^r by its Taylor polynomial to r^13 (remainder
@@ -85,103 +88,28 @@ __device__ double kmc_exp(double x) {
     return p * __longlong_as_double((long long)(ki + 1023) << 52);
 }
 
-__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
-__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
-
-// one Gauss-Legendre panel of the S->D integrand over s in [a, b]
-__device__ double sd_panel(double a, double b, double d2, double A, double c) {
-    const double h = 0.5 * (b - a), m = 0.5 * (a + b);
-    double acc = 0.0;
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const double s = m + h * kGLx[k];
-        const double x = sqrt(d2 + s * s) - c;
-        acc = acc + kGLw[k] * kmc_exp(-(A * (x * x)));
-    }
-    return h * acc;
+// FP32 e^x for the S->D integrand: the same reduction with ln2 split into
+// 0.693145751953125 (15 significant bits, k ln2_hi exact for |k| < 2^9) and
+// its tail, Taylor polynomial to r^8 (remainder below 3e-10); results below
+// e^-87 flush to zero
+__device__ float kmc_expf(float x) {
+    if (!(x == x)) return x;
+    if (x < -87.0f) return 0.0f;
+    if (x > 88.0f) return __uint_as_float(0x7f800000u);
+    const float k = floorf(x * 1.4426950216293335f + 0.5f);
+    const float r = (x - k * 0.693145751953125f) - k * 1.428606765330187e-06f;
+    float p = 2.4801587642286904e-05f;
+    p = p * r + 0.00019841270113829523f;
+    p = p * r + 0.0013888889225199819f;
+    p = p * r + 0.008333333767950535f;
+    p = p * r + 0.0416666679084301f;
+    p = p * r + 0.1666666716337204f;
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    return p * __uint_as_float((unsigned)((int)k + 127) << 23);
 }
 
-// the integrand's support within [sA, sB]: |s| in [sl, sh], at most two arcs
-__device__ int sd_support(double d2, double sA, double sB, const KmcType &T, double lo[2], double hi[2]) {
-    const double ro2 = T.rOuter * T.rOuter;
-    if (!(d2 < ro2)) return 0;
-    const double sh = sqrt(ro2 - d2);
-    const double ri = T.c - T.w;
-    const double sl = (ri > 0.0 && ri * ri > d2) ? sqrt(ri * ri - d2) : 0.0;
-    int n = 0;
-    double l = dmax(sA, -sh), h = dmin(sB, -sl);
-    if (h > l) {
-        lo[n] = l;
-        hi[n] = h;
-        n++;
-    }
-    l = dmax(sA, sl);
-    h = dmin(sB, sh);
-    if (h > l) {
-        lo[n] = l;
-        hi[n] = h;
-        n++;
-    }
-    return n;
-}
-
-__device__ __forceinline__ int sd_npanel(double len, double w) {
-    const double q = ceil(len / (0.25 * w));
-    return q < 1.0 ? 1 : (q > 64.0 ? 64 : (int)q);
-}
-
-__device__ __forceinline__ double sd_edge(double lo, double hi, int k, int n) {
-    return k == n ? hi : lo + ((hi - lo) * (double)k) / (double)n;
-}
-
-__device__ double sd_integral(double d2, double sA, double sB, const KmcType &T) {
-    double lo[2], hi[2];
-    const int ni = sd_support(d2, sA, sB, T, lo, hi);
-    double Q = 0.0;
-    for (int i = 0; i < ni; i++) {
-        const int n = sd_npanel(hi[i] - lo[i], T.w);
-        double a = lo[i];
-        for (int k = 1; k <= n; k++) {
-            const double b = sd_edge(lo[i], hi[i], k, n);
-            Q = Q + sd_panel(a, b, d2, T.A, T.c);
-            a = b;
-        }
-    }
-    return Q;
-}
-
-// the s at which the integral from the support start reaches target
-// (0 <= target < the full integral): panel by the running sum, then 60
-// bisections of the panel's partial integral
-__device__ double sd_invert(double d2, double sA, double sB, const KmcType &T, double target) {
-    double lo[2], hi[2];
-    const int ni = sd_support(d2, sA, sB, T, lo, hi);
-    double cum = 0.0, last = sA;
-    for (int i = 0; i < ni; i++) {
-        const int n = sd_npanel(hi[i] - lo[i], T.w);
-        double a = lo[i];
-        for (int k = 1; k <= n; k++) {
-            const double b = sd_edge(lo[i], hi[i], k, n);
-            const double P = sd_panel(a, b, d2, T.A, T.c);
-            if (target < cum + P) {
-                const double t = target - cum;
-                double x0 = a, x1 = b;
-                for (int it = 0; it < 60; it++) {
-                    const double xm = 0.5 * (x0 + x1);
-                    if (sd_panel(a, xm, d2, T.A, T.c) < t)
-                        x0 = xm;
-                    else
-                        x1 = xm;
-                }
-                return 0.5 * (x0 + x1);
-            }
-            cum = cum + P;
-            a = b;
-            last = b;
-        }
-    }
-    return last;
-}
 
 // Philox block b of protein gid at step: counter (gid, step, 'kmc' + b)
 __device__ __forceinline__ void kmc_words(unsigned long long seed, long long gid, long long step, uint32_t b,
@@ -232,39 +160,6 @@ __device__ __forceinline__ void kmc_wrap_point(const KmcRep &Q, double p[3]) {
         if (Q.pbc[d]) p[d] = kmc_wrap(p[d], Q.lo[d], Q.hi[d], Q.L[d]);
 }
 
-// x - c reduced to the minimum image
-__device__ __forceinline__ void kmc_rel(const KmcRep &Q, const double x[3], const double4 &c, double u[3]) {
-    u[0] = x[0] - c.x;
-    u[1] = x[1] - c.y;
-    u[2] = x[2] - c.z;
-    for (int d = 0; d < 3; d++)
-        if (Q.pbc[d]) u[d] = u[d] - Q.L[d] * floor(u[d] / Q.L[d] + 0.5);
-}
-
-// the distinct cells of the 3x3x3 stencil around cell c
-template <class F>
-__device__ void kmc_for_cells(const KmcRep &Q, const int c[3], F &&f) {
-    int lo[3], hi[3];
-    for (int d = 0; d < 3; d++) {
-        const int n = Q.ncell[d];
-        if (Q.pbc[d]) {
-            lo[d] = n >= 3 ? -1 : 0;
-            hi[d] = n >= 3 ? 1 : n - 1;
-        } else {
-            lo[d] = c[d] > 0 ? -1 : 0;
-            hi[d] = c[d] < n - 1 ? 1 : 0;
-        }
-    }
-    for (int dz = lo[2]; dz <= hi[2]; dz++)
-        for (int dy = lo[1]; dy <= hi[1]; dy++)
-            for (int dx = lo[0]; dx <= hi[0]; dx++) {
-                int cc[3] = {c[0] + dx, c[1] + dy, c[2] + dz};
-                for (int d = 0; d < 3; d++)
-                    if (Q.pbc[d]) cc[d] = (cc[d] + Q.ncell[d]) % Q.ncell[d];
-                f(Q.cellOffset + (cc[2] * Q.ncell[1] + cc[1]) * Q.ncell[0] + cc[0]);
-            }
-}
-
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }
 
 // rod view and cell counts
@@ -278,8 +173,8 @@ __global__ void k_kmc_bin(KmcDev K, DevState S) {
         quat_axis(S.qx[r], S.qy[r], S.qz[r], S.qw[r], a);
         const double L = S.len[r];
         const bool sphere = L < 2.0 * S.rad[r];
-        K.rodC[r] = make_double4(p[0], p[1], p[2], 0.5 * L);
-        K.rodA[r] = make_double4(a[0], a[1], a[2], sphere ? 1.0 : 0.0);
+        K.rodC[r] = make_kd4(p[0], p[1], p[2], 0.5 * L);
+        K.rodA[r] = make_kd4(a[0], a[1], a[2], sphere ? 1.0 : 0.0);
         int c[3];
         for (int d = 0; d < 3; d++) c[d] = kmc_cell_coord(p[d], Q.lo[d], Q.cellsz[d], Q.ncell[d]);
         atomicAdd(&K.cellCount[Q.cellOffset + (c[2] * Q.ncell[1] + c[1]) * Q.ncell[0] + c[0]], 1);
@@ -290,183 +185,434 @@ __global__ void k_kmc_scatter(KmcDev K, DevState S) {
     ALENS_PDL_PROLOGUE();
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const KmcRep &Q = K.rep[S.rodRep[r]];
-        const double4 C = K.rodC[r];
+        const KDouble4 C = K.rodC[r];
         const double p[3] = {C.x, C.y, C.z};
         int c[3];
         for (int d = 0; d < 3; d++) c[d] = kmc_cell_coord(p[d], Q.lo[d], Q.cellsz[d], Q.ncell[d]);
         const int cid = Q.cellOffset + (c[2] * Q.ncell[1] + c[1]) * Q.ncell[0] + c[0];
-        K.cellRod[K.cellStart[cid] + atomicAdd(&K.cellCursor[cid], 1)] = r;
+        const int slot = K.cellStart[cid] + atomicAdd(&K.cellCursor[cid], 1);
+        // FP32 screening geometry: centre relative to its cell's origin
+        float rel[3];
+        for (int d = 0; d < 3; d++) rel[d] = (float)(p[d] - (Q.lo[d] + (double)c[d] * Q.cellsz[d]));
+        const KDouble4 A = K.rodA[r];
+        K.cellRod[slot] = r;
+        K.cellRel[slot] = make_float4(rel[0], rel[1], rel[2], (float)C.w);
+        K.cellAx[slot] = make_float4((float)A.x, (float)A.y, (float)A.z, (float)A.w);
     }
 }
 
-// candidate list of one protein, ascending local rod index
-struct KmcCands {
-    int n;
-    bool overflow;
-    int li[kKmcMaxCand];
-    double v0[kKmcMaxCand], v1[kKmcMaxCand], v2[kKmcMaxCand], v3[kKmcMaxCand];
+// ---- S->D integral, FP32 (the FP64 pipe of GB300 issues a warp
+// instruction in 64 cycles, the FP32 pipe in one; a rate needs no more)
+__device__ __forceinline__ float fmaxf_(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float fminf_(float a, float b) { return a < b ? a : b; }
 
-    __device__ void insert(int l, double a, double b, double c, double d) {
-        if (n == kKmcMaxCand) {
-            overflow = true;
-            return;
-        }
-        int k = n;
-        while (k > 0 && li[k - 1] > l) {
-            li[k] = li[k - 1];
-            v0[k] = v0[k - 1];
-            v1[k] = v1[k - 1];
-            v2[k] = v2[k - 1];
-            v3[k] = v3[k - 1];
-            k--;
-        }
-        li[k] = l;
-        v0[k] = a;
-        v1[k] = b;
-        v2[k] = c;
-        v3[k] = d;
-        n++;
+// one Gauss-Legendre panel of the integrand over s in [a, b]
+__device__ float sd_panel(float a, float b, float d2, float A, float c) {
+    const float h = 0.5f * (b - a), m = 0.5f * (a + b);
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const float s = m + h * kGLx[k];
+        const float x = sqrtf(d2 + s * s) - c;
+        acc = acc + kGLw[k] * kmc_expf(-(A * (x * x)));
     }
+    return h * acc;
+}
+
+// per-candidate constants of the integral
+struct SdGeom {
+    float d2, A, c;
+    float lo[2], hi[2], step[2];
+    int n[2];
 };
 
-// the candidate j whose slice of the stacked probabilities p[] (times
-// scale) holds roll, and the roll's fraction within that slice
-__device__ int kmc_pick(const KmcCands &C, const double *p, double scale, double roll, double *frac) {
-    double cum = 0.0;
-    for (int j = 0; j < C.n; j++) {
-        const double pj = p[j] * scale;
-        const double nc = cum + pj;
-        if (roll < nc || j == C.n - 1) {
-            double f = pj > 0.0 ? (roll - cum) / pj : 0.0;
-            *frac = f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f);
-            return j;
-        }
-        cum = nc;
+// the integrand's support within [sA, sB]: head distances within w of c,
+// |s| in [sl, sh]; at most two arcs, each cut into panels of at most w/4
+__device__ __forceinline__ void sd_geom(float d2, float sA, float sB, const KmcType &T, SdGeom &G) {
+    const float rO = T.rOuterf, w = T.wf;
+    G.d2 = d2;
+    G.A = T.Af;
+    G.c = T.cf;
+    G.n[0] = G.n[1] = 0;
+    const float ro2 = rO * rO;
+    if (!(d2 < ro2)) return;
+    const float sh = sqrtf(ro2 - d2);
+    const float ri = G.c - w;
+    const float sl = (ri > 0.0f && ri * ri > d2) ? sqrtf(ri * ri - d2) : 0.0f;
+    int k = 0;
+    float l = fmaxf_(sA, -sh), h = fminf_(sB, -sl);
+    if (h > l) {
+        G.lo[k] = l;
+        G.hi[k] = h;
+        k++;
     }
-    *frac = 0.0;
+    l = fmaxf_(sA, sl);
+    h = fminf_(sB, sh);
+    if (h > l) {
+        G.lo[k] = l;
+        G.hi[k] = h;
+        k++;
+    }
+    for (int i = 0; i < k; i++) {
+        const float q = ceilf((G.hi[i] - G.lo[i]) / (0.25f * w));
+        G.n[i] = q < 1.0f ? 1 : (q > 64.0f ? 64 : (int)q);
+        G.step[i] = (G.hi[i] - G.lo[i]) / (float)G.n[i];
+    }
+}
+
+// edges of panel j (arc 0 first, then arc 1)
+__device__ __forceinline__ void sd_edges(const SdGeom &G, int j, float *a, float *b) {
+    const int i = j < G.n[0] ? 0 : 1;
+    const int k = i == 0 ? j : j - G.n[0];
+    *a = G.lo[i] + G.step[i] * (float)k;
+    *b = k == G.n[i] - 1 ? G.hi[i] : G.lo[i] + G.step[i] * (float)(k + 1);
+}
+
+// the integral of one candidate: panel k on lane k mod 32, each lane's
+// panels summed in order, then the lanes by a fixed tree (16, 8, 4, 2, 1);
+// the result on every lane
+__device__ float sd_integral_warp(const SdGeom &G, int lane) {
+    const int m = G.n[0] + G.n[1];
+    float s = 0.0f;
+    for (int k = lane; k < m; k += 32) {
+        float a, b;
+        sd_edges(G, k, &a, &b);
+        s = s + sd_panel(a, b, G.d2, G.A, G.c);
+    }
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) s = s + __shfl_down_sync(0xffffffffu, s, off);
+    return __shfl_sync(0xffffffffu, s, 0);
+}
+
+// ---- warp-per-protein binding step
+constexpr int kKmcWarps = 4;        // warps per block
+constexpr int kKmcPanels = 128;     // panels of one integral (2 arcs x 64)
+
+struct KmcWarpBuf {
+    int idx[kKmcMaxCand], sidx[kKmcMaxCand];
+    float4 v[kKmcMaxCand], sv[kKmcMaxCand];  // per candidate (gather order / ascending rod)
+    unsigned long long F[kKmcMaxCand];       // per sorted candidate: fixed-point probability
+    float I[kKmcMaxCand];                    // S: integral per sorted candidate
+    float panel[kKmcPanels];
+};
+
+// the 27 stencil cells of cell c, with the offset of each; periodic sides
+// wrap (two cells per side at least: every offset names one image)
+__device__ __forceinline__ void kmc_stencil(const KmcRep &Q, const int c[3], int lo[3], int hi[3]) {
+    for (int d = 0; d < 3; d++) {
+        if (Q.pbc[d]) {
+            lo[d] = -1;
+            hi[d] = 1;
+        } else {
+            lo[d] = c[d] > 0 ? -1 : 0;
+            hi[d] = c[d] < Q.ncell[d] - 1 ? 1 : 0;
+        }
+    }
+}
+
+// Decisions of the U and S stages in fixed point: a probability p (FP32)
+// becomes floor(p 2^53) (2^53 for p >= 1), the roll is the 53-bit integer
+// of the first two Philox words, and an event happens when the roll lies
+// below the stacked integers.  Integer sums are exact; no FP64 issue.
+__device__ __forceinline__ unsigned long long kmc_fix53(float p) {
+    if (!(p > 0.0f)) return 0ull;
+    if (p >= 1.0f) return 1ull << 53;
+    const unsigned bits = __float_as_uint(p);
+    const int ex = (int)((bits >> 23) & 0xffu);
+    if (ex == 0) return 0ull;
+    const unsigned long long man = (unsigned long long)((bits & 0x7fffffu) | 0x800000u);
+    const int sh = ex - 97;  // p = man 2^(ex - 150); p 2^53 = man 2^(ex - 97)
+    return sh >= 0 ? man << sh : (-sh >= 64 ? 0ull : man >> (-sh));
+}
+
+__device__ __forceinline__ unsigned long long kmc_roll53(const uint32_t w[4]) {
+    return ((unsigned long long)(w[0] >> 5) << 26) | (unsigned long long)(w[1] >> 6);
+}
+
+__device__ __forceinline__ int kmc_choose_fix(unsigned long long F0, unsigned long long F1, unsigned long long *roll) {
+    const unsigned long long u = *roll;
+    if (u < F0) return 0;
+    if (u < F0 + F1) {
+        *roll = u - F0;
+        return 1;
+    }
     return -1;
 }
 
-// code per protein: final stage (bits 0-1), transition + 1 (bits 2-4:
-// 1 U->S, 2 S->U, 3 S->D, 4 D->S), candidates (bits 8-)
-__global__ void __launch_bounds__(128) k_kmc_bind(KmcDev K, int *code) {
+// the sorted candidate whose slice of the stacked integers holds roll, and
+// the roll's fraction of that slice (FP32)
+__device__ int kmc_pick_fix(const KmcWarpBuf &B, int n, unsigned long long roll, float *frac) {
+    unsigned long long cum = 0ull;
+    int last = -1;
+    for (int j = 0; j < n; j++) {
+        const unsigned long long Fj = B.F[j];
+        if (Fj == 0ull) continue;
+        last = j;
+        if (roll < cum + Fj) {
+            *frac = (float)(roll - cum) / (float)Fj;
+            return j;
+        }
+        cum = cum + Fj;
+    }
+    *frac = 1.0f;
+    return last;
+}
+
+// prepared per unbound / singly bound protein for the warp kernel: the
+// stencil centre cell, the search point relative to it (FP32), the bound
+// head's rod axis (FP32), the stage
+struct KmcTask {
+    int4 cell;      // c[0..2], nb | (b << 2)
+    float4 rel;     // point relative to the cell origin, w: bound rod (bits)
+    float4 ab;      // bound rod axis
+};
+
+// code per protein: final stage (bits 0-1), transition (bits 2-4: 1 U->S,
+// 2 S->U, 3 S->D, 4 D->S), candidates (bits 8-); -1: for k_kmc_bind
+//
+// One thread per protein: ends on rods the replica no longer holds are
+// released (the reference releases an end whose rod it cannot find);
+// doubly bound proteins take their D -> S step here (FP64, one exp); the
+// others get their task.
+__global__ void __launch_bounds__(256) k_kmc_prep(KmcDev K, int *code, KmcTask *task) {
     ALENS_PDL_PROLOGUE();
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.nProt; p += gridDim.x * blockDim.x) {
-        AlensProtein pr = K.prot[p];
-        const KmcRep &Q = K.rep[K.protRep[p]];
-        const KmcType &T = K.types[K.protRep[p] * K.nTypes + pr.type];
-        // an end bound to a rod the replica no longer holds is released
-        // (the reference releases an end whose rod it cannot find)
+        const int rep = K.protRep[p];
+        const KmcRep &Q = K.rep[rep];
+        AlensProtein &pp = K.prot[p];
+        int id[2] = {pp.idBind[0], pp.idBind[1]};
         for (int e = 0; e < 2; e++)
-            if (pr.idBind[e] < 0 || pr.idBind[e] >= Q.nRods) pr.idBind[e] = -1;
-        double4 Cb[2], Ab[2];
+            if (id[e] < 0 || id[e] >= Q.nRods) id[e] = -1;
         double P[2][3];
         for (int e = 0; e < 2; e++) {
-            if (pr.idBind[e] < 0) continue;
-            const int r = Q.rodOffset + pr.idBind[e];
-            Cb[e] = K.rodC[r];
-            Ab[e] = K.rodA[r];
-            P[e][0] = Cb[e].x + pr.distBind[e] * Ab[e].x;
-            P[e][1] = Cb[e].y + pr.distBind[e] * Ab[e].y;
-            P[e][2] = Cb[e].z + pr.distBind[e] * Ab[e].z;
+            if (id[e] < 0) continue;
+            const int r = Q.rodOffset + id[e];
+            const KDouble4 C = K.rodC[r], A = K.rodA[r];
+            const double dist = pp.distBind[e];
+            P[e][0] = C.x + dist * A.x;
+            P[e][1] = C.y + dist * A.y;
+            P[e][2] = C.z + dist * A.z;
         }
-        const int nb = (pr.idBind[0] >= 0 ? 1 : 0) + (pr.idBind[1] >= 0 ? 1 : 0);
-        uint32_t w[4];
-        kmc_words(Q.seed, pr.gid, K.step, 0, w);
-        double roll = u53(w[0], w[1]);
-        int trans = 0, ncand = 0;
-        bool overflow = false;
-        KmcCands C;
-        C.n = 0;
-        C.overflow = false;
-        if (nb == 0) {
-            double X[3] = {pr.pos[0], pr.pos[1], pr.pos[2]};
-            kmc_wrap_point(Q, X);
-            pr.pos[0] = X[0];
-            pr.pos[1] = X[1];
-            pr.pos[2] = X[2];
-            const double r2 = T.rcap * T.rcap;
-            int c[3];
-            for (int d = 0; d < 3; d++) c[d] = kmc_cell_coord(X[d], Q.lo[d], Q.cellsz[d], Q.ncell[d]);
-            kmc_for_cells(Q, c, [&](int cid) {
-                for (int s = K.cellStart[cid]; s < K.cellStart[cid + 1]; s++) {
-                    const int r = K.cellRod[s];
-                    const double4 Cr = K.rodC[r], Ar = K.rodA[r];
-                    if (Ar.w != 0.0) continue;
-                    double u[3];
-                    kmc_rel(Q, X, Cr, u);
-                    const double t0 = u[0] * Ar.x + u[1] * Ar.y + u[2] * Ar.z;
-                    const double q0 = u[0] - t0 * Ar.x, q1 = u[1] - t0 * Ar.y, q2 = u[2] - t0 * Ar.z;
-                    const double d2 = q0 * q0 + q1 * q1 + q2 * q2;
-                    if (!(d2 < r2)) continue;
-                    const double hc = sqrt(r2 - d2);
-                    const double lo = dmax(-Cr.w, t0 - hc), hi = dmin(Cr.w, t0 + hc);
-                    const double Lc = hi - lo;
-                    if (!(Lc > 0.0)) continue;
-                    C.insert(r - Q.rodOffset, Lc, lo, Cr.w, 0.0);
-                }
-            });
-            ncand = C.n;
-            overflow = C.overflow;
-            if (!overflow) {
-                double P0 = 0.0, P1 = 0.0;
-                for (int j = 0; j < C.n; j++) P0 = P0 + C.v0[j] * T.usCoef[0];
-                for (int j = 0; j < C.n; j++) P1 = P1 + C.v0[j] * T.usCoef[1];
-                const int e = kmc_choose(P0, P1, &roll);
-                if (e >= 0) {
-                    double frac;
-                    const int j = kmc_pick(C, C.v0, T.usCoef[e], roll, &frac);
-                    double s = C.v1[j] + frac * C.v0[j];
-                    s = dmax(-C.v2[j], dmin(C.v2[j], s));
-                    pr.idBind[e] = C.li[j];
-                    pr.distBind[e] = s;
-                    trans = 1;
+        const int nb = (id[0] >= 0 ? 1 : 0) + (id[1] >= 0 ? 1 : 0);
+        if (nb == 2) {
+            const KmcType &T = K.types[rep * K.nTypes + pp.type];
+            uint32_t w[4];
+            kmc_words(Q.seed, pp.gid, K.step, 0, w);
+            double roll = u53(w[0], w[1]);
+            double dv[3] = {P[1][0] - P[0][0], P[1][1] - P[0][1], P[1][2] - P[0][2]};
+            for (int k = 0; k < 3; k++)
+                if (Q.pbc[k]) dv[k] = dv[k] - Q.L[k] * floor(dv[k] / Q.L[k] + 0.5);
+            const double ell = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+            const double x = (ell - K.D) - T.ell0;
+            const double M = T.Ads * (x * x);
+            const double g = kmc_exp(M);
+            const double p0 = (T.koD[0] * g) * T.dt, p1 = (T.koD[1] * g) * T.dt;
+            const int e = kmc_choose(p0, p1, &roll);
+            int trans = 0;
+            if (e >= 0) {
+                pp.idBind[e] = -1;
+                trans = 4;
+            }
+            code[p] = (e >= 0 ? 1 : 2) | (trans << 2);
+            continue;
+        }
+        pp.idBind[0] = id[0];
+        pp.idBind[1] = id[1];
+        const int b = id[0] >= 0 ? 0 : 1;
+        double X[3];
+        for (int d = 0; d < 3; d++) X[d] = nb == 0 ? pp.pos[d] : P[b][d];
+        kmc_wrap_point(Q, X);
+        if (nb == 0)
+            for (int d = 0; d < 3; d++) pp.pos[d] = X[d];
+        KmcTask t;
+        int c[3];
+        float r[3];
+        for (int d = 0; d < 3; d++) {
+            c[d] = kmc_cell_coord(X[d], Q.lo[d], Q.cellsz[d], Q.ncell[d]);
+            r[d] = (float)(X[d] - (Q.lo[d] + (double)c[d] * Q.cellsz[d]));
+        }
+        float ab[3] = {0.0f, 0.0f, 0.0f};
+        if (nb == 1) {
+            const KDouble4 A = K.rodA[Q.rodOffset + id[b]];
+            ab[0] = (float)A.x;
+            ab[1] = (float)A.y;
+            ab[2] = (float)A.z;
+        }
+        t.cell = make_int4(c[0], c[1], c[2], nb | (b << 2));
+        t.rel = make_float4(r[0], r[1], r[2], __int_as_float(nb == 1 ? id[b] : -1));
+        t.ab = make_float4(ab[0], ab[1], ab[2], 0.0f);
+        task[p] = t;
+        code[p] = -1;
+    }
+}
+
+// One warp per unbound or singly bound protein: the candidate rods of the
+// 27 cells around the protein (all cell ranges in one load, the rods spread
+// over the lanes, FP32 geometry), ascending rod index, the S->D integrals
+// (one panel per lane), then the event (fixed-point decisions on lane 0).
+__global__ void __launch_bounds__(32 * kKmcWarps) k_kmc_bind(KmcDev K, int *code, const KmcTask *task) {
+    ALENS_PDL_PROLOGUE();
+    __shared__ KmcWarpBuf bufs[kKmcWarps];
+    KmcWarpBuf &B = bufs[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    for (int p = blockIdx.x * kKmcWarps + (threadIdx.x >> 5); p < K.nProt; p += gridDim.x * kKmcWarps) {
+        if (code[p] >= 0) continue;   // doubly bound: done in k_kmc_prep
+        const KmcTask tk = task[p];
+        const int rep = K.protRep[p];
+        const KmcRep &Q = K.rep[rep];
+        const long long gid = K.prot[p].gid;
+        const KmcType &T = K.types[rep * K.nTypes + K.prot[p].type];
+        const int nb = tk.cell.w & 3, b = (tk.cell.w >> 2) & 1, f = 1 - b;
+        const int idb = __float_as_int(tk.rel.w);
+        const int c[3] = {tk.cell.x, tk.cell.y, tk.cell.z};
+        const float rx[3] = {tk.rel.x, tk.rel.y, tk.rel.z};
+        int lo[3], hi[3];
+        kmc_stencil(Q, c, lo, hi);
+        // stencil cell k = lane (k < 27; offsets -1..1 per side; clipped
+        // cells empty): its rod range
+        const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
+        int cs0 = 0, cn = 0;
+        if (lane < 27 && ox >= lo[0] && ox <= hi[0] && oy >= lo[1] && oy <= hi[1] && oz >= lo[2] && oz <= hi[2]) {
+            int cc[3] = {c[0] + ox, c[1] + oy, c[2] + oz};
+            for (int d = 0; d < 3; d++)
+                if (Q.pbc[d]) cc[d] = (cc[d] + Q.ncell[d]) % Q.ncell[d];
+            const int cid = Q.cellOffset + (cc[2] * Q.ncell[1] + cc[1]) * Q.ncell[0] + cc[0];
+            cs0 = K.cellStart[cid];
+            cn = K.cellStart[cid + 1] - cs0;
+        }
+        int incl = cn;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int excl = incl - cn;
+        const float csf[3] = {Q.cellszf[0], Q.cellszf[1], Q.cellszf[2]};
+        const float r2 = T.rcapf * T.rcapf;
+        const float ro2 = T.rOuterf * T.rOuterf;
+        int n = 0;
+        for (int base = 0; base < total; base += 32) {
+            const int i = base + lane;
+            bool cand = false;
+            float4 rec = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            int li = 0;
+            int k = 0;
+            for (int j = 1; j < 27; j++)
+                if (__shfl_sync(0xffffffffu, excl, j) <= i) k = j;
+            const int kstart = __shfl_sync(0xffffffffu, cs0, k);
+            const int kex = __shfl_sync(0xffffffffu, excl, k);
+            if (i < total) {
+                const int s = kstart + (i - kex);
+                const float4 R = K.cellRel[s], Ax = K.cellAx[s];
+                li = K.cellRod[s] - Q.rodOffset;
+                const float sh0 = (float)(k % 3 - 1) * csf[0];
+                const float sh1 = (float)((k / 3) % 3 - 1) * csf[1];
+                const float sh2 = (float)(k / 9 - 1) * csf[2];
+                const float v0 = (rx[0] - R.x) - sh0;
+                const float v1 = (rx[1] - R.y) - sh1;
+                const float v2 = (rx[2] - R.z) - sh2;
+                const float t0 = (v0 * Ax.x + v1 * Ax.y) + v2 * Ax.z;
+                const float q0 = v0 - t0 * Ax.x, q1 = v1 - t0 * Ax.y, q2 = v2 - t0 * Ax.z;
+                const float d2 = (q0 * q0 + q1 * q1) + q2 * q2;
+                if (Ax.w == 0.0f) {
+                    if (nb == 0) {
+                        if (d2 < r2) {
+                            const float hc = sqrtf(r2 - d2);
+                            const float l = fmaxf_(-R.w, t0 - hc), h = fminf_(R.w, t0 + hc);
+                            const float Lc = h - l;
+                            if (Lc > 0.0f) {
+                                cand = true;
+                                rec = make_float4(Lc, l, R.w, 0.0f);
+                            }
+                        }
+                    } else if (li != idb && d2 < ro2) {
+                        cand = true;
+                        rec = make_float4(t0, d2, R.w, (Ax.x * tk.ab.x + Ax.y * tk.ab.y) + Ax.z * tk.ab.z);
+                    }
                 }
             }
-        } else if (nb == 1) {
-            const int b = pr.idBind[0] >= 0 ? 0 : 1, f = 1 - b;
-            double X[3] = {P[b][0], P[b][1], P[b][2]};
-            kmc_wrap_point(Q, X);
-            const double ro2 = T.rOuter * T.rOuter;
-            const double4 Abb = Ab[b];
-            int c[3];
-            for (int d = 0; d < 3; d++) c[d] = kmc_cell_coord(X[d], Q.lo[d], Q.cellsz[d], Q.ncell[d]);
-            kmc_for_cells(Q, c, [&](int cid) {
-                for (int s = K.cellStart[cid]; s < K.cellStart[cid + 1]; s++) {
-                    const int r = K.cellRod[s];
-                    if (r - Q.rodOffset == pr.idBind[b]) continue;
-                    const double4 Cr = K.rodC[r], Ar = K.rodA[r];
-                    if (Ar.w != 0.0) continue;
-                    double u[3];
-                    kmc_rel(Q, X, Cr, u);
-                    const double t0 = u[0] * Ar.x + u[1] * Ar.y + u[2] * Ar.z;
-                    const double q0 = u[0] - t0 * Ar.x, q1 = u[1] - t0 * Ar.y, q2 = u[2] - t0 * Ar.z;
-                    const double d2 = q0 * q0 + q1 * q1 + q2 * q2;
-                    if (!(d2 < ro2)) continue;
-                    const double I = sd_integral(d2, -Cr.w - t0, Cr.w - t0, T);
-                    if (!(I > 0.0)) continue;
-                    const bool par = Ar.x * Abb.x + Ar.y * Abb.y + Ar.z * Abb.z > 0.0;
-                    double pref = 1.0;
-                    if (par && T.PtoAP < 1.0)
-                        pref = T.PtoAP;
-                    else if (!par && T.PtoAP > 1.0)
-                        pref = 1.0 / T.PtoAP;
-                    C.insert(r - Q.rodOffset, (pref * T.sdCoef[f]) * I, t0, d2, I);
+            const unsigned m = __ballot_sync(0xffffffffu, cand);
+            if (cand) {
+                const int slot = n + __popc(m & ((1u << lane) - 1u));
+                if (slot < kKmcMaxCand) {
+                    B.idx[slot] = li;
+                    B.v[slot] = rec;
                 }
-            });
-            ncand = C.n;
-            overflow = C.overflow;
-            if (!overflow) {
-                double Pb = 0.0;
-                for (int j = 0; j < C.n; j++) Pb = Pb + C.v0[j];
-                const double pU = T.suProb[b];
-                const int e = kmc_choose(b == 0 ? pU : Pb, b == 0 ? Pb : pU, &roll);
-                if (e == b) {
+            }
+            n += __popc(m);
+        }
+        __syncwarp();
+        const int nc = n < kKmcMaxCand ? n : kKmcMaxCand;
+        // ascending rod index (a rod appears once: one image within reach)
+        for (int k = lane; k < nc; k += 32) {
+            const int me = B.idx[k];
+            int rank = 0;
+            for (int j = 0; j < nc; j++) rank += B.idx[j] < me ? 1 : 0;
+            B.sidx[rank] = me;
+            B.sv[rank] = B.v[k];
+        }
+        __syncwarp();
+        uint32_t w[4];
+        kmc_words(Q.seed, gid, K.step, 0, w);
+        unsigned long long roll = kmc_roll53(w);
+        int trans = 0;
+        if (n > kKmcMaxCand) {
+            if (lane == 0) atomicOr(K.err, kKmcErrCand);
+        } else if (nb == 0) {
+            if (lane == 0) {
+                unsigned long long S0 = 0ull, S1 = 0ull;
+                for (int j = 0; j < nc; j++) S0 = S0 + kmc_fix53(B.sv[j].x * T.usCoeff[0]);
+                for (int j = 0; j < nc; j++) S1 = S1 + kmc_fix53(B.sv[j].x * T.usCoeff[1]);
+                const int e = kmc_choose_fix(S0, S1, &roll);
+                if (e >= 0) {
+                    for (int j = 0; j < nc; j++) B.F[j] = kmc_fix53(B.sv[j].x * T.usCoeff[e]);
+                    float frac;
+                    const int j = kmc_pick_fix(B, nc, roll, &frac);
+                    if (j >= 0) {
+                        const float4 cv = B.sv[j];
+                        const double hl = K.rodC[Q.rodOffset + B.sidx[j]].w;
+                        const double s = (double)(cv.y + frac * cv.x);
+                        AlensProtein &pp = K.prot[p];
+                        pp.idBind[e] = B.sidx[j];
+                        pp.distBind[e] = s > hl ? hl : (s < -hl ? -hl : s);
+                        trans = 1;
+                    }
+                }
+            }
+        } else {
+            // S->D integral of every candidate
+            for (int j = 0; j < nc; j++) {
+                const float4 cv = B.sv[j];
+                SdGeom G;
+                sd_geom(cv.y, -cv.z - cv.x, cv.z - cv.x, T, G);
+                const float Iq = sd_integral_warp(G, lane);
+                if (lane == 0) {
+                    const float pref = cv.w > 0.0f ? T.prefPar : T.prefAnti;
+                    B.I[j] = Iq;
+                    B.F[j] = kmc_fix53((pref * T.sdCoeff[f]) * Iq);
+                }
+            }
+            __syncwarp();
+            int e = -2, j = -1;
+            float frac = 0.0f;
+            if (lane == 0) {
+                unsigned long long Sb = 0ull;
+                for (int k = 0; k < nc; k++) Sb = Sb + B.F[k];
+                const unsigned long long FU = kmc_fix53(T.suProbf[b]);
+                e = kmc_choose_fix(b == 0 ? FU : Sb, b == 0 ? Sb : FU, &roll);
+                if (e == f) j = kmc_pick_fix(B, nc, roll, &frac);
+            }
+            e = __shfl_sync(0xffffffffu, e, 0);
+            j = __shfl_sync(0xffffffffu, j, 0);
+            frac = __shfl_sync(0xffffffffu, frac, 0);
+            if (e == b) {
+                if (lane == 0) {
                     // released uniformly in the capture sphere around the head
                     double off[3] = {0.0, 0.0, 0.0};
                     for (uint32_t k = 0; k < 32; k++) {
                         uint32_t v[4];
-                        kmc_words(Q.seed, pr.gid, K.step, 2 + k, v);
+                        kmc_words(Q.seed, gid, K.step, 2 + k, v);
                         const double x = 2.0 * (((double)v[0] + 0.5) * 2.3283064365386963e-10) - 1.0;
                         const double y = 2.0 * (((double)v[1] + 0.5) * 2.3283064365386963e-10) - 1.0;
                         const double z = 2.0 * (((double)v[2] + 0.5) * 2.3283064365386963e-10) - 1.0;
@@ -477,96 +623,168 @@ __global__ void __launch_bounds__(128) k_kmc_bind(KmcDev K, int *code) {
                             break;
                         }
                     }
-                    pr.pos[0] = P[b][0] + T.rcap * off[0];
-                    pr.pos[1] = P[b][1] + T.rcap * off[1];
-                    pr.pos[2] = P[b][2] + T.rcap * off[2];
-                    pr.idBind[b] = -1;
+                    AlensProtein &pp = K.prot[p];
+                    const int r = Q.rodOffset + pp.idBind[b];
+                    const KDouble4 C = K.rodC[r], A = K.rodA[r];
+                    const double dist = pp.distBind[b];
+                    pp.pos[0] = (C.x + dist * A.x) + T.rcap * off[0];
+                    pp.pos[1] = (C.y + dist * A.y) + T.rcap * off[1];
+                    pp.pos[2] = (C.z + dist * A.z) + T.rcap * off[2];
+                    pp.idBind[b] = -1;
                     trans = 2;
-                } else if (e == f) {
-                    double frac;
-                    const int j = kmc_pick(C, C.v0, 1.0, roll, &frac);
-                    const int r = Q.rodOffset + C.li[j];
-                    const double hl = K.rodC[r].w;
-                    const double t0 = C.v1[j];
-                    const double sStar = sd_invert(C.v2[j], -hl - t0, hl - t0, T, frac * C.v3[j]);
-                    pr.idBind[f] = C.li[j];
-                    pr.distBind[f] = dmax(-hl, dmin(hl, t0 + sStar));
+                }
+            } else if (e == f && j >= 0) {
+                // the binding point: the panel holding the target (running
+                // sum in panel order), then four rounds of a 32-way search of
+                // that panel's partial integral
+                const float4 cv = B.sv[j];
+                SdGeom G;
+                sd_geom(cv.y, -cv.z - cv.x, cv.z - cv.x, T, G);
+                const int m = G.n[0] + G.n[1];
+                for (int k = lane; k < m; k += 32) {
+                    float a, bb;
+                    sd_edges(G, k, &a, &bb);
+                    B.panel[k] = sd_panel(a, bb, G.d2, G.A, G.c);
+                }
+                __syncwarp();
+                const float target = frac * B.I[j];
+                int kp = m - 1;
+                float t = -1.0f;
+                if (lane == 0) {
+                    float cum = 0.0f;
+                    for (int k = 0; k < m; k++) {
+                        const float Pk = B.panel[k];
+                        if (target < cum + Pk) {
+                            kp = k;
+                            t = target - cum;
+                            break;
+                        }
+                        cum = cum + Pk;
+                    }
+                }
+                kp = __shfl_sync(0xffffffffu, kp, 0);
+                t = __shfl_sync(0xffffffffu, t, 0);
+                float a, bb;
+                sd_edges(G, kp, &a, &bb);
+                float sStar = bb;
+                if (t >= 0.0f) {
+                    float x0 = a, x1 = bb;
+                    for (int round = 0; round < 4; round++) {
+                        const float step = (x1 - x0) / 32.0f;
+                        const float xk = lane == 31 ? x1 : x0 + step * (float)(lane + 1);
+                        const bool ge = !(sd_panel(a, xk, G.d2, G.A, G.c) < t);
+                        const unsigned gm = __ballot_sync(0xffffffffu, ge);
+                        const int first = gm ? __ffs(gm) - 1 : 31;
+                        const float nx1 = __shfl_sync(0xffffffffu, xk, first);
+                        const float nx0 = __shfl_sync(0xffffffffu, xk, first > 0 ? first - 1 : 0);
+                        x0 = first > 0 ? nx0 : x0;
+                        x1 = nx1;
+                    }
+                    sStar = 0.5f * (x0 + x1);
+                }
+                if (lane == 0) {
+                    const double hl = K.rodC[Q.rodOffset + B.sidx[j]].w;
+                    const double s = (double)(cv.x + sStar);
+                    AlensProtein &pp = K.prot[p];
+                    pp.idBind[f] = B.sidx[j];
+                    pp.distBind[f] = s > hl ? hl : (s < -hl ? -hl : s);
                     trans = 3;
                 }
             }
-        } else {
-            double dv[3] = {P[1][0] - P[0][0], P[1][1] - P[0][1], P[1][2] - P[0][2]};
-            for (int d = 0; d < 3; d++)
-                if (Q.pbc[d]) dv[d] = dv[d] - Q.L[d] * floor(dv[d] / Q.L[d] + 0.5);
-            const double ell = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
-            const double x = (ell - K.D) - T.ell0;
-            const double M = T.Ads * (x * x);
-            const double g = kmc_exp(M);
-            const double p0 = (T.koD[0] * g) * T.dt, p1 = (T.koD[1] * g) * T.dt;
-            const int e = kmc_choose(p0, p1, &roll);
-            if (e >= 0) {
-                pr.idBind[e] = -1;
-                trans = 4;
-            }
         }
-        if (overflow) atomicOr(K.err, kKmcErrCand);
-        // the new geometry
+        if (lane == 0) {
+            const int nb2 = nb + (trans == 1 || trans == 3 ? 1 : 0) - (trans == 2 ? 1 : 0);
+            code[p] = nb2 | (trans << 2) | (n << 8);
+        }
+        __syncwarp();
+    }
+}
+
+// One thread per protein: head positions and centre of the new state
+// (bound head; midpoint of the heads, minimum image; the free point),
+// wrapped into the box; unbound ends NaN.
+__global__ void __launch_bounds__(256) k_kmc_geom(KmcDev K) {
+    ALENS_PDL_PROLOGUE();
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.nProt; p += gridDim.x * blockDim.x) {
+        const KmcRep &Q = K.rep[K.protRep[p]];
+        AlensProtein &pr = K.prot[p];
+        const int id[2] = {pr.idBind[0], pr.idBind[1]};
+        double E[2][3];
         for (int e = 0; e < 2; e++) {
-            if (pr.idBind[e] < 0) {
+            if (id[e] < 0) {
                 pr.distBind[e] = qnan();
                 pr.posEnd[e][0] = pr.posEnd[e][1] = pr.posEnd[e][2] = qnan();
                 continue;
             }
-            const int r = Q.rodOffset + pr.idBind[e];
-            const double4 Cr = K.rodC[r], Ar = K.rodA[r];
-            pr.posEnd[e][0] = Cr.x + pr.distBind[e] * Ar.x;
-            pr.posEnd[e][1] = Cr.y + pr.distBind[e] * Ar.y;
-            pr.posEnd[e][2] = Cr.z + pr.distBind[e] * Ar.z;
+            const int r = Q.rodOffset + id[e];
+            const KDouble4 Cr = K.rodC[r], Ar = K.rodA[r];
+            const double dist = pr.distBind[e];
+            E[e][0] = Cr.x + dist * Ar.x;
+            E[e][1] = Cr.y + dist * Ar.y;
+            E[e][2] = Cr.z + dist * Ar.z;
+            pr.posEnd[e][0] = E[e][0];
+            pr.posEnd[e][1] = E[e][1];
+            pr.posEnd[e][2] = E[e][2];
         }
-        const int nb2 = (pr.idBind[0] >= 0 ? 1 : 0) + (pr.idBind[1] >= 0 ? 1 : 0);
-        if (nb2 == 1) {
-            const int b = pr.idBind[0] >= 0 ? 0 : 1;
-            pr.pos[0] = pr.posEnd[b][0];
-            pr.pos[1] = pr.posEnd[b][1];
-            pr.pos[2] = pr.posEnd[b][2];
-        } else if (nb2 == 2) {
-            double dv[3];
+        const int nb = (id[0] >= 0 ? 1 : 0) + (id[1] >= 0 ? 1 : 0);
+        double X[3] = {pr.pos[0], pr.pos[1], pr.pos[2]};
+        if (nb == 1) {
+            const int bb = id[0] >= 0 ? 0 : 1;
+            X[0] = E[bb][0];
+            X[1] = E[bb][1];
+            X[2] = E[bb][2];
+        } else if (nb == 2) {
             for (int d = 0; d < 3; d++) {
-                dv[d] = pr.posEnd[1][d] - pr.posEnd[0][d];
-                if (Q.pbc[d]) dv[d] = dv[d] - Q.L[d] * floor(dv[d] / Q.L[d] + 0.5);
-                pr.pos[d] = pr.posEnd[0][d] + 0.5 * dv[d];
+                double dv = E[1][d] - E[0][d];
+                if (Q.pbc[d]) dv = dv - Q.L[d] * floor(dv / Q.L[d] + 0.5);
+                X[d] = E[0][d] + 0.5 * dv;
             }
         }
-        double X[3] = {pr.pos[0], pr.pos[1], pr.pos[2]};
         kmc_wrap_point(Q, X);
         pr.pos[0] = X[0];
         pr.pos[1] = X[1];
         pr.pos[2] = X[2];
-        K.prot[p] = pr;
-        code[p] = nb2 | (trans << 2) | (ncand << 8);
     }
 }
 
-// per replica: stage counts, transitions and the most candidates
+// per replica: stage counts, transitions and the most candidates; each
+// warp adds its lanes' counts with one atomic per counter when all its
+// proteins belong to one replica (replicas own contiguous protein ranges)
 __global__ void __launch_bounds__(256) k_kmc_stats(KmcDev K, const int *code) {
     ALENS_PDL_PROLOGUE();
-    __shared__ int cnt[8];
-    if (threadIdx.x < 8) cnt[threadIdx.x] = 0;
-    __syncthreads();
-    const KmcRep &Q = K.rep[blockIdx.x];
-    int loc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int i = threadIdx.x; i < Q.nProt; i += blockDim.x) {
-        const int c = code[Q.protOffset + i];
-        loc[c & 3]++;
-        const int t = (c >> 2) & 7;
-        if (t > 0) loc[2 + t]++;
-        loc[7] = max(loc[7], c >> 8);
+    const int lane = threadIdx.x & 31;
+    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < K.nProt;
+         base += gridDim.x * blockDim.x) {
+        const int p = base + lane;
+        const bool on = p < K.nProt;
+        const int c = on ? code[p] : 0;
+        const int rep = on ? K.protRep[p] : -1;
+        int v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (on) {
+            v[c & 3] = 1;
+            const int t = (c >> 2) & 7;
+            if (t > 0) v[2 + t] = 1;
+            v[7] = c >> 8;
+        }
+        const int rep0 = __shfl_sync(0xffffffffu, rep, 0);
+        const bool uniform = __all_sync(0xffffffffu, !on || rep == rep0);
+        if (uniform) {
+            int s[8];
+#pragma unroll
+            for (int k = 0; k < 7; k++) s[k] = __reduce_add_sync(0xffffffffu, (unsigned)v[k]);
+            s[7] = __reduce_max_sync(0xffffffffu, (unsigned)v[7]);
+            if (lane == 0) {
+#pragma unroll
+                for (int k = 0; k < 7; k++)
+                    if (s[k]) atomicAdd(&K.stats[8 * rep0 + k], s[k]);
+                atomicMax(&K.stats[8 * rep0 + 7], s[7]);
+            }
+        } else if (on) {
+            for (int k = 0; k < 7; k++)
+                if (v[k]) atomicAdd(&K.stats[8 * rep + k], v[k]);
+            atomicMax(&K.stats[8 * rep + 7], v[7]);
+        }
     }
-    for (int k = 0; k < 7; k++)
-        if (loc[k]) atomicAdd(&cnt[k], loc[k]);
-    atomicMax(&cnt[7], loc[7]);
-    __syncthreads();
-    if (threadIdx.x < 8) K.stats[8 * blockIdx.x + threadIdx.x] = cnt[threadIdx.x];
 }
 
 __global__ void k_kmc_dflag(KmcDev K) {
@@ -646,8 +864,12 @@ void launch_kmc_scatter(const KmcDev &K, const DevState &S, cudaStream_t st) {
 // rewrites afterwards
 void launch_kmc_bind(const KmcDev &K, cudaStream_t st) {
     if (K.nProt <= 0) return;
-    launch_pdl(k_kmc_bind, dim3(grid_kmc(K.nProt, 128)), dim3(128), 0, st, K, K.dScan);
-    launch_pdl(k_kmc_stats, dim3(K.R), dim3(256), 0, st, K, (const int *)K.dScan);
+    KmcTask *task = reinterpret_cast<KmcTask *>(K.task);
+    launch_pdl(k_kmc_prep, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K, K.dScan, task);
+    launch_pdl(k_kmc_bind, dim3(grid_kmc(K.nProt, kKmcWarps)), dim3(32 * kKmcWarps), 0, st, K, K.dScan,
+               (const KmcTask *)task);
+    launch_pdl(k_kmc_geom, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K);
+    launch_pdl(k_kmc_stats, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K, (const int *)K.dScan);
 }
 
 int launch_kmc_springs(const KmcDev &K, const DevState &S, int userTotal, int linkCap, cudaStream_t st) {

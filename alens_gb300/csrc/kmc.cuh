@@ -6,10 +6,12 @@
 //              concatenated in the order they were set
 //   species    KmcType per protein type (rates folded with dt, see below)
 //   rod view   per rod (global index): wrapped centre + half-length, unit
-//              axis + sphere flag (two double4, 64 B), rebuilt each step
+//              axis + sphere flag (2 x 32 B, FP64), rebuilt each step
 //   cells      uniform grid per replica whose edge is at least the binding
 //              reach (largest rod half-length + largest capture distance):
-//              count / exclusive start / cursor per cell, rod indices by cell
+//              count / exclusive start / cursor per cell; by cell slot the
+//              rod index and its FP32 screening geometry (centre relative
+//              to the cell origin, half-length, axis: 32 B)
 //   springs    doubly bound flag and its exclusive scan per protein; the
 //              springs are written into the context's link rows
 #pragma once
@@ -17,6 +19,12 @@
 #include "engine.cuh"
 
 namespace alens {
+
+// four doubles on a 32-byte boundary (one 32-byte load)
+struct __align__(32) KDouble4 {
+    double x, y, z, w;
+};
+__host__ __device__ inline KDouble4 make_kd4(double x, double y, double z, double w) { return KDouble4{x, y, z, w}; }
 
 // Per species: the rates of Protein/ProteinModel.md with dt folded in.
 struct KmcType {
@@ -34,10 +42,17 @@ struct KmcType {
     double koD[2];      // ko_d
     double dt;
     double kappa;       // spring constant of the D-stage spring
+    // FP32 copies for the unbound / singly bound stages (the conversions
+    // would issue on the FP64 pipe)
+    float rcapf, rOuterf, wf, Af, cf;
+    float usCoeff[2], suProbf[2], sdCoeff[2];
+    float prefPar, prefAnti;  // PtoAPratio prefactor for a parallel / antiparallel rod
+    float pad;
 };
 
 struct KmcRep {
     double lo[3], hi[3], L[3], cellsz[3];
+    float cellszf[3];
     int pbc[3], ncell[3];
     int cellOffset, rodOffset, nRods, protOffset, nProt;
     int userLinks;      // links of alens_set_links (their rows come first)
@@ -50,10 +65,13 @@ struct KmcDev {
     int *protRep;
     const KmcType *types;   // nTypes per replica (dt is per replica)
     const KmcRep *rep;
-    double4 *rodC;      // wrapped centre, half-length
-    double4 *rodA;      // axis, 1 for a sphere-shaped rod
+    KDouble4 *rodC;      // wrapped centre, half-length
+    KDouble4 *rodA;      // axis, 1 for a sphere-shaped rod
     int *cellCount, *cellStart, *cellCursor, *cellRod;
+    float4 *cellRel;     // by cell slot: centre relative to the cell origin, half-length (FP32)
+    float4 *cellAx;      // by cell slot: axis, 1 for a sphere-shaped rod
     int *dFlag, *dScan;  // nProt + 1 each
+    void *task;          // per protein: 48-byte task of the unbound / singly bound stages
     int *stats;          // 8 per replica: nU nS nD nUS nSU nSD nDS maxCand
     int *dCount;         // doubly bound proteins per replica
     int *err;

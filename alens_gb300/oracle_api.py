@@ -64,6 +64,7 @@ def load_oracle(rebuild: bool = True) -> C.CDLL:
         "orc_get_proteins": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), vp]),
         "orc_protein_bind_step": (C.c_int, [vp, C.POINTER(AlensKmcStats)]),
         "orc_kmc_exp": (C.c_double, [C.c_double]),
+        "orc_kmc_expf": (C.c_float, [C.c_float]),
         "orc_kmc_sd_integral": (C.c_double, [C.POINTER(AlensProteinType), C.c_double, C.c_double, C.c_double,
                                              C.c_double, C.c_double, C.c_double]),
         "orc_kmc_sd_invert": (C.c_double, [C.POINTER(AlensProteinType), C.c_double, C.c_double, C.c_double,
@@ -136,6 +137,10 @@ def mobility(length: float, radius: float, viscosity: float):
 
 def kmc_exp(x: float) -> float:
     return load_oracle().orc_kmc_exp(float(x))
+
+
+def kmc_expf(x: float) -> float:
+    return load_oracle().orc_kmc_expf(float(x))
 
 
 def kmc_sd_integral(ptype: AlensProteinType, kbt: float, d: float, dt: float, d2: float, sA: float,

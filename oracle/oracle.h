@@ -62,6 +62,7 @@ int orc_set_proteins(OrcCtx *ctx, int n, const AlensProtein *proteins);
 int orc_get_proteins(OrcCtx *ctx, int cap, int *n, AlensProtein *proteins);
 int orc_protein_bind_step(OrcCtx *ctx, AlensKmcStats *stats);
 double orc_kmc_exp(double x);
+float orc_kmc_expf(float x);
 double orc_kmc_sd_integral(const AlensProteinType *t, double KBT, double D, double dt, double d2, double sA,
                            double sB);
 double orc_kmc_sd_invert(const AlensProteinType *t, double KBT, double D, double dt, double d2, double sA,

@@ -33,8 +33,9 @@
 //   * S->D: the integral of exp(-(1-lambda) kappa / (2 kT) (l_f(s) - ell0)^2)
 //     over the rod, l_f = sqrt(d^2 + s^2) - D (lookupType 0), by composite
 //     8-point Gauss-Legendre quadrature over the support where the exponent
-//     is above -36 (instead of the table), the binding point by inverting
-//     the cumulative integral (panel search, then 60 bisections).
+//     is above -36 (instead of the table; the integrand in FP32, edges and
+//     sums in FP64), the binding point by inverting the cumulative integral
+//     (panel search, then 40 bisections).
 // Rolls: Philox4x32-10 with key = rngSeed and counter (gid, step,
 // 0x6B6D6300 + block), a 53-bit uniform from the first two words of block 0.
 //
@@ -43,7 +44,7 @@
 // part) is UNPINNED: no golden outputs exist for it.
 //
 // Canonical arithmetic as in oracle.cpp: fixed evaluation order, no FMA
-// contraction, IEEE +,-,*,/,sqrt and the project's own exp.
+// contraction, IEEE +,-,*,/,sqrt in FP64 and FP32 and the project's own exp.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -56,10 +57,13 @@
 namespace {
 
 constexpr double kPi = 3.141592653589793;
-const double kX8[8] = {-0.9602898564975362, -0.7966664774136267, -0.525532409916329, -0.18343464249564978,
-                       0.18343464249564978, 0.525532409916329,   0.7966664774136267, 0.9602898564975362};
-const double kW8[8] = {0.10122853629037706, 0.22238103445337443, 0.3137066458778869, 0.36268378337836166,
-                       0.36268378337836166, 0.3137066458778869,  0.22238103445337443, 0.10122853629037706};
+// 8-point Gauss-Legendre nodes and weights on [-1, 1], rounded to FP32
+const float kX8[8] = {
+    -0.9602898359298706f, -0.7966665029525757f, -0.5255324244499207f, -0.1834346354007721f,
+    0.1834346354007721f,  0.5255324244499207f,  0.7966665029525757f,  0.9602898359298706f};
+const float kW8[8] = {
+    0.10122853517532349f, 0.22238104045391083f, 0.313706636428833f, 0.3626837730407715f,
+    0.3626837730407715f,  0.313706636428833f,   0.22238104045391083f, 0.10122853517532349f};
 
 double bits_to_double(uint64_t b) {
     double d;
@@ -102,11 +106,42 @@ double kexp(double x) {
     return p * bits_to_double((uint64_t)(int64_t)(ki + 1023) << 52);
 }
 
+float bits_to_float(uint32_t b) {
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+// FP32 e^x of the S->D integrand: ln2 = 0.693145751953125 + 1.428606765330187e-06
+// (head exact for |k| < 2^9), Taylor polynomial of e^r to r^8; below e^-87
+// the result is zero
+float kexpf(float x) {
+    if (!(x == x)) return x;
+    if (x < -87.0f) return 0.0f;
+    if (x > 88.0f) return std::numeric_limits<float>::infinity();
+    const float k = std::floor(x * 1.4426950216293335f + 0.5f);
+    const float r = (x - k * 0.693145751953125f) - k * 1.428606765330187e-06f;
+    float p = 2.4801587642286904e-05f;
+    p = p * r + 0.00019841270113829523f;
+    p = p * r + 0.0013888889225199819f;
+    p = p * r + 0.008333333767950535f;
+    p = p * r + 0.0416666679084301f;
+    p = p * r + 0.1666666716337204f;
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    return p * bits_to_float((unsigned)((int)k + 127) << 23);
+}
+
 // species constants (the same folding of dt as the library's table)
 struct Kt {
     double ell0, c, A, w, rOuter, Ads, rcap, PtoAP;
     double usCoef[2], suProb[2], sdCoef[2], koD[2];
     double dt, kappa;
+    // FP32 copies used by the unbound / singly bound stages
+    float rcapf, rOuterf, wf, Af, cf;
+    float usCoeff[2], suProbf[2], sdCoeff[2];
+    float prefPar, prefAnti;
 };
 
 double bind_volume(double a, double c) {
@@ -143,94 +178,140 @@ Kt make_type(const AlensProteinType &in, double KBT, double D, double dt) {
     }
     T.dt = dt;
     T.kappa = in.kappa;
+    T.rcapf = (float)T.rcap;
+    T.rOuterf = (float)T.rOuter;
+    T.wf = (float)T.w;
+    T.Af = (float)T.A;
+    T.cf = (float)T.c;
+    for (int e = 0; e < 2; e++) {
+        T.usCoeff[e] = (float)T.usCoef[e];
+        T.suProbf[e] = (float)T.suProb[e];
+        T.sdCoeff[e] = (float)T.sdCoef[e];
+    }
+    // Protein/ProteinData.hpp:110-124: the prefactor never exceeds 1
+    const float r = (float)in.PtoAPratio;
+    T.prefPar = r < 1.0f ? r : 1.0f;
+    T.prefAnti = r > 1.0f ? 1.0f / r : 1.0f;
     return T;
 }
 
-double panel(double a, double b, double d2, double A, double c) {
-    const double h = 0.5 * (b - a), m = 0.5 * (a + b);
-    double acc = 0.0;
+// ---- the S->D integral in FP32: support, panels, sums in a fixed order
+float fmaxf_(float a, float b) { return a > b ? a : b; }
+float fminf_(float a, float b) { return a < b ? a : b; }
+
+float panel(float a, float b, float d2, float A, float c) {
+    const float h = 0.5f * (b - a), m = 0.5f * (a + b);
+    float acc = 0.0f;
     for (int k = 0; k < 8; k++) {
-        const double s = m + h * kX8[k];
-        const double x = std::sqrt(d2 + s * s) - c;
-        acc = acc + kW8[k] * kexp(-(A * (x * x)));
+        const float s = m + h * kX8[k];
+        const float x = std::sqrt(d2 + s * s) - c;
+        acc = acc + kW8[k] * kexpf(-(A * (x * x)));
     }
     return h * acc;
 }
 
-int support(double d2, double sA, double sB, const Kt &T, double lo[2], double hi[2]) {
-    const double ro2 = T.rOuter * T.rOuter;
-    if (!(d2 < ro2)) return 0;
-    const double sh = std::sqrt(ro2 - d2);
-    const double ri = T.c - T.w;
-    const double sl = (ri > 0.0 && ri * ri > d2) ? std::sqrt(ri * ri - d2) : 0.0;
-    int n = 0;
-    double l = sA > -sh ? sA : -sh, h = sB < -sl ? sB : -sl;
+// support of the integrand within [sA, sB]: head distances within w of
+// c = ell0 + D, i.e. |s| in [sl, sh]; at most two arcs of at most 64
+// panels of width <= w/4 each
+struct SdGeom {
+    float d2, A, c;
+    float lo[2], hi[2], step[2];
+    int n[2];
+};
+
+SdGeom sd_geom(float d2, float sA, float sB, const Kt &T) {
+    SdGeom G{};
+    const float rO = T.rOuterf, w = T.wf;
+    G.d2 = d2;
+    G.A = T.Af;
+    G.c = T.cf;
+    const float ro2 = rO * rO;
+    if (!(d2 < ro2)) return G;
+    const float sh = std::sqrt(ro2 - d2);
+    const float ri = G.c - w;
+    const float sl = (ri > 0.0f && ri * ri > d2) ? std::sqrt(ri * ri - d2) : 0.0f;
+    int k = 0;
+    float l = fmaxf_(sA, -sh), h = fminf_(sB, -sl);
     if (h > l) {
-        lo[n] = l;
-        hi[n] = h;
-        n++;
+        G.lo[k] = l;
+        G.hi[k] = h;
+        k++;
     }
-    l = sA > sl ? sA : sl;
-    h = sB < sh ? sB : sh;
+    l = fmaxf_(sA, sl);
+    h = fminf_(sB, sh);
     if (h > l) {
-        lo[n] = l;
-        hi[n] = h;
-        n++;
+        G.lo[k] = l;
+        G.hi[k] = h;
+        k++;
     }
-    return n;
+    for (int i = 0; i < k; i++) {
+        const float q = std::ceil((G.hi[i] - G.lo[i]) / (0.25f * w));
+        G.n[i] = q < 1.0f ? 1 : (q > 64.0f ? 64 : (int)q);
+        G.step[i] = (G.hi[i] - G.lo[i]) / (float)G.n[i];
+    }
+    return G;
 }
 
-int npanel(double len, double w) {
-    const double q = std::ceil(len / (0.25 * w));
-    return q < 1.0 ? 1 : (q > 64.0 ? 64 : (int)q);
+void sd_edges(const SdGeom &G, int j, float *a, float *b) {
+    const int i = j < G.n[0] ? 0 : 1;
+    const int k = i == 0 ? j : j - G.n[0];
+    *a = G.lo[i] + G.step[i] * (float)k;
+    *b = k == G.n[i] - 1 ? G.hi[i] : G.lo[i] + G.step[i] * (float)(k + 1);
 }
 
-double edge(double lo, double hi, int k, int n) { return k == n ? hi : lo + ((hi - lo) * (double)k) / (double)n; }
+// the integral: panel k into partial sum k mod 32 (in panel order), then
+// the 32 partial sums by a fixed pairwise tree (offsets 16, 8, 4, 2, 1)
+float sd_integral(const SdGeom &G) {
+    float s[32];
+    for (int l = 0; l < 32; l++) s[l] = 0.0f;
+    const int m = G.n[0] + G.n[1];
+    for (int k = 0; k < m; k++) {
+        float a, b;
+        sd_edges(G, k, &a, &b);
+        s[k % 32] = s[k % 32] + panel(a, b, G.d2, G.A, G.c);
+    }
+    for (int off = 16; off >= 1; off >>= 1)
+        for (int l = 0; l < off; l++) s[l] = s[l] + s[l + off];
+    return s[0];
+}
 
-double sd_integral(double d2, double sA, double sB, const Kt &T) {
-    double lo[2], hi[2];
-    const int ni = support(d2, sA, sB, T, lo, hi);
-    double Q = 0.0;
-    for (int i = 0; i < ni; i++) {
-        const int n = npanel(hi[i] - lo[i], T.w);
-        double a = lo[i];
-        for (int k = 1; k <= n; k++) {
-            const double b = edge(lo[i], hi[i], k, n);
-            Q = Q + panel(a, b, d2, T.A, T.c);
-            a = b;
+// s where the integral from the support start reaches target: the panel
+// by the running sum in panel order, then four rounds of a 32-way search of
+// that panel's partial integral (the first of 32 equal sub-steps whose
+// partial integral is not below the remainder)
+float sd_invert(const SdGeom &G, float target) {
+    const int m = G.n[0] + G.n[1];
+    int kp = m - 1;
+    float t = -1.0f, cum = 0.0f;
+    for (int k = 0; k < m; k++) {
+        float a, b;
+        sd_edges(G, k, &a, &b);
+        const float P = panel(a, b, G.d2, G.A, G.c);
+        if (target < cum + P) {
+            kp = k;
+            t = target - cum;
+            break;
         }
+        cum = cum + P;
     }
-    return Q;
-}
-
-double sd_invert(double d2, double sA, double sB, const Kt &T, double target) {
-    double lo[2], hi[2];
-    const int ni = support(d2, sA, sB, T, lo, hi);
-    double cum = 0.0, last = sA;
-    for (int i = 0; i < ni; i++) {
-        const int n = npanel(hi[i] - lo[i], T.w);
-        double a = lo[i];
-        for (int k = 1; k <= n; k++) {
-            const double b = edge(lo[i], hi[i], k, n);
-            const double P = panel(a, b, d2, T.A, T.c);
-            if (target < cum + P) {
-                const double t = target - cum;
-                double x0 = a, x1 = b;
-                for (int it = 0; it < 60; it++) {
-                    const double xm = 0.5 * (x0 + x1);
-                    if (panel(a, xm, d2, T.A, T.c) < t)
-                        x0 = xm;
-                    else
-                        x1 = xm;
-                }
-                return 0.5 * (x0 + x1);
+    float a, b;
+    sd_edges(G, kp, &a, &b);
+    if (!(t >= 0.0f)) return b;
+    float x0 = a, x1 = b;
+    for (int round = 0; round < 4; round++) {
+        const float step = (x1 - x0) / 32.0f;
+        float xk[32];
+        int first = 31;
+        for (int k = 0; k < 32; k++) xk[k] = k == 31 ? x1 : x0 + step * (float)(k + 1);
+        for (int k = 0; k < 32; k++)
+            if (!(panel(a, xk[k], G.d2, G.A, G.c) < t)) {
+                first = k;
+                break;
             }
-            cum = cum + P;
-            a = b;
-            last = b;
-        }
+        x0 = first > 0 ? xk[first - 1] : x0;
+        x1 = xk[first];
     }
-    return last;
+    return 0.5f * (x0 + x1);
 }
 
 void words(uint64_t seed, int64_t gid, int64_t step, uint32_t b, uint32_t out[4]) {
@@ -244,6 +325,49 @@ double u53(uint32_t hi, uint32_t lo) {
     return ((double)(hi >> 5) * 67108864.0 + (double)(lo >> 6)) * (1.0 / 9007199254740992.0);
 }
 
+// Decisions of the U and S stages in fixed point: an FP32 probability p
+// becomes floor(p 2^53) (2^53 for p >= 1); the roll is the 53-bit integer
+// of the first two Philox words; the event is the stacked slice holding it
+uint64_t fix53(float p) {
+    if (!(p > 0.0f)) return 0;
+    if (p >= 1.0f) return 1ull << 53;
+    uint32_t bits;
+    std::memcpy(&bits, &p, 4);
+    const int ex = (int)((bits >> 23) & 0xffu);
+    if (ex == 0) return 0;
+    const uint64_t man = (uint64_t)((bits & 0x7fffffu) | 0x800000u);
+    const int sh = ex - 97;
+    return sh >= 0 ? man << sh : (-sh >= 64 ? 0 : man >> (-sh));
+}
+
+uint64_t roll53(const uint32_t w[4]) { return ((uint64_t)(w[0] >> 5) << 26) | (uint64_t)(w[1] >> 6); }
+
+int choose_fix(uint64_t F0, uint64_t F1, uint64_t *roll) {
+    const uint64_t u = *roll;
+    if (u < F0) return 0;
+    if (u < F0 + F1) {
+        *roll = u - F0;
+        return 1;
+    }
+    return -1;
+}
+
+int pick_fix(const std::vector<uint64_t> &F, uint64_t roll, float *frac) {
+    uint64_t cum = 0;
+    int last = -1;
+    for (int j = 0; j < (int)F.size(); j++) {
+        if (F[j] == 0) continue;
+        last = j;
+        if (roll < cum + F[j]) {
+            *frac = (float)(roll - cum) / (float)F[j];
+            return j;
+        }
+        cum = cum + F[j];
+    }
+    *frac = 1.0f;
+    return last;
+}
+
 int choose(double p0, double p1, double *roll) {
     const double u = *roll;
     if (u < p0) return 0;
@@ -253,12 +377,6 @@ int choose(double p0, double p1, double *roll) {
     }
     return -1;
 }
-
-// the rod view of a binding step: wrapped centre, axis, half-length
-struct RodView {
-    std::vector<double> c, a, hl;
-    std::vector<uint8_t> sphere;
-};
 
 double wrap1(double v, double lo, double hi, double L) {
     for (int k = 0; k < 64; k++) {
@@ -283,6 +401,29 @@ double min_image(const AlensConfig &c, int d, double v) {
     return v - L * std::floor(v / L + 0.5);
 }
 
+// The binding grid: cells of edge >= reach (largest rod half-length plus
+// the largest capture distance), at most max(64, 2 n) cells with two per
+// periodic side at least, so that every rod within reach of a point lies
+// in one of the 27 cells around it, each offset naming one image.
+struct Grid {
+    int nc[3] = {1, 1, 1};
+    double cs[3] = {1, 1, 1};
+    std::vector<int> start, rod;  // rods by cell, ascending within a cell
+};
+
+int cell_of(const AlensConfig &c, const Grid &G, int d, double v) {
+    const double f = std::floor((v - c.simBoxLow[d]) / G.cs[d]);
+    return f < 0.0 ? 0 : (f > (double)(G.nc[d] - 1) ? G.nc[d] - 1 : (int)f);
+}
+
+// per rod: wrapped centre, axis, half-length (FP64) and the FP32 screening
+// geometry (centre relative to its cell origin, half-length, axis)
+struct RodView {
+    std::vector<double> c, a, hl;
+    std::vector<uint8_t> sphere;
+    std::vector<float> rel, af, hlf;
+};
+
 RodView rod_view(const OrcCtx *x) {
     RodView V;
     const int n = x->n;
@@ -306,31 +447,115 @@ RodView rod_view(const OrcCtx *x) {
     return V;
 }
 
+Grid make_grid(const OrcCtx *x, RodView &V, double reach) {
+    const AlensConfig &cf = x->cfg;
+    Grid G;
+    for (int d = 0; d < 3; d++) {
+        const double L = cf.simBoxHigh[d] - cf.simBoxLow[d];
+        const double f = reach > 0.0 ? std::floor(L / reach) : 1.0;
+        G.nc[d] = f < 1.0 ? 1 : (f > 512.0 ? 512 : (int)f);
+    }
+    const long long limit = std::max<long long>(64, 2LL * x->n);
+    while ((long long)G.nc[0] * G.nc[1] * G.nc[2] > limit) {
+        int d = -1;
+        for (int e = 0; e < 3; e++)
+            if (G.nc[e] > (cf.simBoxPBC[e] ? 2 : 1) && (d < 0 || G.nc[e] > G.nc[d])) d = e;
+        if (d < 0) break;
+        G.nc[d] = std::max(cf.simBoxPBC[d] ? 2 : 1, G.nc[d] / 2);
+    }
+    for (int d = 0; d < 3; d++) G.cs[d] = (cf.simBoxHigh[d] - cf.simBoxLow[d]) / G.nc[d];
+    const int ncell = G.nc[0] * G.nc[1] * G.nc[2];
+    std::vector<int> cnt(ncell + 1, 0), cell(x->n);
+    V.rel.resize(3 * (size_t)x->n);
+    V.af.resize(3 * (size_t)x->n);
+    V.hlf.resize(x->n);
+    for (int r = 0; r < x->n; r++) {
+        int c[3];
+        for (int d = 0; d < 3; d++) {
+            c[d] = cell_of(cf, G, d, V.c[3 * r + d]);
+            V.rel[3 * r + d] = (float)(V.c[3 * r + d] - (cf.simBoxLow[d] + (double)c[d] * G.cs[d]));
+            V.af[3 * r + d] = (float)V.a[3 * r + d];
+        }
+        V.hlf[r] = (float)V.hl[r];
+        cell[r] = (c[2] * G.nc[1] + c[1]) * G.nc[0] + c[0];
+        cnt[cell[r] + 1]++;
+    }
+    for (int k = 0; k < ncell; k++) cnt[k + 1] += cnt[k];
+    G.start = cnt;
+    G.rod.resize(x->n);
+    for (int r = 0; r < x->n; r++) G.rod[cnt[cell[r]]++] = r;
+    return G;
+}
+
 struct Cand {
     int li;
-    double v0, v1, v2, v3;
+    float v0, v1, v2, v3;  // U: Lc, lo, hl; S: t0, d2, hl, axis dot
 };
 
-int pick(const std::vector<Cand> &C, double scale, double roll, double *frac) {
-    double cum = 0.0;
-    const int n = (int)C.size();
-    for (int j = 0; j < n; j++) {
-        const double pj = C[j].v0 * scale;
-        const double nc = cum + pj;
-        if (roll < nc || j == n - 1) {
-            const double f = pj > 0.0 ? (roll - cum) / pj : 0.0;
-            *frac = f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f);
-            return j;
+// the rods of the 27 stencil cells around X that pass the stage's distance
+// test, ascending rod index
+std::vector<Cand> gather(const OrcCtx *x, const RodView &V, const Grid &G, const Kt &T, const double X[3],
+                         int stage, int idb, const float ab[3]) {
+    const AlensConfig &cf = x->cfg;
+    int c[3], lo[3], hi[3];
+    float rx[3], csf[3];
+    for (int d = 0; d < 3; d++) {
+        c[d] = cell_of(cf, G, d, X[d]);
+        rx[d] = (float)(X[d] - (cf.simBoxLow[d] + (double)c[d] * G.cs[d]));
+        csf[d] = (float)G.cs[d];
+        if (cf.simBoxPBC[d]) {
+            lo[d] = -1;
+            hi[d] = 1;
+        } else {
+            lo[d] = c[d] > 0 ? -1 : 0;
+            hi[d] = c[d] < G.nc[d] - 1 ? 1 : 0;
         }
-        cum = nc;
     }
-    *frac = 0.0;
-    return -1;
+    const float r2 = T.rcapf * T.rcapf;
+    const float ro2 = T.rOuterf * T.rOuterf;
+    std::vector<Cand> C;
+    for (int oz = lo[2]; oz <= hi[2]; oz++)
+        for (int oy = lo[1]; oy <= hi[1]; oy++)
+            for (int ox = lo[0]; ox <= hi[0]; ox++) {
+                const int o[3] = {ox, oy, oz};
+                int cc[3];
+                for (int d = 0; d < 3; d++) {
+                    cc[d] = c[d] + o[d];
+                    if (cf.simBoxPBC[d]) cc[d] = (cc[d] + G.nc[d]) % G.nc[d];
+                }
+                const int k = (cc[2] * G.nc[1] + cc[1]) * G.nc[0] + cc[0];
+                const float sh[3] = {(float)o[0] * csf[0], (float)o[1] * csf[1], (float)o[2] * csf[2]};
+                for (int s = G.start[k]; s < G.start[k + 1]; s++) {
+                    const int r = G.rod[s];
+                    if (V.sphere[r]) continue;
+                    const float *R = &V.rel[3 * r], *A = &V.af[3 * r];
+                    const float hl = V.hlf[r];
+                    const float v0 = (rx[0] - R[0]) - sh[0];
+                    const float v1 = (rx[1] - R[1]) - sh[1];
+                    const float v2 = (rx[2] - R[2]) - sh[2];
+                    const float t0 = (v0 * A[0] + v1 * A[1]) + v2 * A[2];
+                    const float q0 = v0 - t0 * A[0], q1 = v1 - t0 * A[1], q2 = v2 - t0 * A[2];
+                    const float d2 = (q0 * q0 + q1 * q1) + q2 * q2;
+                    if (stage == 0) {
+                        if (!(d2 < r2)) continue;
+                        const float hc = std::sqrt(r2 - d2);
+                        const float l = fmaxf_(-hl, t0 - hc), h = fminf_(hl, t0 + hc);
+                        const float Lc = h - l;
+                        if (!(Lc > 0.0f)) continue;
+                        C.push_back(Cand{r, Lc, l, hl, 0.0f});
+                    } else {
+                        if (r == idb || !(d2 < ro2)) continue;
+                        C.push_back(Cand{r, t0, d2, hl, (A[0] * ab[0] + A[1] * ab[1]) + A[2] * ab[2]});
+                    }
+                }
+            }
+    std::sort(C.begin(), C.end(), [](const Cand &a, const Cand &b) { return a.li < b.li; });
+    return C;
 }
 
 // one protein's binding step; returns the transition (0 none, 1 U->S,
 // 2 S->U, 3 S->D, 4 D->S) and the number of candidate rods
-int protein_step(const OrcCtx *x, const RodView &V, const Kt &T, AlensProtein &pr, int *ncand) {
+int protein_step(const OrcCtx *x, const RodView &V, const Grid &G, const Kt &T, AlensProtein &pr, int *ncand) {
     const AlensConfig &cf = x->cfg;
     const double qnan = std::numeric_limits<double>::quiet_NaN();
     for (int e = 0; e < 2; e++)
@@ -346,77 +571,55 @@ int protein_step(const OrcCtx *x, const RodView &V, const Kt &T, AlensProtein &p
     words(cf.rngSeed, pr.gid, x->step, 0, w);
     double roll = u53(w[0], w[1]);
     int trans = 0;
-    std::vector<Cand> C;
+    *ncand = 0;
     if (nb == 0) {
         double X[3] = {pr.pos[0], pr.pos[1], pr.pos[2]};
         wrap_point(cf, X);
         pr.pos[0] = X[0];
         pr.pos[1] = X[1];
         pr.pos[2] = X[2];
-        const double r2 = T.rcap * T.rcap;
-        for (int r = 0; r < x->n; r++) {
-            if (V.sphere[r]) continue;
-            const double *c = &V.c[3 * r], *a = &V.a[3 * r];
-            double u[3];
-            for (int d = 0; d < 3; d++) u[d] = min_image(cf, d, X[d] - c[d]);
-            const double t0 = u[0] * a[0] + u[1] * a[1] + u[2] * a[2];
-            const double q0 = u[0] - t0 * a[0], q1 = u[1] - t0 * a[1], q2 = u[2] - t0 * a[2];
-            const double d2 = q0 * q0 + q1 * q1 + q2 * q2;
-            if (!(d2 < r2)) continue;
-            const double hc = std::sqrt(r2 - d2);
-            const double hl = V.hl[r];
-            const double lo = -hl > t0 - hc ? -hl : t0 - hc;
-            const double hi = hl < t0 + hc ? hl : t0 + hc;
-            const double Lc = hi - lo;
-            if (!(Lc > 0.0)) continue;
-            C.push_back(Cand{r, Lc, lo, hl, 0.0});
-        }
-        double P0 = 0.0, P1 = 0.0;
-        for (const Cand &k : C) P0 = P0 + k.v0 * T.usCoef[0];
-        for (const Cand &k : C) P1 = P1 + k.v0 * T.usCoef[1];
-        const int e = choose(P0, P1, &roll);
+        const float ab[3] = {0.0f, 0.0f, 0.0f};
+        const std::vector<Cand> C = gather(x, V, G, T, X, 0, -1, ab);
+        *ncand = (int)C.size();
+        uint64_t R = roll53(w);
+        uint64_t S0 = 0, S1 = 0;
+        for (const Cand &k : C) S0 = S0 + fix53(k.v0 * T.usCoeff[0]);
+        for (const Cand &k : C) S1 = S1 + fix53(k.v0 * T.usCoeff[1]);
+        const int e = choose_fix(S0, S1, &R);
         if (e >= 0) {
-            double frac;
-            const int j = pick(C, T.usCoef[e], roll, &frac);
-            double s = C[j].v1 + frac * C[j].v0;
-            s = s > C[j].v2 ? C[j].v2 : s;
-            s = s < -C[j].v2 ? -C[j].v2 : s;
-            pr.idBind[e] = C[j].li;
-            pr.distBind[e] = s;
-            trans = 1;
+            std::vector<uint64_t> F;
+            for (const Cand &k : C) F.push_back(fix53(k.v0 * T.usCoeff[e]));
+            float frac;
+            const int j = pick_fix(F, R, &frac);
+            if (j >= 0) {
+                const double hl = V.hl[C[j].li];
+                const double s = (double)(C[j].v1 + frac * C[j].v0);
+                pr.idBind[e] = C[j].li;
+                pr.distBind[e] = s > hl ? hl : (s < -hl ? -hl : s);
+                trans = 1;
+            }
         }
     } else if (nb == 1) {
         const int b = pr.idBind[0] >= 0 ? 0 : 1, f = 1 - b;
         double X[3] = {P[b][0], P[b][1], P[b][2]};
         wrap_point(cf, X);
-        const double ro2 = T.rOuter * T.rOuter;
-        const double *ab = &V.a[3 * pr.idBind[b]];
-        for (int r = 0; r < x->n; r++) {
-            if (r == pr.idBind[b] || V.sphere[r]) continue;
-            const double *c = &V.c[3 * r], *a = &V.a[3 * r];
-            double u[3];
-            for (int d = 0; d < 3; d++) u[d] = min_image(cf, d, X[d] - c[d]);
-            const double t0 = u[0] * a[0] + u[1] * a[1] + u[2] * a[2];
-            const double q0 = u[0] - t0 * a[0], q1 = u[1] - t0 * a[1], q2 = u[2] - t0 * a[2];
-            const double d2 = q0 * q0 + q1 * q1 + q2 * q2;
-            if (!(d2 < ro2)) continue;
-            const double hl = V.hl[r];
-            const double I = sd_integral(d2, -hl - t0, hl - t0, T);
-            if (!(I > 0.0)) continue;
-            // Protein/ProteinData.hpp:110-124: parallel when the axes' dot
-            // product is positive; the prefactor never exceeds 1
-            const bool par = a[0] * ab[0] + a[1] * ab[1] + a[2] * ab[2] > 0.0;
-            double pref = 1.0;
-            if (par && T.PtoAP < 1.0)
-                pref = T.PtoAP;
-            else if (!par && T.PtoAP > 1.0)
-                pref = 1.0 / T.PtoAP;
-            C.push_back(Cand{r, (pref * T.sdCoef[f]) * I, t0, d2, I});
+        const int rb = pr.idBind[b];
+        const float ab[3] = {(float)V.a[3 * rb], (float)V.a[3 * rb + 1], (float)V.a[3 * rb + 2]};
+        const std::vector<Cand> C = gather(x, V, G, T, X, 1, rb, ab);
+        *ncand = (int)C.size();
+        std::vector<uint64_t> F(C.size());
+        std::vector<float> I(C.size());
+        for (size_t j = 0; j < C.size(); j++) {
+            I[j] = sd_integral(sd_geom(C[j].v1, -C[j].v2 - C[j].v0, C[j].v2 - C[j].v0, T));
+            // parallel when the axes' dot product is positive
+            const float pref = C[j].v3 > 0.0f ? T.prefPar : T.prefAnti;
+            F[j] = fix53((pref * T.sdCoeff[f]) * I[j]);
         }
-        double Pb = 0.0;
-        for (const Cand &k : C) Pb = Pb + k.v0;
-        const double pU = T.suProb[b];
-        const int e = choose(b == 0 ? pU : Pb, b == 0 ? Pb : pU, &roll);
+        uint64_t Sb = 0;
+        for (uint64_t v : F) Sb = Sb + v;
+        const uint64_t FU = fix53(T.suProbf[b]);
+        uint64_t R = roll53(w);
+        const int e = choose_fix(b == 0 ? FU : Sb, b == 0 ? Sb : FU, &R);
         if (e == b) {
             double off[3] = {0.0, 0.0, 0.0};
             for (uint32_t k = 0; k < 32; k++) {
@@ -436,18 +639,17 @@ int protein_step(const OrcCtx *x, const RodView &V, const Kt &T, AlensProtein &p
             pr.idBind[b] = -1;
             trans = 2;
         } else if (e == f) {
-            double frac;
-            const int j = pick(C, 1.0, roll, &frac);
-            const int r = C[j].li;
-            const double hl = V.hl[r];
-            const double t0 = C[j].v1;
-            const double sStar = sd_invert(C[j].v2, -hl - t0, hl - t0, T, frac * C[j].v3);
-            double s = t0 + sStar;
-            s = s > hl ? hl : s;
-            s = s < -hl ? -hl : s;
-            pr.idBind[f] = r;
-            pr.distBind[f] = s;
-            trans = 3;
+            float frac;
+            const int j = pick_fix(F, R, &frac);
+            if (j >= 0) {
+                const SdGeom Gj = sd_geom(C[j].v1, -C[j].v2 - C[j].v0, C[j].v2 - C[j].v0, T);
+                const float sStar = sd_invert(Gj, frac * I[j]);
+                const double hl = V.hl[C[j].li];
+                const double s = (double)(C[j].v0 + sStar);
+                pr.idBind[f] = C[j].li;
+                pr.distBind[f] = s > hl ? hl : (s < -hl ? -hl : s);
+                trans = 3;
+            }
         }
     } else {
         double dv[3];
@@ -463,7 +665,6 @@ int protein_step(const OrcCtx *x, const RodView &V, const Kt &T, AlensProtein &p
             trans = 4;
         }
     }
-    *ncand = (int)C.size();
     for (int e = 0; e < 2; e++) {
         if (pr.idBind[e] < 0) {
             pr.distBind[e] = qnan;
@@ -565,13 +766,23 @@ int orc_protein_bind_step(OrcCtx *x, AlensKmcStats *st) {
     AlensKmcStats s{};
     if (!x->prot.empty()) {
         if (x->ptypes.empty()) return ALENS_NOT_READY;
-        const RodView V = rod_view(x);
+        RodView V = rod_view(x);
         std::vector<Kt> T;
-        for (const AlensProteinType &t : x->ptypes) T.push_back(make_type(t, x->kmcKBT, x->kmcD, x->cfg.dt));
+        double reach = 0.0, hl = 0.0;
+        for (const AlensProteinType &t : x->ptypes) {
+            T.push_back(make_type(t, x->kmcKBT, x->kmcD, x->cfg.dt));
+            reach = std::max(reach, std::max(T.back().rcap, T.back().rOuter));
+        }
+        for (int r = 0; r < x->n; r++) hl = std::max(hl, V.hl[r]);
+        reach += hl;
+        for (int d = 0; d < 3; d++)
+            if (x->cfg.simBoxPBC[d] && !(x->cfg.simBoxHigh[d] - x->cfg.simBoxLow[d] >= 2.0 * reach))
+                return ALENS_INVALID_ARG;
+        const Grid G = make_grid(x, V, reach);
         const int np = (int)x->prot.size();
         std::vector<int> trans(np), nc(np);
 #pragma omp parallel for schedule(dynamic, 64)
-        for (int p = 0; p < np; p++) trans[p] = protein_step(x, V, T[x->prot[p].type], x->prot[p], &nc[p]);
+        for (int p = 0; p < np; p++) trans[p] = protein_step(x, V, G, T[x->prot[p].type], x->prot[p], &nc[p]);
         for (int p = 0; p < np; p++) {
             const AlensProtein &q = x->prot[p];
             const int nb = (q.idBind[0] >= 0 ? 1 : 0) + (q.idBind[1] >= 0 ? 1 : 0);
@@ -589,14 +800,16 @@ int orc_protein_bind_step(OrcCtx *x, AlensKmcStats *st) {
 
 double orc_kmc_exp(double x) { return kexp(x); }
 
+float orc_kmc_expf(float x) { return kexpf(x); }
+
 double orc_kmc_sd_integral(const AlensProteinType *t, double KBT, double D, double dt, double d2, double sA,
                            double sB) {
-    return sd_integral(d2, sA, sB, make_type(*t, KBT, D, dt));
+    return (double)sd_integral(sd_geom((float)d2, (float)sA, (float)sB, make_type(*t, KBT, D, dt)));
 }
 
 double orc_kmc_sd_invert(const AlensProteinType *t, double KBT, double D, double dt, double d2, double sA,
                          double sB, double target) {
-    return sd_invert(d2, sA, sB, make_type(*t, KBT, D, dt), target);
+    return (double)sd_invert(sd_geom((float)d2, (float)sA, (float)sB, make_type(*t, KBT, D, dt)), (float)target);
 }
 
 double orc_kmc_bind_volume(const AlensProteinType *t, double KBT, double D) {

@@ -79,6 +79,7 @@ def _integrand(t, d2, s):
                                      (0.08, -0.3, -0.02), (0.1, -1.0, 1.0), (0.02, 0.05, 0.06), (0.04, -0.02, 0.02)])
 @pytest.mark.parametrize("kappa,lam", [(200.0, 0.5), (300.0, 0.25822), (50.0, 0.0)])
 def test_sd_integral_and_inverse_against_adaptive_quadrature(d, sA, sB, kappa, lam):
+    """The integrand in FP32: the integral within 2e-6 (relative) of scipy's."""
     t = capi.make_protein_type(kappa=kappa, lambda_=lam, freeLength=0.025)
     d2 = d * d
     got = oa.kmc_sd_integral(t, KBT, D, 1e-5, d2, sA, sB)
@@ -86,13 +87,14 @@ def test_sd_integral_and_inverse_against_adaptive_quadrature(d, sA, sB, kappa, l
            if sA < p < sB]
     ref, _ = integrate.quad(lambda s: _integrand(t, d2, s), sA, sB, points=pts or None, epsabs=0.0,
                             epsrel=1e-13, limit=500)
-    assert abs(got - ref) <= 1e-10 * max(ref, 1e-300) + 1e-16, (got, ref)
+    # the integrand is evaluated in FP32
+    assert abs(got - ref) <= 2e-6 * max(ref, 1e-300) + 1e-12, (got, ref)
     if ref > 1e-12:
         for u in (0.0, 0.1, 0.5, 0.9, 0.999):
             s = oa.kmc_sd_invert(t, KBT, D, 1e-5, d2, sA, sB, u * got)
-            assert sA <= s <= sB
+            assert sA - 1e-7 <= s <= sB + 1e-7      # FP32 bounds
             part, _ = integrate.quad(lambda x: _integrand(t, d2, x), sA, s, epsabs=0.0, epsrel=1e-13, limit=500)
-            assert abs(part - u * got) <= 1e-9 * got, (u, part, u * got)
+            assert abs(part - u * got) <= 5e-6 * got, (u, part, u * got)
 
 
 def test_bind_volume_closed_form():
@@ -114,6 +116,12 @@ def test_exp_accuracy():
     assert rel.max() <= 4e-16, rel.max()
     assert oa.kmc_exp(0.0) == 1.0
     assert oa.kmc_exp(-800.0) == 0.0 and math.isinf(oa.kmc_exp(800.0))
+    # the FP32 exp of the S->D integrand, on its range [-87, 0]
+    xf = np.linspace(-87.0, 0.0, 20001).astype(np.float32)
+    gotf = np.array([oa.kmc_expf(float(v)) for v in xf])
+    reff = np.exp(xf.astype(np.float64))
+    assert float(np.max(np.abs(gotf - reff) / reff)) <= 6e-7
+    assert oa.kmc_expf(-100.0) == 0.0
 
 
 # ----------------------------------------------------------- whole steps
