@@ -1553,7 +1553,7 @@ void Engine::uploadProteins() {
     K_.protRep = alloc<int>(protAllocs_, total);
     K_.dFlag = alloc<int>(protAllocs_, total + 1);
     K_.dScan = alloc<int>(protAllocs_, total + 1);
-    K_.task = alloc<float4>(protAllocs_, 3 * (size_t)total);
+    K_.task = alloc<float4>(protAllocs_, 4 * (size_t)total);
     std::vector<AlensProtein> all;
     std::vector<int> rep;
     all.reserve(total);
@@ -1733,8 +1733,7 @@ int Engine::proteinBindStep(AlensKmcStats *stats) {
     launch_kmc_bin(K_, S_, stream_);
     int n = 1 + launch_scan(K_.cellCount, K_.cellStart, K_.nCells + 1, S_.scanTmp, stream_);
     launch_kmc_scatter(K_, S_, stream_);
-    launch_kmc_bind(K_, stream_);
-    n += 3;
+    n += 1 + launch_kmc_bind(K_, stream_);
     n += launch_kmc_springs(K_, S_, userLinkTotal_, linkCap_, stream_);
     CK(cudaGetLastError());
     launches_ += n;

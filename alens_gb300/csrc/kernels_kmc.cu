@@ -365,6 +365,7 @@ struct KmcTask {
     int4 cell;      // c[0..2], nb | (b << 2)
     float4 rel;     // point relative to the cell origin, w: bound rod (bits)
     float4 ab;      // bound rod axis
+    int4 roll;      // the 53-bit roll (low, high words)
 };
 
 // code per protein: final stage (bits 0-1), transition (bits 2-4: 1 U->S,
@@ -441,6 +442,10 @@ __global__ void __launch_bounds__(256) k_kmc_prep(KmcDev K, int *code, KmcTask *
         t.cell = make_int4(c[0], c[1], c[2], nb | (b << 2));
         t.rel = make_float4(r[0], r[1], r[2], __int_as_float(nb == 1 ? id[b] : -1));
         t.ab = make_float4(ab[0], ab[1], ab[2], 0.0f);
+        uint32_t w[4];
+        kmc_words(Q.seed, pp.gid, K.step, 0, w);
+        const unsigned long long roll = kmc_roll53(w);
+        t.roll = make_int4((int)(unsigned)roll, (int)(unsigned)(roll >> 32), 0, 0);
         task[p] = t;
         code[p] = -1;
     }
@@ -475,7 +480,7 @@ __global__ void __launch_bounds__(32 * kKmcWarps) k_kmc_bind(KmcDev K, int *code
         if (lane < 27 && ox >= lo[0] && ox <= hi[0] && oy >= lo[1] && oy <= hi[1] && oz >= lo[2] && oz <= hi[2]) {
             int cc[3] = {c[0] + ox, c[1] + oy, c[2] + oz};
             for (int d = 0; d < 3; d++)
-                if (Q.pbc[d]) cc[d] = (cc[d] + Q.ncell[d]) % Q.ncell[d];
+                if (Q.pbc[d]) cc[d] = cc[d] < 0 ? cc[d] + Q.ncell[d] : (cc[d] >= Q.ncell[d] ? cc[d] - Q.ncell[d] : cc[d]);
             const int cid = Q.cellOffset + (cc[2] * Q.ncell[1] + cc[1]) * Q.ncell[0] + cc[0];
             cs0 = K.cellStart[cid];
             cn = K.cellStart[cid + 1] - cs0;
@@ -497,9 +502,17 @@ __global__ void __launch_bounds__(32 * kKmcWarps) k_kmc_bind(KmcDev K, int *code
             bool cand = false;
             float4 rec = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             int li = 0;
-            int k = 0;
-            for (int j = 1; j < 27; j++)
-                if (__shfl_sync(0xffffffffu, excl, j) <= i) k = j;
+            // the last stencil cell whose first flattened rod is <= i
+            // (prefixes ascend): five rounds of a binary search
+            int k = 0, khi = 26;
+#pragma unroll
+            for (int it = 0; it < 5; it++) {
+                const int mid = (k + khi + 1) >> 1;
+                if (__shfl_sync(0xffffffffu, excl, mid) <= i)
+                    k = mid;
+                else
+                    khi = mid - 1;
+            }
             const int kstart = __shfl_sync(0xffffffffu, cs0, k);
             const int kex = __shfl_sync(0xffffffffu, excl, k);
             if (i < total) {
@@ -553,9 +566,8 @@ __global__ void __launch_bounds__(32 * kKmcWarps) k_kmc_bind(KmcDev K, int *code
             B.sv[rank] = B.v[k];
         }
         __syncwarp();
-        uint32_t w[4];
-        kmc_words(Q.seed, gid, K.step, 0, w);
-        unsigned long long roll = kmc_roll53(w);
+        unsigned long long roll =
+            ((unsigned long long)(unsigned)tk.roll.y << 32) | (unsigned long long)(unsigned)tk.roll.x;
         int trans = 0;
         if (n > kKmcMaxCand) {
             if (lane == 0) atomicOr(K.err, kKmcErrCand);
@@ -862,14 +874,15 @@ void launch_kmc_scatter(const KmcDev &K, const DevState &S, cudaStream_t st) {
 
 // code[] reuses the doubly bound flags' buffer, which the springs pass
 // rewrites afterwards
-void launch_kmc_bind(const KmcDev &K, cudaStream_t st) {
-    if (K.nProt <= 0) return;
+int launch_kmc_bind(const KmcDev &K, cudaStream_t st) {
+    if (K.nProt <= 0) return 0;
     KmcTask *task = reinterpret_cast<KmcTask *>(K.task);
     launch_pdl(k_kmc_prep, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K, K.dScan, task);
     launch_pdl(k_kmc_bind, dim3(grid_kmc(K.nProt, kKmcWarps)), dim3(32 * kKmcWarps), 0, st, K, K.dScan,
                (const KmcTask *)task);
     launch_pdl(k_kmc_geom, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K);
     launch_pdl(k_kmc_stats, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K, (const int *)K.dScan);
+    return 4;
 }
 
 int launch_kmc_springs(const KmcDev &K, const DevState &S, int userTotal, int linkCap, cudaStream_t st) {

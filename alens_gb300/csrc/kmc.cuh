@@ -71,7 +71,7 @@ struct KmcDev {
     float4 *cellRel;     // by cell slot: centre relative to the cell origin, half-length (FP32)
     float4 *cellAx;      // by cell slot: axis, 1 for a sphere-shaped rod
     int *dFlag, *dScan;  // nProt + 1 each
-    void *task;          // per protein: 48-byte task of the unbound / singly bound stages
+    void *task;          // per protein: 64-byte task of the unbound / singly bound stages
     int *stats;          // 8 per replica: nU nS nD nUS nSU nSD nDS maxCand
     int *dCount;         // doubly bound proteins per replica
     int *err;
@@ -85,7 +85,7 @@ constexpr int kKmcErrSpring = 2;    // a spring row fell outside the link capaci
 
 void launch_kmc_bin(const KmcDev &K, const DevState &S, cudaStream_t st);
 void launch_kmc_scatter(const KmcDev &K, const DevState &S, cudaStream_t st);
-void launch_kmc_bind(const KmcDev &K, cudaStream_t st);
+int launch_kmc_bind(const KmcDev &K, cudaStream_t st);  // returns kernels launched
 // doubly bound flags, their scan and the spring rows at link offset
 // userTotal (capacity linkCap); dCount per replica
 int launch_kmc_springs(const KmcDev &K, const DevState &S, int userTotal, int linkCap, cudaStream_t st);

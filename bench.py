@@ -509,6 +509,8 @@ def other_workloads(torch, stream, flush, mlp, steps):
     for lab, warm, prec, attach in (("zero_fp64", capi.WARM_ZERO, capi.PREC_FP64, False),
                                     ("previous_gamma_fp64", capi.WARM_PREV, capi.PREC_FP64, False),
                                     ("learned_fp64", capi.WARM_MLP, capi.PREC_FP64, True),
+                                    ("zero_mixed", capi.WARM_ZERO, capi.PREC_MIXED, False),
+                                    ("previous_gamma_mixed", capi.WARM_PREV, capi.PREC_MIXED, False),
                                     ("learned_mixed", capi.WARM_MLP, capi.PREC_MIXED, True)):
         cfg = workloads.config_with(w4.cfg, warmStart=warm, precision=prec)
         t, it = timed_steps(torch, stream, maker(cfg, rods4, attach=attach), steps, flush)
@@ -557,7 +559,82 @@ def other_workloads(torch, stream, flush, mlp, steps):
         "sequential_64_contexts_rod_steps_per_s": nr * steps / (ts * 1e-3),
         "speedup_vs_sequential": ts / te, "max_iterations_per_step": ite,
         "autotuned_solver": chosen}
+    # protein binding kinetics: the dense monolayer with 20,000 proteins of
+    # its example crosslinker, and the 200,000-rod cube with 200,000
+    out["protein_binding_monolayer_20000_rods_20000_proteins"] = kmc_workload(
+        torch, stream, flush, workloads.dense_monolayer(), None, 20000, capi.make_protein_type(), steps)
+    out["protein_binding_cube_200000_rods_200000_proteins"] = kmc_workload(
+        torch, stream, flush, w4, rods4, 200000,
+        capi.make_protein_type(rc=0.03, ko_s=(200.0, 150.0), Ka=(0.01, 0.012), ko_d=(100.0, 80.0), Ke=(0.5, 0.4)),
+        steps)
     return out
+
+
+KMC_KBT = 0.00411   # pN um (ProteinConfig KBT of the examples)
+KMC_D = 0.025       # um (RunConfig sylinderDiameter of the examples)
+
+
+def kmc_workload(torch, stream, flush, w, rods, nprot, ptype, steps):
+    """Protein binding steps (alens_protein_bind_step) on a rod state:
+    device time per call (CUDA events on the library stream, L2 flushed
+    before each call; the call includes its host read-back of the stage
+    counts), proteins per second, the stage counts of the last call, and
+    the oracle on the host cores over a bounded sample of the same calls."""
+    from alens_gb300 import capi, workloads
+    rods = rods if rods is not None else w.rods
+    pairs = workloads.pair_list(capi.GpuSystem, w.cfg, rods, 0.05)
+    prots = workloads.protein_population(w.cfg, rods, nprot, pairs=pairs, seed=1)
+    c = workloads.config_with(w.cfg)
+    c.stream = stream.cuda_stream
+    g = capi.GpuSystem(c)
+    g.set_rods(rods)
+    g.set_protein_types([ptype], KMC_KBT, KMC_D)
+    g.set_proteins(prots)
+    for _ in range(3):
+        g.protein_bind_step()
+    ms = []
+    st = None
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = g.protein_bind_step()[0]
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    launches0 = g.launch_count()
+    g.protein_bind_step()
+    per_call = g.launch_count() - launches0
+    state = g.get_proteins()
+    g.close()
+    # CPU baseline: the oracle (OpenMP, all host threads) from the same
+    # protein state, a bounded number of calls
+    from alens_gb300 import oracle_api
+    threads = os.cpu_count() or 1
+    oracle_api.set_threads(threads)
+    o = oracle_api.OracleSystem(w.cfg)
+    o.set_rods(rods)
+    o.set_protein_types([ptype], KMC_KBT, KMC_D)
+    o.set_proteins(state)
+    o.protein_bind_step()
+    t0 = time.perf_counter()
+    n = 0
+    while n < 50:
+        o.protein_bind_step()
+        n += 1
+        if time.perf_counter() - t0 > 5.0:
+            break
+    cpu_ms = (time.perf_counter() - t0) / n * 1e3
+    o.close()
+    med = statistics.median(ms)
+    return {"rods": rods.n, "proteins": nprot, "bind_steps": steps,
+            "ms_per_bind_step": med, "protein_steps_per_s": nprot / (med * 1e-3),
+            "kernels_per_bind_step": per_call, "last_step_counts": st,
+            "cpu_baseline": {"value": cpu_ms, "unit": "ms per bind step", "cores": threads, "kind": "port",
+                             "sample": f"{n} bind steps of the oracle from the GPU's protein state"},
+            "speedup_vs_cpu_baseline": cpu_ms / med}
 
 
 def profile_case(args):
