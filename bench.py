@@ -88,6 +88,10 @@ def parse():
     ap.add_argument("--profile-ensemble", action="store_true",
                     help="one step of the 64-replica ensemble (mixed precision, direct launches) "
                          "between cudaProfilerStart/Stop, after 3 warm-up steps; no JSON line")
+    ap.add_argument("--profile-kmc", action="store_true",
+                    help="protein binding steps on the 200,000-rod cube with 200,000 proteins: 3 warm-up "
+                         "calls, then 2 calls between cudaProfilerStart/Stop; prints the stage counts; "
+                         "no JSON line")
     return ap.parse_args()
 
 
@@ -724,8 +728,35 @@ def profile_ensemble(args):
     g.close()
 
 
+def profile_kmc(args):
+    """Two protein binding steps of the bench's 200,000-protein workload
+    inside cudaProfilerStart/Stop, after 3 warm-up calls."""
+    import torch
+    from alens_gb300 import capi, workloads
+    w = workloads.large_eval(n=200000, box=40.0, seed=0)
+    pairs = workloads.pair_list(capi.GpuSystem, w.cfg, w.rods, 0.05)
+    prots = workloads.protein_population(w.cfg, w.rods, 200000, pairs=pairs, seed=1)
+    t = capi.make_protein_type(rc=0.03, ko_s=(200.0, 150.0), Ka=(0.01, 0.012), ko_d=(100.0, 80.0), Ke=(0.5, 0.4))
+    g = capi.GpuSystem(w.cfg)
+    g.set_rods(w.rods)
+    g.set_protein_types([t], KMC_KBT, KMC_D)
+    g.set_proteins(prots)
+    for _ in range(3):
+        g.protein_bind_step()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    for _ in range(2):
+        print(g.protein_bind_step()[0], flush=True)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    g.close()
+
+
 def main():
     args = parse()
+    if args.profile_kmc:
+        profile_kmc(args)
+        return
     if args.profile_case:
         profile_case(args)
         return
