@@ -1430,10 +1430,11 @@ KmcType make_kmc_type(const AlensProteinType &in, double KBT, double D, double d
     const double Ka[2] = {in.Ka[0] / 602.0, in.Ka[1] / 602.0};
     const double Ke[2] = {in.useBindVol ? in.Ke[0] / 602.0 : in.Ke[0], in.useBindVol ? in.Ke[1] / 602.0 : in.Ke[1]};
     T.ell0 = in.freeLength;
-    T.c = in.freeLength + D;
+    T.lookup = in.lookupType;
+    T.c = in.lookupType == 0 ? in.freeLength + D : in.freeLength;
     T.A = ((1.0 - in.lambda) * in.kappa) / (2.0 * KBT);
     T.w = 6.0 / std::sqrt(T.A);
-    T.rOuter = T.c + T.w;
+    T.rOuter = (in.freeLength + D) + T.w;
     T.Ads = (in.lambda * in.kappa) / (2.0 * KBT);
     const double rd = std::sqrt((6.0 * in.diffUnbound) * dt);
     T.rcap = in.rc > rd ? in.rc : rd;
@@ -1461,6 +1462,7 @@ KmcType make_kmc_type(const AlensProteinType &in, double KBT, double D, double d
     const float r = (float)in.PtoAPratio;
     T.prefPar = r < 1.0f ? r : 1.0f;
     T.prefAnti = r > 1.0f ? 1.0f / r : 1.0f;
+    T.Df = (float)D;
     return T;
 }
 
@@ -1471,7 +1473,7 @@ void Engine::setProteinTypes(int n, const AlensProteinType *t, double KBT, doubl
         throw ApiError(ALENS_INVALID_ARG);
     for (int k = 0; k < n; k++) {
         const AlensProteinType &p = t[k];
-        bool ok = p.lookupType == 0 && std::isfinite(p.kappa) && p.kappa > 0.0 && std::isfinite(p.lambda) &&
+        bool ok = (p.lookupType == 0 || p.lookupType == 1) && std::isfinite(p.kappa) && p.kappa > 0.0 && std::isfinite(p.lambda) &&
                   p.lambda >= 0.0 && p.lambda < 1.0 && finite_nonneg(p.freeLength) && std::isfinite(p.rc) &&
                   p.rc > 0.0 && finite_nonneg(p.eps) && finite_nonneg(p.diffUnbound) &&
                   std::isfinite(p.PtoAPratio) && p.PtoAPratio > 0.0;
@@ -1710,7 +1712,8 @@ void Engine::rebuildSprings() {
     if (ptypes_.empty()) throw ApiError(ALENS_NOT_READY);
     prepareKmc();
     CK(cudaMemsetAsync(K_.stats, 0, sizeof(int) * (9 * R_ + 1), stream_));
-    launches_ += launch_kmc_springs(K_, S_, userLinkTotal_, linkCap_, stream_);
+    launch_kmc_view(K_, S_, stream_);  // lookupType 1 rest lengths read the rods
+    launches_ += 1 + launch_kmc_springs(K_, S_, userLinkTotal_, linkCap_, stream_);
     CK(cudaGetLastError());
     readSprings(nullptr);
 }

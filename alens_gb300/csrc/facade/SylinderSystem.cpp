@@ -464,6 +464,12 @@ void SylinderSystem::writeResult() {
     writeResult(folder + "SylinderAscii_" + std::to_string(snapID_) + ".dat");
     writeSylinderVTK(folder, snapID_, getContainer());
     writeConBlockVTK(folder, snapID_, getConBlocks());
+    if (haveProteins_) {
+        std::vector<int64_t> gid;
+        for (const Sylinder &r : getContainer()) gid.push_back(r.gid);
+        writeProteinAscii(folder + "ProteinAscii_" + std::to_string(snapID_) + ".dat", getProteins(), proteinTags_,
+                          gid, runConfig.dt * (double)getStepCount());
+    }
     std::FILE *f = std::fopen("TimeStepInfo.txt", "w");
     if (!f) throw std::runtime_error("cannot write TimeStepInfo.txt");
     std::fprintf(f, "%ld\n%d\n%.17g\n", getStepCount(), snapID_, runConfig.dt * (double)getStepCount());
@@ -753,6 +759,58 @@ void SylinderSystem::printTimingSummary() const {
     std::printf("rodSystem step %ld: %d collisions, %d bilateral, %d BBPGD iterations, residual %.3e, %.3f ms\n",
                 (long)stats_.step, stats_.nCollision, stats_.nBilateral, stats_.iterations, stats_.residual,
                 lastStepMs_);
+}
+
+
+void SylinderSystem::setProteinTypes(const std::vector<AlensProteinType> &types, double KBT) {
+    if (!ctx_) throw std::runtime_error("setProteinTypes: initialize() first");
+    check(alens_set_protein_types(ctx_, (int)types.size(), types.data(), KBT, runConfig.sylinderDiameter),
+          "alens_set_protein_types");
+    proteinTags_.clear();
+    for (const AlensProteinType &t : types) proteinTags_.push_back(t.tag);
+}
+
+void SylinderSystem::setProteins(const std::vector<AlensProtein> &proteins) {
+    if (!ctx_) throw std::runtime_error("setProteins: initialize() first");
+    check(alens_set_proteins(ctx_, 0, (int)proteins.size(), proteins.data()), "alens_set_proteins");
+    haveProteins_ = !proteins.empty();
+}
+
+std::vector<AlensProtein> SylinderSystem::getProteins() {
+    if (!ctx_) return {};
+    int n = 0;
+    const int rc = alens_get_proteins(ctx_, 0, 0, &n, nullptr);
+    if (rc != ALENS_OK && rc != ALENS_CAPACITY) check(rc, "alens_get_proteins");
+    std::vector<AlensProtein> out(n);
+    if (n > 0) check(alens_get_proteins(ctx_, 0, n, &n, out.data()), "alens_get_proteins");
+    return out;
+}
+
+AlensKmcStats SylinderSystem::calcBindInteraction() {
+    if (!ctx_) throw std::runtime_error("calcBindInteraction: initialize() first");
+    AlensKmcStats st{};
+    check(alens_protein_bind_step(ctx_, &st), "alens_protein_bind_step");
+    return st;
+}
+
+void SylinderSystem::writeProteinAscii(const std::string &path, const std::vector<AlensProtein> &proteins,
+                                       const std::vector<int> &typeTag, const std::vector<int64_t> &rodGid,
+                                       double time) {
+    std::FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) throw std::runtime_error("cannot write " + path);
+    std::fprintf(f, "%d \n %lf\n", (int)proteins.size(), time);
+    for (const AlensProtein &p : proteins) {
+        long long g[2];
+        for (int e = 0; e < 2; e++) g[e] = p.idBind[e] >= 0 ? (long long)rodGid.at(p.idBind[e]) : -1LL;
+        const double *a = p.pos, *b = p.pos;
+        if (g[0] != -1 && g[1] != -1) {
+            a = p.posEnd[0];
+            b = p.posEnd[1];
+        }
+        std::fprintf(f, "P %lld %d %.6g %.6g %.6g %.6g %.6g %.6g %lld %lld\n", (long long)p.gid,
+                     typeTag.at(p.type), a[0], a[1], a[2], b[0], b[1], b[2], g[0], g[1]);
+    }
+    std::fclose(f);
 }
 
 }  // namespace gpu

@@ -209,6 +209,23 @@ class SylinderSystem {
     // TimeStepInfo.txt: exactly three numbers (step, snapID, time); false
     // for anything else (a SylinderAscii snapshot, say)
     static bool readTimeStepInfo(const std::string &path, long *step, int *snapID, double *time);
+    // Protein binding kinetics on the device.  The species in
+    // ProteinConfig.yaml units (the rod diameter is runConfig's
+    // sylinderDiameter), the proteins with bound rods as container indices.
+    void setProteinTypes(const std::vector<AlensProteinType> &types, double KBT);
+    void setProteins(const std::vector<AlensProtein> &proteins);
+    std::vector<AlensProtein> getProteins();
+    // TubuleSystem::calcBindInteraction + setProteinConstraints
+    // (SRC/TubuleSystem.cpp:232-259, 694-745): one binding step of every
+    // protein; the doubly bound ones are springs of the next runStep()
+    AlensKmcStats calcBindInteraction();
+    // ProteinAscii_<snapID>.dat (Protein/ProteinData.hpp:545-564, 705-718):
+    // header "count \n time", then "P gid tag end0 end1 gid0 gid1" per
+    // protein (the heads when both are bound, the centre twice otherwise;
+    // bound rods as gids).  Same bytes as alens_gb300.io.write_protein_ascii.
+    static void writeProteinAscii(const std::string &path, const std::vector<AlensProtein> &proteins,
+                                  const std::vector<int> &typeTag, const std::vector<int64_t> &rodGid, double time);
+    AlensCtx *context() const { return ctx_; }
     const AlensStepStats &lastStats() const { return stats_; }
     std::array<double, 9> conStress() const { return stress_; }
     std::array<double, 3> polarOrder() const { return polar_; }
@@ -220,6 +237,8 @@ class SylinderSystem {
     void check(int rc, const char *where) const;
 
     AlensCtx *ctx_ = nullptr;
+    std::vector<int> proteinTags_;   // tag per species
+    bool haveProteins_ = false;
     std::vector<Sylinder> rods_;
     std::vector<std::array<int64_t, 2>> links_;  // 'L a b' lines (gids): plus end of a to minus end of b
     void applyLinks();

@@ -17,6 +17,20 @@
 // usage: facade_driver --write-vtk TubuleInitial.dat folder snapID
 // Reads the rods and writes Sylinder_<snapID>.pvtp and its piece (no device).
 //
+// usage: facade_driver --write-protein-ascii records.txt out.dat time
+// Writes a ProteinAscii file with SylinderSystem::writeProteinAscii (no
+// device).  records: "T tag..." (tag per species), "R gid..." (rod gids),
+// then "gid type idBind0 idBind1 pos(3) posEnd0(3) posEnd1(3)" per protein.
+//
+// usage: facade_driver --proteins RunConfig.yaml TubuleInitial.dat setup.txt KBT steps out.txt
+// Steps proteins and rods in TubuleSystem::step()'s order
+// (SRC/TubuleSystem.cpp:196-224): calcBindInteraction(), then runStep().
+// setup: "S tag fixedEnd0 useBindVol lookupType freeLength kappa lambda
+// PtoAPratio diffUnbound rc eps ko_s(2) ko_d(2) Ka(2) Ke(2)" per species and
+// "P gid type idBind0 idBind1 distBind0 distBind1 x y z" per protein.  Writes
+// the final proteins to out.txt ("gid type idBind0 idBind1 distBind(2)
+// pos(3) posEnd(6)", %.17g) and prints one JSON line of per-step counts.
+//
 // usage: facade_driver --restart-check RunConfig.yaml TubuleInitial.dat steps
 // Steps a system, calling writeResult() before each runStep (where the
 // reference's runStep writes its snapshot), then restarts a second system
@@ -143,7 +157,150 @@ int restartCheck(const char *yaml, const char *dat, int steps) {
 
 }  // namespace
 
+namespace {
+
+std::vector<std::string> tokens(const std::string &line) {
+    std::vector<std::string> t;
+    std::string cur;
+    for (char ch : line) {
+        if (ch == ' ' || ch == '\t' || ch == '\r') {
+            if (!cur.empty()) t.push_back(cur);
+            cur.clear();
+        } else {
+            cur += ch;
+        }
+    }
+    if (!cur.empty()) t.push_back(cur);
+    return t;
+}
+
+double num(const std::string &s) { return std::strtod(s.c_str(), nullptr); }
+
+int writeProteinAsciiMode(const char *records, const char *out, double time) {
+    std::ifstream in(records);
+    std::string line;
+    std::vector<int> tags;
+    std::vector<int64_t> gids;
+    std::vector<AlensProtein> prot;
+    while (std::getline(in, line)) {
+        const auto t = tokens(line);
+        if (t.empty()) continue;
+        if (t[0] == "T") {
+            for (size_t k = 1; k < t.size(); k++) tags.push_back(std::atoi(t[k].c_str()));
+        } else if (t[0] == "R") {
+            for (size_t k = 1; k < t.size(); k++) gids.push_back(std::atoll(t[k].c_str()));
+        } else if (t.size() >= 13) {
+            AlensProtein p{};
+            p.gid = std::atoll(t[0].c_str());
+            p.type = std::atoi(t[1].c_str());
+            p.idBind[0] = std::atoi(t[2].c_str());
+            p.idBind[1] = std::atoi(t[3].c_str());
+            for (int d = 0; d < 3; d++) {
+                p.pos[d] = num(t[4 + d]);
+                p.posEnd[0][d] = num(t[7 + d]);
+                p.posEnd[1][d] = num(t[10 + d]);
+            }
+            prot.push_back(p);
+        }
+    }
+    gpu::SylinderSystem::writeProteinAscii(out, prot, tags, gids, time);
+    return 0;
+}
+
+int proteinsMode(const char *runConfig, const char *tubules, const char *setup, double kbt, int steps,
+                 const char *out) {
+    gpu::SylinderSystem rodSystem;
+    rodSystem.initialize(runConfig, tubules, 0, nullptr);
+    rodSystem.setTimer(false);
+    std::ifstream in(setup);
+    std::string line;
+    std::vector<AlensProteinType> types;
+    std::vector<AlensProtein> prot;
+    while (std::getline(in, line)) {
+        const auto t = tokens(line);
+        if (t.empty()) continue;
+        if (t[0] == "S" && t.size() >= 20) {
+            AlensProteinType y{};
+            y.tag = std::atoi(t[1].c_str());
+            y.fixedEnd0 = std::atoi(t[2].c_str());
+            y.useBindVol = std::atoi(t[3].c_str());
+            y.lookupType = std::atoi(t[4].c_str());
+            y.freeLength = num(t[5]);
+            y.kappa = num(t[6]);
+            y.lambda = num(t[7]);
+            y.PtoAPratio = num(t[8]);
+            y.diffUnbound = num(t[9]);
+            y.rc = num(t[10]);
+            y.eps = num(t[11]);
+            for (int e = 0; e < 2; e++) {
+                y.ko_s[e] = num(t[12 + e]);
+                y.ko_d[e] = num(t[14 + e]);
+                y.Ka[e] = num(t[16 + e]);
+                y.Ke[e] = num(t[18 + e]);
+            }
+            types.push_back(y);
+        } else if (t[0] == "P" && t.size() >= 10) {
+            AlensProtein p{};
+            p.gid = std::atoll(t[1].c_str());
+            p.type = std::atoi(t[2].c_str());
+            p.idBind[0] = std::atoi(t[3].c_str());
+            p.idBind[1] = std::atoi(t[4].c_str());
+            p.distBind[0] = num(t[5]);
+            p.distBind[1] = num(t[6]);
+            for (int d = 0; d < 3; d++) p.pos[d] = num(t[7 + d]);
+            prot.push_back(p);
+        }
+    }
+    if (types.empty()) throw std::runtime_error(std::string("no species in ") + setup);
+    rodSystem.setProteinTypes(types, kbt);
+    rodSystem.setProteins(prot);
+    std::string counts;
+    for (int s = 0; s < steps; s++) {
+        rodSystem.prepareStep();
+        const AlensKmcStats st = rodSystem.calcBindInteraction();
+        rodSystem.runStep();
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "%s[%d, %d, %d, %d, %d, %d, %d, %d]", s ? ", " : "", st.nU, st.nS, st.nD,
+                      st.nUS, st.nSU, st.nSD, st.nDS, rodSystem.lastStats().nBilateral);
+        counts += buf;
+    }
+    const auto res = rodSystem.getProteins();
+    std::FILE *f = std::fopen(out, "w");
+    if (!f) throw std::runtime_error(std::string("cannot write ") + out);
+    for (const AlensProtein &p : res) {
+        std::fprintf(f, "%lld %d %d %d %.17g %.17g", (long long)p.gid, p.type, p.idBind[0], p.idBind[1],
+                     p.distBind[0], p.distBind[1]);
+        for (int d = 0; d < 3; d++) std::fprintf(f, " %.17g", p.pos[d]);
+        for (int e = 0; e < 2; e++)
+            for (int d = 0; d < 3; d++) std::fprintf(f, " %.17g", p.posEnd[e][d]);
+        std::fprintf(f, "\n");
+    }
+    std::fclose(f);
+    std::printf("{\"steps\": %d, \"counts\": [%s], \"step_count\": %ld}\n", steps, counts.c_str(),
+                rodSystem.getStepCount());
+    return 0;
+}
+
+}  // namespace
+
 int main(int argc, char **argv) {
+    if (argc == 5 && std::strcmp(argv[1], "--write-protein-ascii") == 0) {
+        try {
+            return writeProteinAsciiMode(argv[2], argv[3], std::strtod(argv[4], nullptr));
+        } catch (const std::exception &e) {
+            std::fprintf(stderr, "facade_driver: %s\n", e.what());
+            return 1;
+        }
+    }
+    if (argc == 8 && std::strcmp(argv[1], "--proteins") == 0) {
+        try {
+            return proteinsMode(argv[2], argv[3], argv[4], std::strtod(argv[5], nullptr), std::atoi(argv[6]),
+                                argv[7]);
+        } catch (const std::exception &e) {
+            std::fprintf(stderr, "facade_driver: %s\n", e.what());
+            return 1;
+        }
+    }
     if (argc >= 3 && std::strcmp(argv[1], "--host-checks") == 0) return hostChecks(argv[2], argc - 3, argv + 3);
     if (argc == 5 && std::strcmp(argv[1], "--write-vtk") == 0) {
         try {

@@ -163,7 +163,7 @@ __device__ __forceinline__ void kmc_wrap_point(const KmcRep &Q, double p[3]) {
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }
 
 // rod view and cell counts
-__global__ void k_kmc_bin(KmcDev K, DevState S) {
+__global__ void k_kmc_bin(KmcDev K, DevState S, int count) {
     ALENS_PDL_PROLOGUE();
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         const KmcRep &Q = K.rep[S.rodRep[r]];
@@ -175,6 +175,7 @@ __global__ void k_kmc_bin(KmcDev K, DevState S) {
         const bool sphere = L < 2.0 * S.rad[r];
         K.rodC[r] = make_kd4(p[0], p[1], p[2], 0.5 * L);
         K.rodA[r] = make_kd4(a[0], a[1], a[2], sphere ? 1.0 : 0.0);
+        if (!count) continue;
         int c[3];
         for (int d = 0; d < 3; d++) c[d] = kmc_cell_coord(p[d], Q.lo[d], Q.cellsz[d], Q.ncell[d]);
         atomicAdd(&K.cellCount[Q.cellOffset + (c[2] * Q.ncell[1] + c[1]) * Q.ncell[0] + c[0]], 1);
@@ -207,13 +208,13 @@ __device__ __forceinline__ float fmaxf_(float a, float b) { return a > b ? a : b
 __device__ __forceinline__ float fminf_(float a, float b) { return a < b ? a : b; }
 
 // one Gauss-Legendre panel of the integrand over s in [a, b]
-__device__ float sd_panel(float a, float b, float d2, float A, float c) {
+__device__ float sd_panel(float a, float b, float d2, float A, float c, float sc) {
     const float h = 0.5f * (b - a), m = 0.5f * (a + b);
     float acc = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         const float s = m + h * kGLx[k];
-        const float x = sqrtf(d2 + s * s) - c;
+        const float x = sc * sqrtf(d2 + s * s) - c;
         acc = acc + kGLw[k] * kmc_expf(-(A * (x * x)));
     }
     return h * acc;
@@ -221,23 +222,34 @@ __device__ float sd_panel(float a, float b, float d2, float A, float c) {
 
 // per-candidate constants of the integral
 struct SdGeom {
-    float d2, A, c;
+    float d2, A, c, k;   // exponent -A (k r - c)^2, r = sqrt(d2 + s^2)
     float lo[2], hi[2], step[2];
     int n[2];
 };
 
 // the integrand's support within [sA, sB]: head distances within w of c,
 // |s| in [sl, sh]; at most two arcs, each cut into panels of at most w/4
+// lookupType 1: the stretch is (1 - D/d) r, d the distance from the axis;
+// head distances up to ell0 + D + w as for lookupType 0, none when d <= D
 __device__ __forceinline__ void sd_geom(float d2, float sA, float sB, const KmcType &T, SdGeom &G) {
     const float rO = T.rOuterf, w = T.wf;
     G.d2 = d2;
     G.A = T.Af;
     G.c = T.cf;
+    G.k = 1.0f;
     G.n[0] = G.n[1] = 0;
-    const float ro2 = rO * rO;
+    float ro2 = rO * rO;
     if (!(d2 < ro2)) return;
+    float ri = G.c - w;
+    if (T.lookup == 1) {
+        G.k = 1.0f - T.Df / sqrtf(d2);
+        if (!(G.k > 0.0f)) return;
+        const float rh = (G.c + w) / G.k;
+        if (rh < rO) ro2 = rh * rh;
+        if (!(d2 < ro2)) return;
+        ri = (G.c - w) / G.k;
+    }
     const float sh = sqrtf(ro2 - d2);
-    const float ri = G.c - w;
     const float sl = (ri > 0.0f && ri * ri > d2) ? sqrtf(ri * ri - d2) : 0.0f;
     int k = 0;
     float l = fmaxf_(sA, -sh), h = fminf_(sB, -sl);
@@ -277,7 +289,7 @@ __device__ float sd_integral_warp(const SdGeom &G, int lane) {
     for (int k = lane; k < m; k += 32) {
         float a, b;
         sd_edges(G, k, &a, &b);
-        s = s + sd_panel(a, b, G.d2, G.A, G.c);
+        s = s + sd_panel(a, b, G.d2, G.A, G.c, G.k);
     }
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) s = s + __shfl_down_sync(0xffffffffu, s, off);
@@ -358,6 +370,28 @@ __device__ int kmc_pick_fix(const KmcWarpBuf &B, int n, unsigned long long roll,
     return last;
 }
 
+// Distance from point P to the axis segment of rod r (minimum image).
+__device__ __forceinline__ double kmc_dist_point_seg(const KmcDev &K, const KmcRep &Q, const double P[3], int r) {
+    const KDouble4 C = K.rodC[r], A = K.rodA[r];
+    double u[3] = {P[0] - C.x, P[1] - C.y, P[2] - C.z};
+    for (int d = 0; d < 3; d++)
+        if (Q.pbc[d]) u[d] = u[d] - Q.L[d] * floor(u[d] / Q.L[d] + 0.5);
+    double t = u[0] * A.x + u[1] * A.y + u[2] * A.z;
+    t = t > C.w ? C.w : (t < -C.w ? -C.w : t);
+    const double q0 = u[0] - t * A.x, q1 = u[1] - t * A.y, q2 = u[2] - t * A.z;
+    return sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+}
+
+// ProteinData::getProteinForceLength (Protein/ProteinData.hpp:171-195): the
+// heads' distance ell less the rod diameter (lookupType 0), or scaled by
+// 1 - D/d, d the distance of head 0 from the segment of head 1's rod (1)
+__device__ __forceinline__ double kmc_force_length(const KmcDev &K, const KmcRep &Q, const KmcType &T,
+                                                   const double P0[3], int r1, double ell) {
+    if (T.lookup == 0) return ell - K.D;
+    const double d = kmc_dist_point_seg(K, Q, P0, r1);
+    return (1.0 - K.D / d) * ell;
+}
+
 // prepared per unbound / singly bound protein for the warp kernel: the
 // stencil centre cell, the search point relative to it (FP32), the bound
 // head's rod axis (FP32), the stage
@@ -404,7 +438,7 @@ __global__ void __launch_bounds__(256) k_kmc_prep(KmcDev K, int *code, KmcTask *
             for (int k = 0; k < 3; k++)
                 if (Q.pbc[k]) dv[k] = dv[k] - Q.L[k] * floor(dv[k] / Q.L[k] + 0.5);
             const double ell = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
-            const double x = (ell - K.D) - T.ell0;
+            const double x = kmc_force_length(K, Q, T, P[0], Q.rodOffset + id[1], ell) - T.ell0;
             const double M = T.Ads * (x * x);
             const double g = kmc_exp(M);
             const double p0 = (T.koD[0] * g) * T.dt, p1 = (T.koD[1] * g) * T.dt;
@@ -656,7 +690,7 @@ __global__ void __launch_bounds__(32 * kKmcWarps) k_kmc_bind(KmcDev K, int *code
                 for (int k = lane; k < m; k += 32) {
                     float a, bb;
                     sd_edges(G, k, &a, &bb);
-                    B.panel[k] = sd_panel(a, bb, G.d2, G.A, G.c);
+                    B.panel[k] = sd_panel(a, bb, G.d2, G.A, G.c, G.k);
                 }
                 __syncwarp();
                 const float target = frac * B.I[j];
@@ -684,7 +718,7 @@ __global__ void __launch_bounds__(32 * kKmcWarps) k_kmc_bind(KmcDev K, int *code
                     for (int round = 0; round < 4; round++) {
                         const float step = (x1 - x0) / 32.0f;
                         const float xk = lane == 31 ? x1 : x0 + step * (float)(lane + 1);
-                        const bool ge = !(sd_panel(a, xk, G.d2, G.A, G.c) < t);
+                        const bool ge = !(sd_panel(a, xk, G.d2, G.A, G.c, G.k) < t);
                         const unsigned gm = __ballot_sync(0xffffffffu, ge);
                         const int first = gm ? __ffs(gm) - 1 : 31;
                         const float nx1 = __shfl_sync(0xffffffffu, xk, first);
@@ -836,7 +870,22 @@ __global__ void k_kmc_springs(KmcDev K, DevState S, int userTotal, int linkCap) 
         S.linkLocal[L] = Q.userLinks + (K.dScan[p] - K.dScan[Q.protOffset]);
         S.linkSI[L] = pr.distBind[0];
         S.linkSJ[L] = pr.distBind[1];
-        S.linkRest[L] = T.c;
+        double rest = T.c;
+        if (T.lookup == 1) {
+            // rest length so that the spring's separation (head distance -
+            // rest) is the lookupType 1 stretch at the current geometry
+            const int r0 = Q.rodOffset + pr.idBind[0], r1 = Q.rodOffset + pr.idBind[1];
+            const KDouble4 C0 = K.rodC[r0], A0 = K.rodA[r0], C1 = K.rodC[r1], A1 = K.rodA[r1];
+            const double P0[3] = {C0.x + pr.distBind[0] * A0.x, C0.y + pr.distBind[0] * A0.y,
+                                  C0.z + pr.distBind[0] * A0.z};
+            double dv[3] = {(C1.x + pr.distBind[1] * A1.x) - P0[0], (C1.y + pr.distBind[1] * A1.y) - P0[1],
+                            (C1.z + pr.distBind[1] * A1.z) - P0[2]};
+            for (int d = 0; d < 3; d++)
+                if (Q.pbc[d]) dv[d] = dv[d] - Q.L[d] * floor(dv[d] / Q.L[d] + 0.5);
+            const double ell = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+            rest = T.ell0 + (K.D * ell) / kmc_dist_point_seg(K, Q, P0, r1);
+        }
+        S.linkRest[L] = rest;
         S.linkKappa[L] = T.kappa;
     }
 }
@@ -865,7 +914,11 @@ int grid_kmc(int n, int threads) {
 }  // namespace
 
 void launch_kmc_bin(const KmcDev &K, const DevState &S, cudaStream_t st) {
-    launch_pdl(k_kmc_bin, dim3(grid_kmc(S.nRods, 256)), dim3(256), 0, st, K, S);
+    launch_pdl(k_kmc_bin, dim3(grid_kmc(S.nRods, 256)), dim3(256), 0, st, K, S, 1);
+}
+
+void launch_kmc_view(const KmcDev &K, const DevState &S, cudaStream_t st) {
+    launch_pdl(k_kmc_bin, dim3(grid_kmc(S.nRods, 256)), dim3(256), 0, st, K, S, 0);
 }
 
 void launch_kmc_scatter(const KmcDev &K, const DevState &S, cudaStream_t st) {

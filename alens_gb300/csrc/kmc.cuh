@@ -29,10 +29,10 @@ __host__ __device__ inline KDouble4 make_kd4(double x, double y, double z, doubl
 // Per species: the rates of Protein/ProteinModel.md with dt folded in.
 struct KmcType {
     double ell0;        // rest length (freeLength)
-    double c;           // head distance of zero stretch: ell0 + D (lookupType 0)
+    double c;           // centre of the S->D exponent: ell0 + D (lookupType 0), ell0 (1)
     double A;           // (1 - lambda) kappa / (2 KBT): S->D Boltzmann exponent
     double w;           // support half-width of the S->D integrand in head distance
-    double rOuter;      // c + w: farthest head distance with a non-zero S->D rate
+    double rOuter;      // ell0 + D + w: farthest head distance with a non-zero S->D rate
     double Ads;         // lambda kappa / (2 KBT): D->S load sensitivity
     double rcap;        // U->S capture radius: max(rc, sqrt(6 diffUnbound dt))
     double PtoAP;       // parallel / antiparallel S->D binding ratio
@@ -47,7 +47,8 @@ struct KmcType {
     float rcapf, rOuterf, wf, Af, cf;
     float usCoeff[2], suProbf[2], sdCoeff[2];
     float prefPar, prefAnti;  // PtoAPratio prefactor for a parallel / antiparallel rod
-    float pad;
+    float Df;                 // rod diameter (lookupType 1 stretch factor 1 - D/d)
+    int lookup;               // 0: stretch r - D; 1: (1 - D/d) r (Protein/ProteinData.hpp:171-195)
 };
 
 struct KmcRep {
@@ -84,6 +85,7 @@ constexpr int kKmcErrCand = 1;      // a protein had more candidates (its state 
 constexpr int kKmcErrSpring = 2;    // a spring row fell outside the link capacity
 
 void launch_kmc_bin(const KmcDev &K, const DevState &S, cudaStream_t st);
+void launch_kmc_view(const KmcDev &K, const DevState &S, cudaStream_t st);  // rod view only, no cell counts
 void launch_kmc_scatter(const KmcDev &K, const DevState &S, cudaStream_t st);
 int launch_kmc_bind(const KmcDev &K, cudaStream_t st);  // returns kernels launched
 // doubly bound flags, their scan and the spring rows at link offset

@@ -369,3 +369,217 @@ def read_time_step_info(path):
     with open(path) as f:
         vals = f.read().split()
     return int(vals[0]), int(vals[1]), float(vals[2])
+
+
+# ---------------------------------------------------------------- proteins
+_PROTEIN_KEYS_SCALAR = ("tag", "fixedEnd0", "useBindVol", "lookupType", "freeLength", "kappa", "lambda",
+                        "PtoAPratio", "diffUnbound", "rc", "eps", "freeNumber")
+_PROTEIN_KEYS_PAIR = ("ko_s", "ko_d", "Ka", "Ke")
+
+
+def read_protein_config(path):
+    """ProteinConfig.yaml (Protein/ProteinConfig.cpp:6-45, keys of
+    ProteinType::readFromYaml, Protein/ProteinType.hpp:81-129): KBT and the
+    `proteins:` list, parsed as flat YAML.  Returns (KBT, species) with one
+    AlensProteinType per list entry, in file order, and the entries' raw
+    dicts (freeNumber, fixedLocationPerMT, ...) beside them."""
+    from .capi import make_protein_type
+    kbt, entries, cur, inside = 0.00411, [], None, False
+
+    def val(v):
+        v = v.strip().strip("\"'")
+        if v.startswith("["):
+            return [val(x) for x in v.strip("[] ").split(",") if x.strip()]
+        low = v.lower()
+        if low in ("true", "yes"):
+            return 1
+        if low in ("false", "no"):
+            return 0
+        try:
+            return float(v)
+        except ValueError:
+            return v
+
+    with open(path) as f:
+        for raw in f:
+            line = raw.split("#", 1)[0]
+            if not line.strip():
+                continue
+            nested = line[0] in " \t-"
+            if not nested:
+                k, _, v = line.partition(":")
+                inside = k.strip() == "proteins"
+                if k.strip() == "KBT":
+                    kbt = float(v)
+                continue
+            if not inside:
+                continue
+            t = line.strip()
+            if t.startswith("-"):
+                cur = {}
+                entries.append(cur)
+                t = t[1:].strip()
+            if ":" not in t or cur is None:
+                continue
+            k, v = (x.strip() for x in t.split(":", 1))
+            cur[k] = val(v) if v else []
+    species = []
+    for e in entries:
+        pair = {k: tuple(float(x) for x in (e.get(k) or [0.0, 0.0])) for k in _PROTEIN_KEYS_PAIR}
+        species.append(make_protein_type(
+            tag=int(e.get("tag", 0)), freeLength=float(e.get("freeLength", 0.05)), rc=float(e.get("rc", 0.0)),
+            kappa=float(e.get("kappa", 204.7)), lambda_=float(e.get("lambda", 0.0)),
+            diffUnbound=float(e.get("diffUnbound", 4.5)), useBindVol=bool(e.get("useBindVol", 0)),
+            eps=float(e.get("eps", 0.0)), PtoAPratio=float(e.get("PtoAPratio", 1.0)),
+            fixedEnd0=bool(e.get("fixedEnd0", 0)), lookupType=int(e.get("lookupType", 0)), **pair))
+    return kbt, species, entries
+
+
+def read_protein_ascii(path):
+    """ProteinAscii_<id>.dat / ProteinInitial.dat: two header lines (count,
+    time), then 'P gid tag x0 y0 z0 x1 y1 z1 idBind0 idBind1' lines
+    (Protein/ProteinData.hpp:545-564; read as
+    TubuleSystem::setInitialProteinFromFile, SRC/TubuleSystem.cpp:761-789).
+    idBind are rod gids (-1 unbound)."""
+    gid, tag, end0, end1, ids = [], [], [], [], []
+    with open(path) as f:
+        lines = f.read().splitlines()
+    for ln in lines[2:]:
+        p = ln.split()
+        if len(p) < 11 or p[0] != "P":
+            continue
+        gid.append(int(p[1]))
+        tag.append(int(p[2]))
+        end0.append([float(x) for x in p[3:6]])
+        end1.append([float(x) for x in p[6:9]])
+        ids.append([int(p[9]), int(p[10])])
+    return {"gid": np.array(gid, np.int64), "tag": np.array(tag, np.int32),
+            "end0": np.array(end0, float).reshape(-1, 3), "end1": np.array(end1, float).reshape(-1, 3),
+            "idBind": np.array(ids, np.int64).reshape(-1, 2)}
+
+
+def proteins_from_ascii(rec, rods: RodState, species, cfg: AlensConfig):
+    """AlensProtein records from read_protein_ascii's output: the binding of
+    each end rebuilt from its position as TubuleSystem::updateBindWithGid
+    does with reconstruct = true (SRC/TubuleSystem.cpp:482-563): the bound
+    rod's periodic image nearest the protein, distBind = (end - centre) .
+    direction; kept inside L/2, clamped within 1.01 L/2 (or on a sphere),
+    the end released otherwise.  Tags select the species (list order)."""
+    from .capi import protein_array
+    n = rec["gid"].shape[0]
+    out = protein_array(n)
+    index = {int(g): i for i, g in enumerate(rods.gid)}
+    tag_index = {int(t.tag): k for k, t in enumerate(species)}
+    axis = quat_to_axis(rods.quat)
+    lo = np.array([cfg.simBoxLow[d] for d in range(3)])
+    L = np.array([cfg.simBoxHigh[d] - cfg.simBoxLow[d] for d in range(3)])
+    pbc = [bool(cfg.simBoxPBC[d]) for d in range(3)]
+    for p in range(n):
+        t = int(rec["tag"][p])
+        if t not in tag_index:
+            raise ValueError(f"protein {int(rec['gid'][p])}: tag {t} not in the species list")
+        out["gid"][p] = rec["gid"][p]
+        out["type"][p] = tag_index[t]
+        ends = (rec["end0"][p], rec["end1"][p])
+        pos = 0.5 * (ends[0] + ends[1])
+        out["pos"][p] = pos
+        for e in range(2):
+            g = int(rec["idBind"][p, e])
+            if g == -1:
+                continue
+            if g not in index:
+                raise ValueError(f"protein {int(rec['gid'][p])}: rod gid {g} not found")
+            r = index[g]
+            c = rods.pos[r].copy()
+            for d in range(3):
+                if pbc[d]:
+                    c[d] += L[d] * np.round((pos[d] - c[d]) / L[d])
+            dist = float(np.dot(ends[e] - c, axis[r]))
+            half = 0.5 * float(rods.length[r])
+            sphere = rods.length[r] < 2.0 * rods.radius[r]
+            if -half < dist < half:
+                pass
+            elif -1.01 * half < dist < 1.01 * half or sphere:
+                dist = min(max(dist, -half), half)
+            else:
+                continue
+            out["idBind"][p, e] = r
+            out["distBind"][p, e] = dist
+    return out
+
+
+def write_protein_ascii(path, proteins, species, rod_gid, time: float = 0.0):
+    """ProteinAscii_<id>.dat: the header of ProteinAsciiHeader::writeAscii
+    and one line per protein as ProteinData::writeAscii
+    (Protein/ProteinData.hpp:545-564, 705-718): the heads' positions when
+    both are bound, the centre twice otherwise; bound rods as gids.  Same
+    bytes as the C++ facade's writer."""
+    n = proteins.shape[0]
+    lines = [f"{n} \n {time:f}\n"]
+    for p in proteins:
+        ids = [int(rod_gid[i]) if i >= 0 else -1 for i in p["idBind"]]
+        if ids[0] != -1 and ids[1] != -1:
+            a, b = p["posEnd"][0], p["posEnd"][1]
+        else:
+            a = b = p["pos"]
+        tag = int(species[int(p["type"])].tag)
+        lines.append("P %d %d %.6g %.6g %.6g %.6g %.6g %.6g %d %d\n"
+                     % (int(p["gid"]), tag, a[0], a[1], a[2], b[0], b[1], b[2], ids[0], ids[1]))
+    with open(path, "w") as f:
+        f.write("".join(lines))
+
+
+def read_init_box(path):
+    """initBoxLow / initBoxHigh of a RunConfig.yaml (default: the sim box)."""
+    vals = {}
+    with open(path) as f:
+        for line in f:
+            line = line.split("#", 1)[0]
+            if ":" in line and line[:1] not in " \t-":
+                k, v = line.split(":", 1)
+                vals[k.strip()] = v.strip()
+
+    def vec(key, default):
+        v = vals.get(key, vals.get(default))
+        return np.array([float(x) for x in v.strip("[] ").split(",")])
+    return vec("initBoxLow", "simBoxLow"), vec("initBoxHigh", "simBoxHigh")
+
+
+def proteins_from_config(entries, species, rods: RodState, init_low, init_high, seed: int = 0):
+    """Initial proteins from ProteinConfig.yaml's numbers, as
+    TubuleSystem::setInitialProteinFromConfig (SRC/TubuleSystem.cpp:331-442):
+    per species, freeNumber unbound proteins uniform in the init box, then
+    for every rod one singly bound protein (end 0) per fixedLocationPerMT
+    entry, at entry x L/2 from the centre (uniform on the rod when the entry
+    lies outside [-1, 1]).  Gids run over all species without repeats (the
+    reference numbers each species from 0, which would give proteins of
+    different species the same rolls); the random numbers come from numpy
+    (seed), not the reference's generator.  initCircularX is not applied."""
+    from .capi import protein_array
+    rng = np.random.default_rng(seed)
+    parts = []
+    gid = 0
+    for k, e in enumerate(entries):
+        nfree = int(e.get("freeNumber", 0) or 0)
+        locs = e.get("fixedLocationPerMT") or []
+        locs = locs if isinstance(locs, list) else [locs]
+        p = protein_array(nfree)
+        p["gid"] = gid + np.arange(nfree)
+        p["type"] = k
+        p["pos"] = init_low + rng.uniform(0.0, 1.0, (nfree, 3)) * (init_high - init_low)
+        gid += nfree
+        parts.append(p)
+        if locs:
+            nf = rods.n * len(locs)
+            q = protein_array(nf)
+            q["gid"] = gid + np.arange(nf)
+            q["type"] = k
+            r = np.repeat(np.arange(rods.n), len(locs))
+            loc = np.tile(np.array(locs, float), rods.n)
+            dist = np.where(np.abs(loc) > 1.0, (rng.uniform(0.0, 1.0, nf) - 0.5) * rods.length[r],
+                            loc * rods.length[r] * 0.5)
+            q["idBind"][:, 0] = r
+            q["distBind"][:, 0] = dist
+            gid += nf
+            parts.append(q)
+    return np.concatenate(parts) if parts else protein_array(0)

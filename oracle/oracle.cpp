@@ -777,9 +777,9 @@ void build_constraints(OrcCtx *x) {
     };
     for (size_t L = 0; L < x->linkI.size(); L++)
         add_link(x->linkI[L], x->linkJ[L], x->linkSI[L], x->linkSJ[L], x->linkRest[L], x->linkKappa[L]);
-    kmc_springs(x);
     for (size_t L = 0; L < x->springI.size(); L++)
-        add_link(x->springI[L], x->springJ[L], x->springSI[L], x->springSJ[L], x->springRest[L],
+        if (x->springI[L] < n && x->springJ[L] < n)
+            add_link(x->springI[L], x->springJ[L], x->springSI[L], x->springSJ[L], x->springRest[L],
                  x->springKappa[L]);
     x->nbil = (int)x->blocks.size();
     const int nc = x->ncoll + x->nbil;
@@ -1196,7 +1196,9 @@ int orc_set_rods(OrcCtx *x, int n, const int64_t *gid, const double *pos,
     x->prevKeys.clear();
     x->prevGamma.clear();
     x->detected = x->solved = false;
-    return setup_grid(x);
+    const int rc = setup_grid(x);
+    kmc_springs(x);  // the protein springs are rebuilt from the new rods
+    return rc;
 }
 
 int orc_update_rods(OrcCtx *x, int n, const double *pos, const double *orientation) {
@@ -1255,6 +1257,7 @@ int orc_set_links(OrcCtx *x, int n, const int32_t *idxI, const int32_t *idxJ, co
     x->linkSJ.assign(sJ, sJ + n);
     x->linkRest.assign(rest, rest + n);
     x->linkKappa.assign(kappa, kappa + n);
+    kmc_springs(x);  // the library rebuilds the protein springs with its link rows
     return ALENS_OK;
 }
 

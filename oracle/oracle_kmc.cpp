@@ -142,6 +142,8 @@ struct Kt {
     float rcapf, rOuterf, wf, Af, cf;
     float usCoeff[2], suProbf[2], sdCoeff[2];
     float prefPar, prefAnti;
+    float Df;
+    int lookup;
 };
 
 double bind_volume(double a, double c) {
@@ -160,10 +162,13 @@ Kt make_type(const AlensProteinType &in, double KBT, double D, double dt) {
     const double Ka[2] = {in.Ka[0] / 602.0, in.Ka[1] / 602.0};
     const double Ke[2] = {in.useBindVol ? in.Ke[0] / 602.0 : in.Ke[0], in.useBindVol ? in.Ke[1] / 602.0 : in.Ke[1]};
     T.ell0 = in.freeLength;
-    T.c = in.freeLength + D;
+    T.lookup = in.lookupType;
+    // centre of the S->D exponent: the head distance less D equals ell0
+    // (lookupType 0), or the scaled distance (1 - D/d) r equals ell0 (1)
+    T.c = in.lookupType == 0 ? in.freeLength + D : in.freeLength;
     T.A = ((1.0 - in.lambda) * in.kappa) / (2.0 * KBT);
     T.w = 6.0 / std::sqrt(T.A);
-    T.rOuter = T.c + T.w;
+    T.rOuter = (in.freeLength + D) + T.w;
     T.Ads = (in.lambda * in.kappa) / (2.0 * KBT);
     const double rd = std::sqrt((6.0 * in.diffUnbound) * dt);
     T.rcap = in.rc > rd ? in.rc : rd;
@@ -192,6 +197,7 @@ Kt make_type(const AlensProteinType &in, double KBT, double D, double dt) {
     const float r = (float)in.PtoAPratio;
     T.prefPar = r < 1.0f ? r : 1.0f;
     T.prefAnti = r > 1.0f ? 1.0f / r : 1.0f;
+    T.Df = (float)D;
     return T;
 }
 
@@ -199,12 +205,12 @@ Kt make_type(const AlensProteinType &in, double KBT, double D, double dt) {
 float fmaxf_(float a, float b) { return a > b ? a : b; }
 float fminf_(float a, float b) { return a < b ? a : b; }
 
-float panel(float a, float b, float d2, float A, float c) {
+float panel(float a, float b, float d2, float A, float c, float sc) {
     const float h = 0.5f * (b - a), m = 0.5f * (a + b);
     float acc = 0.0f;
     for (int k = 0; k < 8; k++) {
         const float s = m + h * kX8[k];
-        const float x = std::sqrt(d2 + s * s) - c;
+        const float x = sc * std::sqrt(d2 + s * s) - c;
         acc = acc + kW8[k] * kexpf(-(A * (x * x)));
     }
     return h * acc;
@@ -213,8 +219,11 @@ float panel(float a, float b, float d2, float A, float c) {
 // support of the integrand within [sA, sB]: head distances within w of
 // c = ell0 + D, i.e. |s| in [sl, sh]; at most two arcs of at most 64
 // panels of width <= w/4 each
+// lookupType 1 (stretch (1 - D/d) r, d the distance from the axis): the
+// exponent -A (k r - c)^2 with k = 1 - D/d, head distances up to
+// ell0 + D + w as for lookupType 0, no support when d <= D
 struct SdGeom {
-    float d2, A, c;
+    float d2, A, c, k;
     float lo[2], hi[2], step[2];
     int n[2];
 };
@@ -225,10 +234,19 @@ SdGeom sd_geom(float d2, float sA, float sB, const Kt &T) {
     G.d2 = d2;
     G.A = T.Af;
     G.c = T.cf;
-    const float ro2 = rO * rO;
+    G.k = 1.0f;
+    float ro2 = rO * rO;
     if (!(d2 < ro2)) return G;
+    float ri = G.c - w;
+    if (T.lookup == 1) {
+        G.k = 1.0f - T.Df / std::sqrt(d2);
+        if (!(G.k > 0.0f)) return G;
+        const float rh = (G.c + w) / G.k;
+        if (rh < rO) ro2 = rh * rh;
+        if (!(d2 < ro2)) return G;
+        ri = (G.c - w) / G.k;
+    }
     const float sh = std::sqrt(ro2 - d2);
-    const float ri = G.c - w;
     const float sl = (ri > 0.0f && ri * ri > d2) ? std::sqrt(ri * ri - d2) : 0.0f;
     int k = 0;
     float l = fmaxf_(sA, -sh), h = fminf_(sB, -sl);
@@ -268,7 +286,7 @@ float sd_integral(const SdGeom &G) {
     for (int k = 0; k < m; k++) {
         float a, b;
         sd_edges(G, k, &a, &b);
-        s[k % 32] = s[k % 32] + panel(a, b, G.d2, G.A, G.c);
+        s[k % 32] = s[k % 32] + panel(a, b, G.d2, G.A, G.c, G.k);
     }
     for (int off = 16; off >= 1; off >>= 1)
         for (int l = 0; l < off; l++) s[l] = s[l] + s[l + off];
@@ -286,7 +304,7 @@ float sd_invert(const SdGeom &G, float target) {
     for (int k = 0; k < m; k++) {
         float a, b;
         sd_edges(G, k, &a, &b);
-        const float P = panel(a, b, G.d2, G.A, G.c);
+        const float P = panel(a, b, G.d2, G.A, G.c, G.k);
         if (target < cum + P) {
             kp = k;
             t = target - cum;
@@ -304,7 +322,7 @@ float sd_invert(const SdGeom &G, float target) {
         int first = 31;
         for (int k = 0; k < 32; k++) xk[k] = k == 31 ? x1 : x0 + step * (float)(k + 1);
         for (int k = 0; k < 32; k++)
-            if (!(panel(a, xk[k], G.d2, G.A, G.c) < t)) {
+            if (!(panel(a, xk[k], G.d2, G.A, G.c, G.k) < t)) {
                 first = k;
                 break;
             }
@@ -487,6 +505,25 @@ Grid make_grid(const OrcCtx *x, RodView &V, double reach) {
     return G;
 }
 
+// distance from P to the axis segment of rod r (minimum image)
+double dist_point_seg(const OrcCtx *x, const RodView &V, const double P[3], int r) {
+    double u[3];
+    for (int d = 0; d < 3; d++) u[d] = min_image(x->cfg, d, P[d] - V.c[3 * r + d]);
+    const double *a = &V.a[3 * r];
+    double t = u[0] * a[0] + u[1] * a[1] + u[2] * a[2];
+    t = t > V.hl[r] ? V.hl[r] : (t < -V.hl[r] ? -V.hl[r] : t);
+    const double q0 = u[0] - t * a[0], q1 = u[1] - t * a[1], q2 = u[2] - t * a[2];
+    return std::sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+}
+
+// ProteinData::getProteinForceLength (Protein/ProteinData.hpp:171-195): the
+// heads' distance ell less D (lookupType 0), or scaled by 1 - D/d with d the
+// distance of head 0 from the segment of head 1's rod (lookupType 1)
+double force_length(const OrcCtx *x, const RodView &V, const Kt &T, const double P0[3], int r1, double ell) {
+    if (T.lookup == 0) return ell - x->kmcD;
+    return (1.0 - x->kmcD / dist_point_seg(x, V, P0, r1)) * ell;
+}
+
 struct Cand {
     int li;
     float v0, v1, v2, v3;  // U: Lc, lo, hl; S: t0, d2, hl, axis dot
@@ -655,7 +692,7 @@ int protein_step(const OrcCtx *x, const RodView &V, const Grid &G, const Kt &T, 
         double dv[3];
         for (int d = 0; d < 3; d++) dv[d] = min_image(cf, d, P[1][d] - P[0][d]);
         const double ell = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
-        const double xx = (ell - x->kmcD) - T.ell0;
+        const double xx = force_length(x, V, T, P[0], pr.idBind[1], ell) - T.ell0;
         const double M = T.Ads * (xx * xx);
         const double g = kexp(M);
         const double p0 = (T.koD[0] * g) * T.dt, p1 = (T.koD[1] * g) * T.dt;
@@ -691,7 +728,7 @@ int protein_step(const OrcCtx *x, const RodView &V, const Grid &G, const Kt &T, 
 bool nonneg(double v) { return std::isfinite(v) && v >= 0.0; }
 
 bool type_ok(const AlensProteinType &p) {
-    bool ok = p.lookupType == 0 && std::isfinite(p.kappa) && p.kappa > 0.0 && std::isfinite(p.lambda) &&
+    bool ok = (p.lookupType == 0 || p.lookupType == 1) && std::isfinite(p.kappa) && p.kappa > 0.0 && std::isfinite(p.lambda) &&
               p.lambda >= 0.0 && p.lambda < 1.0 && nonneg(p.freeLength) && std::isfinite(p.rc) && p.rc > 0.0 &&
               nonneg(p.eps) && nonneg(p.diffUnbound) && std::isfinite(p.PtoAPratio) && p.PtoAPratio > 0.0;
     for (int e = 0; e < 2; e++)
@@ -708,14 +745,28 @@ void kmc_springs(OrcCtx *x) {
     x->springSJ.clear();
     x->springRest.clear();
     x->springKappa.clear();
+    if (x->prot.empty() || x->ptypes.empty()) return;
+    const RodView V = rod_view(x);
     for (const AlensProtein &p : x->prot) {
         if (p.idBind[0] < 0 || p.idBind[0] >= x->n || p.idBind[1] < 0 || p.idBind[1] >= x->n) continue;
         const AlensProteinType &t = x->ptypes[p.type];
+        double rest = t.freeLength + x->kmcD;
+        if (t.lookupType == 1) {
+            // rest length so that head distance - rest is the lookupType 1
+            // stretch at the current geometry
+            const int r0 = p.idBind[0], r1 = p.idBind[1];
+            double P0[3], dv[3];
+            for (int d = 0; d < 3; d++) P0[d] = V.c[3 * r0 + d] + p.distBind[0] * V.a[3 * r0 + d];
+            for (int d = 0; d < 3; d++)
+                dv[d] = min_image(x->cfg, d, (V.c[3 * r1 + d] + p.distBind[1] * V.a[3 * r1 + d]) - P0[d]);
+            const double ell = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+            rest = t.freeLength + (x->kmcD * ell) / dist_point_seg(x, V, P0, r1);
+        }
         x->springI.push_back(p.idBind[0]);
         x->springJ.push_back(p.idBind[1]);
         x->springSI.push_back(p.distBind[0]);
         x->springSJ.push_back(p.distBind[1]);
-        x->springRest.push_back(t.freeLength + x->kmcD);
+        x->springRest.push_back(rest);
         x->springKappa.push_back(t.kappa);
     }
 }
@@ -731,6 +782,7 @@ int orc_set_protein_types(OrcCtx *x, int n, const AlensProteinType *t, double KB
     x->ptypes.assign(t, t + n);
     x->kmcKBT = KBT;
     x->kmcD = D;
+    kmc_springs(x);
     return ALENS_OK;
 }
 
@@ -750,6 +802,7 @@ int orc_set_proteins(OrcCtx *x, int n, const AlensProtein *p) {
             return ALENS_INVALID_ARG;
     }
     x->prot.assign(p, p + n);
+    kmc_springs(x);
     return ALENS_OK;
 }
 
@@ -794,6 +847,7 @@ int orc_protein_bind_step(OrcCtx *x, AlensKmcStats *st) {
             s.maxCandidates = std::max(s.maxCandidates, nc[p]);
         }
     }
+    kmc_springs(x);
     if (st) *st = s;
     return ALENS_OK;
 }

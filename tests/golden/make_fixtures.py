@@ -8,6 +8,14 @@ physical settings (Examples/DenseMonoLayer/RunConfig.yaml) on a closed
 (non-periodic) 4 x 4 window.  Golden outputs: five oracle steps with one
 bilateral spring between the first two rods (the facade driver's protocol).
 
+Second fixture, proteins: Examples/MixMotorSliding (two parallel 20 um
+rods 0.07 um apart, the first immovable, 100 doubly bound motors of two
+species): its rods (TubuleInitial.dat lines), its proteins (the 'P' lines of
+ProteinInitial.dat), the species of its ProteinConfig.yaml re-emitted as flat
+keys, and the run settings of its RunConfig.yaml.  Golden outputs: the
+oracle's stage counts over five binding + rod steps (a regression pin of the
+oracle; the reference ships no outputs for this path).
+
 usage: python tests/golden/make_fixtures.py /path/to/aLENS
 """
 import json
@@ -109,6 +117,86 @@ def golden(steps=5):
             "pos_head": pos[:8].tolist(), "quat_head": quat[:8].tolist()}
 
 
+MIX_KEYS = ("rngSeed", "dt", "timeSnap", "simBoxHigh", "simBoxLow", "simBoxPBC", "monolayer", "viscosity", "KBT",
+            "conMaxIte", "conResTol", "conSolverChoice", "sylinderColBuf", "sylinderDiameterColRatio",
+            "sylinderLengthColRatio", "sylinderDiameter")
+SPECIES_KEYS = ("tag", "fixedEnd0", "useBindVol", "lookupType", "freeLength", "kappa", "lambda", "PtoAPratio",
+                "diffUnbound", "rc", "eps", "ko_s", "ko_d", "Ka", "Ke")
+
+
+def write_mixmotor_fixture(ref):
+    from alens_gb300 import io
+    src = os.path.join(ref, "Examples", "MixMotorSliding")
+    with open(os.path.join(src, "TubuleInitial.dat")) as f:
+        rods = [ln for ln in f.read().splitlines() if ln[:1] in ("C", "S")]
+    with open(os.path.join(HERE, "mixmotor_tubules.dat"), "w") as out:
+        out.write(f"{len(rods)}\n0\n" + "\n".join(rods) + "\n")
+    with open(os.path.join(src, "ProteinInitial.dat")) as f:
+        lines = f.read().splitlines()
+    prots = [ln for ln in lines[2:] if ln[:1] == "P"]
+    with open(os.path.join(HERE, "mixmotor_proteins.dat"), "w") as out:
+        out.write(f"{len(prots)} \n 0.000000\n" + "\n".join(prots) + "\n")
+    keep = []
+    with open(os.path.join(src, "RunConfig.yaml")) as f:
+        for ln in f:
+            k = ln.split("#", 1)[0].split(":", 1)[0].strip()
+            if k in MIX_KEYS and ln[:1] not in " \t-":
+                keep.append(ln.split("#", 1)[0].rstrip())
+    with open(os.path.join(HERE, "mixmotor_run.yaml"), "w") as out:
+        out.write("# run settings of Examples/MixMotorSliding/RunConfig.yaml\n" + "\n".join(keep) + "\n")
+    kbt, _, entries = io.read_protein_config(os.path.join(src, "ProteinConfig.yaml"))
+    text = ["# species of Examples/MixMotorSliding/ProteinConfig.yaml", f"KBT: {kbt!r}", "proteins:"]
+    for e in entries:
+        first = True
+        for k in SPECIES_KEYS:
+            if k not in e:
+                continue
+            v = e[k]
+            v = "[" + ", ".join(repr(float(x)) for x in v) + "]" if isinstance(v, list) else repr(v)
+            text.append(("  - " if first else "    ") + f"{k}: {v}")
+            first = False
+    with open(os.path.join(HERE, "mixmotor_species.yaml"), "w") as out:
+        out.write("\n".join(text) + "\n")
+    return len(rods), len(prots)
+
+
+def load_mixmotor():
+    from alens_gb300 import io
+    cfg = io.read_run_config(os.path.join(HERE, "mixmotor_run.yaml"))
+    rods, _ = io.read_sylinder_ascii(os.path.join(HERE, "mixmotor_tubules.dat"))
+    kbt, species, _ = io.read_protein_config(os.path.join(HERE, "mixmotor_species.yaml"))
+    rec = io.read_protein_ascii(os.path.join(HERE, "mixmotor_proteins.dat"))
+    prots = io.proteins_from_ascii(rec, rods, species, cfg)
+    return cfg, rods, kbt, species, prots
+
+
+def mixmotor_golden(steps=5):
+    from alens_gb300 import oracle_api as O
+    cfg, rods, kbt, species, prots = load_mixmotor()
+    o = O.OracleSystem(cfg)
+    o.set_rods(rods)
+    o.set_protein_types(species, kbt, float(cfg_diameter(cfg)))
+    o.set_proteins(prots)
+    counts = []
+    for _ in range(steps):
+        st = o.protein_bind_step()
+        r = o.step()
+        counts.append([st[k] for k in ("nU", "nS", "nD", "nUS", "nSU", "nSD", "nDS")] + [r["nBilateral"]])
+    q = o.get_proteins()
+    o.close()
+    return {"steps": steps, "counts": counts, "idBind": q["idBind"].tolist(),
+            "distBind_sum": float(np.nansum(q["distBind"]))}
+
+
+def cfg_diameter(cfg):
+    """sylinderDiameter of the MixMotorSliding run (RunConfig key)."""
+    with open(os.path.join(HERE, "mixmotor_run.yaml")) as f:
+        for ln in f:
+            if ln.split(":", 1)[0].strip() == "sylinderDiameter":
+                return float(ln.split(":", 1)[1].split("#", 1)[0])
+    return 0.025
+
+
 if __name__ == "__main__":
     if len(sys.argv) != 2:
         raise SystemExit("usage: python tests/golden/make_fixtures.py /path/to/aLENS")
@@ -118,3 +206,8 @@ if __name__ == "__main__":
     with open(os.path.join(HERE, "monolayer_window_golden.json"), "w") as f:
         json.dump(g, f, indent=1)
     print(n, "rods;", g["iterations"], g["collisions"])
+    nr, npr = write_mixmotor_fixture(ref)
+    gm = mixmotor_golden()
+    with open(os.path.join(HERE, "mixmotor_golden.json"), "w") as f:
+        json.dump(gm, f, indent=1)
+    print(nr, "rods,", npr, "proteins;", gm["counts"])

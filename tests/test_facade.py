@@ -178,3 +178,51 @@ def test_facade_snapshot_and_restart(gpu_lib, tmp_path):
     assert 'NumberOfLines="0"' not in (folder / "ConBlock_r0_2.vtp").read_text()
     assert len(names) == 15
     assert (tmp_path / "TimeStepInfo.txt").read_text().split()[:2] == ["4", "2"]
+
+
+def test_facade_protein_steps_match_oracle(gpu_lib, tmp_path):
+    """TubuleSystem::step()'s order through the facade (calcBindInteraction,
+    then runStep) on the MixMotorSliding example: two parallel 20 um rods,
+    100 motors of two lookupType 1 species read from its ProteinInitial.dat.
+    After five steps the proteins and the per-step counts equal the oracle's
+    and the committed golden."""
+    cfg, rods, kbt, species, prots = make_fixtures.load_mixmotor()
+    gold = json.load(open(os.path.join(GOLDEN, "mixmotor_golden.json")))
+    setup = tmp_path / "setup.txt"
+    with open(setup, "w") as f:
+        for t in species:
+            f.write("S %d %d %d %d %r %r %r %r %r %r %r %r %r %r %r %r %r %r %r\n" % (
+                t.tag, t.fixedEnd0, t.useBindVol, t.lookupType, t.freeLength, t.kappa, t.lambda_, t.PtoAPratio,
+                t.diffUnbound, t.rc, t.eps, t.ko_s[0], t.ko_s[1], t.ko_d[0], t.ko_d[1], t.Ka[0], t.Ka[1], t.Ke[0],
+                t.Ke[1]))
+        for p in prots:
+            f.write("P %d %d %d %d %r %r %r %r %r\n" % (int(p["gid"]), int(p["type"]), int(p["idBind"][0]),
+                                                      int(p["idBind"][1]), float(p["distBind"][0]),
+                                                      float(p["distBind"][1]), *map(float, p["pos"])))
+    out = tmp_path / "out.txt"
+    exe = build.build_facade_driver()
+    steps = gold["steps"]
+    proc = subprocess.run([str(exe), "--proteins", os.path.join(GOLDEN, "mixmotor_run.yaml"),
+                           os.path.join(GOLDEN, "mixmotor_tubules.dat"), str(setup), repr(kbt), str(steps), str(out)],
+                          capture_output=True, text=True, timeout=300)
+    assert proc.returncode == 0, proc.stderr
+    res = json.loads(proc.stdout.strip().splitlines()[-1])
+    assert res["counts"] == gold["counts"] and res["step_count"] == steps
+    from alens_gb300.oracle_api import OracleSystem
+    o = OracleSystem(cfg)
+    o.set_rods(rods)
+    o.set_protein_types(species, kbt, make_fixtures.cfg_diameter(cfg))
+    o.set_proteins(prots)
+    for _ in range(steps):
+        o.protein_bind_step()
+        o.step()
+    q = o.get_proteins()
+    o.close()
+    rows = [ln.split() for ln in out.read_text().splitlines()]
+    assert len(rows) == q.shape[0]
+    for r, p in zip(rows, q):
+        assert int(r[0]) == int(p["gid"]) and int(r[1]) == int(p["type"])
+        assert [int(r[2]), int(r[3])] == p["idBind"].tolist()
+        got = np.array([float(v) for v in r[4:]])
+        want = np.concatenate([p["distBind"], p["pos"], p["posEnd"].ravel()])
+        assert np.array_equal(got, want, equal_nan=True)

@@ -136,3 +136,45 @@ def test_facade_conblock_writer_matches_python(tmp_path):
         io.write_conblock_pvtp(str(py), 4, b, gid)
         for name in ("ConBlock_4.pvtp", "ConBlock_r0_4.vtp"):
             assert (cpp / name).read_bytes() == (py / name).read_bytes(), (label, name)
+
+
+def test_facade_protein_ascii_writer_matches_python(tmp_path):
+    """The facade's ProteinAscii writer (SylinderSystem::writeProteinAscii)
+    and io.write_protein_ascii produce the same bytes: doubly bound (head
+    positions), singly bound and unbound (the centre twice) proteins of two
+    species, rod gids for the bound ends."""
+    import numpy as np
+    from alens_gb300 import capi, io
+    rng = np.random.default_rng(5)
+    n = 30
+    species = [capi.make_protein_type(tag=7), capi.make_protein_type(tag=2)]
+    rod_gid = np.arange(1000, 1040, dtype=np.int64)
+    p = capi.protein_array(n)
+    p["gid"] = rng.integers(0, 10**6, n)
+    p["type"] = np.arange(n) % 2
+    p["pos"] = rng.uniform(-3, 40, (n, 3))
+    p["idBind"][:10] = rng.integers(0, 40, (10, 2))
+    p["posEnd"][:10] = rng.uniform(0, 40, (10, 2, 3)) * 1.0000001
+    p["idBind"][10:20, 0] = rng.integers(0, 40, 10)
+    p["posEnd"][10:20, 0] = rng.uniform(0, 40, (10, 3))
+    p["pos"][5] = [1e-7, -2.5e-5, 123456.789]
+    build.build_lib()
+    exe = build.build_facade_driver()
+    rec = tmp_path / "prot.txt"
+    with open(rec, "w") as f:
+        f.write("T " + " ".join(str(t.tag) for t in species) + "\n")
+        f.write("R " + " ".join(str(int(g)) for g in rod_gid) + "\n")
+        for q in p:
+            vals = [int(q["gid"]), int(q["type"]), int(q["idBind"][0]), int(q["idBind"][1])]
+            vals += [repr(float(v)) for v in (*q["pos"], *q["posEnd"][0], *q["posEnd"][1])]
+            f.write(" ".join(str(v) for v in vals) + "\n")
+    cpp, py = tmp_path / "cpp.dat", tmp_path / "py.dat"
+    proc = subprocess.run([str(exe), "--write-protein-ascii", str(rec), str(cpp), "0.0125"], capture_output=True,
+                          text=True, timeout=120)
+    assert proc.returncode == 0, proc.stderr
+    io.write_protein_ascii(str(py), p, species, rod_gid, time=0.0125)
+    assert cpp.read_bytes() == py.read_bytes()
+    # and it reads back
+    back = io.read_protein_ascii(str(py))
+    assert np.array_equal(back["gid"], p["gid"])
+    assert np.array_equal(back["tag"], [species[t].tag for t in p["type"]])

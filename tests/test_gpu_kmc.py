@@ -17,9 +17,9 @@ D = 0.025
 
 
 def species():
-    """Three species that exercise every branch at dt = 1e-4: plain rates,
+    """Four species that exercise every branch at dt = 1e-4: plain rates,
     bind volume with load-dependent unbinding and PtoAPratio < 1, fixed end
-    0 with PtoAPratio > 1."""
+    0 with PtoAPratio > 1, and the lookupType 1 stretch."""
     return [
         capi.make_protein_type(tag=0, rc=0.03, ko_s=(200.0, 150.0), Ka=(0.01, 0.012), ko_d=(100.0, 80.0),
                                Ke=(0.5, 0.4), eps=400.0, kappa=200.0, lambda_=0.0, freeLength=0.025,
@@ -30,6 +30,9 @@ def species():
         capi.make_protein_type(tag=2, rc=0.04, ko_s=(60.0, 60.0), Ka=(0.01, 0.01), ko_d=(50.0, 70.0),
                                Ke=(0.6, 0.6), eps=300.0, kappa=300.0, lambda_=0.25822, freeLength=0.053,
                                fixedEnd0=True, PtoAPratio=2.0, diffUnbound=0.5),
+        capi.make_protein_type(tag=3, rc=0.035, ko_s=(150.0, 100.0), Ka=(0.015, 0.015), ko_d=(80.0, 80.0),
+                               Ke=(0.8, 0.8), eps=400.0, kappa=100.0, lambda_=0.5, freeLength=0.05,
+                               lookupType=1, diffUnbound=1.0),
     ]
 
 
@@ -42,7 +45,7 @@ def same(a, b):
 
 def _pair(w, nprot, seed, steps, move=True, links=None):
     pairs = workloads.pair_list(OracleSystem, w.cfg, w.rods, 0.05)
-    prots = workloads.protein_population(w.cfg, w.rods, nprot, pairs=pairs, seed=seed, ntypes=3)
+    prots = workloads.protein_population(w.cfg, w.rods, nprot, pairs=pairs, seed=seed, ntypes=4)
     g = capi.GpuSystem(w.cfg)
     o = OracleSystem(w.cfg)
     for s in (g, o):
@@ -126,7 +129,7 @@ def test_replicas_are_independent(gpu_lib):
     orc = []
     for r, (w, c) in enumerate(zip(ws, cfgs)):
         pairs = workloads.pair_list(OracleSystem, c, w.rods, 0.05)
-        prots = workloads.protein_population(c, w.rods, 1500 + 500 * r, pairs=pairs, seed=r, ntypes=3)
+        prots = workloads.protein_population(c, w.rods, 1500 + 500 * r, pairs=pairs, seed=r, ntypes=4)
         g.set_rods(w.rods, replica=r)
         g.set_proteins(prots, replica=r)
         o = OracleSystem(c)
@@ -158,7 +161,7 @@ def test_protein_api_edges(gpu_lib):
     with pytest.raises(capi.AlensError):
         g.set_proteins(capi.protein_array(1))
     with pytest.raises(capi.AlensError):
-        g.set_protein_types([capi.make_protein_type(lookupType=1)])
+        g.set_protein_types([capi.make_protein_type(lookupType=2)])
     g.set_protein_types([capi.make_protein_type()], KBT, D)
     # no proteins: a bind step is a no-op
     assert g.protein_bind_step()[0]["nU"] == 0

@@ -97,6 +97,27 @@ def test_sd_integral_and_inverse_against_adaptive_quadrature(d, sA, sB, kappa, l
             assert abs(part - u * got) <= 5e-6 * got, (u, part, u * got)
 
 
+@pytest.mark.parametrize("d,sA,sB", [(0.03, -0.5, 0.5), (0.049, -0.2, 0.7), (0.07, -0.3, 0.3), (0.026, -0.5, 0.5),
+                                     (0.1, -1.0, 1.0), (0.02, -0.5, 0.5)])
+def test_sd_integral_lookup_type_1(d, sA, sB):
+    """lookupType 1: stretch (1 - D/d) sqrt(d^2 + s^2) (Protein/ProteinModel.md),
+    head distances up to ell0 + D + w; no binding when d <= D."""
+    t = capi.make_protein_type(kappa=100.0, lambda_=0.5, freeLength=0.05, lookupType=1)
+    A = 0.5 * 100.0 / (2 * KBT)
+    rcap = 0.05 + D + 6 / math.sqrt(A)
+    got = oa.kmc_sd_integral(t, KBT, D, 1e-5, d * d, sA, sB)
+    if d <= D:
+        assert got == 0.0
+        return
+    k = 1 - D / d
+    smax = math.sqrt(max(rcap * rcap - d * d, 0.0))
+    lo, hi = max(sA, -smax), min(sB, smax)
+    f = lambda s: math.exp(-A * (k * math.sqrt(d * d + s * s) - 0.05) ** 2)
+    ref = integrate.quad(f, lo, hi, epsabs=0.0, epsrel=1e-13, limit=500)[0] if hi > lo else 0.0
+    # FP32 integrand; the scale 1 - D/d adds a rounding of its own
+    assert abs(got - ref) <= 5e-6 * max(ref, 1e-300) + 1e-12, (got, ref)
+
+
 def test_bind_volume_closed_form():
     for kappa, lam, ell0 in ((200.0, 0.5, 0.025), (300.0, 0.25822, 0.053), (1.0, 0.0, 1.0)):
         t = capi.make_protein_type(kappa=kappa, lambda_=lam, freeLength=ell0)
@@ -264,6 +285,67 @@ def test_load_dependent_unbinding():
     o.close()
 
 
+def test_load_dependent_unbinding_lookup_type_1():
+    """lookupType 1: the stretch is (1 - D/d) ell - ell0, d the distance of
+    head 0 from the segment of head 1's rod (Protein/ProteinData.hpp:171-195)."""
+    lam, kappa, ell0 = 0.4, 100.0, 0.02
+    t = capi.make_protein_type(ko_s=(0.0, 0.0), ko_d=(5.0, 5.0), Ka=(0.0, 0.0), Ke=(0.0, 0.0), lambda_=lam,
+                               kappa=kappa, freeLength=ell0, lookupType=1)
+    sep = 0.07
+    o, cfg = _one_rod_system(extra=([2.0, 2.0 + sep, 2.0], [1.0, 0.0, 0.0]))
+    o.set_protein_types([t], KBT, D)
+    n = 40000
+    p = capi.protein_array(n)
+    p["gid"] = np.arange(n)
+    p["idBind"][:, 0] = 0
+    p["idBind"][:, 1] = 1
+    p["distBind"][:, 0] = 0.0
+    p["distBind"][:, 1] = 0.03
+    o.set_proteins(p)
+    st = o.protein_bind_step()
+    ell = math.hypot(sep, 0.03)
+    stretch = (1 - D / sep) * ell - ell0
+    rate = 5.0 * math.exp(lam * kappa * stretch ** 2 / (2 * KBT))
+    assert _binom_ok(st["nDS"], n, 2 * rate * cfg.dt)
+    o.close()
+
+
+def test_springs_lookup_type_1():
+    """The spring's separation is the lookupType 1 stretch at the geometry
+    of the step that built it."""
+    o, cfg = _one_rod_system(extra=([2.0, 2.07, 2.0], [1.0, 0.0, 0.0]))
+    o.set_protein_types([capi.make_protein_type(freeLength=0.05, lookupType=1)], KBT, D)
+    p = capi.protein_array(1)
+    p["idBind"][0] = [0, 1]
+    p["distBind"][0] = [0.0, 0.04]
+    o.set_proteins(p)
+    o.detect()
+    c = o.constraints()
+    ell = math.hypot(0.07, 0.04)
+    assert c["gamma"].shape[0] - c["ncoll"] == 1
+    assert abs(c["delta0"][-1] - ((1 - D / 0.07) * ell - 0.05)) < 1e-12
+    o.close()
+
+
+def test_mixmotor_example_fixture():
+    """The MixMotorSliding example (two parallel 20 um rods, 100 doubly bound
+    motors of two lookupType 1 species) read with the protein readers and
+    stepped by the oracle: the stage counts against the committed golden."""
+    import json
+    import os
+    sys_path = os.path.join(os.path.dirname(__file__), "golden")
+    import sys
+    sys.path.insert(0, sys_path)
+    import make_fixtures as mf
+    cfg, rods, kbt, species, prots = mf.load_mixmotor()
+    # 97 doubly bound motors and 3 singly bound ones in the example file
+    assert prots.shape[0] == 100 and np.all(prots["idBind"][:, 0] >= 0)
+    assert int(np.sum(prots["idBind"][:, 1] >= 0)) == 97
+    assert [t.lookupType for t in species] == [1, 1]
+    g = json.load(open(os.path.join(sys_path, "mixmotor_golden.json")))
+    assert mf.mixmotor_golden(g["steps"]) == g
+
+
 def test_doubly_bound_proteins_become_springs():
     w = workloads.small_periodic(n=300, box=3.0, seed=2)
     pairs = workloads.pair_list(oa.OracleSystem, w.cfg, w.rods, 0.05)
@@ -298,7 +380,7 @@ def test_invalid_protein_input_is_rejected():
     with pytest.raises(capi.AlensError):
         o.set_proteins(p)                      # no species yet
     with pytest.raises(capi.AlensError):
-        o.set_protein_types([capi.make_protein_type(lookupType=1)])
+        o.set_protein_types([capi.make_protein_type(lookupType=2)])
     with pytest.raises(capi.AlensError):
         o.set_protein_types([capi.make_protein_type(lambda_=1.0)])
     o.set_protein_types([capi.make_protein_type()])
