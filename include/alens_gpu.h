@@ -468,16 +468,16 @@ int alens_autotune(AlensCtx *ctx, int reps, char *report, int reportCap);
  * a number per binding site).  The library applies readFromYaml's
  * conversion (Ka /= 602, Ke /= 602 when useBindVol) and, for fixedEnd0, the
  * rule of Protein/ProteinModel.md ("When fixedEnd0==true": ko_s[0] =
- * ko_d[0] = 0).  Only lookupType 0 (stretch length = head distance - rod
- * diameter) is supported; lookupType 1 is rejected (the reference marks it
- * as not to be used, Protein/ProteinType.hpp:162-164).  The walking and
- * diffusion fields of ProteinType belong to the motion step, which this
- * library does not run. */
+ * ko_d[0] = 0).  lookupType 0: stretch = head distance - rod diameter D;
+ * lookupType 1: stretch = (1 - D/d) x head distance, d the distance of the
+ * bound head from the other rod's axis (Protein/ProteinData.hpp:171-195);
+ * other values are rejected.  The walking and diffusion fields of
+ * ProteinType belong to the motion step, which this library does not run. */
 typedef struct AlensProteinType {
     int32_t tag;
     int32_t fixedEnd0;
     int32_t useBindVol;
-    int32_t lookupType;   /* must be 0 */
+    int32_t lookupType;   /* 0 or 1 */
     double freeLength;    /* rest length ell0, um */
     double kappa;         /* spring constant, pN/um */
     double lambda;        /* unbinding load sensitivity */
@@ -528,8 +528,12 @@ int alens_set_protein_types(AlensCtx *ctx, int n, const AlensProteinType *types,
  * readProteinVTK, SRC/TubuleSystem.cpp:761-872).  Bound heads must name a
  * rod of the replica (ALENS_INVALID_ARG otherwise); pos of a bound protein
  * is recomputed from its heads.  Doubly bound proteins are bilateral
- * springs of the next step (rest length freeLength + rodDiameter, stiffness
- * kappa), after the replica's alens_set_links links.  n = 0 removes them. */
+ * springs of the next step (stiffness kappa; rest length freeLength +
+ * rodDiameter, or for lookupType 1 the length whose difference from the
+ * head distance is that type's stretch at the geometry when the springs are
+ * built: by this call, alens_set_protein_types, alens_set_rods,
+ * alens_set_links and each binding step), after the replica's
+ * alens_set_links links.  n = 0 removes them. */
 int alens_set_proteins(AlensCtx *ctx, int replica, int n, const AlensProtein *proteins);
 
 /* The current proteins of one replica, in the order they were set.  cap too
