@@ -150,15 +150,31 @@ class AlensProteinType(C.Structure):
         ("ko_d", C.c_double * 2),
         ("Ka", C.c_double * 2),
         ("Ke", C.c_double * 2),
+        ("walkOff", C.c_int32),
+        ("vdrag", C.c_int32 * 2),
+        ("pad2", C.c_int32),
+        ("fstall", C.c_double),
+        ("vmax", C.c_double * 2),
+        ("vmaxAP", C.c_double * 2),
+        ("diffBoundS", C.c_double * 2),
+        ("diffBoundD", C.c_double * 2),
     ]
 
 
 def make_protein_type(tag=0, freeLength=0.025, rc=0.025, kappa=200.0, lambda_=0.5, diffUnbound=1.0,
                       useBindVol=False, eps=400.0, Ka=(100.0, 100.0), ko_s=(28.1, 28.1), Ke=(100.0, 100.0),
-                      ko_d=(28.1, 28.1), PtoAPratio=1.0, fixedEnd0=False, lookupType=0) -> AlensProteinType:
+                      ko_d=(28.1, 28.1), PtoAPratio=1.0, fixedEnd0=False, lookupType=0, walkOff=True,
+                      vdrag=(False, False), fstall=5.0, vmax=(0.5, 0.5), vmaxAP=None, diffBoundS=(0.0, 0.0),
+                      diffBoundD=(0.0, 0.0)) -> AlensProteinType:
     """A species; the defaults are the symmetric crosslinker of the dense
-    monolayer example (Examples/DenseMonoLayer/ProteinConfig.yaml)."""
+    monolayer example (Examples/DenseMonoLayer/ProteinConfig.yaml); vmaxAP
+    defaults to vmax as in ProteinType::readFromYaml."""
     t = AlensProteinType()
+    vmaxAP = vmax if vmaxAP is None else vmaxAP
+    t.walkOff, t.fstall = int(walkOff), float(fstall)
+    for e in range(2):
+        t.vdrag[e], t.vmax[e], t.vmaxAP[e] = int(vdrag[e]), float(vmax[e]), float(vmaxAP[e])
+        t.diffBoundS[e], t.diffBoundD[e] = float(diffBoundS[e]), float(diffBoundD[e])
     t.tag, t.fixedEnd0, t.useBindVol, t.lookupType = int(tag), int(fixedEnd0), int(useBindVol), int(lookupType)
     t.freeLength, t.kappa, t.lambda_, t.PtoAPratio = float(freeLength), float(kappa), float(lambda_), float(PtoAPratio)
     t.diffUnbound, t.rc, t.eps = float(diffUnbound), float(rc), float(eps)
@@ -292,6 +308,7 @@ def load_library(path: str | Path | None = None) -> C.CDLL:
         "alens_set_proteins": (C.c_int, [vp, C.c_int, C.c_int, vp]),
         "alens_get_proteins": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_int), vp]),
         "alens_protein_bind_step": (C.c_int, [vp, C.POINTER(AlensKmcStats)]),
+        "alens_protein_motion_step": (C.c_int, [vp, C.POINTER(AlensKmcStats)]),
         "alens_mlp_create": (C.c_int, [C.c_uint64, C.c_int64, C.POINTER(vp)]),
         "alens_mlp_destroy": (C.c_int, [vp]),
         "alens_mlp_get_params": (C.c_int, [vp, _PF]),
@@ -463,6 +480,11 @@ class GpuSystem:
     def protein_bind_step(self) -> list[dict]:
         st = (AlensKmcStats * self.nrep)()
         self._ck(self.lib.alens_protein_bind_step(self.h, st), "alens_protein_bind_step")
+        return [st[r].as_dict() for r in range(self.nrep)]
+
+    def protein_motion_step(self) -> list[dict]:
+        st = (AlensKmcStats * self.nrep)()
+        self._ck(self.lib.alens_protein_motion_step(self.h, st), "alens_protein_motion_step")
         return [st[r].as_dict() for r in range(self.nrep)]
 
     def set_boundaries(self, boundaries, replica: int = 0):

@@ -287,6 +287,11 @@ int alens_get_proteins(AlensCtx *ctx, int replica, int cap, int *n, AlensProtein
     });
 }
 
+int alens_protein_motion_step(AlensCtx *ctx, AlensKmcStats *stats) {
+    if (!ctx) return ALENS_INVALID_ARG;
+    return guarded_ctx(ctx, [&] { return ctx->eng->proteinMotionStep(stats); });
+}
+
 int alens_protein_bind_step(AlensCtx *ctx, AlensKmcStats *stats) {
     if (!ctx) return ALENS_INVALID_ARG;
     return guarded_ctx(ctx, [&] { return ctx->eng->proteinBindStep(stats); });

@@ -1463,6 +1463,18 @@ KmcType make_kmc_type(const AlensProteinType &in, double KBT, double D, double d
     T.prefPar = r < 1.0f ? r : 1.0f;
     T.prefAnti = r > 1.0f ? 1.0f / r : 1.0f;
     T.Df = (float)D;
+    T.walkOff = in.walkOff ? 1 : 0;
+    T.fstall = in.fstall;
+    for (int e = 0; e < 2; e++) {
+        T.vdrag[e] = in.vdrag[e] ? 1 : 0;
+        T.vmax[e] = in.vmax[e];
+        T.vmaxAP[e] = in.vmaxAP[e];
+        T.diffS[e] = std::sqrt((dt * in.diffBoundS[e]) * 2.0);
+        T.diffD[e] = std::sqrt((dt * in.diffBoundD[e]) * 2.0);
+        T.dragD[e] = in.diffBoundD[e];
+    }
+    T.diffU = std::sqrt((dt * in.diffUnbound) * 2.0);
+    T.KBT = KBT;
     return T;
 }
 
@@ -1477,9 +1489,11 @@ void Engine::setProteinTypes(int n, const AlensProteinType *t, double KBT, doubl
                   p.lambda >= 0.0 && p.lambda < 1.0 && finite_nonneg(p.freeLength) && std::isfinite(p.rc) &&
                   p.rc > 0.0 && finite_nonneg(p.eps) && finite_nonneg(p.diffUnbound) &&
                   std::isfinite(p.PtoAPratio) && p.PtoAPratio > 0.0;
+        ok = ok && std::isfinite(p.fstall) && p.fstall != 0.0;
         for (int e = 0; e < 2; e++)
             ok = ok && finite_nonneg(p.ko_s[e]) && finite_nonneg(p.ko_d[e]) && finite_nonneg(p.Ka[e]) &&
-                 finite_nonneg(p.Ke[e]);
+                 finite_nonneg(p.Ke[e]) && std::isfinite(p.vmax[e]) && std::isfinite(p.vmaxAP[e]) &&
+                 finite_nonneg(p.diffBoundS[e]) && finite_nonneg(p.diffBoundD[e]);
         if (!ok) throw ApiError(ALENS_INVALID_ARG);
     }
     syncProteinsToHost();
@@ -1716,6 +1730,30 @@ void Engine::rebuildSprings() {
     launches_ += 1 + launch_kmc_springs(K_, S_, userLinkTotal_, linkCap_, stream_);
     CK(cudaGetLastError());
     readSprings(nullptr);
+}
+
+int Engine::proteinMotionStep(AlensKmcStats *stats) {
+    if (haveDetect_ || haveSolve_) throw ApiError(ALENS_NOT_READY);
+    finalize();
+    uploadLinks();
+    uploadBoundaries();
+    uploadProteins();
+    if (nProt_ == 0) {
+        rebuildSprings();
+        if (stats) std::memset(stats, 0, sizeof(AlensKmcStats) * R_);
+        return ALENS_OK;
+    }
+    if (ptypes_.empty()) throw ApiError(ALENS_NOT_READY);
+    prepareKmc();
+    CK(cudaMemsetAsync(K_.stats, 0, sizeof(int) * (9 * R_ + 1), stream_));
+    launch_kmc_view(K_, S_, stream_);
+    int n = 1 + launch_kmc_motion(K_, S_, stream_);
+    n += launch_kmc_springs(K_, S_, userLinkTotal_, linkCap_, stream_);
+    CK(cudaGetLastError());
+    launches_ += n;
+    protDevNewer_ = true;
+    readSprings(stats);
+    return ALENS_OK;
 }
 
 int Engine::proteinBindStep(AlensKmcStats *stats) {

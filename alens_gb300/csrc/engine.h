@@ -58,6 +58,7 @@ class Engine {
     void setProteins(int rep, int n, const AlensProtein *p);
     void getProteins(int rep, int cap, int *n, AlensProtein *out);
     int proteinBindStep(AlensKmcStats *stats);
+    int proteinMotionStep(AlensKmcStats *stats);
     int detect(AlensStepStats *out);
     int solve(AlensStepStats *out);
     int advance(AlensStepStats *out);

@@ -786,6 +786,13 @@ std::vector<AlensProtein> SylinderSystem::getProteins() {
     return out;
 }
 
+AlensKmcStats SylinderSystem::updateProteinMotion() {
+    if (!ctx_) throw std::runtime_error("updateProteinMotion: initialize() first");
+    AlensKmcStats st{};
+    check(alens_protein_motion_step(ctx_, &st), "alens_protein_motion_step");
+    return st;
+}
+
 AlensKmcStats SylinderSystem::calcBindInteraction() {
     if (!ctx_) throw std::runtime_error("calcBindInteraction: initialize() first");
     AlensKmcStats st{};

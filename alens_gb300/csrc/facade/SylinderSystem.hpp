@@ -219,6 +219,10 @@ class SylinderSystem {
     // (SRC/TubuleSystem.cpp:232-259, 694-745): one binding step of every
     // protein; the doubly bound ones are springs of the next runStep()
     AlensKmcStats calcBindInteraction();
+    // TubuleSystem::updateProteinMotion (SRC/TubuleSystem.cpp:261-306):
+    // walking, drag and diffusion of the heads, diffusion of unbound
+    // proteins, walk-off at rod ends, boundaries
+    AlensKmcStats updateProteinMotion();
     // ProteinAscii_<snapID>.dat (Protein/ProteinData.hpp:545-564, 705-718):
     // header "count \n time", then "P gid tag end0 end1 gid0 gid1" per
     // protein (the heads when both are bound, the centre twice otherwise;

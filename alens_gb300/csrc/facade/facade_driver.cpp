@@ -24,9 +24,11 @@
 //
 // usage: facade_driver --proteins RunConfig.yaml TubuleInitial.dat setup.txt KBT steps out.txt
 // Steps proteins and rods in TubuleSystem::step()'s order
-// (SRC/TubuleSystem.cpp:196-224): calcBindInteraction(), then runStep().
+// (SRC/TubuleSystem.cpp:185-224): updateProteinMotion(),
+// calcBindInteraction(), then runStep().
 // setup: "S tag fixedEnd0 useBindVol lookupType freeLength kappa lambda
-// PtoAPratio diffUnbound rc eps ko_s(2) ko_d(2) Ka(2) Ke(2)" per species and
+// PtoAPratio diffUnbound rc eps ko_s(2) ko_d(2) Ka(2) Ke(2) walkOff vdrag(2)
+// fstall vmax(2) vmaxAP(2) diffBoundS(2) diffBoundD(2)" per species and
 // "P gid type idBind0 idBind1 distBind0 distBind1 x y z" per protein.  Writes
 // the final proteins to out.txt ("gid type idBind0 idBind1 distBind(2)
 // pos(3) posEnd(6)", %.17g) and prints one JSON line of per-step counts.
@@ -219,7 +221,7 @@ int proteinsMode(const char *runConfig, const char *tubules, const char *setup, 
     while (std::getline(in, line)) {
         const auto t = tokens(line);
         if (t.empty()) continue;
-        if (t[0] == "S" && t.size() >= 20) {
+        if (t[0] == "S" && t.size() >= 32) {
             AlensProteinType y{};
             y.tag = std::atoi(t[1].c_str());
             y.fixedEnd0 = std::atoi(t[2].c_str());
@@ -237,6 +239,16 @@ int proteinsMode(const char *runConfig, const char *tubules, const char *setup, 
                 y.ko_d[e] = num(t[14 + e]);
                 y.Ka[e] = num(t[16 + e]);
                 y.Ke[e] = num(t[18 + e]);
+            }
+            y.walkOff = std::atoi(t[20].c_str());
+            y.vdrag[0] = std::atoi(t[21].c_str());
+            y.vdrag[1] = std::atoi(t[22].c_str());
+            y.fstall = num(t[23]);
+            for (int e = 0; e < 2; e++) {
+                y.vmax[e] = num(t[24 + e]);
+                y.vmaxAP[e] = num(t[26 + e]);
+                y.diffBoundS[e] = num(t[28 + e]);
+                y.diffBoundD[e] = num(t[30 + e]);
             }
             types.push_back(y);
         } else if (t[0] == "P" && t.size() >= 10) {
@@ -257,6 +269,7 @@ int proteinsMode(const char *runConfig, const char *tubules, const char *setup, 
     std::string counts;
     for (int s = 0; s < steps; s++) {
         rodSystem.prepareStep();
+        rodSystem.updateProteinMotion();
         const AlensKmcStats st = rodSystem.calcBindInteraction();
         rodSystem.runStep();
         char buf[160];

@@ -746,6 +746,162 @@ __global__ void __launch_bounds__(32 * kKmcWarps) k_kmc_bind(KmcDev K, int *code
     }
 }
 
+// ---- motion step (TubuleSystem::updateProteinMotion)
+
+// Box-Muller pair from two Philox words (24-bit uniforms, FP32, the
+// project's log and sincos, as the rods' noise)
+__device__ __forceinline__ void kmc_normal_pair(uint32_t wa, uint32_t wb, double *z0, double *z1) {
+    const float ua = ((float)(wa >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    const float ub = ((float)(wb >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    const float r = sqrtf(-2.0f * det_logf(ua));
+    const float ang = ub * 6.28318531f - 3.14159265f;
+    float sn, cs;
+    det_sincosf(ang, &sn, &cs);
+    *z0 = (double)(r * -cs);
+    *z1 = (double)(r * -sn);
+}
+
+// a point outside a boundary is moved onto it (Boundary::project as
+// SRC/TubuleSystem.cpp:285-305 uses it): wall, sphere (inside / outside),
+// tube (inside)
+__device__ __forceinline__ void kmc_project(const BoundaryDev &B, double x[3]) {
+    const double v[3] = {x[0] - B.c[0], x[1] - B.c[1], x[2] - B.c[2]};
+    if (B.type == 0) {
+        const double s = v[0] * B.a[0] + v[1] * B.a[1] + v[2] * B.a[2];
+        if (s < 0.0)
+            for (int d = 0; d < 3; d++) x[d] = x[d] - s * B.a[d];
+    } else if (B.type == 1) {
+        const double r = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        const bool out = B.inside ? r > B.R : r < B.R;
+        if (out && r > 0.0)
+            for (int d = 0; d < 3; d++) x[d] = B.c[d] + (B.R / r) * v[d];
+    } else {
+        const double s = v[0] * B.a[0] + v[1] * B.a[1] + v[2] * B.a[2];
+        const double q[3] = {v[0] - s * B.a[0], v[1] - s * B.a[1], v[2] - s * B.a[2]};
+        const double r = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+        if (r > B.R)
+            for (int d = 0; d < 3; d++) x[d] = (B.c[d] + s * B.a[d]) + (B.R / r) * q[d];
+    }
+}
+
+// One thread per protein (ProteinData::updatePosWalk / updatePosDiffuse,
+// Protein/ProteinData.hpp:318-406, walk velocity :459-478, drag :489-498):
+// rolls from Philox (seed, gid, step, 'mot' + block): block 0 gives the
+// uniform (53 bits) and normals z0, z1, block 1 gives z2.
+__global__ void __launch_bounds__(256) k_kmc_motion(KmcDev K, DevState S, int *code) {
+    ALENS_PDL_PROLOGUE();
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.nProt; p += gridDim.x * blockDim.x) {
+        const int rep = K.protRep[p];
+        const KmcRep &Q = K.rep[rep];
+        AlensProtein &pr = K.prot[p];
+        const KmcType &T = K.types[rep * K.nTypes + pr.type];
+        int id[2] = {pr.idBind[0], pr.idBind[1]};
+        for (int e = 0; e < 2; e++)
+            if (id[e] < 0 || id[e] >= Q.nRods) id[e] = -1;
+        const int nb = (id[0] >= 0 ? 1 : 0) + (id[1] >= 0 ? 1 : 0);
+        uint32_t w[4], v[4];
+        w[0] = (uint32_t)(unsigned long long)pr.gid;
+        w[1] = (uint32_t)((unsigned long long)pr.gid >> 32);
+        w[2] = (uint32_t)(unsigned long long)K.step;
+        w[3] = 0x6D6F7400u;
+        v[0] = w[0];
+        v[1] = w[1];
+        v[2] = w[2];
+        v[3] = 0x6D6F7401u;
+        philox4x32_10(w, (uint32_t)Q.seed, (uint32_t)(Q.seed >> 32));
+        philox4x32_10(v, (uint32_t)Q.seed, (uint32_t)(Q.seed >> 32));
+        const double u01 = u53(w[0], w[1]);
+        double z0, z1, z2, z3;
+        kmc_normal_pair(w[2], w[3], &z0, &z1);
+        kmc_normal_pair(v[0], v[1], &z2, &z3);
+        int trans = 0;
+        if (nb == 0) {
+            pr.idBind[0] = pr.idBind[1] = -1;
+            pr.pos[0] = pr.pos[0] + T.diffU * z0;
+            pr.pos[1] = pr.pos[1] + T.diffU * z1;
+            pr.pos[2] = pr.pos[2] + T.diffU * z2;
+        } else {
+            double dist[2] = {pr.distBind[0], pr.distBind[1]};
+            if (nb == 2) {
+                // spring load on each head (ProteinData::updateForceTorqueBind)
+                double P[2][3];
+                KDouble4 Ax[2];
+                for (int e = 0; e < 2; e++) {
+                    const int r = Q.rodOffset + id[e];
+                    const KDouble4 C = K.rodC[r];
+                    Ax[e] = K.rodA[r];
+                    P[e][0] = C.x + dist[e] * Ax[e].x;
+                    P[e][1] = C.y + dist[e] * Ax[e].y;
+                    P[e][2] = C.z + dist[e] * Ax[e].z;
+                }
+                double rv[3] = {P[0][0] - P[1][0], P[0][1] - P[1][1], P[0][2] - P[1][2]};
+                for (int d = 0; d < 3; d++)
+                    if (Q.pbc[d]) rv[d] = rv[d] - Q.L[d] * floor(rv[d] / Q.L[d] + 0.5);
+                const double ell = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+                const double force = (kmc_force_length(K, Q, T, P[0], Q.rodOffset + id[1], ell) - T.ell0) * T.kappa;
+                const double f0[3] = {-force * (rv[0] / ell), -force * (rv[1] / ell), -force * (rv[2] / ell)};
+                const double par = Ax[0].x * Ax[1].x + Ax[0].y * Ax[1].y + Ax[0].z * Ax[1].z;
+                const double z[2] = {z0, z1};
+                for (int e = 0; e < 2; e++) {
+                    const double sg = e == 0 ? 1.0 : -1.0;  // f1 = -f0
+                    const double fdir = sg * (f0[0] * Ax[e].x + f0[1] * Ax[e].y + f0[2] * Ax[e].z);
+                    const double sgn = T.vmax[e] > 0.0 ? 1.0 : (T.vmax[e] < 0.0 ? -1.0 : 0.0);
+                    const double fproj = (sgn * fdir) / fabs(T.fstall);
+                    const double one = 1.0 + fproj;
+                    const double vfrac = one < 0.0 ? 0.0 : (one > 1.0 ? 1.0 : one);
+                    const double vel = (par > 0.0 ? T.vmax[e] : T.vmaxAP[e]) * vfrac;
+                    const double drag = T.vdrag[e] ? (fdir * T.dragD[e]) / T.KBT : 0.0;
+                    dist[e] = dist[e] + ((vel + drag) * T.dt + T.diffD[e] * z[e]);
+                }
+            } else {
+                const int b = id[0] >= 0 ? 0 : 1;
+                dist[b] = dist[b] + (T.vmax[b] * T.dt + T.diffS[b] * (b == 0 ? z0 : z1));
+            }
+            bool off[2] = {false, false};
+            double half[2] = {0.0, 0.0};
+            for (int e = 0; e < 2; e++) {
+                if (id[e] < 0) continue;
+                half[e] = K.rodC[Q.rodOffset + id[e]].w;
+                off[e] = dist[e] > half[e] || dist[e] < -half[e];
+            }
+            if (T.walkOff) {
+                if (off[0] && off[1]) {
+                    const int e = u01 < 0.5 ? 0 : 1;
+                    id[e] = -1;
+                    dist[1 - e] = dist[1 - e] > half[1 - e] ? half[1 - e] : (dist[1 - e] < -half[1 - e] ? -half[1 - e] : dist[1 - e]);
+                } else if (off[0]) {
+                    id[0] = -1;
+                } else if (off[1]) {
+                    id[1] = -1;
+                }
+            } else {
+                for (int e = 0; e < 2; e++)
+                    if (id[e] >= 0) dist[e] = dist[e] > half[e] ? half[e] : (dist[e] < -half[e] ? -half[e] : dist[e]);
+            }
+            const int nb2 = (id[0] >= 0 ? 1 : 0) + (id[1] >= 0 ? 1 : 0);
+            if (nb2 < nb) trans = nb == 2 ? 4 : 2;
+            // a protein that walked off its only rod keeps its centre (the
+            // last head position): ProteinBindStatus::updatePosWithEndBind
+            // leaves an unbound protein's position alone
+            for (int e = 0; e < 2; e++) {
+                pr.idBind[e] = id[e];
+                pr.distBind[e] = dist[e];
+            }
+        }
+        // unbound proteins outside a boundary are moved onto it
+        // (SRC/TubuleSystem.cpp:285-305: after the motion, every protein
+        // that is unbound then)
+        if (pr.idBind[0] < 0 && pr.idBind[1] < 0) {
+            double x[3] = {pr.pos[0], pr.pos[1], pr.pos[2]};
+            for (int b = S.bndStart[rep]; b < S.bndStart[rep + 1]; b++) kmc_project(S.bnd[b], x);
+            pr.pos[0] = x[0];
+            pr.pos[1] = x[1];
+            pr.pos[2] = x[2];
+        }
+        code[p] = ((pr.idBind[0] >= 0 ? 1 : 0) + (pr.idBind[1] >= 0 ? 1 : 0)) | (trans << 2);
+    }
+}
+
 // One thread per protein: head positions and centre of the new state
 // (bound head; midpoint of the heads, minimum image; the free point),
 // wrapped into the box; unbound ends NaN.
@@ -936,6 +1092,14 @@ int launch_kmc_bind(const KmcDev &K, cudaStream_t st) {
     launch_pdl(k_kmc_geom, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K);
     launch_pdl(k_kmc_stats, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K, (const int *)K.dScan);
     return 4;
+}
+
+int launch_kmc_motion(const KmcDev &K, const DevState &S, cudaStream_t st) {
+    if (K.nProt <= 0) return 0;
+    launch_pdl(k_kmc_motion, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K, S, K.dScan);
+    launch_pdl(k_kmc_geom, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K);
+    launch_pdl(k_kmc_stats, dim3(grid_kmc(K.nProt, 256)), dim3(256), 0, st, K, (const int *)K.dScan);
+    return 3;
 }
 
 int launch_kmc_springs(const KmcDev &K, const DevState &S, int userTotal, int linkCap, cudaStream_t st) {

@@ -49,6 +49,12 @@ struct KmcType {
     float prefPar, prefAnti;  // PtoAPratio prefactor for a parallel / antiparallel rod
     float Df;                 // rod diameter (lookupType 1 stretch factor 1 - D/d)
     int lookup;               // 0: stretch r - D; 1: (1 - D/d) r (Protein/ProteinData.hpp:171-195)
+    // motion step (Protein/ProteinData.hpp:318-498)
+    int walkOff, vdrag[2], pad;
+    double fstall, vmax[2], vmaxAP[2];
+    double diffS[2], diffD[2], diffU;  // sqrt(dt D 2) of the bound heads and the free protein
+    double dragD[2];                   // diffBoundD (drag velocity = load x diffBoundD / KBT)
+    double KBT;
 };
 
 struct KmcRep {
@@ -88,6 +94,9 @@ void launch_kmc_bin(const KmcDev &K, const DevState &S, cudaStream_t st);
 void launch_kmc_view(const KmcDev &K, const DevState &S, cudaStream_t st);  // rod view only, no cell counts
 void launch_kmc_scatter(const KmcDev &K, const DevState &S, cudaStream_t st);
 int launch_kmc_bind(const KmcDev &K, cudaStream_t st);  // returns kernels launched
+// one motion step (walk, drag, diffusion, walk-off, boundaries) then the
+// new geometry and the per-replica counts; returns kernels launched
+int launch_kmc_motion(const KmcDev &K, const DevState &S, cudaStream_t st);
 // doubly bound flags, their scan and the spring rows at link offset
 // userTotal (capacity linkCap); dCount per replica
 int launch_kmc_springs(const KmcDev &K, const DevState &S, int userTotal, int linkCap, cudaStream_t st);

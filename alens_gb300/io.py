@@ -431,7 +431,13 @@ def read_protein_config(path):
             kappa=float(e.get("kappa", 204.7)), lambda_=float(e.get("lambda", 0.0)),
             diffUnbound=float(e.get("diffUnbound", 4.5)), useBindVol=bool(e.get("useBindVol", 0)),
             eps=float(e.get("eps", 0.0)), PtoAPratio=float(e.get("PtoAPratio", 1.0)),
-            fixedEnd0=bool(e.get("fixedEnd0", 0)), lookupType=int(e.get("lookupType", 0)), **pair))
+            fixedEnd0=bool(e.get("fixedEnd0", 0)), lookupType=int(e.get("lookupType", 0)),
+            walkOff=bool(e.get("walkOff", 1)), fstall=float(e.get("fstall", 1.0)),
+            vmax=tuple(float(x) for x in (e.get("vmax") or [0.0, 0.0])),
+            vmaxAP=tuple(float(x) for x in (e.get("vmaxAP") or e.get("vmax") or [0.0, 0.0])),
+            vdrag=tuple(bool(x) for x in (e.get("vdrag") or [0, 0])),
+            diffBoundS=tuple(float(x) for x in (e.get("diffBoundS") or [0.0, 0.0])),
+            diffBoundD=tuple(float(x) for x in (e.get("diffBoundD") or [0.0, 0.0])), **pair))
     return kbt, species, entries
 
 

@@ -63,6 +63,7 @@ def load_oracle(rebuild: bool = True) -> C.CDLL:
         "orc_set_proteins": (C.c_int, [vp, C.c_int, vp]),
         "orc_get_proteins": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), vp]),
         "orc_protein_bind_step": (C.c_int, [vp, C.POINTER(AlensKmcStats)]),
+        "orc_protein_motion_step": (C.c_int, [vp, C.POINTER(AlensKmcStats)]),
         "orc_kmc_exp": (C.c_double, [C.c_double]),
         "orc_kmc_expf": (C.c_float, [C.c_float]),
         "orc_kmc_sd_integral": (C.c_double, [C.POINTER(AlensProteinType), C.c_double, C.c_double, C.c_double,
@@ -262,6 +263,11 @@ class OracleSystem:
     def protein_bind_step(self) -> dict:
         st = AlensKmcStats()
         _ck(self.lib.orc_protein_bind_step(self.h, C.byref(st)), "orc_protein_bind_step")
+        return st.as_dict()
+
+    def protein_motion_step(self) -> dict:
+        st = AlensKmcStats()
+        _ck(self.lib.orc_protein_motion_step(self.h, C.byref(st)), "orc_protein_motion_step")
         return st.as_dict()
 
     def set_boundaries(self, boundaries):

@@ -471,8 +471,9 @@ int alens_autotune(AlensCtx *ctx, int reps, char *report, int reportCap);
  * ko_d[0] = 0).  lookupType 0: stretch = head distance - rod diameter D;
  * lookupType 1: stretch = (1 - D/d) x head distance, d the distance of the
  * bound head from the other rod's axis (Protein/ProteinData.hpp:171-195);
- * other values are rejected.  The walking and diffusion fields of
- * ProteinType belong to the motion step, which this library does not run. */
+ * other values are rejected.  The motion fields (walkOff, vdrag, fstall,
+ * vmax, vmaxAP, diffBoundS, diffBoundD) are used by
+ * alens_protein_motion_step; diffUnbound by both steps. */
 typedef struct AlensProteinType {
     int32_t tag;
     int32_t fixedEnd0;
@@ -486,6 +487,15 @@ typedef struct AlensProteinType {
     double rc;            /* capture radius, um */
     double eps;           /* binding sites per um of rod */
     double ko_s[2], ko_d[2], Ka[2], Ke[2];
+    /* motion (Protein/ProteinType.hpp:30-52) */
+    int32_t walkOff;      /* 1: a head that walks past a rod end unbinds; 0: clamped */
+    int32_t vdrag[2];     /* 1: a doubly bound head is also dragged by its load */
+    int32_t pad2;
+    double fstall;        /* stall force, pN */
+    double vmax[2];       /* walking speed per head, um/s, + towards the plus end */
+    double vmaxAP[2];     /* walking speed on antiparallel rods (doubly bound) */
+    double diffBoundS[2]; /* head diffusivity when singly bound, um^2/s */
+    double diffBoundD[2]; /* head diffusivity when doubly bound, um^2/s */
 } AlensProteinType;
 
 /* One protein (the binding part of ProteinData / ProteinBindStatus,
@@ -552,6 +562,22 @@ int alens_get_proteins(AlensCtx *ctx, int replica, int cap, int *n, AlensProtein
  * and independent of the device.  stats (nullable) receives one record per
  * replica.  Not between alens_detect and alens_advance (ALENS_NOT_READY). */
 int alens_protein_bind_step(AlensCtx *ctx, AlensKmcStats *stats);
+
+/* One motion step of every protein of every replica on the current rod
+ * state (TubuleSystem::updateProteinMotion, SRC/TubuleSystem.cpp:261-306,
+ * with ProteinData::updatePosWalk / updatePosDiffuse,
+ * Protein/ProteinData.hpp:318-406): unbound proteins diffuse with
+ * diffUnbound and are projected back onto the replica's boundaries when
+ * outside; bound heads walk (vmax, or vmaxAP on antiparallel rods, slowed
+ * linearly by the spring load towards fstall, Protein/ProteinData.hpp:459-478),
+ * are dragged by the load when vdrag (:489-498) and diffuse along the rod;
+ * a head past a rod end unbinds (walkOff; both past: one of them, chosen by
+ * the roll) or is clamped to the end.  Philox rolls keyed by (rngSeed,
+ * protein gid, step count), distinct from the binding step's.  stats
+ * (nullable, one per replica): stages after the motion, nSU and nDS count
+ * walk-offs.  The springs of doubly bound proteins are rebuilt.  aLENS calls
+ * it before the binding step (SRC/TubuleSystem.cpp:185-189). */
+int alens_protein_motion_step(AlensCtx *ctx, AlensKmcStats *stats);
 
 /* CUDA-event times (ms) of the stages of the last step when stageTiming is
  * on: ms[0] detect, ms[1] main solve kernel (FP32 kernel in mixed mode),

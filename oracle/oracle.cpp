@@ -1427,6 +1427,18 @@ double orc_log(double x) { return det_log(x); }
 
 void orc_sincos(double x, double *s, double *c) { det_sincos(x, s, c); }
 
+void orc_normal_pair(uint32_t wa, uint32_t wb, double *z0, double *z1) {
+    // one Box-Muller pair of normals6 on two Philox words
+    const float ua = ((float)(wa >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    const float ub = ((float)(wb >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    const float r = std::sqrt(-2.0f * det_logf(ua));
+    const float ang = ub * 6.28318531f - 3.14159265f;
+    float sn, cs;
+    det_sincosf(ang, &sn, &cs);
+    *z0 = (double)(r * -cs);
+    *z1 = (double)(r * -sn);
+}
+
 void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
     philox(ctr, key, out);
 }

@@ -61,6 +61,8 @@ int orc_set_protein_types(OrcCtx *ctx, int n, const AlensProteinType *types, dou
 int orc_set_proteins(OrcCtx *ctx, int n, const AlensProtein *proteins);
 int orc_get_proteins(OrcCtx *ctx, int cap, int *n, AlensProtein *proteins);
 int orc_protein_bind_step(OrcCtx *ctx, AlensKmcStats *stats);
+int orc_protein_motion_step(OrcCtx *ctx, AlensKmcStats *stats);
+void orc_normal_pair(uint32_t wa, uint32_t wb, double *z0, double *z1);
 double orc_kmc_exp(double x);
 float orc_kmc_expf(float x);
 double orc_kmc_sd_integral(const AlensProteinType *t, double KBT, double D, double dt, double d2, double sA,

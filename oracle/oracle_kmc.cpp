@@ -144,6 +144,9 @@ struct Kt {
     float prefPar, prefAnti;
     float Df;
     int lookup;
+    // motion step
+    int walkOff, vdrag[2];
+    double fstall, vmax[2], vmaxAP[2], diffS[2], diffD[2], diffU, dragD[2], KBT;
 };
 
 double bind_volume(double a, double c) {
@@ -198,6 +201,19 @@ Kt make_type(const AlensProteinType &in, double KBT, double D, double dt) {
     T.prefPar = r < 1.0f ? r : 1.0f;
     T.prefAnti = r > 1.0f ? 1.0f / r : 1.0f;
     T.Df = (float)D;
+    T.walkOff = in.walkOff ? 1 : 0;
+    T.fstall = in.fstall;
+    for (int e = 0; e < 2; e++) {
+        T.vdrag[e] = in.vdrag[e] ? 1 : 0;
+        T.vmax[e] = in.vmax[e];
+        T.vmaxAP[e] = in.vmaxAP[e];
+        // sqrt(dt D 2) as ProteinData::updatePosWalk / updatePosDiffuse
+        T.diffS[e] = std::sqrt((dt * in.diffBoundS[e]) * 2.0);
+        T.diffD[e] = std::sqrt((dt * in.diffBoundD[e]) * 2.0);
+        T.dragD[e] = in.diffBoundD[e];
+    }
+    T.diffU = std::sqrt((dt * in.diffUnbound) * 2.0);
+    T.KBT = KBT;
     return T;
 }
 
@@ -725,14 +741,156 @@ int protein_step(const OrcCtx *x, const RodView &V, const Grid &G, const Kt &T, 
     return trans;
 }
 
+// a point outside a boundary is moved onto it: wall, sphere (inside /
+// outside), tube (inside)
+void project(const OrcCtx::Bnd &B, double x[3]) {
+    const double v[3] = {x[0] - B.c[0], x[1] - B.c[1], x[2] - B.c[2]};
+    if (B.type == 0) {
+        const double s = v[0] * B.a[0] + v[1] * B.a[1] + v[2] * B.a[2];
+        if (s < 0.0)
+            for (int d = 0; d < 3; d++) x[d] = x[d] - s * B.a[d];
+    } else if (B.type == 1) {
+        const double r = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        const bool out = B.inside ? r > B.R : r < B.R;
+        if (out && r > 0.0)
+            for (int d = 0; d < 3; d++) x[d] = B.c[d] + (B.R / r) * v[d];
+    } else {
+        const double s = v[0] * B.a[0] + v[1] * B.a[1] + v[2] * B.a[2];
+        const double q[3] = {v[0] - s * B.a[0], v[1] - s * B.a[1], v[2] - s * B.a[2]};
+        const double r = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+        if (r > B.R)
+            for (int d = 0; d < 3; d++) x[d] = (B.c[d] + s * B.a[d]) + (B.R / r) * q[d];
+    }
+}
+
+// one protein's motion step (ProteinData::updatePosWalk / updatePosDiffuse,
+// Protein/ProteinData.hpp:318-406; walk velocity :459-478; drag :489-498;
+// spring load of updateForceTorqueBind :418-440); returns the transition
+// (0 none, 2 S->U, 4 D->S by walking off a rod end)
+int protein_motion(const OrcCtx *x, const RodView &V, const Kt &T, AlensProtein &pr) {
+    const AlensConfig &cf = x->cfg;
+    int id[2] = {pr.idBind[0], pr.idBind[1]};
+    for (int e = 0; e < 2; e++)
+        if (id[e] < 0 || id[e] >= x->n) id[e] = -1;
+    const int nb = (id[0] >= 0 ? 1 : 0) + (id[1] >= 0 ? 1 : 0);
+    const uint32_t key[2] = {(uint32_t)cf.rngSeed, (uint32_t)(cf.rngSeed >> 32)};
+    const uint32_t c0[4] = {(uint32_t)(uint64_t)pr.gid, (uint32_t)((uint64_t)pr.gid >> 32), (uint32_t)(uint64_t)x->step,
+                            0x6D6F7400u};
+    const uint32_t c1[4] = {c0[0], c0[1], c0[2], 0x6D6F7401u};
+    uint32_t w[4], v[4];
+    orc_philox4x32(c0, key, w);
+    orc_philox4x32(c1, key, v);
+    const double u01 = u53(w[0], w[1]);
+    double z0, z1, z2, z3;
+    orc_normal_pair(w[2], w[3], &z0, &z1);
+    orc_normal_pair(v[0], v[1], &z2, &z3);
+    int trans = 0;
+    if (nb == 0) {
+        pr.idBind[0] = pr.idBind[1] = -1;
+        pr.pos[0] = pr.pos[0] + T.diffU * z0;
+        pr.pos[1] = pr.pos[1] + T.diffU * z1;
+        pr.pos[2] = pr.pos[2] + T.diffU * z2;
+    } else {
+        double dist[2] = {pr.distBind[0], pr.distBind[1]};
+        if (nb == 2) {
+            double P[2][3];
+            for (int e = 0; e < 2; e++)
+                for (int d = 0; d < 3; d++) P[e][d] = V.c[3 * id[e] + d] + dist[e] * V.a[3 * id[e] + d];
+            double rv[3];
+            for (int d = 0; d < 3; d++) rv[d] = min_image(cf, d, P[0][d] - P[1][d]);
+            const double ell = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+            const double force = (force_length(x, V, T, P[0], id[1], ell) - T.ell0) * T.kappa;
+            const double f0[3] = {-force * (rv[0] / ell), -force * (rv[1] / ell), -force * (rv[2] / ell)};
+            const double *a0 = &V.a[3 * id[0]], *a1 = &V.a[3 * id[1]];
+            const double par = a0[0] * a1[0] + a0[1] * a1[1] + a0[2] * a1[2];
+            const double z[2] = {z0, z1};
+            for (int e = 0; e < 2; e++) {
+                const double *a = e == 0 ? a0 : a1;
+                const double sg = e == 0 ? 1.0 : -1.0;  // the other head's load is -f0
+                const double fdir = sg * (f0[0] * a[0] + f0[1] * a[1] + f0[2] * a[2]);
+                const double sgn = T.vmax[e] > 0.0 ? 1.0 : (T.vmax[e] < 0.0 ? -1.0 : 0.0);
+                const double fproj = (sgn * fdir) / std::fabs(T.fstall);
+                const double one = 1.0 + fproj;
+                const double vfrac = one < 0.0 ? 0.0 : (one > 1.0 ? 1.0 : one);
+                const double vel = (par > 0.0 ? T.vmax[e] : T.vmaxAP[e]) * vfrac;
+                const double drag = T.vdrag[e] ? (fdir * T.dragD[e]) / T.KBT : 0.0;
+                dist[e] = dist[e] + ((vel + drag) * T.dt + T.diffD[e] * z[e]);
+            }
+        } else {
+            const int b = id[0] >= 0 ? 0 : 1;
+            dist[b] = dist[b] + (T.vmax[b] * T.dt + T.diffS[b] * (b == 0 ? z0 : z1));
+        }
+        bool off[2] = {false, false};
+        double half[2] = {0.0, 0.0};
+        for (int e = 0; e < 2; e++) {
+            if (id[e] < 0) continue;
+            half[e] = V.hl[id[e]];
+            off[e] = dist[e] > half[e] || dist[e] < -half[e];
+        }
+        auto clamp = [](double d, double h) { return d > h ? h : (d < -h ? -h : d); };
+        if (T.walkOff) {
+            if (off[0] && off[1]) {
+                const int e = u01 < 0.5 ? 0 : 1;
+                id[e] = -1;
+                dist[1 - e] = clamp(dist[1 - e], half[1 - e]);
+            } else if (off[0]) {
+                id[0] = -1;
+            } else if (off[1]) {
+                id[1] = -1;
+            }
+        } else {
+            for (int e = 0; e < 2; e++)
+                if (id[e] >= 0) dist[e] = clamp(dist[e], half[e]);
+        }
+        const int nb2 = (id[0] >= 0 ? 1 : 0) + (id[1] >= 0 ? 1 : 0);
+        if (nb2 < nb) trans = nb == 2 ? 4 : 2;
+        for (int e = 0; e < 2; e++) {
+            pr.idBind[e] = id[e];
+            pr.distBind[e] = dist[e];
+        }
+    }
+    if (pr.idBind[0] < 0 && pr.idBind[1] < 0)
+        for (const OrcCtx::Bnd &B : x->bnd) project(B, pr.pos);
+    return trans;
+}
+
+// head positions and centre of a protein's state, wrapped
+void protein_geometry(const OrcCtx *x, const RodView &V, AlensProtein &pr) {
+    const AlensConfig &cf = x->cfg;
+    const double qnan = std::numeric_limits<double>::quiet_NaN();
+    for (int e = 0; e < 2; e++) {
+        if (pr.idBind[e] < 0) {
+            pr.distBind[e] = qnan;
+            pr.posEnd[e][0] = pr.posEnd[e][1] = pr.posEnd[e][2] = qnan;
+            continue;
+        }
+        const int r = pr.idBind[e];
+        for (int d = 0; d < 3; d++) pr.posEnd[e][d] = V.c[3 * r + d] + pr.distBind[e] * V.a[3 * r + d];
+    }
+    const int nb = (pr.idBind[0] >= 0 ? 1 : 0) + (pr.idBind[1] >= 0 ? 1 : 0);
+    if (nb == 1) {
+        const int b = pr.idBind[0] >= 0 ? 0 : 1;
+        for (int d = 0; d < 3; d++) pr.pos[d] = pr.posEnd[b][d];
+    } else if (nb == 2) {
+        for (int d = 0; d < 3; d++) {
+            const double dv = min_image(cf, d, pr.posEnd[1][d] - pr.posEnd[0][d]);
+            pr.pos[d] = pr.posEnd[0][d] + 0.5 * dv;
+        }
+    }
+    wrap_point(cf, pr.pos);
+}
+
 bool nonneg(double v) { return std::isfinite(v) && v >= 0.0; }
 
 bool type_ok(const AlensProteinType &p) {
     bool ok = (p.lookupType == 0 || p.lookupType == 1) && std::isfinite(p.kappa) && p.kappa > 0.0 && std::isfinite(p.lambda) &&
               p.lambda >= 0.0 && p.lambda < 1.0 && nonneg(p.freeLength) && std::isfinite(p.rc) && p.rc > 0.0 &&
               nonneg(p.eps) && nonneg(p.diffUnbound) && std::isfinite(p.PtoAPratio) && p.PtoAPratio > 0.0;
+    ok = ok && std::isfinite(p.fstall) && p.fstall != 0.0;
     for (int e = 0; e < 2; e++)
-        ok = ok && nonneg(p.ko_s[e]) && nonneg(p.ko_d[e]) && nonneg(p.Ka[e]) && nonneg(p.Ke[e]);
+        ok = ok && nonneg(p.ko_s[e]) && nonneg(p.ko_d[e]) && nonneg(p.Ka[e]) && nonneg(p.Ke[e]) &&
+             std::isfinite(p.vmax[e]) && std::isfinite(p.vmaxAP[e]) && nonneg(p.diffBoundS[e]) &&
+             nonneg(p.diffBoundD[e]);
     return ok;
 }
 
@@ -845,6 +1003,34 @@ int orc_protein_bind_step(OrcCtx *x, AlensKmcStats *st) {
             if (trans[p] == 3) s.nSD++;
             if (trans[p] == 4) s.nDS++;
             s.maxCandidates = std::max(s.maxCandidates, nc[p]);
+        }
+    }
+    kmc_springs(x);
+    if (st) *st = s;
+    return ALENS_OK;
+}
+
+int orc_protein_motion_step(OrcCtx *x, AlensKmcStats *st) {
+    if (!x) return ALENS_INVALID_ARG;
+    AlensKmcStats s{};
+    if (!x->prot.empty()) {
+        if (x->ptypes.empty()) return ALENS_NOT_READY;
+        const RodView V = rod_view(x);
+        std::vector<Kt> T;
+        for (const AlensProteinType &t : x->ptypes) T.push_back(make_type(t, x->kmcKBT, x->kmcD, x->cfg.dt));
+        const int np = (int)x->prot.size();
+        std::vector<int> trans(np);
+#pragma omp parallel for schedule(static)
+        for (int p = 0; p < np; p++) {
+            trans[p] = protein_motion(x, V, T[x->prot[p].type], x->prot[p]);
+            protein_geometry(x, V, x->prot[p]);
+        }
+        for (int p = 0; p < np; p++) {
+            const AlensProtein &q = x->prot[p];
+            const int nb = (q.idBind[0] >= 0 ? 1 : 0) + (q.idBind[1] >= 0 ? 1 : 0);
+            (nb == 0 ? s.nU : nb == 1 ? s.nS : s.nD)++;
+            if (trans[p] == 2) s.nSU++;
+            if (trans[p] == 4) s.nDS++;
         }
     }
     kmc_springs(x);

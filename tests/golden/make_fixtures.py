@@ -13,8 +13,8 @@ rods 0.07 um apart, the first immovable, 100 doubly bound motors of two
 species): its rods (TubuleInitial.dat lines), its proteins (the 'P' lines of
 ProteinInitial.dat), the species of its ProteinConfig.yaml re-emitted as flat
 keys, and the run settings of its RunConfig.yaml.  Golden outputs: the
-oracle's stage counts over five binding + rod steps (a regression pin of the
-oracle; the reference ships no outputs for this path).
+oracle's stage counts over five motion + binding + rod steps (a regression
+pin of the oracle; the reference ships no outputs for this path).
 
 usage: python tests/golden/make_fixtures.py /path/to/aLENS
 """
@@ -121,7 +121,8 @@ MIX_KEYS = ("rngSeed", "dt", "timeSnap", "simBoxHigh", "simBoxLow", "simBoxPBC",
             "conMaxIte", "conResTol", "conSolverChoice", "sylinderColBuf", "sylinderDiameterColRatio",
             "sylinderLengthColRatio", "sylinderDiameter")
 SPECIES_KEYS = ("tag", "fixedEnd0", "useBindVol", "lookupType", "freeLength", "kappa", "lambda", "PtoAPratio",
-                "diffUnbound", "rc", "eps", "ko_s", "ko_d", "Ka", "Ke")
+                "diffUnbound", "rc", "eps", "ko_s", "ko_d", "Ka", "Ke", "walkOff", "fstall", "vmax", "vmaxAP",
+                "vdrag", "diffBoundS", "diffBoundD")
 
 
 def write_mixmotor_fixture(ref):
@@ -179,6 +180,7 @@ def mixmotor_golden(steps=5):
     o.set_proteins(prots)
     counts = []
     for _ in range(steps):
+        o.protein_motion_step()
         st = o.protein_bind_step()
         r = o.step()
         counts.append([st[k] for k in ("nU", "nS", "nD", "nUS", "nSU", "nSD", "nDS")] + [r["nBilateral"]])

@@ -181,8 +181,9 @@ def test_facade_snapshot_and_restart(gpu_lib, tmp_path):
 
 
 def test_facade_protein_steps_match_oracle(gpu_lib, tmp_path):
-    """TubuleSystem::step()'s order through the facade (calcBindInteraction,
-    then runStep) on the MixMotorSliding example: two parallel 20 um rods,
+    """TubuleSystem::step()'s order through the facade (updateProteinMotion,
+    calcBindInteraction, then runStep) on the MixMotorSliding example: two
+    parallel 20 um rods,
     100 motors of two lookupType 1 species read from its ProteinInitial.dat.
     After five steps the proteins and the per-step counts equal the oracle's
     and the committed golden."""
@@ -191,10 +192,13 @@ def test_facade_protein_steps_match_oracle(gpu_lib, tmp_path):
     setup = tmp_path / "setup.txt"
     with open(setup, "w") as f:
         for t in species:
-            f.write("S %d %d %d %d %r %r %r %r %r %r %r %r %r %r %r %r %r %r %r\n" % (
+            f.write("S %d %d %d %d %r %r %r %r %r %r %r %r %r %r %r %r %r %r %r" % (
                 t.tag, t.fixedEnd0, t.useBindVol, t.lookupType, t.freeLength, t.kappa, t.lambda_, t.PtoAPratio,
                 t.diffUnbound, t.rc, t.eps, t.ko_s[0], t.ko_s[1], t.ko_d[0], t.ko_d[1], t.Ka[0], t.Ka[1], t.Ke[0],
                 t.Ke[1]))
+            f.write(" %d %d %d %r %r %r %r %r %r %r %r %r\n" % (
+                t.walkOff, t.vdrag[0], t.vdrag[1], t.fstall, t.vmax[0], t.vmax[1], t.vmaxAP[0], t.vmaxAP[1],
+                t.diffBoundS[0], t.diffBoundS[1], t.diffBoundD[0], t.diffBoundD[1]))
         for p in prots:
             f.write("P %d %d %d %d %r %r %r %r %r\n" % (int(p["gid"]), int(p["type"]), int(p["idBind"][0]),
                                                       int(p["idBind"][1]), float(p["distBind"][0]),
@@ -214,6 +218,7 @@ def test_facade_protein_steps_match_oracle(gpu_lib, tmp_path):
     o.set_protein_types(species, kbt, make_fixtures.cfg_diameter(cfg))
     o.set_proteins(prots)
     for _ in range(steps):
+        o.protein_motion_step()
         o.protein_bind_step()
         o.step()
     q = o.get_proteins()

@@ -19,20 +19,24 @@ D = 0.025
 def species():
     """Four species that exercise every branch at dt = 1e-4: plain rates,
     bind volume with load-dependent unbinding and PtoAPratio < 1, fixed end
-    0 with PtoAPratio > 1, and the lookupType 1 stretch."""
+    0 with PtoAPratio > 1, and the lookupType 1 stretch; motors walking both
+    ways (fast enough to walk off rod ends within a few steps), drag, bound
+    diffusion, clamped ends."""
     return [
         capi.make_protein_type(tag=0, rc=0.03, ko_s=(200.0, 150.0), Ka=(0.01, 0.012), ko_d=(100.0, 80.0),
                                Ke=(0.5, 0.4), eps=400.0, kappa=200.0, lambda_=0.0, freeLength=0.025,
-                               diffUnbound=1.0),
+                               diffUnbound=1.0, vmax=(50.0, 50.0), diffBoundS=(0.01, 0.01), fstall=2.0),
         capi.make_protein_type(tag=1, rc=0.025, ko_s=(120.0, 120.0), Ka=(0.02, 0.02), ko_d=(90.0, 90.0),
                                Ke=(0.2, 0.2), eps=400.0, kappa=150.0, lambda_=0.3, freeLength=0.03,
-                               useBindVol=True, PtoAPratio=0.5, diffUnbound=2.0),
+                               useBindVol=True, PtoAPratio=0.5, diffUnbound=2.0, vmax=(-80.0, 30.0),
+                               vmaxAP=(-20.0, 10.0), vdrag=(True, False), diffBoundD=(0.02, 0.0), walkOff=False),
         capi.make_protein_type(tag=2, rc=0.04, ko_s=(60.0, 60.0), Ka=(0.01, 0.01), ko_d=(50.0, 70.0),
                                Ke=(0.6, 0.6), eps=300.0, kappa=300.0, lambda_=0.25822, freeLength=0.053,
-                               fixedEnd0=True, PtoAPratio=2.0, diffUnbound=0.5),
+                               fixedEnd0=True, PtoAPratio=2.0, diffUnbound=0.5, vmax=(0.0, 100.0)),
         capi.make_protein_type(tag=3, rc=0.035, ko_s=(150.0, 100.0), Ka=(0.015, 0.015), ko_d=(80.0, 80.0),
                                Ke=(0.8, 0.8), eps=400.0, kappa=100.0, lambda_=0.5, freeLength=0.05,
-                               lookupType=1, diffUnbound=1.0),
+                               lookupType=1, diffUnbound=1.0, vmax=(40.0, -40.0), fstall=1.0,
+                               diffBoundS=(0.005, 0.0), diffBoundD=(0.005, 0.005)),
     ]
 
 
@@ -43,7 +47,7 @@ def same(a, b):
         assert np.array_equal(a[f], b[f], equal_nan=True), f
 
 
-def _pair(w, nprot, seed, steps, move=True, links=None):
+def _pair(w, nprot, seed, steps, move=True, links=None, boundaries=None, motion=True):
     pairs = workloads.pair_list(OracleSystem, w.cfg, w.rods, 0.05)
     prots = workloads.protein_population(w.cfg, w.rods, nprot, pairs=pairs, seed=seed, ntypes=4)
     g = capi.GpuSystem(w.cfg)
@@ -52,16 +56,25 @@ def _pair(w, nprot, seed, steps, move=True, links=None):
         s.set_rods(w.rods)
         if links is not None:
             s.set_links(links)
+        if boundaries is not None:
+            s.set_boundaries(boundaries)
         s.set_protein_types(species(), KBT, D)
     g.set_proteins(prots)
     o.set_proteins(prots)
     same(g.get_proteins(), o.get_proteins())
-    totals = np.zeros(4, dtype=np.int64)
+    totals = np.zeros(6, dtype=np.int64)
     for _ in range(steps):
+        if motion:
+            # TubuleSystem::step(): motion, then binding, then the rods
+            mg = g.protein_motion_step()[0]
+            mo = o.protein_motion_step()
+            assert mg == mo, (mg, mo)
+            totals[4:] += [mg["nSU"], mg["nDS"]]
+            same(g.get_proteins(), o.get_proteins())
         sg = g.protein_bind_step()[0]
         so = o.protein_bind_step()
         assert sg == so, (sg, so)
-        totals += [sg["nUS"], sg["nSU"], sg["nSD"], sg["nDS"]]
+        totals[:4] += [sg["nUS"], sg["nSU"], sg["nSD"], sg["nDS"]]
         same(g.get_proteins(), o.get_proteins())
         if move:
             rg = g.step()
@@ -79,6 +92,23 @@ def test_bind_steps_match_oracle_with_rod_steps(gpu_lib):
     g, o, tot = _pair(w, 4000, seed=7, steps=6)
     # every transition happened
     assert np.all(tot > 0), tot
+    g.close()
+    o.close()
+
+
+def test_protein_steps_with_a_boundary(gpu_lib):
+    """Unbound proteins that diffuse or walk off below a wall are moved onto
+    it; rods get the wall's contacts in the same solve."""
+    w = workloads.small_periodic(n=800, box=4.5, seed=5)
+    w.cfg.simBoxPBC[2] = 0   # a wall in z: z is not periodic
+    wall = capi.make_boundary(capi.BOUNDARY_WALL, center=(0.0, 0.0, 0.3), axis=(0.0, 0.0, 1.0))
+    g, o, tot = _pair(w, 3000, seed=5, steps=4, boundaries=[wall])
+    # after a motion step every unbound protein is on the allowed side
+    assert g.protein_motion_step()[0] == o.protein_motion_step()
+    q = g.get_proteins()
+    same(q, o.get_proteins())
+    unbound = (q["idBind"] < 0).all(axis=1)
+    assert unbound.sum() > 0 and np.all(q["pos"][unbound, 2] >= 0.3 - 1e-12)
     g.close()
     o.close()
 

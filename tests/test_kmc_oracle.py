@@ -397,3 +397,170 @@ def test_invalid_protein_input_is_rejected():
     o.set_proteins(p)
     assert o.protein_bind_step()["nU"] == 1
     o.close()
+
+
+# ------------------------------------------------------------ motion step
+def _motion_system(extra_axis=(1.0, 0.0, 0.0), sep=0.06, walk_type=None, boundaries=None):
+    o, cfg = _one_rod_system(extra=([2.0, 2.0 + sep, 2.0], list(extra_axis)))
+    if boundaries:
+        o.set_boundaries(boundaries)
+    o.set_protein_types([walk_type], KBT, D)
+    return o, cfg
+
+
+def test_unbound_diffusion():
+    """Unbound proteins: pos += sqrt(2 diffUnbound dt) N(0, 1)^3
+    (ProteinData::updatePosDiffuse, Protein/ProteinData.hpp:395-402)."""
+    t = capi.make_protein_type(diffUnbound=2.0, Ka=(0.0, 0.0), Ke=(0.0, 0.0))
+    o, cfg = _motion_system(walk_type=t)
+    n = 40000
+    p = capi.protein_array(n)
+    p["gid"] = np.arange(n)
+    p["pos"] = [1.0, 1.0, 1.0]
+    o.set_proteins(p)
+    st = o.protein_motion_step()
+    assert st["nU"] == n
+    d = o.get_proteins()["pos"] - 1.0
+    msd = float(np.mean(np.sum(d * d, axis=1)))
+    assert abs(msd / (6 * 2.0 * cfg.dt) - 1.0) < 0.03
+    assert abs(float(np.mean(d))) < 5 * math.sqrt(2 * 2.0 * cfg.dt / (3 * n))
+    o.close()
+
+
+def test_singly_bound_walk_and_walk_off():
+    """A singly bound head walks vmax dt (no load, Protein/ProteinData.hpp:328-331);
+    past the rod end it unbinds (walkOff) or is clamped to the end."""
+    for walk_off in (True, False):
+        t = capi.make_protein_type(vmax=(0.8, -0.3), walkOff=walk_off, Ka=(0.0, 0.0), Ke=(0.0, 0.0),
+                                   ko_s=(0.0, 0.0), ko_d=(0.0, 0.0))
+        o, cfg = _motion_system(walk_type=t)
+        p = capi.protein_array(3)
+        p["gid"] = [0, 1, 2]
+        p["idBind"][0, 0], p["distBind"][0, 0] = 0, 0.1           # end 0 walks +0.8 dt
+        p["idBind"][1, 1], p["distBind"][1, 1] = 0, -0.2          # end 1 walks -0.3 dt
+        p["idBind"][2, 0], p["distBind"][2, 0] = 0, 0.5 - 1e-6    # walks past the plus end
+        p["pos"][2] = [2.0 + 0.5 - 1e-6, 2.0, 2.0]                 # its centre: the head
+        o.set_proteins(p)
+        st = o.protein_motion_step()
+        q = o.get_proteins()
+        assert q["distBind"][0, 0] == 0.1 + (0.8 * cfg.dt + 0.0)
+        assert q["distBind"][1, 1] == -0.2 + (-0.3 * cfg.dt + 0.0)
+        if walk_off:
+            assert q["idBind"][2].tolist() == [-1, -1] and st["nSU"] == 1 and st["nU"] == 1
+            # the centre stays at the last head position
+            assert np.allclose(q["pos"][2], [2.0 + 0.5 - 1e-6, 2.0, 2.0], atol=1e-12)
+        else:
+            assert q["idBind"][2, 0] == 0 and q["distBind"][2, 0] == 0.5 and st["nSU"] == 0
+        o.close()
+
+
+def _expected_walk(t, sep, da, db, antiparallel):
+    """Walk velocities of both heads of a doubly bound protein on rods along
+    +x (head 0) and +x or -x (head 1) at distance sep in y, from
+    ProteinData::calcEndWalkVelocity / calcEndDragVelocity and the spring
+    load of updateForceTorqueBind (lookupType 0)."""
+    a0 = np.array([1.0, 0.0, 0.0])
+    a1 = -a0 if antiparallel else a0
+    P0 = np.array([2.0, 2.0, 2.0]) + da * a0
+    P1 = np.array([2.0, 2.0 + sep, 2.0]) + db * a1
+    r = P0 - P1
+    ell = np.linalg.norm(r)
+    force = (ell - D - t.freeLength) * t.kappa
+    f = [-force * r / ell, force * r / ell]
+    out = []
+    for e, a in enumerate((a0, a1)):
+        fdir = float(f[e] @ a)
+        sgn = np.sign(t.vmax[e])
+        vfrac = min(1.0, max(0.0, 1.0 + sgn * fdir / abs(t.fstall)))
+        vel = (t.vmaxAP[e] if antiparallel else t.vmax[e]) * vfrac
+        drag = fdir * t.diffBoundD[e] / KBT if t.vdrag[e] else 0.0
+        out.append(vel + drag)
+    return out
+
+
+@pytest.mark.parametrize("antiparallel", [False, True])
+def test_doubly_bound_walk_under_load(antiparallel):
+    """Each head walks vmax (vmaxAP on antiparallel rods) times
+    clamp(1 + sign(vmax) f.dir / fstall, 0, 1), f the spring load
+    (Protein/ProteinData.hpp:418-478)."""
+    t = capi.make_protein_type(vmax=(0.6, -0.4), vmaxAP=(0.2, -0.1), fstall=3.0, kappa=200.0, freeLength=0.02,
+                               Ka=(0.0, 0.0), Ke=(0.0, 0.0), ko_s=(0.0, 0.0), ko_d=(0.0, 0.0))
+    ax = (-1.0, 0.0, 0.0) if antiparallel else (1.0, 0.0, 0.0)
+    o, cfg = _motion_system(extra_axis=ax, sep=0.06, walk_type=t)
+    da, db = np.array([0.0, 0.05, -0.1]), np.array([0.03, -0.02, 0.0])
+    p = capi.protein_array(3)
+    p["gid"] = [0, 1, 2]
+    p["idBind"][:] = [0, 1]
+    p["distBind"][:, 0], p["distBind"][:, 1] = da, db
+    o.set_proteins(p)
+    o.protein_motion_step()
+    q = o.get_proteins()
+    for k in range(3):
+        v = _expected_walk(t, 0.06, da[k], db[k], antiparallel)
+        assert abs(q["distBind"][k, 0] - (da[k] + v[0] * cfg.dt)) < 1e-15
+        assert abs(q["distBind"][k, 1] - (db[k] + v[1] * cfg.dt)) < 1e-15
+    o.close()
+
+
+def test_drag_and_bound_diffusion():
+    """vdrag adds load x diffBoundD / KBT to a doubly bound head's velocity;
+    the head also diffuses with diffBoundD (mean over many proteins)."""
+    t = capi.make_protein_type(vmax=(0.0, 0.0), vdrag=(True, True), diffBoundD=(0.05, 0.05), kappa=200.0,
+                               freeLength=0.02, Ka=(0.0, 0.0), Ke=(0.0, 0.0), ko_s=(0.0, 0.0), ko_d=(0.0, 0.0))
+    o, cfg = _motion_system(sep=0.06, walk_type=t)
+    n = 20000
+    p = capi.protein_array(n)
+    p["gid"] = np.arange(n)
+    p["idBind"][:] = [0, 1]
+    p["distBind"][:] = [0.0, 0.04]
+    o.set_proteins(p)
+    o.protein_motion_step()
+    q = o.get_proteins()
+    v = _expected_walk(t, 0.06, 0.0, 0.04, False)
+    sd = math.sqrt(2 * 0.05 * cfg.dt)
+    for e, d0 in enumerate((0.0, 0.04)):
+        mean = float(np.mean(q["distBind"][:, e] - d0))
+        assert abs(mean - v[e] * cfg.dt) < 5 * sd / math.sqrt(n)
+        assert abs(float(np.std(q["distBind"][:, e])) / sd - 1.0) < 0.05
+    o.close()
+
+
+def test_doubly_bound_both_ends_off():
+    """Both heads past their rod ends: one head, chosen by the roll with
+    probability 1/2, unbinds; the other is clamped (Protein/ProteinData.hpp:352-381)."""
+    t = capi.make_protein_type(vmax=(1.0, -1.0), fstall=1e9, Ka=(0.0, 0.0), Ke=(0.0, 0.0), ko_s=(0.0, 0.0),
+                               ko_d=(0.0, 0.0))
+    o, cfg = _motion_system(sep=0.06, walk_type=t)
+    n = 4000
+    p = capi.protein_array(n)
+    p["gid"] = np.arange(n)
+    p["idBind"][:] = [0, 1]
+    p["distBind"][:] = [0.5 - 1e-6, -0.5 + 1e-6]
+    o.set_proteins(p)
+    st = o.protein_motion_step()
+    q = o.get_proteins()
+    assert st["nDS"] == n and st["nS"] == n
+    k0 = int(np.sum(q["idBind"][:, 0] == -1))
+    assert _binom_ok(k0, n, 0.5)
+    kept0 = q["idBind"][:, 0] == 0
+    assert np.all(q["distBind"][kept0, 0] == 0.5) and np.all(q["distBind"][~kept0, 1] == -0.5)
+    o.close()
+
+
+def test_unbound_boundary_projection():
+    """Unbound proteins outside a boundary after the motion are moved onto it
+    (SRC/TubuleSystem.cpp:285-305): wall, and inside a sphere."""
+    t = capi.make_protein_type(diffUnbound=0.0, Ka=(0.0, 0.0), Ke=(0.0, 0.0))
+    wall = capi.make_boundary(capi.BOUNDARY_WALL, center=(0.0, 0.0, 1.5), axis=(0.0, 0.0, 1.0))
+    sph = capi.make_boundary(capi.BOUNDARY_SPHERE, center=(2.0, 2.0, 2.0), radius=1.2, inside=True)
+    o, cfg = _motion_system(walk_type=t, boundaries=[wall, sph])
+    p = capi.protein_array(3)
+    p["gid"] = [0, 1, 2]
+    p["pos"] = [[2.0, 2.0, 1.2], [2.0, 3.5, 2.0], [2.1, 2.0, 2.0]]
+    o.set_proteins(p)
+    o.protein_motion_step()
+    q = o.get_proteins()
+    assert np.allclose(q["pos"][0], [2.0, 2.0, 1.5], atol=1e-12)      # onto the wall
+    assert np.allclose(q["pos"][1], [2.0, 3.2, 2.0], atol=1e-12)      # onto the sphere
+    assert np.allclose(q["pos"][2], [2.1, 2.0, 2.0], atol=1e-15)      # inside both: unchanged
+    o.close()
