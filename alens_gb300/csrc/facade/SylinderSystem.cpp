@@ -467,8 +467,10 @@ void SylinderSystem::writeResult() {
     if (haveProteins_) {
         std::vector<int64_t> gid;
         for (const Sylinder &r : getContainer()) gid.push_back(r.gid);
-        writeProteinAscii(folder + "ProteinAscii_" + std::to_string(snapID_) + ".dat", getProteins(), proteinTags_,
-                          gid, runConfig.dt * (double)getStepCount());
+        const auto prot = getProteins();
+        writeProteinAscii(folder + "ProteinAscii_" + std::to_string(snapID_) + ".dat", prot, proteinTags_, gid,
+                          runConfig.dt * (double)getStepCount());
+        writeProteinVTK(folder, snapID_, prot, proteinTags_, gid);
     }
     std::FILE *f = std::fopen("TimeStepInfo.txt", "w");
     if (!f) throw std::runtime_error("cannot write TimeStepInfo.txt");
@@ -798,6 +800,52 @@ AlensKmcStats SylinderSystem::calcBindInteraction() {
     AlensKmcStats st{};
     check(alens_protein_bind_step(ctx_, &st), "alens_protein_bind_step");
     return st;
+}
+
+void SylinderSystem::writeProteinVTK(const std::string &folder, int snapID, const std::vector<AlensProtein> &proteins,
+                                     const std::vector<int> &typeTag, const std::vector<int64_t> &rodGid) {
+    const size_t n = proteins.size();
+    std::vector<double> pts(6 * n);
+    std::vector<int32_t> conn(2 * n), offs(n), ids(2 * n), gid(n), tag(n);
+    for (size_t k = 0; k < n; k++) {
+        const AlensProtein &p = proteins[k];
+        const bool both = p.idBind[0] >= 0 && p.idBind[1] >= 0;
+        for (int d = 0; d < 3; d++) {
+            pts[6 * k + d] = both ? p.posEnd[0][d] : p.pos[d];
+            pts[6 * k + 3 + d] = both ? p.posEnd[1][d] : p.pos[d];
+        }
+        for (int e = 0; e < 2; e++) ids[2 * k + e] = p.idBind[e] >= 0 ? (int32_t)rodGid.at(p.idBind[e]) : -1;
+        conn[2 * k] = (int32_t)(2 * k);
+        conn[2 * k + 1] = (int32_t)(2 * k + 1);
+        offs[k] = (int32_t)(2 * k + 2);
+        gid[k] = (int32_t)p.gid;
+        tag[k] = typeTag.at(p.type);
+    }
+    const std::string sep = (folder.empty() || folder.back() == '/') ? "" : "/";
+    const std::string piece = "Protein_r0_" + std::to_string(snapID) + ".vtp";
+    const char *head = "<?xml version=\"1.0\"?>\n";
+    {
+        std::ofstream f(folder + sep + piece, std::ios::binary);
+        if (!f) throw std::runtime_error("cannot write " + folder + sep + piece);
+        f << head << "<VTKFile type=\"PolyData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+          << "<PolyData>\n<Piece NumberOfPoints=\"" << 2 * n << "\" NumberOfVerts=\"0\" NumberOfLines=\"" << n
+          << "\" NumberOfStrips=\"0\" NumberOfPolys=\"0\">\n"
+          << "<Points>\n" << dataArray("position", "Float64", 3, pts) << "</Points>\n"
+          << "<Lines>\n" << dataArray("connectivity", "Int32", 1, conn) << dataArray("offsets", "Int32", 1, offs)
+          << "</Lines>\n<PointData Scalars=\"scalars\">\n" << dataArray("idBind", "Int32", 1, ids)
+          << "</PointData>\n<CellData Scalars=\"scalars\">\n" << dataArray("gid", "Int32", 1, gid)
+          << dataArray("tag", "Int32", 1, tag) << "</CellData>\n</Piece>\n</PolyData>\n</VTKFile>\n";
+    }
+    std::ofstream f(folder + sep + "Protein_" + std::to_string(snapID) + ".pvtp", std::ios::binary);
+    if (!f) throw std::runtime_error("cannot write the index of " + piece);
+    f << head << "<VTKFile type=\"PPolyData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+      << "<PPolyData GhostLevel=\"0\">\n<PPoints>\n"
+      << "<PDataArray type=\"Float64\" Name=\"position\" NumberOfComponents=\"3\"/>\n</PPoints>\n"
+      << "<PPointData Scalars=\"scalars\">\n<PDataArray type=\"Int32\" Name=\"idBind\" NumberOfComponents=\"1\"/>\n"
+      << "</PPointData>\n<PCellData Scalars=\"scalars\">\n"
+      << "<PDataArray type=\"Int32\" Name=\"gid\" NumberOfComponents=\"1\"/>\n"
+      << "<PDataArray type=\"Int32\" Name=\"tag\" NumberOfComponents=\"1\"/>\n"
+      << "</PCellData>\n<Piece Source=\"" << piece << "\"/>\n</PPolyData>\n</VTKFile>\n";
 }
 
 void SylinderSystem::writeProteinAscii(const std::string &path, const std::vector<AlensProtein> &proteins,

@@ -229,6 +229,14 @@ class SylinderSystem {
     // bound rods as gids).  Same bytes as alens_gb300.io.write_protein_ascii.
     static void writeProteinAscii(const std::string &path, const std::vector<AlensProtein> &proteins,
                                   const std::vector<int> &typeTag, const std::vector<int64_t> &rodGid, double time);
+    // Protein_<snapID>.pvtp and its piece Protein_r0_<snapID>.vtp in
+    // `folder` (ProteinData::writeVTP / writePVTP,
+    // Protein/ProteinData.hpp:583-700): two points per protein (the heads
+    // when both are bound, the centre twice otherwise) joined by a line
+    // cell, point data idBind (rod gids), cell data gid and tag.  Same bytes
+    // as alens_gb300.io.write_protein_pvtp.
+    static void writeProteinVTK(const std::string &folder, int snapID, const std::vector<AlensProtein> &proteins,
+                                const std::vector<int> &typeTag, const std::vector<int64_t> &rodGid);
     AlensCtx *context() const { return ctx_; }
     const AlensStepStats &lastStats() const { return stats_; }
     std::array<double, 9> conStress() const { return stress_; }

@@ -18,8 +18,9 @@
 // Reads the rods and writes Sylinder_<snapID>.pvtp and its piece (no device).
 //
 // usage: facade_driver --write-protein-ascii records.txt out.dat time
-// Writes a ProteinAscii file with SylinderSystem::writeProteinAscii (no
-// device).  records: "T tag..." (tag per species), "R gid..." (rod gids),
+// usage: facade_driver --write-protein-vtk records.txt folder snapID
+// Writes a ProteinAscii file with SylinderSystem::writeProteinAscii, or
+// Protein_<snapID>.pvtp and its piece with writeProteinVTK (no device).  records: "T tag..." (tag per species), "R gid..." (rod gids),
 // then "gid type idBind0 idBind1 pos(3) posEnd0(3) posEnd1(3)" per protein.
 //
 // usage: facade_driver --proteins RunConfig.yaml TubuleInitial.dat setup.txt KBT steps out.txt
@@ -178,7 +179,7 @@ std::vector<std::string> tokens(const std::string &line) {
 
 double num(const std::string &s) { return std::strtod(s.c_str(), nullptr); }
 
-int writeProteinAsciiMode(const char *records, const char *out, double time) {
+int writeProteinAsciiMode(const char *records, const char *out, double time, int vtkSnap = -1) {
     std::ifstream in(records);
     std::string line;
     std::vector<int> tags;
@@ -205,7 +206,10 @@ int writeProteinAsciiMode(const char *records, const char *out, double time) {
             prot.push_back(p);
         }
     }
-    gpu::SylinderSystem::writeProteinAscii(out, prot, tags, gids, time);
+    if (vtkSnap >= 0)
+        gpu::SylinderSystem::writeProteinVTK(out, vtkSnap, prot, tags, gids);
+    else
+        gpu::SylinderSystem::writeProteinAscii(out, prot, tags, gids, time);
     return 0;
 }
 
@@ -297,6 +301,14 @@ int proteinsMode(const char *runConfig, const char *tubules, const char *setup, 
 }  // namespace
 
 int main(int argc, char **argv) {
+    if (argc == 5 && std::strcmp(argv[1], "--write-protein-vtk") == 0) {
+        try {
+            return writeProteinAsciiMode(argv[2], argv[3], 0.0, std::atoi(argv[4]));
+        } catch (const std::exception &e) {
+            std::fprintf(stderr, "facade_driver: %s\n", e.what());
+            return 1;
+        }
+    }
     if (argc == 5 && std::strcmp(argv[1], "--write-protein-ascii") == 0) {
         try {
             return writeProteinAsciiMode(argv[2], argv[3], std::strtod(argv[4], nullptr));

@@ -331,12 +331,85 @@ def write_conblock_pvtp(folder, snap_id: int, blocks: dict, gid):
         f.write(f'</PCellData>\n<Piece Source="{piece}"/>\n</PPolyData>\n</VTKFile>\n')
 
 
+def protein_points(proteins, rod_gid):
+    """The two points per protein of its snapshot lines (the heads when both
+    are bound, the centre twice otherwise) and the bound rods as gids."""
+    n = proteins.shape[0]
+    both = (proteins["idBind"] >= 0).all(axis=1)
+    pts = np.empty((2 * n, 3))
+    pts[0::2] = np.where(both[:, None], proteins["posEnd"][:, 0], proteins["pos"])
+    pts[1::2] = np.where(both[:, None], proteins["posEnd"][:, 1], proteins["pos"])
+    rg = np.asarray(rod_gid, dtype=np.int64)
+    ids = np.where(proteins["idBind"] >= 0, rg[np.maximum(proteins["idBind"], 0)] if rg.size else -1, -1)
+    return pts, ids
+
+
+def write_protein_pvtp(folder, snap_id: int, proteins, species, rod_gid):
+    """Protein_<id>.pvtp and its piece Protein_r0_<id>.vtp in `folder`
+    (ProteinData::writeVTP / writePVTP, Protein/ProteinData.hpp:583-700):
+    two points per protein joined by a line cell, point data idBind (the
+    bound rods' gids, -1 unbound), cell data gid and tag (Int32 as the
+    reference writes them).  The C++ facade writes the same bytes."""
+    import os
+    n = proteins.shape[0]
+    pts, ids = protein_points(proteins, rod_gid)
+    tags = np.array([species[int(t)].tag for t in proteins["type"]], dtype="<i4")
+    piece = f"Protein_r0_{snap_id}.vtp"
+    head = '<?xml version="1.0"?>\n'
+    with open(os.path.join(folder, piece), "w") as f:
+        f.write(head + '<VTKFile type="PolyData" version="1.0" byte_order="LittleEndian" header_type="UInt64">\n')
+        f.write(f'<PolyData>\n<Piece NumberOfPoints="{2 * n}" NumberOfVerts="0" NumberOfLines="{n}" '
+                'NumberOfStrips="0" NumberOfPolys="0">\n')
+        f.write("<Points>\n" + _b64_array("position", "Float64", pts.astype("<f8"), 3) + "</Points>\n")
+        f.write("<Lines>\n" + _b64_array("connectivity", "Int32", np.arange(2 * n, dtype="<i4"), 1)
+                + _b64_array("offsets", "Int32", 2 * np.arange(1, n + 1, dtype="<i4"), 1) + "</Lines>\n")
+        f.write('<PointData Scalars="scalars">\n' + _b64_array("idBind", "Int32", ids.reshape(-1).astype("<i4"), 1)
+                + "</PointData>\n")
+        f.write('<CellData Scalars="scalars">\n' + _b64_array("gid", "Int32", proteins["gid"].astype("<i4"), 1)
+                + _b64_array("tag", "Int32", tags, 1) + "</CellData>\n</Piece>\n</PolyData>\n</VTKFile>\n")
+    with open(os.path.join(folder, f"Protein_{snap_id}.pvtp"), "w") as f:
+        f.write(head + '<VTKFile type="PPolyData" version="1.0" byte_order="LittleEndian" header_type="UInt64">\n')
+        f.write('<PPolyData GhostLevel="0">\n<PPoints>\n'
+                '<PDataArray type="Float64" Name="position" NumberOfComponents="3"/>\n</PPoints>\n')
+        f.write('<PPointData Scalars="scalars">\n<PDataArray type="Int32" Name="idBind" NumberOfComponents="1"/>\n'
+                '</PPointData>\n<PCellData Scalars="scalars">\n'
+                '<PDataArray type="Int32" Name="gid" NumberOfComponents="1"/>\n'
+                '<PDataArray type="Int32" Name="tag" NumberOfComponents="1"/>\n')
+        f.write(f'</PCellData>\n<Piece Source="{piece}"/>\n</PPolyData>\n</VTKFile>\n')
+
+
+def read_protein_pvtp(path):
+    """The proteins of a Protein_<id>.pvtp snapshot (its pieces, in order),
+    as read_protein_ascii returns them, for the restart of
+    TubuleSystem::readProteinVTK (SRC/TubuleSystem.cpp:811-872): rebuild the
+    bindings with proteins_from_ascii."""
+    import os
+    import re
+    text = open(path).read()
+    pieces = re.findall(r'<Piece Source="([^"]+)"', text)
+    parts = []
+    for pc in pieces:
+        body = open(os.path.join(os.path.dirname(path), pc)).read()
+
+        def arr(name, dtype):
+            m = re.search(rf'Name="{name}" NumberOfComponents="\d+" format="binary">([^<]*)<', body)
+            return read_vtk_binary_array(m.group(1), dtype)
+        pts = arr("position", "<f8").reshape(-1, 3)
+        ids = arr("idBind", "<i4").reshape(-1, 2)
+        parts.append({"gid": arr("gid", "<i4").astype(np.int64), "tag": arr("tag", "<i4").astype(np.int32),
+                      "end0": pts[0::2], "end1": pts[1::2], "idBind": ids.astype(np.int64)})
+    return {k: np.concatenate([p[k] for p in parts]) for k in ("gid", "tag", "end0", "end1", "idBind")}
+
+
 def write_snapshot(snap_id: int, rods: RodState, step: int, time: float, root: str = "./result", links=(),
-                   group=None, info_path: str = "TimeStepInfo.txt", blocks: dict | None = None) -> str:
-    """One aLENS snapshot: SylinderAscii_<id>.dat, Sylinder_<id>.pvtp (+ piece)
-    and, with `blocks` (GpuSystem.constraint_blocks() of the last step),
-    ConBlock_<id>.pvtp (+ piece) in result_folder(snap_id, root), then the
-    restart bookkeeping file.  Returns the folder."""
+                   group=None, info_path: str = "TimeStepInfo.txt", blocks: dict | None = None,
+                   proteins=None, species=None) -> str:
+    """One aLENS snapshot: SylinderAscii_<id>.dat, Sylinder_<id>.pvtp (+ piece),
+    with `blocks` (GpuSystem.constraint_blocks() of the last step)
+    ConBlock_<id>.pvtp (+ piece), with `proteins` and `species`
+    ProteinAscii_<id>.dat and Protein_<id>.pvtp (+ piece), in
+    result_folder(snap_id, root), then the restart bookkeeping file.
+    Returns the folder."""
     import os
     folder = result_folder(snap_id, root)
     os.makedirs(folder, exist_ok=True)
@@ -345,6 +418,10 @@ def write_snapshot(snap_id: int, rods: RodState, step: int, time: float, root: s
     write_sylinder_pvtp(folder, snap_id, rods, group=group)
     if blocks is not None:
         write_conblock_pvtp(folder, snap_id, blocks, rods.gid)
+    if proteins is not None:
+        write_protein_ascii(os.path.join(folder, f"ProteinAscii_{snap_id}.dat"), proteins, species, rods.gid,
+                            time=time)
+        write_protein_pvtp(folder, snap_id, proteins, species, rods.gid)
     write_time_step_info(info_path, step, snap_id, time)
     return folder
 

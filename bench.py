@@ -571,7 +571,75 @@ def other_workloads(torch, stream, flush, mlp, steps):
         torch, stream, flush, w4, rods4, 200000,
         capi.make_protein_type(rc=0.03, ko_s=(200.0, 150.0), Ka=(0.01, 0.012), ko_d=(100.0, 80.0), Ke=(0.5, 0.4)),
         steps)
+    out["full_step_monolayer_20000_rods_20000_proteins"] = full_step_workload(torch, stream, flush, steps)
     return out
+
+
+def full_step_workload(torch, stream, flush, steps):
+    """The whole aLENS step with proteins, in TubuleSystem::step()'s order:
+    protein motion, binding (doubly bound proteins become springs), then the
+    rod step (FP64 solver, the plain arm's configuration), on the dense
+    monolayer with 20,000 proteins of its example crosslinker (walking
+    0.5 um/s).  Device time per step (CUDA events, L2 flushed), springs per
+    step, and the oracle over a bounded sample of the same steps."""
+    from alens_gb300 import capi, oracle_api, workloads
+    w = workloads.dense_monolayer()
+    cfg = workloads.config_with(w.cfg, precision=capi.PREC_FP64, warmStart=capi.WARM_ZERO)
+    pairs = workloads.pair_list(capi.GpuSystem, cfg, w.rods, 0.05)
+    prots = workloads.protein_population(cfg, w.rods, 20000, pairs=pairs, seed=1)
+    ptype = capi.make_protein_type()
+    c = workloads.config_with(cfg)
+    c.stream = stream.cuda_stream
+    g = capi.GpuSystem(c)
+    g.set_rods(w.rods)
+    g.set_protein_types([ptype], KMC_KBT, KMC_D)
+    g.set_proteins(prots)
+    for _ in range(3):
+        g.protein_motion_step()
+        g.protein_bind_step()
+        g.step()
+    ms, springs, iters = [], [], []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.protein_motion_step()
+        kb = g.protein_bind_step()[0]
+        st = g.step()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        springs.append(kb["nD"])
+        iters.append(st["iterations"])
+    pos, quat = g.get_rods()
+    state = g.get_proteins()
+    g.close()
+    threads = os.cpu_count() or 1
+    oracle_api.set_threads(threads)
+    o = oracle_api.OracleSystem(cfg)
+    o.set_rods(capi.RodState(w.rods.gid, pos, quat, w.rods.length, w.rods.radius))
+    o.set_protein_types([ptype], KMC_KBT, KMC_D)
+    o.set_proteins(state)
+    t0 = time.perf_counter()
+    n = 0
+    while n < 20:
+        o.protein_motion_step()
+        o.protein_bind_step()
+        o.step()
+        n += 1
+        if time.perf_counter() - t0 > 10.0:
+            break
+    cpu_ms = (time.perf_counter() - t0) / n * 1e3
+    o.close()
+    med = statistics.median(ms)
+    return {"rods": w.rods.n, "proteins": 20000, "steps": steps, "ms_per_step": med,
+            "rod_steps_per_s": w.rods.n / (med * 1e-3), "springs_per_step": float(np.mean(springs)),
+            "iterations_per_step": float(np.mean(iters)),
+            "cpu_baseline": {"value": cpu_ms, "unit": "ms per step", "cores": threads, "kind": "port",
+                             "sample": f"{n} steps of the oracle from the GPU's state"},
+            "speedup_vs_cpu_baseline": cpu_ms / med}
 
 
 KMC_KBT = 0.00411   # pN um (ProteinConfig KBT of the examples)

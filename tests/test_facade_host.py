@@ -139,10 +139,12 @@ def test_facade_conblock_writer_matches_python(tmp_path):
 
 
 def test_facade_protein_ascii_writer_matches_python(tmp_path):
-    """The facade's ProteinAscii writer (SylinderSystem::writeProteinAscii)
-    and io.write_protein_ascii produce the same bytes: doubly bound (head
-    positions), singly bound and unbound (the centre twice) proteins of two
-    species, rod gids for the bound ends."""
+    """The facade's ProteinAscii and Protein_<id>.pvtp writers
+    (SylinderSystem::writeProteinAscii / writeProteinVTK) and
+    io.write_protein_ascii / write_protein_pvtp produce the same bytes:
+    doubly bound (head positions), singly bound and unbound (the centre
+    twice) proteins of two species, rod gids for the bound ends; both read
+    back."""
     import numpy as np
     from alens_gb300 import capi, io
     rng = np.random.default_rng(5)
@@ -174,6 +176,20 @@ def test_facade_protein_ascii_writer_matches_python(tmp_path):
     assert proc.returncode == 0, proc.stderr
     io.write_protein_ascii(str(py), p, species, rod_gid, time=0.0125)
     assert cpp.read_bytes() == py.read_bytes()
+    # the VTK snapshot pair, same bytes, and read back as the restart does
+    vc, vp = tmp_path / "vtk_cpp", tmp_path / "vtk_py"
+    vc.mkdir()
+    vp.mkdir()
+    proc = subprocess.run([str(exe), "--write-protein-vtk", str(rec), str(vc), "9"], capture_output=True,
+                          text=True, timeout=120)
+    assert proc.returncode == 0, proc.stderr
+    io.write_protein_pvtp(str(vp), 9, p, species, rod_gid)
+    for name in ("Protein_9.pvtp", "Protein_r0_9.vtp"):
+        assert (vc / name).read_bytes() == (vp / name).read_bytes(), name
+    rv = io.read_protein_pvtp(str(vp / "Protein_9.pvtp"))
+    pts, ids = io.protein_points(p, rod_gid)
+    assert np.array_equal(rv["gid"], p["gid"]) and np.array_equal(rv["idBind"], ids)
+    assert np.array_equal(rv["end0"], pts[0::2]) and np.array_equal(rv["end1"], pts[1::2])
     # and it reads back
     back = io.read_protein_ascii(str(py))
     assert np.array_equal(back["gid"], p["gid"])

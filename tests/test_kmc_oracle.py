@@ -564,3 +564,41 @@ def test_unbound_boundary_projection():
     assert np.allclose(q["pos"][1], [2.0, 3.2, 2.0], atol=1e-12)      # onto the sphere
     assert np.allclose(q["pos"][2], [2.1, 2.0, 2.0], atol=1e-15)      # inside both: unchanged
     o.close()
+
+
+def test_protein_snapshot_restart_round_trip(tmp_path):
+    """write_snapshot(proteins=...) writes ProteinAscii_<id>.dat and
+    Protein_<id>.pvtp; reading the .pvtp back and rebuilding the bindings
+    (the restart of TubuleSystem::readProteinVTK) gives the same stages,
+    rods and arc positions."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_fixtures as mf
+    from alens_gb300 import io
+    cfg, rods, kbt, species, prots = mf.load_mixmotor()
+    o = oa.OracleSystem(cfg)
+    o.set_rods(rods)
+    o.set_protein_types(species, kbt, mf.cfg_diameter(cfg))
+    o.set_proteins(prots)
+    for _ in range(2):
+        o.protein_motion_step()
+        o.protein_bind_step()
+        o.step()
+    # the snapshot is taken where aLENS writes it: after the binding step,
+    # before the rods move (SRC/TubuleSystem.cpp:205-224)
+    o.protein_motion_step()
+    o.protein_bind_step()
+    q = o.get_proteins()
+    pos, quat = o.get_rods()
+    o.close()
+    now = capi.RodState(rods.gid, pos, quat, rods.length, rods.radius, rods.immovable)
+    folder = io.write_snapshot(3, now, step=2, time=2 * cfg.dt, root=str(tmp_path / "result"),
+                               info_path=str(tmp_path / "TimeStepInfo.txt"), proteins=q, species=species)
+    assert os.path.exists(folder + "ProteinAscii_3.dat") and os.path.exists(folder + "Protein_r0_3.vtp")
+    back = io.proteins_from_ascii(io.read_protein_pvtp(folder + "Protein_3.pvtp"), now, species, cfg)
+    assert np.array_equal(back["idBind"], q["idBind"]) and np.array_equal(back["gid"], q["gid"])
+    bound = q["idBind"] >= 0
+    assert np.allclose(back["distBind"][bound], q["distBind"][bound], rtol=0, atol=1e-12)
+    txt = io.read_protein_ascii(folder + "ProteinAscii_3.dat")
+    assert np.array_equal(txt["gid"], q["gid"])
