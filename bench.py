@@ -572,10 +572,12 @@ def other_workloads(torch, stream, flush, mlp, steps):
         capi.make_protein_type(rc=0.03, ko_s=(200.0, 150.0), Ka=(0.01, 0.012), ko_d=(100.0, 80.0), Ke=(0.5, 0.4)),
         steps)
     out["full_step_monolayer_20000_rods_20000_proteins"] = full_step_workload(torch, stream, flush, steps)
+    out["full_step_monolayer_20000_rods_20000_proteins"]["fast_form"] = full_step_workload(
+        torch, stream, flush, steps, fast=True, cpu=False)
     return out
 
 
-def full_step_workload(torch, stream, flush, steps):
+def full_step_workload(torch, stream, flush, steps, fast=False, cpu=True):
     """The whole aLENS step with proteins, in TubuleSystem::step()'s order:
     protein motion, binding (doubly bound proteins become springs), then the
     rod step (FP64 solver, the plain arm's configuration), on the dense
@@ -584,7 +586,11 @@ def full_step_workload(torch, stream, flush, steps):
     step, and the oracle over a bounded sample of the same steps."""
     from alens_gb300 import capi, oracle_api, workloads
     w = workloads.dense_monolayer()
-    cfg = workloads.config_with(w.cfg, precision=capi.PREC_FP64, warmStart=capi.WARM_ZERO)
+    if fast:
+        # the fast form's solver settings without the learned start
+        cfg = workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_PREV, conResTol=FAST_TOL)
+    else:
+        cfg = workloads.config_with(w.cfg, precision=capi.PREC_FP64, warmStart=capi.WARM_ZERO)
     pairs = workloads.pair_list(capi.GpuSystem, cfg, w.rods, 0.05)
     prots = workloads.protein_population(cfg, w.rods, 20000, pairs=pairs, seed=1)
     ptype = capi.make_protein_type()
@@ -616,6 +622,13 @@ def full_step_workload(torch, stream, flush, steps):
     pos, quat = g.get_rods()
     state = g.get_proteins()
     g.close()
+    med = statistics.median(ms)
+    res = {"rods": w.rods.n, "proteins": 20000, "steps": steps, "ms_per_step": med,
+           "rod_steps_per_s": w.rods.n / (med * 1e-3), "springs_per_step": float(np.mean(springs)),
+           "iterations_per_step": float(np.mean(iters)),
+           "solver": "mixed precision, previous-gamma start, conResTol 1e-6" if fast else "FP64, zero start"}
+    if not cpu:
+        return res
     threads = os.cpu_count() or 1
     oracle_api.set_threads(threads)
     o = oracle_api.OracleSystem(cfg)
@@ -633,13 +646,10 @@ def full_step_workload(torch, stream, flush, steps):
             break
     cpu_ms = (time.perf_counter() - t0) / n * 1e3
     o.close()
-    med = statistics.median(ms)
-    return {"rods": w.rods.n, "proteins": 20000, "steps": steps, "ms_per_step": med,
-            "rod_steps_per_s": w.rods.n / (med * 1e-3), "springs_per_step": float(np.mean(springs)),
-            "iterations_per_step": float(np.mean(iters)),
-            "cpu_baseline": {"value": cpu_ms, "unit": "ms per step", "cores": threads, "kind": "port",
-                             "sample": f"{n} steps of the oracle from the GPU's state"},
-            "speedup_vs_cpu_baseline": cpu_ms / med}
+    res["cpu_baseline"] = {"value": cpu_ms, "unit": "ms per step", "cores": threads, "kind": "port",
+                           "sample": f"{n} steps of the oracle from the GPU's state"}
+    res["speedup_vs_cpu_baseline"] = cpu_ms / med
+    return res
 
 
 KMC_KBT = 0.00411   # pN um (ProteinConfig KBT of the examples)
