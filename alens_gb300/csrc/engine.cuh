@@ -176,7 +176,8 @@ struct DevState {
     int *tileRep;   // tileCap
     double *stress; // 9 x R outputs
     // single-system solver (kernels_fast.cu): per-block records (2 parities
-    // x kFastMaxGrid blocks x 64 bytes), the spatial row permutation and its
+    // x kFastMaxGrid blocks: 32-byte FP64 records, then 16-byte FP32
+    // records), the spatial row permutation and its
     // inverse (constraint capacity), constraints per cell in Morton order and
     // their exclusive scan (nCells + 1 each), scan scratch, and the cells in
     // Morton order (fixed per context)

@@ -82,15 +82,21 @@ constexpr int kGatherWarp0 = 4;          // warps kGatherWarp0.. copy the halo
 constexpr int kEntSrcMask = (1 << 28) - 1;
 constexpr int kEntOwn = 1 << 30;
 
-// One block's record of a pass (64 bytes): FP64 sums and max (FP64 passes),
-// FP32 sums and max (FP32 passes), the misfit flag.
+// One block's record of a pass.  FP32 passes: one float4 (s.s, s.y, y.y,
+// residual max), the records of all blocks contiguous so that warp 0 of
+// every block reads 32 of them per coalesced load; a block whose rows fit
+// no layout writes kMisfitBits as its residual max (above every float's bit
+// pattern, +inf included, under the integer max that combines them).
+// FP64 passes: FP64 sums and max (32 bytes).
 struct FastRecord {
     double d[4];
-    float f[4];
-    int misfit;
-    int pad[3];
 };
-static_assert(sizeof(FastRecord) == 64, "record size");
+static_assert(sizeof(FastRecord) == 32, "record size");
+constexpr int kMisfitBits = 0x7fffffff;
+// the records region: FP64 records [2][kFastMaxGrid], then FP32 records
+// [2][kFastMaxGrid] (fits the 2 x 8 x kFastMaxGrid doubles of DevState)
+static_assert(2 * kFastMaxGrid * (sizeof(FastRecord) + sizeof(float4)) <= 2 * 8 * kFastMaxGrid * sizeof(double),
+              "records region");
 
 // dynamic shared memory layout (bytes)
 constexpr int kOffOwnSt = 0;                                   // float2 [2][kFastRows]
@@ -169,11 +175,12 @@ __device__ __forceinline__ bool fast_barrier(const DevState &S, int bi, int G, u
 }
 
 // Block record: warp sums in Real, then warp 0 adds the eight warp values
-// in Real (fixed xor tree; lane = 4 * warp + quantity) and lanes 0-3 store
-// the four values (FP32 passes: f, FP64 passes: d), lane 0 the misfit flag.
+// in Real (fixed xor tree; lane = 4 * warp + quantity); FP32 passes: lane 0
+// stores the four values as one float4 (the misfit flag in the residual
+// max), FP64 passes: lanes 0-3 store one value each.
 template <class Real>
 __device__ __forceinline__ void block_record(Real v0, Real v1, Real v2, Real vm, int misfit, FastShared &sh,
-                                             FastRecord *rec) {
+                                             FastRecord *rec, float4 *rec32) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     v0 = warp_tree_sum_t<Real>(v0);
     v1 = warp_tree_sum_t<Real>(v1);
@@ -209,32 +216,27 @@ __device__ __forceinline__ void block_record(Real v0, Real v1, Real v2, Real vm,
             const Real o = __shfl_xor_sync(0xffffffffu, v, off);
             v = q == 3 ? (o > v ? o : v) : v + o;
         }
-        if (lane < 4) {
-            if constexpr (sizeof(Real) == 4)
-                __stcg(&rec->f[lane], v);
-            else
-                __stcg(&rec->d[lane], v);
+        if constexpr (sizeof(Real) == 4) {
+            const float r1 = __shfl_sync(0xffffffffu, v, 1), r2 = __shfl_sync(0xffffffffu, v, 2);
+            const float r3 = __shfl_sync(0xffffffffu, v, 3);
+            if (lane == 0) __stcg(rec32, make_float4(v, r1, r2, misfit ? __int_as_float(kMisfitBits) : r3));
+        } else {
+            if (lane < 4) __stcg(&rec->d[lane], v);
         }
-        if (lane == 0) __stcg(&rec->misfit, misfit);
     }
 }
 
 // FP32 records of all G blocks, summed by warp 0 in double-float in block
 // order (lane l adds blocks l, l+32, ..., then a fixed xor tree), residual
 // max through the bit patterns of non-negative floats.  Results in lane 0.
-__device__ __forceinline__ void grid_records32(const FastRecord *rec, int G, FastShared &sh) {
+__device__ __forceinline__ void grid_records32(const float4 *rec, int G, FastShared &sh) {
     const int lane = threadIdx.x & 31;
     constexpr int kMaxPer = (kFastMaxGrid + 31) / 32;
     float4 v[kMaxPer];
-    int mis = 0;
 #pragma unroll
     for (int j = 0; j < kMaxPer; j++) {
         const int bb = lane + 32 * j;
-        v[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (bb < G) {
-            v[j] = __ldcg(reinterpret_cast<const float4 *>(rec[bb].f));
-            mis |= __ldcg(&rec[bb].misfit);
-        }
+        v[j] = bb < G ? __ldcg(rec + bb) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f, h2 = 0.0f, l2 = 0.0f;
     int m = 0;
@@ -257,7 +259,6 @@ __device__ __forceinline__ void grid_records32(const FastRecord *rec, int G, Fas
         df_add(h2, l2, a2, b2);
         m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
     }
-    mis = __reduce_or_sync(0xffffffffu, mis);
     if (lane == 0) {
         // the double-float sums rounded to FP32 (the FP32 phase decides and
         // steps in FP32)
@@ -265,12 +266,12 @@ __device__ __forceinline__ void grid_records32(const FastRecord *rec, int G, Fas
         sh.red32[1] = h1;
         sh.red32[2] = h2;
         sh.red32[3] = __int_as_float(m);
-        sh.misfit = mis;
+        sh.misfit = m == kMisfitBits ? 1 : 0;
     }
 }
 
 // FP64 records of all G blocks: warp q (0-2) accumulates quantity q in FP64
-// in block order, warp 3 the max and misfit flags (the warps run on
+// in block order, warp 3 the max (the warps run on
 // different SM sub-partitions).  Results after the next __syncthreads.
 __device__ __forceinline__ void grid_records64(const FastRecord *rec, int G, FastShared &sh) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -291,14 +292,12 @@ __device__ __forceinline__ void grid_records64(const FastRecord *rec, int G, Fas
         if (lane == 0) sh.red[warp] = a;
     } else if (warp == 3) {
         long long m = 0;
-        int f = 0;
 #pragma unroll
         for (int j = 0; j < kMaxPer; j++) {
             const int bb = lane + 32 * j;
             if (bb < G) {
                 const long long mb = __double_as_longlong(__ldcg(&rec[bb].d[3]));
                 m = mb > m ? mb : m;
-                f |= __ldcg(&rec[bb].misfit);
             }
         }
 #pragma unroll
@@ -306,10 +305,9 @@ __device__ __forceinline__ void grid_records64(const FastRecord *rec, int G, Fas
             const long long o = __shfl_xor_sync(0xffffffffu, m, off);
             m = o > m ? o : m;
         }
-        f = __reduce_or_sync(0xffffffffu, f);
         if (lane == 0) {
             sh.red[3] = __longlong_as_double(m);
-            sh.misfit = f;
+            sh.misfit = 0;  // reported by the first (FP32) pass's records
         }
     }
 }
@@ -414,7 +412,8 @@ __device__ __forceinline__ double lb64_of(int kind, int col, const double *lbGen
     return kind == 0 ? 0.0 : (kind == 1 ? -INFINITY : lbGeneral[col]);
 }
 
-__global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, FastRecord *recs, const int *perm,
+__global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, FastRecord *recs, float4 *recs32,
+                                                              const int *perm,
                                                               const int *inv, unsigned long long timeout_ns) {
     __shared__ FastShared sh;
     // NaNs met by this kernel's row updates are recorded here, not in the
@@ -676,6 +675,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
 #endif
         const bool odd = (p & 1) != 0;
         const FastRecord *recIn = recs + (size_t)((p - 1) & 1) * kFastMaxGrid;
+        const float4 *rec32In = recs32 + (size_t)((p - 1) & 1) * kFastMaxGrid;
         if (sh.phase == kPh32) {
             // the previous pass ran in FP32: this pass (FP32 or the FP64
             // check) needs the halo columns' FP32 iterates; warp 0 reads the
@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                 asm volatile("cp.async.wait_all;" ::: "memory");
             }
             if (p > 0 && warp == 0) {
-                grid_records32(recIn, G, sh);
+                grid_records32(rec32In, G, sh);
                 if (lane == 0) fast_decide(sh, tol, maxIte);
             }
         } else {
@@ -705,6 +705,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
         if (sh.stop) break;
         const int phase = sh.phase, mode = sh.mode;
         FastRecord *recOut = recs + (size_t)(p & 1) * kFastMaxGrid + b;
+        float4 *rec32Out = recs32 + (size_t)(p & 1) * kFastMaxGrid + b;
         if (phase == kPh32) {
             const float alpha = sh.alpha32;
             const float2 *ownIn = ownSt + (odd ? kFastRows : 0);
@@ -857,7 +858,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
             __syncthreads();
             tE = clock64();
 #endif
-            block_record<float>(a0, a1, a2, am, !fit, sh, recOut);
+            block_record<float>(a0, a1, a2, am, !fit, sh, recOut, rec32Out);
 #ifdef ALENS_TRACE_FAST
             tF = clock64();
 #endif
@@ -903,7 +904,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                 am = rm > am ? rm : am;
                 stOut[k] = make_double2(xk, gn);
             }
-            block_record<double>(0.0, 0.0, 0.0, am, !fit, sh, recOut);
+            block_record<double>(0.0, 0.0, 0.0, am, !fit, sh, recOut, rec32Out);
         } else {
             // FP64 refinement: canonical rows of this block, global memory
             const double alpha = sh.alpha;
@@ -918,7 +919,7 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                 a2 = a2 + v2;
                 am = rm > am ? rm : am;
             }
-            block_record<double>(a0, a1, a2, am, !fit, sh, recOut);
+            block_record<double>(a0, a1, a2, am, !fit, sh, recOut, rec32Out);
         }
         lastOut = p;
         if (!fast_barrier(S, p, G, timeout_ns)) return;
@@ -1073,6 +1074,7 @@ cudaError_t launch_solve_fast(const DevState &S, int grid, unsigned long long ti
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, k_solve_fast, S, reinterpret_cast<FastRecord *>(S.fastPart),
+                              reinterpret_cast<float4 *>(S.fastPart + 2 * 4 * (size_t)kFastMaxGrid),
                               (const int *)S.fastPerm, (const int *)S.fastInv, timeout_ns);
 }
 
