@@ -21,10 +21,14 @@
 //     with the rod as I (collisions, then crosslinker and user blocks) in
 //     ascending canonical order, read from the rod rows.  Deterministic.
 //   Rows: block b owns permuted rows [r0, r1) and caches their operator rows
-//     in shared memory (8 bytes per entry).  Each entry's column is either one
-//     of the block's own rows (its iterate is read from the block's own
-//     shared-memory copy) or a halo column, copied from global memory at the
-//     start of each pass (~10 % of the entries on the 20,000-rod layer).
+//     in shared memory (8 bytes per entry: column slot, FP32 value).  Each
+//     entry's column is either one of the block's own rows (its iterate is
+//     the block's own shared-memory copy) or a halo column, copied from
+//     global memory at the start of each pass (~10 % of the entries on the
+//     20,000-rod layer).  After the pass's decision every column's value
+//     (iterate, gradient or projected step, by the pass's mode) is formed
+//     once into a shared-memory slot, so a row entry costs one 8-byte entry
+//     load, one 4-byte gather and one FMA.
 //   FP32 passes: the step size alternates BB1/BB2 as in the other forms.
 //     Each block writes ONE record per pass: s.s, s.y, y.y (FP32 products
 //     summed in FP32 over the block's rows) and the residual max.  After the
@@ -76,9 +80,10 @@ constexpr int kMaxSlices = kFastRows / kSlice;
 constexpr int kFastHalo = 3000;          // halo columns per block
 constexpr int kFastCellRods = 256;       // rods per cell staged in shared memory by the ordering
 constexpr int kRowBatch = 8;             // row entries loaded together
+constexpr int kRegEnts = 16;             // a thread's row entries held in registers for the whole solve
 constexpr int kGatherWarp0 = 4;          // warps kGatherWarp0.. copy the halo
 
-// entry: x = source index | kind << 28 | own << 30, y = FP32 value bits
+// streaming entry: x = source index | kind << 28 | own << 30, y = FP32 value bits
 constexpr int kEntSrcMask = (1 << 28) - 1;
 constexpr int kEntOwn = 1 << 30;
 
@@ -105,12 +110,13 @@ constexpr int kOffOwnLb = kOffOwnQc + kFastRows * 8;            // float [kFastR
 constexpr int kOffRowBeg = kOffOwnLb + kFastRows * 4;           // int [kFastRows + 4]
 constexpr int kOffOwnK = kOffRowBeg + (kFastRows + 4) * 4;      // int [kFastRows] canonical row
 constexpr int kOffOwnA = kOffOwnK + kFastRows * 4;              // int [kFastRows] first entry (aptr)
-constexpr int kOffEnt = kOffOwnA + kFastRows * 4;               // int2 [kFastEnts]
-constexpr int kOffEntCol = kOffEnt + kFastEnts * 8;             // int [kFastEnts] canonical column
-constexpr int kOffHaloPos = kOffEntCol + kFastEnts * 4;         // int [kFastHalo] permuted column
+constexpr int kOffEnt = kOffOwnA + kFastRows * 4;               // int2 [kFastEnts] (column slot, value)
+constexpr int kOffHaloPos = kOffEnt + kFastEnts * 8;            // int [kFastHalo] permuted column
 constexpr int kOffHaloCol = kOffHaloPos + kFastHalo * 4;        // int [kFastHalo] canonical column
-constexpr int kOffGv = kOffHaloCol + kFastHalo * 4;             // float2 [kFastHalo] gathered iterates
-constexpr int kFastSmem = kOffGv + kFastHalo * 8;
+constexpr int kOffHaloLb = kOffHaloCol + kFastHalo * 4;         // float [kFastHalo] lower bound
+constexpr int kOffGv = kOffHaloLb + kFastHalo * 4;              // float2 [kFastHalo] gathered iterates
+constexpr int kOffXcol = kOffGv + kFastHalo * 8;                // float [kFastRows + kFastHalo] column values
+constexpr int kFastSmem = kOffXcol + (kFastRows + kFastHalo) * 4;
 static_assert(kOffEnt % 16 == 0 && kOffGv % 8 == 0, "shared-memory alignment");
 static_assert(kFastSmem + 1024 <= 227 * 1024, "shared memory per block");
 // the streaming layout's sort keys, slot order and slice table alias the
@@ -431,9 +437,12 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
     int *ownK = reinterpret_cast<int *>(smem + kOffOwnK);
     int *ownA = reinterpret_cast<int *>(smem + kOffOwnA);
     int2 *ent = reinterpret_cast<int2 *>(smem + kOffEnt);
-    int *entCol = reinterpret_cast<int *>(smem + kOffEntCol);
     int *haloPos = reinterpret_cast<int *>(smem + kOffHaloPos);
     int *haloCol = reinterpret_cast<int *>(smem + kOffHaloCol);
+    float *haloLb = reinterpret_cast<float *>(smem + kOffHaloLb);
+    // this pass's value of every column the rows read: slots [0, nr) the
+    // block's own rows, kFastRows + h halo column h
+    float *xcol = reinterpret_cast<float *>(smem + kOffXcol);
     float2 *gv = reinterpret_cast<float2 *>(smem + kOffGv);
     // streaming layout (aliases the entry region)
     int *sortKey = reinterpret_cast<int *>(smem + kOffEnt);
@@ -450,6 +459,8 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
     const long long tStart = clock64();
     long long tLoad = 0;
     long long trSum[6] = {0, 0, 0, 0, 0, 0}, trN = 0;
+    __shared__ long long trWarp[kFastWarps];  // each warp's end of its rows
+    long long trW[kFastWarps] = {0, 0, 0, 0, 0, 0, 0, 0};
 #endif
     if (tid == 0) {
         nanSeen = 0;
@@ -503,18 +514,19 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                 const int4 en = __ldg(S.aent32 + ownA[i] + (e - rowBeg[i]));
                 const int pc = __ldcg(inv + en.x);
                 const bool own = (unsigned int)(pc - r0) < (unsigned int)nr;
-                int src;
+                int slot;
                 if (own) {
-                    src = pc - r0;
+                    slot = pc - r0;
                 } else {
-                    src = atomicAdd(&sh.haloCount, 1);
-                    if (src < kFastHalo) {
-                        haloPos[src] = pc;
-                        haloCol[src] = en.x;
+                    const int h = atomicAdd(&sh.haloCount, 1);
+                    if (h < kFastHalo) {
+                        haloPos[h] = pc;
+                        haloCol[h] = en.x;
+                        haloLb[h] = lb32_of(en.y & 3, en.x, S.lb);
                     }
+                    slot = kFastRows + h;  // unused when the halo overflows (the block streams)
                 }
-                ent[e] = make_int2((src & kEntSrcMask) | ((en.y & 3) << 28) | (own ? kEntOwn : 0), en.z);
-                entCol[e] = en.x;
+                ent[e] = make_int2(slot, en.z);
             }
         }
     }
@@ -630,6 +642,22 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
     }
     __syncthreads();
     const int nHalo = (fit && !big) ? sh.haloCount : 0;
+    // when every row of the block has its own thread, a row of at most
+    // kRegEnts entries stays in its thread's registers for the whole solve
+    // (column slot and value; entries past the row end: own column, 0)
+    int regSlot[kRegEnts];
+    float regVal[kRegEnts];
+    bool inRegs = false;
+    if (fit && !big && nr <= kFastThreads && tid < nr) {
+        const int e0 = rowBeg[tid], len = rowBeg[tid + 1] - e0;
+        inRegs = len <= kRegEnts;
+#pragma unroll
+        for (int j = 0; j < kRegEnts; j++) {
+            const int2 en = (inRegs && j < len) ? ent[e0 + j] : make_int2(tid, 0);
+            regSlot[j] = en.x;
+            regVal[j] = __int_as_float(en.y);
+        }
+    }
 #ifdef ALENS_TRACE_FAST
     tLoad = clock64();
 #endif
@@ -812,51 +840,66 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                     if (t < nr) finish_row(i, acc, gam, gold, lbk, xk);
                 }
             }
+            if (fit && !big) {
+                // every column's value for this pass, once: the iterate
+                // (G0), the gradient (AG) or the projected step (iterations)
+                auto colval = [&](float2 v, float lb) {
+                    if (mode == kModeG0) return v.x;
+                    if (mode == kModeAG) return v.y;
+                    return projlb<float>(fmaf(-alpha, v.y, v.x), lb);
+                };
+                const float2 *ownIn = ownSt + (odd ? kFastRows : 0);
+                for (int i = tid; i < nr; i += kFastThreads) xcol[i] = colval(ownIn[i], ownLb[i]);
+                for (int h = tid; h < nHalo; h += kFastThreads) xcol[kFastRows + h] = colval(gv[h], haloLb[h]);
+                __syncthreads();
+            }
             for (int i = tid; i < nr && fit && !big; i += kFastThreads) {
                 const int e0 = rowBeg[i], e1 = rowBeg[i + 1];
                 // the row's own iterate and its x (the diagonal entry's column)
                 const float2 own = ownIn[i];
                 const float gam = own.x, gold = own.y, lbk = ownLb[i];
-                float xk;
-                if (mode == kModeG0)
-                    xk = gam;
-                else if (mode == kModeAG)
-                    xk = gold;
-                else
-                    xk = projlb<float>(fmaf(-alpha, gold, gam), lbk);
+                const float xk = xcol[i];
                 float acc = 0.0f;
-                for (int eb = e0; eb < e1; eb += kRowBatch) {
-                    // all entries of the batch, then all their iterates, are
-                    // requested before any is used; entries past the row end
-                    // read the row's own iterate with value 0
+                if (inRegs) {
+                    // the entries from registers: only the column values are
+                    // read (padding entries add exact zeros)
+                    float xl[kRegEnts];
+#pragma unroll
+                    for (int j = 0; j < kRegEnts; j++) xl[j] = regVal[j] != 0.0f ? xcol[regSlot[j]] : 0.0f;
+#pragma unroll
+                    for (int j = 0; j < kRegEnts; j++) acc = fmaf(regVal[j], xl[j], acc);
+                }
+                for (int eb = e0; eb < e1 && !inRegs; eb += kRowBatch) {
+                    // all entries of the batch, then all their column values,
+                    // are requested before any is used; entries past the row
+                    // end read the row's own column with value 0
                     int2 en[kRowBatch];
-                    float2 sv[kRowBatch];
+                    float xl[kRowBatch];
 #pragma unroll
-                    for (int j = 0; j < kRowBatch; j++) en[j] = eb + j < e1 ? ent[eb + j] : make_int2(i | kEntOwn, 0);
+                    for (int j = 0; j < kRowBatch; j++) en[j] = eb + j < e1 ? ent[eb + j] : make_int2(i, 0);
 #pragma unroll
-                    for (int j = 0; j < kRowBatch; j++) {
-                        const int src = en[j].x & kEntSrcMask;
-                        sv[j] = (en[j].x & kEntOwn) ? ownIn[src] : gv[src];
-                    }
+                    for (int j = 0; j < kRowBatch; j++) xl[j] = xcol[en[j].x];
 #pragma unroll
-                    for (int j = 0; j < kRowBatch; j++) {
-                        const int kind = (en[j].x >> 28) & 3;
-                        const float lbl = kind == 0 ? 0.0f : (kind == 1 ? -INFINITY : (float)S.lb[entCol[eb + j]]);
-                        float xl;
-                        if (mode == kModeG0)
-                            xl = sv[j].x;
-                        else if (mode == kModeAG)
-                            xl = sv[j].y;
-                        else
-                            xl = projlb<float>(fmaf(-alpha, sv[j].y, sv[j].x), lbl);
-                        acc = fmaf(__int_as_float(en[j].y), xl, acc);
-                    }
+                    for (int j = 0; j < kRowBatch; j++) acc = fmaf(__int_as_float(en[j].y), xl[j], acc);
                 }
                 finish_row(i, acc, gam, gold, lbk, xk);
             }
 #ifdef ALENS_TRACE_FAST
+            if (lane == 0) trWarp[warp] = clock64();
             __syncthreads();
             tE = clock64();
+            if (tid == 0) {
+                long long lo = trWarp[0], hi = trWarp[0];
+                for (int w = 1; w < kFastWarps; w++) {
+                    lo = trWarp[w] < lo ? trWarp[w] : lo;
+                    hi = trWarp[w] > hi ? trWarp[w] : hi;
+                }
+                if (p > 2) {
+                    trSum[4] += lo - tB;  // first warp done with its rows
+                    trSum[5] += hi - tB;  // last warp done
+                    for (int w = 0; w < kFastWarps; w++) trW[w] += trWarp[w] - tB;
+                }
+            }
 #endif
             block_record<float>(a0, a1, a2, am, !fit, sh, recOut, rec32Out);
 #ifdef ALENS_TRACE_FAST
@@ -883,10 +926,9 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
                         xs = (unsigned int)(pc - r0) < (unsigned int)nr ? ownIn[pc - r0].x : gIn[pc].x;
                         lbl = lb64_of(e64.y & 3, e64.x, S.lb);
                     } else {
-                        const int2 en = ent[e];
-                        const int src = en.x & kEntSrcMask;
-                        xs = (en.x & kEntOwn) ? ownIn[src].x : gv[src].x;
-                        lbl = lb64_of((en.x >> 28) & 3, entCol[e], S.lb);
+                        const int slot = ent[e].x;
+                        xs = slot < kFastRows ? ownIn[slot].x : gv[slot - kFastRows].x;
+                        lbl = lb64_of(e64.y & 3, e64.x, S.lb);
                     }
                     double xl = (double)xs;
                     xl = xl < lbl ? lbl : xl;
@@ -935,10 +977,15 @@ __global__ void __launch_bounds__(kFastThreads, 1) k_solve_fast(DevState S, Fast
 #endif
     }
 #ifdef ALENS_TRACE_FAST
+    if (tid == 0 && trN > 0 && b == 0)
+        printf("fast trace block 0 warps: %lld %lld %lld %lld %lld %lld %lld %lld\n", trW[0] / trN, trW[1] / trN,
+               trW[2] / trN, trW[3] / trN, trW[4] / trN, trW[5] / trN, trW[6] / trN, trW[7] / trN);
     if (tid == 0 && trN > 0 && (b == 0 || b == G / 2 || b == G - 1))
         printf("fast trace block %d: row loading %lld cycles; %d FP32 passes: halo+records+decision %lld, rows %lld, "
-               "block record %lld, barrier %lld cycles per pass; rows %d halo %d\n",
-               b, tLoad - tStart, (int)trN, trSum[0] / trN, trSum[1] / trN, trSum[2] / trN, trSum[3] / trN, nr,
+               "block record %lld, barrier %lld cycles per pass (warps done with rows after %lld..%lld); rows %d "
+               "halo %d\n",
+               b, tLoad - tStart, (int)trN, trSum[0] / trN, trSum[1] / trN, trSum[2] / trN, trSum[3] / trN,
+               trSum[4] / trN, trSum[5] / trN, nr,
                nHalo);
 #endif
     if (b == 0 && tid == 0) {
