@@ -89,15 +89,53 @@ __device__ int merge_rows(const DevState &S, int k, const RowLists &L, int out0)
     return cnt;
 }
 
-__global__ void k_arow_count(DevState S) {
+// The same merge for rod rows of at most kMergeStage entries, staged in
+// shared memory: both rows are loaded with independent loads (one memory
+// round trip instead of one per merge step), each thread's copy in the
+// column of its lane ([entry][lane]: no bank conflicts whatever entry each
+// lane reads).  One warp per block.  Outputs and (eI, eJ) as merge_rows.
+constexpr int kMergeStage = 16;
+constexpr int kMergeThreads = 32;
+template <bool fill>
+__device__ int merge_rows_staged(const DevState &S, int k, const RowLists &L, int out0, int *stA, int *stB) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < kMergeStage; q++) {
+        if (q < L.nI) stA[q * kMergeThreads + lane] = __ldg(S.rowEnt + L.aI0 + q) >> 1;
+        if (q < L.nJ) stB[q * kMergeThreads + lane] = __ldg(S.rowEnt + L.aJ0 + q) >> 1;
+    }
+    auto at = [&](const int *st, int q, int n) { return q < n ? st[q * kMergeThreads + lane] : 0x7fffffff; };
+    int a = 0, b = 0, cnt = 0;
+    int la = at(stA, 0, L.nI), lb = at(stB, 0, L.nJ);
+    while (a < L.nI || b < L.nJ) {
+        const int l = la < lb ? la : lb;
+        const int eI = la == l ? L.aI0 + a : -1, eJ = lb == l ? L.aJ0 + b : -1;
+        while (la == l) la = at(stA, ++a, L.nI);
+        while (lb == l) lb = at(stB, ++b, L.nJ);
+        if (fill) S.aent[out0 + cnt] = make_int4(k, eI, eJ, l);
+        cnt++;
+    }
+    return cnt;
+}
+
+template <bool fill>
+__device__ __forceinline__ int merge_any(const DevState &S, int k, int out0, int *stA, int *stB) {
+    const RowLists L = row_lists(S, k);
+    if (L.nI <= kMergeStage && L.nJ <= kMergeStage) return merge_rows_staged<fill>(S, k, L, out0, stA, stB);
+    return merge_rows<fill>(S, k, L, out0);
+}
+
+__global__ void __launch_bounds__(kMergeThreads) k_arow_count(DevState S) {
+    __shared__ int stA[kMergeStage * kMergeThreads], stB[kMergeStage * kMergeThreads];
     ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < S.cap; k += gridDim.x * blockDim.x)
-        S.annz[k] = k < nc ? merge_rows<false>(S, k, row_lists(S, k), 0) : 0;
+        S.annz[k] = k < nc ? merge_any<false>(S, k, 0, stA, stB) : 0;
 }
 
-__global__ void k_arow_struct(DevState S) {
+__global__ void __launch_bounds__(kMergeThreads) k_arow_struct(DevState S) {
+    __shared__ int stA[kMergeStage * kMergeThreads], stB[kMergeStage * kMergeThreads];
     ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int nc = S.ctl->totalCon;
@@ -108,7 +146,7 @@ __global__ void k_arow_struct(DevState S) {
         return;
     }
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += gridDim.x * blockDim.x)
-        merge_rows<true>(S, k, row_lists(S, k), S.aptr[k]);
+        merge_any<true>(S, k, S.aptr[k], stA, stB);
 }
 
 // A_kl = dt * (sum over l's entries in rod I's row of J_k,I . W_l,s, then
@@ -156,9 +194,9 @@ void launch_weights(const DevState &S, cudaStream_t st) { k_weights<<<grid_for(2
 // Row structure on `st`; the values need the weights, which the caller
 // launched on `side` (recorded in `join`) while the rows were sorted.
 int launch_assemble(const DevState &S, cudaStream_t st, cudaStream_t side, cudaEvent_t join) {
-    launch_pdl(k_arow_count, dim3(grid_for(S.cap, 32)), dim3(32), 0, st, S);
+    launch_pdl(k_arow_count, dim3(grid_for(S.cap, kMergeThreads)), dim3(kMergeThreads), 0, st, S);
     const int n = launch_scan(S.annz, S.aptr, S.cap, S.scanTmp, st);
-    launch_pdl(k_arow_struct, dim3(grid_for(S.cap, 32)), dim3(32), 0, st, S);
+    launch_pdl(k_arow_struct, dim3(grid_for(S.cap, kMergeThreads)), dim3(kMergeThreads), 0, st, S);
     cudaEventRecord(join, side);
     cudaStreamWaitEvent(st, join, 0);
     k_arow_values<<<grid_for(S.nnzCap, 64), 64, 0, st>>>(S);

@@ -481,21 +481,45 @@ __device__ __noinline__ bool exact_pair(const DevState &S, int i, int j, const R
 
 // One thread per (neighbour cell, cell-sorted slot) item, slot-fastest: the
 // lanes of a warp hold consecutive rods of (mostly) one home cell looking
-// at the same neighbour offset, so candidate loads are broadcasts.  FP32
-// screen, FP64 decision only within the screening margin.
+// at the same neighbour offset, so candidate loads are broadcasts.  Half
+// shell: a rod looks at its home cell's later slots and at the neighbour
+// offsets that follow the home cell in (z, y, x) order, so every pair and
+// periodic image is met once (its mirror, from the partner's side, would
+// have the negated offset); a pair met from its larger rod index is
+// recorded as (smaller index, larger index, mirrored image), the
+// orientation the FP64 decision and the keys use.  Two stages per warp: every lane runs the cheap bounding-sphere test on its
+// cell's candidates and appends the pairs that pass to a warp queue in
+// shared memory; full warps then take 32 queued pairs at a time through the
+// FP32 segment distance (the lanes' candidates pass the sphere test at
+// different times, so a per-lane distance would hold the whole warp on
+// most candidates).  FP32 screen, FP64 decision only within the screening
+// margin.
+constexpr int kPairQ = 64;  // per-warp queue: fewer than 32 waiting + one round of 32
 __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
     ALENS_PDL_PROLOGUE();
+    constexpr int kW = kPairThreads / 32;
+    __shared__ int qm[kW][kPairQ];             // queued candidate (cell-sorted slot)
+    __shared__ unsigned char qo[kW][kPairQ];   // the lane that queued it
+    __shared__ float4 oA[kPairThreads], oB[kPairThreads], oC[kPairThreads];  // per lane: (ci, h), (u, r), (off, colBuf)
+    __shared__ int oI[kPairThreads], oImg[kPairThreads], oCnt[kPairThreads];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     // stencil of Wx x Wy x Wz cells (widths 1, 3 or 5)
     const int Wx = S.pairW[0], Wy = S.pairW[1], Wz = S.pairW[2];
-    const bool valid = item < (long long)(Wx * Wy * Wz) * S.nRods && !(flags(S) & kErrNaN);
+    const int W3 = Wx * Wy * Wz;
+    const bool valid = item < (long long)((W3 + 1) / 2) * S.nRods && !(flags(S) & kErrNaN);
     unsigned long long buf[kPairBuf];
     int nb = 0;
+    int i = 0, img = kImageNone, m0 = 0, len = 0;
+    float3 ci = make_float3(0.0f, 0.0f, 0.0f);
+    float hi_ = 0.0f, ri = 0.0f, cutHi = 0.0f;
+    float3 off = make_float3(0.0f, 0.0f, 0.0f);
     if (valid) {
         const int t = (int)(item % S.nRods);
-        const int nbr = (int)(item / S.nRods);
+        const int nbr = (int)(item / S.nRods) + (W3 - 1) / 2;  // the home cell and the offsets after it
         const int ox = nbr % Wx - (Wx >> 1), oy = (nbr / Wx) % Wy - (Wy >> 1), oz = nbr / (Wx * Wy) - (Wz >> 1);
-        const int i = S.sidx[t];
+        const bool home = ox == 0 && oy == 0 && oz == 0;
+        i = S.sidx[t];
         const RepParams &P = S.par[S.rodRep[i]];
         const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
         const int lc = S.cellOf[i] - P.cellOffset;
@@ -525,18 +549,16 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
             else { z -= nz; sz = 1; }
             if (z < 0 || z >= nz) ok = false;
         }
-        int cnt = 0;
         if (ok) {
             const float4 Ai = S.sA[t], Bi = S.sB[t];
-            const float3 ci = make_float3(Ai.x, Ai.y, Ai.z);
-            const float3 ui = make_float3(Bi.x, Bi.y, Bi.z);
-            const float hi_ = Ai.w, ri = Bi.w;
+            ci = make_float3(Ai.x, Ai.y, Ai.z);
+            hi_ = Ai.w;
+            ri = Bi.w;
             const float colBuf = P.colBuf32;
-            const float cutLo = colBuf - kScreenMargin, cutHi = colBuf + kScreenMargin;
-            const int img = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
+            cutHi = colBuf + kScreenMargin;
+            img = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
             // the neighbour cell's origin relative to ours
-            const float3 off = make_float3((float)ox * P.cellsz32[0], (float)oy * P.cellsz32[1],
-                                           (float)oz * P.cellsz32[2]);
+            off = make_float3((float)ox * P.cellsz32[0], (float)oy * P.cellsz32[1], (float)oz * P.cellsz32[2]);
             // skip the whole cell when its box lies beyond any partner's reach
             // (exact: every rod centre of that cell is at least this far)
             {
@@ -547,48 +569,132 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
                 const float thr = hi_ + ri + P.halfReach32 + cutHi + kScreenMargin;
                 if (bx * bx + by * by + bz * bz > thr * thr) ok = false;
             }
-            const int cell = P.cellOffset + (z * ny + y) * nx + xx;
-            const int m1 = ok ? S.cellStart[cell + 1] : 0;
-            for (int m = ok ? S.cellStart[cell] : 0; m < m1; m++) {
-                const int j = S.sidx[m];
-                if (j < i) continue;
-                if (j == i && img <= kImageNone) continue;
-                const float4 Aj = S.sA[m];
-                const float3 cj = make_float3(Aj.x + off.x, Aj.y + off.y, Aj.z + off.z);
-                const float d0 = ci.x - cj.x, d1 = ci.y - cj.y, d2 = ci.z - cj.z;
-                const float4 Bj = S.sB[m];
-                const float lim = hi_ + Aj.w + ri + Bj.w + cutHi;
-                if (d0 * d0 + d1 * d1 + d2 * d2 > lim * lim) continue;
-                const float sep = dcp_dist32(ci, ui, hi_, cj, make_float3(Bj.x, Bj.y, Bj.z), Aj.w) - ri - Bj.w;
-                if (sep >= cutHi) continue;
-                if (sep >= cutLo) {
+            if (ok) {
+                const int cell = P.cellOffset + (z * ny + y) * nx + xx;
+                m0 = home ? t + 1 : S.cellStart[cell];  // home cell: the slots after this rod's
+                len = S.cellStart[cell + 1] - m0;
+            }
+            oA[threadIdx.x] = make_float4(ci.x, ci.y, ci.z, hi_);
+            oB[threadIdx.x] = make_float4(Bi.x, Bi.y, Bi.z, ri);
+            oC[threadIdx.x] = make_float4(off.x, off.y, off.z, colBuf);
+        }
+    }
+    oI[threadIdx.x] = i;
+    oImg[threadIdx.x] = img;
+    oCnt[threadIdx.x] = 0;
+    __syncwarp();
+    // queued pairs through the FP32 segment distance, lane q taking entry q
+    auto drain = [&](int n) {
+        bool hit = false, border = false;
+        int bi = 0, bj = 0, bimg = 0;
+        unsigned long long key = 0ULL;
+        if (lane < n) {
+            const int m = qm[warp][lane];
+            const int ow = warp * 32 + qo[warp][lane];
+            const float4 A = oA[ow], B = oB[ow], C = oC[ow];
+            int i2 = oI[ow], img2 = oImg[ow];
+            int j = S.sidx[m];
+            const float4 Aj = S.sA[m], Bj = S.sB[m];
+            const float3 cj = make_float3(Aj.x + C.x, Aj.y + C.y, Aj.z + C.z);
+            const float sep = dcp_dist32(make_float3(A.x, A.y, A.z), make_float3(B.x, B.y, B.z), A.w, cj,
+                                         make_float3(Bj.x, Bj.y, Bj.z), Aj.w) -
+                              B.w - Bj.w;
+            const float cLo = C.w - kScreenMargin, cHi = C.w + kScreenMargin;
+            if (sep < cHi) {
+                // (smaller index, larger index, image of the larger's copy)
+                if (j < i2 || (j == i2 && img2 < kImageNone)) {
+                    const int tmp = i2;
+                    i2 = j;
+                    j = tmp;
+                    img2 = 26 - img2;
+                }
+                if (sep >= cLo) {
                     // within the screen's margin: decided in FP64 by
-                    // k_pairs_exact, with full warps (here one lane's FP64
-                    // segment distance would hold its whole warp)
-                    const int slot = atomicAdd(&S.ctl->borderCount, 1);
-                    if (slot < S.cap)
-                        S.border[slot] = make_int4(i, j, img, 0);
+                    // k_pairs_exact
+                    border = true;
+                    bi = i2;
+                    bj = j;
+                    bimg = img2;
+                } else {
+                    hit = true;
+                    key = pair_key(i2, j, img2);
+                    if (i2 == oI[ow])
+                        atomicAdd(&oCnt[ow], 1);
                     else
-                        atomicOr(&S.ctl->errFlags, kErrOverflow);
-                    continue;
+                        atomicAdd(&S.pairCount[i2], 1);
                 }
-                if (nb == kPairBuf) {
-                    flush_keys(S, buf, nb);
-                    nb = 0;
-                }
-                buf[nb++] = pair_key(i, j, img);
-                cnt++;
             }
         }
-        if (cnt) atomicAdd(&S.pairCount[i], cnt);
+        const unsigned int bb = __ballot_sync(0xffffffffu, border);
+        if (bb) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&S.ctl->borderCount, __popc(bb));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (border) {
+                const int slot = base + __popc(bb & ((1u << lane) - 1u));
+                if (slot < S.cap)
+                    S.border[slot] = make_int4(bi, bj, bimg, 0);
+                else
+                    atomicOr(&S.ctl->errFlags, kErrOverflow);
+            }
+        }
+        if (hit) {
+            if (nb == kPairBuf) {
+                flush_keys(S, buf, nb);
+                nb = 0;
+            }
+            buf[nb++] = key;
+        }
+    };
+    const int maxLen = __reduce_max_sync(0xffffffffu, len);
+    int qn = 0;  // queued pairs (the same in every lane)
+    for (int u = 0; u < maxLen; u++) {
+        bool pass = false;
+        const int m = m0 + u;
+        if (u < len) {
+            const float4 Aj = S.sA[m];
+            const float3 cj = make_float3(Aj.x + off.x, Aj.y + off.y, Aj.z + off.z);
+            const float d0 = ci.x - cj.x, d1 = ci.y - cj.y, d2 = ci.z - cj.z;
+            const float4 Bj = S.sB[m];
+            const float lim = hi_ + Aj.w + ri + Bj.w + cutHi;
+            pass = !(d0 * d0 + d1 * d1 + d2 * d2 > lim * lim);
+        }
+        const unsigned int bal = __ballot_sync(0xffffffffu, pass);
+        if (pass) {
+            const int pos = qn + __popc(bal & ((1u << lane) - 1u));
+            qm[warp][pos] = m;
+            qo[warp][pos] = (unsigned char)lane;
+        }
+        qn += __popc(bal);
+        if (qn >= 32) {
+            __syncwarp();
+            drain(32);
+            // the rest (fewer than 32) to the front
+            int mm = 0;
+            unsigned char oo = 0;
+            if (lane < qn - 32) {
+                mm = qm[warp][32 + lane];
+                oo = qo[warp][32 + lane];
+            }
+            __syncwarp();
+            if (lane < qn - 32) {
+                qm[warp][lane] = mm;
+                qo[warp][lane] = oo;
+            }
+            qn -= 32;
+            __syncwarp();
+        }
     }
+    __syncwarp();
+    if (qn > 0) drain(qn);
+    __syncwarp();
+    if (oCnt[threadIdx.x]) atomicAdd(&S.pairCount[i], oCnt[threadIdx.x]);
     // warp-aggregated append of the remaining keys
-    const int lane = threadIdx.x & 31;
     int incl = nb;
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const int o = __shfl_up_sync(0xffffffffu, incl, off);
-        if (lane >= off) incl += o;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     int base = 0;
@@ -1052,7 +1158,8 @@ int sm_count_detect() {
 }
 
 void launch_pairs(const DevState &S, cudaStream_t st) {
-    const long long items = (long long)S.pairW[0] * S.pairW[1] * S.pairW[2] * S.nRods;
+    // half shell: the home cell and the offsets after it
+    const long long items = (long long)((S.pairW[0] * S.pairW[1] * S.pairW[2] + 1) / 2) * S.nRods;
     const long long g = (items + kPairThreads - 1) / kPairThreads;
     launch_pdl(k_pairs, dim3((unsigned)(g > 0 ? g : 1)), dim3(kPairThreads), 0, st, S);
     launch_pdl(k_pairs_exact, dim3(2 * sm_count_detect()), dim3(64), 0, st, S);
