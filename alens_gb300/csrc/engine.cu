@@ -86,8 +86,12 @@ Engine::Engine(const AlensConfig *cfgs, int nrep) {
     }
     CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&side2_, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&side3_, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&orderJoin_, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&orderFork_, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&rowsDone_, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&weightsDone_, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&warmJoin_, cudaEventDisableTiming));
     for (int i = 0; i < 3; i++) {
         CK(cudaEventCreateWithFlags(&forkEv_[i], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&joinEv_[i], cudaEventDisableTiming));
@@ -131,8 +135,11 @@ Engine::~Engine() {
     }
     if (side_) cudaStreamDestroy(side_);
     if (side2_) cudaStreamDestroy(side2_);
+    if (side3_) cudaStreamDestroy(side3_);
     if (orderJoin_) cudaEventDestroy(orderJoin_);
     if (orderFork_) cudaEventDestroy(orderFork_);
+    for (cudaEvent_t e : {rowsDone_, weightsDone_, warmJoin_})
+        if (e) cudaEventDestroy(e);
     if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -745,8 +752,21 @@ int Engine::enqueueDetect() {
     CK(cudaEventRecord(forkEv_[1], stream_));
     CK(cudaStreamWaitEvent(side_, forkEv_[1], 0));
     launch_weights(S, side_);
+    CK(cudaEventRecord(weightsDone_, side_));
     n += 3;
     n += launch_rows(S, stream_);
+    // the learned warm start reads the constraints, the rod rows and the
+    // weights, not the assembled operator: a branch of its own beside the
+    // assembly, joined before the solve
+    const bool warmSide = warm_ == ALENS_WARM_MLP && mlp_;
+    if (warmSide) {
+        CK(cudaEventRecord(rowsDone_, stream_));
+        CK(cudaStreamWaitEvent(side3_, rowsDone_, 0));
+        CK(cudaStreamWaitEvent(side3_, weightsDone_, 0));
+        launch_mlp_warm(S, mlp_->view(), side3_);
+        CK(cudaEventRecord(warmJoin_, side3_));
+        n += 1;
+    }
     // the single-system solver's spatial row order (from the cell list and
     // the rod rows) on a third branch, beside the operator assembly;
     // computed whenever that form may run, so that the autotuner can try it
@@ -759,13 +779,11 @@ int Engine::enqueueDetect() {
         CK(cudaEventRecord(orderJoin_, side2_));
     }
     n += launch_assemble(S, stream_, side_, joinEv_[1]);
-    if (warm_ == ALENS_WARM_MLP && mlp_) {
-        launch_mlp_warm(S, mlp_->view(), stream_);
-        n += 1;
-    } else if (S.feat) {
+    if (!warmSide && S.feat) {
         launch_mlp_features(S, stream_);
         n += 1;
     }
+    if (warmSide) CK(cudaStreamWaitEvent(stream_, warmJoin_, 0));
     if (order) CK(cudaStreamWaitEvent(stream_, orderJoin_, 0));
     CK(cudaGetLastError());
     return n;

@@ -129,7 +129,9 @@ class Engine {
     cudaStream_t stream_ = nullptr;
     cudaStream_t side_ = nullptr;  // concurrent branch of the detect stage
     cudaStream_t side2_ = nullptr; // the single-system solver's row order, beside the assembly
+    cudaStream_t side3_ = nullptr; // the learned warm start, beside the assembly
     cudaEvent_t orderJoin_ = nullptr, orderFork_ = nullptr;
+    cudaEvent_t rowsDone_ = nullptr, weightsDone_ = nullptr, warmJoin_ = nullptr;
     cudaEvent_t forkEv_[3] = {nullptr, nullptr, nullptr}, joinEv_[3] = {nullptr, nullptr, nullptr};
     bool ownStream_ = false;
     int precision_ = 0, warm_ = 0;

@@ -57,6 +57,15 @@ __device__ __forceinline__ float dsiluf_(float a) {
 }
 
 // --------------------------------------------------------------- features
+// FP64 six-term dot product without contraction (the operator assembly's
+// arithmetic)
+__device__ __forceinline__ double dot6_rn(const double *a, const double *b) {
+    double s = __dmul_rn(a[0], b[0]);
+#pragma unroll
+    for (int c = 1; c < 6; c++) s = __dadd_rn(s, __dmul_rn(a[c], b[c]));
+    return s;
+}
+
 // Features of constraint k; false when k is not a collision constraint or
 // its operator diagonal is not positive (immovable rods).
 __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], float &scale) {
@@ -69,26 +78,48 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
     const int I = S.conI[k], J = S.conJ[k];
     const float q = (float)S.q[k];
     const float d = (float)S.rcol[I] + (float)S.rcol[J];
-    float akk = 0.0f, nb = 0.0f;
-    const int e0 = S.aptr[k], e1 = S.aptr[k + 1];
-    constexpr int kB = 8;
-    for (int eb = e0; eb < e1; eb += kB) {
-        // the batch's entries, then all their neighbours' q, are requested
-        // before any is used; the sum keeps the entry order
-        int4 en[kB];
+    // A_kk as the operator assembly forms it (FP64: dt times rod I's side
+    // J_kI . W_kI plus rod J's side), and the coupling to the compressed
+    // neighbours sum_l A_kl (-q_l) over collisions l != k with q_l < 0,
+    // taken over the rod rows of I and J (A_kl = dt sum over the shared
+    // rods of J_k,side . W_l,s), so no assembled operator is needed
+    const double dt = S.par[S.rodRep[I]].dt;
+    const double *Jk = S.jac + 12 * (size_t)k;
+    const double *Wk = S.W + 12 * (size_t)k;
+    double a = 0.0;
+    a = __dadd_rn(a, dot6_rn(Jk, Wk));
+    a = __dadd_rn(a, dot6_rn(Jk + 6, Wk + 6));
+    const float akk = (float)__dmul_rn(dt, a);
+    float nb = 0.0f;
+    const float dtf = (float)dt;
 #pragma unroll
-        for (int j = 0; j < kB; j++) en[j] = eb + j < e1 ? __ldg(S.aent + eb + j) : make_int4(k, 1, 0, 0);
-        float ql[kB];
+    for (int side = 0; side < 2; side++) {
+        const int r = side == 0 ? I : J;
+        float jk[6];
 #pragma unroll
-        for (int j = 0; j < kB; j++) ql[j] = (en[j].x != k && en[j].y == 0) ? (float)S.q[en[j].x] : 0.0f;
+        for (int c = 0; c < 6; c++) jk[c] = (float)Jk[6 * side + c];
+        const int e1 = S.rowPtr[r + 1];
+        constexpr int kB = 8;
+        for (int eb = S.rowPtr[r]; eb < e1; eb += kB) {
+            // the batch's entries, then their q and lower-bound kinds, are
+            // requested before any is used
+            int ent[kB];
 #pragma unroll
-        for (int j = 0; j < kB; j++) {
-            if (eb + j < e1) {
-                const float v = (float)__hiloint2double(en[j].w, en[j].z);
-                if (en[j].x == k) {
-                    akk = v;
-                } else if (en[j].y == 0) {
-                    if (ql[j] < 0.0f) nb = fmaf(v, -ql[j], nb);
+            for (int j = 0; j < kB; j++) ent[j] = eb + j < e1 ? __ldg(S.rowEnt + eb + j) : 2 * k;
+            float ql[kB];
+#pragma unroll
+            for (int j = 0; j < kB; j++) {
+                const int l = ent[j] >> 1;
+                ql[j] = (l != k && S.lbKind[l] == 0) ? (float)S.q[l] : 0.0f;
+            }
+#pragma unroll
+            for (int j = 0; j < kB; j++) {
+                if (ql[j] < 0.0f) {
+                    const double *W = S.W + 12 * (size_t)(ent[j] >> 1) + 6 * (ent[j] & 1);
+                    float v = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < 6; c++) v = fmaf(jk[c], (float)W[c], v);
+                    nb = fmaf(dtf * v, -ql[j], nb);
                 }
             }
         }
