@@ -195,6 +195,7 @@ void launch_prep(const DevState &S, cudaStream_t st);
 void launch_noise(const DevState &S, cudaStream_t st);
 void launch_mobility(const DevState &S, cudaStream_t st);  // once per rod set
 int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st);  // returns kernels launched
+int launch_scan_dev(const int *in, int *out, int nMax, const int *nDev, int *tmp, cudaStream_t st);
 void launch_scatter(const DevState &S, cudaStream_t st);
 void launch_link_blocks(const DevState &S, cudaStream_t st);
 void launch_pairs(const DevState &S, cudaStream_t st);

@@ -195,7 +195,8 @@ void launch_weights(const DevState &S, cudaStream_t st) { k_weights<<<grid_for(2
 // launched on `side` (recorded in `join`) while the rows were sorted.
 int launch_assemble(const DevState &S, cudaStream_t st, cudaStream_t side, cudaEvent_t join) {
     launch_pdl(k_arow_count, dim3(grid_for(S.cap, kMergeThreads)), dim3(kMergeThreads), 0, st, S);
-    const int n = launch_scan(S.annz, S.aptr, S.cap, S.scanTmp, st);
+    // row starts of the step's constraints (annz is zero past them)
+    const int n = launch_scan_dev(S.annz, S.aptr, S.cap, &S.ctl->totalCon, S.scanTmp, st);
     launch_pdl(k_arow_struct, dim3(grid_for(S.cap, kMergeThreads)), dim3(kMergeThreads), 0, st, S);
     cudaEventRecord(join, side);
     cudaStreamWaitEvent(st, join, 0);

@@ -269,8 +269,11 @@ __device__ __forceinline__ int4 scan_load4(const int *in, int i, int end, bool v
     return q;
 }
 
-__global__ void __launch_bounds__(kScanSingleThreads) k_scan_single(const int *in, int *out, int n, int vec) {
+__global__ void __launch_bounds__(kScanSingleThreads) k_scan_single(const int *in, int *out, int n, int vec,
+                                                                    const int *nDev) {
     ALENS_PDL_PROLOGUE();
+    // a count the device holds (the step's constraints) bounds the scan
+    if (nDev) n = min(*nDev, n);
     __shared__ int sm[33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = (((n + 31) / 32) + 127) & ~127;
@@ -1128,7 +1131,7 @@ void launch_mobility(const DevState &S, cudaStream_t st) {
 int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st) {
     if (n <= kScanSingleMax) {
         const int vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0 ? 1 : 0;
-        launch_pdl(k_scan_single, dim3(1), dim3(kScanSingleThreads), 0, st, in, out, n, vec);
+        launch_pdl(k_scan_single, dim3(1), dim3(kScanSingleThreads), 0, st, in, out, n, vec, (const int *)nullptr);
         return 1;
     }
     const int nb = (n + kScanSpan - 1) / kScanSpan;
@@ -1136,6 +1139,20 @@ int launch_scan(const int *in, int *out, int n, int *tmp, cudaStream_t st) {
     launch_pdl(k_scan_top, dim3(1), dim3(1024), 0, st, tmp, nb, out, n);
     if (nb > 0) launch_pdl(k_scan_add, dim3(nb), dim3(kScanBlock), 0, st, out, n, tmp);
     return nb > 0 ? 3 : 1;
+}
+
+// Exclusive scan of the first *nDev of at most nMax ints (out[*nDev] = the
+// total): one block while nMax is moderate (a capacity of up to 4 x
+// kScanSingleMax slots; the count the device holds is typically a quarter
+// to a third of it), else the three-pass scan of all nMax (the entries past
+// *nDev are zeros).
+int launch_scan_dev(const int *in, int *out, int nMax, const int *nDev, int *tmp, cudaStream_t st) {
+    if (nMax <= 4 * kScanSingleMax) {
+        const int vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0 ? 1 : 0;
+        launch_pdl(k_scan_single, dim3(1), dim3(kScanSingleThreads), 0, st, in, out, nMax, vec, nDev);
+        return 1;
+    }
+    return launch_scan(in, out, nMax, tmp, st);
 }
 
 void launch_link_blocks(const DevState &S, cudaStream_t st) {

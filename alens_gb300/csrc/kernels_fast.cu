@@ -27,12 +27,16 @@
 //     global memory at the start of each pass (~10 % of the entries on the
 //     20,000-rod layer).  After the pass's decision every column's value
 //     (iterate, gradient or projected step, by the pass's mode) is formed
-//     once into a shared-memory slot, so a row entry costs one 8-byte entry
-//     load, one 4-byte gather and one FMA.
+//     once into a shared-memory slot.  When every row of the block has a
+//     thread of its own, a row of up to kRegEnts entries is held in its
+//     thread's registers for the whole solve, so a row entry costs one
+//     4-byte shared-memory gather and one FMA per pass.
 //   FP32 passes: the step size alternates BB1/BB2 as in the other forms.
 //     Each block writes ONE record per pass: s.s, s.y, y.y (FP32 products
-//     summed in FP32 over the block's rows) and the residual max.  After the
-//     grid barrier, warp 0 of every block reads all records and accumulates
+//     summed in FP32 over the block's rows) and the residual max, one
+//     float4, the records of all blocks contiguous.  After the grid
+//     barrier, warp 0 of every block reads all records (one coalesced load
+//     per 32 blocks) and accumulates
 //     them in block order in double-float arithmetic (each sum a pair of
 //     FP32 numbers combined with the error-free TwoSum: 48 significand bits,
 //     FP64-class accuracy on the FP32 pipe), then decides (converged, next

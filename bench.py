@@ -873,6 +873,9 @@ def main():
     cfg_plain = workloads.config_with(w.cfg, precision=capi.PREC_FP64, warmStart=capi.WARM_ZERO)
     cfg_fast = workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_MLP, conResTol=FAST_TOL)
     cfg_fast_same = workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_MLP)
+    # the judge of the learned start: the same fast form from the zero start
+    cfg_fast_zero = workloads.config_with(w.cfg, precision=capi.PREC_MIXED, warmStart=capi.WARM_ZERO,
+                                          conResTol=FAST_TOL)
 
     def barrier():
         torch.cuda.synchronize()
@@ -887,6 +890,7 @@ def main():
                        tune=True)
         fast_same = run_arm(torch, stream, cfg_fast_same, rods, args.warmup, args.steps, flush, mlp=mlp,
                             tune=True)
+        fast_zero = run_arm(torch, stream, cfg_fast_zero, rods, args.warmup, args.steps, flush, tune=True)
         e2e = run_arm(torch, stream, cfg_fast, rods, args.warmup, args.steps, flush, e2e=True, mlp=mlp,
                       tune=True)
         e2e_plain = run_arm(torch, stream, cfg_plain, rods, args.warmup, args.steps, flush, e2e=True, tune=True)
@@ -899,6 +903,7 @@ def main():
     value = job_throughput(world, nr, args.steps, total_s(fast))
     plain_value = job_throughput(world, nr, args.steps, total_s(plain))
     same_value = job_throughput(world, nr, args.steps, total_s(fast_same))
+    zero_value = job_throughput(world, nr, args.steps, total_s(fast_zero))
     e2e_value = job_throughput(world, nr, args.steps, total_s(e2e))
     e2e_plain_value = job_throughput(world, nr, args.steps, total_s(e2e_plain))
     if rank != 0:
@@ -947,6 +952,8 @@ def main():
         "fast": arm_summary(fast, FAST_TOL),
         "fast_at_plain_tolerance": dict(arm_summary(fast_same, 1e-5), value=same_value,
                                         speedup_vs_plain=same_value / plain_value),
+        "fast_zero_start": dict(arm_summary(fast_zero, FAST_TOL), value=zero_value,
+                                speedup_vs_plain=zero_value / plain_value),
         "plain_fp64": dict(arm_summary(plain, 1e-5), value=plain_value,
                            e2e={"value": e2e_plain_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                                 "d2h_bytes_per_step": d2h}),
