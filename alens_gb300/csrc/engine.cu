@@ -329,6 +329,7 @@ void Engine::finalize() {
     S.sph = alloc<unsigned char>(G, N);
     S.unc = alloc<double>(G, 6 * (size_t)N);
     S.vel = alloc<double>(G, 6 * (size_t)N);
+    S.rodV = alloc<float>(G, 6 * (size_t)N);
     S.alphaBuf = alloc<double>(G, 2 * (size_t)R_);
     S.stage = alloc<double>(G, 7 * (size_t)N);
     S.cellOf = alloc<int>(G, N);
@@ -763,9 +764,10 @@ int Engine::enqueueDetect() {
         CK(cudaEventRecord(rowsDone_, stream_));
         CK(cudaStreamWaitEvent(side3_, rowsDone_, 0));
         CK(cudaStreamWaitEvent(side3_, weightsDone_, 0));
+        launch_rod_coupling(S, side3_);
         launch_mlp_warm(S, mlp_->view(), side3_);
         CK(cudaEventRecord(warmJoin_, side3_));
-        n += 1;
+        n += 2;
     }
     // the single-system solver's spatial row order (from the cell list and
     // the rod rows) on a third branch, beside the operator assembly;
@@ -780,8 +782,9 @@ int Engine::enqueueDetect() {
     }
     n += launch_assemble(S, stream_, side_, joinEv_[1]);
     if (!warmSide && S.feat) {
+        launch_rod_coupling(S, stream_);
         launch_mlp_features(S, stream_);
-        n += 1;
+        n += 2;
     }
     if (warmSide) CK(cudaStreamWaitEvent(stream_, warmJoin_, 0));
     if (order) CK(cudaStreamWaitEvent(stream_, orderJoin_, 0));

@@ -140,6 +140,8 @@ struct DevState {
     // constraints
     int *conI, *conJ, *conImg;
     float2 *conST;             // contact parameters (s / h_I, t / h_J) of collisions
+    float *rodV;               // learned warm start: per rod, sum over its compressed collisions l
+                               // (q_l < 0) of (-q_l) W_l at the rod's side (6 x nRods, SoA)
     float *feat, *fscale;      // learned warm start: 12 features and A_kk / d per
                                // constraint (allocated while features are recorded)
     double *jac;

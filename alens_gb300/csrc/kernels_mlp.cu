@@ -90,40 +90,17 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
     a = __dadd_rn(a, dot6_rn(Jk, Wk));
     a = __dadd_rn(a, dot6_rn(Jk + 6, Wk + 6));
     const float akk = (float)__dmul_rn(dt, a);
-    float nb = 0.0f;
+    // sum_l A_kl (-q_l) over all compressed collisions l sharing a rod with
+    // k (k included), from the per-rod sums, less k's own term (-q_k) A_kk
     const float dtf = (float)dt;
+    float vI = 0.0f, vJ = 0.0f;
 #pragma unroll
-    for (int side = 0; side < 2; side++) {
-        const int r = side == 0 ? I : J;
-        float jk[6];
-#pragma unroll
-        for (int c = 0; c < 6; c++) jk[c] = (float)Jk[6 * side + c];
-        const int e1 = S.rowPtr[r + 1];
-        constexpr int kB = 8;
-        for (int eb = S.rowPtr[r]; eb < e1; eb += kB) {
-            // the batch's entries, then their q and lower-bound kinds, are
-            // requested before any is used
-            int ent[kB];
-#pragma unroll
-            for (int j = 0; j < kB; j++) ent[j] = eb + j < e1 ? __ldg(S.rowEnt + eb + j) : 2 * k;
-            float ql[kB];
-#pragma unroll
-            for (int j = 0; j < kB; j++) {
-                const int l = ent[j] >> 1;
-                ql[j] = (l != k && S.lbKind[l] == 0) ? (float)S.q[l] : 0.0f;
-            }
-#pragma unroll
-            for (int j = 0; j < kB; j++) {
-                if (ql[j] < 0.0f) {
-                    const double *W = S.W + 12 * (size_t)(ent[j] >> 1) + 6 * (ent[j] & 1);
-                    float v = 0.0f;
-#pragma unroll
-                    for (int c = 0; c < 6; c++) v = fmaf(jk[c], (float)W[c], v);
-                    nb = fmaf(dtf * v, -ql[j], nb);
-                }
-            }
-        }
+    for (int c = 0; c < 6; c++) {
+        vI = fmaf((float)Jk[c], S.rodV[(size_t)c * S.nRods + I], vI);
+        vJ = fmaf((float)Jk[6 + c], S.rodV[(size_t)c * S.nRods + J], vJ);
     }
+    float nb = dtf * (vI + vJ);
+    if (q < 0.0f) nb = fmaf(-q, -akk, nb);
     if (!(akk > 0.0f) || !(d > 0.0f)) return false;
     // the previous step's multiplier of this key: the constraint build
     // already looked it up for the warm-start modes (gamma0 = max(0, prev))
@@ -162,6 +139,30 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
     f[11] = nb / akk * invd;
     scale = akk * invd;
     return true;
+}
+
+// Per rod r: sum over the collisions l in its rod row with q_l < 0 of
+// (-q_l) W_l at r's side (FP32), the neighbour coupling of the features
+// without the assembled operator.
+__global__ void k_rod_coupling(DevState S) {
+    ALENS_PDL_PROLOGUE();
+    if (ld_volatile_i32(&S.ctl->errFlags) & (kErrNaN | kErrOverflow)) return;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
+        float v[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        const int e1 = S.rowPtr[r + 1];
+        for (int e = S.rowPtr[r]; e < e1; e++) {
+            const int ent = __ldg(S.rowEnt + e);
+            const int l = ent >> 1;
+            if (S.lbKind[l] != 0) continue;
+            const float ql = (float)S.q[l];
+            if (!(ql < 0.0f)) continue;
+            const double *W = S.W + 12 * (size_t)l + 6 * (ent & 1);
+#pragma unroll
+            for (int c = 0; c < 6; c++) v[c] = fmaf(-ql, (float)W[c], v[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 6; c++) S.rodV[(size_t)c * S.nRods + r] = v[c];
+    }
 }
 
 // ------------------------------------------------------- inference tile
@@ -705,6 +706,10 @@ void launch_mlp_warm(const DevState &S, const MlpView &V, cudaStream_t st) {
     const int tiles = (S.cap + kMlpTile - 1) / kMlpTile;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
     launch_pdl(k_mlp_warm, dim3(grid > 0 ? grid : 1), dim3(kInferThreads), 0, st, S, V);
+}
+
+void launch_rod_coupling(const DevState &S, cudaStream_t st) {
+    launch_pdl(k_rod_coupling, dim3((S.nRods + 127) / 128 > 0 ? (S.nRods + 127) / 128 : 1), dim3(128), 0, st, S);
 }
 
 void launch_mlp_features(const DevState &S, cudaStream_t st) {
