@@ -150,15 +150,32 @@ __global__ void k_rod_coupling(DevState S) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
         float v[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         const int e1 = S.rowPtr[r + 1];
-        for (int e = S.rowPtr[r]; e < e1; e++) {
-            const int ent = __ldg(S.rowEnt + e);
-            const int l = ent >> 1;
-            if (S.lbKind[l] != 0) continue;
-            const float ql = (float)S.q[l];
-            if (!(ql < 0.0f)) continue;
-            const double *W = S.W + 12 * (size_t)l + 6 * (ent & 1);
+        constexpr int kB = 8;
+        for (int eb = S.rowPtr[r]; eb < e1; eb += kB) {
+            // the batch's entries, then their q and kinds, then their W, are
+            // requested before any is used; the sum keeps the entry order
+            int ent[kB];
 #pragma unroll
-            for (int c = 0; c < 6; c++) v[c] = fmaf(-ql, (float)W[c], v[c]);
+            for (int j = 0; j < kB; j++) ent[j] = eb + j < e1 ? __ldg(S.rowEnt + eb + j) : -1;
+            float ql[kB];
+#pragma unroll
+            for (int j = 0; j < kB; j++) {
+                const int l = ent[j] >> 1;
+                ql[j] = (ent[j] >= 0 && S.lbKind[l] == 0) ? (float)S.q[l] : 0.0f;
+                if (ent[j] < 0) ent[j] = 0;  // padding: a valid address, weight 0
+            }
+            float w[kB][6];
+#pragma unroll
+            for (int j = 0; j < kB; j++) {
+                const double *W = S.W + 12 * (size_t)(ent[j] >> 1) + 6 * (ent[j] & 1);
+#pragma unroll
+                for (int c = 0; c < 6; c++) w[j][c] = ql[j] < 0.0f ? (float)W[c] : 0.0f;
+            }
+#pragma unroll
+            for (int j = 0; j < kB; j++)
+                if (ql[j] < 0.0f)
+#pragma unroll
+                    for (int c = 0; c < 6; c++) v[c] = fmaf(-ql[j], w[j][c], v[c]);
         }
 #pragma unroll
         for (int c = 0; c < 6; c++) S.rodV[(size_t)c * S.nRods + r] = v[c];
