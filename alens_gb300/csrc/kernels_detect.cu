@@ -252,9 +252,9 @@ __global__ void k_scan_top(int *tmp, int nb, int *out, int n) {
 // one launch instead of three for the per-rod and per-cell counts.  Warp w owns the contiguous segment [w G, (w + 1) G) (G a
 // multiple of 128); its lanes read consecutive int4 (coalesced), a round's
 // loads all in flight together.  Pass 1 sums each segment, one block scan
-// over the 32 segment totals gives the offsets, pass 2 re-reads the
-// segment and writes the prefixes (warp scan per 128 elements plus a
-// running carry).
+// over the 32 segment totals gives the offsets, pass 2 writes the prefixes
+// (warp scan per 128 elements plus a running carry) from the values kept
+// in registers (up to kScanSingleMax counts) or read again.
 constexpr int kScanSingleThreads = 1024;
 constexpr int kScanSingleMax = 32768;  // above this the three-pass scan is faster
 constexpr int kScanRound = 4;  // int4 loads per lane per round
@@ -278,13 +278,30 @@ __global__ void __launch_bounds__(kScanSingleThreads) k_scan_single(const int *i
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = (((n + 31) / 32) + 127) & ~127;
     const int s0 = min(warp * G, n), s1 = min(s0 + G, n);
+    // up to kScanSingleMax counts a warp's segment (G <= 1024) fits two
+    // rounds of int4 per lane: it is read once and kept in registers
+    constexpr int kIt = kScanSingleMax / 32 / (128 * kScanRound);
+    const bool inRegs = n <= kScanSingleMax;
+    int4 qr[kIt][kScanRound];
     int s = 0;
-    for (int r = s0; r < s1; r += 128 * kScanRound) {
-        int4 q[kScanRound];
+    if (inRegs) {
 #pragma unroll
-        for (int j = 0; j < kScanRound; j++) q[j] = scan_load4(in, r + 128 * j + 4 * lane, s1, vec != 0);
+        for (int it = 0; it < kIt; it++) {
+            const int r = s0 + it * 128 * kScanRound;
 #pragma unroll
-        for (int j = 0; j < kScanRound; j++) s += q[j].x + q[j].y + q[j].z + q[j].w;
+            for (int j = 0; j < kScanRound; j++) {
+                qr[it][j] = r < s1 ? scan_load4(in, r + 128 * j + 4 * lane, s1, vec != 0) : make_int4(0, 0, 0, 0);
+                s += qr[it][j].x + qr[it][j].y + qr[it][j].z + qr[it][j].w;
+            }
+        }
+    } else {
+        for (int r = s0; r < s1; r += 128 * kScanRound) {
+            int4 q[kScanRound];
+#pragma unroll
+            for (int j = 0; j < kScanRound; j++) q[j] = scan_load4(in, r + 128 * j + 4 * lane, s1, vec != 0);
+#pragma unroll
+            for (int j = 0; j < kScanRound; j++) s += q[j].x + q[j].y + q[j].z + q[j].w;
+        }
     }
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
@@ -292,38 +309,50 @@ __global__ void __launch_bounds__(kScanSingleThreads) k_scan_single(const int *i
     // every lane of a warp holds the same s: the block scan sees it once
     const int segOff = block_exclusive_scan(lane == 0 ? s : 0, sm, &tot);
     int carry = __shfl_sync(0xffffffffu, segOff, 0);
-    for (int r = s0; r < s1; r += 128 * kScanRound) {
-        int4 q[kScanRound];
+    // prefixes of one 128-element chunk (warp scan plus the running carry)
+    auto emit = [&](const int4 &q, int i) {
+        const int t = q.x + q.y + q.z + q.w;
+        int inc = t;
 #pragma unroll
-        for (int j = 0; j < kScanRound; j++) q[j] = scan_load4(in, r + 128 * j + 4 * lane, s1, vec != 0);
+        for (int off = 1; off < 32; off <<= 1) {
+            const int o = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += o;
+        }
+        int ex = carry + inc - t;
+        int4 o;
+        o.x = ex;
+        ex += q.x;
+        o.y = ex;
+        ex += q.y;
+        o.z = ex;
+        ex += q.z;
+        o.w = ex;
+        if (vec && i + 3 < s1) {
+            *reinterpret_cast<int4 *>(out + i) = o;
+        } else {
+            if (i < s1) out[i] = o.x;
+            if (i + 1 < s1) out[i + 1] = o.y;
+            if (i + 2 < s1) out[i + 2] = o.z;
+            if (i + 3 < s1) out[i + 3] = o.w;
+        }
+        carry += __shfl_sync(0xffffffffu, inc, 31);
+    };
+    if (inRegs) {
 #pragma unroll
-        for (int j = 0; j < kScanRound; j++) {
-            const int i = r + 128 * j + 4 * lane;
-            const int t = q[j].x + q[j].y + q[j].z + q[j].w;
-            int inc = t;
+        for (int it = 0; it < kIt; it++) {
+            const int r = s0 + it * 128 * kScanRound;
+            if (r < s1) {
 #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const int o = __shfl_up_sync(0xffffffffu, inc, off);
-                if (lane >= off) inc += o;
+                for (int j = 0; j < kScanRound; j++) emit(qr[it][j], r + 128 * j + 4 * lane);
             }
-            int ex = carry + inc - t;
-            int4 o;
-            o.x = ex;
-            ex += q[j].x;
-            o.y = ex;
-            ex += q[j].y;
-            o.z = ex;
-            ex += q[j].z;
-            o.w = ex;
-            if (vec && i + 3 < s1) {
-                *reinterpret_cast<int4 *>(out + i) = o;
-            } else {
-                if (i < s1) out[i] = o.x;
-                if (i + 1 < s1) out[i + 1] = o.y;
-                if (i + 2 < s1) out[i + 2] = o.z;
-                if (i + 3 < s1) out[i + 3] = o.w;
-            }
-            carry += __shfl_sync(0xffffffffu, inc, 31);
+        }
+    } else {
+        for (int r = s0; r < s1; r += 128 * kScanRound) {
+            int4 q[kScanRound];
+#pragma unroll
+            for (int j = 0; j < kScanRound; j++) q[j] = scan_load4(in, r + 128 * j + 4 * lane, s1, vec != 0);
+#pragma unroll
+            for (int j = 0; j < kScanRound; j++) emit(q[j], r + 128 * j + 4 * lane);
         }
     }
     if (threadIdx.x == 0) out[n] = tot;
