@@ -755,19 +755,19 @@ int Engine::enqueueDetect() {
     launch_weights(S, side_);
     CK(cudaEventRecord(weightsDone_, side_));
     n += 3;
-    n += launch_rows(S, stream_);
-    // the learned warm start reads the constraints, the rod rows and the
-    // weights, not the assembled operator: a branch of its own beside the
-    // assembly, joined before the solve
+    // the learned warm start reads the constraints, the rod rows, the
+    // weights and the per-rod coupling sums (formed by the row sort when
+    // features are wanted), not the assembled operator: a branch of its own
+    // beside the assembly, joined before the solve
     const bool warmSide = warm_ == ALENS_WARM_MLP && mlp_;
+    const bool coupling = warmSide || S.feat;
+    n += launch_rows(S, stream_, coupling ? weightsDone_ : nullptr);
     if (warmSide) {
         CK(cudaEventRecord(rowsDone_, stream_));
         CK(cudaStreamWaitEvent(side3_, rowsDone_, 0));
-        CK(cudaStreamWaitEvent(side3_, weightsDone_, 0));
-        launch_rod_coupling(S, side3_);
         launch_mlp_warm(S, mlp_->view(), side3_);
         CK(cudaEventRecord(warmJoin_, side3_));
-        n += 2;
+        n += 1;
     }
     // the single-system solver's spatial row order (from the cell list and
     // the rod rows) on a third branch, beside the operator assembly;
@@ -782,9 +782,8 @@ int Engine::enqueueDetect() {
     }
     n += launch_assemble(S, stream_, side_, joinEv_[1]);
     if (!warmSide && S.feat) {
-        launch_rod_coupling(S, stream_);
         launch_mlp_features(S, stream_);
-        n += 2;
+        n += 1;
     }
     if (warmSide) CK(cudaStreamWaitEvent(stream_, warmJoin_, 0));
     if (order) CK(cudaStreamWaitEvent(stream_, orderJoin_, 0));

@@ -141,7 +141,8 @@ struct DevState {
     int *conI, *conJ, *conImg;
     float2 *conST;             // contact parameters (s / h_I, t / h_J) of collisions
     float *rodV;               // learned warm start: per rod, sum over its compressed collisions l
-                               // (q_l < 0) of (-q_l) W_l at the rod's side (6 x nRods, SoA)
+                               // (q_l < 0) of (-q_l) W_l at the rod's side (6 x nRods, SoA;
+                               // formed by k_rows_sort when features are wanted)
     float *feat, *fscale;      // learned warm start: 12 features and A_kk / d per
                                // constraint (allocated while features are recorded)
     double *jac;
@@ -205,7 +206,9 @@ void launch_boundary_pairs(const DevState &S, cudaStream_t st);  // only when S.
 int launch_pair_sort(const DevState &S, cudaStream_t st);
 void launch_ranges(const DevState &S, cudaStream_t st);
 void launch_build(const DevState &S, cudaStream_t st);
-int launch_rows(const DevState &S, cudaStream_t st);
+// rod rows (scan, fill, sort); with `weights` (an event after the weights
+// kernel) the sort also forms the learned warm start's per-rod sums
+int launch_rows(const DevState &S, cudaStream_t st, cudaEvent_t weights);
 // ---- Delassus operator (kernels_assemble.cu)
 void launch_weights(const DevState &S, cudaStream_t st);
 int launch_assemble(const DevState &S, cudaStream_t st, cudaStream_t side, cudaEvent_t join);

@@ -1075,19 +1075,86 @@ __global__ void k_rows_fill(DevState S) {
     }
 }
 
-__global__ void k_rows_sort(DevState S) {
+// Bitonic sorting network over registers (ascending; every index a
+// compile-time constant).
+constexpr int kSortRegs = 16;
+__device__ __forceinline__ void sort_regs(int (&v)[kSortRegs]) {
+#pragma unroll
+    for (int k = 2; k <= kSortRegs; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+            for (int i = 0; i < kSortRegs; i++) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const int a = v[i], b = v[l];
+                    const int lo = a < b ? a : b, hi = a < b ? b : a;
+                    v[i] = (i & k) == 0 ? lo : hi;
+                    v[l] = (i & k) == 0 ? hi : lo;
+                }
+            }
+        }
+    }
+}
+
+// Each rod's row ascending.  A row of at most kSortRegs entries is loaded
+// once, sorted in registers and stored once; a longer one is sorted in
+// place.  With `coupling` (the learned warm start's features) the rod's
+// sum over its compressed collisions l (q_l < 0) of (-q_l) W_l at the rod's
+// side is formed from the sorted row, in entry order (FP32).
+__global__ void k_rows_sort(DevState S, int coupling) {
     ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
-        const int b = S.rowPtr[r], e = S.rowPtr[r + 1];
-        for (int x = b + 1; x < e; x++) {
-            const int v = S.rowEnt[x];
-            int y = x - 1;
-            while (y >= b && S.rowEnt[y] > v) {
-                S.rowEnt[y + 1] = S.rowEnt[y];
-                y--;
+        const int b = S.rowPtr[r], e = S.rowPtr[r + 1], len = e - b;
+        float cv[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        auto add = [&](int ent, float ql) {
+            const double *W = S.W + 12 * (size_t)(ent >> 1) + 6 * (ent & 1);
+#pragma unroll
+            for (int c = 0; c < 6; c++) cv[c] = fmaf(-ql, (float)W[c], cv[c]);
+        };
+        if (len <= kSortRegs) {
+            int v[kSortRegs];
+#pragma unroll
+            for (int q = 0; q < kSortRegs; q++) v[q] = q < len ? S.rowEnt[b + q] : 0x7fffffff;
+            sort_regs(v);
+#pragma unroll
+            for (int q = 0; q < kSortRegs; q++)
+                if (q < len) S.rowEnt[b + q] = v[q];
+            if (coupling) {
+                float ql[kSortRegs];
+#pragma unroll
+                for (int q = 0; q < kSortRegs; q++) {
+                    const int l = q < len ? v[q] >> 1 : 0;  // padding: a valid index, weight 0
+                    ql[q] = (q < len && S.lbKind[l] == 0) ? (float)S.q[l] : 0.0f;
+                }
+#pragma unroll
+                for (int q = 0; q < kSortRegs; q++)
+                    if (ql[q] < 0.0f) add(v[q], ql[q]);
             }
-            S.rowEnt[y + 1] = v;
+        } else {
+            for (int x = b + 1; x < e; x++) {
+                const int v = S.rowEnt[x];
+                int y = x - 1;
+                while (y >= b && S.rowEnt[y] > v) {
+                    S.rowEnt[y + 1] = S.rowEnt[y];
+                    y--;
+                }
+                S.rowEnt[y + 1] = v;
+            }
+            if (coupling) {
+                for (int x = b; x < e; x++) {
+                    const int ent = S.rowEnt[x];
+                    const int l = ent >> 1;
+                    if (S.lbKind[l] != 0) continue;
+                    const float ql = (float)S.q[l];
+                    if (ql < 0.0f) add(ent, ql);
+                }
+            }
+        }
+        if (coupling) {
+#pragma unroll
+            for (int c = 0; c < 6; c++) S.rodV[(size_t)c * S.nRods + r] = cv[c];
         }
     }
 }
@@ -1227,10 +1294,12 @@ void launch_build(const DevState &S, cudaStream_t st) {
     k_build<<<grid_for(S.cap, 32, 8192), 32, 0, st>>>(S);
 }
 
-int launch_rows(const DevState &S, cudaStream_t st) {
+int launch_rows(const DevState &S, cudaStream_t st, cudaEvent_t weights) {
     const int n = launch_scan(S.rowCount, S.rowPtr, S.nRods, S.scanTmp, st);
     launch_pdl(k_rows_fill, dim3(grid_for(S.cap, 256)), dim3(256), 0, st, S);
-    launch_pdl(k_rows_sort, dim3(grid_for(S.nRods, 32)), dim3(32), 0, st, S);
+    // the per-rod coupling sums read the weights (launched on another stream)
+    if (weights) cudaStreamWaitEvent(st, weights, 0);
+    launch_pdl(k_rows_sort, dim3(grid_for(S.nRods, 32)), dim3(32), 0, st, S, weights ? 1 : 0);
     return n + 2;
 }
 

@@ -141,47 +141,6 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
     return true;
 }
 
-// Per rod r: sum over the collisions l in its rod row with q_l < 0 of
-// (-q_l) W_l at r's side (FP32), the neighbour coupling of the features
-// without the assembled operator.
-__global__ void k_rod_coupling(DevState S) {
-    ALENS_PDL_PROLOGUE();
-    if (ld_volatile_i32(&S.ctl->errFlags) & (kErrNaN | kErrOverflow)) return;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.nRods; r += gridDim.x * blockDim.x) {
-        float v[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        const int e1 = S.rowPtr[r + 1];
-        constexpr int kB = 8;
-        for (int eb = S.rowPtr[r]; eb < e1; eb += kB) {
-            // the batch's entries, then their q and kinds, then their W, are
-            // requested before any is used; the sum keeps the entry order
-            int ent[kB];
-#pragma unroll
-            for (int j = 0; j < kB; j++) ent[j] = eb + j < e1 ? __ldg(S.rowEnt + eb + j) : -1;
-            float ql[kB];
-#pragma unroll
-            for (int j = 0; j < kB; j++) {
-                const int l = ent[j] >> 1;
-                ql[j] = (ent[j] >= 0 && S.lbKind[l] == 0) ? (float)S.q[l] : 0.0f;
-                if (ent[j] < 0) ent[j] = 0;  // padding: a valid address, weight 0
-            }
-            float w[kB][6];
-#pragma unroll
-            for (int j = 0; j < kB; j++) {
-                const double *W = S.W + 12 * (size_t)(ent[j] >> 1) + 6 * (ent[j] & 1);
-#pragma unroll
-                for (int c = 0; c < 6; c++) w[j][c] = ql[j] < 0.0f ? (float)W[c] : 0.0f;
-            }
-#pragma unroll
-            for (int j = 0; j < kB; j++)
-                if (ql[j] < 0.0f)
-#pragma unroll
-                    for (int c = 0; c < 6; c++) v[c] = fmaf(-ql[j], w[j][c], v[c]);
-        }
-#pragma unroll
-        for (int c = 0; c < 6; c++) S.rodV[(size_t)c * S.nRods + r] = v[c];
-    }
-}
-
 // ------------------------------------------------------- inference tile
 struct InferSmem {
     alignas(1024) uint8_t x[kMlpTile * kMlpInPad * 2];   // 4 KB
@@ -723,10 +682,6 @@ void launch_mlp_warm(const DevState &S, const MlpView &V, cudaStream_t st) {
     const int tiles = (S.cap + kMlpTile - 1) / kMlpTile;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
     launch_pdl(k_mlp_warm, dim3(grid > 0 ? grid : 1), dim3(kInferThreads), 0, st, S, V);
-}
-
-void launch_rod_coupling(const DevState &S, cudaStream_t st) {
-    launch_pdl(k_rod_coupling, dim3((S.nRods + 127) / 128 > 0 ? (S.nRods + 127) / 128 : 1), dim3(128), 0, st, S);
 }
 
 void launch_mlp_features(const DevState &S, cudaStream_t st) {

@@ -42,7 +42,6 @@ struct MlpView {
 struct DevState;
 
 // launchers (kernels_mlp.cu)
-void launch_rod_coupling(const DevState &S, cudaStream_t st);  // per-rod sums the features read
 void launch_mlp_warm(const DevState &S, const MlpView &V, cudaStream_t st);
 void launch_mlp_features(const DevState &S, cudaStream_t st);
 void launch_mlp_append(const DevState &S, int k0, int n, float *dsFeat, float *dsLabel, cudaStream_t st);
