@@ -797,6 +797,30 @@ __global__ void k_boundary_pairs(DevState S) {
     }
 }
 
+// Bitonic sorting network over registers (ascending; N a power of two,
+// every index a compile-time constant).
+template <class T, int N>
+__device__ __forceinline__ void sort_regs(T (&v)[N]) {
+#pragma unroll
+    for (int k = 2; k <= N; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const T a = v[i], b = v[l];
+                    const T lo = a < b ? a : b, hi = a < b ? b : a;
+                    v[i] = (i & k) == 0 ? lo : hi;
+                    v[l] = (i & k) == 0 ? hi : lo;
+                }
+            }
+        }
+    }
+}
+constexpr int kSortRegs = 16;  // rod-row entries sorted in registers
+constexpr int kKeyRegs = 8;    // pair keys of one rod sorted in registers
+
 // Place raw keys into their rod's segment, then sort each segment: the
 // canonical order is (i, j, image) ascending.
 __global__ void k_pair_bucket(DevState S) {
@@ -816,6 +840,17 @@ __global__ void k_pair_segsort(DevState S) {
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nRods; i += gridDim.x * blockDim.x) {
         const int b = S.pairOff[i], e = S.pairOff[i + 1];
+        if (e - b <= kKeyRegs) {
+            // loaded once, sorted in registers, stored once
+            unsigned long long v[kKeyRegs];
+#pragma unroll
+            for (int q = 0; q < kKeyRegs; q++) v[q] = b + q < e ? S.keys[b + q] : ~0ULL;
+            sort_regs<unsigned long long, kKeyRegs>(v);
+#pragma unroll
+            for (int q = 0; q < kKeyRegs; q++)
+                if (b + q < e) S.keys[b + q] = v[q];
+            continue;
+        }
         for (int x = b + 1; x < e; x++) {
             const unsigned long long v = S.keys[x];
             int y = x - 1;
@@ -1075,27 +1110,6 @@ __global__ void k_rows_fill(DevState S) {
     }
 }
 
-// Bitonic sorting network over registers (ascending; every index a
-// compile-time constant).
-constexpr int kSortRegs = 16;
-__device__ __forceinline__ void sort_regs(int (&v)[kSortRegs]) {
-#pragma unroll
-    for (int k = 2; k <= kSortRegs; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-#pragma unroll
-            for (int i = 0; i < kSortRegs; i++) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const int a = v[i], b = v[l];
-                    const int lo = a < b ? a : b, hi = a < b ? b : a;
-                    v[i] = (i & k) == 0 ? lo : hi;
-                    v[l] = (i & k) == 0 ? hi : lo;
-                }
-            }
-        }
-    }
-}
 
 // Each rod's row ascending.  A row of at most kSortRegs entries is loaded
 // once, sorted in registers and stored once; a longer one is sorted in
@@ -1117,7 +1131,7 @@ __global__ void k_rows_sort(DevState S, int coupling) {
             int v[kSortRegs];
 #pragma unroll
             for (int q = 0; q < kSortRegs; q++) v[q] = q < len ? S.rowEnt[b + q] : 0x7fffffff;
-            sort_regs(v);
+            sort_regs<int, kSortRegs>(v);
 #pragma unroll
             for (int q = 0; q < kSortRegs; q++)
                 if (q < len) S.rowEnt[b + q] = v[q];
