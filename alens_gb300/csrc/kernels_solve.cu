@@ -146,13 +146,23 @@ __global__ void k_advance(DevState S) {
         }
         double F[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         const int e1 = S.rowPtr[r + 1];
-        for (int e = S.rowPtr[r]; e < e1; e++) {
-            const int ent = S.rowEnt[e];
-            const int k = ent >> 1;
-            const double *J = S.jac + 12 * (size_t)k + 6 * (ent & 1);
-            const double gk = fin[k].x;
+        constexpr int kB = 8;
+        for (int eb = S.rowPtr[r]; eb < e1; eb += kB) {
+            // the batch's entries, then their multipliers and Jacobian rows,
+            // are requested before any is used; the sums keep entry order
+            int ent[kB];
 #pragma unroll
-            for (int c = 0; c < 6; c++) F[c] = F[c] + gk * J[c];
+            for (int j = 0; j < kB; j++) ent[j] = eb + j < e1 ? S.rowEnt[eb + j] : -1;
+            double gk[kB];
+#pragma unroll
+            for (int j = 0; j < kB; j++) gk[j] = ent[j] >= 0 ? fin[ent[j] >> 1].x : 0.0;
+#pragma unroll
+            for (int j = 0; j < kB; j++) {
+                if (ent[j] < 0) continue;
+                const double *J = S.jac + 12 * (size_t)(ent[j] >> 1) + 6 * (ent[j] & 1);
+#pragma unroll
+                for (int c = 0; c < 6; c++) F[c] = F[c] + gk[j] * J[c];
+            }
         }
         const double a[3] = {S.ax[r], S.ay[r], S.az[r]};
         const double m[3] = {S.m0[r], S.m1[r], S.m2[r]};
