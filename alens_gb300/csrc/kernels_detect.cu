@@ -519,13 +519,12 @@ __device__ __noinline__ bool exact_pair(const DevState &S, int i, int j, const R
 // periodic image is met once (its mirror, from the partner's side, would
 // have the negated offset); a pair met from its larger rod index is
 // recorded as (smaller index, larger index, mirrored image), the
-// orientation the FP64 decision and the keys use.  Two stages per warp: every lane runs the cheap bounding-sphere test on its
-// cell's candidates and appends the pairs that pass to a warp queue in
-// shared memory; full warps then take 32 queued pairs at a time through the
-// FP32 segment distance (the lanes' candidates pass the sphere test at
-// different times, so a per-lane distance would hold the whole warp on
-// most candidates).  FP32 screen, FP64 decision only within the screening
-// margin.
+// orientation the FP64 decision and the keys use.  Two stages per warp:
+// every lane runs the cheap bounding-sphere test on its cell's candidates
+// and appends the pairs that pass to a warp queue in shared memory; full
+// warps then take 32 queued pairs at a time through the FP32 segment
+// distance, every lane busy.  FP32 screen, FP64 decision only within the
+// screening margin.
 constexpr int kPairQ = 64;  // per-warp queue: fewer than 32 waiting + one round of 32
 __global__ void __launch_bounds__(kPairThreads) k_pairs(DevState S) {
     ALENS_PDL_PROLOGUE();
