@@ -280,8 +280,9 @@ __device__ __forceinline__ void store_features(uint8_t *x, int row, const float 
     tc::st_bf16x8(x, tc::core_off(row, 8, kMlpInPad), f + 8);
 }
 
-// Warm start of every collision constraint of the step (after the
-// operator assembly, before the solve).  Optionally records the features.
+// Warm start of every collision constraint of the step (after the rod rows
+// and the weights, beside the operator assembly, before the solve).
+// Optionally records the features.
 __global__ void __launch_bounds__(kInferThreads) k_mlp_warm(DevState S, MlpView V) {
     ALENS_PDL_PROLOGUE();
     __shared__ InferSmem sh;
