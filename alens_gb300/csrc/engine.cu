@@ -717,6 +717,7 @@ void Engine::uploadBlocks() {
 int Engine::enqueueDetect() {
     DevState &S = S_;
     int n = 0;
+    S.warmNet = (warm_ == ALENS_WARM_MLP && mlp_) ? 1 : 0;
     ensureSolverGrid();
     launch_step_clear(S, stream_);  // rawCount, errFlags and the per-cell / per-rod counters
     launch_prep(S, stream_);

@@ -111,6 +111,8 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
 struct DevState {
     int R, nRods, cap, nCells, tileCap, workCap, blockCap, nnzCap;
     int warm, precision;
+    int warmNet;               // 1: the learned warm start's network runs this step (ALENS_WARM_MLP with
+                               // a model): its features look up the previous multipliers themselves
     int solveMinTiles;         // BBPGD: at least this many 64-row tiles per solver block
     int barrierExtra;          // solver grid barriers wait for this many blocks more than launched
                                // (0; 1 only to test the bounded-wait path: every wait runs out)

@@ -974,7 +974,11 @@ __global__ void k_build(DevState S) {
     ALENS_PDL_PROLOGUE();
     if (flags(S) & (kErrNaN | kErrOverflow)) return;
     const int totalColl = S.ctl->totalColl, totalBil = S.ctl->totalBil;
-    const bool warmPrev = S.warm == ALENS_WARM_PREV || S.warm == ALENS_WARM_MLP;
+    // the previous step's multiplier of each key as the start: the
+    // previous-gamma mode, and the learned mode without a network; with
+    // the network its features look it up on the warm-start branch, and
+    // only the boundary contacts it does not score are looked up here
+    const bool warmPrev = S.warm == ALENS_WARM_PREV || (S.warm == ALENS_WARM_MLP && !S.warmNet);
     const int prevN = *S.prevCount;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < totalColl; p += gridDim.x * blockDim.x) {
         const unsigned long long key = S.keys[p];
@@ -983,7 +987,7 @@ __global__ void k_build(DevState S) {
         const RepParams &P = S.par[rep];
         const int k = p + S.bilPrefix[rep];
         double g0 = 0.0;
-        if (warmPrev && prevN > 0) {
+        if ((warmPrev || (S.warmNet && img >= kImageBoundary)) && prevN > 0) {
             int lo = 0, hi = prevN;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;

@@ -103,10 +103,11 @@ __device__ bool mlp_features(const DevState &S, int k, float (&f)[kMlpInPad], fl
     if (q < 0.0f) nb = fmaf(-q, -akk, nb);
     if (!(akk > 0.0f) || !(d > 0.0f)) return false;
     // the previous step's multiplier of this key: the constraint build
-    // already looked it up for the warm-start modes (gamma0 = max(0, prev))
+    // looked it up in the previous-gamma mode (gamma0 = max(0, prev)); with
+    // the network running it is looked up here, on the warm-start branch
     float gprev = 0.0f;
     const int prevN = *S.prevCount;
-    if (S.warm != ALENS_WARM_ZERO) {
+    if (S.warm == ALENS_WARM_PREV || (S.warm == ALENS_WARM_MLP && !S.warmNet)) {
         gprev = (float)S.gamma[k];
     } else if (prevN > 0) {
         const int rep = S.rodRep[I];
